@@ -1,0 +1,144 @@
+r"""Python front end of the CPU oracle (test infrastructure only).
+
+Loads ``oracle/build/liboracle.so`` (the C restatement in ``pyci_oracle.c``)
+with ctypes and offers numpy-level helpers: determinant enumeration, the
+reference-layout CSR build (lower triangle + diagonal when symmetric), SpMV,
+and reference eigenvalues.  Only tests, the smoke check and the CPU-baseline
+leg of the benchmark use this module; the product never imports it.
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "build", "liboracle.so")
+
+DOCI, FULLCI, GENCI, GENCI_REF = 0, 1, 2, 3
+_lib = None
+
+_i64 = ctypes.c_int64
+_p = ctypes.c_void_p
+
+
+def build():
+    r"""Compile the C restatement (make -C oracle port)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE, "port"])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            build()
+        L = ctypes.CDLL(_LIB)
+        L.orc_binomial.restype = _i64
+        L.orc_binomial.argtypes = [_i64, _i64]
+        L.orc_rank_colex.restype = _i64
+        L.orc_rank_colex.argtypes = [_i64, _i64, _p]
+        L.orc_ndet_all.restype = _i64
+        L.orc_ndet_all.argtypes = [ctypes.c_int, _i64, _i64, _i64]
+        L.orc_add_all_dets.restype = ctypes.c_int
+        L.orc_add_all_dets.argtypes = [ctypes.c_int, _i64, _i64, _i64, _p]
+        L.orc_csr_count.restype = ctypes.c_int
+        L.orc_csr_count.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _i64, _i64,
+                                    ctypes.c_int, ctypes.c_int, _p]
+        L.orc_csr_fill.restype = ctypes.c_int
+        L.orc_csr_fill.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _i64, _i64,
+                                   ctypes.c_int, _p, _p, _p, _p, _p, ctypes.c_int, _p, _p, _p]
+        for f in (L.orc_spmv_general, L.orc_spmv_sym_lower):
+            f.restype = None
+            f.argtypes = [_i64, _p, _p, _p, _p, _p, ctypes.c_int]
+        L.orc_phase_single.restype = ctypes.c_int
+        L.orc_phase_single.argtypes = [_p, _i64, _i64]
+        L.orc_phase_double.restype = ctypes.c_int
+        L.orc_phase_double.argtypes = [_p, _i64, _i64, _i64, _i64]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def nword(nbasis):
+    return (nbasis + 63) // 64
+
+
+def all_dets(kind, nbasis, nocc_up, nocc_dn):
+    r"""Every determinant in add_all_dets order: uint64[ndet, nwords]."""
+    L = lib()
+    nd = L.orc_ndet_all(kind, nbasis, nocc_up, nocc_dn)
+    nw = nword(nbasis) * (2 if kind == FULLCI else 1)
+    dets = np.zeros((nd, nw), dtype=np.uint64)
+    if L.orc_add_all_dets(kind, nbasis, nocc_up, nocc_dn, _ptr(dets)):
+        raise RuntimeError("orc_add_all_dets failed")
+    return dets
+
+
+def senzero(one_mo, two_mo):
+    r"""h, v, w exactly as pyci/src/squantop.cpp:175-182 derives them."""
+    n = one_mo.shape[0]
+    h = np.ascontiguousarray(np.diagonal(one_mo).copy())
+    idx = np.arange(n)
+    v = np.ascontiguousarray(two_mo[idx[:, None], idx[:, None], idx[None, :], idx[None, :]])
+    w = np.ascontiguousarray(two_mo[idx[:, None], idx[None, :], idx[:, None], idx[None, :]] * 2
+                             - two_mo[idx[:, None], idx[None, :], idx[None, :], idx[:, None]])
+    return h, v, w
+
+
+def build_csr(kind, nbasis, nocc_up, nocc_dn, dets, one_mo, two_mo, nrow=-1, ncol=-1,
+              symmetric=True, nthreads=None):
+    r"""Reference-layout CSR (data f64, indices i64, indptr i64)."""
+    L = lib()
+    dets = np.ascontiguousarray(dets, dtype=np.uint64)
+    ndet = dets.shape[0]
+    nrow = ndet if nrow < 0 else nrow
+    ncol = ndet if ncol < 0 else ncol
+    nthreads = nthreads or os.cpu_count() or 1
+    one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+    two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+    h, v, w = senzero(one_mo, two_mo)
+    indptr = np.zeros(nrow + 1, dtype=np.int64)
+    args = (kind, nbasis, nocc_up, nocc_dn, ndet, _ptr(dets), nrow, ncol, int(bool(symmetric)))
+    if L.orc_csr_count(*args, nthreads, _ptr(indptr)):
+        raise RuntimeError("orc_csr_count failed")
+    nnz = int(indptr[-1])
+    indices = np.empty(nnz, dtype=np.int64)
+    data = np.empty(nnz, dtype=np.float64)
+    if L.orc_csr_fill(*args, _ptr(one_mo), _ptr(two_mo), _ptr(h), _ptr(v), _ptr(w), nthreads,
+                      _ptr(indptr), _ptr(indices), _ptr(data)):
+        raise RuntimeError("orc_csr_fill failed")
+    return data, indices, indptr
+
+
+def spmv(data, indices, indptr, x, symmetric=True, nthreads=None):
+    L = lib()
+    nrow = indptr.shape[0] - 1
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(nrow, dtype=np.float64)
+    f = L.orc_spmv_sym_lower if symmetric else L.orc_spmv_general
+    f(nrow, _ptr(indptr), _ptr(indices), _ptr(data), _ptr(x), _ptr(y), nthreads or os.cpu_count())
+    return y
+
+
+def full_matrix(data, indices, indptr, ncol=None):
+    r"""scipy CSR of the full symmetric matrix from its lower triangle."""
+    import scipy.sparse as sp
+    n = indptr.shape[0] - 1
+    low = sp.csr_matrix((data, indices, indptr), shape=(n, ncol or n))
+    return (low + low.T - sp.diags(low.diagonal())).tocsr()
+
+
+def lowest_eigenvalues(data, indices, indptr, nroot=1, tol=1e-12):
+    r"""Lowest eigenvalues (ascending) of the symmetric matrix given by its lower CSR."""
+    import scipy.sparse.linalg as spl
+    m = full_matrix(data, indices, indptr)
+    n = m.shape[0]
+    if n <= 3000:
+        return np.linalg.eigvalsh(m.toarray())[:nroot]
+    vals = spl.eigsh(m, k=nroot, which="SA", tol=tol, return_eigenvectors=False,
+                     v0=np.ones(n) / np.sqrt(n), ncv=max(2 * nroot + 1, 20))
+    return np.sort(vals)

@@ -1,0 +1,731 @@
+/* CPU restatement of PyCI's CI hot path (see pyci_oracle.h).
+ *
+ * TEST INFRASTRUCTURE ONLY -- the checker for the GPU path and the timed CPU
+ * baseline.  Each routine restates the reference routine cited beside it
+ * (paths relative to the PyCI source tree).  The determinant index is an
+ * open-addressing table keyed on the determinant words; the reference keys a
+ * hash map on a 128-bit SpookyHash of the same words
+ * (pyci/src/onespinwfn.cpp:123-126), and both return the insertion index.
+ *
+ * Row-parallel with pthreads: the reference's sparse_op loop
+ * (pyci/src/sparseop.cpp:186-201) is serial; rows are independent, so
+ * splitting them over threads changes no result.
+ */
+#define _POSIX_C_SOURCE 200809L
+#include "pyci_oracle.h"
+
+#include <limits.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define WORD_BITS 64
+
+/* pyci/src/common.cpp:41-66 (binomial with overflow guard -> INT64_MAX). */
+int64_t orc_binomial(int64_t n, int64_t k) {
+    if (k < 0 || n < 0)
+        return 0;
+    if (k == 0)
+        return 1;
+    if (k == 1)
+        return n;
+    if (k >= n)
+        return k == n;
+    if (k > n / 2)
+        k = n - k;
+    __int128 b = 1;
+    for (int64_t d = 1; d <= k; ++d) {
+        b = b * (n - k + d) / d;
+        if (b > INT64_MAX)
+            return INT64_MAX;
+    }
+    return (int64_t)b;
+}
+
+/* pyci/src/common.cpp:280-282 */
+int64_t orc_nword(int64_t nbasis) { return nbasis / WORD_BITS + ((nbasis % WORD_BITS) ? 1 : 0); }
+
+/* pyci/src/common.cpp:85-97 */
+static int64_t fill_occs(int64_t nword, const uint64_t *det, int64_t *occs) {
+    int64_t j = 0;
+    for (int64_t i = 0; i < nword; ++i) {
+        uint64_t word = det[i];
+        while (word) {
+            int p = __builtin_ctzll(word);
+            occs[j++] = p + i * WORD_BITS;
+            word &= word - 1;
+        }
+    }
+    return j;
+}
+
+/* pyci/src/common.cpp:99-113 */
+static int64_t fill_virs(int64_t nword, int64_t nbasis, const uint64_t *det, int64_t *virs) {
+    int64_t j = 0;
+    for (int64_t i = 0; i < nword; ++i) {
+        int64_t left = nbasis - i * WORD_BITS;
+        uint64_t mask = (left < WORD_BITS) ? ((1ULL << left) - 1) : ~0ULL;
+        uint64_t word = det[i] ^ mask;
+        while (word) {
+            int p = __builtin_ctzll(word);
+            virs[j++] = p + i * WORD_BITS;
+            word &= word - 1;
+        }
+    }
+    return j;
+}
+
+/* pyci/src/common.cpp:124-137 (colex rank = sum over occupied p_k of C(p_k, k+1)). */
+int64_t orc_rank_colex(int64_t nbasis, int64_t nocc, const uint64_t *det) {
+    int64_t k = 0, rank = 0;
+    for (int64_t i = 0; i < nbasis && k < nocc; ++i) {
+        if (det[i / WORD_BITS] & (1ULL << (i % WORD_BITS))) {
+            ++k;
+            rank += orc_binomial(i, k);
+        }
+    }
+    return rank;
+}
+
+/* pyci/src/common.cpp:139-153 */
+void orc_unrank_colex(int64_t nbasis, int64_t nocc, int64_t rank, int64_t *occs) {
+    for (int64_t i = 0; i < nocc; ++i) {
+        int64_t j = nocc - i;
+        int64_t binom = orc_binomial(nbasis, j);
+        if (binom <= rank) {
+            for (int64_t k = 0; k < j; ++k)
+                occs[k] = k;
+            break;
+        }
+        while (binom > rank)
+            binom = orc_binomial(--nbasis, j);
+        occs[j - 1] = nbasis;
+        rank -= binom;
+    }
+}
+
+/* pyci/src/common.cpp:155-161 */
+static uint64_t mask_above(int64_t n) { return (n >= WORD_BITS - 1) ? 0ULL : ~((1ULL << (n + 1)) - 1); }
+static uint64_t mask_below(int64_t m) { return (m >= WORD_BITS) ? ~0ULL : (1ULL << m) - 1; }
+
+/* Number of occupied orbitals strictly between i and a. */
+static int64_t perm_between(const uint64_t *det, int64_t i, int64_t a) {
+    int64_t high = (i > a) ? i : a, low = (i > a) ? a : i;
+    int64_t k = high / WORD_BITS, m = high % WORD_BITS, j = low / WORD_BITS, n = low % WORD_BITS;
+    int64_t nperm = 0;
+    if (j == k) {
+        nperm += __builtin_popcountll(det[j] & mask_below(m) & mask_above(n));
+    } else {
+        nperm += __builtin_popcountll(det[j] & mask_above(n));
+        nperm += __builtin_popcountll(det[k] & mask_below(m));
+        for (int64_t l = j + 1; l < k; ++l)
+            nperm += __builtin_popcountll(det[l]);
+    }
+    return nperm;
+}
+
+/* pyci/src/common.cpp:163-194 */
+int orc_phase_single(const uint64_t *det, int64_t i, int64_t a) {
+    return (perm_between(det, i, a) % 2) ? -1 : 1;
+}
+
+/* pyci/src/common.cpp:196-261 */
+int orc_phase_double(const uint64_t *det, int64_t i1, int64_t i2, int64_t a1, int64_t a2) {
+    int64_t nperm = perm_between(det, i1, a1) + perm_between(det, i2, a2);
+    if ((i2 < a1) || (i1 > a2))
+        ++nperm;
+    return (nperm % 2) ? -1 : 1;
+}
+
+int64_t orc_ndet_all(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn) {
+    int64_t a = orc_binomial(nbasis, nocc_up);
+    if (kind != ORC_FULLCI)
+        return (a == INT64_MAX) ? -1 : a;
+    int64_t b = orc_binomial(nbasis, nocc_dn);
+    if (a == INT64_MAX || b == INT64_MAX || (b && a > INT64_MAX / b))
+        return -1;
+    return a * b;
+}
+
+static void fill_det(int64_t nocc, const int64_t *occs, uint64_t *det) {
+    for (int64_t i = 0; i < nocc; ++i)
+        det[occs[i] / WORD_BITS] |= 1ULL << (occs[i] % WORD_BITS);
+}
+
+/* pyci/src/onespinwfn.cpp:173-217 and pyci/src/twospinwfn.cpp:181-245:
+ * determinant r has colex rank r (one spin); for two spins, det r has
+ * alpha rank r / C(n, nocc_dn) and beta rank r % C(n, nocc_dn). */
+int orc_add_all_dets(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, uint64_t *dets) {
+    int64_t nword = orc_nword(nbasis);
+    int64_t occs[WORD_BITS * 64];
+    if (nocc_up > (int64_t)(sizeof(occs) / sizeof(occs[0])))
+        return -1;
+    if (kind != ORC_FULLCI) {
+        int64_t nd = orc_binomial(nbasis, nocc_up);
+        memset(dets, 0, sizeof(uint64_t) * nword * nd);
+        for (int64_t r = 0; r < nd; ++r) {
+            orc_unrank_colex(nbasis, nocc_up, r, occs);
+            fill_det(nocc_up, occs, dets + r * nword);
+        }
+        return 0;
+    }
+    int64_t na = orc_binomial(nbasis, nocc_up), nb = orc_binomial(nbasis, nocc_dn);
+    int64_t nword2 = 2 * nword;
+    memset(dets, 0, sizeof(uint64_t) * nword2 * na * nb);
+    uint64_t *beta = calloc((size_t)(nb * nword), sizeof(uint64_t));
+    if (!beta)
+        return -1;
+    for (int64_t r = 0; r < nb; ++r) {
+        orc_unrank_colex(nbasis, nocc_dn, r, occs);
+        fill_det(nocc_dn, occs, beta + r * nword);
+    }
+    uint64_t alpha[64];
+    for (int64_t ra = 0; ra < na; ++ra) {
+        memset(alpha, 0, sizeof(alpha));
+        orc_unrank_colex(nbasis, nocc_up, ra, occs);
+        fill_det(nocc_up, occs, alpha);
+        for (int64_t rb = 0; rb < nb; ++rb) {
+            uint64_t *d = dets + (ra * nb + rb) * nword2;
+            memcpy(d, alpha, sizeof(uint64_t) * nword);
+            memcpy(d + nword, beta + rb * nword, sizeof(uint64_t) * nword);
+        }
+    }
+    free(beta);
+    return 0;
+}
+
+/* ---------------- determinant -> index table ---------------- */
+
+typedef struct {
+    int64_t nwords, mask;
+    int64_t *slots;
+    const uint64_t *dets;
+} det_index;
+
+static uint64_t mix64(uint64_t x) {
+    x ^= x >> 30;
+    x *= 0xbf58476d1ce4e5b9ULL;
+    x ^= x >> 27;
+    x *= 0x94d049bb133111ebULL;
+    x ^= x >> 31;
+    return x;
+}
+
+static uint64_t hash_det(const uint64_t *d, int64_t nwords) {
+    uint64_t h = 0x84222325cbf29ce4ULL;
+    for (int64_t i = 0; i < nwords; ++i)
+        h = mix64(h ^ (d[i] + 0x9e3779b97f4a7c15ULL * (uint64_t)(i + 1)));
+    return h;
+}
+
+static int index_build(det_index *ix, int64_t ndet, int64_t nwords, const uint64_t *dets) {
+    int64_t cap = 16;
+    while (cap < 2 * ndet)
+        cap <<= 1;
+    ix->nwords = nwords;
+    ix->mask = cap - 1;
+    ix->dets = dets;
+    ix->slots = malloc(sizeof(int64_t) * cap);
+    if (!ix->slots)
+        return -1;
+    for (int64_t i = 0; i < cap; ++i)
+        ix->slots[i] = -1;
+    for (int64_t i = 0; i < ndet; ++i) {
+        int64_t s = (int64_t)(hash_det(dets + i * nwords, nwords) & (uint64_t)ix->mask);
+        for (;;) {
+            int64_t cur = ix->slots[s];
+            if (cur < 0) {
+                ix->slots[s] = i;
+                break;
+            }
+            if (!memcmp(dets + cur * nwords, dets + i * nwords, sizeof(uint64_t) * nwords))
+                break; /* duplicate: the first insertion keeps its index */
+            s = (s + 1) & ix->mask;
+        }
+    }
+    return 0;
+}
+
+static int64_t index_find(const det_index *ix, const uint64_t *d) {
+    int64_t s = (int64_t)(hash_det(d, ix->nwords) & (uint64_t)ix->mask);
+    for (;;) {
+        int64_t cur = ix->slots[s];
+        if (cur < 0)
+            return -1;
+        if (!memcmp(ix->dets + cur * ix->nwords, d, sizeof(uint64_t) * ix->nwords))
+            return cur;
+        s = (s + 1) & ix->mask;
+    }
+}
+
+/* ---------------- Slater-Condon rows ---------------- */
+
+typedef struct {
+    int kind;
+    int64_t nbasis, nocc_up, nocc_dn, ndet, nrow, ncol, nword;
+    int symmetric;
+    const uint64_t *dets;
+    const double *one_mo, *two_mo, *h, *v, *w;
+    const int64_t *indptr;
+    int64_t *indices, *counts;
+    double *data;
+    det_index ix;
+    int nthreads;
+} job;
+
+typedef struct {
+    int64_t n, cap;
+    int64_t *col;
+    double *val;
+} rowbuf;
+
+static void row_push(rowbuf *r, int64_t col, double val) {
+    if (r->n == r->cap) {
+        r->cap = r->cap ? 2 * r->cap : 1024;
+        r->col = realloc(r->col, sizeof(int64_t) * r->cap);
+        r->val = realloc(r->val, sizeof(double) * r->cap);
+    }
+    r->col[r->n] = col;
+    r->val[r->n] = val;
+    ++r->n;
+}
+
+/* Keeps a candidate column when the reference does: found, below the
+ * symmetric cut-off, and inside the column range (pyci/src/sparseop.cpp:243). */
+static int keep(const job *jb, int64_t idet, int64_t jdet) {
+    int64_t jmin = jb->symmetric ? idet : INT64_MAX;
+    return (jdet != -1) && (jdet < jmin) && (jdet < jb->ncol);
+}
+
+#define TWO(i, k, j, l) two[(i) * n3 + (k) * n2 + (j) * n1 + (l)]
+
+/* pyci/src/sparseop.cpp:220-258 */
+static void row_doci(const job *jb, int64_t idet, rowbuf *rb, int values) {
+    const int64_t nw = jb->nword, n = jb->nbasis;
+    uint64_t det[64];
+    int64_t occs[256], virs[4096];
+    memcpy(det, jb->dets + idet * nw, sizeof(uint64_t) * nw);
+    int64_t no = fill_occs(nw, det, occs), nv = fill_virs(nw, n, det, virs);
+    double val1 = 0.0, val2 = 0.0;
+    for (int64_t i = 0; i < no; ++i) {
+        int64_t k = occs[i];
+        if (values) {
+            val1 += jb->v[k * (n + 1)];
+            val2 += jb->h[k];
+            for (int64_t j = i + 1; j < no; ++j)
+                val2 += jb->w[k * n + occs[j]];
+        }
+        for (int64_t j = 0; j < nv; ++j) {
+            int64_t l = virs[j];
+            det[k / WORD_BITS] &= ~(1ULL << (k % WORD_BITS));
+            det[l / WORD_BITS] |= 1ULL << (l % WORD_BITS);
+            int64_t jdet = index_find(&jb->ix, det);
+            if (keep(jb, idet, jdet))
+                row_push(rb, jdet, values ? jb->v[k * n + l] : 0.0);
+            det[l / WORD_BITS] &= ~(1ULL << (l % WORD_BITS));
+            det[k / WORD_BITS] |= 1ULL << (k % WORD_BITS);
+        }
+    }
+    if (idet < jb->ncol)
+        row_push(rb, idet, val1 + val2 * 2);
+}
+
+static inline void excite(uint64_t *d, int64_t i, int64_t a) {
+    d[i / WORD_BITS] &= ~(1ULL << (i % WORD_BITS));
+    d[a / WORD_BITS] |= 1ULL << (a % WORD_BITS);
+}
+
+/* pyci/src/sparseop.cpp:260-427 */
+static void row_fullci(const job *jb, int64_t idet, rowbuf *rb, int values) {
+    const int64_t nw = jb->nword, n1 = jb->nbasis, n2 = n1 * n1, n3 = n1 * n2;
+    const double *one = jb->one_mo, *two = jb->two_mo;
+    const uint64_t *rup = jb->dets + idet * 2 * nw, *rdn = rup + nw;
+    uint64_t det[128];
+    uint64_t *dup = det, *ddn = det + nw;
+    int64_t ou[256], od[256], vu[4096], vd[4096];
+    memcpy(det, rup, sizeof(uint64_t) * 2 * nw);
+    int64_t nou = fill_occs(nw, rup, ou), nod = fill_occs(nw, rdn, od);
+    int64_t nvu = fill_virs(nw, n1, rup, vu), nvd = fill_virs(nw, n1, rdn, vd);
+    double val1, val2 = 0.0;
+    for (int64_t i = 0; i < nou; ++i) {
+        int64_t ii = ou[i];
+        if (values) {
+            val2 += one[(n1 + 1) * ii];
+            for (int64_t k = i + 1; k < nou; ++k) {
+                int64_t kk = ou[k];
+                val2 += TWO(ii, kk, ii, kk) - TWO(ii, kk, kk, ii);
+            }
+            for (int64_t k = 0; k < nod; ++k) {
+                int64_t kk = od[k];
+                val2 += TWO(ii, kk, ii, kk);
+            }
+        }
+        for (int64_t j = 0; j < nvu; ++j) {
+            int64_t jj = vu[j];
+            excite(dup, ii, jj);
+            int64_t jdet = index_find(&jb->ix, det);
+            if (keep(jb, idet, jdet)) {
+                double val = 0.0;
+                if (values) {
+                    int sign_up = orc_phase_single(rup, ii, jj);
+                    val1 = one[n1 * ii + jj];
+                    for (int64_t k = 0; k < nou; ++k) {
+                        int64_t kk = ou[k];
+                        val1 += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                    }
+                    for (int64_t k = 0; k < nod; ++k) {
+                        int64_t kk = od[k];
+                        val1 += TWO(ii, kk, jj, kk);
+                    }
+                    val = sign_up * val1;
+                }
+                row_push(rb, jdet, val);
+            }
+            int sign_up = orc_phase_single(rup, ii, jj);
+            for (int64_t k = 0; k < nod; ++k) {
+                int64_t kk = od[k];
+                for (int64_t l = 0; l < nvd; ++l) {
+                    int64_t ll = vd[l];
+                    excite(ddn, kk, ll);
+                    jdet = index_find(&jb->ix, det);
+                    if (keep(jb, idet, jdet))
+                        row_push(rb, jdet,
+                                 values ? sign_up * orc_phase_single(rdn, kk, ll) * TWO(ii, kk, jj, ll)
+                                        : 0.0);
+                    excite(ddn, ll, kk);
+                }
+            }
+            for (int64_t k = i + 1; k < nou; ++k) {
+                int64_t kk = ou[k];
+                for (int64_t l = j + 1; l < nvu; ++l) {
+                    int64_t ll = vu[l];
+                    excite(dup, kk, ll);
+                    jdet = index_find(&jb->ix, det);
+                    if (keep(jb, idet, jdet))
+                        row_push(rb, jdet,
+                                 values ? orc_phase_double(rup, ii, kk, jj, ll) *
+                                              (TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj))
+                                        : 0.0);
+                    excite(dup, ll, kk);
+                }
+            }
+            excite(dup, jj, ii);
+        }
+    }
+    for (int64_t i = 0; i < nod; ++i) {
+        int64_t ii = od[i];
+        if (values) {
+            val2 += one[(n1 + 1) * ii];
+            for (int64_t k = i + 1; k < nod; ++k) {
+                int64_t kk = od[k];
+                val2 += TWO(ii, kk, ii, kk) - TWO(ii, kk, kk, ii);
+            }
+        }
+        for (int64_t j = 0; j < nvd; ++j) {
+            int64_t jj = vd[j];
+            excite(ddn, ii, jj);
+            int64_t jdet = index_find(&jb->ix, det);
+            if (keep(jb, idet, jdet)) {
+                double val = 0.0;
+                if (values) {
+                    val1 = one[n1 * ii + jj];
+                    for (int64_t k = 0; k < nou; ++k) {
+                        int64_t kk = ou[k];
+                        val1 += TWO(ii, kk, jj, kk);
+                    }
+                    for (int64_t k = 0; k < nod; ++k) {
+                        int64_t kk = od[k];
+                        val1 += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                    }
+                    val = orc_phase_single(rdn, ii, jj) * val1;
+                }
+                row_push(rb, jdet, val);
+            }
+            for (int64_t k = i + 1; k < nod; ++k) {
+                int64_t kk = od[k];
+                for (int64_t l = j + 1; l < nvd; ++l) {
+                    int64_t ll = vd[l];
+                    excite(ddn, kk, ll);
+                    jdet = index_find(&jb->ix, det);
+                    if (keep(jb, idet, jdet))
+                        row_push(rb, jdet,
+                                 values ? orc_phase_double(rdn, ii, kk, jj, ll) *
+                                              (TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj))
+                                        : 0.0);
+                    excite(ddn, ll, kk);
+                }
+            }
+            excite(ddn, jj, ii);
+        }
+    }
+    if (idet < jb->ncol)
+        row_push(rb, idet, val2);
+}
+
+/* pyci/src/sparseop.cpp:429-502.
+ *
+ * With kind ORC_GENCI_REF the virtual loop runs to the reference's
+ * wfn.nvir = 2 * nbasis - nocc (pyci/src/wfn.cpp:62), nbasis more entries than
+ * there are virtual spin-orbitals; the extra entries of the reference's
+ * zero-initialised virs buffer (pyci/src/sparseop.cpp:190) are orbital 0.
+ * This reproduces the reference's GenCI matrix exactly, including the
+ * duplicate entries and the lost orbital-0 electron that follow.  ORC_GENCI
+ * loops over the true virtual spin-orbitals only (the Slater-Condon rules). */
+static void row_genci(const job *jb, int64_t idet, rowbuf *rb, int values) {
+    const int64_t nw = jb->nword, n1 = jb->nbasis, n2 = n1 * n1, n3 = n1 * n2;
+    const double *one = jb->one_mo, *two = jb->two_mo;
+    const uint64_t *rdet = jb->dets + idet * nw;
+    uint64_t det[64];
+    int64_t occs[512], virs[8192];
+    memcpy(det, rdet, sizeof(uint64_t) * nw);
+    int64_t no = fill_occs(nw, rdet, occs), nv = fill_virs(nw, n1, rdet, virs);
+    if (jb->kind == ORC_GENCI_REF) {
+        int64_t nv_ref = 2 * n1 - jb->nocc_up - jb->nocc_dn;
+        for (int64_t j = nv; j < nv_ref; ++j)
+            virs[j] = 0;
+        nv = nv_ref;
+    }
+    double val1, val2 = 0.0;
+    for (int64_t i = 0; i < no; ++i) {
+        int64_t ii = occs[i];
+        if (values) {
+            val2 += one[(n1 + 1) * ii];
+            for (int64_t k = i + 1; k < no; ++k) {
+                int64_t kk = occs[k];
+                val2 += TWO(ii, kk, ii, kk) - TWO(ii, kk, kk, ii);
+            }
+        }
+        for (int64_t j = 0; j < nv; ++j) {
+            int64_t jj = virs[j];
+            excite(det, ii, jj);
+            int64_t jdet = index_find(&jb->ix, det);
+            if (keep(jb, idet, jdet)) {
+                double val = 0.0;
+                if (values) {
+                    val1 = one[n1 * ii + jj];
+                    for (int64_t k = 0; k < no; ++k) {
+                        int64_t kk = occs[k];
+                        val1 += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                    }
+                    val = orc_phase_single(rdet, ii, jj) * val1;
+                }
+                row_push(rb, jdet, val);
+            }
+            for (int64_t k = i + 1; k < no; ++k) {
+                int64_t kk = occs[k];
+                for (int64_t l = j + 1; l < nv; ++l) {
+                    int64_t ll = virs[l];
+                    excite(det, kk, ll);
+                    jdet = index_find(&jb->ix, det);
+                    if (keep(jb, idet, jdet))
+                        row_push(rb, jdet,
+                                 values ? orc_phase_double(rdet, ii, kk, jj, ll) *
+                                              (TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj))
+                                        : 0.0);
+                    excite(det, ll, kk);
+                }
+            }
+            excite(det, jj, ii);
+        }
+    }
+    if (idet < jb->ncol)
+        row_push(rb, idet, val2);
+}
+
+/* pyci/src/sparseop.cpp:214-218: sort (value, column) pairs by column. */
+static void sort_row(rowbuf *rb) {
+    for (int64_t a = 1; a < rb->n; ++a) {
+        int64_t c = rb->col[a];
+        double v = rb->val[a];
+        int64_t b = a - 1;
+        while (b >= 0 && rb->col[b] > c) {
+            rb->col[b + 1] = rb->col[b];
+            rb->val[b + 1] = rb->val[b];
+            --b;
+        }
+        rb->col[b + 1] = c;
+        rb->val[b + 1] = v;
+    }
+}
+
+typedef struct {
+    job *jb;
+    int tid, values;
+} worker_arg;
+
+static void *worker(void *p) {
+    worker_arg *wa = p;
+    job *jb = wa->jb;
+    rowbuf rb = {0, 0, NULL, NULL};
+    const int64_t chunk = 64;
+    for (int64_t start = (int64_t)wa->tid * chunk; start < jb->nrow;
+         start += (int64_t)jb->nthreads * chunk) {
+        int64_t end = start + chunk < jb->nrow ? start + chunk : jb->nrow;
+        for (int64_t idet = start; idet < end; ++idet) {
+            rb.n = 0;
+            if (jb->kind == ORC_DOCI)
+                row_doci(jb, idet, &rb, wa->values);
+            else if (jb->kind == ORC_FULLCI)
+                row_fullci(jb, idet, &rb, wa->values);
+            else
+                row_genci(jb, idet, &rb, wa->values);
+            if (!wa->values) {
+                jb->counts[idet] = rb.n;
+            } else {
+                sort_row(&rb);
+                int64_t off = jb->indptr[idet];
+                memcpy(jb->indices + off, rb.col, sizeof(int64_t) * rb.n);
+                memcpy(jb->data + off, rb.val, sizeof(double) * rb.n);
+            }
+        }
+    }
+    free(rb.col);
+    free(rb.val);
+    return NULL;
+}
+
+static int run(job *jb, int values) {
+    int nt = jb->nthreads < 1 ? 1 : jb->nthreads;
+    jb->nthreads = nt;
+    pthread_t *th = malloc(sizeof(pthread_t) * nt);
+    worker_arg *args = malloc(sizeof(worker_arg) * nt);
+    if (!th || !args) {
+        free(th);
+        free(args);
+        return -1;
+    }
+    for (int t = 0; t < nt; ++t) {
+        args[t].jb = jb;
+        args[t].tid = t;
+        args[t].values = values;
+        pthread_create(&th[t], NULL, worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    free(th);
+    free(args);
+    return 0;
+}
+
+static int job_init(job *jb, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                    int64_t ndet, const uint64_t *dets, int64_t nrow, int64_t ncol, int symmetric,
+                    int nthreads) {
+    memset(jb, 0, sizeof(*jb));
+    if (nrow > ndet || nrow < 0 || ncol < 0 || nbasis > 4096)
+        return -1;
+    jb->kind = kind;
+    jb->nbasis = nbasis;
+    jb->nocc_up = nocc_up;
+    jb->nocc_dn = nocc_dn;
+    jb->ndet = ndet;
+    jb->nrow = nrow;
+    jb->ncol = ncol;
+    jb->symmetric = symmetric;
+    jb->dets = dets;
+    jb->nword = orc_nword(nbasis);
+    jb->nthreads = nthreads;
+    int64_t nwords = (kind == ORC_FULLCI) ? 2 * jb->nword : jb->nword;
+    return index_build(&jb->ix, ndet, nwords, dets);
+}
+
+int orc_csr_count(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                  const uint64_t *dets, int64_t nrow, int64_t ncol, int symmetric, int nthreads,
+                  int64_t *indptr) {
+    job jb;
+    if (job_init(&jb, kind, nbasis, nocc_up, nocc_dn, ndet, dets, nrow, ncol, symmetric, nthreads))
+        return -1;
+    jb.counts = indptr + 1;
+    int rc = run(&jb, 0);
+    free(jb.ix.slots);
+    indptr[0] = 0;
+    for (int64_t i = 0; i < nrow; ++i)
+        indptr[i + 1] += indptr[i];
+    return rc;
+}
+
+int orc_csr_fill(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                 const uint64_t *dets, int64_t nrow, int64_t ncol, int symmetric,
+                 const double *one_mo, const double *two_mo, const double *h, const double *v,
+                 const double *w, int nthreads, const int64_t *indptr, int64_t *indices,
+                 double *data) {
+    job jb;
+    if (job_init(&jb, kind, nbasis, nocc_up, nocc_dn, ndet, dets, nrow, ncol, symmetric, nthreads))
+        return -1;
+    jb.one_mo = one_mo;
+    jb.two_mo = two_mo;
+    jb.h = h;
+    jb.v = v;
+    jb.w = w;
+    jb.indptr = indptr;
+    jb.indices = indices;
+    jb.data = data;
+    int rc = run(&jb, 1);
+    free(jb.ix.slots);
+    return rc;
+}
+
+/* ---------------- sparse matrix-vector products ---------------- */
+
+typedef struct {
+    int64_t nrow;
+    const int64_t *indptr, *indices;
+    const double *data, *x;
+    double *y, *ybuf;
+    int nthreads, tid, lower;
+} spmv_arg;
+
+static void *spmv_worker(void *p) {
+    spmv_arg *a = p;
+    int64_t per = (a->nrow + a->nthreads - 1) / a->nthreads;
+    int64_t r0 = per * a->tid, r1 = r0 + per < a->nrow ? r0 + per : a->nrow;
+    double *yt = a->lower ? a->ybuf + (int64_t)a->tid * a->nrow : NULL;
+    if (yt)
+        memset(yt, 0, sizeof(double) * a->nrow);
+    for (int64_t i = r0; i < r1; ++i) {
+        double s = 0.0;
+        for (int64_t k = a->indptr[i]; k < a->indptr[i + 1]; ++k) {
+            int64_t j = a->indices[k];
+            s += a->data[k] * a->x[j];
+            if (yt && j != i)
+                yt[j] += a->data[k] * a->x[i];
+        }
+        a->y[i] = s;
+    }
+    return NULL;
+}
+
+static void spmv_run(int64_t nrow, const int64_t *indptr, const int64_t *indices,
+                     const double *data, const double *x, double *y, int nthreads, int lower) {
+    int nt = nthreads < 1 ? 1 : nthreads;
+    if (nrow < nt)
+        nt = 1;
+    double *ybuf = lower ? malloc(sizeof(double) * nrow * nt) : NULL;
+    pthread_t th[256];
+    spmv_arg args[256];
+    if (nt > 256)
+        nt = 256;
+    for (int t = 0; t < nt; ++t) {
+        args[t] = (spmv_arg){nrow, indptr, indices, data, x, y, ybuf, nt, t, lower};
+        pthread_create(&th[t], NULL, spmv_worker, &args[t]);
+    }
+    for (int t = 0; t < nt; ++t)
+        pthread_join(th[t], NULL);
+    if (lower) {
+        for (int t = 0; t < nt; ++t)
+            for (int64_t i = 0; i < nrow; ++i)
+                y[i] += ybuf[(int64_t)t * nrow + i];
+        free(ybuf);
+    }
+}
+
+/* Eigen row-major CSR times vector, as used by pyci/src/sparseop.cpp:96-104. */
+void orc_spmv_general(int64_t nrow, const int64_t *indptr, const int64_t *indices,
+                      const double *data, const double *x, double *y, int nthreads) {
+    spmv_run(nrow, indptr, indices, data, x, y, nthreads, 0);
+}
+
+/* Eigen selfadjointView<Lower> product, pyci/src/sparseop.cpp:106-112. */
+void orc_spmv_sym_lower(int64_t nrow, const int64_t *indptr, const int64_t *indices,
+                        const double *data, const double *x, double *y, int nthreads) {
+    spmv_run(nrow, indptr, indices, data, x, y, nthreads, 1);
+}

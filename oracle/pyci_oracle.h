@@ -1,0 +1,61 @@
+/* CPU restatement of PyCI's CI hot path: determinant enumeration, the
+ * Slater-Condon CSR build and the sparse matrix-vector products.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU path
+ * (tests, smoke check, and the timed CPU baseline); the product never links
+ * or calls it.  Every function follows a reference routine, cited per
+ * function in pyci_oracle.c.  Plain C11 + pthreads.
+ */
+#ifndef PYCI_ORACLE_H
+#define PYCI_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ORC_GENCI: Slater-Condon rules over the true virtual spin-orbitals.
+ * ORC_GENCI_REF: the reference's GenCI row loop verbatim, including its
+ * virtual-count quirk (see row_genci in pyci_oracle.c). */
+enum { ORC_DOCI = 0, ORC_FULLCI = 1, ORC_GENCI = 2, ORC_GENCI_REF = 3 };
+
+int64_t orc_binomial(int64_t n, int64_t k);
+int64_t orc_nword(int64_t nbasis);
+int64_t orc_rank_colex(int64_t nbasis, int64_t nocc, const uint64_t *det);
+void orc_unrank_colex(int64_t nbasis, int64_t nocc, int64_t rank, int64_t *occs);
+int orc_phase_single(const uint64_t *det, int64_t i, int64_t a);
+int orc_phase_double(const uint64_t *det, int64_t i1, int64_t i2, int64_t a1, int64_t a2);
+
+/* Number of determinants add_all_dets produces, or -1 on overflow. */
+int64_t orc_ndet_all(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn);
+
+/* Writes every determinant in the reference's add_all_dets order.  dets has
+ * room for ndet * (nword for DOCI/GenCI, 2 * nword for FullCI) words. */
+int orc_add_all_dets(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, uint64_t *dets);
+
+/* Two-pass CSR build.  Pass 1 writes indptr[0..nrow] (row counts then the
+ * prefix sum); pass 2 writes indices/data for the same rows.  Layout and
+ * element order match the reference exactly (row-sorted columns; with
+ * symmetric != 0, only columns < row plus the diagonal). */
+int orc_csr_count(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                  const uint64_t *dets, int64_t nrow, int64_t ncol, int symmetric, int nthreads,
+                  int64_t *indptr);
+int orc_csr_fill(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                 const uint64_t *dets, int64_t nrow, int64_t ncol, int symmetric,
+                 const double *one_mo, const double *two_mo, const double *h, const double *v,
+                 const double *w, int nthreads, const int64_t *indptr, int64_t *indices,
+                 double *data);
+
+/* y = A x for a general CSR matrix. */
+void orc_spmv_general(int64_t nrow, const int64_t *indptr, const int64_t *indices,
+                      const double *data, const double *x, double *y, int nthreads);
+/* y = (L + L^T - diag L) x for a lower-triangle CSR matrix L (nrow x nrow). */
+void orc_spmv_sym_lower(int64_t nrow, const int64_t *indptr, const int64_t *indices,
+                        const double *data, const double *x, double *y, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
