@@ -1,0 +1,186 @@
+/* pyci_gb300 -- GB300 (sm_103a) implementation of PyCI's CI hot path behind a C ABI.
+ *
+ * The hot path is the sparse CI Hamiltonian operator of PyCI: the CSR build
+ * (pyci::SparseOp constructors and update, pyci/src/sparseop.cpp:49-71,186-201,
+ * 220-502), its matrix-vector product (perform_op / perform_op_symm,
+ * pyci/src/sparseop.cpp:96-112) and the lowest-eigenpair solve (solve_ci,
+ * pyci/src/sparseop.cpp:114-146).  In the reference these are methods of the
+ * C++ class pyci::SparseOp (pyci/include/pyci.h:621-693) bound to Python as
+ * `pyci.sparse_op` (pyci/src/binding.cpp:884-1088).  Every entry point below
+ * takes plain pointers and sizes; all array arguments are HOST memory unless
+ * the name says `_device`.  Calls on one handle must not overlap; calls are
+ * synchronous (results are on the host on return), as in the reference.
+ *
+ * Status codes: 0 on success, negative on failure; pyci_gpu_last_error()
+ * returns the message of the calling thread's last failure.  The codes map to
+ * the exceptions the reference raises for the same condition:
+ *   PYCI_GPU_EINVAL  -> ValueError   (std::invalid_argument, std::domain_error)
+ *   PYCI_GPU_ETYPE   -> TypeError    (pybind11::type_error)
+ *   PYCI_GPU_ENOCONV -> RuntimeError ("did not converge")
+ *   PYCI_GPU_ECUDA, PYCI_GPU_ENOMEM, PYCI_GPU_EUNSUPPORTED -> RuntimeError
+ */
+#ifndef PYCI_GB300_H
+#define PYCI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PYCI_GPU_OK 0
+#define PYCI_GPU_EINVAL (-1)
+#define PYCI_GPU_ETYPE (-2)
+#define PYCI_GPU_ENOCONV (-3)
+#define PYCI_GPU_ECUDA (-4)
+#define PYCI_GPU_ENOMEM (-5)
+#define PYCI_GPU_EUNSUPPORTED (-6)
+
+/* Wave-function kinds (pyci/include/pyci.h:520-617). */
+#define PYCI_WFN_DOCI 0   /* DOCIWfn: one spin string of nbasis spatial orbitals (pairs)  */
+#define PYCI_WFN_FULLCI 1 /* FullCIWfn: alpha string then beta string, nword words each    */
+#define PYCI_WFN_GENCI 2  /* GenCIWfn: one string of nbasis spin-orbitals                  */
+
+/* Build flags. */
+#define PYCI_BUILD_FULL_COLEX 0x1   /* dets are exactly add_all_dets' list; dets may be NULL */
+#define PYCI_BUILD_GENCI_EXACT 0x2  /* GenCI: Slater-Condon rules over the true virtuals
+                                       instead of the reference's virtual-count quirk       */
+#define PYCI_BUILD_FORCE_HASH 0x4   /* look columns up in the hash table even for full spaces */
+
+/* Solve modes. */
+#define PYCI_SOLVE_FP64 0  /* FP64 CSR values, FP64 vectors, FP64 SpMM                      */
+#define PYCI_SOLVE_MIXED 1 /* FP32 values/vectors/SpMM with FP64 Rayleigh-Ritz,
+                              re-orthogonalisation and FP64 residual refinement           */
+
+/* Precisions of pyci_gpu_csr_spmm_device. */
+#define PYCI_PREC_FP64 0       /* values f64, x/y f64                                      */
+#define PYCI_PREC_FP32 1       /* values f32 (high part), x/y f32                          */
+#define PYCI_PREC_FP64_SPLIT 2 /* values f32 high + f32 low summed in f64, x/y f64         */
+
+typedef struct pyci_gpu_ctx pyci_gpu_ctx;
+typedef struct pyci_gpu_csr pyci_gpu_csr;
+
+typedef struct pyci_gpu_solve_stats {
+    int64_t iterations;   /* Davidson iterations                                  */
+    int64_t matvecs;      /* vectors multiplied by H (all precisions)             */
+    int64_t matvecs_fp64; /* of which in FP64 (refinement steps in mixed mode)    */
+    int64_t restarts;
+    int64_t refinements;
+    double seconds;       /* wall time inside the solve                           */
+    double seconds_spmm;  /* device time of the SpMM launches (CUDA events)       */
+    double max_residual;  /* final max over roots of ||H x - theta x||, FP64      */
+} pyci_gpu_solve_stats;
+
+/* Thread-local message of the last failure of the calling thread. */
+const char *pyci_gpu_last_error(void);
+
+/* Library version string. */
+const char *pyci_gpu_version(void);
+
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (diagnostic; no counterpart in the reference, which has no GPU code). */
+int64_t pyci_gpu_kernel_launches(void);
+
+/* Context: one CUDA device, one stream.  Replaces nothing in the reference
+ * (which is host-only); every SparseOp of the reference maps to one csr
+ * handle created on a context. */
+int pyci_gpu_ctx_create(int device, pyci_gpu_ctx **out);
+int pyci_gpu_ctx_destroy(pyci_gpu_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer (for device-pointer calls). */
+void *pyci_gpu_ctx_stream(pyci_gpu_ctx *ctx);
+
+/* Build the CI Hamiltonian in CSR form on the device.
+ * Replaces SparseOp::SparseOp(ham, wfn, nrow, ncol, symmetric)
+ * (pyci/src/sparseop.cpp:49-71) and the row loop it runs (update + add_row,
+ * pyci/src/sparseop.cpp:186-201,220-502).
+ *   kind      PYCI_WFN_*; nbasis/nocc_up/nocc_dn as in Wfn::init (pyci/src/wfn.cpp:51-70)
+ *   ndet      number of determinants in the wave function
+ *   dets      uint64[ndet][nwords], nwords = ceil(nbasis/64) (x2 for FULLCI), in the
+ *             wave function's insertion order; may be NULL with PYCI_BUILD_FULL_COLEX
+ *   nrow,ncol -1 means ndet (pyci/src/sparseop.cpp:51-52)
+ *   one_mo    f64[nbasis][nbasis]; two_mo f64[nbasis]^4, physicist's notation
+ *             (the arrays of pyci::SQuantOp, pyci/include/pyci.h:285-302)
+ * The handle stores both triangles when symmetric (for a gather-only SpMV);
+ * pyci_gpu_csr_export returns the reference's layout. */
+int pyci_gpu_csr_build(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up,
+                       int64_t nocc_dn, int64_t ndet, const uint64_t *dets, int64_t nrow,
+                       int64_t ncol, int symmetric, const double *one_mo, const double *two_mo,
+                       int flags, pyci_gpu_csr **out);
+
+/* Append rows [old nrow, ndet) for a grown wave function (new determinants at the end).
+ * Replaces SparseOp::py_update (pyci/src/sparseop.cpp:175-178), which calls
+ * update(ham, wfn, ndet, ndet, nrow).  Requires a symmetric operator. */
+int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
+                        const double *one_mo, const double *two_mo, int flags);
+
+int pyci_gpu_csr_free(pyci_gpu_csr *csr);
+/* Deep copy (SparseOp's copy constructor, pyci/src/sparseop.cpp:31-34). */
+int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out);
+
+/* nrow, ncol, size (reference nnz: lower triangle + diagonal when symmetric)
+ * and the number of entries stored on the device. */
+int pyci_gpu_csr_shape(const pyci_gpu_csr *csr, int64_t *nrow, int64_t *ncol, int64_t *size,
+                       int64_t *nnz_stored);
+
+/* Copy the CSR arrays out in the reference's layout: data f64[size],
+ * indices i64[size], indptr i64[nrow+1] (SparseOp::py_data/py_indices/py_indptr,
+ * pyci/src/sparseop.cpp:504-514).  Any pointer may be NULL to skip it. */
+int pyci_gpu_csr_export(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
+
+/* Element (i, j) of the reference's stored matrix, 0.0 when absent
+ * (SparseOp::get_element, pyci/src/sparseop.cpp:89-94). */
+int pyci_gpu_csr_get_element(const pyci_gpu_csr *csr, int64_t i, int64_t j, double *out);
+
+/* y[nrow] = H x[ncol] in FP64, host buffers (SparseOp::perform_op,
+ * pyci/src/sparseop.cpp:96-112; the symmetric operator applies L + L^T - D). */
+int pyci_gpu_csr_matvec(const pyci_gpu_csr *csr, const double *x, double *y);
+
+/* Y = H X on device buffers for k vectors stored interleaved ([ncol][k] and
+ * [nrow][k], element (row, vector) at row*k + vector), on `stream` (a
+ * cudaStream_t, or NULL for the context's stream).  precision PYCI_PREC_*;
+ * FP32 and FP64_SPLIT need pyci_gpu_csr_prepare_mixed first.  Asynchronous.
+ * The device form of perform_op, used by the eigensolver and benchmarks. */
+int pyci_gpu_csr_spmm_device(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x,
+                             void *y, void *stream);
+
+/* Derive the FP32 high/low value split used by the mixed-precision solve.
+ * With drop_fp64 != 0 the FP64 values are freed afterwards (FP64 products then
+ * use high + low, which reproduces every FP64 value to within 2^-48 relative). */
+int pyci_gpu_csr_prepare_mixed(pyci_gpu_csr *csr, int drop_fp64);
+
+/* Lowest n eigenpairs of the symmetric operator plus ecore
+ * (SparseOp::solve_ci / py_solve_ci, pyci/src/sparseop.cpp:114-173).
+ *   c0       optional f64[nrow] initial guess (NULL for the default guess)
+ *   ncv      maximum subspace dimension (-1: default)
+ *   maxiter  maximum iterations (-1: default)
+ *   tol      convergence: ||H x - theta x|| <= tol * max(eps^(2/3), |theta|) per root
+ *   evals    f64[n]; evecs f64[n][nrow] (eigenvector per row)
+ * Eigenpairs are returned in decreasing order of eigenvalue, as the reference
+ * returns them.  Errors: EINVAL when n >= nrow (nrow > 1), ETYPE when
+ * nrow != ncol or the operator is not symmetric, ENOCONV on no convergence. */
+int pyci_gpu_csr_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv,
+                       int64_t maxiter, double tol, double ecore, int mode, double *evals,
+                       double *evecs, pyci_gpu_solve_stats *stats);
+
+/* Order-independent digest of the reference-layout CSR, for checking
+ * full-size builds against a digest computed from the reference's arrays:
+ *   pattern_sum = sum over stored (i, j) of mix64(i * 2^32 + j)  (mod 2^64)
+ *   pattern_xor = xor of the same terms
+ *   value_sum   = sum of data, value_abs_sum = sum of |data|, value_wsum =
+ *   sum of data * (1 + ((i * 31 + j * 17) mod 1024) / 1024)   (FP64)
+ * where mix64 is the splitmix64 finaliser. */
+int pyci_gpu_csr_digest(const pyci_gpu_csr *csr, uint64_t *pattern_sum, uint64_t *pattern_xor,
+                        double *value_sum, double *value_abs_sum, double *value_wsum);
+
+/* Generate add_all_dets' determinant list on the device (colex unranking)
+ * and copy it to `dets` (uint64[ndet][nwords]).  Replaces
+ * OneSpinWfn::add_all_dets / TwoSpinWfn::add_all_dets
+ * (pyci/src/onespinwfn.cpp:173-217, pyci/src/twospinwfn.cpp:181-245). */
+int pyci_gpu_add_all_dets(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up,
+                          int64_t nocc_dn, uint64_t *dets);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -118,6 +118,8 @@ def spmv(data, indices, indptr, x, symmetric=True, nthreads=None):
     L = lib()
     nrow = indptr.shape[0] - 1
     x = np.ascontiguousarray(x, dtype=np.float64)
+    if symmetric and x.shape[0] < nrow:
+        raise ValueError("self-adjoint product needs len(x) >= nrow")
     y = np.zeros(nrow, dtype=np.float64)
     f = L.orc_spmv_sym_lower if symmetric else L.orc_spmv_general
     f(nrow, _ptr(indptr), _ptr(indices), _ptr(data), _ptr(x), _ptr(y), nthreads or os.cpu_count())
@@ -133,12 +135,18 @@ def full_matrix(data, indices, indptr, ncol=None):
 
 
 def lowest_eigenvalues(data, indices, indptr, nroot=1, tol=1e-12):
-    r"""Lowest eigenvalues (ascending) of the symmetric matrix given by its lower CSR."""
+    r"""Lowest eigenvalues (ascending) of the symmetric matrix given by its lower CSR.
+
+    Dense eigh for small matrices; ARPACK's implicitly restarted Lanczos
+    (scipy.sparse.linalg.eigsh) on the oracle's threaded symmetric SpMV
+    otherwise, which never forms the full matrix.
+    """
     import scipy.sparse.linalg as spl
-    m = full_matrix(data, indices, indptr)
-    n = m.shape[0]
+    n = indptr.shape[0] - 1
     if n <= 3000:
-        return np.linalg.eigvalsh(m.toarray())[:nroot]
-    vals = spl.eigsh(m, k=nroot, which="SA", tol=tol, return_eigenvectors=False,
+        return np.linalg.eigvalsh(full_matrix(data, indices, indptr).toarray())[:nroot]
+    op = spl.LinearOperator((n, n), matvec=lambda x: spmv(data, indices, indptr, np.ravel(x)),
+                            dtype=np.float64)
+    vals = spl.eigsh(op, k=nroot, which="SA", tol=tol, return_eigenvectors=False,
                      v0=np.ones(n) / np.sqrt(n), ncv=max(2 * nroot + 1, 20))
     return np.sort(vals)

@@ -1,0 +1,222 @@
+r"""ctypes binding of the C ABI in include/pyci_gb300.h.
+
+The same calls a host written in another language would bind (cgo, JNI,
+N-API): plain pointers and sizes, integer status codes, and
+``pyci_gpu_last_error`` for the message.  Status codes map to the exceptions
+the reference raises (ValueError, TypeError, RuntimeError).
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY = os.path.join(_HERE, "lib", "libpyci_gb300.so")
+
+OK, EINVAL, ETYPE, ENOCONV, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
+WFN_DOCI, WFN_FULLCI, WFN_GENCI = 0, 1, 2
+BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH = 0x1, 0x2, 0x4
+SOLVE_FP64, SOLVE_MIXED = 0, 1
+PREC_FP64, PREC_FP32, PREC_FP64_SPLIT = 0, 1, 2
+
+# Every symbol the header declares.
+SYMBOLS = [
+    "pyci_gpu_last_error", "pyci_gpu_version", "pyci_gpu_kernel_launches", "pyci_gpu_ctx_create", "pyci_gpu_ctx_destroy",
+    "pyci_gpu_ctx_stream", "pyci_gpu_csr_build", "pyci_gpu_csr_update", "pyci_gpu_csr_free",
+    "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
+    "pyci_gpu_csr_matvec", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
+    "pyci_gpu_csr_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
+]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("matvecs", ctypes.c_int64),
+                ("matvecs_fp64", ctypes.c_int64), ("restarts", ctypes.c_int64),
+                ("refinements", ctypes.c_int64), ("seconds", ctypes.c_double),
+                ("seconds_spmm", ctypes.c_double), ("max_residual", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_}
+
+
+_lib = None
+_p = ctypes.c_void_p
+_i64 = ctypes.c_int64
+_int = ctypes.c_int
+
+
+def lib():
+    r"""Load libpyci_gb300.so (fails loudly if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBRARY):
+            raise OSError("libpyci_gb300.so is not built; run `python -m pyci_gb300.build`")
+        L = ctypes.CDLL(LIBRARY)
+        sig = {
+            "pyci_gpu_last_error": (ctypes.c_char_p, []),
+            "pyci_gpu_version": (ctypes.c_char_p, []),
+            "pyci_gpu_kernel_launches": (_i64, []),
+            "pyci_gpu_ctx_create": (_int, [_int, ctypes.POINTER(_p)]),
+            "pyci_gpu_ctx_destroy": (_int, [_p]),
+            "pyci_gpu_ctx_stream": (_p, [_p]),
+            "pyci_gpu_csr_build": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _i64, _i64, _int, _p, _p,
+                                          _int, ctypes.POINTER(_p)]),
+            "pyci_gpu_csr_update": (_int, [_p, _i64, _p, _p, _p, _int]),
+            "pyci_gpu_csr_free": (_int, [_p]),
+            "pyci_gpu_csr_clone": (_int, [_p, ctypes.POINTER(_p)]),
+            "pyci_gpu_csr_shape": (_int, [_p, _p, _p, _p, _p]),
+            "pyci_gpu_csr_export": (_int, [_p, _p, _p, _p]),
+            "pyci_gpu_csr_get_element": (_int, [_p, _i64, _i64, _p]),
+            "pyci_gpu_csr_matvec": (_int, [_p, _p, _p]),
+            "pyci_gpu_csr_spmm_device": (_int, [_p, _int, _i64, _p, _p, _p]),
+            "pyci_gpu_csr_prepare_mixed": (_int, [_p, _int]),
+            "pyci_gpu_csr_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, ctypes.c_double, _int,
+                                          _p, _p, ctypes.POINTER(SolveStats)]),
+            "pyci_gpu_csr_digest": (_int, [_p, _p, _p, _p, _p, _p]),
+            "pyci_gpu_add_all_dets": (_int, [_p, _int, _i64, _i64, _i64, _p]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class GpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+def check(rc):
+    if rc == OK:
+        return
+    msg = lib().pyci_gpu_last_error().decode()
+    if rc == EINVAL:
+        raise ValueError(msg)
+    if rc == ETYPE:
+        raise TypeError(msg)
+    raise GpuError(rc, msg)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Context:
+    r"""A device context (one CUDA device, one stream)."""
+
+    def __init__(self, device=0):
+        h = _p()
+        check(lib().pyci_gpu_ctx_create(device, ctypes.byref(h)))
+        self.handle = h
+
+    @property
+    def stream(self):
+        return lib().pyci_gpu_ctx_stream(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().pyci_gpu_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_all_dets(self, kind, nbasis, nocc_up, nocc_dn):
+        from math import comb
+        nd = comb(nbasis, nocc_up) * (comb(nbasis, nocc_dn) if kind == WFN_FULLCI else 1)
+        nw = ((nbasis + 63) // 64) * (2 if kind == WFN_FULLCI else 1)
+        out = np.zeros((nd, nw), dtype=np.uint64)
+        check(lib().pyci_gpu_add_all_dets(self.handle, kind, nbasis, nocc_up, nocc_dn, _ptr(out)))
+        return out
+
+
+class Csr:
+    r"""A device CSR handle (pyci_gpu_csr)."""
+
+    def __init__(self, ctx, kind, nbasis, nocc_up, nocc_dn, dets, one_mo, two_mo, nrow=-1, ncol=-1,
+                 symmetric=True, flags=0, ndet=None):
+        self.ctx = ctx
+        one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+        two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+        if dets is not None:
+            dets = np.ascontiguousarray(dets, dtype=np.uint64)
+            ndet = dets.shape[0]
+        h = _p()
+        check(lib().pyci_gpu_csr_build(ctx.handle, kind, nbasis, nocc_up, nocc_dn, ndet, _ptr(dets), nrow,
+                                       ncol, int(bool(symmetric)), _ptr(one_mo), _ptr(two_mo), flags,
+                                       ctypes.byref(h)))
+        self.handle = h
+
+    def free(self):
+        if self.handle:
+            lib().pyci_gpu_csr_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def shape(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        check(lib().pyci_gpu_csr_shape(self.handle, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)  # nrow, ncol, size, nnz_stored
+
+    def export(self):
+        nrow, ncol, size, _ = self.shape()
+        data = np.empty(size, dtype=np.float64)
+        indices = np.empty(size, dtype=np.int64)
+        indptr = np.empty(nrow + 1, dtype=np.int64)
+        check(lib().pyci_gpu_csr_export(self.handle, _ptr(data), _ptr(indices), _ptr(indptr)))
+        return data, indices, indptr
+
+    def get_element(self, i, j):
+        out = ctypes.c_double()
+        check(lib().pyci_gpu_csr_get_element(self.handle, i, j, ctypes.byref(out)))
+        return out.value
+
+    def matvec(self, x):
+        nrow, ncol, _, _ = self.shape()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(nrow, dtype=np.float64)
+        check(lib().pyci_gpu_csr_matvec(self.handle, _ptr(x), _ptr(y)))
+        return y
+
+    def spmm_device(self, precision, k, x_ptr, y_ptr, stream=None):
+        check(lib().pyci_gpu_csr_spmm_device(self.handle, precision, k, x_ptr, y_ptr, stream))
+
+    def prepare_mixed(self, drop_fp64=False):
+        check(lib().pyci_gpu_csr_prepare_mixed(self.handle, int(bool(drop_fp64))))
+
+    def solve(self, n=1, c0=None, ncv=-1, maxiter=-1, tol=1e-12, ecore=0.0, mode=SOLVE_FP64):
+        nrow = self.shape()[0]
+        evals = np.empty(n, dtype=np.float64)
+        evecs = np.empty((n, nrow), dtype=np.float64)
+        st = SolveStats()
+        c0 = None if c0 is None else np.ascontiguousarray(c0, dtype=np.float64)
+        check(lib().pyci_gpu_csr_solve(self.handle, n, _ptr(c0), ncv, maxiter, tol, ecore, mode, _ptr(evals),
+                                       _ptr(evecs), ctypes.byref(st)))
+        return evals, evecs, st.as_dict()
+
+    def digest(self):
+        ps, px = ctypes.c_uint64(), ctypes.c_uint64()
+        vs, va, vw = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().pyci_gpu_csr_digest(self.handle, ctypes.byref(ps), ctypes.byref(px), ctypes.byref(vs),
+                                        ctypes.byref(va), ctypes.byref(vw)))
+        return {"pattern_sum": str(ps.value), "pattern_xor": str(px.value), "value_sum": vs.value,
+                "value_abs_sum": va.value, "value_wsum": vw.value}
+
+    def update(self, dets, one_mo, two_mo, flags=0):
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+        two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+        check(lib().pyci_gpu_csr_update(self.handle, dets.shape[0], _ptr(dets), _ptr(one_mo), _ptr(two_mo),
+                                        flags))

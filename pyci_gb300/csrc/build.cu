@@ -1,0 +1,1064 @@
+// Two-pass CSR build of the CI Hamiltonian on sm_103a.
+//
+// Replaces the serial row loop of pyci::SparseOp (update + add_row,
+// pyci/src/sparseop.cpp:186-502).  Pass 1 counts the stored entries of every
+// row, an exclusive scan turns the counts into row pointers, and pass 2
+// enumerates the same excitations again, evaluates the Slater-Condon matrix
+// elements in FP64 with the reference's summation order, sorts each row by
+// column in shared memory (bitonic network) and writes it in place.
+//
+// One thread block per row: its threads split the row's candidate
+// excitations (singles, same-spin doubles, opposite-spin doubles) by index,
+// so a row of ~1,700 entries (FCI 12 orbitals, 5+5 electrons) is generated
+// by 256 threads without any per-thread list.  Columns come either from the
+// colex rank of the excited determinant (when the wave function is the full
+// add_all_dets space) or from the device hash table.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <vector>
+
+#include "detops.cuh"
+#include "internal.h"
+
+namespace pyci_gpu {
+
+constexpr int32_t kSentinel = INT32_MAX;
+
+struct BuildParams {
+    int kind;
+    int nbasis;
+    int nocc_up, nocc_dn;
+    int genci_exact;
+    int colex;
+    int symmetric;
+    int64_t ndet, nrow, ncol;
+    int64_t legacy_nrow, legacy_ncol;
+    int64_t nbeta;          // C(nbasis, nocc_dn): FCI column = rank_a * nbeta + rank_b
+    const int64_t *binom;   // [(nbasis + 1) * ldk]
+    int ldk;
+    DetTable table;
+    const uint64_t *dets;   // [ndet * nwords] (hash mode) or null
+    const double *one_mo, *two_mo, *h, *v, *w;
+    int64_t *counts;        // pass 1 output [nrow]
+    const int64_t *rowptr;  // pass 2 input [nrow + 1]
+    int32_t *cols;
+    double *vals;
+    int32_t *lower_len;
+    double *diag;
+    int *error;             // set to a nonzero code on an internal inconsistency
+};
+
+// Column limit of a row's own (lower / general) entries: update() keeps the
+// rows built before it with their old column range (pyci/src/sparseop.cpp:175-201).
+__device__ __forceinline__ int64_t row_limit(const BuildParams &p, int64_t r) {
+    return (r < p.legacy_nrow) ? p.legacy_ncol : p.ncol;
+}
+
+// Whether row i stores column j (reference filters at pyci/src/sparseop.cpp:243,
+// 301, 321, 343, 381, 401, 461, 483: found, j < idet when symmetric, j < ncol).
+// Symmetric operators also store the mirror of every lower entry.
+__device__ __forceinline__ bool keep_entry(const BuildParams &p, int64_t i, int64_t j) {
+    if (j < 0)
+        return false;
+    if (!p.symmetric)
+        return j < row_limit(p, i);
+    if (j < i)
+        return j < row_limit(p, i);
+    if (j == i)
+        return i < row_limit(p, i);
+    return j < p.nrow && i < row_limit(p, j);
+}
+
+struct RowState {
+    int no_a, no_b, nv_a, nv_b;
+    int16_t occ_a[kMaxOcc], occ_b[kMaxOcc];
+    int16_t vir_a[kMaxVir], vir_b[kMaxVir];
+    uint64_t ra[4], rb[4];
+};
+
+__device__ __forceinline__ void decode_pair(int q, int &i, int &k) {
+    // q = k (k - 1) / 2 + i with 0 <= i < k.
+    int kk = static_cast<int>((1.0f + sqrtf(1.0f + 8.0f * static_cast<float>(q))) * 0.5f);
+    while (kk * (kk - 1) / 2 > q)
+        --kk;
+    while ((kk + 1) * kk / 2 <= q)
+        ++kk;
+    k = kk;
+    i = q - kk * (kk - 1) / 2;
+}
+
+__device__ __forceinline__ double two_mo_at(const double *two, int n, int i, int k, int j, int l) {
+    const int64_t n1 = n, n2 = n1 * n1, n3 = n2 * n1;
+    return __ldg(&two[i * n3 + k * n2 + j * n1 + l]);
+}
+
+// Load the row's determinant and occupation lists into shared memory.
+template<int NW>
+__device__ void load_row(const BuildParams &p, int64_t row, RowState &s) {
+    if (threadIdx.x == 0) {
+        uint64_t a[NW], b[NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+            a[w] = b[w] = 0;
+        if (p.kind == PYCI_WFN_FULLCI) {
+            if (p.colex) {
+                unrank_colex<NW>(row / p.nbeta, p.nbasis, p.nocc_up, p.binom, p.ldk, a);
+                unrank_colex<NW>(row % p.nbeta, p.nbasis, p.nocc_dn, p.binom, p.ldk, b);
+            } else {
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    a[w] = p.dets[row * 2 * NW + w];
+                    b[w] = p.dets[row * 2 * NW + NW + w];
+                }
+            }
+        } else {
+            if (p.colex) {
+                unrank_colex<NW>(row, p.nbasis, p.nocc_up, p.binom, p.ldk, a);
+            } else {
+#pragma unroll
+                for (int w = 0; w < NW; ++w)
+                    a[w] = p.dets[row * NW + w];
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            s.ra[w] = a[w];
+            s.rb[w] = b[w];
+        }
+        s.no_a = occ_list<NW>(a, s.occ_a);
+        s.nv_a = vir_list<NW>(a, p.nbasis, s.vir_a);
+        if (p.kind == PYCI_WFN_FULLCI) {
+            s.no_b = occ_list<NW>(b, s.occ_b);
+            s.nv_b = vir_list<NW>(b, p.nbasis, s.vir_b);
+        } else {
+            s.no_b = s.nv_b = 0;
+        }
+    }
+    __syncthreads();
+}
+
+// Column of an excited determinant.
+template<int NW>
+__device__ __forceinline__ int64_t column_of(const BuildParams &p, const uint64_t *a,
+                                             const uint64_t *b) {
+    if (p.kind == PYCI_WFN_FULLCI) {
+        if (p.colex)
+            return rank_colex<NW>(a, p.binom, p.ldk) * p.nbeta + rank_colex<NW>(b, p.binom, p.ldk);
+        uint64_t key[2 * NW];
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            key[w] = a[w];
+            key[NW + w] = b[w];
+        }
+        return p.table.find<2 * NW>(key);
+    }
+    if (p.colex)
+        return rank_colex<NW>(a, p.binom, p.ldk);
+    return p.table.find<NW>(a);
+}
+
+// Number of candidate excitations of a row (diagonal excluded).
+__device__ __forceinline__ int num_candidates(const BuildParams &p, const RowState &s) {
+    if (p.kind == PYCI_WFN_DOCI)
+        return s.no_a * s.nv_a;
+    const int sa = s.no_a * s.nv_a;
+    const int da = (s.no_a * (s.no_a - 1) / 2) * (s.nv_a * (s.nv_a - 1) / 2);
+    if (p.kind == PYCI_WFN_GENCI)
+        return sa + da;
+    const int sb = s.no_b * s.nv_b;
+    const int db = (s.no_b * (s.no_b - 1) / 2) * (s.nv_b * (s.nv_b - 1) / 2);
+    return sa + sb + da + db + sa * sb;
+}
+
+// Candidate c of row `row`: its column (or -1) and, when VALUES, its matrix
+// element.  Element formulas and summation order follow add_row
+// (pyci/src/sparseop.cpp:220-258 DOCI, 260-427 FullCI, 429-502 GenCI).
+template<int NW, bool VALUES>
+__device__ int64_t candidate(const BuildParams &p, const RowState &s, int64_t row, int c,
+                             double &val) {
+    const int n = p.nbasis;
+    const double *one = p.one_mo, *two = p.two_mo;
+    uint64_t a[NW], b[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        a[w] = s.ra[w];
+        b[w] = s.rb[w];
+    }
+    if (p.kind == PYCI_WFN_DOCI) {
+        const int i = c / s.nv_a, x = c % s.nv_a;
+        const int k = s.occ_a[i], l = s.vir_a[x];
+        flip(a, k);
+        flip(a, l);
+        const int64_t col = column_of<NW>(p, a, b);
+        if (VALUES && keep_entry(p, row, col))
+            val = __ldg(&p.v[k * n + l]);
+        return col;
+    }
+    const int sa = s.no_a * s.nv_a;
+    const int pa = s.no_a * (s.no_a - 1) / 2, qa = s.nv_a * (s.nv_a - 1) / 2;
+    if (c < sa) {
+        // Single excitation of the first string (alpha, or the GenCI string).
+        const int i = c / s.nv_a, x = c % s.nv_a;
+        const int ii = s.occ_a[i], jj = s.vir_a[x];
+        flip(a, ii);
+        flip(a, jj);
+        const int64_t col = column_of<NW>(p, a, b);
+        if (VALUES && keep_entry(p, row, col)) {
+            double v1 = __ldg(&one[ii * n + jj]);
+            for (int t = 0; t < s.no_a; ++t) {
+                const int kk = s.occ_a[t];
+                v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
+            }
+            for (int t = 0; t < s.no_b; ++t) {
+                const int kk = s.occ_b[t];
+                v1 += two_mo_at(two, n, ii, kk, jj, kk);
+            }
+            val = phase_single<NW>(s.ra, ii, jj) * v1;
+        }
+        return col;
+    }
+    c -= sa;
+    if (p.kind == PYCI_WFN_GENCI) {
+        // Same-string double (GenCI).
+        const int po = c / qa, pv = c % qa;
+        int i, k, x, y;
+        decode_pair(po, i, k);
+        decode_pair(pv, x, y);
+        const int ii = s.occ_a[i], kk = s.occ_a[k], jj = s.vir_a[x], ll = s.vir_a[y];
+        flip(a, ii);
+        flip(a, kk);
+        flip(a, jj);
+        flip(a, ll);
+        const int64_t col = column_of<NW>(p, a, b);
+        if (VALUES && keep_entry(p, row, col))
+            val = phase_double<NW>(s.ra, ii, kk, jj, ll) *
+                  (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+        return col;
+    }
+    const int sb = s.no_b * s.nv_b;
+    const int pb = s.no_b * (s.no_b - 1) / 2, qb = s.nv_b * (s.nv_b - 1) / 2;
+    if (c < sb) {
+        // Beta single (0-1 excitation).
+        const int i = c / s.nv_b, x = c % s.nv_b;
+        const int ii = s.occ_b[i], jj = s.vir_b[x];
+        flip(b, ii);
+        flip(b, jj);
+        const int64_t col = column_of<NW>(p, a, b);
+        if (VALUES && keep_entry(p, row, col)) {
+            double v1 = __ldg(&one[ii * n + jj]);
+            for (int t = 0; t < s.no_a; ++t) {
+                const int kk = s.occ_a[t];
+                v1 += two_mo_at(two, n, ii, kk, jj, kk);
+            }
+            for (int t = 0; t < s.no_b; ++t) {
+                const int kk = s.occ_b[t];
+                v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
+            }
+            val = phase_single<NW>(s.rb, ii, jj) * v1;
+        }
+        return col;
+    }
+    c -= sb;
+    if (c < pa * qa || c < pa * qa + pb * qb) {
+        const bool alpha = c < pa * qa;
+        const int q = alpha ? c : c - pa * qa;
+        const int qq = alpha ? qa : qb;
+        const int po = q / qq, pv = q % qq;
+        int i, k, x, y;
+        decode_pair(po, i, k);
+        decode_pair(pv, x, y);
+        const int16_t *occ = alpha ? s.occ_a : s.occ_b;
+        const int16_t *vir = alpha ? s.vir_a : s.vir_b;
+        const int ii = occ[i], kk = occ[k], jj = vir[x], ll = vir[y];
+        uint64_t *d = alpha ? a : b;
+        flip(d, ii);
+        flip(d, kk);
+        flip(d, jj);
+        flip(d, ll);
+        const int64_t col = column_of<NW>(p, a, b);
+        if (VALUES && keep_entry(p, row, col))
+            val = phase_double<NW>(alpha ? s.ra : s.rb, ii, kk, jj, ll) *
+                  (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+        return col;
+    }
+    c -= pa * qa + pb * qb;
+    // Opposite-spin double (1-1 excitation).
+    const int ia = c / sb, ib = c % sb;
+    const int ii = s.occ_a[ia / s.nv_a], jj = s.vir_a[ia % s.nv_a];
+    const int kk = s.occ_b[ib / s.nv_b], ll = s.vir_b[ib % s.nv_b];
+    flip(a, ii);
+    flip(a, jj);
+    flip(b, kk);
+    flip(b, ll);
+    const int64_t col = column_of<NW>(p, a, b);
+    if (VALUES && keep_entry(p, row, col))
+        val = (phase_single<NW>(s.ra, ii, jj) * phase_single<NW>(s.rb, kk, ll)) *
+              two_mo_at(two, n, ii, kk, jj, ll);
+    return col;
+}
+
+// Diagonal element in the reference's summation order.
+__device__ double diagonal(const BuildParams &p, const RowState &s) {
+    const int n = p.nbasis;
+    const double *one = p.one_mo, *two = p.two_mo;
+    if (p.kind == PYCI_WFN_DOCI) {
+        double v1 = 0.0, v2 = 0.0;
+        for (int i = 0; i < s.no_a; ++i) {
+            const int k = s.occ_a[i];
+            v1 += __ldg(&p.v[k * (n + 1)]);
+            v2 += __ldg(&p.h[k]);
+            for (int j = i + 1; j < s.no_a; ++j)
+                v2 += __ldg(&p.w[k * n + s.occ_a[j]]);
+        }
+        return v1 + v2 * 2;
+    }
+    double v2 = 0.0;
+    for (int i = 0; i < s.no_a; ++i) {
+        const int ii = s.occ_a[i];
+        v2 += __ldg(&one[(n + 1) * ii]);
+        for (int k = i + 1; k < s.no_a; ++k) {
+            const int kk = s.occ_a[k];
+            v2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
+        }
+        for (int k = 0; k < s.no_b; ++k) {
+            const int kk = s.occ_b[k];
+            v2 += two_mo_at(two, n, ii, kk, ii, kk);
+        }
+    }
+    for (int i = 0; i < s.no_b; ++i) {
+        const int ii = s.occ_b[i];
+        v2 += __ldg(&one[(n + 1) * ii]);
+        for (int k = i + 1; k < s.no_b; ++k) {
+            const int kk = s.occ_b[k];
+            v2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
+        }
+    }
+    return v2;
+}
+
+// Pass 1: stored entries per row.
+template<int NW>
+__global__ void __launch_bounds__(256) count_kernel(BuildParams p, int64_t row0) {
+    __shared__ RowState s;
+    __shared__ int total;
+    const int64_t row = row0 + blockIdx.x;
+    if (row >= p.nrow)
+        return;
+    if (threadIdx.x == 0)
+        total = 0;
+    load_row<NW>(p, row, s);
+    const int nc = num_candidates(p, s);
+    int mine = 0;
+    double dummy = 0.0;
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+        const int64_t col = candidate<NW, false>(p, s, row, c, dummy);
+        mine += keep_entry(p, row, col) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(&total, mine);
+    __syncthreads();
+    if (threadIdx.x == 0)
+        p.counts[row] = total + (keep_entry(p, row, row) ? 1 : 0);
+}
+
+// Pass 2: matrix elements, in-row sort, write-out.  Dynamic shared memory
+// holds `cap` (power of two >= candidates + 1) keys and values.
+template<int NW>
+__global__ void __launch_bounds__(256) fill_kernel(BuildParams p, int64_t row0, int cap) {
+    __shared__ RowState s;
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *sval = reinterpret_cast<double *>(smem);
+    int32_t *skey = reinterpret_cast<int32_t *>(smem + sizeof(double) * cap);
+    const int64_t row = row0 + blockIdx.x;
+    if (row >= p.nrow)
+        return;
+    load_row<NW>(p, row, s);
+    const int nc = num_candidates(p, s);
+    for (int c = threadIdx.x; c < cap; c += blockDim.x) {
+        int32_t key = kSentinel;
+        double val = 0.0;
+        if (c < nc) {
+            const int64_t col = candidate<NW, true>(p, s, row, c, val);
+            if (keep_entry(p, row, col))
+                key = static_cast<int32_t>(col);
+        } else if (c == nc) {
+            if (keep_entry(p, row, row)) {
+                key = static_cast<int32_t>(row);
+                val = diagonal(p, s);
+            }
+        }
+        skey[c] = key;
+        sval[c] = val;
+    }
+    __syncthreads();
+    // Bitonic sort of (key, value) pairs by key, ascending.
+    for (int size = 2; size <= cap; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < cap / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = ((lo & size) == 0);
+                const int32_t klo = skey[lo], khi = skey[hi];
+                if ((klo > khi) == up) {
+                    skey[lo] = khi;
+                    skey[hi] = klo;
+                    const double vlo = sval[lo];
+                    sval[lo] = sval[hi];
+                    sval[hi] = vlo;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const int64_t start = p.rowptr[row];
+    const int len = static_cast<int>(p.rowptr[row + 1] - start);
+    if (threadIdx.x == 0) {
+        if (len > cap || (len > 0 && skey[len - 1] == kSentinel) || (len < cap && skey[len] != kSentinel))
+            atomicExch(p.error, 1);
+    }
+    for (int t = threadIdx.x; t < len && t < cap; t += blockDim.x) {
+        const int32_t key = skey[t];
+        p.cols[start + t] = key;
+        p.vals[start + t] = sval[t];
+        if (key == row)
+            p.diag[row] = sval[t];
+        const bool last_lower = (key <= row) && (t + 1 == len || skey[t + 1] > row);
+        if (last_lower && p.lower_len)
+            p.lower_len[row] = t + 1;
+    }
+    if (threadIdx.x == 0 && p.lower_len && (len == 0 || skey[0] > row))
+        p.lower_len[row] = 0;
+}
+
+// Insert every determinant index into the table (linear probing).
+template<int NWT>
+__global__ void table_insert_kernel(int32_t *slots, uint64_t mask, const uint64_t *dets,
+                                    int64_t ndet, int *error) {
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= ndet)
+        return;
+    uint64_t key[NWT];
+#pragma unroll
+    for (int w = 0; w < NWT; ++w)
+        key[w] = dets[i * NWT + w];
+    uint64_t s = hash_words(key, NWT) & mask;
+    for (uint64_t probe = 0; probe <= mask; ++probe) {
+        const int32_t prev = atomicCAS(&slots[s], -1, static_cast<int32_t>(i));
+        if (prev == -1)
+            return;
+        bool eq = true;
+#pragma unroll
+        for (int w = 0; w < NWT; ++w)
+            eq &= (dets[static_cast<int64_t>(prev) * NWT + w] == key[w]);
+        if (eq) {
+            // Duplicate determinant: keep the smaller (first-inserted) index.
+            atomicMin(&slots[s], static_cast<int32_t>(i));
+            return;
+        }
+        s = (s + 1) & mask;
+    }
+    atomicExch(error, 2);
+}
+
+// ---------------- exclusive scan of int64 counts ----------------
+
+constexpr int kScanBlock = 1024;
+
+__global__ void scan_block_sums(const int64_t *in, int64_t n, int64_t *sums) {
+    __shared__ int64_t red[32];
+    const int64_t i0 = static_cast<int64_t>(blockIdx.x) * kScanBlock;
+    int64_t v = 0;
+    for (int t = threadIdx.x; t < kScanBlock; t += blockDim.x)
+        if (i0 + t < n)
+            v += in[i0 + t];
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0)
+            sums[blockIdx.x] = v;
+    }
+}
+
+// Exclusive scan of the block sums in place, single block.
+__global__ void scan_sums_serial(int64_t *sums, int64_t nblocks, int64_t *total) {
+    if (threadIdx.x != 0 || blockIdx.x != 0)
+        return;
+    int64_t acc = 0;
+    for (int64_t b = 0; b < nblocks; ++b) {
+        const int64_t v = sums[b];
+        sums[b] = acc;
+        acc += v;
+    }
+    *total = acc;
+}
+
+// out[i] = sums[block] + exclusive scan within the block; out has n + 1 slots.
+__global__ void scan_apply(const int64_t *in, int64_t n, const int64_t *sums, const int64_t *total,
+                           int64_t *out) {
+    __shared__ int64_t buf[kScanBlock];
+    const int64_t i0 = static_cast<int64_t>(blockIdx.x) * kScanBlock;
+    for (int t = threadIdx.x; t < kScanBlock; t += blockDim.x)
+        buf[t] = (i0 + t < n) ? in[i0 + t] : 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t acc = sums[blockIdx.x];
+        for (int t = 0; t < kScanBlock; ++t) {
+            const int64_t v = buf[t];
+            buf[t] = acc;
+            acc += v;
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kScanBlock; t += blockDim.x)
+        if (i0 + t < n)
+            out[i0 + t] = buf[t];
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        out[n] = *total;
+}
+
+// ---------------- GenCI in the reference's own row loop ----------------
+//
+// GenCIWfn inherits Wfn::init's nvir = 2 * nbasis - nocc (pyci/src/wfn.cpp:62),
+// although nbasis already counts spin-orbitals, and add_row<GenCIWfn>
+// (pyci/src/sparseop.cpp:429-502) loops j < wfn.nvir over a virs buffer whose
+// entries past the true virtual count stay 0 (zero-initialised at
+// pyci/src/sparseop.cpp:190).  The loop therefore also "excites" into orbital
+// 0, and its excite_det restores (clear i, set a) can drop orbital 0 from the
+// working determinant for the rest of the row.  These kernels replay that
+// loop step by step (one thread per row) so the matrix matches the
+// reference's entry for entry; PYCI_BUILD_GENCI_EXACT selects the
+// Slater-Condon rules over the true virtuals instead.
+
+__device__ __forceinline__ void excite_ref(uint64_t *det, int i, int a) {
+    det[i >> 6] &= ~(1ULL << (i & 63));
+    det[a >> 6] |= 1ULL << (a & 63);
+}
+
+__device__ __forceinline__ bool keep_ref(const BuildParams &p, int64_t idet, int64_t jdet) {
+    const int64_t jmin = p.symmetric ? idet : INT64_MAX;
+    return (jdet != -1) && (jdet < jmin) && (jdet < row_limit(p, idet));
+}
+
+// Replays one row; calls emit(col, value) for every appended entry.
+template<int NW, bool VALUES, class Emit>
+__device__ void genci_ref_row(const BuildParams &p, int64_t idet, Emit emit) {
+    const int n = p.nbasis;
+    const double *one = p.one_mo, *two = p.two_mo;
+    uint64_t rdet[NW], det[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+        rdet[w] = det[w] = p.dets[idet * NW + w];
+    int16_t occs[kMaxOcc], virs[2 * kMaxVir];
+    const int no = occ_list<NW>(rdet, occs);
+    const int nv_true = vir_list<NW>(rdet, n, virs);
+    const int nv = 2 * n - p.nocc_up - p.nocc_dn;
+    for (int j = nv_true; j < nv; ++j)
+        virs[j] = 0;
+    double val2 = 0.0;
+    for (int i = 0; i < no; ++i) {
+        const int ii = occs[i];
+        if (VALUES) {
+            val2 += __ldg(&one[(n + 1) * ii]);
+            for (int k = i + 1; k < no; ++k) {
+                const int kk = occs[k];
+                val2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
+            }
+        }
+        for (int j = 0; j < nv; ++j) {
+            const int jj = virs[j];
+            excite_ref(det, ii, jj);
+            int64_t jdet = p.table.find<NW>(det);
+            if (keep_ref(p, idet, jdet)) {
+                double v = 0.0;
+                if (VALUES) {
+                    double v1 = __ldg(&one[n * ii + jj]);
+                    for (int k = 0; k < no; ++k) {
+                        const int kk = occs[k];
+                        v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
+                    }
+                    v = phase_single<NW>(rdet, ii, jj) * v1;
+                }
+                emit(jdet, v);
+            }
+            for (int k = i + 1; k < no; ++k) {
+                const int kk = occs[k];
+                for (int l = j + 1; l < nv; ++l) {
+                    const int ll = virs[l];
+                    excite_ref(det, kk, ll);
+                    jdet = p.table.find<NW>(det);
+                    if (keep_ref(p, idet, jdet))
+                        emit(jdet, VALUES ? phase_double<NW>(rdet, ii, kk, jj, ll) *
+                                                (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj))
+                                          : 0.0);
+                    excite_ref(det, ll, kk);
+                }
+            }
+            excite_ref(det, jj, ii);
+        }
+    }
+    if (idet < row_limit(p, idet))
+        emit(idet, val2);
+}
+
+template<int NW>
+__global__ void genci_ref_count_kernel(BuildParams p) {
+    const int64_t row = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (row >= p.nrow)
+        return;
+    int64_t cnt = 0;
+    genci_ref_row<NW, false>(p, row, [&](int64_t, double) { ++cnt; });
+    p.counts[row] = cnt;
+}
+
+// One block per row: thread 0 replays the row into shared memory, then the
+// block sorts it by column and writes it out.
+template<int NW>
+__global__ void __launch_bounds__(256) genci_ref_fill_kernel(BuildParams p, int64_t row0, int cap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *sval = reinterpret_cast<double *>(smem);
+    int32_t *skey = reinterpret_cast<int32_t *>(smem + sizeof(double) * cap);
+    const int64_t row = row0 + blockIdx.x;
+    if (row >= p.nrow)
+        return;
+    for (int c = threadIdx.x; c < cap; c += blockDim.x) {
+        skey[c] = kSentinel;
+        sval[c] = 0.0;
+    }
+    __syncthreads();
+    const int64_t start = p.rowptr[row];
+    const int len = static_cast<int>(p.rowptr[row + 1] - start);
+    if (threadIdx.x == 0) {
+        int t = 0;
+        genci_ref_row<NW, true>(p, row, [&](int64_t col, double v) {
+            if (t < cap) {
+                skey[t] = static_cast<int32_t>(col);
+                sval[t] = v;
+            }
+            ++t;
+        });
+        if (t != len)
+            atomicExch(p.error, 3);
+    }
+    __syncthreads();
+    for (int size = 2; size <= cap; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < cap / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = ((lo & size) == 0);
+                const int32_t klo = skey[lo], khi = skey[hi];
+                if ((klo > khi) == up) {
+                    skey[lo] = khi;
+                    skey[hi] = klo;
+                    const double vlo = sval[lo];
+                    sval[lo] = sval[hi];
+                    sval[hi] = vlo;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int t = threadIdx.x; t < len && t < cap; t += blockDim.x) {
+        p.cols[start + t] = skey[t];
+        p.vals[start + t] = sval[t];
+        if (skey[t] == row)
+            p.diag[row] = sval[t];
+    }
+    if (threadIdx.x == 0 && p.lower_len)
+        p.lower_len[row] = len;
+}
+
+__global__ void max_kernel(const int64_t *v, int64_t n, unsigned long long *out) {
+    unsigned long long m = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        m = max(m, static_cast<unsigned long long>(v[i]));
+    for (int o = 16; o > 0; o >>= 1)
+        m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0)
+        atomicMax(out, m);
+}
+
+__global__ void widen_kernel(const int32_t *in, int64_t *out, int64_t n) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = in[i];
+}
+
+} // namespace pyci_gpu
+
+using namespace pyci_gpu;
+
+int64_t host_binomial(int64_t n, int64_t k) {
+    if (k < 0 || n < 0 || k > n)
+        return 0;
+    if (k == 0 || k == n)
+        return 1;
+    if (k > n / 2)
+        k = n - k;
+    __int128 b = 1;
+    for (int64_t d = 1; d <= k; ++d) {
+        b = b * (n - k + d) / d;
+        if (b > INT64_MAX)
+            return INT64_MAX;
+    }
+    return static_cast<int64_t>(b);
+}
+
+// Exclusive scan of counts[n] into out[n + 1] on `stream`.
+int device_exclusive_scan(const int64_t *counts, int64_t n, int64_t *out, cudaStream_t stream) {
+    const int64_t nblocks = (n + kScanBlock - 1) / kScanBlock;
+    int64_t *sums = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(&sums, sizeof(int64_t) * (nblocks + 1), stream));
+    if (nblocks > 0) {
+        scan_block_sums<<<nblocks, 256, 0, stream>>>(counts, n, sums), ::pyci_gpu::note_launch();
+        scan_sums_serial<<<1, 32, 0, stream>>>(sums, nblocks, sums + nblocks), ::pyci_gpu::note_launch();
+        scan_apply<<<nblocks, 256, 0, stream>>>(counts, n, sums, sums + nblocks, out), ::pyci_gpu::note_launch();
+    } else {
+        PYCI_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(int64_t), stream));
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    PYCI_CUDA_TRY(cudaFreeAsync(sums, stream));
+    return PYCI_GPU_OK;
+}
+
+namespace {
+
+struct DeviceBuffers {
+    cudaStream_t s;
+    std::vector<void *> ptrs;
+    explicit DeviceBuffers(cudaStream_t st) : s(st) {}
+    template<typename T>
+    cudaError_t alloc(T **p, size_t count) {
+        cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(p), sizeof(T) * (count ? count : 1), s);
+        if (e == cudaSuccess)
+            ptrs.push_back(*p);
+        return e;
+    }
+    ~DeviceBuffers() {
+        for (void *p : ptrs)
+            cudaFreeAsync(p, s);
+    }
+};
+
+int pick_nw(int64_t nbasis) {
+    if (nbasis <= 64)
+        return 1;
+    if (nbasis <= 128)
+        return 2;
+    if (nbasis <= 256)
+        return 4;
+    return 0;
+}
+
+template<int NW>
+int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap) {
+    cudaStream_t st = ctx->stream;
+    const int64_t chunk = 1 << 20; // rows per launch (grid.x limit is generous; keeps launches short)
+    for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
+        const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
+        count_kernel<NW><<<static_cast<unsigned>(nb), 256, 0, st>>>(p, r0), ::pyci_gpu::note_launch();
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    int rc = device_exclusive_scan(p.counts, p.nrow, csr->rowptr, st);
+    if (rc)
+        return rc;
+    int64_t nnz = 0;
+    PYCI_CUDA_TRY(cudaMemcpyAsync(&nnz, csr->rowptr + p.nrow, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    PYCI_CUDA_TRY(cudaStreamSynchronize(st));
+    csr->nnz = nnz;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->cols), sizeof(int32_t) * (nnz ? nnz : 1), st));
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->vals), sizeof(double) * (nnz ? nnz : 1), st));
+    PYCI_CUDA_TRY(cudaMemsetAsync(csr->diag, 0, sizeof(double) * (p.nrow ? p.nrow : 1), st));
+    p.rowptr = csr->rowptr;
+    p.cols = csr->cols;
+    p.vals = csr->vals;
+    p.diag = csr->diag;
+    p.lower_len = csr->lower_len;
+    const size_t smem = static_cast<size_t>(cap) * (sizeof(double) + sizeof(int32_t));
+    if (smem > 48 * 1024) {
+        if (smem > ctx->smem_optin) {
+            set_error("a row has %d candidate entries, more than shared memory holds", cap);
+            return PYCI_GPU_EUNSUPPORTED;
+        }
+        PYCI_CUDA_TRY(cudaFuncSetAttribute(fill_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem)));
+    }
+    const int threads = cap >= 512 ? 256 : (cap >= 256 ? 128 : 64);
+    for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
+        const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
+        fill_kernel<NW><<<static_cast<unsigned>(nb), threads, smem, st>>>(p, r0, cap), ::pyci_gpu::note_launch();
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+template<int NW>
+int run_build_genci_ref(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr) {
+    cudaStream_t st = ctx->stream;
+    if (p.nrow > 0)
+        genci_ref_count_kernel<NW><<<static_cast<unsigned>((p.nrow + 127) / 128), 128, 0, st>>>(p), ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    int rc = device_exclusive_scan(p.counts, p.nrow, csr->rowptr, st);
+    if (rc)
+        return rc;
+    unsigned long long *d_max = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&d_max), sizeof(unsigned long long), st));
+    PYCI_CUDA_TRY(cudaMemsetAsync(d_max, 0, sizeof(unsigned long long), st));
+    if (p.nrow > 0)
+        max_kernel<<<static_cast<unsigned>(std::min<int64_t>((p.nrow + 255) / 256, 1024)), 256, 0, st>>>(p.counts, p.nrow, d_max), ::pyci_gpu::note_launch();
+    unsigned long long maxlen = 0;
+    int64_t nnz = 0;
+    PYCI_CUDA_TRY(cudaMemcpyAsync(&maxlen, d_max, sizeof(maxlen), cudaMemcpyDeviceToHost, st));
+    PYCI_CUDA_TRY(cudaMemcpyAsync(&nnz, csr->rowptr + p.nrow, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    PYCI_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFreeAsync(d_max, st);
+    csr->nnz = nnz;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->cols), sizeof(int32_t) * (nnz ? nnz : 1), st));
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->vals), sizeof(double) * (nnz ? nnz : 1), st));
+    PYCI_CUDA_TRY(cudaMemsetAsync(csr->diag, 0, sizeof(double) * (p.nrow ? p.nrow : 1), st));
+    p.rowptr = csr->rowptr;
+    p.cols = csr->cols;
+    p.vals = csr->vals;
+    p.diag = csr->diag;
+    p.lower_len = csr->lower_len;
+    int cap = 2;
+    while (static_cast<unsigned long long>(cap) < maxlen)
+        cap <<= 1;
+    const size_t smem = static_cast<size_t>(cap) * (sizeof(double) + sizeof(int32_t));
+    if (smem > ctx->smem_optin) {
+        set_error("a GenCI row has %llu entries, more than shared memory holds", maxlen);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    if (smem > 48 * 1024)
+        PYCI_CUDA_TRY(cudaFuncSetAttribute(genci_ref_fill_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(smem)));
+    const int64_t chunk = 1 << 20;
+    for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
+        const int64_t nb = std::min(chunk, p.nrow - r0);
+        genci_ref_fill_kernel<NW><<<static_cast<unsigned>(nb), 128, smem, st>>>(p, r0, cap), ::pyci_gpu::note_launch();
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+} // namespace
+
+int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_host,
+                     const double *one_mo, const double *two_mo, int64_t legacy_nrow,
+                     int64_t legacy_ncol) {
+    cudaStream_t st = ctx->stream;
+    const int64_t n = csr->nbasis;
+    const int nw = pick_nw(n);
+    if (nw == 0) {
+        set_error("nbasis = %lld exceeds the 256 orbitals the GPU build supports", (long long)n);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    if (csr->nocc_up > kMaxOcc || csr->nocc_dn > kMaxOcc || n - csr->nocc_dn > kMaxVir) {
+        set_error("occupation numbers exceed the GPU build's limits (%d occupied)", kMaxOcc);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    if (csr->ndet >= INT32_MAX || csr->ncol >= INT32_MAX) {
+        set_error("more than 2^31 - 1 determinants is not supported");
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    const bool genci_ref = (csr->kind == PYCI_WFN_GENCI) && !(csr->flags & PYCI_BUILD_GENCI_EXACT);
+    const bool colex = (csr->flags & PYCI_BUILD_FULL_COLEX) && !(csr->flags & PYCI_BUILD_FORCE_HASH) && !genci_ref;
+    csr->lower_only = genci_ref && csr->symmetric;
+    if (genci_ref && dets_host == nullptr && csr->ndet > 0) {
+        set_error("the reference GenCI row loop needs the determinant array");
+        return PYCI_GPU_EINVAL;
+    }
+    if (!colex && dets_host == nullptr && csr->ndet > 0) {
+        set_error("determinant array is required unless the wave function is the full space");
+        return PYCI_GPU_EINVAL;
+    }
+    const int kind = csr->kind;
+    const int64_t nwords = (kind == PYCI_WFN_FULLCI ? 2 : 1) * static_cast<int64_t>(nw);
+    const int64_t host_nword = (n + 63) / 64;
+
+    DeviceBuffers tmp(st);
+    BuildParams p{};
+    p.kind = kind;
+    p.nbasis = static_cast<int>(n);
+    p.nocc_up = static_cast<int>(csr->nocc_up);
+    p.nocc_dn = static_cast<int>(csr->nocc_dn);
+    p.genci_exact = (csr->flags & PYCI_BUILD_GENCI_EXACT) ? 1 : 0;
+    p.colex = colex ? 1 : 0;
+    p.symmetric = csr->symmetric ? 1 : 0;
+    p.ndet = csr->ndet;
+    p.nrow = csr->nrow;
+    p.ncol = csr->ncol;
+    p.legacy_nrow = legacy_nrow;
+    p.legacy_ncol = legacy_ncol;
+    p.nbeta = (kind == PYCI_WFN_FULLCI) ? host_binomial(n, csr->nocc_dn) : 1;
+
+    // Binomial table C(m, k), m <= nbasis, k <= max occupation + 1.
+    const int ldk = static_cast<int>(std::max(csr->nocc_up, csr->nocc_dn) + 2);
+    std::vector<int64_t> binom((n + 1) * ldk);
+    for (int64_t m = 0; m <= n; ++m)
+        for (int k = 0; k < ldk; ++k)
+            binom[m * ldk + k] = host_binomial(m, k);
+    int64_t *d_binom = nullptr;
+    PYCI_CUDA_TRY(tmp.alloc(&d_binom, binom.size()));
+    PYCI_CUDA_TRY(cudaMemcpyAsync(d_binom, binom.data(), sizeof(int64_t) * binom.size(),
+                                  cudaMemcpyHostToDevice, st));
+    p.binom = d_binom;
+    p.ldk = ldk;
+
+    // Integrals and the seniority-zero h, v, w (pyci/src/squantop.cpp:175-182).
+    const int64_t n2 = n * n, n4 = n2 * n2;
+    double *d_one = nullptr, *d_two = nullptr, *d_h = nullptr, *d_v = nullptr, *d_w = nullptr;
+    PYCI_CUDA_TRY(tmp.alloc(&d_one, n2));
+    PYCI_CUDA_TRY(tmp.alloc(&d_two, n4));
+    PYCI_CUDA_TRY(cudaMemcpyAsync(d_one, one_mo, sizeof(double) * n2, cudaMemcpyHostToDevice, st));
+    PYCI_CUDA_TRY(cudaMemcpyAsync(d_two, two_mo, sizeof(double) * n4, cudaMemcpyHostToDevice, st));
+    if (kind == PYCI_WFN_DOCI) {
+        std::vector<double> h(n), v(n2), w(n2);
+        for (int64_t i = 0; i < n; ++i) {
+            h[i] = one_mo[i * (n + 1)];
+            for (int64_t j = 0; j < n; ++j) {
+                v[i * n + j] = two_mo[i * n * n2 + i * n2 + j * n + j];
+                w[i * n + j] = two_mo[i * n * n2 + j * n2 + i * n + j] * 2 - two_mo[i * n * n2 + j * n2 + j * n + i];
+            }
+        }
+        PYCI_CUDA_TRY(tmp.alloc(&d_h, n));
+        PYCI_CUDA_TRY(tmp.alloc(&d_v, n2));
+        PYCI_CUDA_TRY(tmp.alloc(&d_w, n2));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_h, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_v, v.data(), sizeof(double) * n2, cudaMemcpyHostToDevice, st));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_w, w.data(), sizeof(double) * n2, cudaMemcpyHostToDevice, st));
+        // The host vectors die at scope end: wait for the copies.
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    p.one_mo = d_one;
+    p.two_mo = d_two;
+    p.h = d_h;
+    p.v = d_v;
+    p.w = d_w;
+
+    int *d_err = nullptr;
+    PYCI_CUDA_TRY(tmp.alloc(&d_err, 1));
+    PYCI_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+    p.error = d_err;
+
+    // Determinants (repacked to nw words per string) and the hash table.
+    if (!colex) {
+        std::vector<uint64_t> packed(static_cast<size_t>(csr->ndet * nwords), 0ULL);
+        const int nstr = (kind == PYCI_WFN_FULLCI) ? 2 : 1;
+        for (int64_t i = 0; i < csr->ndet; ++i)
+            for (int sidx = 0; sidx < nstr; ++sidx)
+                for (int64_t w = 0; w < host_nword; ++w)
+                    packed[i * nwords + sidx * nw + w] = dets_host[(i * nstr + sidx) * host_nword + w];
+        uint64_t *d_dets = nullptr;
+        PYCI_CUDA_TRY(tmp.alloc(&d_dets, packed.size()));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_dets, packed.data(), sizeof(uint64_t) * packed.size(),
+                                      cudaMemcpyHostToDevice, st));
+        uint64_t cap = 16;
+        while (cap < static_cast<uint64_t>(2 * csr->ndet))
+            cap <<= 1;
+        int32_t *slots = nullptr;
+        PYCI_CUDA_TRY(tmp.alloc(&slots, cap));
+        PYCI_CUDA_TRY(cudaMemsetAsync(slots, 0xff, sizeof(int32_t) * cap, st));
+        const unsigned blocks = static_cast<unsigned>((csr->ndet + 255) / 256);
+        if (blocks) {
+            switch (nwords) {
+            case 1: table_insert_kernel<1><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, csr->ndet, d_err), ::pyci_gpu::note_launch(); break;
+            case 2: table_insert_kernel<2><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, csr->ndet, d_err), ::pyci_gpu::note_launch(); break;
+            case 4: table_insert_kernel<4><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, csr->ndet, d_err), ::pyci_gpu::note_launch(); break;
+            case 8: table_insert_kernel<8><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, csr->ndet, d_err), ::pyci_gpu::note_launch(); break;
+            default: set_error("unsupported determinant width"); return PYCI_GPU_EUNSUPPORTED;
+            }
+            PYCI_CUDA_TRY(cudaGetLastError());
+        }
+        p.dets = d_dets;
+        p.table = DetTable{slots, d_dets, cap - 1, static_cast<int>(nwords)};
+        // `packed` must outlive the copy.
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+
+    // Candidate capacity: largest row, rounded up to a power of two.
+    int64_t no_a = csr->nocc_up, no_b = (kind == PYCI_WFN_FULLCI) ? csr->nocc_dn : 0;
+    int64_t nv_a = n - no_a, nv_b = (kind == PYCI_WFN_FULLCI) ? n - no_b : 0;
+    int64_t ncand;
+    if (kind == PYCI_WFN_DOCI) {
+        ncand = no_a * nv_a;
+    } else {
+        const int64_t sa = no_a * nv_a, sb = no_b * nv_b;
+        const int64_t da = (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
+        const int64_t db = (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
+        ncand = sa + sb + da + db + sa * sb;
+    }
+    int64_t cap = 2;
+    while (cap < ncand + 1)
+        cap <<= 1;
+    if (cap > (1 << 22)) {
+        set_error("rows with %lld candidate excitations are not supported", (long long)ncand);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+
+    int64_t *d_counts = nullptr;
+    PYCI_CUDA_TRY(tmp.alloc(&d_counts, csr->nrow));
+    p.counts = d_counts;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->rowptr), sizeof(int64_t) * (csr->nrow + 1), st));
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->diag), sizeof(double) * (csr->nrow ? csr->nrow : 1), st));
+    if (csr->symmetric) {
+        PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->lower_len), sizeof(int32_t) * (csr->nrow ? csr->nrow : 1), st));
+        PYCI_CUDA_TRY(cudaMemsetAsync(csr->lower_len, 0, sizeof(int32_t) * (csr->nrow ? csr->nrow : 1), st));
+    }
+
+    int rc;
+    if (genci_ref) {
+        switch (nw) {
+        case 1: rc = run_build_genci_ref<1>(ctx, p, csr); break;
+        case 2: rc = run_build_genci_ref<2>(ctx, p, csr); break;
+        default: rc = run_build_genci_ref<4>(ctx, p, csr); break;
+        }
+    } else {
+        switch (nw) {
+        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap)); break;
+        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap)); break;
+        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap)); break;
+        }
+    }
+    if (rc)
+        return rc;
+
+    // Reference-layout row pointers (symmetric: prefix sums of lower_len).
+    if (csr->symmetric) {
+        int64_t *lens64 = nullptr;
+        PYCI_CUDA_TRY(tmp.alloc(&lens64, csr->nrow));
+        if (csr->nrow > 0)
+            widen_kernel<<<static_cast<unsigned>(std::min<int64_t>((csr->nrow + 255) / 256, 1 << 16)), 256, 0, st>>>(
+                csr->lower_len, lens64, csr->nrow), ::pyci_gpu::note_launch();
+        PYCI_CUDA_TRY(cudaGetLastError());
+        PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->ref_rowptr), sizeof(int64_t) * (csr->nrow + 1), st));
+        rc = device_exclusive_scan(lens64, csr->nrow, csr->ref_rowptr, st);
+        if (rc)
+            return rc;
+        PYCI_CUDA_TRY(cudaMemcpyAsync(&csr->nnz_ref, csr->ref_rowptr + csr->nrow, sizeof(int64_t),
+                                      cudaMemcpyDeviceToHost, st));
+    } else {
+        csr->nnz_ref = csr->nnz;
+    }
+    int herr = 0;
+    PYCI_CUDA_TRY(cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PYCI_CUDA_TRY(cudaStreamSynchronize(st));
+    if (herr) {
+        set_error("internal inconsistency in the CSR build (code %d)", herr);
+        return PYCI_GPU_ECUDA;
+    }
+    return PYCI_GPU_OK;
+}
+

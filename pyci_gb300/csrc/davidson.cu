@@ -1,0 +1,726 @@
+// Block Davidson eigensolver on the device CSR, replacing SparseOp::solve_ci
+// (pyci/src/sparseop.cpp:114-146), which runs Spectra's implicitly restarted
+// Lanczos on the host.  Same contract: the n algebraically smallest
+// eigenpairs, ecore added, returned in decreasing order (Spectra's result
+// order), ValueError / TypeError / RuntimeError conditions preserved.
+//
+// Layout: basis V and W = H V as [m][N] (one vector per row, contiguous, for
+// coalesced tall-skinny products); the SpMM reads an interleaved [N][k]
+// copy.  Per iteration: W_new = H V_new (one SpMM for the whole block),
+// Gram column V^T W_new, Rayleigh-Ritz on the host (m <= ~64), Ritz vectors
+// and residuals, diagonal (Davidson) preconditioning, two-pass block
+// Gram-Schmidt, thick restart to the lowest Ritz vectors.
+//
+// Two precisions:
+//   FP64  -- values, vectors and products in FP64.
+//   MIXED -- FP32 values (high part of an exact FP32 high/low split), FP32
+//            vectors and SpMM; Gram sums finish in FP64; Rayleigh-Ritz in
+//            FP64.  When the FP32 residuals meet the tolerance, the Ritz
+//            vectors are rebuilt in FP64, multiplied by the FP64 operator
+//            (high + low values), re-orthonormalised and Rayleigh-Ritz'd in
+//            FP64; FP64 residuals decide convergence and, if still too large,
+//            seed further FP32 iterations.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#include "dense.h"
+#include "internal.h"
+
+namespace pyci_gpu {
+
+constexpr int kGramTile = 32;
+constexpr int kMaxGramP = 128;
+constexpr int kMaxQ = 8;
+
+// Xi[r * k + j] = V[j * N + r]
+template<typename T>
+__global__ void pack_kernel(const T *__restrict__ V, int64_t N, int k, T *__restrict__ Xi) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        for (int j = 0; j < k; ++j)
+            Xi[r * k + j] = V[j * N + r];
+}
+
+template<typename T>
+__global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, T *__restrict__ W) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        for (int j = 0; j < k; ++j)
+            W[j * N + r] = Yi[r * k + j];
+}
+
+// Partial Gram products: partial[block][i * q + j] = sum over the block's rows
+// of A[i][r] * B[j][r], for p <= kMaxGramP, q <= kMaxQ.  Rows are staged in
+// shared memory tiles of kGramTile; each tile's products are summed in the
+// storage type and added to an FP64 accumulator.
+template<typename T>
+__global__ void __launch_bounds__(256) gram_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
+                                                   int q, int64_t N, double *__restrict__ partial) {
+    __shared__ T sa[kMaxGramP][kGramTile + 1];
+    __shared__ T sb[kMaxQ][kGramTile + 1];
+    const int pq = p * q;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const int64_t ntiles = (N + kGramTile - 1) / kGramTile;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t r0 = t * kGramTile;
+        for (int e = threadIdx.x; e < p * kGramTile; e += blockDim.x) {
+            const int i = e / kGramTile, c = e % kGramTile;
+            sa[i][c] = (r0 + c < N) ? A[i * N + r0 + c] : T(0);
+        }
+        for (int e = threadIdx.x; e < q * kGramTile; e += blockDim.x) {
+            const int j = e / kGramTile, c = e % kGramTile;
+            sb[j][c] = (r0 + c < N) ? B[j * N + r0 + c] : T(0);
+        }
+        __syncthreads();
+        int slot = 0;
+        for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot) {
+            const int i = idx / q, j = idx % q;
+            T s = 0;
+#pragma unroll 8
+            for (int c = 0; c < kGramTile; ++c)
+                s += sa[i][c] * sb[j][c];
+            acc[slot] += static_cast<double>(s);
+        }
+        __syncthreads();
+    }
+    int slot = 0;
+    for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot)
+        partial[static_cast<int64_t>(blockIdx.x) * pq + idx] = acc[slot];
+}
+
+__global__ void reduce_partials_kernel(const double *__restrict__ partial, int nblocks, int pq,
+                                       double *__restrict__ out) {
+    const int idx = blockIdx.x;
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+        s += partial[static_cast<int64_t>(b) * pq + idx];
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0)
+        red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1)
+            s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0)
+            out[idx] = s;
+    }
+}
+
+// out[j][r] = beta * out[j][r] + sum_{i < p} Y[i * q + j] * V[i][r]
+// (accumulated in ACC; q <= kMaxQ).
+template<typename TV, typename TO, typename ACC>
+__global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, int p, int64_t N,
+                                                      const double *__restrict__ Y, int q,
+                                                      double beta, TO *__restrict__ out) {
+    __shared__ ACC sy[kMaxGramP * kMaxQ];
+    for (int e = threadIdx.x; e < p * q; e += blockDim.x)
+        sy[e] = static_cast<ACC>(Y[e]);
+    __syncthreads();
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        ACC acc[kMaxQ];
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+            acc[j] = 0;
+        for (int i = 0; i < p; ++i) {
+            const ACC v = static_cast<ACC>(V[i * N + r]);
+#pragma unroll
+            for (int j = 0; j < kMaxQ; ++j)
+                if (j < q)
+                    acc[j] += sy[i * q + j] * v;
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+            if (j < q) {
+                TO *o = out + j * N + r;
+                *o = (beta == 0.0) ? static_cast<TO>(acc[j])
+                                   : static_cast<TO>(static_cast<ACC>(beta) * static_cast<ACC>(*o) + acc[j]);
+            }
+    }
+}
+
+// R[j] = AX[j] - theta[j] X[j]; then, if precondition, R[j] /= (theta[j] - D)
+// with |theta - D| floored at 1e-8 (Davidson's diagonal preconditioner).
+template<typename T>
+__global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const double *__restrict__ theta,
+                                int q, int64_t N, T *__restrict__ R) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        for (int j = 0; j < q; ++j)
+            R[j * N + r] = static_cast<T>(static_cast<double>(AX[j * N + r]) - theta[j] * static_cast<double>(X[j * N + r]));
+}
+
+template<typename TI, typename TO>
+__global__ void precondition_kernel(const TI *__restrict__ R, const double *__restrict__ theta,
+                                    const double *__restrict__ diag, int q, int64_t N, TO *__restrict__ out) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double d = diag[r];
+        for (int j = 0; j < q; ++j) {
+            double den = theta[j] - d;
+            if (fabs(den) < 1e-8)
+                den = (den < 0.0) ? -1e-8 : 1e-8;
+            out[j * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
+        }
+    }
+}
+
+template<typename T>
+__global__ void scale_kernel(T *v, int64_t N, double s) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        v[r] = static_cast<T>(static_cast<double>(v[r]) * s);
+}
+
+template<typename TI, typename TO>
+__global__ void convert_kernel(const TI *__restrict__ in, TO *__restrict__ out, int64_t n) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < n;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[r] = static_cast<TO>(in[r]);
+}
+
+// V[j] = unit vector e_{idx[j]}.
+template<typename T>
+__global__ void unit_kernel(T *V, int64_t N, const int64_t *idx, int k) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        for (int j = 0; j < k; ++j)
+            V[j * N + r] = (r == idx[j]) ? T(1) : T(0);
+}
+
+// ------------------------------------------------------------------------
+
+struct Timer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    double total_ms = 0.0;
+};
+
+template<typename T>
+class Davidson {
+public:
+    Davidson(pyci_gpu_csr *csr, int64_t nroot, int64_t mmax, bool mixed)
+        : csr_(csr), st_(csr->ctx->stream), N_(csr->nrow), nroot_(nroot), mmax_(mmax), mixed_(mixed) {}
+
+    ~Davidson() {
+        for (void *p : allocs_)
+            cudaFreeAsync(p, st_);
+        if (ev0_)
+            cudaEventDestroy(ev0_);
+        if (ev1_)
+            cudaEventDestroy(ev1_);
+        cudaStreamSynchronize(st_);
+    }
+
+    int run(const double *c0, int64_t maxiter, double tol, double ecore, double *evals, double *evecs,
+            pyci_gpu_solve_stats *stats);
+
+private:
+    template<typename U>
+    int alloc(U **p, int64_t n) {
+        void *q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, sizeof(U) * std::max<int64_t>(n, 1), st_);
+        if (e != cudaSuccess)
+            return cuda_status(e, "cudaMallocAsync (eigensolver workspace)");
+        allocs_.push_back(q);
+        *p = static_cast<U *>(q);
+        return PYCI_GPU_OK;
+    }
+
+    unsigned grid(int64_t n) const {
+        const int64_t want = (n + 255) / 256;
+        return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, csr_->ctx->num_sms * 8)));
+    }
+
+    // C (p x q, row-major, host) = A^T B for vector sets A (p) and B (q).
+    template<typename U>
+    int gram(const U *A, int p, const U *B, int q, std::vector<double> &C) {
+        C.assign(static_cast<size_t>(p) * q, 0.0);
+        for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
+            const int pp = std::min(kMaxGramP, p - i0);
+            for (int j0 = 0; j0 < q; j0 += kMaxQ) {
+                const int qq = std::min(kMaxQ, q - j0);
+                const unsigned nb = std::min<unsigned>(gram_blocks_, static_cast<unsigned>((N_ + kGramTile - 1) / kGramTile));
+                gram_kernel<U><<<nb, 256, 0, st_>>>(A + static_cast<int64_t>(i0) * N_, pp,
+                                                     B + static_cast<int64_t>(j0) * N_, qq, N_, d_partial_), ::pyci_gpu::note_launch();
+                reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq, d_small_), ::pyci_gpu::note_launch();
+                std::vector<double> tmp(static_cast<size_t>(pp) * qq);
+                cudaError_t e = cudaMemcpyAsync(tmp.data(), d_small_, sizeof(double) * pp * qq,
+                                                cudaMemcpyDeviceToHost, st_);
+                if (e != cudaSuccess)
+                    return cuda_status(e, "gram copy");
+                e = cudaStreamSynchronize(st_);
+                if (e != cudaSuccess)
+                    return cuda_status(e, "gram");
+                for (int i = 0; i < pp; ++i)
+                    for (int j = 0; j < qq; ++j)
+                        C[static_cast<size_t>(i0 + i) * q + j0 + j] = tmp[static_cast<size_t>(i) * qq + j];
+            }
+        }
+        return PYCI_GPU_OK;
+    }
+
+    // out[j] = beta out[j] + sum_i Y[i][j] V[i]  (Y host, p x q row-major).
+    template<typename TV, typename TO, typename ACC>
+    int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out) {
+        for (int j0 = 0; j0 < q; j0 += kMaxQ) {
+            const int qq = std::min(kMaxQ, q - j0);
+            for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
+                const int pp = std::min(kMaxGramP, p - i0);
+                std::vector<double> sub(static_cast<size_t>(pp) * qq);
+                for (int i = 0; i < pp; ++i)
+                    for (int j = 0; j < qq; ++j)
+                        sub[static_cast<size_t>(i) * qq + j] = Y[static_cast<size_t>(i0 + i) * q + j0 + j];
+                cudaError_t e = cudaMemcpyAsync(d_coef_, sub.data(), sizeof(double) * sub.size(),
+                                                cudaMemcpyHostToDevice, st_);
+                if (e != cudaSuccess)
+                    return cuda_status(e, "combine coefficients");
+                combine_kernel<TV, TO, ACC><<<grid(N_), 256, 0, st_>>>(
+                    V + static_cast<int64_t>(i0) * N_, pp, N_, d_coef_, qq, (i0 == 0) ? beta : 1.0,
+                    out + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
+                // sub must stay alive until the copy has been consumed.
+                e = cudaStreamSynchronize(st_);
+                if (e != cudaSuccess)
+                    return cuda_status(e, "combine");
+            }
+        }
+        return PYCI_GPU_OK;
+    }
+
+    // W[0..k) = H V[0..k) (storage precision of T; FP64 uses f64 values).
+    int apply(const T *V, int k, T *W, int prec) {
+        for (int j0 = 0; j0 < k; j0 += kMaxQ) {
+            const int kk = std::min(kMaxQ, k - j0);
+            pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, Xi_), ::pyci_gpu::note_launch();
+            cudaEventRecord(ev0_, st_);
+            int rc = csr_spmm(csr_, prec, kk, Xi_, Yi_, st_);
+            if (rc)
+                return rc;
+            cudaEventRecord(ev1_, st_);
+            unpack_kernel<T><<<grid(N_), 256, 0, st_>>>(Yi_, N_, kk, W + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
+            cudaError_t e = cudaEventSynchronize(ev1_);
+            if (e != cudaSuccess)
+                return cuda_status(e, "SpMM");
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, ev0_, ev1_);
+            spmm_ms_ += ms;
+            matvecs_ += kk;
+        }
+        return PYCI_GPU_OK;
+    }
+
+    // Orthonormalise vectors V[m..m+k) against V[0..m) and each other
+    // (classical Gram-Schmidt, two passes); drops near-dependent vectors.
+    // Returns the number kept (compacted to V[m..)).
+    int orthonormalize(T *V, int m, int k, int &kept);
+
+    pyci_gpu_csr *csr_;
+    cudaStream_t st_;
+    int64_t N_, nroot_, mmax_;
+    bool mixed_;
+    std::vector<void *> allocs_;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    double spmm_ms_ = 0.0;
+    int64_t matvecs_ = 0, matvecs64_ = 0;
+    unsigned gram_blocks_ = 1;
+    T *Xi_ = nullptr, *Yi_ = nullptr;
+    double *d_partial_ = nullptr, *d_small_ = nullptr, *d_coef_ = nullptr, *d_theta_ = nullptr;
+};
+
+template<typename T>
+int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
+    const double drop = mixed_ ? 1e-3 : 1e-8;
+    kept = 0;
+    std::vector<double> C;
+    for (int j = 0; j < k; ++j) {
+        T *t = V + static_cast<int64_t>(m + j) * N_;
+        int rc = gram<T>(t, 1, t, 1, C);
+        if (rc)
+            return rc;
+        const double n0 = std::sqrt(std::max(C[0], 0.0));
+        if (!(n0 > 0.0) || !std::isfinite(n0))
+            continue;
+        const int have = m + kept;
+        for (int pass = 0; pass < 2 && have > 0; ++pass) {
+            rc = gram<T>(V, have, t, 1, C);
+            if (rc)
+                return rc;
+            for (double &c : C)
+                c = -c;
+            rc = combine<T, T, double>(V, have, C, 1, 1.0, t);
+            if (rc)
+                return rc;
+        }
+        rc = gram<T>(t, 1, t, 1, C);
+        if (rc)
+            return rc;
+        const double n1 = std::sqrt(std::max(C[0], 0.0));
+        if (!(n1 > drop * n0))
+            continue;
+        T *dst = V + static_cast<int64_t>(m + kept) * N_;
+        scale_kernel<T><<<grid(N_), 256, 0, st_>>>(t, N_, 1.0 / n1), ::pyci_gpu::note_launch();
+        if (dst != t)
+            cudaMemcpyAsync(dst, t, sizeof(T) * N_, cudaMemcpyDeviceToDevice, st_);
+        ++kept;
+    }
+    return PYCI_GPU_OK;
+}
+
+template<typename T>
+int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore, double *evals,
+                     double *evecs, pyci_gpu_solve_stats *stats) {
+    const auto t_start = std::chrono::steady_clock::now();
+    const int64_t N = N_;
+    const int b = static_cast<int>(nroot_);
+    const int mmax = static_cast<int>(mmax_);
+    const bool full_space = (N <= mmax);
+    const int prec = mixed_ ? PYCI_PREC_FP32 : PYCI_PREC_FP64;
+    int rc;
+    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess)
+        return cuda_status(cudaGetLastError(), "cudaEventCreate");
+    gram_blocks_ = static_cast<unsigned>(csr_->ctx->num_sms * 4);
+
+    T *V, *W, *Xr, *AXr, *R;
+    // Vectors kept at a thick restart; leaves room for a full new block.
+    const int nkeep_max = std::max(b, std::min(mmax - b, std::max(2 * b, b + 4)));
+    if ((rc = alloc(&V, static_cast<int64_t>(mmax) * N)) || (rc = alloc(&W, static_cast<int64_t>(mmax) * N)) ||
+        (rc = alloc(&Xr, static_cast<int64_t>(std::max(nkeep_max, b)) * N)) ||
+        (rc = alloc(&AXr, static_cast<int64_t>(std::max(nkeep_max, b)) * N)) ||
+        (rc = alloc(&R, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi_, N * kMaxQ)) ||
+        (rc = alloc(&Yi_, N * kMaxQ)) || (rc = alloc(&d_partial_, static_cast<int64_t>(gram_blocks_) * kMaxGramP * kMaxQ)) ||
+        (rc = alloc(&d_small_, kMaxGramP * kMaxQ)) || (rc = alloc(&d_coef_, kMaxGramP * kMaxQ)) ||
+        (rc = alloc(&d_theta_, std::max(mmax, b))))
+        return rc;
+    double *d_diag = csr_->diag;
+
+    // Diagonal on the host for the initial guess.
+    std::vector<double> diag(N);
+    PYCI_CUDA_TRY(cudaMemcpyAsync(diag.data(), d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
+    PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+
+    // Initial block.
+    int m = 0, knew = 0;
+    if (full_space) {
+        std::vector<int64_t> idx(N);
+        std::iota(idx.begin(), idx.end(), 0);
+        int64_t *d_idx;
+        if ((rc = alloc(&d_idx, N)))
+            return rc;
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice, st_));
+        for (int64_t j0 = 0; j0 < N; j0 += 64)
+            unit_kernel<T><<<grid(N), 256, 0, st_>>>(V + j0 * N, N, d_idx + j0, static_cast<int>(std::min<int64_t>(64, N - j0))), ::pyci_gpu::note_launch();
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+        knew = static_cast<int>(N);
+    } else {
+        // Unit vectors on the lowest diagonal elements (after c0, if given),
+        // topped up until the block holds b independent vectors.
+        std::vector<int64_t> order(N);
+        std::iota(order.begin(), order.end(), 0);
+        const int64_t nsort = std::min<int64_t>(N, 2 * b + 8);
+        std::partial_sort(order.begin(), order.begin() + nsort, order.end(),
+                          [&](int64_t x, int64_t y) { return diag[x] < diag[y] || (diag[x] == diag[y] && x < y); });
+        int64_t *d_idx;
+        if ((rc = alloc(&d_idx, 1)))
+            return rc;
+        int64_t next = 0;
+        if (c0) {
+            std::vector<T> hc(N);
+            for (int64_t r = 0; r < N; ++r)
+                hc[r] = static_cast<T>(c0[r]);
+            PYCI_CUDA_TRY(cudaMemcpyAsync(V, hc.data(), sizeof(T) * N, cudaMemcpyHostToDevice, st_));
+            PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+            if ((rc = orthonormalize(V, 0, 1, knew)))
+                return rc;
+        }
+        while (knew < b && next < N) {
+            const int64_t pick = (next < nsort) ? order[next] : next;
+            ++next;
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_idx, &pick, sizeof(int64_t), cudaMemcpyHostToDevice, st_));
+            unit_kernel<T><<<grid(N), 256, 0, st_>>>(V + static_cast<int64_t>(knew) * N, N, d_idx, 1), ::pyci_gpu::note_launch();
+            PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+            int got = 0;
+            if ((rc = orthonormalize(V, knew, 1, got)))
+                return rc;
+            knew += got;
+        }
+        if (knew < b) {
+            set_error("could not build an initial block");
+            return PYCI_GPU_ENOCONV;
+        }
+    }
+
+    std::vector<double> G(static_cast<size_t>(mmax) * mmax, 0.0), theta, Y, Gc;
+    std::vector<double> rnorm(b, 0.0);
+    const double eps23 = std::pow(std::numeric_limits<double>::epsilon(), 2.0 / 3.0);
+    const double mixed_floor = 1e-5;
+    int64_t iter = 0, restarts = 0, refinements = 0;
+    bool converged = false;
+    std::vector<double> final_theta(b);
+    double max_res = 0.0;
+    double *X64 = nullptr, *AX64 = nullptr, *R64 = nullptr, *Xi64 = nullptr, *Yi64 = nullptr;
+
+    for (iter = 0; iter < maxiter; ++iter) {
+        // W for the new block.
+        if (knew > 0) {
+            if ((rc = apply(V + static_cast<int64_t>(m) * N, knew, W + static_cast<int64_t>(m) * N, prec)))
+                return rc;
+            // Projected matrix: new columns.
+            if ((rc = gram<T>(V, m + knew, W + static_cast<int64_t>(m) * N, knew, Gc)))
+                return rc;
+            for (int i = 0; i < m + knew; ++i)
+                for (int j = 0; j < knew; ++j) {
+                    G[static_cast<size_t>(i) * mmax + m + j] = Gc[static_cast<size_t>(i) * knew + j];
+                    G[static_cast<size_t>(m + j) * mmax + i] = Gc[static_cast<size_t>(i) * knew + j];
+                }
+            m += knew;
+        }
+        std::vector<double> Gm(static_cast<size_t>(m) * m);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < m; ++j)
+                Gm[static_cast<size_t>(i) * m + j] = G[static_cast<size_t>(i) * mmax + j];
+        if (!symmetric_eigen(m, Gm, theta, Y)) {
+            set_error("Rayleigh-Ritz eigensolver failed");
+            return PYCI_GPU_ENOCONV;
+        }
+        // Ritz vectors and residuals of the b lowest.
+        std::vector<double> Yb(static_cast<size_t>(m) * b);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < b; ++j)
+                Yb[static_cast<size_t>(i) * b + j] = Y[static_cast<size_t>(i) * m + j];
+        if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
+            return rc;
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+        residual_kernel<T><<<grid(N), 256, 0, st_>>>(AXr, Xr, d_theta_, b, N, R), ::pyci_gpu::note_launch();
+        bool all = true;
+        std::vector<int> todo;
+        for (int j = 0; j < b; ++j) {
+            if ((rc = gram<T>(R + static_cast<int64_t>(j) * N, 1, R + static_cast<int64_t>(j) * N, 1, Gc)))
+                return rc;
+            rnorm[j] = std::sqrt(std::max(Gc[0], 0.0));
+            double thr = tol * std::max(eps23, std::fabs(theta[j]));
+            if (mixed_)
+                thr = std::max(thr, mixed_floor);
+            if (full_space)
+                thr = std::numeric_limits<double>::infinity();
+            if (!(rnorm[j] <= thr)) {
+                all = false;
+                todo.push_back(j);
+            }
+        }
+        if (all) {
+            if (!mixed_) {
+                converged = true;
+                final_theta.assign(theta.begin(), theta.begin() + b);
+                max_res = *std::max_element(rnorm.begin(), rnorm.end());
+                break;
+            }
+            // FP64 refinement of the Ritz block.
+            ++refinements;
+            if (!X64) {
+                if ((rc = alloc(&X64, static_cast<int64_t>(b) * N)) || (rc = alloc(&AX64, static_cast<int64_t>(b) * N)) ||
+                    (rc = alloc(&R64, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi64, N * kMaxQ)) ||
+                    (rc = alloc(&Yi64, N * kMaxQ)))
+                    return rc;
+            }
+            if ((rc = combine<T, double, double>(V, m, Yb, b, 0.0, X64)))
+                return rc;
+            // Orthonormalise X64 in FP64 (modified Gram-Schmidt, two passes).
+            for (int j = 0; j < b; ++j) {
+                double *xj = X64 + static_cast<int64_t>(j) * N;
+                for (int pass = 0; pass < 2 && j > 0; ++pass) {
+                    if ((rc = gram<double>(X64, j, xj, 1, Gc)))
+                        return rc;
+                    for (double &c : Gc)
+                        c = -c;
+                    if ((rc = combine<double, double, double>(X64, j, Gc, 1, 1.0, xj)))
+                        return rc;
+                }
+                if ((rc = gram<double>(xj, 1, xj, 1, Gc)))
+                    return rc;
+                scale_kernel<double><<<grid(N), 256, 0, st_>>>(xj, N, 1.0 / std::sqrt(Gc[0])), ::pyci_gpu::note_launch();
+            }
+            for (int j0 = 0; j0 < b; j0 += kMaxQ) {
+                const int kk = std::min(kMaxQ, b - j0);
+                pack_kernel<double><<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, Xi64), ::pyci_gpu::note_launch();
+                cudaEventRecord(ev0_, st_);
+                if ((rc = csr_spmm(csr_, PYCI_PREC_FP64_SPLIT, kk, Xi64, Yi64, st_)))
+                    return rc;
+                cudaEventRecord(ev1_, st_);
+                unpack_kernel<double><<<grid(N), 256, 0, st_>>>(Yi64, N, kk, AX64 + static_cast<int64_t>(j0) * N), ::pyci_gpu::note_launch();
+                PYCI_CUDA_TRY(cudaEventSynchronize(ev1_));
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, ev0_, ev1_);
+                spmm_ms_ += ms;
+                matvecs_ += kk;
+                matvecs64_ += kk;
+            }
+            std::vector<double> G64, th64, Z;
+            if ((rc = gram<double>(X64, b, AX64, b, G64)))
+                return rc;
+            if (!symmetric_eigen(b, G64, th64, Z)) {
+                set_error("Rayleigh-Ritz eigensolver failed");
+                return PYCI_GPU_ENOCONV;
+            }
+            // Rotate X64 and AX64 into the FP64 Ritz basis (via Xr/AXr scratch is
+            // not FP64 for mixed; use R64 as scratch).
+            if ((rc = combine<double, double, double>(X64, b, Z, b, 0.0, R64)))
+                return rc;
+            PYCI_CUDA_TRY(cudaMemcpyAsync(X64, R64, sizeof(double) * b * N, cudaMemcpyDeviceToDevice, st_));
+            if ((rc = combine<double, double, double>(AX64, b, Z, b, 0.0, R64)))
+                return rc;
+            PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * b * N, cudaMemcpyDeviceToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+            residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, b, N, R64), ::pyci_gpu::note_launch();
+            bool ok64 = true;
+            todo.clear();
+            max_res = 0.0;
+            for (int j = 0; j < b; ++j) {
+                if ((rc = gram<double>(R64 + static_cast<int64_t>(j) * N, 1, R64 + static_cast<int64_t>(j) * N, 1, Gc)))
+                    return rc;
+                const double r64 = std::sqrt(std::max(Gc[0], 0.0));
+                max_res = std::max(max_res, r64);
+                const double thr = std::max(tol * std::max(eps23, std::fabs(th64[j])), 2.0 * mixed_floor);
+                if (!(r64 <= thr)) {
+                    ok64 = false;
+                    todo.push_back(j);
+                }
+            }
+            if (ok64 || refinements >= 8) {
+                converged = ok64;
+                final_theta = th64;
+                break;
+            }
+            // Seed the FP32 subspace with the FP64-preconditioned residuals.
+            if (m + static_cast<int>(todo.size()) > mmax) {
+                // Collapse onto the FP64 Ritz vectors.
+                convert_kernel<double, T><<<grid(static_cast<int64_t>(b) * N), 256, 0, st_>>>(X64, V, static_cast<int64_t>(b) * N), ::pyci_gpu::note_launch();
+                convert_kernel<double, T><<<grid(static_cast<int64_t>(b) * N), 256, 0, st_>>>(AX64, W, static_cast<int64_t>(b) * N), ::pyci_gpu::note_launch();
+                // X64/AX64 are in the FP64 Ritz basis: the projected matrix is diag(th64).
+                std::fill(G.begin(), G.end(), 0.0);
+                for (int i = 0; i < b; ++i)
+                    for (int j = 0; j < b; ++j)
+                        G[static_cast<size_t>(i) * mmax + j] = (i == j) ? th64[i] : 0.0;
+                m = b;
+                ++restarts;
+            }
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+            int q = 0;
+            for (int j : todo) {
+                precondition_kernel<double, T><<<grid(N), 256, 0, st_>>>(R64 + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
+                                                                        V + static_cast<int64_t>(m + q) * N), ::pyci_gpu::note_launch();
+                ++q;
+            }
+            if ((rc = orthonormalize(V, m, q, knew)))
+                return rc;
+            continue;
+        }
+        if (full_space) {
+            set_error("Rayleigh-Ritz on the full space left residuals above the tolerance");
+            return PYCI_GPU_ENOCONV;
+        }
+        // Thick restart when the block does not fit.
+        const int nt = static_cast<int>(todo.size());
+        if (m + nt > mmax) {
+            const int nkeep = std::min(m, nkeep_max);
+            std::vector<double> Yk(static_cast<size_t>(m) * nkeep);
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < nkeep; ++j)
+                    Yk[static_cast<size_t>(i) * nkeep + j] = Y[static_cast<size_t>(i) * m + j];
+            T *tmpX = Xr, *tmpW = AXr; // both hold nkeep_max vectors
+            if ((rc = combine<T, T, T>(V, m, Yk, nkeep, 0.0, tmpX)) || (rc = combine<T, T, T>(W, m, Yk, nkeep, 0.0, tmpW)))
+                return rc;
+            PYCI_CUDA_TRY(cudaMemcpyAsync(V, tmpX, sizeof(T) * nkeep * N, cudaMemcpyDeviceToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(W, tmpW, sizeof(T) * nkeep * N, cudaMemcpyDeviceToDevice, st_));
+            std::fill(G.begin(), G.end(), 0.0);
+            for (int i = 0; i < nkeep; ++i)
+                G[static_cast<size_t>(i) * mmax + i] = theta[i];
+            m = nkeep;
+            ++restarts;
+        }
+        // Preconditioned residuals of the unconverged roots.
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+        int q = 0;
+        for (int j : todo) {
+            precondition_kernel<T, T><<<grid(N), 256, 0, st_>>>(R + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
+                                                               V + static_cast<int64_t>(m + q) * N), ::pyci_gpu::note_launch();
+            ++q;
+        }
+        if ((rc = orthonormalize(V, m, q, knew)))
+            return rc;
+        if (knew == 0) {
+            set_error("did not converge");
+            return PYCI_GPU_ENOCONV;
+        }
+    }
+    if (!converged) {
+        set_error("did not converge");
+        return PYCI_GPU_ENOCONV;
+    }
+    // Results: decreasing order (Spectra's result order).
+    std::vector<double> h(static_cast<size_t>(N));
+    for (int c = 0; c < b; ++c) {
+        const int src = b - 1 - c;
+        evals[c] = final_theta[src] + ecore;
+        if (evecs) {
+            if (mixed_) {
+                PYCI_CUDA_TRY(cudaMemcpyAsync(evecs + static_cast<int64_t>(c) * N, X64 + static_cast<int64_t>(src) * N,
+                                              sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
+            } else {
+                PYCI_CUDA_TRY(cudaMemcpyAsync(evecs + static_cast<int64_t>(c) * N, Xr + static_cast<int64_t>(src) * N,
+                                              sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
+            }
+        }
+    }
+    PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+    if (stats) {
+        stats->iterations = iter + 1;
+        stats->matvecs = matvecs_;
+        stats->matvecs_fp64 = mixed_ ? matvecs64_ : matvecs_;
+        stats->restarts = restarts;
+        stats->refinements = refinements;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        stats->seconds_spmm = spmm_ms_ * 1e-3;
+        stats->max_residual = max_res;
+    }
+    return PYCI_GPU_OK;
+}
+
+} // namespace pyci_gpu
+
+using namespace pyci_gpu;
+
+int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, int64_t maxiter,
+                   double tol, double ecore, int mode, double *evals, double *evecs,
+                   pyci_gpu_solve_stats *stats) {
+    const int64_t N = csr->nrow;
+    int64_t mmax = (ncv > 0) ? ncv : std::max<int64_t>(8 * n, 24);
+    mmax = std::max<int64_t>(mmax, 2 * n + 2);
+    if (N <= std::max<int64_t>(64, 3 * n) || N <= mmax)
+        mmax = std::max<int64_t>(mmax, N); // full space: exact Rayleigh-Ritz
+    mmax = std::min<int64_t>(mmax, std::max<int64_t>(N, 1));
+    if (mmax > N)
+        mmax = N;
+    const int64_t iters = (maxiter > 0) ? maxiter : std::max<int64_t>(1000, 10 * n);
+    if (mode == PYCI_SOLVE_MIXED) {
+        int rc = csr_prepare_mixed_device(csr, 0);
+        if (rc)
+            return rc;
+        Davidson<float> d(csr, n, mmax, true);
+        return d.run(c0, iters, tol, ecore, evals, evecs, stats);
+    }
+    if (!csr->vals) {
+        set_error("FP64 solve needs FP64 values (dropped by prepare_mixed)");
+        return PYCI_GPU_EINVAL;
+    }
+    Davidson<double> d(csr, n, mmax, false);
+    return d.run(c0, iters, tol, ecore, evals, evecs, stats);
+}

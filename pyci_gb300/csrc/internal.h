@@ -1,0 +1,85 @@
+// Internal host-side definitions shared by the CUDA translation units of
+// libpyci_gb300.so.  Nothing here is part of the C ABI (include/pyci_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "pyci_gb300.h"
+
+struct pyci_gpu_ctx {
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+};
+
+// Device-resident CSR of the CI Hamiltonian.
+//
+// Storage: rows 0..nrow-1, columns sorted ascending in each row, int32
+// column indices, int64 row pointers.  For a symmetric operator both
+// triangles are stored (so the SpMV is a pure gather); the reference's
+// lower-triangle layout is the prefix of each row up to and including the
+// diagonal, whose length is kept in lower_len.
+struct pyci_gpu_csr {
+    pyci_gpu_ctx *ctx = nullptr;
+    int kind = 0;
+    int flags = 0;
+    int64_t nbasis = 0, nocc_up = 0, nocc_dn = 0;
+    int64_t ndet = 0, nrow = 0, ncol = 0;
+    bool symmetric = true;
+    int64_t nnz = 0;      // entries stored on the device
+    int64_t nnz_ref = 0;  // entries in the reference's layout
+    int64_t *rowptr = nullptr;   // [nrow + 1]
+    int32_t *cols = nullptr;     // [nnz]
+    double *vals = nullptr;      // [nnz] FP64 values (null after prepare_mixed(drop))
+    float *hi = nullptr;         // [nnz] FP32 high part (mixed precision)
+    float *lo = nullptr;         // [nnz] FP32 low part: f32(v - hi)
+    int32_t *lower_len = nullptr; // [nrow] reference entries per row (symmetric)
+    int64_t *ref_rowptr = nullptr; // [nrow + 1] prefix sum of lower_len (symmetric)
+    double *diag = nullptr;      // [nrow] diagonal (0 where absent)
+    int spmm_lanes = 32;         // lanes per row chosen for the SpMV kernels
+    // GenCI in the reference's own row loop (see genci_ref_* in build.cu):
+    // only the reference's layout is stored; a symmetric product then
+    // scatters the transpose with atomics.
+    bool lower_only = false;
+};
+
+namespace pyci_gpu {
+// Kernel launches issued by this library (diagnostic counter).
+void note_launch();
+} // namespace pyci_gpu
+
+// Thread-local error message.
+void set_error(const char *fmt, ...);
+
+// Map a CUDA failure to a status code and message.
+int cuda_status(cudaError_t err, const char *what);
+
+#define PYCI_CUDA_TRY(expr)                                                                        \
+    do {                                                                                           \
+        cudaError_t e_ = (expr);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return cuda_status(e_, #expr);                                                         \
+    } while (0)
+
+// Internal launchers (implemented in the .cu files).
+int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_host,
+                     const double *one_mo, const double *two_mo, int64_t legacy_nrow,
+                     int64_t legacy_ncol);
+int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, void *y,
+             cudaStream_t stream);
+void csr_release(pyci_gpu_csr *csr);
+int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
+int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,
+                      double *vabs, double *vwsum);
+int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64);
+int add_all_dets_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up,
+                        int64_t nocc_dn, uint64_t *dets_host);
+int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, int64_t maxiter,
+                   double tol, double ecore, int mode, double *evals, double *evecs,
+                   pyci_gpu_solve_stats *stats);
+
+int64_t host_binomial(int64_t n, int64_t k);

@@ -1,0 +1,282 @@
+// Sparse matrix times a block of vectors (SpMV / SpMM) for the CI
+// Hamiltonian's device CSR, replacing SparseOp::perform_op(_symm)
+// (pyci/src/sparseop.cpp:96-112), which the reference evaluates with Eigen on
+// one core.
+//
+// The product is HBM-bound: each stored entry is read once (4-byte column +
+// 8- or 4-byte value) while the vector block x ([ncol][k], interleaved) is
+// gathered from L2.  A group of LANES threads owns one row; lanes stream the
+// row's entries with 16-byte vector loads (evict-first, so the matrix does not
+// push x out of L2), each lane keeps k accumulators, and a butterfly shuffle
+// reduces them.  Symmetric operators store both triangles, so no scatter or
+// atomics are needed and results are deterministic.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+namespace pyci_gpu {
+
+enum ValueKind { kF64 = 0, kF32 = 1, kSplit = 2 };
+
+template<int VK>
+struct Values;
+
+template<>
+struct Values<kF64> {
+    typedef double acc_t;
+    typedef double x_t;
+    const double *v;
+    __device__ __forceinline__ double at(int64_t e) const { return __ldcs(v + e); }
+    __device__ __forceinline__ void quad(int64_t e, double out[4]) const {
+        const double2 a = __ldcs(reinterpret_cast<const double2 *>(v + e));
+        const double2 b = __ldcs(reinterpret_cast<const double2 *>(v + e + 2));
+        out[0] = a.x;
+        out[1] = a.y;
+        out[2] = b.x;
+        out[3] = b.y;
+    }
+};
+
+template<>
+struct Values<kF32> {
+    typedef float acc_t;
+    typedef float x_t;
+    const float *v;
+    __device__ __forceinline__ float at(int64_t e) const { return __ldcs(v + e); }
+    __device__ __forceinline__ void quad(int64_t e, float out[4]) const {
+        const float4 a = __ldcs(reinterpret_cast<const float4 *>(v + e));
+        out[0] = a.x;
+        out[1] = a.y;
+        out[2] = a.z;
+        out[3] = a.w;
+    }
+};
+
+template<>
+struct Values<kSplit> {
+    typedef double acc_t;
+    typedef double x_t;
+    const float *hi, *lo;
+    __device__ __forceinline__ double at(int64_t e) const {
+        return static_cast<double>(__ldcs(hi + e)) + static_cast<double>(__ldcs(lo + e));
+    }
+    __device__ __forceinline__ void quad(int64_t e, double out[4]) const {
+        const float4 a = __ldcs(reinterpret_cast<const float4 *>(hi + e));
+        const float4 b = __ldcs(reinterpret_cast<const float4 *>(lo + e));
+        out[0] = static_cast<double>(a.x) + static_cast<double>(b.x);
+        out[1] = static_cast<double>(a.y) + static_cast<double>(b.y);
+        out[2] = static_cast<double>(a.z) + static_cast<double>(b.z);
+        out[3] = static_cast<double>(a.w) + static_cast<double>(b.w);
+    }
+};
+
+template<int VK, int K, int LANES>
+__global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
+                                                   const int32_t *__restrict__ cols, Values<VK> vals,
+                                                   const typename Values<VK>::x_t *__restrict__ x,
+                                                   int64_t ldx,
+                                                   typename Values<VK>::x_t *__restrict__ y,
+                                                   int64_t ldy) {
+    typedef typename Values<VK>::acc_t acc_t;
+    typedef typename Values<VK>::x_t x_t;
+    const int lane = threadIdx.x % LANES;
+    const int64_t group = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / LANES;
+    const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
+    for (int64_t r = group; r < nrow; r += ngroups) {
+        const int64_t start = rowptr[r], end = rowptr[r + 1];
+        acc_t acc[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            acc[k] = 0;
+        // Head: entries before the first 4-aligned index.
+        const int64_t a0 = min(end, (start + 3) & ~static_cast<int64_t>(3));
+        const int64_t a1 = max(a0, end & ~static_cast<int64_t>(3));
+        if (start + lane < a0) {
+            const int64_t e = start + lane;
+            const int64_t c = __ldcs(cols + e);
+            const acc_t v = vals.at(e);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                acc[k] += v * static_cast<acc_t>(__ldg(x + c * ldx + k));
+        }
+        // Body: 4 entries per lane per step, 16-byte loads.
+        for (int64_t e = a0 + 4 * lane; e < a1; e += 4 * LANES) {
+            const int4 c4 = __ldcs(reinterpret_cast<const int4 *>(cols + e));
+            acc_t v[4];
+            vals.quad(e, v);
+            const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const x_t *xr = x + static_cast<int64_t>(cc[q]) * ldx;
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    acc[k] += v[q] * static_cast<acc_t>(__ldg(xr + k));
+            }
+        }
+        // Tail.
+        if (a1 + lane < end) {
+            const int64_t e = a1 + lane;
+            const int64_t c = __ldcs(cols + e);
+            const acc_t v = vals.at(e);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                acc[k] += v * static_cast<acc_t>(__ldg(x + c * ldx + k));
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1)
+                acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o, LANES);
+        }
+        if (lane < K) {
+            acc_t out = acc[0];
+#pragma unroll
+            for (int k = 1; k < K; ++k)
+                if (lane == k)
+                    out = acc[k];
+            y[r * ldy + lane] = static_cast<x_t>(out);
+        }
+    }
+}
+
+template<int VK, int K, int LANES>
+void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
+                int64_t ldy, cudaStream_t st) {
+    typedef typename Values<VK>::x_t x_t;
+    const int threads = 256;
+    const int64_t groups_needed = csr->nrow;
+    const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (groups_needed * LANES + threads - 1) / threads));
+    spmm_kernel<VK, K, LANES><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+        csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
+        static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
+}
+
+template<int VK, int LANES>
+void launch_k(const pyci_gpu_csr *csr, Values<VK> vals, int K, const void *x, int64_t ldx, void *y,
+              int64_t ldy, cudaStream_t st) {
+    switch (K) {
+    case 1: launch_one<VK, 1, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 2: launch_one<VK, 2, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 3: launch_one<VK, 3, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 4: launch_one<VK, 4, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 5: launch_one<VK, 5, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 6: launch_one<VK, 6, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    case 7: launch_one<VK, 7, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    default: launch_one<VK, 8, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+    }
+}
+
+template<int VK>
+void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *x, void *y,
+               cudaStream_t st) {
+    typedef typename Values<VK>::x_t x_t;
+    for (int64_t j0 = 0; j0 < k; j0 += 8) {
+        const int K = static_cast<int>(std::min<int64_t>(8, k - j0));
+        const void *xs = static_cast<const x_t *>(x) + j0;
+        void *ys = static_cast<x_t *>(y) + j0;
+        if (csr->spmm_lanes >= 32)
+            launch_k<VK, 32>(csr, vals, K, xs, k, ys, k, st);
+        else if (csr->spmm_lanes >= 16)
+            launch_k<VK, 16>(csr, vals, K, xs, k, ys, k, st);
+        else
+            launch_k<VK, 8>(csr, vals, K, xs, k, ys, k, st);
+    }
+}
+
+// Self-adjoint product from a lower-triangle CSR (only used for operators that
+// keep just the reference layout): y += L x + L^T x - D x with atomics; y must
+// be zeroed first.  Equivalent to the Eigen selfadjointView<Lower> product of
+// pyci/src/sparseop.cpp:106-112.
+template<typename T>
+__global__ void spmm_lower_kernel(int64_t nrow, const int64_t *rowptr, const int32_t *cols,
+                                  const double *vals, const float *hi, const float *lo,
+                                  const T *x, int k, T *y) {
+    for (int64_t e0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e0 < nrow;
+         e0 += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = e0;
+        for (int64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) {
+            const int64_t c = cols[e];
+            const double v = vals ? vals[e] : static_cast<double>(hi[e]) + static_cast<double>(lo[e]);
+            for (int j = 0; j < k; ++j) {
+                atomicAdd(&y[r * k + j], static_cast<T>(v * static_cast<double>(x[c * k + j])));
+                if (c != r)
+                    atomicAdd(&y[c * k + j], static_cast<T>(v * static_cast<double>(x[r * k + j])));
+            }
+        }
+    }
+}
+
+} // namespace pyci_gpu
+
+using namespace pyci_gpu;
+
+static int spmm_lower(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, void *y,
+                      cudaStream_t st) {
+    const bool f32 = (precision == PYCI_PREC_FP32);
+    const size_t es = f32 ? sizeof(float) : sizeof(double);
+    PYCI_CUDA_TRY(cudaMemsetAsync(y, 0, es * csr->nrow * k, st));
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>((csr->nrow + 255) / 256, 65536));
+    const double *vals = (precision == PYCI_PREC_FP64 && csr->vals) ? csr->vals : nullptr;
+    if (f32)
+        spmm_lower_kernel<float><<<blocks, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, nullptr,
+                                                        csr->hi, csr->lo, static_cast<const float *>(x),
+                                                        static_cast<int>(k), static_cast<float *>(y)), ::pyci_gpu::note_launch();
+    else
+        spmm_lower_kernel<double><<<blocks, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, vals,
+                                                         csr->hi, csr->lo, static_cast<const double *>(x),
+                                                         static_cast<int>(k), static_cast<double *>(y)), ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, void *y,
+             cudaStream_t stream) {
+    if (k <= 0) {
+        set_error("k must be positive");
+        return PYCI_GPU_EINVAL;
+    }
+    if (csr->nrow == 0)
+        return PYCI_GPU_OK;
+    if (csr->lower_only) {
+        if ((precision == PYCI_PREC_FP32 && !csr->hi) || (precision == PYCI_PREC_FP64_SPLIT && !csr->hi) ||
+            (precision == PYCI_PREC_FP64 && !csr->vals && !csr->hi)) {
+            set_error("operator lacks the values for this precision");
+            return PYCI_GPU_EINVAL;
+        }
+        return spmm_lower(csr, precision, k, x, y, stream);
+    }
+    switch (precision) {
+    case PYCI_PREC_FP64:
+        if (csr->vals) {
+            launch_vk<kF64>(csr, Values<kF64>{csr->vals}, k, x, y, stream);
+        } else if (csr->hi && csr->lo) {
+            launch_vk<kSplit>(csr, Values<kSplit>{csr->hi, csr->lo}, k, x, y, stream);
+        } else {
+            set_error("operator has no values");
+            return PYCI_GPU_EINVAL;
+        }
+        break;
+    case PYCI_PREC_FP32:
+        if (!csr->hi) {
+            set_error("FP32 product needs pyci_gpu_csr_prepare_mixed first");
+            return PYCI_GPU_EINVAL;
+        }
+        launch_vk<kF32>(csr, Values<kF32>{csr->hi}, k, x, y, stream);
+        break;
+    case PYCI_PREC_FP64_SPLIT:
+        if (!csr->hi || !csr->lo) {
+            set_error("split product needs pyci_gpu_csr_prepare_mixed first");
+            return PYCI_GPU_EINVAL;
+        }
+        launch_vk<kSplit>(csr, Values<kSplit>{csr->hi, csr->lo}, k, x, y, stream);
+        break;
+    default:
+        set_error("unknown precision %d", precision);
+        return PYCI_GPU_EINVAL;
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}

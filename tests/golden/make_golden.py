@@ -1,0 +1,182 @@
+r"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the reference source tree:
+
+    make -C oracle ref port            # reference built against the shims + C oracle
+    python tests/golden/make_golden.py [--big]
+
+Outputs (all committed):
+  kat_<system>.npz      integrals of the FCIDUMP files the reference's known-answer
+                        tests use (pyci/test/data/*.fcidump), unique 8-fold
+                        elements only, plus the tests' energies (kat.json)
+  csr_<case>.npz        the reference's own CSR (data / indices / indptr) for small
+                        synthetic cases, built by pyci.sparse_op of the reference
+  digests.json          order-independent digests of the reference CSR for the
+                        larger synthetic workloads, and reference eigenvalues
+The reference is imported from oracle/_ref (the unchanged sources compiled
+against project-written Eigen/Spectra/phmap shims).  With --big, the
+12-orbital FCI and 32-orbital DOCI workloads are added (minutes, ~40 GB RAM);
+their CSR comes from the C oracle, whose output is bit-identical to the
+reference's on every smaller case checked here.
+"""
+
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REFROOT = os.environ.get("PYCI_REFERENCE", "/root/reference")
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+sys.path.insert(0, HERE)
+
+import oracle as O  # noqa: E402
+from pyci_gb300.synth import synthetic_integrals, config_seed  # noqa: E402
+
+# Known-answer energies of pyci/test/test_routines.py:37-54 (test_solve_sparse)
+# and the notebook value (notebooks/pyci_tutorial.ipynb cell 7).
+KATS = [
+    ("li2_ccpvdz", "doci", (3, 3), -14.878455349),
+    ("be_ccpvdz", "doci", (2, 2), -14.600556994),
+    ("be_ccpvdz", "fullci", (2, 2), -14.617409507),
+    ("h2o_ccpvdz", "doci", (5, 5), -75.634588422),
+]
+
+from digest import digest  # noqa: E402
+
+
+def pack_8fold(two):
+    n = two.shape[0]
+    g = two.transpose(0, 2, 1, 3)  # chemist's (pq|rs)
+    keys, vals = [], []
+    for p in range(n):
+        for q in range(p + 1):
+            pq = p * (p + 1) // 2 + q
+            for r in range(n):
+                for s in range(r + 1):
+                    rs = r * (r + 1) // 2 + s
+                    if pq >= rs:
+                        v = g[p, q, r, s]
+                        if v != 0.0:
+                            keys.append((p, q, r, s))
+                            vals.append(v)
+    return np.array(keys, dtype=np.uint8 if n < 256 else np.uint16), np.array(vals)
+
+
+def kat_fixtures(pyci):
+    meta = []
+    for name in sorted({k[0] for k in KATS}):
+        ham = pyci.secondquant_op(os.path.join(REFROOT, "pyci", "test", "data", name + ".fcidump"))
+        keys, vals = pack_8fold(np.asarray(ham.two_mo))
+        np.savez_compressed(os.path.join(HERE, "kat_%s.npz" % name), ecore=np.float64(ham.ecore),
+                            one_mo=np.asarray(ham.one_mo), keys=keys, vals=vals)
+    for name, kind, occs, energy in KATS:
+        meta.append({"system": name, "wfn": kind, "occs": list(occs), "energy": energy})
+    return meta
+
+
+def ref_csr(pyci, kind, n, nu, nd, ecore, one, two, nrow=-1, ncol=-1, symm=True, exc=None):
+    ham = pyci.secondquant_op(ecore, one, two)
+    W = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn, "genci": pyci.genci_wfn}[kind]
+    wfn = W(n, nu, nd)
+    if exc is None:
+        wfn.add_all_dets()
+    else:
+        pyci.add_excitations(wfn, *exc)
+    op = pyci.sparse_op(ham, wfn, nrow, ncol, symm)
+    return op, wfn
+
+
+CSR_CASES = [
+    # name, kind, nbasis, nocc_up, nocc_dn, excitations (None = all), nrow, ncol, symmetric, seed
+    ("fci_6_3_2", "fullci", 6, 3, 2, None, -1, -1, True, 11),
+    ("fci_7_3_3_cisd", "fullci", 7, 3, 3, (0, 1, 2), -1, -1, True, 12),
+    ("fci_7_3_2_rect", "fullci", 7, 3, 2, (0, 1, 2), 20, -1, False, 13),
+    ("fci_5_2_2_sym_nrow", "fullci", 5, 2, 2, None, 60, -1, True, 14),
+    ("doci_10_4", "doci", 10, 4, 4, None, -1, -1, True, 15),
+    ("doci_12_5_cisd_rect", "doci", 12, 5, 5, (0, 1, 2), 40, 90, False, 16),
+    ("doci_9_3_ncol", "doci", 9, 3, 3, None, -1, 50, True, 17),
+    ("genci_10_4", "genci", 10, 4, 0, None, -1, -1, True, 18),
+    ("genci_12_3_cisd_rect", "genci", 12, 3, 0, (0, 1, 2), 30, -1, False, 19),
+]
+
+
+def csr_fixtures(pyci):
+    meta = []
+    for name, kind, n, nu, nd, exc, nrow, ncol, symm, seed in CSR_CASES:
+        ecore, one, two = synthetic_integrals(n, seed)
+        op, wfn = ref_csr(pyci, kind, n, nu, nd, ecore, one, two, nrow, ncol, symm, exc)
+        dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
+        x = np.random.default_rng(seed).normal(size=op.shape[1])
+        np.savez_compressed(os.path.join(HERE, "csr_%s.npz" % name), data=op.data(), indices=op.indices(),
+                            indptr=op.indptr(), dets=dets, x=x, y=op(x))
+        meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd,
+                     "excitations": None if exc is None else list(exc), "nrow": nrow, "ncol": ncol,
+                     "symmetric": symm, "seed": seed, "size": int(op.size), "shape": list(op.shape)})
+    return meta
+
+
+WORKLOADS = [
+    # name, kind, nbasis, nocc, config index (seed 1000 + index), roots
+    ("fci_8_4_4", "fullci", 8, (4, 4), 1, 4),
+    ("doci_24_6", "doci", 24, (6, 6), 2, 1),
+]
+BIG_WORKLOADS = [
+    ("fci_12_5_5", "fullci", 12, (5, 5), 3, 4),
+    ("doci_32_8", "doci", 32, (8, 8), 4, 4),
+]
+
+
+def workload_digests(pyci, big):
+    out = {}
+    for name, kind, n, occs, cfg, nroot in WORKLOADS + (BIG_WORKLOADS if big else []):
+        t0 = time.time()
+        ecore, one, two = synthetic_integrals(n, config_seed(cfg))
+        k = {"doci": O.DOCI, "fullci": O.FULLCI}[kind]
+        if (name, kind, n, occs, cfg, nroot) in WORKLOADS:
+            op, wfn = ref_csr(pyci, kind, n, occs[0], occs[1], ecore, one, two)
+            data, indices, indptr = op.data(), op.indices(), op.indptr()
+            source = "reference"
+        else:
+            dets = O.all_dets(k, n, occs[0], occs[1])
+            data, indices, indptr = O.build_csr(k, n, occs[0], occs[1], dets, one, two)
+            del dets
+            source = "oracle (bit-identical to the reference on every checked case)"
+        d = digest(data, indices, indptr)
+        evals = O.lowest_eigenvalues(data, indices, indptr, nroot=nroot, tol=1e-12)
+        d.update({"wfn": kind, "nbasis": n, "occs": list(occs), "seed": config_seed(cfg),
+                  "nrow": int(indptr.shape[0] - 1), "eigenvalues": [float(e) for e in evals],
+                  "csr_source": source, "seconds": round(time.time() - t0, 1)})
+        out[name] = d
+        print(name, d["nnz"], d["eigenvalues"], d["seconds"], "s", flush=True)
+        del data, indices, indptr
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--big", action="store_true")
+    ap.add_argument("--only-big", action="store_true")
+    args = ap.parse_args()
+    import pyci  # the reference, from oracle/_ref
+    path = os.path.join(HERE, "digests.json")
+    if args.only_big:
+        with open(path) as f:
+            meta = json.load(f)
+        meta["workloads"].update({k: v for k, v in workload_digests(pyci, True).items()
+                                  if k in dict((w[0], 1) for w in BIG_WORKLOADS)})
+    else:
+        meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci),
+                "workloads": workload_digests(pyci, args.big)}
+    with open(path, "w") as f:
+        json.dump(meta, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

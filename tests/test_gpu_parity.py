@@ -1,0 +1,211 @@
+r"""GPU parity through the C ABI: CSR pattern bit-exact and FP64 values equal to
+the reference's (golden arrays from the reference's own sparse_op, digests of
+its full-size CSR), SpMV/SpMM against the oracle, eigenvalues against the
+reference tests' known answers and the oracle."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_csr_case, load_kat
+from pyci_gb300 import capi
+from pyci_gb300.synth import synthetic_integrals
+
+pytestmark = pytest.mark.gpu
+
+WFN = {"doci": capi.WFN_DOCI, "fullci": capi.WFN_FULLCI, "genci": capi.WFN_GENCI}
+OKIND = {"doci": O.DOCI, "fullci": O.FULLCI}
+CASES = ["fci_6_3_2", "fci_7_3_3_cisd", "fci_7_3_2_rect", "fci_5_2_2_sym_nrow", "doci_10_4",
+         "doci_12_5_cisd_rect", "doci_9_3_ncol", "genci_10_4", "genci_12_3_cisd_rect"]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = capi.Context(0)
+    yield c
+    c.close()
+
+
+def build_case(ctx, meta, dets, flags=0):
+    ecore, one, two = synthetic_integrals(meta["nbasis"], meta["seed"])
+    return capi.Csr(ctx, WFN[meta["wfn"]], meta["nbasis"], meta["nocc_up"], meta["nocc_dn"], dets, one, two,
+                    meta["nrow"], meta["ncol"], meta["symmetric"], flags)
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("mode", ["colex", "hash"])
+def test_csr_matches_reference(ctx, golden, case, mode):
+    meta = {m["name"]: m for m in golden["csr_cases"]}[case]
+    ref = load_csr_case(case)
+    full_space = meta["excitations"] is None
+    if mode == "colex" and not full_space:
+        pytest.skip("colex ranking applies to full spaces only")
+    flags = capi.BUILD_FULL_COLEX if mode == "colex" else capi.BUILD_FORCE_HASH
+    csr = build_case(ctx, meta, ref["dets"], flags)
+    nrow, ncol, size, stored = csr.shape()
+    assert (nrow, ncol) == tuple(meta["shape"]) and size == meta["size"]
+    data, indices, indptr = csr.export()
+    assert np.array_equal(indptr, ref["indptr"])
+    assert np.array_equal(indices, ref["indices"])
+    if meta["wfn"] == "genci":
+        for r in range(nrow):
+            s, e = indptr[r], indptr[r + 1]
+            assert sorted(zip(indices[s:e], data[s:e])) == sorted(zip(ref["indices"][s:e], ref["data"][s:e]))
+    else:
+        assert np.array_equal(data, ref["data"])  # bit-exact FP64 matrix elements
+    if not (meta["symmetric"] and ncol < nrow):
+        y = csr.matvec(ref["x"])
+        np.testing.assert_allclose(y, ref["y"], rtol=1e-12, atol=1e-11)
+    # get_element agrees with the exported arrays
+    for r in range(0, nrow, max(1, nrow // 7)):
+        for t in range(indptr[r], indptr[r + 1], max(1, (indptr[r + 1] - indptr[r]) // 3)):
+            assert csr.get_element(r, int(indices[t])) == pytest.approx(
+                data[indptr[r]:indptr[r + 1]][indices[indptr[r]:indptr[r + 1]] == indices[t]].sum(), abs=1e-14)
+    csr.free()
+
+
+def test_genci_exact_mode_reproduces_fullci_energy(ctx):
+    # Slater-Condon rules over the true virtuals: a spin-orbital GenCI space of
+    # 2 alpha + 2 beta electrons in 5 spatial orbitals has the FCI ground state.
+    n = 5
+    ecore, one, two = synthetic_integrals(n, 3)
+    N = 2 * n
+    one_g = np.zeros((N, N))
+    one_g[:n, :n] = one
+    one_g[n:, n:] = one
+    two_g = np.zeros((N, N, N, N))
+    for s1 in (0, 1):
+        for s2 in (0, 1):
+            two_g[s1 * n:(s1 + 1) * n, s2 * n:(s2 + 1) * n, s1 * n:(s1 + 1) * n, s2 * n:(s2 + 1) * n] = two
+    gdets = O.all_dets(O.GENCI, N, 4, 0)
+    g = capi.Csr(ctx, capi.WFN_GENCI, N, 4, 0, gdets, one_g, two_g, flags=capi.BUILD_GENCI_EXACT)
+    d, i, p = g.export()
+    og = O.build_csr(O.GENCI, N, 4, 0, gdets, one_g, two_g)
+    assert np.array_equal(i, og[1]) and np.array_equal(p, og[2]) and np.array_equal(d, og[0])
+    fdets = O.all_dets(O.FULLCI, n, 2, 2)
+    f = capi.Csr(ctx, capi.WFN_FULLCI, n, 2, 2, fdets, one, two, flags=capi.BUILD_FULL_COLEX)
+    eg = g.solve(n=1, tol=1e-10)[0][0]
+    ef = f.solve(n=1, tol=1e-10)[0][0]
+    assert eg == pytest.approx(ef, abs=1e-9)
+
+
+@pytest.mark.parametrize("name", ["fci_8_4_4", "doci_24_6"])
+def test_workload_digest_and_eigenvalues(ctx, golden, name):
+    w = golden["workloads"][name]
+    ecore, one, two = synthetic_integrals(w["nbasis"], w["seed"])
+    csr = capi.Csr(ctx, WFN[w["wfn"]], w["nbasis"], w["occs"][0], w["occs"][1], None, one, two,
+                   flags=capi.BUILD_FULL_COLEX, ndet=w["nrow"])
+    nrow, ncol, size, stored = csr.shape()
+    assert size == w["nnz"]
+    d = csr.digest()
+    assert d["pattern_sum"] == w["pattern_sum"] and d["pattern_xor"] == w["pattern_xor"]
+    assert d["value_sum"] == pytest.approx(w["value_sum"], rel=1e-12, abs=1e-9)
+    assert d["value_abs_sum"] == pytest.approx(w["value_abs_sum"], rel=1e-12)
+    assert d["value_wsum"] == pytest.approx(w["value_wsum"], rel=1e-12, abs=1e-9)
+    nroot = len(w["eigenvalues"])
+    for mode in (capi.SOLVE_FP64, capi.SOLVE_MIXED):
+        evals, evecs, st = csr.solve(n=nroot, tol=1e-8 if mode == capi.SOLVE_FP64 else 1e-6, mode=mode)
+        assert np.all(np.diff(evals) <= 0)  # decreasing, the reference's order
+        err = np.abs(np.sort(evals) - np.array(w["eigenvalues"]))
+        assert err.max() < 1e-6, (mode, err)  # within 1 microhartree
+        # eigenvectors: unit norm, H x = e x to the solver's residual
+        for k in range(nroot):
+            assert np.linalg.norm(evecs[k]) == pytest.approx(1.0, abs=1e-6)
+    csr.free()
+
+
+@pytest.mark.parametrize("kat", [0, 1, 2, 3])
+def test_known_answer_energies(ctx, golden, kat):
+    # pyci/test/test_routines.py:37-54 with the reference's solve(n=1, ncv=30, tol=1e-6).
+    k = golden["kats"][kat]
+    ecore, one, two = load_kat(k["system"])
+    n = one.shape[0]
+    dets = O.all_dets(OKIND[k["wfn"]], n, *k["occs"])
+    csr = capi.Csr(ctx, WFN[k["wfn"]], n, k["occs"][0], k["occs"][1], dets, one, two, flags=capi.BUILD_FULL_COLEX)
+    evals, _, _ = csr.solve(n=1, ncv=30, tol=1e-6, ecore=ecore)
+    assert abs(evals[0] - k["energy"]) < 1e-9
+    csr.free()
+
+
+def test_spmm_precisions_against_oracle(ctx):
+    import torch
+    ecore, one, two = synthetic_integrals(8, 1001)
+    dets = O.all_dets(O.FULLCI, 8, 4, 4)
+    ref = O.build_csr(O.FULLCI, 8, 4, 4, dets, one, two)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, 8, 4, 4, dets, one, two, flags=capi.BUILD_FULL_COLEX)
+    csr.prepare_mixed()
+    N = dets.shape[0]
+    rng = np.random.default_rng(5)
+    for k in (1, 3, 4, 8, 11):
+        X = rng.normal(size=(N, k))
+        Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
+        xd = torch.tensor(X, dtype=torch.float64, device="cuda")
+        yd = torch.empty((N, k), dtype=torch.float64, device="cuda")
+        for prec in (capi.PREC_FP64, capi.PREC_FP64_SPLIT):
+            csr.spmm_device(prec, k, xd.data_ptr(), yd.data_ptr(), None)
+            torch.cuda.synchronize()
+            np.testing.assert_allclose(yd.cpu().numpy(), Y_ref, rtol=1e-12, atol=1e-11)
+        xf = xd.float()
+        yf = torch.empty((N, k), dtype=torch.float32, device="cuda")
+        csr.spmm_device(capi.PREC_FP32, k, xf.data_ptr(), yf.data_ptr(), None)
+        torch.cuda.synchronize()
+        # FP32 values and accumulation: relative error ~ sqrt(row length) * 2^-24
+        err = np.abs(yf.cpu().numpy() - Y_ref).max() / np.abs(Y_ref).max()
+        assert err < 1e-5
+    csr.free()
+
+
+def test_add_all_dets_on_device(ctx):
+    for kind, ok, n, nu, nd in [(capi.WFN_FULLCI, O.FULLCI, 8, 3, 2), (capi.WFN_DOCI, O.DOCI, 70, 2, 2),
+                                (capi.WFN_GENCI, O.GENCI, 12, 4, 0), (capi.WFN_FULLCI, O.FULLCI, 65, 2, 1)]:
+        d = ctx.add_all_dets(kind, n, nu, nd)
+        assert np.array_equal(d, O.all_dets(ok, n, nu, nd))
+
+
+def test_errors_map_to_reference_exceptions(ctx):
+    ecore, one, two = synthetic_integrals(6, 9)
+    dets = O.all_dets(O.FULLCI, 6, 2, 2)
+    sym = capi.Csr(ctx, capi.WFN_FULLCI, 6, 2, 2, dets, one, two)
+    with pytest.raises(ValueError):
+        sym.solve(n=dets.shape[0])  # n >= nrow
+    rect = capi.Csr(ctx, capi.WFN_FULLCI, 6, 2, 2, dets, one, two, nrow=50, symmetric=False)
+    with pytest.raises(TypeError):
+        rect.solve(n=1)  # nrow != ncol
+    with pytest.raises(ValueError):
+        capi.Csr(ctx, capi.WFN_DOCI, 6, 3, 2, None, one, two, ndet=10)  # nocc_up != nocc_dn
+    with pytest.raises(capi.GpuError):
+        sym.solve(n=2, maxiter=1, tol=1e-14)  # did not converge -> RuntimeError
+    sym.free()
+    rect.free()
+
+
+def test_update_appends_rows_like_reference(ctx):
+    # op.update(ham, wfn) after growing the wave function (pyci/src/sparseop.cpp:175-201):
+    # rows built before keep their columns; new rows are appended.
+    ecore, one, two = synthetic_integrals(7, 21)
+    full = O.all_dets(O.FULLCI, 7, 3, 2)
+    small = full[:300]
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, 7, 3, 2, small, one, two)
+    csr.update(full, one, two)
+    d, i, p = csr.export()
+    ref = O.build_csr(O.FULLCI, 7, 3, 2, full, one, two)  # symmetric: identical to a fresh build
+    assert np.array_equal(p, ref[2]) and np.array_equal(i, ref[1]) and np.array_equal(d, ref[0])
+    csr.free()
+
+
+def test_clone_is_deep(ctx):
+    ecore, one, two = synthetic_integrals(6, 4)
+    dets = O.all_dets(O.DOCI, 6, 3, 3)
+    a = capi.Csr(ctx, capi.WFN_DOCI, 6, 3, 3, dets, one, two)
+    h = capi.lib()
+    import ctypes
+    out = ctypes.c_void_p()
+    capi.check(h.pyci_gpu_csr_clone(a.handle, ctypes.byref(out)))
+    da = a.export()
+    a.free()
+    b = capi.Csr.__new__(capi.Csr)
+    b.handle = out
+    db = b.export()
+    for x, y in zip(da, db):
+        assert np.array_equal(x, y)
+    b.free()

@@ -1,0 +1,94 @@
+r"""The CPU oracle pinned against the reference: golden CSR arrays built by the
+reference's own sparse_op, the reference tests' known-answer energies, and
+digests of the reference CSR for the 8- and 24-orbital workloads."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_csr_case, load_kat
+from pyci_gb300.synth import synthetic_integrals, config_seed
+
+KIND = {"doci": O.DOCI, "fullci": O.FULLCI, "genci": O.GENCI_REF}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    O.build()
+
+
+def test_binomial_and_colex_roundtrip():
+    L = O.lib()
+    assert L.orc_binomial(12, 5) == 792
+    assert L.orc_binomial(32, 8) == 10518300
+    for n, k in [(8, 4), (10, 3), (70, 2), (130, 2)]:
+        dets = O.all_dets(O.DOCI, n, k, k)
+        assert dets.shape[0] == L.orc_binomial(n, k)
+        ranks = [L.orc_rank_colex(n, k, O._ptr(np.ascontiguousarray(d))) for d in dets[:: max(1, len(dets) // 97)]]
+        assert ranks == list(range(0, len(dets), max(1, len(dets) // 97)))
+
+
+def test_phase_conventions():
+    L = O.lib()
+    det = np.array([0b1011011], dtype=np.uint64)  # orbitals 0,1,3,4,6
+    # single 1 -> 5: occupied strictly between are 3, 4 -> +1
+    assert L.orc_phase_single(O._ptr(det), 1, 5) == 1
+    # single 0 -> 2: occupied between: 1 -> -1
+    assert L.orc_phase_single(O._ptr(det), 0, 2) == -1
+    # double (0,1)->(2,5): perms 1 (0->2 passes 1) + 2 (1->5 passes 3,4) = 3, and
+    # i2=1 < a1=2 adds one -> even -> +1
+    assert L.orc_phase_double(O._ptr(det), 0, 1, 2, 5) == 1
+
+
+@pytest.mark.parametrize("case", [c for c in [
+    "fci_6_3_2", "fci_7_3_3_cisd", "fci_7_3_2_rect", "fci_5_2_2_sym_nrow", "doci_10_4",
+    "doci_12_5_cisd_rect", "doci_9_3_ncol", "genci_10_4", "genci_12_3_cisd_rect"]])
+def test_oracle_csr_matches_reference(golden, case):
+    meta = {m["name"]: m for m in golden["csr_cases"]}[case]
+    ref = load_csr_case(case)
+    ecore, one, two = synthetic_integrals(meta["nbasis"], meta["seed"])
+    data, indices, indptr = O.build_csr(KIND[meta["wfn"]], meta["nbasis"], meta["nocc_up"], meta["nocc_dn"],
+                                        ref["dets"], one, two, meta["nrow"], meta["ncol"], meta["symmetric"])
+    assert np.array_equal(indptr, ref["indptr"])
+    assert np.array_equal(indices, ref["indices"])
+    if meta["wfn"] == "genci":
+        # Rows may hold repeated columns (the reference's GenCI quirk); their
+        # order under std::sort is unspecified, so compare per row as multisets.
+        for r in range(indptr.shape[0] - 1):
+            s, e = indptr[r], indptr[r + 1]
+            assert sorted(zip(indices[s:e], data[s:e])) == sorted(zip(ref["indices"][s:e], ref["data"][s:e]))
+    else:
+        assert np.array_equal(data, ref["data"])  # bit-exact FP64
+    nrow, ncol = meta["shape"]
+    if meta["symmetric"] and ncol < nrow:
+        return  # the reference's self-adjoint product reads x past ncol here (undefined)
+    y = O.spmv(data, indices, indptr, ref["x"], symmetric=meta["symmetric"])
+    np.testing.assert_allclose(y, ref["y"], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["fci_8_4_4", "doci_24_6"])
+def test_oracle_workload_digest(golden, name):
+    from digest import digest
+    w = golden["workloads"][name]
+    kind = KIND[w["wfn"]]
+    ecore, one, two = synthetic_integrals(w["nbasis"], w["seed"])
+    dets = O.all_dets(kind, w["nbasis"], *w["occs"])
+    data, indices, indptr = O.build_csr(kind, w["nbasis"], w["occs"][0], w["occs"][1], dets, one, two)
+    d = digest(data, indices, indptr)
+    assert d["nnz"] == w["nnz"]
+    assert d["pattern_sum"] == w["pattern_sum"] and d["pattern_xor"] == w["pattern_xor"]
+    assert d["value_sum"] == pytest.approx(w["value_sum"], rel=1e-12, abs=1e-9)
+    assert d["value_wsum"] == pytest.approx(w["value_wsum"], rel=1e-12, abs=1e-9)
+
+
+@pytest.mark.parametrize("kat", [0, 1, 2, 3])
+def test_oracle_known_answer_energies(golden, kat):
+    # pyci/test/test_routines.py:37-54: lowest energy to atol 1e-9.
+    k = golden["kats"][kat]
+    ecore, one, two = load_kat(k["system"])
+    n = one.shape[0]
+    kind = KIND[k["wfn"]]
+    dets = O.all_dets(kind, n, *k["occs"])
+    csr = O.build_csr(kind, n, k["occs"][0], k["occs"][1], dets, one, two)
+    e = O.lowest_eigenvalues(*csr, nroot=1)[0] + ecore
+    assert abs(e - k["energy"]) < 1e-9
