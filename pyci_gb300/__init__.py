@@ -8,7 +8,7 @@ helpers and ``add_excitations``.  The operator runs on the GPU through
 ``libpyci_gb300.so``; importing works without a GPU, building an operator
 does not.
 
-The native parts are built in-tree by ``python -m pyci_gb300.build`` (or
+The native parts are built in-tree by ``python pyci_gb300/build.py`` (or
 ``__graft_entry__.build()``); importing fails loudly if they are missing.
 """
 
@@ -38,7 +38,7 @@ try:
     )
 except ImportError as exc:  # pragma: no cover - exercised only on a broken build
     raise ImportError(
-        "pyci_gb300's native module is not built; run `python -m pyci_gb300.build` "
+        "pyci_gb300's native module is not built; run `python pyci_gb300/build.py` "
         "(needs nvcc for sm_103a): " + str(exc)
     ) from exc
 

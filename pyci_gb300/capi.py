@@ -51,7 +51,7 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIBRARY):
-            raise OSError("libpyci_gb300.so is not built; run `python -m pyci_gb300.build`")
+            raise OSError("libpyci_gb300.so is not built; run `python pyci_gb300/build.py`")
         L = ctypes.CDLL(LIBRARY)
         sig = {
             "pyci_gpu_last_error": (ctypes.c_char_p, []),
