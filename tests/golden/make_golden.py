@@ -114,8 +114,13 @@ def csr_fixtures(pyci):
         op, wfn = ref_csr(pyci, kind, n, nu, nd, ecore, one, two, nrow, ncol, symm, exc)
         dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
         x = np.random.default_rng(seed).normal(size=op.shape[1])
+        keys, vals = pack_8fold(two)
+        # The integrals travel with the fixture: numpy's einsum may round the
+        # last bit differently on another machine, and the CSR values are
+        # compared bit for bit.
         np.savez_compressed(os.path.join(HERE, "csr_%s.npz" % name), data=op.data(), indices=op.indices(),
-                            indptr=op.indptr(), dets=dets, x=x, y=op(x))
+                            indptr=op.indptr(), dets=dets, x=x, y=op(x), ecore=np.float64(ecore),
+                            one_mo=one, keys=keys, vals=vals)
         meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd,
                      "excitations": None if exc is None else list(exc), "nrow": nrow, "ncol": ncol,
                      "symmetric": symm, "seed": seed, "size": int(op.size), "shape": list(op.shape)})

@@ -52,10 +52,9 @@ def test_sparse_rectangular(system, wfn_type, occs):
 
 @pytest.mark.parametrize("case", ["fci_6_3_2", "doci_10_4", "fci_7_3_3_cisd", "genci_10_4"])
 def test_arrays_match_reference(golden, case):
-    from pyci_gb300.synth import synthetic_integrals
     meta = {m["name"]: m for m in golden["csr_cases"]}[case]
     ref = load_csr_case(case)
-    ham = pyci.secondquant_op(*synthetic_integrals(meta["nbasis"], meta["seed"]))
+    ham = pyci.secondquant_op(ref["ecore"], ref["one_mo"], ref["two_mo"])
     W = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn, "genci": pyci.genci_wfn}[meta["wfn"]]
     wfn = W(meta["nbasis"], meta["nocc_up"], meta["nocc_dn"])
     if meta["excitations"] is None:

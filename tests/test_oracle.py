@@ -46,7 +46,7 @@ def test_phase_conventions():
 def test_oracle_csr_matches_reference(golden, case):
     meta = {m["name"]: m for m in golden["csr_cases"]}[case]
     ref = load_csr_case(case)
-    ecore, one, two = synthetic_integrals(meta["nbasis"], meta["seed"])
+    one, two = ref["one_mo"], ref["two_mo"]
     data, indices, indptr = O.build_csr(KIND[meta["wfn"]], meta["nbasis"], meta["nocc_up"], meta["nocc_dn"],
                                         ref["dets"], one, two, meta["nrow"], meta["ncol"], meta["symmetric"])
     assert np.array_equal(indptr, ref["indptr"])
