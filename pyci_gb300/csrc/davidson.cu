@@ -287,10 +287,7 @@ private:
                 combine_kernel<TV, TO, ACC><<<grid(N_), 256, 0, st_>>>(
                     V + static_cast<int64_t>(i0) * N_, pp, N_, d_coef_, qq, (i0 == 0) ? beta : 1.0,
                     out + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
-                // sub must stay alive until the copy has been consumed.
-                e = cudaStreamSynchronize(st_);
-                if (e != cudaSuccess)
-                    return cuda_status(e, "combine");
+                // `sub` is pageable: cudaMemcpyAsync has staged it before returning.
             }
         }
         return PYCI_GPU_OK;
@@ -318,10 +315,12 @@ private:
         return PYCI_GPU_OK;
     }
 
-    // Orthonormalise vectors V[m..m+k) against V[0..m) and each other
-    // (classical Gram-Schmidt, two passes); drops near-dependent vectors.
-    // Returns the number kept (compacted to V[m..)).
+    // Orthonormalise vectors V[m..m+k) against V[0..m) and each other;
+    // returns the number kept (compacted to V[m..)).
     int orthonormalize(T *V, int m, int k, int &kept);
+    // Vector-by-vector classical Gram-Schmidt (two passes); drops
+    // near-dependent vectors.
+    int orthonormalize_mgs(T *V, int m, int k, int &kept);
 
     pyci_gpu_csr *csr_;
     cudaStream_t st_;
@@ -332,12 +331,82 @@ private:
     double spmm_ms_ = 0.0;
     int64_t matvecs_ = 0, matvecs64_ = 0;
     unsigned gram_blocks_ = 1;
-    T *Xi_ = nullptr, *Yi_ = nullptr;
+    T *Xi_ = nullptr, *Yi_ = nullptr, *Sb_ = nullptr;
     double *d_partial_ = nullptr, *d_small_ = nullptr, *d_coef_ = nullptr, *d_theta_ = nullptr;
 };
 
 template<typename T>
 int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
+    // Block classical Gram-Schmidt against V[0..m) (two passes), then two
+    // Cholesky-QR passes inside the block: 4 small Gram products per call
+    // instead of one per vector.  A near-singular block falls back to the
+    // vector-by-vector path, which drops dependent directions.
+    T *Tb = V + static_cast<int64_t>(m) * N_;
+    std::vector<double> C, S;
+    int rc;
+    if (k > 1 && k <= kMaxQ) {
+        for (int pass = 0; pass < 2 && m > 0; ++pass) {
+            if ((rc = gram<T>(V, m, Tb, k, C)))
+                return rc;
+            for (double &c : C)
+                c = -c;
+            if ((rc = combine<T, T, double>(V, m, C, k, 1.0, Tb)))
+                return rc;
+        }
+        const double piv_tol = mixed_ ? 1e-6 : 1e-14;
+        bool ok = true;
+        for (int pass = 0; pass < 2 && ok; ++pass) {
+            if ((rc = gram<T>(Tb, k, Tb, k, S)))
+                return rc;
+            // S = L L^T; coefficients of T L^{-T}: column j = row j of L^{-1}.
+            std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
+            for (int j = 0; j < k && ok; ++j) {
+                double d = S[static_cast<size_t>(j) * k + j];
+                for (int t = 0; t < j; ++t)
+                    d -= L[static_cast<size_t>(j) * k + t] * L[static_cast<size_t>(j) * k + t];
+                if (!(d > piv_tol * S[static_cast<size_t>(j) * k + j]) || !(d > 0.0)) {
+                    ok = false;
+                    break;
+                }
+                L[static_cast<size_t>(j) * k + j] = std::sqrt(d);
+                for (int i = j + 1; i < k; ++i) {
+                    double x = S[static_cast<size_t>(i) * k + j];
+                    for (int t = 0; t < j; ++t)
+                        x -= L[static_cast<size_t>(i) * k + t] * L[static_cast<size_t>(j) * k + t];
+                    L[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(j) * k + j];
+                }
+            }
+            if (!ok)
+                break;
+            std::vector<double> Linv(static_cast<size_t>(k) * k, 0.0);
+            for (int j = 0; j < k; ++j) {
+                Linv[static_cast<size_t>(j) * k + j] = 1.0 / L[static_cast<size_t>(j) * k + j];
+                for (int i = j + 1; i < k; ++i) {
+                    double x = 0.0;
+                    for (int t = j; t < i; ++t)
+                        x -= L[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(t) * k + j];
+                    Linv[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(i) * k + i];
+                }
+            }
+            // new_j = sum_i Linv[j][i] T_i  ->  coefficient matrix Y[i][j] = Linv[j][i]
+            std::vector<double> Y(static_cast<size_t>(k) * k);
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j)
+                    Y[static_cast<size_t>(i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
+            if ((rc = combine<T, T, double>(Tb, k, Y, k, 0.0, Sb_)))
+                return rc;
+            PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
+        }
+        if (ok) {
+            kept = k;
+            return PYCI_GPU_OK;
+        }
+    }
+    return orthonormalize_mgs(V, m, k, kept);
+}
+
+template<typename T>
+int Davidson<T>::orthonormalize_mgs(T *V, int m, int k, int &kept) {
     const double drop = mixed_ ? 1e-3 : 1e-8;
     kept = 0;
     std::vector<double> C;
@@ -396,7 +465,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         (rc = alloc(&Xr, static_cast<int64_t>(std::max(nkeep_max, b)) * N)) ||
         (rc = alloc(&AXr, static_cast<int64_t>(std::max(nkeep_max, b)) * N)) ||
         (rc = alloc(&R, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi_, N * kMaxQ)) ||
-        (rc = alloc(&Yi_, N * kMaxQ)) || (rc = alloc(&d_partial_, static_cast<int64_t>(gram_blocks_) * kMaxGramP * kMaxQ)) ||
+        (rc = alloc(&Yi_, N * kMaxQ)) || (rc = alloc(&Sb_, N * kMaxQ)) || (rc = alloc(&d_partial_, static_cast<int64_t>(gram_blocks_) * kMaxGramP * kMaxQ)) ||
         (rc = alloc(&d_small_, kMaxGramP * kMaxQ)) || (rc = alloc(&d_coef_, kMaxGramP * kMaxQ)) ||
         (rc = alloc(&d_theta_, std::max(mmax, b))))
         return rc;
@@ -502,10 +571,10 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         residual_kernel<T><<<grid(N), 256, 0, st_>>>(AXr, Xr, d_theta_, b, N, R), ::pyci_gpu::note_launch();
         bool all = true;
         std::vector<int> todo;
+        if ((rc = gram<T>(R, b, R, b, Gc)))
+            return rc;
         for (int j = 0; j < b; ++j) {
-            if ((rc = gram<T>(R + static_cast<int64_t>(j) * N, 1, R + static_cast<int64_t>(j) * N, 1, Gc)))
-                return rc;
-            rnorm[j] = std::sqrt(std::max(Gc[0], 0.0));
+            rnorm[j] = std::sqrt(std::max(Gc[static_cast<size_t>(j) * b + j], 0.0));
             double thr = tol * std::max(eps23, std::fabs(theta[j]));
             if (mixed_)
                 thr = std::max(thr, mixed_floor);

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 
 #include "internal.h"
 
@@ -72,7 +73,41 @@ struct Values<kSplit> {
     }
 };
 
-template<int VK, int K, int LANES>
+// Gather one row of the interleaved vector block x (K consecutive elements).
+// With VEC the row is read with 8- or 16-byte vector loads (the caller has
+// checked alignment); otherwise element by element.
+template<bool VEC, int K, typename XT, typename AT>
+__device__ __forceinline__ void load_x(const XT *__restrict__ xr, AT out[K]) {
+    constexpr int BYTES = K * static_cast<int>(sizeof(XT));
+    if constexpr (VEC && BYTES % 16 == 0) {
+        constexpr int NV = BYTES / 16;
+        constexpr int PER = 16 / static_cast<int>(sizeof(XT));
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            if constexpr (sizeof(XT) == 4) {
+                const float4 q = __ldg(reinterpret_cast<const float4 *>(xr) + v);
+                out[v * PER + 0] = static_cast<AT>(q.x);
+                out[v * PER + 1] = static_cast<AT>(q.y);
+                out[v * PER + 2] = static_cast<AT>(q.z);
+                out[v * PER + 3] = static_cast<AT>(q.w);
+            } else {
+                const double2 q = __ldg(reinterpret_cast<const double2 *>(xr) + v);
+                out[v * PER + 0] = static_cast<AT>(q.x);
+                out[v * PER + 1] = static_cast<AT>(q.y);
+            }
+        }
+    } else if constexpr (VEC && BYTES == 8 && sizeof(XT) == 4) {
+        const float2 q = __ldg(reinterpret_cast<const float2 *>(xr));
+        out[0] = static_cast<AT>(q.x);
+        out[1] = static_cast<AT>(q.y);
+    } else {
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            out[k] = static_cast<AT>(__ldg(xr + k));
+    }
+}
+
+template<int VK, int K, int LANES, bool VEC>
 __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
                                                    const int32_t *__restrict__ cols, Values<VK> vals,
                                                    const typename Values<VK>::x_t *__restrict__ x,
@@ -90,6 +125,7 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
 #pragma unroll
         for (int k = 0; k < K; ++k)
             acc[k] = 0;
+        acc_t xv[K];
         // Head: entries before the first 4-aligned index.
         const int64_t a0 = min(end, (start + 3) & ~static_cast<int64_t>(3));
         const int64_t a1 = max(a0, end & ~static_cast<int64_t>(3));
@@ -97,11 +133,12 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
             const int64_t e = start + lane;
             const int64_t c = __ldcs(cols + e);
             const acc_t v = vals.at(e);
+            load_x<VEC, K>(x + c * ldx, xv);
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                acc[k] += v * static_cast<acc_t>(__ldg(x + c * ldx + k));
+                acc[k] += v * xv[k];
         }
-        // Body: 4 entries per lane per step, 16-byte loads.
+        // Body: 4 entries per lane per step, 16-byte loads of columns and values.
         for (int64_t e = a0 + 4 * lane; e < a1; e += 4 * LANES) {
             const int4 c4 = __ldcs(reinterpret_cast<const int4 *>(cols + e));
             acc_t v[4];
@@ -109,10 +146,10 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
             const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                const x_t *xr = x + static_cast<int64_t>(cc[q]) * ldx;
+                load_x<VEC, K>(x + static_cast<int64_t>(cc[q]) * ldx, xv);
 #pragma unroll
                 for (int k = 0; k < K; ++k)
-                    acc[k] += v[q] * static_cast<acc_t>(__ldg(xr + k));
+                    acc[k] += v[q] * xv[k];
             }
         }
         // Tail.
@@ -120,9 +157,10 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
             const int64_t e = a1 + lane;
             const int64_t c = __ldcs(cols + e);
             const acc_t v = vals.at(e);
+            load_x<VEC, K>(x + c * ldx, xv);
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                acc[k] += v * static_cast<acc_t>(__ldg(x + c * ldx + k));
+                acc[k] += v * xv[k];
         }
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -149,9 +187,18 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
     const int64_t groups_needed = csr->nrow;
     const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (groups_needed * LANES + threads - 1) / threads));
-    spmm_kernel<VK, K, LANES><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
-        csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
-        static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
+    // Vector gathers need every x row on a 16-byte (or 8-byte) boundary.
+    const size_t rowbytes = static_cast<size_t>(ldx) * sizeof(x_t);
+    const size_t vbytes = (K * sizeof(x_t)) % 16 == 0 ? 16 : ((K * sizeof(x_t)) == 8 ? 8 : 0);
+    const bool vec = vbytes && (reinterpret_cast<uintptr_t>(x) % vbytes == 0) && (rowbytes % vbytes == 0);
+    if (vec)
+        spmm_kernel<VK, K, LANES, true><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+            csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
+            static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
+    else
+        spmm_kernel<VK, K, LANES, false><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+            csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
+            static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
 }
 
 template<int VK, int LANES>
