@@ -336,6 +336,35 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_case(args):
+    r"""Profiling driver (for ncu): build one FCI operator and run its SpMM
+    kernels, or only mixed solves, with nothing else in the launch list."""
+    import torch
+    from pyci_gb300 import capi
+    from pyci_gb300.synth import synthetic_integrals
+    nb, nu, nd = args.case
+    ecore, one, two = synthetic_integrals(nb, 1000 + nb)
+    from math import comb
+    ctx = capi.Context(0)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                   ndet=comb(nb, nu) * comb(nb, nd))
+    csr.prepare_mixed()
+    N = csr.shape()[0]
+    if args.profile == "spmm":
+        x32 = torch.randn((N, 4), dtype=torch.float32, device="cuda")
+        y32 = torch.empty_like(x32)
+        x64 = torch.randn((N, 1), dtype=torch.float64, device="cuda")
+        y64 = torch.empty_like(x64)
+        for _ in range(args.reps):
+            csr.spmm_device(capi.PREC_FP32, 4, x32.data_ptr(), y32.data_ptr(), ctx.stream)
+            csr.spmm_device(capi.PREC_FP64, 1, x64.data_ptr(), y64.data_ptr(), ctx.stream)
+        torch.cuda.synchronize()
+    else:
+        for _ in range(args.reps):
+            csr.solve(n=4, tol=TOL, ecore=ecore, mode=capi.SOLVE_MIXED)
+    print(json.dumps({"profile": args.profile, "case": list(args.case), "ndet": N, "nnz_stored": csr.shape()[3]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -343,7 +372,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline sample")
+    ap.add_argument("--profile", choices=["spmm", "solve"], default=None,
+                    help="profiling driver: only SpMM launches, or only mixed solves, on --case")
+    ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
+    ap.add_argument("--reps", type=int, default=5)
     args = ap.parse_args()
+    if args.profile:
+        run_profile_case(args)
+        return
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
