@@ -135,6 +135,22 @@ int pyci_gpu_csr_get_element(const pyci_gpu_csr *csr, int64_t i, int64_t j, doub
  * pyci/src/sparseop.cpp:96-112; the symmetric operator applies L + L^T - D). */
 int pyci_gpu_csr_matvec(const pyci_gpu_csr *csr, const double *x, double *y);
 
+/* Largest nrow / ncol pyci_gpu_csr_matvec_noalloc accepts. */
+#define PYCI_GPU_NOALLOC_MAX_ROWS (1 << 20)
+
+/* y[nrow] = H x[ncol] in FP64 like pyci_gpu_csr_matvec, but without allocating
+ * any device memory: x and y are staged in two fixed device arrays of
+ * PYCI_GPU_NOALLOC_MAX_ROWS doubles each that the library keeps on every GPU
+ * it is loaded on.  No counterpart in the reference (whose product runs on
+ * the host); it is for callers that cannot allocate device memory -- a host
+ * that gives the whole GPU to its own memory arena, code inside a CUDA-graph
+ * stream capture, loops that cannot take an allocation's implicit
+ * synchronisation.  Returns PYCI_GPU_EINVAL when nrow or ncol exceeds the
+ * maximum.  The first call on a device looks up the arrays' addresses; make
+ * it before any stream capture.  All calls on a device share the arrays:
+ * calls that overlap on the GPU race, so serialise them. */
+int pyci_gpu_csr_matvec_noalloc(const pyci_gpu_csr *csr, const double *x, double *y);
+
 /* Y = H X on device buffers for k vectors stored interleaved ([ncol][k] and
  * [nrow][k], element (row, vector) at row*k + vector), on `stream` (a
  * cudaStream_t, or NULL for the context's stream).  precision PYCI_PREC_*;

@@ -25,7 +25,7 @@ SYMBOLS = [
     "pyci_gpu_last_error", "pyci_gpu_version", "pyci_gpu_kernel_launches", "pyci_gpu_ctx_create", "pyci_gpu_ctx_destroy",
     "pyci_gpu_ctx_stream", "pyci_gpu_csr_build", "pyci_gpu_csr_update", "pyci_gpu_csr_free",
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
-    "pyci_gpu_csr_matvec", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
+    "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
 ]
 
@@ -69,6 +69,7 @@ def lib():
             "pyci_gpu_csr_export": (_int, [_p, _p, _p, _p]),
             "pyci_gpu_csr_get_element": (_int, [_p, _i64, _i64, _p]),
             "pyci_gpu_csr_matvec": (_int, [_p, _p, _p]),
+            "pyci_gpu_csr_matvec_noalloc": (_int, [_p, _p, _p]),
             "pyci_gpu_csr_spmm_device": (_int, [_p, _int, _i64, _p, _p, _p]),
             "pyci_gpu_csr_prepare_mixed": (_int, [_p, _int]),
             "pyci_gpu_csr_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, ctypes.c_double, _int,
@@ -188,6 +189,14 @@ class Csr:
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.empty(nrow, dtype=np.float64)
         check(lib().pyci_gpu_csr_matvec(self.handle, _ptr(x), _ptr(y)))
+        return y
+
+    def matvec_noalloc(self, x):
+        r"""op(x) staged in the library's fixed device arrays (no device allocation)."""
+        nrow, ncol, _, _ = self.shape()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.empty(nrow, dtype=np.float64)
+        check(lib().pyci_gpu_csr_matvec_noalloc(self.handle, _ptr(x), _ptr(y)))
         return y
 
     def spmm_device(self, precision, k, x_ptr, y_ptr, stream=None):
