@@ -350,7 +350,7 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
                 return rc;
             for (double &c : C)
                 c = -c;
-            if ((rc = combine<T, T, double>(V, m, C, k, 1.0, Tb)))
+            if ((rc = combine<T, T, T>(V, m, C, k, 1.0, Tb)))
                 return rc;
         }
         const double piv_tol = mixed_ ? 1e-6 : 1e-14;
@@ -393,7 +393,7 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
             for (int i = 0; i < k; ++i)
                 for (int j = 0; j < k; ++j)
                     Y[static_cast<size_t>(i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
-            if ((rc = combine<T, T, double>(Tb, k, Y, k, 0.0, Sb_)))
+            if ((rc = combine<T, T, T>(Tb, k, Y, k, 0.0, Sb_)))
                 return rc;
             PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
         }
@@ -425,7 +425,7 @@ int Davidson<T>::orthonormalize_mgs(T *V, int m, int k, int &kept) {
                 return rc;
             for (double &c : C)
                 c = -c;
-            rc = combine<T, T, double>(V, have, C, 1, 1.0, t);
+            rc = combine<T, T, T>(V, have, C, 1, 1.0, t);
             if (rc)
                 return rc;
         }
