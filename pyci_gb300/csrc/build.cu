@@ -42,6 +42,8 @@ struct BuildParams {
     DetTable table;
     const uint64_t *dets;   // [ndet * nwords] (hash mode) or null
     const double *one_mo, *two_mo, *h, *v, *w;
+    int ncache;             // rank-cache entries per row (0: no cache)
+    int binom_smem;         // binomial-table entries staged in shared memory (0: read from global)
     int64_t *counts;        // pass 1 output [nrow]
     const int64_t *rowptr;  // pass 2 input [nrow + 1]
     int32_t *cols;
@@ -173,131 +175,249 @@ __device__ __forceinline__ int num_candidates(const BuildParams &p, const RowSta
     return sa + sb + da + db + sa * sb;
 }
 
-// Candidate c of row `row`: its column (or -1) and, when VALUES, its matrix
-// element.  Element formulas and summation order follow add_row
-// (pyci/src/sparseop.cpp:220-258 DOCI, 260-427 FullCI, 429-502 GenCI).
-template<int NW, bool VALUES>
-__device__ int64_t candidate(const BuildParams &p, const RowState &s, int64_t row, int c,
-                             double &val) {
-    const int n = p.nbasis;
-    const double *one = p.one_mo, *two = p.two_mo;
+// One candidate excitation of a row, decoded from its index.
+struct Exc {
+    int type;            // kDociPair, kSingleA, kSingleB, kDoubleAA, kDoubleBB, kDoubleAB
+    int ii, jj, kk, ll;  // occupied/virtual orbitals (singles: ii -> jj; doubles: ii,kk -> jj,ll)
+    int sa_idx, sb_idx;  // index among the row's alpha / beta singles (opposite-spin doubles)
+    int q;               // index among the row's same-spin doubles
+};
+enum { kDociPair = 0, kSingleA = 1, kSingleB = 2, kDoubleAA = 3, kDoubleBB = 4, kDoubleAB = 5 };
+
+// Candidate c: singles of the first string (alpha, or the GenCI/DOCI string),
+// then [FullCI] beta singles, then same-spin doubles (alpha, then beta), then
+// opposite-spin doubles.  The order only fixes the index; rows are sorted.
+__device__ __forceinline__ Exc decode(const BuildParams &p, const RowState &s, int c) {
+    Exc e{};
+    const int sa = s.no_a * s.nv_a;
+    if (p.kind == PYCI_WFN_DOCI) {
+        e.type = kDociPair;
+        e.sa_idx = c;
+        e.ii = s.occ_a[c / s.nv_a];
+        e.jj = s.vir_a[c % s.nv_a];
+        return e;
+    }
+    if (c < sa) {
+        e.type = kSingleA;
+        e.sa_idx = c;
+        e.ii = s.occ_a[c / s.nv_a];
+        e.jj = s.vir_a[c % s.nv_a];
+        return e;
+    }
+    c -= sa;
+    const int qa = s.nv_a * (s.nv_a - 1) / 2;
+    const int sb = s.no_b * s.nv_b;
+    if (p.kind == PYCI_WFN_FULLCI) {
+        if (c < sb) {
+            e.type = kSingleB;
+            e.sb_idx = c;
+            e.ii = s.occ_b[c / s.nv_b];
+            e.jj = s.vir_b[c % s.nv_b];
+            return e;
+        }
+        c -= sb;
+    }
+    const int pa = s.no_a * (s.no_a - 1) / 2;
+    const int pb = s.no_b * (s.no_b - 1) / 2, qb = s.nv_b * (s.nv_b - 1) / 2;
+    if (c < pa * qa || (p.kind == PYCI_WFN_FULLCI && c < pa * qa + pb * qb)) {
+        const bool alpha = c < pa * qa;
+        const int q = alpha ? c : c - pa * qa;
+        const int qq = alpha ? qa : qb;
+        int i, k, x, y;
+        decode_pair(q / qq, i, k);
+        decode_pair(q % qq, x, y);
+        const int16_t *occ = alpha ? s.occ_a : s.occ_b;
+        const int16_t *vir = alpha ? s.vir_a : s.vir_b;
+        e.type = alpha ? kDoubleAA : kDoubleBB;
+        e.q = q;
+        e.ii = occ[i];
+        e.kk = occ[k];
+        e.jj = vir[x];
+        e.ll = vir[y];
+        return e;
+    }
+    c -= pa * qa + pb * qb;
+    e.type = kDoubleAB;
+    e.sa_idx = c / sb;
+    e.sb_idx = c % sb;
+    e.ii = s.occ_a[e.sa_idx / s.nv_a];
+    e.jj = s.vir_a[e.sa_idx % s.nv_a];
+    e.kk = s.occ_b[e.sb_idx / s.nv_b];
+    e.ll = s.vir_b[e.sb_idx % s.nv_b];
+    return e;
+}
+
+// Column of an excitation: from the row's rank cache (full spaces) or by
+// building the excited determinant and ranking / looking it up.
+template<int NW>
+__device__ __forceinline__ int64_t exc_column(const BuildParams &p, const RowState &s, int64_t row,
+                                              const Exc &e, const int32_t *cache) {
+    if (cache) {
+        const int sa = s.no_a * s.nv_a, sb = s.no_b * s.nv_b;
+        const int da = (s.no_a * (s.no_a - 1) / 2) * (s.nv_a * (s.nv_a - 1) / 2);
+        if (p.kind != PYCI_WFN_FULLCI)
+            return (e.type == kDoubleAA) ? cache[sa + e.q] : cache[e.sa_idx];
+        const int64_t ra = row / p.nbeta, rb = row % p.nbeta;
+        switch (e.type) {
+        case kSingleA: return cache[e.sa_idx] * p.nbeta + rb;
+        case kSingleB: return ra * p.nbeta + cache[sa + e.sb_idx];
+        case kDoubleAA: return cache[sa + sb + e.q] * p.nbeta + rb;
+        case kDoubleBB: return ra * p.nbeta + cache[sa + sb + da + e.q];
+        default: return cache[e.sa_idx] * p.nbeta + cache[sa + e.sb_idx];
+        }
+    }
     uint64_t a[NW], b[NW];
 #pragma unroll
     for (int w = 0; w < NW; ++w) {
         a[w] = s.ra[w];
         b[w] = s.rb[w];
     }
-    if (p.kind == PYCI_WFN_DOCI) {
-        const int i = c / s.nv_a, x = c % s.nv_a;
-        const int k = s.occ_a[i], l = s.vir_a[x];
-        flip(a, k);
-        flip(a, l);
-        const int64_t col = column_of<NW>(p, a, b);
-        if (VALUES && keep_entry(p, row, col))
-            val = __ldg(&p.v[k * n + l]);
-        return col;
+    switch (e.type) {
+    case kDociPair:
+    case kSingleA:
+        flip(a, e.ii);
+        flip(a, e.jj);
+        break;
+    case kSingleB:
+        flip(b, e.ii);
+        flip(b, e.jj);
+        break;
+    case kDoubleAA:
+        flip(a, e.ii);
+        flip(a, e.kk);
+        flip(a, e.jj);
+        flip(a, e.ll);
+        break;
+    case kDoubleBB:
+        flip(b, e.ii);
+        flip(b, e.kk);
+        flip(b, e.jj);
+        flip(b, e.ll);
+        break;
+    default:
+        flip(a, e.ii);
+        flip(a, e.jj);
+        flip(b, e.kk);
+        flip(b, e.ll);
+        break;
     }
-    const int sa = s.no_a * s.nv_a;
-    const int pa = s.no_a * (s.no_a - 1) / 2, qa = s.nv_a * (s.nv_a - 1) / 2;
-    if (c < sa) {
-        // Single excitation of the first string (alpha, or the GenCI string).
-        const int i = c / s.nv_a, x = c % s.nv_a;
-        const int ii = s.occ_a[i], jj = s.vir_a[x];
-        flip(a, ii);
-        flip(a, jj);
-        const int64_t col = column_of<NW>(p, a, b);
-        if (VALUES && keep_entry(p, row, col)) {
-            double v1 = __ldg(&one[ii * n + jj]);
-            for (int t = 0; t < s.no_a; ++t) {
-                const int kk = s.occ_a[t];
-                v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
-            }
-            for (int t = 0; t < s.no_b; ++t) {
-                const int kk = s.occ_b[t];
-                v1 += two_mo_at(two, n, ii, kk, jj, kk);
-            }
-            val = phase_single<NW>(s.ra, ii, jj) * v1;
+    return column_of<NW>(p, a, b);
+}
+
+// Matrix element of an excitation, with the formulas and summation order of
+// add_row (pyci/src/sparseop.cpp:220-258 DOCI, 260-427 FullCI, 429-502 GenCI).
+template<int NW>
+__device__ double exc_value(const BuildParams &p, const RowState &s, const Exc &e) {
+    const int n = p.nbasis;
+    const double *one = p.one_mo, *two = p.two_mo;
+    const int ii = e.ii, jj = e.jj, kk = e.kk, ll = e.ll;
+    switch (e.type) {
+    case kDociPair:
+        return __ldg(&p.v[ii * n + jj]);
+    case kSingleA: {
+        // 1-0 excitation (or the GenCI single)
+        double v1 = __ldg(&one[ii * n + jj]);
+        for (int t = 0; t < s.no_a; ++t) {
+            const int k2 = s.occ_a[t];
+            v1 += two_mo_at(two, n, ii, k2, jj, k2) - two_mo_at(two, n, ii, k2, k2, jj);
         }
-        return col;
-    }
-    c -= sa;
-    if (p.kind == PYCI_WFN_GENCI) {
-        // Same-string double (GenCI).
-        const int po = c / qa, pv = c % qa;
-        int i, k, x, y;
-        decode_pair(po, i, k);
-        decode_pair(pv, x, y);
-        const int ii = s.occ_a[i], kk = s.occ_a[k], jj = s.vir_a[x], ll = s.vir_a[y];
-        flip(a, ii);
-        flip(a, kk);
-        flip(a, jj);
-        flip(a, ll);
-        const int64_t col = column_of<NW>(p, a, b);
-        if (VALUES && keep_entry(p, row, col))
-            val = phase_double<NW>(s.ra, ii, kk, jj, ll) *
-                  (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
-        return col;
-    }
-    const int sb = s.no_b * s.nv_b;
-    const int pb = s.no_b * (s.no_b - 1) / 2, qb = s.nv_b * (s.nv_b - 1) / 2;
-    if (c < sb) {
-        // Beta single (0-1 excitation).
-        const int i = c / s.nv_b, x = c % s.nv_b;
-        const int ii = s.occ_b[i], jj = s.vir_b[x];
-        flip(b, ii);
-        flip(b, jj);
-        const int64_t col = column_of<NW>(p, a, b);
-        if (VALUES && keep_entry(p, row, col)) {
-            double v1 = __ldg(&one[ii * n + jj]);
-            for (int t = 0; t < s.no_a; ++t) {
-                const int kk = s.occ_a[t];
-                v1 += two_mo_at(two, n, ii, kk, jj, kk);
-            }
-            for (int t = 0; t < s.no_b; ++t) {
-                const int kk = s.occ_b[t];
-                v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
-            }
-            val = phase_single<NW>(s.rb, ii, jj) * v1;
+        for (int t = 0; t < s.no_b; ++t) {
+            const int k2 = s.occ_b[t];
+            v1 += two_mo_at(two, n, ii, k2, jj, k2);
         }
-        return col;
+        return phase_single<NW>(s.ra, ii, jj) * v1;
     }
-    c -= sb;
-    if (c < pa * qa || c < pa * qa + pb * qb) {
-        const bool alpha = c < pa * qa;
-        const int q = alpha ? c : c - pa * qa;
-        const int qq = alpha ? qa : qb;
-        const int po = q / qq, pv = q % qq;
-        int i, k, x, y;
-        decode_pair(po, i, k);
-        decode_pair(pv, x, y);
-        const int16_t *occ = alpha ? s.occ_a : s.occ_b;
-        const int16_t *vir = alpha ? s.vir_a : s.vir_b;
-        const int ii = occ[i], kk = occ[k], jj = vir[x], ll = vir[y];
-        uint64_t *d = alpha ? a : b;
-        flip(d, ii);
-        flip(d, kk);
-        flip(d, jj);
-        flip(d, ll);
-        const int64_t col = column_of<NW>(p, a, b);
-        if (VALUES && keep_entry(p, row, col))
-            val = phase_double<NW>(alpha ? s.ra : s.rb, ii, kk, jj, ll) *
-                  (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
-        return col;
+    case kSingleB: {
+        // 0-1 excitation
+        double v1 = __ldg(&one[ii * n + jj]);
+        for (int t = 0; t < s.no_a; ++t) {
+            const int k2 = s.occ_a[t];
+            v1 += two_mo_at(two, n, ii, k2, jj, k2);
+        }
+        for (int t = 0; t < s.no_b; ++t) {
+            const int k2 = s.occ_b[t];
+            v1 += two_mo_at(two, n, ii, k2, jj, k2) - two_mo_at(two, n, ii, k2, k2, jj);
+        }
+        return phase_single<NW>(s.rb, ii, jj) * v1;
     }
-    c -= pa * qa + pb * qb;
-    // Opposite-spin double (1-1 excitation).
-    const int ia = c / sb, ib = c % sb;
-    const int ii = s.occ_a[ia / s.nv_a], jj = s.vir_a[ia % s.nv_a];
-    const int kk = s.occ_b[ib / s.nv_b], ll = s.vir_b[ib % s.nv_b];
-    flip(a, ii);
-    flip(a, jj);
-    flip(b, kk);
-    flip(b, ll);
-    const int64_t col = column_of<NW>(p, a, b);
+    case kDoubleAA:
+        return phase_double<NW>(s.ra, ii, kk, jj, ll) *
+               (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+    case kDoubleBB:
+        return phase_double<NW>(s.rb, ii, kk, jj, ll) *
+               (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+    default:
+        // 1-1 excitation: alpha ii -> jj, beta kk -> ll
+        return (phase_single<NW>(s.ra, ii, jj) * phase_single<NW>(s.rb, kk, ll)) *
+               two_mo_at(two, n, ii, kk, jj, ll);
+    }
+}
+
+// Candidate c of row `row`: its column (or -1) and, when VALUES and the entry
+// is kept, its matrix element.
+template<int NW, bool VALUES>
+__device__ __forceinline__ int64_t candidate(const BuildParams &p, const RowState &s, int64_t row, int c,
+                                             double &val, const int32_t *cache) {
+    const Exc e = decode(p, s, c);
+    const int64_t col = exc_column<NW>(p, s, row, e, cache);
     if (VALUES && keep_entry(p, row, col))
-        val = (phase_single<NW>(s.ra, ii, jj) * phase_single<NW>(s.rb, kk, ll)) *
-              two_mo_at(two, n, ii, kk, jj, ll);
+        val = exc_value<NW>(p, s, e);
     return col;
+}
+
+// Fill the row's rank cache: the colex rank of every singly / doubly excited
+// string, in decode()'s order (alpha singles, beta singles, alpha doubles,
+// beta doubles; DOCI/GenCI: singles then doubles).  Full spaces only.
+template<int NW>
+__device__ void fill_rank_cache(const BuildParams &p, const RowState &s, const int64_t *binom, int32_t *cache) {
+    const int sa = s.no_a * s.nv_a, sb = s.no_b * s.nv_b;
+    const int pa = s.no_a * (s.no_a - 1) / 2, qa = s.nv_a * (s.nv_a - 1) / 2;
+    const int pb = s.no_b * (s.no_b - 1) / 2, qb = s.nv_b * (s.nv_b - 1) / 2;
+    const bool two = (p.kind == PYCI_WFN_FULLCI);
+    const int nsingle_b = two ? sb : 0;
+    const int ndouble_a = (p.kind == PYCI_WFN_DOCI) ? 0 : pa * qa;
+    const int ndouble_b = two ? pb * qb : 0;
+    const int total = sa + nsingle_b + ndouble_a + ndouble_b;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        uint64_t d[NW];
+        const bool alpha = (t < sa) || (t >= sa + nsingle_b && t < sa + nsingle_b + ndouble_a);
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+            d[w] = alpha ? s.ra[w] : s.rb[w];
+        if (t < sa) {
+            flip(d, s.occ_a[t / s.nv_a]);
+            flip(d, s.vir_a[t % s.nv_a]);
+        } else if (t < sa + nsingle_b) {
+            const int u = t - sa;
+            flip(d, s.occ_b[u / s.nv_b]);
+            flip(d, s.vir_b[u % s.nv_b]);
+        } else {
+            const int u = alpha ? t - sa - nsingle_b : t - sa - nsingle_b - ndouble_a;
+            const int qq = alpha ? qa : qb;
+            const int16_t *occ = alpha ? s.occ_a : s.occ_b;
+            const int16_t *vir = alpha ? s.vir_a : s.vir_b;
+            int i, k, x, y;
+            decode_pair(u / qq, i, k);
+            decode_pair(u % qq, x, y);
+            flip(d, occ[i]);
+            flip(d, occ[k]);
+            flip(d, vir[x]);
+            flip(d, vir[y]);
+        }
+        int64_t r = 0;
+        int cnt = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            uint64_t x = d[w];
+            while (x) {
+                const int pbit = __ffsll(static_cast<long long>(x)) - 1 + 64 * w;
+                ++cnt;
+                r += binom[pbit * p.ldk + cnt];
+                x &= x - 1;
+            }
+        }
+        cache[t] = static_cast<int32_t>(r);
+    }
 }
 
 // Diagonal element in the reference's summation order.
@@ -339,22 +459,49 @@ __device__ double diagonal(const BuildParams &p, const RowState &s) {
     return v2;
 }
 
+// Shared-memory scratch shared by both passes: [rank cache][binomial table].
+struct RowScratch {
+    int32_t *cache;
+    const int64_t *binom;
+};
+
+__device__ __forceinline__ RowScratch setup_scratch(const BuildParams &p, unsigned char *base) {
+    RowScratch r;
+    r.cache = p.ncache ? reinterpret_cast<int32_t *>(base) : nullptr;
+    const size_t off = (static_cast<size_t>(p.ncache) * sizeof(int32_t) + 7) & ~static_cast<size_t>(7);
+    if (p.binom_smem) {
+        int64_t *b = reinterpret_cast<int64_t *>(base + off);
+        for (int t = threadIdx.x; t < p.binom_smem; t += blockDim.x)
+            b[t] = p.binom[t];
+        r.binom = b;
+    } else {
+        r.binom = p.binom;
+    }
+    return r;
+}
+
 // Pass 1: stored entries per row.
 template<int NW>
 __global__ void __launch_bounds__(256) count_kernel(BuildParams p, int64_t row0) {
     __shared__ RowState s;
     __shared__ int total;
+    extern __shared__ __align__(16) unsigned char dyn[];
     const int64_t row = row0 + blockIdx.x;
     if (row >= p.nrow)
         return;
     if (threadIdx.x == 0)
         total = 0;
+    const RowScratch sc = setup_scratch(p, dyn);
     load_row<NW>(p, row, s);
+    if (sc.cache) {
+        fill_rank_cache<NW>(p, s, sc.binom, sc.cache);
+        __syncthreads();
+    }
     const int nc = num_candidates(p, s);
     int mine = 0;
     double dummy = 0.0;
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-        const int64_t col = candidate<NW, false>(p, s, row, c, dummy);
+        const int64_t col = candidate<NW, false>(p, s, row, c, dummy, sc.cache);
         mine += keep_entry(p, row, col) ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1)
@@ -377,13 +524,18 @@ __global__ void __launch_bounds__(256) fill_kernel(BuildParams p, int64_t row0, 
     const int64_t row = row0 + blockIdx.x;
     if (row >= p.nrow)
         return;
+    const RowScratch sc = setup_scratch(p, smem + (sizeof(double) + sizeof(int32_t)) * static_cast<size_t>(cap));
     load_row<NW>(p, row, s);
+    if (sc.cache) {
+        fill_rank_cache<NW>(p, s, sc.binom, sc.cache);
+        __syncthreads();
+    }
     const int nc = num_candidates(p, s);
     for (int c = threadIdx.x; c < cap; c += blockDim.x) {
         int32_t key = kSentinel;
         double val = 0.0;
         if (c < nc) {
-            const int64_t col = candidate<NW, true>(p, s, row, c, val);
+            const int64_t col = candidate<NW, true>(p, s, row, c, val, sc.cache);
             if (keep_entry(p, row, col))
                 key = static_cast<int32_t>(col);
         } else if (c == nc) {
@@ -766,9 +918,15 @@ template<int NW>
 int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap) {
     cudaStream_t st = ctx->stream;
     const int64_t chunk = 1 << 20; // rows per launch (grid.x limit is generous; keeps launches short)
+    // Shared-memory scratch: rank cache + binomial table (see setup_scratch).
+    const size_t scratch = ((static_cast<size_t>(p.ncache) * sizeof(int32_t) + 7) & ~static_cast<size_t>(7)) +
+                           static_cast<size_t>(p.binom_smem) * sizeof(int64_t);
+    if (scratch > 48 * 1024)
+        PYCI_CUDA_TRY(cudaFuncSetAttribute(count_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(scratch)));
     for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
         const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
-        count_kernel<NW><<<static_cast<unsigned>(nb), 256, 0, st>>>(p, r0), ::pyci_gpu::note_launch();
+        count_kernel<NW><<<static_cast<unsigned>(nb), 256, scratch, st>>>(p, r0), ::pyci_gpu::note_launch();
     }
     PYCI_CUDA_TRY(cudaGetLastError());
     int rc = device_exclusive_scan(p.counts, p.nrow, csr->rowptr, st);
@@ -786,7 +944,7 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap) {
     p.vals = csr->vals;
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
-    const size_t smem = static_cast<size_t>(cap) * (sizeof(double) + sizeof(int32_t));
+    const size_t smem = static_cast<size_t>(cap) * (sizeof(double) + sizeof(int32_t)) + scratch;
     if (smem > 48 * 1024) {
         if (smem > ctx->smem_optin) {
             set_error("a row has %d candidate entries, more than shared memory holds", cap);
@@ -1007,6 +1165,21 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         set_error("rows with %lld candidate excitations are not supported", (long long)ncand);
         return PYCI_GPU_EUNSUPPORTED;
     }
+
+    // Rank cache (full spaces): every row has the same number of excitations.
+    p.ncache = 0;
+    if (colex) {
+        const int64_t pa = no_a * (no_a - 1) / 2, qa = nv_a * (nv_a - 1) / 2;
+        const int64_t pb = no_b * (no_b - 1) / 2, qb = nv_b * (nv_b - 1) / 2;
+        int64_t nc = no_a * nv_a;
+        if (kind == PYCI_WFN_FULLCI)
+            nc += no_b * nv_b + pa * qa + pb * qb;
+        else if (kind == PYCI_WFN_GENCI)
+            nc += pa * qa;
+        if (nc * static_cast<int64_t>(sizeof(int32_t)) <= 64 * 1024)
+            p.ncache = static_cast<int>(nc);
+    }
+    p.binom_smem = (binom.size() * sizeof(int64_t) <= 16 * 1024) ? static_cast<int>(binom.size()) : 0;
 
     int64_t *d_counts = nullptr;
     PYCI_CUDA_TRY(tmp.alloc(&d_counts, csr->nrow));

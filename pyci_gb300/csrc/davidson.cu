@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <numeric>
@@ -39,22 +40,26 @@ constexpr int kGramTile = 32;
 constexpr int kMaxGramP = 128;
 constexpr int kMaxQ = 8;
 
-// Xi[r * k + j] = V[j * N + r]
+// Xi[r * kp + j] = V[j * N + r] for j < k, 0 for k <= j < kp (padding to a
+// width the SpMM gathers with vector loads).
 template<typename T>
-__global__ void pack_kernel(const T *__restrict__ V, int64_t N, int k, T *__restrict__ Xi) {
+__global__ void pack_kernel(const T *__restrict__ V, int64_t N, int k, int kp, T *__restrict__ Xi) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        for (int j = 0; j < k; ++j)
-            Xi[r * k + j] = V[j * N + r];
+        for (int j = 0; j < kp; ++j)
+            Xi[r * kp + j] = (j < k) ? V[j * N + r] : T(0);
 }
 
 template<typename T>
-__global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, T *__restrict__ W) {
+__global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, int kp, T *__restrict__ W) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x)
         for (int j = 0; j < k; ++j)
-            W[j * N + r] = Yi[r * k + j];
+            W[j * N + r] = Yi[r * kp + j];
 }
+
+// Width the SpMM reads with 8/16-byte vector gathers: 3 -> 4, 5..7 -> 8.
+inline int padded_width(int k) { return k == 3 ? 4 : (k > 4 && k < 8 ? 8 : k); }
 
 // Partial Gram products: partial[block][i * q + j] = sum over the block's rows
 // of A[i][r] * B[j][r], for p <= kMaxGramP, q <= kMaxQ.  Rows are staged in
@@ -208,8 +213,11 @@ struct Timer {
 template<typename T>
 class Davidson {
 public:
-    Davidson(pyci_gpu_csr *csr, int64_t nroot, int64_t mmax, bool mixed)
-        : csr_(csr), st_(csr->ctx->stream), N_(csr->nrow), nroot_(nroot), mmax_(mmax), mixed_(mixed) {}
+    // nroot: block size (Ritz pairs tracked); nwant <= nroot: roots that must
+    // converge and are returned (the rest are buffer vectors).
+    Davidson(pyci_gpu_csr *csr, int64_t nroot, int64_t nwant, int64_t mmax, bool mixed)
+        : csr_(csr), st_(csr->ctx->stream), N_(csr->nrow), nroot_(nroot), nwant_(nwant), mmax_(mmax),
+          mixed_(mixed) {}
 
     ~Davidson() {
         for (void *p : allocs_)
@@ -297,13 +305,14 @@ private:
     int apply(const T *V, int k, T *W, int prec) {
         for (int j0 = 0; j0 < k; j0 += kMaxQ) {
             const int kk = std::min(kMaxQ, k - j0);
-            pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, Xi_), ::pyci_gpu::note_launch();
+            const int kp = padded_width(kk);
+            pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_), ::pyci_gpu::note_launch();
             cudaEventRecord(ev0_, st_);
-            int rc = csr_spmm(csr_, prec, kk, Xi_, Yi_, st_);
+            int rc = csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
             if (rc)
                 return rc;
             cudaEventRecord(ev1_, st_);
-            unpack_kernel<T><<<grid(N_), 256, 0, st_>>>(Yi_, N_, kk, W + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
+            unpack_kernel<T><<<grid(N_), 256, 0, st_>>>(Yi_, N_, kk, kp, W + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
             cudaError_t e = cudaEventSynchronize(ev1_);
             if (e != cudaSuccess)
                 return cuda_status(e, "SpMM");
@@ -324,7 +333,7 @@ private:
 
     pyci_gpu_csr *csr_;
     cudaStream_t st_;
-    int64_t N_, nroot_, mmax_;
+    int64_t N_, nroot_, nwant_, mmax_;
     bool mixed_;
     std::vector<void *> allocs_;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
@@ -450,6 +459,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     const auto t_start = std::chrono::steady_clock::now();
     const int64_t N = N_;
     const int b = static_cast<int>(nroot_);
+    const int nw = static_cast<int>(nwant_);
     const int mmax = static_cast<int>(mmax_);
     const bool full_space = (N <= mmax);
     const int prec = mixed_ ? PYCI_PREC_FP32 : PYCI_PREC_FP64;
@@ -581,7 +591,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if (full_space)
                 thr = std::numeric_limits<double>::infinity();
             if (!(rnorm[j] <= thr)) {
-                all = false;
+                if (j < nw)
+                    all = false;
                 todo.push_back(j);
             }
         }
@@ -589,7 +600,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if (!mixed_) {
                 converged = true;
                 final_theta.assign(theta.begin(), theta.begin() + b);
-                max_res = *std::max_element(rnorm.begin(), rnorm.end());
+                max_res = *std::max_element(rnorm.begin(), rnorm.begin() + nw);
                 break;
             }
             // FP64 refinement of the Ritz block.
@@ -619,12 +630,13 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             }
             for (int j0 = 0; j0 < b; j0 += kMaxQ) {
                 const int kk = std::min(kMaxQ, b - j0);
-                pack_kernel<double><<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, Xi64), ::pyci_gpu::note_launch();
+                const int kp = padded_width(kk);
+                pack_kernel<double><<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, Xi64), ::pyci_gpu::note_launch();
                 cudaEventRecord(ev0_, st_);
-                if ((rc = csr_spmm(csr_, PYCI_PREC_FP64_SPLIT, kk, Xi64, Yi64, st_)))
+                if ((rc = csr_spmm(csr_, PYCI_PREC_FP64_SPLIT, kp, Xi64, Yi64, st_)))
                     return rc;
                 cudaEventRecord(ev1_, st_);
-                unpack_kernel<double><<<grid(N), 256, 0, st_>>>(Yi64, N, kk, AX64 + static_cast<int64_t>(j0) * N), ::pyci_gpu::note_launch();
+                unpack_kernel<double><<<grid(N), 256, 0, st_>>>(Yi64, N, kk, kp, AX64 + static_cast<int64_t>(j0) * N), ::pyci_gpu::note_launch();
                 PYCI_CUDA_TRY(cudaEventSynchronize(ev1_));
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, ev0_, ev1_);
@@ -656,10 +668,12 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 if ((rc = gram<double>(R64 + static_cast<int64_t>(j) * N, 1, R64 + static_cast<int64_t>(j) * N, 1, Gc)))
                     return rc;
                 const double r64 = std::sqrt(std::max(Gc[0], 0.0));
-                max_res = std::max(max_res, r64);
                 const double thr = std::max(tol * std::max(eps23, std::fabs(th64[j])), 2.0 * mixed_floor);
+                if (j < nw)
+                    max_res = std::max(max_res, r64);
                 if (!(r64 <= thr)) {
-                    ok64 = false;
+                    if (j < nw)
+                        ok64 = false;
                     todo.push_back(j);
                 }
             }
@@ -736,8 +750,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     }
     // Results: decreasing order (Spectra's result order).
     std::vector<double> h(static_cast<size_t>(N));
-    for (int c = 0; c < b; ++c) {
-        const int src = b - 1 - c;
+    for (int c = 0; c < nw; ++c) {
+        const int src = nw - 1 - c;
         evals[c] = final_theta[src] + ecore;
         if (evecs) {
             if (mixed_) {
@@ -771,25 +785,30 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
                    double tol, double ecore, int mode, double *evals, double *evecs,
                    pyci_gpu_solve_stats *stats) {
     const int64_t N = csr->nrow;
-    int64_t mmax = (ncv > 0) ? ncv : std::max<int64_t>(8 * n, 24);
-    mmax = std::max<int64_t>(mmax, 2 * n + 2);
+    // Block size: the n wanted roots plus PYCI_GPU_DAVIDSON_EXTRA buffer vectors
+    // (default 0), never more than N - 1.
+    int64_t extra = 0;
+    if (const char *env = std::getenv("PYCI_GPU_DAVIDSON_EXTRA"))
+        extra = std::max<int64_t>(0, std::atol(env));
+    const int64_t b = std::max<int64_t>(n, std::min<int64_t>(n + extra, N - 1));
+    int64_t mmax = (ncv > 0) ? ncv : std::max<int64_t>(8 * b, 24);
+    mmax = std::max<int64_t>(mmax, 2 * b + 2);
     if (N <= std::max<int64_t>(64, 3 * n) || N <= mmax)
         mmax = std::max<int64_t>(mmax, N); // full space: exact Rayleigh-Ritz
     mmax = std::min<int64_t>(mmax, std::max<int64_t>(N, 1));
-    if (mmax > N)
-        mmax = N;
+    const int64_t blk = (mmax >= N) ? n : b;
     const int64_t iters = (maxiter > 0) ? maxiter : std::max<int64_t>(1000, 10 * n);
     if (mode == PYCI_SOLVE_MIXED) {
         int rc = csr_prepare_mixed_device(csr, 0);
         if (rc)
             return rc;
-        Davidson<float> d(csr, n, mmax, true);
+        Davidson<float> d(csr, blk, n, mmax, true);
         return d.run(c0, iters, tol, ecore, evals, evecs, stats);
     }
     if (!csr->vals) {
         set_error("FP64 solve needs FP64 values (dropped by prepare_mixed)");
         return PYCI_GPU_EINVAL;
     }
-    Davidson<double> d(csr, n, mmax, false);
+    Davidson<double> d(csr, blk, n, mmax, false);
     return d.run(c0, iters, tol, ecore, evals, evecs, stats);
 }
