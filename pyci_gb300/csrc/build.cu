@@ -842,6 +842,13 @@ __global__ void max_kernel(const int64_t *v, int64_t n, unsigned long long *out)
         atomicMax(out, m);
 }
 
+// rowptr[i] = i * len (every row of a full space keeps all its candidates).
+__global__ void uniform_rowptr_kernel(int64_t *rowptr, int64_t nrow, int64_t len) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i <= nrow;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        rowptr[i] = i * len;
+}
+
 __global__ void widen_kernel(const int32_t *in, int64_t *out, int64_t n) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x)
@@ -915,7 +922,7 @@ int pick_nw(int64_t nbasis) {
 }
 
 template<int NW>
-int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap) {
+int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len) {
     cudaStream_t st = ctx->stream;
     const int64_t chunk = 1 << 20; // rows per launch (grid.x limit is generous; keeps launches short)
     // Shared-memory scratch: rank cache + binomial table (see setup_scratch).
@@ -924,14 +931,21 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap) {
     if (scratch > 48 * 1024)
         PYCI_CUDA_TRY(cudaFuncSetAttribute(count_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            static_cast<int>(scratch)));
-    for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
-        const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
-        count_kernel<NW><<<static_cast<unsigned>(nb), 256, scratch, st>>>(p, r0), ::pyci_gpu::note_launch();
+    if (uniform_len > 0) {
+        // Full space, fresh build, nrow = ncol = ndet: every candidate and the
+        // diagonal are kept, so every row has the same length.
+        uniform_rowptr_kernel<<<static_cast<unsigned>(std::min<int64_t>((p.nrow + 256) / 256, 1 << 16)), 256, 0, st>>>(
+            csr->rowptr, p.nrow, uniform_len), ::pyci_gpu::note_launch();
+    } else {
+        for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
+            const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
+            count_kernel<NW><<<static_cast<unsigned>(nb), 256, scratch, st>>>(p, r0), ::pyci_gpu::note_launch();
+        }
+        PYCI_CUDA_TRY(cudaGetLastError());
+        int rc = device_exclusive_scan(p.counts, p.nrow, csr->rowptr, st);
+        if (rc)
+            return rc;
     }
-    PYCI_CUDA_TRY(cudaGetLastError());
-    int rc = device_exclusive_scan(p.counts, p.nrow, csr->rowptr, st);
-    if (rc)
-        return rc;
     int64_t nnz = 0;
     PYCI_CUDA_TRY(cudaMemcpyAsync(&nnz, csr->rowptr + p.nrow, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     PYCI_CUDA_TRY(cudaStreamSynchronize(st));
@@ -1199,10 +1213,12 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         default: rc = run_build_genci_ref<4>(ctx, p, csr); break;
         }
     } else {
+        const bool uniform = colex && legacy_nrow == 0 && csr->nrow == csr->ndet && csr->ncol == csr->ndet;
+        const int64_t ulen = uniform ? ncand + 1 : 0;
         switch (nw) {
-        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap)); break;
-        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap)); break;
-        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap)); break;
+        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen); break;
+        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen); break;
+        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap), ulen); break;
         }
     }
     if (rc)

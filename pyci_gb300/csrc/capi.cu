@@ -222,6 +222,9 @@ int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
     csr_release(csr);
     const double avg = next.nrow ? static_cast<double>(next.nnz) / next.nrow : 0.0;
     next.spmm_lanes = avg >= 96 ? 32 : (avg >= 24 ? 16 : 8);
+    for (auto &row : next.tuned)
+        for (int &v : row)
+            v = -1; // the matrix changed: tune again
     *csr = next;
     return PYCI_GPU_OK;
 }

@@ -40,7 +40,12 @@ struct pyci_gpu_csr {
     int32_t *lower_len = nullptr; // [nrow] reference entries per row (symmetric)
     int64_t *ref_rowptr = nullptr; // [nrow + 1] prefix sum of lower_len (symmetric)
     double *diag = nullptr;      // [nrow] diagonal (0 where absent)
-    int spmm_lanes = 32;         // lanes per row chosen for the SpMV kernels
+    int spmm_lanes = 32;         // lanes per row suggested by the mean row length
+    // SpMM tile variant chosen by the autotuner per (value kind, width k <= 8),
+    // -1 until the first product with that pair.
+    mutable int tuned[3][9] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1},
+                               {-1, -1, -1, -1, -1, -1, -1, -1, -1},
+                               {-1, -1, -1, -1, -1, -1, -1, -1, -1}};
     // GenCI in the reference's own row loop (see genci_ref_* in build.cu):
     // only the reference's layout is stored; a symmetric product then
     // scatters the transpose with atomics.

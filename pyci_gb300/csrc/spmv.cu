@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 
 #include "internal.h"
 
@@ -107,7 +108,11 @@ __device__ __forceinline__ void load_x(const XT *__restrict__ xr, AT out[K]) {
     }
 }
 
-template<int VK, int K, int LANES, bool VEC>
+// MAP 0: each lane owns 4 consecutive entries per step (16-byte loads of
+// columns and values); MAP 1: lane l owns entries l, l + LANES, ... so one
+// gather instruction covers LANES consecutive columns of the sorted row,
+// which share 32-byte sectors more often.  The autotuner picks per operator.
+template<int VK, int K, int LANES, bool VEC, int MAP>
 __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
                                                    const int32_t *__restrict__ cols, Values<VK> vals,
                                                    const typename Values<VK>::x_t *__restrict__ x,
@@ -126,6 +131,17 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
         for (int k = 0; k < K; ++k)
             acc[k] = 0;
         acc_t xv[K];
+        if (MAP == 1) {
+#pragma unroll 4
+            for (int64_t e = start + lane; e < end; e += LANES) {
+                const int64_t c = __ldcs(cols + e);
+                const acc_t v = vals.at(e);
+                load_x<VEC, K>(x + c * ldx, xv);
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    acc[k] += v * xv[k];
+            }
+        } else {
         // Head: entries before the first 4-aligned index.
         const int64_t a0 = min(end, (start + 3) & ~static_cast<int64_t>(3));
         const int64_t a1 = max(a0, end & ~static_cast<int64_t>(3));
@@ -162,6 +178,7 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
             for (int k = 0; k < K; ++k)
                 acc[k] += v * xv[k];
         }
+        }
 #pragma unroll
         for (int k = 0; k < K; ++k) {
 #pragma unroll
@@ -179,7 +196,7 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
     }
 }
 
-template<int VK, int K, int LANES>
+template<int VK, int K, int LANES, int MAP>
 void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                 int64_t ldy, cudaStream_t st) {
     typedef typename Values<VK>::x_t x_t;
@@ -192,30 +209,67 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
     const size_t vbytes = (K * sizeof(x_t)) % 16 == 0 ? 16 : ((K * sizeof(x_t)) == 8 ? 8 : 0);
     const bool vec = vbytes && (reinterpret_cast<uintptr_t>(x) % vbytes == 0) && (rowbytes % vbytes == 0);
     if (vec)
-        spmm_kernel<VK, K, LANES, true><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+        spmm_kernel<VK, K, LANES, true, MAP><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
             csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
             static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
     else
-        spmm_kernel<VK, K, LANES, false><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
+        spmm_kernel<VK, K, LANES, false, MAP><<<static_cast<unsigned>(blocks), threads, 0, st>>>(
             csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx,
             static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
 }
 
-template<int VK, int LANES>
-void launch_k(const pyci_gpu_csr *csr, Values<VK> vals, int K, const void *x, int64_t ldx, void *y,
-              int64_t ldy, cudaStream_t st) {
-    switch (K) {
-    case 1: launch_one<VK, 1, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 2: launch_one<VK, 2, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 3: launch_one<VK, 3, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 4: launch_one<VK, 4, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 5: launch_one<VK, 5, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 6: launch_one<VK, 6, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    case 7: launch_one<VK, 7, LANES>(csr, vals, x, ldx, y, ldy, st); break;
-    default: launch_one<VK, 8, LANES>(csr, vals, x, ldx, y, ldy, st); break;
+// Tile variants: lanes per row (8, 16, 32) x entry mapping (0, 1).
+constexpr int kVariants = 6;
+inline int variant_lanes(int v) { return v % 3 == 0 ? 8 : (v % 3 == 1 ? 16 : 32); }
+inline int variant_map(int v) { return v / 3; }
+
+template<int VK, int K>
+void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
+                    int64_t ldy, cudaStream_t st) {
+    constexpr bool kMapped = (K == 1 || K == 2 || K == 4 || K == 8);
+    const int map = kMapped ? variant_map(v) : 0;
+    switch (variant_lanes(v) * 2 + map) {
+    case 16: launch_one<VK, K, 8, 0>(csr, vals, x, ldx, y, ldy, st); break;
+    case 32: launch_one<VK, K, 16, 0>(csr, vals, x, ldx, y, ldy, st); break;
+    case 64: launch_one<VK, K, 32, 0>(csr, vals, x, ldx, y, ldy, st); break;
+    case 17: launch_one<VK, K, 8, kMapped ? 1 : 0>(csr, vals, x, ldx, y, ldy, st); break;
+    case 33: launch_one<VK, K, 16, kMapped ? 1 : 0>(csr, vals, x, ldx, y, ldy, st); break;
+    default: launch_one<VK, K, 32, kMapped ? 1 : 0>(csr, vals, x, ldx, y, ldy, st); break;
     }
 }
 
+template<int VK>
+void launch_k(int v, const pyci_gpu_csr *csr, Values<VK> vals, int K, const void *x, int64_t ldx, void *y,
+              int64_t ldy, cudaStream_t st) {
+    switch (K) {
+    case 1: launch_variant<VK, 1>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 2: launch_variant<VK, 2>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 3: launch_variant<VK, 3>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 4: launch_variant<VK, 4>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 5: launch_variant<VK, 5>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 6: launch_variant<VK, 6>(v, csr, vals, x, ldx, y, ldy, st); break;
+    case 7: launch_variant<VK, 7>(v, csr, vals, x, ldx, y, ldy, st); break;
+    default: launch_variant<VK, 8>(v, csr, vals, x, ldx, y, ldy, st); break;
+    }
+}
+
+// Heuristic variant from the mean row length (used when tuning is off).
+inline int heuristic_variant(const pyci_gpu_csr *csr) {
+    return csr->spmm_lanes >= 32 ? 2 : (csr->spmm_lanes >= 16 ? 1 : 0);
+}
+
+bool autotune_enabled() {
+    static const bool on = [] {
+        const char *e = std::getenv("PYCI_GPU_AUTOTUNE");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// Autotuner: the first product of an operator for a (precision, width) pair
+// times every tile variant (one warm-up + two timed launches each, CUDA
+// events on the caller's stream) and keeps the fastest for later calls.
+// Every variant computes the same y, so the tuning call's result is valid.
 template<int VK>
 void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *x, void *y,
                cudaStream_t st) {
@@ -224,12 +278,36 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
         const int K = static_cast<int>(std::min<int64_t>(8, k - j0));
         const void *xs = static_cast<const x_t *>(x) + j0;
         void *ys = static_cast<x_t *>(y) + j0;
-        if (csr->spmm_lanes >= 32)
-            launch_k<VK, 32>(csr, vals, K, xs, k, ys, k, st);
-        else if (csr->spmm_lanes >= 16)
-            launch_k<VK, 16>(csr, vals, K, xs, k, ys, k, st);
-        else
-            launch_k<VK, 8>(csr, vals, K, xs, k, ys, k, st);
+        int &choice = csr->tuned[VK][K];
+        if (choice < 0) {
+            if (!autotune_enabled() || csr->nnz < (1 << 20)) {
+                choice = heuristic_variant(csr);
+            } else {
+                cudaEvent_t a, b;
+                cudaEventCreate(&a);
+                cudaEventCreate(&b);
+                float best = 1e30f;
+                int best_v = heuristic_variant(csr);
+                for (int v = 0; v < kVariants; ++v) {
+                    launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(a, st);
+                    launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                    launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(b, st);
+                    cudaEventSynchronize(b);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (ms < best) {
+                        best = ms;
+                        best_v = v;
+                    }
+                }
+                cudaEventDestroy(a);
+                cudaEventDestroy(b);
+                choice = best_v;
+            }
+        }
+        launch_k<VK>(choice, csr, vals, K, xs, k, ys, k, st);
     }
 }
 
