@@ -336,6 +336,74 @@ def run_ours(args, world, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def batch_problems():
+    r"""The 64 uneven FullCI problems: nbasis in {8, 10, 12}, alpha = beta in
+    [2, nbasis / 2], drawn from default_rng(4242); problem i uses seed 5000 + i."""
+    rng = np.random.default_rng(4242)
+    out = []
+    for i in range(64):
+        n = int(rng.choice([8, 10, 12]))
+        a = int(rng.integers(2, n // 2 + 1))
+        out.append((n, a, 5000 + i))
+    return out
+
+
+def run_batch(args):
+    r"""64 independent FCI problems, lowest 4 roots each, one batched mixed solve."""
+    import torch
+    from math import comb
+    from pyci_gb300 import capi
+    from pyci_gb300.synth import synthetic_integrals
+    ctx = capi.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    probs = batch_problems()
+    ops, ecore = [], []
+    t0 = time.perf_counter()
+    for n, a, seed in probs:
+        e, one, two = synthetic_integrals(n, seed)
+        csr = capi.Csr(ctx, capi.WFN_FULLCI, n, a, a, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                       ndet=comb(n, a) ** 2)
+        csr.prepare_mixed(drop_fp64=True)  # 12 bytes per entry: all 64 fit in HBM together
+        ops.append(csr)
+        ecore.append(e)
+    torch.cuda.synchronize()
+    build_s = time.perf_counter() - t0
+    nnz = sum(c.shape()[3] for c in ops)
+    rows = sum(c.shape()[0] for c in ops)
+    for _ in range(args.warmup):
+        capi.batch_solve(ctx, ops, ecore, n=4, tol=TOL, mode=capi.SOLVE_MIXED)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            evals, st = capi.batch_solve(ctx, ops, ecore, n=4, tol=TOL, mode=capi.SOLVE_MIXED)
+        ev1.record(stream)
+        ev1.synchronize()
+    batch_s = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    # One at a time, same operators, for comparison; FP64 references (high + low values).
+    t0 = time.perf_counter()
+    for i, c in enumerate(ops):
+        c.solve(n=4, tol=TOL, ecore=ecore[i], mode=capi.SOLVE_MIXED)
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    err = []
+    for i, c in enumerate(ops):
+        ref, _, _ = c.solve(n=4, tol=1e-9, ecore=ecore[i], mode=capi.SOLVE_FP64)
+        err.append(float(np.max(np.abs(evals[i] - ref))) * 1e6)
+    line = {"metric": "batched solves/s, 64 uneven FCI problems, 4 roots each (mixed)", "value": 64 / batch_s,
+            "unit": "solves/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": batch_s * 1e3, "higher_is_better": True, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "64 x FullCI, nbasis in {8,10,12}, alpha=beta in [2, nbasis/2], "
+                                   "default_rng(4242), seeds 5000+i", "rows": rows, "nnz_stored": nnz,
+                       "tol": TOL},
+            "build_seconds": build_s, "batched_seconds": batch_s, "sequential_mixed_seconds": seq_s,
+            "batched_speedup_vs_sequential": seq_s / batch_s, "iterations": st["iterations"],
+            "max_error_uHa_vs_fp64": max(err), "per_problem_error_uHa": err,
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_case(args):
     r"""Profiling driver (for ncu): build one FCI operator and run its SpMM
     kernels, or only mixed solves, with nothing else in the launch list."""
@@ -376,9 +444,14 @@ def main():
                     help="profiling driver: only SpMM launches, or only mixed solves, on --case")
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--workload", choices=["fci12", "batch64"], default="fci12",
+                    help="fci12: the headline FCI(12o,10e) line; batch64: the 64-problem batched solve")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args)
+        return
+    if args.workload == "batch64":
+        run_batch(args)
         return
     world, rank, local = dist_init(args)
     if args.impl == "reference":

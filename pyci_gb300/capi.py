@@ -26,7 +26,7 @@ SYMBOLS = [
     "pyci_gpu_ctx_stream", "pyci_gpu_csr_build", "pyci_gpu_csr_update", "pyci_gpu_csr_free",
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
-    "pyci_gpu_csr_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
+    "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
 ]
 
 
@@ -74,6 +74,8 @@ def lib():
             "pyci_gpu_csr_prepare_mixed": (_int, [_p, _int]),
             "pyci_gpu_csr_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, ctypes.c_double, _int,
                                           _p, _p, ctypes.POINTER(SolveStats)]),
+            "pyci_gpu_batch_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, _p, _int, _p,
+                                            ctypes.POINTER(SolveStats)]),
             "pyci_gpu_csr_digest": (_int, [_p, _p, _p, _p, _p, _p]),
             "pyci_gpu_add_all_dets": (_int, [_p, _int, _i64, _i64, _i64, _p]),
         }
@@ -229,3 +231,15 @@ class Csr:
         two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
         check(lib().pyci_gpu_csr_update(self.handle, dets.shape[0], _ptr(dets), _ptr(one_mo), _ptr(two_mo),
                                         flags))
+
+
+def batch_solve(ctx, csrs, ecore, n=4, maxiter=-1, tol=1e-12, mode=SOLVE_FP64):
+    r"""Lowest n eigenvalues of every operator in `csrs` (one batched solve)."""
+    arr = (ctypes.c_void_p * len(csrs))(*[c.handle.value if isinstance(c.handle, ctypes.c_void_p) else c.handle
+                                          for c in csrs])
+    ec = np.ascontiguousarray(ecore, dtype=np.float64)
+    evals = np.empty((len(csrs), n), dtype=np.float64)
+    st = SolveStats()
+    check(lib().pyci_gpu_batch_solve(ctx.handle, len(csrs), ctypes.cast(arr, ctypes.c_void_p), n, maxiter, tol,
+                                     _ptr(ec), mode, _ptr(evals), ctypes.byref(st)))
+    return evals, st.as_dict()

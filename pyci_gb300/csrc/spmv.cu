@@ -15,6 +15,9 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "internal.h"
 
@@ -258,6 +261,30 @@ inline int heuristic_variant(const pyci_gpu_csr *csr) {
     return csr->spmm_lanes >= 32 ? 2 : (csr->spmm_lanes >= 16 ? 1 : 0);
 }
 
+// Tuning results shared by operators of the same shape (rows, columns,
+// stored entries) in this process, so rebuilding an operator does not tune
+// again.
+struct TuneKey {
+    int64_t nrow, ncol, nnz;
+    int vk, k;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(nrow, ncol, nnz, vk, k) < std::tie(o.nrow, o.ncol, o.nnz, o.vk, o.k);
+    }
+};
+std::mutex g_tune_mutex;
+std::map<TuneKey, int> g_tune_cache;
+
+int tuning_cache_lookup(const pyci_gpu_csr *csr, int vk, int k) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune_cache.find(TuneKey{csr->nrow, csr->ncol, csr->nnz, vk, k});
+    return it == g_tune_cache.end() ? -1 : it->second;
+}
+
+void tuning_cache_store(const pyci_gpu_csr *csr, int vk, int k, int v) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[TuneKey{csr->nrow, csr->ncol, csr->nnz, vk, k}] = v;
+}
+
 bool autotune_enabled() {
     static const bool on = [] {
         const char *e = std::getenv("PYCI_GPU_AUTOTUNE");
@@ -279,6 +306,8 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
         const void *xs = static_cast<const x_t *>(x) + j0;
         void *ys = static_cast<x_t *>(y) + j0;
         int &choice = csr->tuned[VK][K];
+        if (choice < 0)
+            choice = tuning_cache_lookup(csr, VK, K);
         if (choice < 0) {
             if (!autotune_enabled() || csr->nnz < (1 << 20)) {
                 choice = heuristic_variant(csr);
@@ -305,6 +334,7 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
                 cudaEventDestroy(a);
                 cudaEventDestroy(b);
                 choice = best_v;
+                tuning_cache_store(csr, VK, K, choice);
             }
         }
         launch_k<VK>(choice, csr, vals, K, xs, k, ys, k, st);
