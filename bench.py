@@ -32,9 +32,18 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = {"workload": "FullCI nbasis=12 5a5b (627264 dets), lowest 4 roots, synthetic seeded integrals",
-            "wfn": "fullci", "nbasis": 12, "nocc_up": 5, "nocc_dn": 5, "nroot": 4, "seed": 1003}
-METRIC = "Davidson s/root at <=1 uHa (FP32-mixed), FCI(12o,10e) 4 roots; SpMV HBM GB/s"
+WORKLOADS = {
+    "fci12": {"workload": "FullCI nbasis=12 5a5b (627264 dets), lowest 4 roots, synthetic seeded integrals",
+              "wfn": "fullci", "nbasis": 12, "nocc_up": 5, "nocc_dn": 5, "nroot": 4, "seed": 1003,
+              "golden": "fci_12_5_5",
+              "metric": "Davidson s/root at <=1 uHa (FP32-mixed), FCI(12o,10e) 4 roots; SpMV HBM GB/s"},
+    "doci32": {"workload": "DOCI nbasis=32 8 pairs (10518300 dets), lowest 4 roots, synthetic seeded integrals",
+               "wfn": "doci", "nbasis": 32, "nocc_up": 8, "nocc_dn": 8, "nroot": 4, "seed": 1004,
+               "golden": "doci_32_8",
+               "metric": "Davidson s/root at <=1 uHa (FP32-mixed), DOCI(32o, 8 pairs) 4 roots; SpMV HBM GB/s"},
+}
+WORKLOAD = WORKLOADS["fci12"]
+METRIC = WORKLOAD["metric"]
 TOL = 1.0e-6  # residual <= 1e-6 * |E| (~1e-5 Ha): eigenvalues converge quadratically, well inside 1 uHa
 
 
@@ -130,7 +139,7 @@ def measured_peaks():
 def reference_eigenvalues():
     try:
         with open(os.path.join(ROOT, "tests", "golden", "digests.json")) as f:
-            w = json.load(f)["workloads"].get("fci_12_5_5")
+            w = json.load(f)["workloads"].get(WORKLOAD["golden"])
         return None if w is None else np.array(w["eigenvalues"])
     except OSError:
         return None
@@ -152,8 +161,9 @@ def cpu_solve(nthreads):
     n = csr[2].shape[0] - 1
     op = spl.LinearOperator((n, n), matvec=lambda x: O.spmv(*csr, np.ravel(x), nthreads=nthreads),
                             dtype=np.float64)
+    # Seeded random start, as the reference's Spectra solver starts from a random vector.
     evals = spl.eigsh(op, k=WORKLOAD["nroot"], which="SA", tol=TOL, return_eigenvectors=False,
-                      v0=np.ones(n) / np.sqrt(n), ncv=2 * WORKLOAD["nroot"] + 12)
+                      v0=np.random.default_rng(7).standard_normal(n), ncv=2 * WORKLOAD["nroot"] + 12)
     t2 = time.perf_counter()
     return t2 - t0, t1 - t0, np.sort(evals) + ecore
 
@@ -194,11 +204,14 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream)
     nb, nu, nd, nroot = WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"], WORKLOAD["nroot"]
     ecore, one, two = synthetic_integrals(nb, WORKLOAD["seed"])
-    ndet = int(np.prod([__import__("math").comb(nb, k) for k in (nu, nd)]))
+    from math import comb
+    fci = WORKLOAD["wfn"] == "fullci"
+    kind = capi.WFN_FULLCI if fci else capi.WFN_DOCI
+    ndet = comb(nb, nu) * (comb(nb, nd) if fci else 1)
 
     # ---- resident CSR, built once (build time reported separately)
     t0 = time.perf_counter()
-    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX, ndet=ndet)
+    csr = capi.Csr(ctx, kind, nb, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX, ndet=ndet)
     torch.cuda.synchronize()
     build_s = time.perf_counter() - t0
     nrow, ncol, size, stored = csr.shape()
@@ -276,7 +289,7 @@ def run_ours(args, world, rank, local):
 
     # ---- end to end through the public API with host buffers
     ham = pyci.secondquant_op(ecore, one, two)
-    wfn = pyci.fullci_wfn(nb, nu, nd)
+    wfn = (pyci.fullci_wfn if fci else pyci.doci_wfn)(nb, nu, nd)
     wfn.add_all_dets()
     csr.free()  # make room: the e2e path builds its own operator
     e2e_times = []
@@ -295,7 +308,7 @@ def run_ours(args, world, rank, local):
 
     # ---- CPU baseline sample (rank 0 only, N = 1)
     cpu = None
-    if rank == 0 and world == 1 and not args.skip_cpu:
+    if rank == 0 and world == 1 and not args.skip_cpu and fci:
         nthreads = os.cpu_count() or 1
         tcpu, tbuild, ev_cpu = cpu_solve(nthreads)
         cpu = {"value": tcpu / nroot, "unit": "s/root", "cores": nthreads, "kind": "port",
@@ -311,9 +324,9 @@ def run_ours(args, world, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": "s/root", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic seeded integrals (seed 1003)",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic seeded integrals (seed %d)" % WORKLOAD["seed"],
         "config": {"workload": WORKLOAD["workload"], "ndet": N, "nnz_stored": stored, "nnz_reference": size,
-                   "roots": nroot, "tol": TOL, "l2": "matrix 8.6 GB >> 129 MB L2; no flush needed",
+                   "roots": nroot, "tol": TOL, "l2": "matrix (GBs) >> 129 MB L2; no flush needed",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"s_per_root": fp64_spr, "iterations": st64["iterations"], "matvecs": st64["matvecs"]},
         "speedup_mixed_vs_fp64": fp64_spr / (ms_step / 1e3 / nroot),
@@ -383,8 +396,9 @@ def run_batch(args):
     batch_s = ev0.elapsed_time(ev1) / 1e3 / args.steps
     # One at a time, same operators, for comparison; FP64 references (high + low values).
     t0 = time.perf_counter()
+    seq_iters = []
     for i, c in enumerate(ops):
-        c.solve(n=4, tol=TOL, ecore=ecore[i], mode=capi.SOLVE_MIXED)
+        seq_iters.append(c.solve(n=4, tol=TOL, ecore=ecore[i], mode=capi.SOLVE_MIXED)[2]["iterations"])
     torch.cuda.synchronize()
     seq_s = time.perf_counter() - t0
     err = []
@@ -399,6 +413,8 @@ def run_batch(args):
                        "tol": TOL},
             "build_seconds": build_s, "batched_seconds": batch_s, "sequential_mixed_seconds": seq_s,
             "batched_speedup_vs_sequential": seq_s / batch_s, "iterations": st["iterations"],
+            "per_problem_iterations": st["per_problem_iterations"], "sequential_iterations": seq_iters,
+            "max_residual_fp64": st["max_residual"], "seconds_spmm": st["seconds_spmm"],
             "max_error_uHa_vs_fp64": max(err), "per_problem_error_uHa": err,
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
@@ -414,8 +430,12 @@ def run_profile_case(args):
     ecore, one, two = synthetic_integrals(nb, 1000 + nb)
     from math import comb
     ctx = capi.Context(0)
-    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX,
-                   ndet=comb(nb, nu) * comb(nb, nd))
+    if args.wfn == "doci":
+        csr = capi.Csr(ctx, capi.WFN_DOCI, nb, nu, nu, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                       ndet=comb(nb, nu))
+    else:
+        csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                       ndet=comb(nb, nu) * comb(nb, nd))
     csr.prepare_mixed()
     N = csr.shape()[0]
     if args.profile == "spmm":
@@ -444,9 +464,15 @@ def main():
                     help="profiling driver: only SpMM launches, or only mixed solves, on --case")
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
-    ap.add_argument("--workload", choices=["fci12", "batch64"], default="fci12",
-                    help="fci12: the headline FCI(12o,10e) line; batch64: the 64-problem batched solve")
+    ap.add_argument("--wfn", choices=["fullci", "doci"], default="fullci", help="wave function of --case")
+    ap.add_argument("--workload", choices=["fci12", "doci32", "batch64"], default="fci12",
+                    help="fci12: the headline FCI(12o,10e) line; doci32: DOCI(32o, 8 pairs); "
+                         "batch64: the 64-problem batched solve")
     args = ap.parse_args()
+    global WORKLOAD, METRIC
+    if args.workload in WORKLOADS:
+        WORKLOAD = WORKLOADS[args.workload]
+        METRIC = WORKLOAD["metric"]
     if args.profile:
         run_profile_case(args)
         return

@@ -178,20 +178,24 @@ int pyci_gpu_csr_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t n
                        int64_t maxiter, double tol, double ecore, int mode, double *evals,
                        double *evecs, pyci_gpu_solve_stats *stats);
 
-/* Lowest 4 eigenpairs' eigenvalues of each of nprob independent operators
- * (square, symmetric, built on ctx), solved together: all problems advance
- * in lockstep through one block-Davidson iteration, with one SpMM launch per
- * iteration for every still-unconverged problem (replayed from a captured
- * CUDA graph), segmented Gram products and per-problem Rayleigh-Ritz.  No
- * counterpart in the reference, which solves one operator at a time
+/* Lowest 4 eigenpairs of each of nprob independent operators (square,
+ * symmetric, built on ctx), solved together: all problems advance through one
+ * block-Davidson iteration, with one SpMM launch per iteration for every
+ * still-unconverged problem (replayed from a captured CUDA graph), segmented
+ * Gram products, and per-problem subspace sizes, Rayleigh-Ritz and restarts.
+ * No counterpart in the reference, which solves one operator at a time
  * (SparseOp::solve_ci, pyci/src/sparseop.cpp:114-146); the convergence test is
- * the one of pyci_gpu_csr_solve.  n must be 4.  evals: f64[nprob][4], each
- * problem's in decreasing order with ecore[p] added.  MIXED mode splits every
- * operator's values (pyci_gpu_csr_prepare_mixed) and finishes each problem
- * with an FP64 Rayleigh-Ritz step. */
+ * the one of pyci_gpu_csr_solve.  n must be 4.
+ *   evals       f64[nprob][4], each problem's in decreasing order with ecore[p] added
+ *   evecs       NULL, or nprob host pointers (each NULL or f64[4][nrow_p]):
+ *               eigenvectors in the order of evals
+ *   iterations  NULL or int64[nprob]: the iteration at which each problem converged
+ * MIXED mode splits every operator's values (pyci_gpu_csr_prepare_mixed) and
+ * finishes each problem with an FP64 Rayleigh-Ritz step; stats->max_residual
+ * is the largest FP64 residual norm over all problems' eigenpairs. */
 int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_csr *const *ops, int64_t n,
                          int64_t maxiter, double tol, const double *ecore, int mode, double *evals,
-                         pyci_gpu_solve_stats *stats);
+                         double *const *evecs, int64_t *iterations, pyci_gpu_solve_stats *stats);
 
 /* Order-independent digest of the reference-layout CSR, for checking
  * full-size builds against a digest computed from the reference's arrays:

@@ -139,7 +139,13 @@ def lowest_eigenvalues(data, indices, indptr, nroot=1, tol=1e-12):
 
     Dense eigh for small matrices; ARPACK's implicitly restarted Lanczos
     (scipy.sparse.linalg.eigsh) on the oracle's threaded symmetric SpMV
-    otherwise, which never forms the full matrix.
+    otherwise, which never forms the full matrix.  The Lanczos start vector is
+    seeded random, as the reference's Spectra solver starts from a random
+    vector (SymEigsSolver::init() without coefficients,
+    pyci/src/sparseop.cpp:131-132): a structured start such as the all-ones
+    vector lies in one spin-flip symmetry sector of a FullCI Hamiltonian with
+    nocc_up == nocc_dn, and the other sector's roots then appear only through
+    rounding.
     """
     import scipy.sparse.linalg as spl
     n = indptr.shape[0] - 1
@@ -148,5 +154,5 @@ def lowest_eigenvalues(data, indices, indptr, nroot=1, tol=1e-12):
     op = spl.LinearOperator((n, n), matvec=lambda x: spmv(data, indices, indptr, np.ravel(x)),
                             dtype=np.float64)
     vals = spl.eigsh(op, k=nroot, which="SA", tol=tol, return_eigenvectors=False,
-                     v0=np.ones(n) / np.sqrt(n), ncv=max(2 * nroot + 1, 20))
+                     v0=np.random.default_rng(7).standard_normal(n), ncv=max(2 * nroot + 1, 20))
     return np.sort(vals)

@@ -74,7 +74,7 @@ def lib():
             "pyci_gpu_csr_prepare_mixed": (_int, [_p, _int]),
             "pyci_gpu_csr_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, ctypes.c_double, _int,
                                           _p, _p, ctypes.POINTER(SolveStats)]),
-            "pyci_gpu_batch_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, _p, _int, _p,
+            "pyci_gpu_batch_solve": (_int, [_p, _i64, _p, _i64, _i64, ctypes.c_double, _p, _int, _p, _p, _p,
                                             ctypes.POINTER(SolveStats)]),
             "pyci_gpu_csr_digest": (_int, [_p, _p, _p, _p, _p, _p]),
             "pyci_gpu_add_all_dets": (_int, [_p, _int, _i64, _i64, _i64, _p]),
@@ -233,13 +233,29 @@ class Csr:
                                         flags))
 
 
-def batch_solve(ctx, csrs, ecore, n=4, maxiter=-1, tol=1e-12, mode=SOLVE_FP64):
-    r"""Lowest n eigenvalues of every operator in `csrs` (one batched solve)."""
+def batch_solve(ctx, csrs, ecore, n=4, maxiter=-1, tol=1e-12, mode=SOLVE_FP64, evecs=False):
+    r"""Lowest n eigenpairs of every operator in `csrs` (one batched solve).
+
+    Returns (evals [nprob][n], stats) with stats["per_problem_iterations"],
+    or (evals, evecs, stats) with evecs a list of [n][nrow_p] arrays when
+    `evecs` is true.
+    """
     arr = (ctypes.c_void_p * len(csrs))(*[c.handle.value if isinstance(c.handle, ctypes.c_void_p) else c.handle
                                           for c in csrs])
     ec = np.ascontiguousarray(ecore, dtype=np.float64)
     evals = np.empty((len(csrs), n), dtype=np.float64)
+    iters = np.zeros(len(csrs), dtype=np.int64)
+    vecs, vptr = None, None
+    if evecs:
+        vecs = [np.empty((n, c.shape()[0]), dtype=np.float64) for c in csrs]
+        vptr = (ctypes.c_void_p * len(csrs))(*[v.ctypes.data for v in vecs])
     st = SolveStats()
     check(lib().pyci_gpu_batch_solve(ctx.handle, len(csrs), ctypes.cast(arr, ctypes.c_void_p), n, maxiter, tol,
-                                     _ptr(ec), mode, _ptr(evals), ctypes.byref(st)))
-    return evals, st.as_dict()
+                                     _ptr(ec), mode, _ptr(evals),
+                                     ctypes.cast(vptr, ctypes.c_void_p) if vptr is not None else None,
+                                     _ptr(iters), ctypes.byref(st)))
+    stats = st.as_dict()
+    stats["per_problem_iterations"] = iters.tolist()
+    if evecs:
+        return evals, vecs, stats
+    return evals, stats

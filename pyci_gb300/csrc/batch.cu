@@ -2,16 +2,20 @@
 //
 // No counterpart in the reference, which solves one operator at a time
 // (SparseOp::solve_ci, pyci/src/sparseop.cpp:114-146).  All problems advance
-// in lockstep through the same block-Davidson iteration as davidson.cu, on
-// vectors concatenated over problems (problem p owns rows [row0_p, row0_p +
-// N_p) of every basis vector):
-//   * one SpMM launch per iteration multiplies every active problem's block
-//     (a block-diagonal product; each row group looks its problem up in the
-//     row-offset table), replayed from a CUDA graph with fixed buffers;
-//   * Gram products and linear combinations are segmented by problem;
-//   * each problem's Rayleigh-Ritz, convergence test, thick restart and
-//     dropping of dependent directions are its own; converged problems leave
-//     the active set (their rows are skipped by the product).
+// together through the block-Davidson iteration of davidson.cu, on vectors
+// concatenated over problems (problem p owns rows [row0_p, row0_p + N_p) of
+// every basis vector):
+//   * one SpMM launch per iteration multiplies every active problem's new
+//     block (a block-diagonal product; each row group looks its problem up in
+//     a row-offset table), replayed from a CUDA graph with fixed buffers;
+//   * Gram products and linear combinations are segmented by problem and
+//     visit only the rows of the problems they concern;
+//   * each problem has its own subspace size: its new block holds only the
+//     corrections of its unconverged roots that survive orthogonalisation,
+//     written at its own next slots, and it restarts on its own when its
+//     next block would not fit;
+//   * each problem's Rayleigh-Ritz, convergence test and restart are its own;
+//     converged problems leave the active set.
 // Mixed mode: FP32 values/vectors; at the end every problem's Ritz block is
 // rebuilt in FP64 and Rayleigh-Ritz'd against the FP64 (high + low) operator.
 #include <cuda_runtime.h>
@@ -37,11 +41,21 @@ struct BatchOp {
     int64_t row0, nrow;
 };
 
-__device__ __forceinline__ int find_problem(const int64_t *row0, int nprob, int64_t r) {
-    int lo = 0, hi = nprob - 1;
+// Rows of a subset of the problems, numbered densely: subset member k is
+// problem aprob[k] and owns dense rows [arow0[k], arow0[k + 1]); *count
+// members.  Every pointer is device memory, so a captured graph sees updates.
+struct RowSet {
+    const int64_t *arow0;
+    const int *aprob;
+    const int *count;
+};
+
+// Last k in [0, n) with start[k] <= r.
+__device__ __forceinline__ int find_segment(const int64_t *start, int n, int64_t r) {
+    int lo = 0, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (row0[mid] <= r)
+        if (start[mid] <= r)
             lo = mid;
         else
             hi = mid - 1;
@@ -49,31 +63,53 @@ __device__ __forceinline__ int find_problem(const int64_t *row0, int nprob, int6
     return lo;
 }
 
-// Y[r][0..K) = sum_e A_p[r][e] X[row0_p + col_e][0..K) for every row r of an
-// active problem; rows of inactive problems are left untouched.
+// Dense row c of the subset -> problem and global row.
+__device__ __forceinline__ void rowset_row(const RowSet &rs, int nseg, const int64_t *row0, int64_t c, int &prob,
+                                           int64_t &r) {
+    const int k = find_segment(rs.arow0, nseg, c);
+    prob = rs.aprob[k];
+    r = row0[prob] + (c - rs.arow0[k]);
+}
+
+// Calls f(prob, r) for every row r of the subset's problems (grid-stride).
+template<typename F>
+__device__ __forceinline__ void for_rows(const RowSet &rs, const int64_t *row0, F &&f) {
+    const int nseg = *rs.count;
+    const int64_t total = rs.arow0[nseg];
+    for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; c < total;
+         c += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int prob;
+        int64_t r;
+        rowset_row(rs, nseg, row0, c, prob, r);
+        f(prob, r);
+    }
+}
+
+// Y[r][0..K) = sum_e A_p[r][e] X[row0_p + col_e][0..K) for every row r of the
+// subset's problems; other rows are left untouched.
 // VK: 0 = FP64 values, 1 = FP32 high part, 2 = FP64 from high + low.
 template<int VK, int K, int LANES, typename XT>
-__global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restrict__ ops, const int64_t *__restrict__ row0,
-                                                         int nprob, int64_t ntotal, const int *__restrict__ active,
+__global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restrict__ ops, RowSet rs,
                                                          const XT *__restrict__ x, XT *__restrict__ y) {
     typedef typename std::conditional<VK == 1, float, double>::type acc_t;
     const int lane = threadIdx.x % LANES;
     const int64_t group = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / LANES;
     const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
-    for (int64_t r = group; r < ntotal; r += ngroups) {
-        const int p = find_problem(row0, nprob, r);
-        if (!active[p])
-            continue;
-        const BatchOp op = ops[p];
-        const int64_t lr = r - op.row0;
+    const int nseg = *rs.count;
+    const int64_t total = rs.arow0[nseg];
+    for (int64_t c = group; c < total; c += ngroups) {
+        const int k = find_segment(rs.arow0, nseg, c);
+        const BatchOp op = ops[rs.aprob[k]];
+        const int64_t lr = c - rs.arow0[k];
+        const int64_t r = op.row0 + lr;
         const int64_t start = op.rowptr[lr], end = op.rowptr[lr + 1];
         const XT *xb = x + op.row0 * K;
         acc_t acc[K];
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-            acc[k] = 0;
+        for (int j = 0; j < K; ++j)
+            acc[j] = 0;
         for (int64_t e = start + lane; e < end; e += LANES) {
-            const int64_t c = __ldcs(op.cols + e);
+            const int64_t col = __ldcs(op.cols + e);
             acc_t v;
             if (VK == 0)
                 v = static_cast<acc_t>(__ldcs(op.vals + e));
@@ -81,7 +117,7 @@ __global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restri
                 v = static_cast<acc_t>(__ldcs(op.hi + e));
             else
                 v = static_cast<acc_t>(static_cast<double>(__ldcs(op.hi + e)) + static_cast<double>(__ldcs(op.lo + e)));
-            const XT *xr = xb + c * K;
+            const XT *xr = xb + col * K;
             if constexpr (K == 4 && sizeof(XT) == 4) {
                 const float4 q = __ldg(reinterpret_cast<const float4 *>(xr));
                 acc[0] += v * q.x;
@@ -90,86 +126,117 @@ __global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restri
                 acc[3] += v * q.w;
             } else {
 #pragma unroll
-                for (int k = 0; k < K; ++k)
-                    acc[k] += v * static_cast<acc_t>(__ldg(xr + k));
+                for (int j = 0; j < K; ++j)
+                    acc[j] += v * static_cast<acc_t>(__ldg(xr + j));
             }
         }
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
+        for (int j = 0; j < K; ++j) {
 #pragma unroll
             for (int o = LANES / 2; o > 0; o >>= 1)
-                acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o, LANES);
+                acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o, LANES);
         }
         if (lane < K) {
             acc_t out = acc[0];
 #pragma unroll
-            for (int k = 1; k < K; ++k)
-                if (lane == k)
-                    out = acc[k];
+            for (int j = 1; j < K; ++j)
+                if (lane == j)
+                    out = acc[j];
             y[r * K + lane] = static_cast<XT>(out);
         }
     }
 }
 
-// Xi[r][0..K) from the K vectors V[j][r] (zero past k).
+// Xi[r][j] = V[base[prob] + j][r], j < K, for the subset's rows.
 template<typename T, int K>
-__global__ void batch_pack_kernel(const T *__restrict__ V, int64_t N, int k, T *__restrict__ Xi) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+__global__ void batch_pack_kernel(const T *__restrict__ V, int64_t N, const int *__restrict__ base, RowSet rs,
+                                  const int64_t *__restrict__ row0, T *__restrict__ Xi) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
+        const int64_t b0 = base[prob];
 #pragma unroll
         for (int j = 0; j < K; ++j)
-            Xi[r * K + j] = (j < k) ? V[j * N + r] : T(0);
+            Xi[r * K + j] = V[(b0 + j) * N + r];
+    });
 }
 
+// W[base[prob] + j][r] = Yi[r][j] and, when Wnew is given, Wnew[j][r] too.
 template<typename T, int K>
-__global__ void batch_unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, T *__restrict__ W) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        for (int j = 0; j < k; ++j)
-            W[j * N + r] = Yi[r * K + j];
+__global__ void batch_unpack_kernel(const T *__restrict__ Yi, int64_t N, const int *__restrict__ base, RowSet rs,
+                                    const int64_t *__restrict__ row0, T *__restrict__ W, T *__restrict__ Wnew) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
+        const int64_t b0 = base[prob];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const T v = Yi[r * K + j];
+            W[(b0 + j) * N + r] = v;
+            if (Wnew)
+                Wnew[j * N + r] = v;
+        }
+    });
 }
 
-// Segmented Gram product.  Tile t covers rows [tile_lo[t], tile_hi[t]) of one
-// problem; partial[t][i * q + j] = sum over those rows of A[i][r] * B[j][r].
-constexpr int kSegTile = 32;
+// Segmented Gram product.  Tile t covers rows [tile_lo[t], tile_hi[t]) of
+// problem tile_prob[t]; partial[t][i * q + j] = sum over those rows of
+// A[i][r] * B[j][r] for i < alen[prob] (zero beyond, and A is not read there).
 constexpr int kSegMaxP = 64;
 constexpr int kSegMaxQ = 8;
 
-template<typename T>
+template<typename T, int PI, int QC>
 __global__ void __launch_bounds__(256) seg_gram_kernel(const T *__restrict__ A, int p, const T *__restrict__ B, int q,
                                                        int64_t N, const int64_t *__restrict__ tile_lo,
-                                                       const int64_t *__restrict__ tile_hi, int ntiles,
-                                                       double *__restrict__ partial) {
-    __shared__ T sa[kSegMaxP][kSegTile + 1];
-    __shared__ T sb[kSegMaxQ][kSegTile + 1];
+                                                       const int64_t *__restrict__ tile_hi,
+                                                       const int *__restrict__ tile_prob, const int *__restrict__ alen,
+                                                       int ntiles, double *__restrict__ partial) {
+    // Block (x, y): tiles x, x + gridDim.x, ...; A rows i in [y * PI, y * PI + PI).
+    const int i0 = blockIdx.y * PI;
     const int pq = p * q;
+    __shared__ double red[8][PI * QC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        double acc[2] = {0.0, 0.0};
-        for (int64_t r0 = tile_lo[t]; r0 < tile_hi[t]; r0 += kSegTile) {
-            const int64_t rend = tile_hi[t];
-            for (int e = threadIdx.x; e < p * kSegTile; e += blockDim.x) {
-                const int i = e / kSegTile, c = e % kSegTile;
-                sa[i][c] = (r0 + c < rend) ? A[i * N + r0 + c] : T(0);
+        const int plim = alen ? min(p, alen[tile_prob[t]]) : p;
+        const int ni = max(0, min(PI, plim - i0));
+        T acc[PI][QC];
+#pragma unroll
+        for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+            for (int j = 0; j < QC; ++j)
+                acc[ii][j] = T(0);
+        if (ni > 0) {
+            for (int64_t r = tile_lo[t] + threadIdx.x; r < tile_hi[t]; r += blockDim.x) {
+                T bv[QC];
+#pragma unroll
+                for (int j = 0; j < QC; ++j)
+                    bv[j] = (j < q) ? B[j * N + r] : T(0);
+#pragma unroll
+                for (int ii = 0; ii < PI; ++ii)
+                    if (ii < ni) {
+                        const T a = A[(i0 + ii) * N + r];
+#pragma unroll
+                        for (int j = 0; j < QC; ++j)
+                            acc[ii][j] += a * bv[j];
+                    }
             }
-            for (int e = threadIdx.x; e < q * kSegTile; e += blockDim.x) {
-                const int j = e / kSegTile, c = e % kSegTile;
-                sb[j][c] = (r0 + c < rend) ? B[j * N + r0 + c] : T(0);
-            }
-            __syncthreads();
-            int slot = 0;
-            for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot) {
-                const int i = idx / q, j = idx % q;
-                T s = 0;
-#pragma unroll 8
-                for (int c = 0; c < kSegTile; ++c)
-                    s += sa[i][c] * sb[j][c];
-                acc[slot] += static_cast<double>(s);
-            }
-            __syncthreads();
         }
-        int slot = 0;
-        for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot)
-            partial[static_cast<int64_t>(t) * pq + idx] = acc[slot];
+#pragma unroll
+        for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+            for (int j = 0; j < QC; ++j) {
+                double v = static_cast<double>(acc[ii][j]);
+                for (int o = 16; o > 0; o >>= 1)
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0)
+                    red[warp][ii * QC + j] = v;
+            }
+        __syncthreads();
+        const int nrow_out = min(PI, p - i0);
+        for (int idx = threadIdx.x; idx < nrow_out * q; idx += blockDim.x) {
+            const int ii = idx / q, j = idx % q;
+            double v = 0.0;
+            for (int w = 0; w < nwarps; ++w)
+                v += red[w][ii * QC + j];
+            partial[static_cast<int64_t>(t) * pq + (i0 + ii) * q + j] = v;
+        }
+        __syncthreads();
     }
 }
 
@@ -194,65 +261,80 @@ __global__ void seg_reduce_kernel(const double *__restrict__ partial, int pq, co
     }
 }
 
-// out[j][r] = beta * out[j][r] + sum_i Y[prob(r)][i * q + j] * V[i][r].
+// out[obase[prob] + j][r] = beta * (same) + sum_{i < vlen[prob]} Y[prob][i * q + j] * V[i][r]
+// for the subset's rows (obase, vlen optional: 0 and p).
 template<typename TV, typename TO, typename ACC>
 __global__ void __launch_bounds__(256) seg_combine_kernel(const TV *__restrict__ V, int p, int64_t N,
-                                                          const double *__restrict__ Y, int q, double beta,
-                                                          const int64_t *__restrict__ row0, int nprob,
+                                                          const double *__restrict__ Y, int q, double beta, RowSet rs,
+                                                          const int64_t *__restrict__ row0,
+                                                          const int *__restrict__ vlen, const int *__restrict__ obase,
                                                           TO *__restrict__ out) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int prob = find_problem(row0, nprob, r);
+    for_rows(rs, row0, [&](int prob, int64_t r) {
         const double *Yp = Y + static_cast<int64_t>(prob) * p * q;
+        const int plim = vlen ? min(p, vlen[prob]) : p;
         ACC acc[kSegMaxQ];
 #pragma unroll
         for (int j = 0; j < kSegMaxQ; ++j)
             acc[j] = 0;
-        for (int i = 0; i < p; ++i) {
+        for (int i = 0; i < plim; ++i) {
             const ACC v = static_cast<ACC>(V[i * N + r]);
 #pragma unroll
             for (int j = 0; j < kSegMaxQ; ++j)
                 if (j < q)
                     acc[j] += static_cast<ACC>(__ldg(&Yp[i * q + j])) * v;
         }
+        const int64_t b0 = obase ? obase[prob] : 0;
 #pragma unroll
         for (int j = 0; j < kSegMaxQ; ++j)
             if (j < q) {
-                TO *o = out + j * N + r;
+                TO *o = out + (b0 + j) * N + r;
                 *o = (beta == 0.0) ? static_cast<TO>(acc[j]) : static_cast<TO>(static_cast<ACC>(*o) + acc[j]);
             }
-    }
+    });
+}
+
+// dst[j][r] = src[j][r], j < ncols, for the subset's rows.
+template<typename T>
+__global__ void seg_copy_kernel(const T *__restrict__ src, int ncols, int64_t N, RowSet rs,
+                                const int64_t *__restrict__ row0, T *__restrict__ dst) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
+        (void)prob;
+        for (int j = 0; j < ncols; ++j)
+            dst[j * N + r] = src[j * N + r];
+    });
 }
 
 // R[j][r] = AX[j][r] - theta[prob(r)][j] X[j][r]
 template<typename T>
 __global__ void seg_residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const double *__restrict__ theta,
-                                    int q, int64_t N, const int64_t *__restrict__ row0, int nprob, T *__restrict__ R) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int prob = find_problem(row0, nprob, r);
+                                    int q, int64_t N, RowSet rs, const int64_t *__restrict__ row0, T *__restrict__ R) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
         for (int j = 0; j < q; ++j)
             R[j * N + r] = static_cast<T>(static_cast<double>(AX[j * N + r]) -
                                           theta[prob * q + j] * static_cast<double>(X[j * N + r]));
-    }
+    });
 }
 
-// out[j][r] = use[prob][j] ? R[j][r] / (theta[prob][j] - D[r]) : 0
+// out[c][r] = R[j][r] / (theta[prob][j] - D[r]) for the root j = sel[prob][c]
+// (c < b), 0 where sel is -1; theta has nt entries per problem.
 template<typename T>
-__global__ void seg_precondition_kernel(const T *__restrict__ R, const double *__restrict__ theta,
-                                        const int *__restrict__ use, const double *__restrict__ diag, int q,
-                                        int64_t N, const int64_t *__restrict__ row0, int nprob, T *__restrict__ out) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int prob = find_problem(row0, nprob, r);
+__global__ void seg_precondition_kernel(const T *__restrict__ R, const double *__restrict__ theta, int nt,
+                                        const int *__restrict__ sel, const double *__restrict__ diag, int b,
+                                        int64_t N, RowSet rs, const int64_t *__restrict__ row0, T *__restrict__ out) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
         const double d = diag[r];
-        for (int j = 0; j < q; ++j) {
-            double den = theta[prob * q + j] - d;
-            if (fabs(den) < 1e-8)
-                den = (den < 0.0) ? -1e-8 : 1e-8;
-            out[j * N + r] = use[prob * q + j] ? static_cast<T>(static_cast<double>(R[j * N + r]) / den) : T(0);
+        for (int c = 0; c < b; ++c) {
+            const int j = sel[prob * b + c];
+            T v = T(0);
+            if (j >= 0) {
+                double den = theta[prob * nt + j] - d;
+                if (fabs(den) < 1e-8)
+                    den = (den < 0.0) ? -1e-8 : 1e-8;
+                v = static_cast<T>(static_cast<double>(R[j * N + r]) / den);
+            }
+            out[c * N + r] = v;
         }
-    }
+    });
 }
 
 template<typename TI, typename TO>
@@ -262,15 +344,18 @@ __global__ void batch_convert_kernel(const TI *__restrict__ in, TO *__restrict__
         out[r] = static_cast<TO>(in[r]);
 }
 
-__global__ void set_units_kernel(float *Vf, double *Vd, int64_t N, const int64_t *pos, int count) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < count) {
-        // pos[t] = slot * N + row
-        if (Vf)
-            Vf[pos[t]] = 1.0f;
-        if (Vd)
-            Vd[pos[t]] = 1.0;
-    }
+// Start block: T[j][r] = [local row == pick[prob][j]] + amp_prob * noise(local row, j)
+// for j < b (pick -1: no unit part); amp_prob = kGuessNoise / sqrt(N_prob).
+template<typename T>
+__global__ void seg_guess_kernel(T *__restrict__ Tb, int b, int64_t N, RowSet rs, const int64_t *__restrict__ row0,
+                                 const int64_t *__restrict__ pick) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
+        const int64_t lr = r - row0[prob];
+        const double amp = kGuessNoise / sqrt(static_cast<double>(row0[prob + 1] - row0[prob]));
+        for (int j = 0; j < b; ++j)
+            Tb[j * N + r] = static_cast<T>((pick[prob * b + j] == lr ? 1.0 : 0.0) +
+                                           amp * guess_noise(static_cast<uint64_t>(lr), static_cast<uint64_t>(j)));
+    });
 }
 
 } // namespace pyci_gpu
@@ -279,13 +364,26 @@ using namespace pyci_gpu;
 
 namespace {
 
+// A RowSet in device memory plus its host mirror.
+struct DevRowSet {
+    int64_t *arow0 = nullptr;
+    int *aprob = nullptr;
+    int *count = nullptr;
+    int64_t total = 0;
+    std::vector<int> members;
+    RowSet view() const { return RowSet{arow0, aprob, count}; }
+};
+
 // Host-side state of the batched solver.
 template<typename T>
 class Batch {
 public:
+    // nroot roots wanted per problem; nroot + 1 Ritz pairs are tracked (one
+    // guard pair, as in the single-operator solver), corrections for at most
+    // nroot of them per iteration.
     Batch(pyci_gpu_ctx *ctx, std::vector<pyci_gpu_csr *> ops, int nroot, int mmax, bool mixed)
         : ctx_(ctx), st_(ctx->stream), ops_(std::move(ops)), P_(static_cast<int>(ops_.size())), b_(nroot),
-          mmax_(mmax), mixed_(mixed) {}
+          nt_(nroot + 1), mmax_(mmax), mixed_(mixed) {}
 
     ~Batch() {
         if (graph_exec_)
@@ -295,7 +393,8 @@ public:
         cudaStreamSynchronize(st_);
     }
 
-    int run(int64_t maxiter, double tol, const double *ecore, double *evals, pyci_gpu_solve_stats *stats);
+    int run(int64_t maxiter, double tol, const double *ecore, double *evals, double *const *evecs,
+            int64_t *iterations, pyci_gpu_solve_stats *stats);
 
 private:
     template<typename U>
@@ -312,18 +411,101 @@ private:
         return static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, ctx_->num_sms * 8)));
     }
 
-    // G[prob] (p x q, row-major) = A^T B segment by segment; A has p vectors, B q.
+    int alloc_rowset(DevRowSet &rs) {
+        int rc;
+        if ((rc = alloc(&rs.arow0, P_ + 1)) || (rc = alloc(&rs.aprob, P_)) || (rc = alloc(&rs.count, 1)))
+            return rc;
+        return PYCI_GPU_OK;
+    }
+
+    // rs = the problems with mask[p] != 0.
+    int set_rowset(DevRowSet &rs, const std::vector<int> &mask) {
+        std::vector<int64_t> a(1, 0);
+        rs.members.clear();
+        for (int p = 0; p < P_; ++p)
+            if (mask[p]) {
+                rs.members.push_back(p);
+                a.push_back(a.back() + ops_[p]->nrow);
+            }
+        const int n = static_cast<int>(rs.members.size());
+        rs.total = a.back();
+        PYCI_CUDA_TRY(cudaMemcpyAsync(rs.arow0, a.data(), sizeof(int64_t) * a.size(), cudaMemcpyHostToDevice, st_));
+        if (n)
+            PYCI_CUDA_TRY(cudaMemcpyAsync(rs.aprob, rs.members.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(rs.count, &n, sizeof(int), cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st_)); // host sources are stack/heap temporaries
+        return PYCI_GPU_OK;
+    }
+
+    // Active set (rows and Gram tiles) = the problems with mask[p] != 0.
+    int set_active(const std::vector<int> &mask) {
+        int rc;
+        if ((rc = set_rowset(act_, mask)))
+            return rc;
+        std::vector<int64_t> tlo, thi;
+        std::vector<int> tprob, tbeg(P_ + 1, 0);
+        const int64_t tile = 8192;
+        for (int p = 0; p < P_; ++p) {
+            tbeg[p] = static_cast<int>(tlo.size());
+            if (!mask[p])
+                continue;
+            for (int64_t r = row0_[p]; r < row0_[p + 1]; r += tile) {
+                tlo.push_back(r);
+                thi.push_back(std::min(r + tile, row0_[p + 1]));
+                tprob.push_back(p);
+            }
+        }
+        tbeg[P_] = static_cast<int>(tlo.size());
+        ntiles_ = static_cast<int>(tlo.size());
+        if (ntiles_) {
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_lo_, tlo.data(), sizeof(int64_t) * ntiles_, cudaMemcpyHostToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_hi_, thi.data(), sizeof(int64_t) * ntiles_, cudaMemcpyHostToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_prob_, tprob.data(), sizeof(int) * ntiles_, cudaMemcpyHostToDevice, st_));
+        }
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_begin_, tbeg.data(), sizeof(int) * (P_ + 1), cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+        return PYCI_GPU_OK;
+    }
+
+    // Per-problem small integer table (e.g. subspace sizes) to the device.
+    int upload_ints(int *dst, const std::vector<int> &v) {
+        PYCI_CUDA_TRY(cudaMemcpyAsync(dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+        return PYCI_GPU_OK;
+    }
+
+    // G[prob] (p x q, row-major) = A^T B over the active problems' rows; A
+    // has p vectors (only the first alen[prob] are read when alen is given),
+    // B has q.  Inactive problems get zeros.
     template<typename U>
-    int gram(const U *A, int p, const U *B, int q, std::vector<double> &G) {
+    int gram(const U *A, int p, const U *B, int q, std::vector<double> &G, const int *alen = nullptr) {
         G.assign(static_cast<size_t>(P_) * p * q, 0.0);
+        if (ntiles_ == 0)
+            return PYCI_GPU_OK;
         for (int i0 = 0; i0 < p; i0 += kSegMaxP) {
             const int pp = std::min(kSegMaxP, p - i0);
             for (int j0 = 0; j0 < q; j0 += kSegMaxQ) {
                 const int qq = std::min(kSegMaxQ, q - j0);
-                const unsigned nb = static_cast<unsigned>(std::min<int64_t>(ntiles_, ctx_->num_sms * 8));
-                seg_gram_kernel<U><<<nb, 256, 0, st_>>>(A + static_cast<int64_t>(i0) * N_, pp, B + static_cast<int64_t>(j0) * N_,
-                                                        qq, N_, d_tile_lo_, d_tile_hi_, ntiles_, d_partial_),
-                    ::pyci_gpu::note_launch();
+                const int pi = (qq <= 4) ? 8 : 4;
+                const unsigned gy = static_cast<unsigned>((pp + pi - 1) / pi);
+                const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(ntiles_, ctx_->num_sms * 8 / gy)));
+                const U *Ai = A + static_cast<int64_t>(i0) * N_;
+                const U *Bj = B + static_cast<int64_t>(j0) * N_;
+                const int *al = (i0 == 0) ? alen : nullptr;
+                const dim3 g(nb, gy);
+                if (qq <= 1)
+                    seg_gram_kernel<U, 8, 1><<<g, 256, 0, st_>>>(Ai, pp, Bj, qq, N_, d_tile_lo_, d_tile_hi_,
+                                                                 d_tile_prob_, al, ntiles_, d_partial_);
+                else if (qq <= 2)
+                    seg_gram_kernel<U, 8, 2><<<g, 256, 0, st_>>>(Ai, pp, Bj, qq, N_, d_tile_lo_, d_tile_hi_,
+                                                                 d_tile_prob_, al, ntiles_, d_partial_);
+                else if (qq <= 4)
+                    seg_gram_kernel<U, 8, 4><<<g, 256, 0, st_>>>(Ai, pp, Bj, qq, N_, d_tile_lo_, d_tile_hi_,
+                                                                 d_tile_prob_, al, ntiles_, d_partial_);
+                else
+                    seg_gram_kernel<U, 4, 8><<<g, 256, 0, st_>>>(Ai, pp, Bj, qq, N_, d_tile_lo_, d_tile_hi_,
+                                                                 d_tile_prob_, al, ntiles_, d_partial_);
+                ::pyci_gpu::note_launch();
                 seg_reduce_kernel<<<P_ * pp * qq, 128, 0, st_>>>(d_partial_, pp * qq, d_tile_begin_, d_small_),
                     ::pyci_gpu::note_launch();
                 std::vector<double> tmp(static_cast<size_t>(P_) * pp * qq);
@@ -339,66 +521,83 @@ private:
         return PYCI_GPU_OK;
     }
 
-    // out[j] = beta out[j] + sum_i Y[prob][i][j] V[i] (Y host: [P][p][q]).
+    // out[obase + j] = beta out[obase + j] + sum_{i < vlen} Y[prob][i][j] V[i]
+    // (Y host: [P][p][q]) over the rows of rs.
     template<typename TV, typename TO, typename ACC>
-    int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out) {
+    int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out, const DevRowSet &rs,
+                const int *vlen = nullptr, const int *obase = nullptr) {
         if (p > kSegMaxP * 4 || q > kSegMaxQ) {
             set_error("batched combine: p = %d, q = %d beyond limits", p, q);
             return PYCI_GPU_EUNSUPPORTED;
         }
+        if (rs.total == 0)
+            return PYCI_GPU_OK;
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_coef_, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, st_));
-        seg_combine_kernel<TV, TO, ACC><<<grid(N_), 256, 0, st_>>>(V, p, N_, d_coef_, q, beta, d_row0_, P_, out),
+        seg_combine_kernel<TV, TO, ACC><<<grid(rs.total), 256, 0, st_>>>(V, p, N_, d_coef_, q, beta, rs.view(), d_row0_,
+                                                                          vlen, obase, out),
             ::pyci_gpu::note_launch();
         return PYCI_GPU_OK;
     }
 
-    // W_new = H V_new for the b-vector block in Tnew_ -> Wnew_ (graph replay).
-    int apply_block(int prec);
+    // W[m_p + j] = H V[m_p + j] (j < b) for every active problem, and the
+    // same products into Wnew_[j]; one graph replay (pack, SpMM, unpack).
+    int apply_block(int prec, T *V, T *W);
+
+    // Two Cholesky-QR passes of the b vectors in Tnew_ inside each active
+    // problem's block: columns with use == 0 are left out, dependent ones are
+    // dropped (use set to 0).  The kept orthonormal vectors of problem p are
+    // written, compacted, to V[base_p], V[base_p + 1], ... (base = d_base_,
+    // zero vectors after them up to b); knew[p] = how many.  tmp: b vectors.
+    int cholqr_block(std::vector<int> &use, T *tmp, T *V, std::vector<int> &knew);
 
     pyci_gpu_ctx *ctx_;
     cudaStream_t st_;
     std::vector<pyci_gpu_csr *> ops_;
-    int P_, b_, mmax_;
+    int P_, b_, nt_, mmax_;
     bool mixed_;
     int64_t N_ = 0;
     int ntiles_ = 0;
     std::vector<void *> allocs_;
     std::vector<int64_t> row0_;
+    DevRowSet act_, sel_;
     int64_t *d_row0_ = nullptr, *d_tile_lo_ = nullptr, *d_tile_hi_ = nullptr;
-    int *d_tile_begin_ = nullptr, *d_active_ = nullptr, *d_use_ = nullptr;
+    int *d_tile_begin_ = nullptr, *d_tile_prob_ = nullptr, *d_sel_ = nullptr, *d_base_ = nullptr, *d_len_ = nullptr;
+    int *d_zero_ = nullptr;
     double *d_partial_ = nullptr, *d_small_ = nullptr, *d_coef_ = nullptr, *d_theta_ = nullptr, *d_diag_ = nullptr;
     BatchOp *d_ops_ = nullptr;
     T *Tnew_ = nullptr, *Wnew_ = nullptr, *Xi_ = nullptr, *Yi_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_prec_ = -1;
+    const void *graph_v_ = nullptr;
     bool all_vals_ = true;
-    int64_t matvecs_ = 0, launches_graph_ = 0;
+    int64_t matvecs_ = 0;
     double spmm_ms_ = 0.0;
 };
 
 template<typename T>
-int Batch<T>::apply_block(int prec) {
-    // One graph: pack the block, one batched SpMM over every active problem,
-    // unpack.  Buffers are fixed, so the graph is captured once per precision.
+int Batch<T>::apply_block(int prec, T *V, T *W) {
+    // Buffers and the row set live at fixed device addresses, so the graph
+    // is captured once per precision and replayed every iteration.
     if (prec == PYCI_PREC_FP64 && !all_vals_)
         prec = PYCI_PREC_FP64_SPLIT;
-    if (!graph_exec_ || graph_prec_ != prec) {
+    if (!graph_exec_ || graph_prec_ != prec || graph_v_ != V) {
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
             graph_exec_ = nullptr;
         }
         cudaGraph_t g;
         PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        const RowSet rs = act_.view();
         const unsigned gr = grid(N_);
-        batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(Tnew_, N_, b_, Xi_);
+        batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ctx_->num_sms * 32, (N_ * 32 + 255) / 256));
         if (prec == PYCI_PREC_FP32)
-            batch_spmm_kernel<1, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, d_row0_, P_, N_, d_active_, Xi_, Yi_);
+            batch_spmm_kernel<1, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
         else if (prec == PYCI_PREC_FP64_SPLIT)
-            batch_spmm_kernel<2, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, d_row0_, P_, N_, d_active_, Xi_, Yi_);
+            batch_spmm_kernel<2, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
         else
-            batch_spmm_kernel<0, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, d_row0_, P_, N_, d_active_, Xi_, Yi_);
-        batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, b_, Wnew_);
+            batch_spmm_kernel<0, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
+        batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, d_base_, rs, d_row0_, W, Wnew_);
         cudaError_t e = cudaStreamEndCapture(st_, &g);
         if (e != cudaSuccess)
             return cuda_status(e, "graph capture");
@@ -407,6 +606,7 @@ int Batch<T>::apply_block(int prec) {
         if (e != cudaSuccess)
             return cuda_status(e, "graph instantiate");
         graph_prec_ = prec;
+        graph_v_ = V;
     }
     cudaEvent_t a, c;
     cudaEventCreate(&a);
@@ -423,33 +623,103 @@ int Batch<T>::apply_block(int prec) {
     spmm_ms_ += ms;
     cudaEventDestroy(a);
     cudaEventDestroy(c);
-    ++launches_graph_;
     return PYCI_GPU_OK;
 }
 
 template<typename T>
-int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *evals, pyci_gpu_solve_stats *stats) {
-    const auto t_start = std::chrono::steady_clock::now();
-    const int b = b_, P = P_, mmax = mmax_;
+int Batch<T>::cholqr_block(std::vector<int> &use, T *tmp, T *V, std::vector<int> &knew) {
+    const int b = b_, P = P_;
+    std::vector<double> Gc;
     int rc;
-    // Problem layout and tiles.
+    knew.assign(P, 0);
+    const T *src = Tnew_;
+    for (int pass = 0; pass < 2; ++pass) {
+        if ((rc = gram<T>(src, b, src, b, Gc)))
+            return rc;
+        std::vector<double> Y(static_cast<size_t>(P) * b * b, 0.0);
+        for (int p = 0; p < P; ++p) {
+            const double *S = &Gc[static_cast<size_t>(p) * b * b];
+            std::vector<double> L(static_cast<size_t>(b) * b, 0.0);
+            std::vector<char> keep(b, 0);
+            for (int j = 0; j < b; ++j) {
+                if (!use[p * b + j])
+                    continue;
+                double d = S[j * b + j];
+                for (int t = 0; t < j; ++t)
+                    if (keep[t])
+                        d -= L[j * b + t] * L[j * b + t];
+                if (!(d > (mixed_ ? 1e-6 : 1e-14) * S[j * b + j]) || !(d > 0.0)) {
+                    use[p * b + j] = 0; // dependent: drop
+                    continue;
+                }
+                keep[j] = 1;
+                L[j * b + j] = std::sqrt(d);
+                for (int i = j + 1; i < b; ++i) {
+                    double x = S[i * b + j];
+                    for (int t = 0; t < j; ++t)
+                        if (keep[t])
+                            x -= L[i * b + t] * L[j * b + t];
+                    L[i * b + j] = x / L[j * b + j];
+                }
+            }
+            // Inverse of the kept lower-triangular factor.
+            std::vector<double> Li(static_cast<size_t>(b) * b, 0.0);
+            for (int j = 0; j < b; ++j) {
+                if (!keep[j])
+                    continue;
+                Li[j * b + j] = 1.0 / L[j * b + j];
+                for (int i = j + 1; i < b; ++i) {
+                    if (!keep[i])
+                        continue;
+                    double x = 0.0;
+                    for (int t = j; t < i; ++t)
+                        if (keep[t])
+                            x -= L[i * b + t] * Li[t * b + j];
+                    Li[i * b + j] = x / L[i * b + i];
+                }
+            }
+            // Output column c = c-th kept vector on the last pass (compacted),
+            // column j = vector j on the first.
+            int c = 0;
+            for (int j = 0; j < b; ++j) {
+                if (!keep[j])
+                    continue;
+                const int col = (pass == 1) ? c : j;
+                for (int i = 0; i < b; ++i)
+                    Y[(static_cast<size_t>(p) * b + i) * b + col] = Li[j * b + i];
+                ++c;
+            }
+            if (pass == 1)
+                knew[p] = c;
+        }
+        if (pass == 0) {
+            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, tmp, act_)))
+                return rc;
+            src = tmp;
+        } else {
+            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, V, act_, nullptr, d_base_)))
+                return rc;
+        }
+    }
+    // After the second pass, kept vectors sit in the first knew slots: the
+    // use flags are re-derived from that order by the caller when needed.
+    return PYCI_GPU_OK;
+}
+
+template<typename T>
+int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *evals, double *const *evecs,
+                  int64_t *iterations, pyci_gpu_solve_stats *stats) {
+    const auto t_start = std::chrono::steady_clock::now();
+    const int b = b_, nt = nt_, P = P_, mmax = mmax_;
+    int rc;
     row0_.assign(P + 1, 0);
     for (int p = 0; p < P; ++p)
         row0_[p + 1] = row0_[p] + ops_[p]->nrow;
     N_ = row0_[P];
     const int64_t N = N_;
-    std::vector<int64_t> tlo, thi;
-    std::vector<int> tbeg(P + 1, 0);
-    const int64_t tile = 8192;
-    for (int p = 0; p < P; ++p) {
-        tbeg[p] = static_cast<int>(tlo.size());
-        for (int64_t r = row0_[p]; r < row0_[p + 1]; r += tile) {
-            tlo.push_back(r);
-            thi.push_back(std::min(r + tile, row0_[p + 1]));
-        }
-    }
-    tbeg[P] = static_cast<int>(tlo.size());
-    ntiles_ = static_cast<int>(tlo.size());
+    int64_t ntiles_all = 0;
+    for (int p = 0; p < P; ++p)
+        ntiles_all += (ops_[p]->nrow + 8191) / 8192;
     for (int p = 0; p < P; ++p)
         all_vals_ = all_vals_ && ops_[p]->vals;
     std::vector<BatchOp> hops(P);
@@ -457,37 +727,47 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         hops[p] = BatchOp{ops_[p]->rowptr, ops_[p]->cols, ops_[p]->vals, ops_[p]->hi, ops_[p]->lo, row0_[p], ops_[p]->nrow};
 
     T *V, *W, *X, *AX, *R, *Xk, *Wk, *Xfinal;
-    const int nkeep = std::max(b, std::min(mmax - b, 2 * b));
+    const int nkeep = std::min(kSegMaxQ, std::max(nt, std::min(mmax - b, 2 * nt)));
     if ((rc = alloc(&V, static_cast<int64_t>(mmax) * N)) || (rc = alloc(&W, static_cast<int64_t>(mmax) * N)) ||
-        (rc = alloc(&X, static_cast<int64_t>(b) * N)) || (rc = alloc(&AX, static_cast<int64_t>(b) * N)) ||
-        (rc = alloc(&R, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xk, static_cast<int64_t>(nkeep) * N)) ||
+        (rc = alloc(&X, static_cast<int64_t>(nt) * N)) || (rc = alloc(&AX, static_cast<int64_t>(nt) * N)) ||
+        (rc = alloc(&R, static_cast<int64_t>(nt) * N)) || (rc = alloc(&Xk, static_cast<int64_t>(nkeep) * N)) ||
         (rc = alloc(&Wk, static_cast<int64_t>(nkeep) * N)) || (rc = alloc(&Xfinal, static_cast<int64_t>(b) * N)) ||
         (rc = alloc(&Tnew_, static_cast<int64_t>(b) * N)) || (rc = alloc(&Wnew_, static_cast<int64_t>(b) * N)) ||
-        (rc = alloc(&Xi_, N * 4)) || (rc = alloc(&Yi_, N * 4)) ||
-        (rc = alloc(&d_row0_, P + 1)) || (rc = alloc(&d_tile_lo_, ntiles_)) || (rc = alloc(&d_tile_hi_, ntiles_)) ||
-        (rc = alloc(&d_tile_begin_, P + 1)) || (rc = alloc(&d_active_, P)) || (rc = alloc(&d_use_, P * b)) ||
-        (rc = alloc(&d_partial_, static_cast<int64_t>(ntiles_) * kSegMaxP * kSegMaxQ)) ||
+        (rc = alloc(&Xi_, N * 4)) || (rc = alloc(&Yi_, N * 4)) || (rc = alloc(&d_row0_, P + 1)) ||
+        (rc = alloc(&d_tile_lo_, ntiles_all)) || (rc = alloc(&d_tile_hi_, ntiles_all)) ||
+        (rc = alloc(&d_tile_prob_, ntiles_all)) || (rc = alloc(&d_tile_begin_, P + 1)) ||
+        (rc = alloc(&d_sel_, P * b)) || (rc = alloc(&d_base_, P)) || (rc = alloc(&d_len_, P)) ||
+        (rc = alloc(&d_zero_, P)) || (rc = alloc(&d_partial_, ntiles_all * kSegMaxP * kSegMaxQ)) ||
         (rc = alloc(&d_small_, static_cast<int64_t>(P) * kSegMaxP * kSegMaxQ)) ||
         (rc = alloc(&d_coef_, static_cast<int64_t>(P) * mmax * std::max(mmax, kSegMaxQ))) ||
-        (rc = alloc(&d_theta_, static_cast<int64_t>(P) * b)) || (rc = alloc(&d_diag_, N)) || (rc = alloc(&d_ops_, P)))
+        (rc = alloc(&d_theta_, static_cast<int64_t>(P) * nt)) || (rc = alloc(&d_diag_, N)) || (rc = alloc(&d_ops_, P)) ||
+        (rc = alloc_rowset(act_)) || (rc = alloc_rowset(sel_)))
         return rc;
+    // Every vector buffer starts at zero, so slots a problem has not written
+    // yet hold finite values wherever a kernel reads them.
+    for (auto pr : {std::make_pair(V, mmax), std::make_pair(W, mmax), std::make_pair(X, nt), std::make_pair(AX, nt),
+                    std::make_pair(R, nt), std::make_pair(Xk, nkeep), std::make_pair(Wk, nkeep),
+                    std::make_pair(Xfinal, b), std::make_pair(Tnew_, b), std::make_pair(Wnew_, b)})
+        PYCI_CUDA_TRY(cudaMemsetAsync(pr.first, 0, sizeof(T) * pr.second * N, st_));
+    PYCI_CUDA_TRY(cudaMemsetAsync(Xi_, 0, sizeof(T) * 4 * N, st_));
+    PYCI_CUDA_TRY(cudaMemsetAsync(Yi_, 0, sizeof(T) * 4 * N, st_));
+    PYCI_CUDA_TRY(cudaMemsetAsync(d_zero_, 0, sizeof(int) * P, st_));
     PYCI_CUDA_TRY(cudaMemcpyAsync(d_row0_, row0_.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, st_));
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_lo_, tlo.data(), sizeof(int64_t) * ntiles_, cudaMemcpyHostToDevice, st_));
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_hi_, thi.data(), sizeof(int64_t) * ntiles_, cudaMemcpyHostToDevice, st_));
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_tile_begin_, tbeg.data(), sizeof(int) * (P + 1), cudaMemcpyHostToDevice, st_));
     PYCI_CUDA_TRY(cudaMemcpyAsync(d_ops_, hops.data(), sizeof(BatchOp) * P, cudaMemcpyHostToDevice, st_));
     for (int p = 0; p < P; ++p)
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_diag_ + row0_[p], ops_[p]->diag, sizeof(double) * ops_[p]->nrow,
                                       cudaMemcpyDeviceToDevice, st_));
     std::vector<int> active(P, 1);
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_active_, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st_));
+    if ((rc = set_active(active)))
+        return rc;
 
-    // Initial block: unit vectors on each problem's b lowest diagonal elements.
+    // Initial block: unit vectors on each problem's b lowest diagonal
+    // elements plus a small seeded component in every row, orthonormalised
+    // inside each problem's block into slots 0..b-1.
     std::vector<double> diag(N);
     PYCI_CUDA_TRY(cudaMemcpyAsync(diag.data(), d_diag_, sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
-    PYCI_CUDA_TRY(cudaMemsetAsync(Tnew_, 0, sizeof(T) * b * N, st_));
     PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
-    std::vector<int64_t> pos;
+    std::vector<int64_t> pick(static_cast<size_t>(P) * b, -1);
     for (int p = 0; p < P; ++p) {
         const int64_t n = ops_[p]->nrow;
         std::vector<int64_t> order(n);
@@ -498,250 +778,242 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             return dx < dy || (dx == dy && x < y);
         });
         for (int j = 0; j < take; ++j)
-            pos.push_back(static_cast<int64_t>(j) * N + row0_[p] + order[j]);
+            pick[static_cast<size_t>(p) * b + j] = order[j];
     }
-    int64_t *d_pos;
-    if ((rc = alloc(&d_pos, static_cast<int64_t>(pos.size()))))
+    int64_t *d_pick;
+    if ((rc = alloc(&d_pick, static_cast<int64_t>(pick.size()))))
         return rc;
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_pos, pos.data(), sizeof(int64_t) * pos.size(), cudaMemcpyHostToDevice, st_));
-    set_units_kernel<<<static_cast<unsigned>((pos.size() + 255) / 256), 256, 0, st_>>>(
-        sizeof(T) == 4 ? reinterpret_cast<float *>(Tnew_) : nullptr,
-        sizeof(T) == 8 ? reinterpret_cast<double *>(Tnew_) : nullptr, N, d_pos, static_cast<int>(pos.size())),
-        ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaMemcpyAsync(d_pick, pick.data(), sizeof(int64_t) * pick.size(), cudaMemcpyHostToDevice, st_));
+    seg_guess_kernel<T><<<grid(N), 256, 0, st_>>>(Tnew_, b, N, act_.view(), d_row0_, d_pick), ::pyci_gpu::note_launch();
 
-    // Per-problem Davidson state.
+    // Per-problem Davidson state: subspace size m[p], projected matrix G[p].
+    std::vector<int> m(P, 0), knew(P, 0);
     std::vector<std::vector<double>> G(P, std::vector<double>(static_cast<size_t>(mmax) * mmax, 0.0));
-    std::vector<std::vector<char>> valid(P, std::vector<char>(mmax, 0));
-    std::vector<std::vector<double>> theta_final(P);
-    std::vector<double> theta_all(static_cast<size_t>(P) * b, 0.0);
-    std::vector<int> use(static_cast<size_t>(P) * b, 1);
+    std::vector<double> theta_all(static_cast<size_t>(P) * nt, 0.0);
+    // use[p][c]: column c of the new block is live; conv[p][j]: tracked root j converged.
+    std::vector<int> use(static_cast<size_t>(P) * b, 1), conv(static_cast<size_t>(P) * nt, 0);
     for (int p = 0; p < P; ++p)
         for (int j = 0; j < b; ++j)
             use[p * b + j] = (j < ops_[p]->nrow) ? 1 : 0;
+    std::vector<int64_t> conv_iter(P, 0);
+    if ((rc = upload_ints(d_base_, m)) || (rc = cholqr_block(use, Xk, V, knew)))
+        return rc;
     const double eps23 = std::pow(std::numeric_limits<double>::epsilon(), 2.0 / 3.0);
     const double floor_ = mixed_ ? 1e-5 : 0.0;
     const int prec = mixed_ ? PYCI_PREC_FP32 : PYCI_PREC_FP64;
-    int m = 0;
-    int64_t iter = 0;
+    int64_t iter = 0, restarts = 0;
     int nactive = P;
     std::vector<double> Gc;
     for (iter = 0; iter < maxiter && nactive > 0; ++iter) {
-        // New block (in Tnew_, already orthonormal): W_new = H T_new, then append.
-        if ((rc = apply_block(prec)))
+        // W = H V on each problem's new slots [m_p, m_p + b) (d_base_ = m).
+        if ((rc = apply_block(prec, V, W)))
             return rc;
-        matvecs_ += static_cast<int64_t>(nactive) * b;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(V + static_cast<int64_t>(m) * N, Tnew_, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
-        PYCI_CUDA_TRY(cudaMemcpyAsync(W + static_cast<int64_t>(m) * N, Wnew_, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
+        int mcap = 0;
         for (int p = 0; p < P; ++p)
-            for (int j = 0; j < b; ++j)
-                valid[p][m + j] = active[p] ? static_cast<char>(use[p * b + j]) : 0;
-        if ((rc = gram<T>(V, m + b, W + static_cast<int64_t>(m) * N, b, Gc)))
+            if (active[p]) {
+                matvecs_ += knew[p];
+                mcap = std::max(mcap, m[p] + knew[p]);
+            }
+        // New columns of the projected matrices.
+        std::vector<int> len(P, 0);
+        for (int p = 0; p < P; ++p)
+            len[p] = m[p] + knew[p];
+        if ((rc = upload_ints(d_len_, len)) || (rc = gram<T>(V, mcap, Wnew_, b, Gc, d_len_)))
             return rc;
-        for (int p = 0; p < P; ++p)
-            for (int i = 0; i < m + b; ++i)
-                for (int j = 0; j < b; ++j) {
-                    const double g = Gc[(static_cast<size_t>(p) * (m + b) + i) * b + j];
-                    G[p][static_cast<size_t>(i) * mmax + m + j] = g;
-                    G[p][static_cast<size_t>(m + j) * mmax + i] = g;
-                }
-        m += b;
-        // Rayleigh-Ritz per active problem over its valid slots.
-        std::vector<double> Yb(static_cast<size_t>(P) * m * b, 0.0), Yk(static_cast<size_t>(P) * m * nkeep, 0.0);
-        std::vector<int> nvalid(P, 0);
         for (int p = 0; p < P; ++p) {
             if (!active[p])
                 continue;
-            std::vector<int> idx;
-            for (int i = 0; i < m; ++i)
-                if (valid[p][i])
-                    idx.push_back(i);
-            const int mv = static_cast<int>(idx.size());
-            nvalid[p] = mv;
+            for (int i = 0; i < m[p] + knew[p]; ++i)
+                for (int j = 0; j < knew[p]; ++j) {
+                    const double g = Gc[(static_cast<size_t>(p) * mcap + i) * b + j];
+                    G[p][static_cast<size_t>(i) * mmax + m[p] + j] = g;
+                    G[p][static_cast<size_t>(m[p] + j) * mmax + i] = g;
+                }
+            m[p] += knew[p];
+        }
+        // Rayleigh-Ritz per active problem.
+        int mrr = 0;
+        for (int p = 0; p < P; ++p)
+            if (active[p])
+                mrr = std::max(mrr, m[p]);
+        std::vector<double> Yb(static_cast<size_t>(P) * mrr * nt, 0.0), Yk(static_cast<size_t>(P) * mrr * nkeep, 0.0);
+        for (int p = 0; p < P; ++p) {
+            if (!active[p])
+                continue;
+            const int mv = m[p];
             std::vector<double> Gm(static_cast<size_t>(mv) * mv), th, Y;
             for (int i = 0; i < mv; ++i)
                 for (int j = 0; j < mv; ++j)
-                    Gm[static_cast<size_t>(i) * mv + j] = G[p][static_cast<size_t>(idx[i]) * mmax + idx[j]];
+                    Gm[static_cast<size_t>(i) * mv + j] = G[p][static_cast<size_t>(i) * mmax + j];
             if (!symmetric_eigen(mv, Gm, th, Y)) {
                 set_error("Rayleigh-Ritz eigensolver failed (problem %d)", p);
                 return PYCI_GPU_ENOCONV;
             }
-            for (int j = 0; j < b; ++j) {
-                theta_all[p * b + j] = (j < mv) ? th[j] : 0.0;
+            for (int j = 0; j < nt; ++j) {
+                theta_all[p * nt + j] = (j < mv) ? th[j] : 0.0;
                 if (j < mv)
                     for (int i = 0; i < mv; ++i)
-                        Yb[(static_cast<size_t>(p) * m + idx[i]) * b + j] = Y[static_cast<size_t>(i) * mv + j];
+                        Yb[(static_cast<size_t>(p) * mrr + i) * nt + j] = Y[static_cast<size_t>(i) * mv + j];
             }
             for (int j = 0; j < std::min(nkeep, mv); ++j)
                 for (int i = 0; i < mv; ++i)
-                    Yk[(static_cast<size_t>(p) * m + idx[i]) * nkeep + j] = Y[static_cast<size_t>(i) * mv + j];
-            theta_final[p].assign(th.begin(), th.begin() + std::min(mv, b));
+                    Yk[(static_cast<size_t>(p) * mrr + i) * nkeep + j] = Y[static_cast<size_t>(i) * mv + j];
         }
-        if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, X)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AX)))
+        if ((rc = upload_ints(d_len_, m)) || (rc = combine<T, T, T>(V, mrr, Yb, nt, 0.0, X, act_, d_len_)) ||
+            (rc = combine<T, T, T>(W, mrr, Yb, nt, 0.0, AX, act_, d_len_)))
             return rc;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta_all.data(), sizeof(double) * P * b, cudaMemcpyHostToDevice, st_));
-        seg_residual_kernel<T><<<grid(N), 256, 0, st_>>>(AX, X, d_theta_, b, N, d_row0_, P, R), ::pyci_gpu::note_launch();
-        if ((rc = gram<T>(R, b, R, b, Gc)))
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta_all.data(), sizeof(double) * P * nt, cudaMemcpyHostToDevice, st_));
+        seg_residual_kernel<T><<<grid(act_.total), 256, 0, st_>>>(AX, X, d_theta_, nt, N, act_.view(), d_row0_, R),
+            ::pyci_gpu::note_launch();
+        if ((rc = gram<T>(R, nt, R, nt, Gc)))
             return rc;
+        std::vector<int> finished;
         for (int p = 0; p < P; ++p) {
             if (!active[p])
                 continue;
             bool done = true;
-            for (int j = 0; j < b; ++j) {
-                const double rn = std::sqrt(std::max(Gc[(static_cast<size_t>(p) * b + j) * b + j], 0.0));
-                double thr = std::max(tol * std::max(eps23, std::fabs(theta_all[p * b + j])), floor_);
-                const bool conv = !(j < ops_[p]->nrow) || rn <= thr || nvalid[p] >= ops_[p]->nrow;
-                use[p * b + j] = conv ? 0 : 1;
-                done = done && conv;
+            for (int j = 0; j < nt; ++j) {
+                const double rn = std::sqrt(std::max(Gc[(static_cast<size_t>(p) * nt + j) * nt + j], 0.0));
+                const double thr = std::max(tol * std::max(eps23, std::fabs(theta_all[p * nt + j])), floor_);
+                const bool cj = !(j < ops_[p]->nrow) || rn <= thr || m[p] >= ops_[p]->nrow;
+                conv[p * nt + j] = cj ? 1 : 0;
+                if (j < b)
+                    done = done && cj; // the guard pair (j = b) need not converge
             }
-            if (done) {
-                // Keep this problem's Ritz vectors for the final FP64 step.
-                active[p] = 0;
-                --nactive;
-                for (int j = 0; j < b; ++j)
-                    PYCI_CUDA_TRY(cudaMemcpyAsync(Xfinal + static_cast<int64_t>(j) * N + row0_[p],
-                                                  X + static_cast<int64_t>(j) * N + row0_[p],
-                                                  sizeof(T) * ops_[p]->nrow, cudaMemcpyDeviceToDevice, st_));
-                for (int j = 0; j < b; ++j)
-                    use[p * b + j] = 0;
-            }
+            if (done)
+                finished.push_back(p);
         }
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_active_, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st_));
+        // Problems whose corrections were all dependent last time cannot grow
+        // their subspace: they finish with their current Ritz vectors.
+        for (int p = 0; p < P; ++p)
+            if (active[p] && iter > 0 && knew[p] == 0 &&
+                std::find(finished.begin(), finished.end(), p) == finished.end())
+                finished.push_back(p);
+        if (!finished.empty()) {
+            std::vector<int> mask(P, 0);
+            for (int p : finished) {
+                mask[p] = 1;
+                active[p] = 0;
+                conv_iter[p] = iter + 1;
+                --nactive;
+            }
+            // Keep the finished problems' Ritz vectors for the final FP64 step.
+            if ((rc = set_rowset(sel_, mask)))
+                return rc;
+            seg_copy_kernel<T><<<grid(sel_.total), 256, 0, st_>>>(X, b, N, sel_.view(), d_row0_, Xfinal),
+                ::pyci_gpu::note_launch();
+            if ((rc = set_active(active)))
+                return rc;
+        }
         if (nactive == 0)
             break;
-        // Thick restart (all problems together) when the next block does not fit.
-        if (m + b > mmax) {
-            if ((rc = combine<T, T, T>(V, m, Yk, nkeep, 0.0, Xk)) || (rc = combine<T, T, T>(W, m, Yk, nkeep, 0.0, Wk)))
-                return rc;
-            PYCI_CUDA_TRY(cudaMemcpyAsync(V, Xk, sizeof(T) * nkeep * N, cudaMemcpyDeviceToDevice, st_));
-            PYCI_CUDA_TRY(cudaMemcpyAsync(W, Wk, sizeof(T) * nkeep * N, cudaMemcpyDeviceToDevice, st_));
-            for (int p = 0; p < P; ++p) {
-                std::fill(G[p].begin(), G[p].end(), 0.0);
-                std::fill(valid[p].begin(), valid[p].end(), 0);
-                if (!active[p])
-                    continue;
-                // Ritz values of the kept vectors (recomputed from the last RR).
-                const int kept = std::min(nkeep, nvalid[p]);
-                std::vector<int> idx;
-                for (int i = 0; i < m; ++i)
-                    idx.push_back(i);
-                for (int j = 0; j < kept; ++j) {
-                    valid[p][j] = 1;
-                }
+        // Thick restart of the problems whose next block would not fit.
+        std::vector<int> rmask(P, 0);
+        bool any_restart = false;
+        for (int p = 0; p < P; ++p)
+            if (active[p] && m[p] + b > mmax) {
+                rmask[p] = 1;
+                any_restart = true;
             }
-            // Projected matrix of the kept Ritz vectors: diagonal of their Ritz values.
+        if (any_restart) {
+            if ((rc = set_rowset(sel_, rmask)) || (rc = combine<T, T, T>(V, mrr, Yk, nkeep, 0.0, Xk, sel_, d_len_)) ||
+                (rc = combine<T, T, T>(W, mrr, Yk, nkeep, 0.0, Wk, sel_, d_len_)))
+                return rc;
+            seg_copy_kernel<T><<<grid(sel_.total), 256, 0, st_>>>(Xk, nkeep, N, sel_.view(), d_row0_, V),
+                ::pyci_gpu::note_launch();
+            seg_copy_kernel<T><<<grid(sel_.total), 256, 0, st_>>>(Wk, nkeep, N, sel_.view(), d_row0_, W),
+                ::pyci_gpu::note_launch();
+            // Projected matrix of the kept Ritz vectors, recomputed.
             if ((rc = gram<T>(V, nkeep, W, nkeep, Gc)))
                 return rc;
-            for (int p = 0; p < P; ++p)
-                for (int i = 0; i < nkeep; ++i)
-                    for (int j = 0; j < nkeep; ++j)
-                        G[p][static_cast<size_t>(i) * mmax + j] = valid[p][i] && valid[p][j]
-                                                                      ? Gc[(static_cast<size_t>(p) * nkeep + i) * nkeep + j]
-                                                                      : 0.0;
-            m = nkeep;
-        }
-        // Corrections of unconverged roots of active problems into Tnew_.
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_use_, use.data(), sizeof(int) * P * b, cudaMemcpyHostToDevice, st_));
-        seg_precondition_kernel<T><<<grid(N), 256, 0, st_>>>(R, d_theta_, d_use_, d_diag_, b, N, d_row0_, P, Tnew_),
-            ::pyci_gpu::note_launch();
-        // Two passes of segmented block Gram-Schmidt against the basis.
-        for (int pass = 0; pass < 2; ++pass) {
-            if ((rc = gram<T>(V, m, Tnew_, b, Gc)))
-                return rc;
-            std::vector<double> C(static_cast<size_t>(P) * m * b, 0.0);
-            for (int p = 0; p < P; ++p)
-                for (int i = 0; i < m; ++i)
-                    if (valid[p][i])
-                        for (int j = 0; j < b; ++j)
-                            C[(static_cast<size_t>(p) * m + i) * b + j] = -Gc[(static_cast<size_t>(p) * m + i) * b + j];
-            if ((rc = combine<T, T, T>(V, m, C, b, 1.0, Tnew_)))
-                return rc;
-        }
-        // Cholesky QR (twice) inside each problem's block, dropping dependent vectors.
-        for (int pass = 0; pass < 2; ++pass) {
-            if ((rc = gram<T>(Tnew_, b, Tnew_, b, Gc)))
-                return rc;
-            std::vector<double> Y(static_cast<size_t>(P) * b * b, 0.0);
             for (int p = 0; p < P; ++p) {
-                const double *S = &Gc[static_cast<size_t>(p) * b * b];
-                std::vector<double> L(static_cast<size_t>(b) * b, 0.0);
-                std::vector<char> keep(b, 0);
-                for (int j = 0; j < b; ++j) {
-                    if (!use[p * b + j])
-                        continue;
-                    double d = S[j * b + j];
-                    for (int t = 0; t < j; ++t)
-                        d -= L[j * b + t] * L[j * b + t];
-                    if (!(d > (mixed_ ? 1e-6 : 1e-14) * S[j * b + j]) || !(d > 0.0)) {
-                        use[p * b + j] = 0; // dependent: drop
-                        continue;
-                    }
-                    keep[j] = 1;
-                    L[j * b + j] = std::sqrt(d);
-                    for (int i = j + 1; i < b; ++i) {
-                        double x = S[i * b + j];
-                        for (int t = 0; t < j; ++t)
-                            x -= L[i * b + t] * L[j * b + t];
-                        L[i * b + j] = x / L[j * b + j];
-                    }
-                }
-                // Inverse of the kept lower-triangular factor.
-                std::vector<double> Li(static_cast<size_t>(b) * b, 0.0);
-                for (int j = 0; j < b; ++j) {
-                    if (!keep[j])
-                        continue;
-                    Li[j * b + j] = 1.0 / L[j * b + j];
-                    for (int i = j + 1; i < b; ++i) {
-                        if (!keep[i])
-                            continue;
-                        double x = 0.0;
-                        for (int t = j; t < i; ++t)
-                            if (keep[t])
-                                x -= L[i * b + t] * Li[t * b + j];
-                        Li[i * b + j] = x / L[i * b + i];
-                    }
-                }
-                for (int i = 0; i < b; ++i)
-                    for (int j = 0; j < b; ++j)
-                        Y[(static_cast<size_t>(p) * b + i) * b + j] = Li[j * b + i];
+                if (!rmask[p])
+                    continue;
+                ++restarts;
+                const int kept = std::min(nkeep, m[p]);
+                std::fill(G[p].begin(), G[p].end(), 0.0);
+                for (int i = 0; i < kept; ++i)
+                    for (int j = 0; j < kept; ++j)
+                        G[p][static_cast<size_t>(i) * mmax + j] = Gc[(static_cast<size_t>(p) * nkeep + i) * nkeep + j];
+                m[p] = kept;
             }
-            if ((rc = combine<T, T, T>(Tnew_, b, Y, b, 0.0, Xk)))
-                return rc;
-            PYCI_CUDA_TRY(cudaMemcpyAsync(Tnew_, Xk, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
         }
+        // Corrections of the lowest unconverged roots (at most b per active
+        // problem) into Tnew_.
+        std::vector<int> sel(static_cast<size_t>(P) * b, -1);
+        for (int p = 0; p < P; ++p) {
+            int c = 0;
+            if (active[p])
+                for (int j = 0; j < nt && c < b; ++j)
+                    if (!conv[p * nt + j])
+                        sel[p * b + c++] = j;
+            for (int cc = 0; cc < b; ++cc)
+                use[p * b + cc] = (sel[p * b + cc] >= 0) ? 1 : 0;
+        }
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_sel_, sel.data(), sizeof(int) * P * b, cudaMemcpyHostToDevice, st_));
+        seg_precondition_kernel<T><<<grid(act_.total), 256, 0, st_>>>(R, d_theta_, nt, d_sel_, d_diag_, b, N,
+                                                                       act_.view(), d_row0_, Tnew_),
+            ::pyci_gpu::note_launch();
+        // Two passes of segmented block Gram-Schmidt against each basis.
+        int mgs = 0;
+        for (int p = 0; p < P; ++p)
+            if (active[p])
+                mgs = std::max(mgs, m[p]);
+        if ((rc = upload_ints(d_len_, m)))
+            return rc;
+        for (int pass = 0; pass < 2; ++pass) {
+            if ((rc = gram<T>(V, mgs, Tnew_, b, Gc, d_len_)))
+                return rc;
+            std::vector<double> C(static_cast<size_t>(P) * mgs * b, 0.0);
+            for (int p = 0; p < P; ++p)
+                if (active[p])
+                    for (int i = 0; i < m[p]; ++i)
+                        for (int j = 0; j < b; ++j)
+                            C[(static_cast<size_t>(p) * mgs + i) * b + j] = -Gc[(static_cast<size_t>(p) * mgs + i) * b + j];
+            if ((rc = combine<T, T, T>(V, mgs, C, b, 1.0, Tnew_, act_, d_len_)))
+                return rc;
+        }
+        // Orthonormalise inside each block into the next slots.
+        if ((rc = upload_ints(d_base_, m)) || (rc = cholqr_block(use, Xk, V, knew)))
+            return rc;
     }
     if (nactive > 0) {
         set_error("did not converge (%d of %d problems)", nactive, P);
         return PYCI_GPU_ENOCONV;
     }
     // Final Rayleigh-Ritz of every problem's Ritz block against the FP64
-    // operator (high + low in mixed mode).
-    double *X64, *AX64, *Xi64, *Yi64;
+    // operator (high + low in mixed mode), with FP64 residual norms.
+    std::fill(active.begin(), active.end(), 1);
+    if ((rc = set_active(active)))
+        return rc;
+    double *X64, *AX64, *E64, *AE64, *R64, *Xi64, *Yi64;
     if ((rc = alloc(&X64, static_cast<int64_t>(b) * N)) || (rc = alloc(&AX64, static_cast<int64_t>(b) * N)) ||
-        (rc = alloc(&Xi64, N * 4)) || (rc = alloc(&Yi64, N * 4)))
+        (rc = alloc(&E64, static_cast<int64_t>(b) * N)) || (rc = alloc(&AE64, static_cast<int64_t>(b) * N)) ||
+        (rc = alloc(&R64, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi64, N * 4)) || (rc = alloc(&Yi64, N * 4)))
         return rc;
     batch_convert_kernel<T, double><<<grid(static_cast<int64_t>(b) * N), 256, 0, st_>>>(Xfinal, X64, static_cast<int64_t>(b) * N),
         ::pyci_gpu::note_launch();
-    std::fill(active.begin(), active.end(), 1);
-    PYCI_CUDA_TRY(cudaMemcpyAsync(d_active_, active.data(), sizeof(int) * P, cudaMemcpyHostToDevice, st_));
     {
+        const RowSet rs = act_.view();
         const unsigned gr = grid(N);
-        batch_pack_kernel<double, 4><<<gr, 256, 0, st_>>>(X64, N, b, Xi64), ::pyci_gpu::note_launch();
+        batch_pack_kernel<double, 4><<<gr, 256, 0, st_>>>(X64, N, d_zero_, rs, d_row0_, Xi64), ::pyci_gpu::note_launch();
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ctx_->num_sms * 32, (N * 32 + 255) / 256));
-        bool split = !all_vals_;
-        if (mixed_)
-            split = true;
-        if (split)
-            batch_spmm_kernel<2, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, d_row0_, P, N, d_active_, Xi64, Yi64),
+        if (mixed_ || !all_vals_)
+            batch_spmm_kernel<2, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi64, Yi64),
                 ::pyci_gpu::note_launch();
         else
-            batch_spmm_kernel<0, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, d_row0_, P, N, d_active_, Xi64, Yi64),
+            batch_spmm_kernel<0, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi64, Yi64),
                 ::pyci_gpu::note_launch();
-        batch_unpack_kernel<double, 4><<<gr, 256, 0, st_>>>(Yi64, N, b, AX64), ::pyci_gpu::note_launch();
+        batch_unpack_kernel<double, 4><<<gr, 256, 0, st_>>>(Yi64, N, d_zero_, rs, d_row0_, AX64, nullptr),
+            ::pyci_gpu::note_launch();
         matvecs_ += static_cast<int64_t>(P) * b;
     }
     std::vector<double> S64, H64;
     if ((rc = gram<double>(X64, b, X64, b, S64)) || (rc = gram<double>(X64, b, AX64, b, H64)))
         return rc;
+    // Coefficients of the FP64 eigenvectors in the Ritz block, per problem,
+    // in decreasing order of eigenvalue (the reference's result order).
+    std::vector<double> C(static_cast<size_t>(P) * b * b, 0.0), eord(static_cast<size_t>(P) * b, 0.0);
     for (int p = 0; p < P; ++p) {
         // Generalised b x b problem H y = e S y via S^{-1/2}.
         const int n = static_cast<int>(std::min<int64_t>(b, ops_[p]->nrow));
@@ -749,7 +1021,7 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         for (int i = 0; i < n; ++i)
             for (int j = 0; j < n; ++j) {
                 S[i * n + j] = S64[(static_cast<size_t>(p) * b + i) * b + j];
-                H[i * n + j] = H64[(static_cast<size_t>(p) * b + i) * b + j];
+                H[i * n + j] = 0.5 * (H64[(static_cast<size_t>(p) * b + i) * b + j] + H64[(static_cast<size_t>(p) * b + j) * b + i]);
             }
         symmetric_eigen(n, S, se, sv);
         std::vector<double> Sm(static_cast<size_t>(n) * n, 0.0); // S^{-1/2}
@@ -767,20 +1039,57 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
                 for (int t = 0; t < n; ++t)
                     A[i * n + j] += tmp[i * n + t] * Sm[t * n + j];
         symmetric_eigen(n, A, e, v);
-        // Decreasing order, ecore added (the reference's result order).
+        for (int c = 0; c < n; ++c) {
+            const int src = n - 1 - c;
+            eord[static_cast<size_t>(p) * b + c] = e[src];
+            // y = S^{-1/2} v[:, src]
+            for (int i = 0; i < n; ++i) {
+                double y = 0.0;
+                for (int t = 0; t < n; ++t)
+                    y += Sm[i * n + t] * v[t * n + src];
+                C[(static_cast<size_t>(p) * b + i) * b + c] = y;
+            }
+        }
         for (int c = 0; c < b; ++c)
-            evals[static_cast<size_t>(p) * b + c] = (c < n) ? e[n - 1 - c] + ecore[p] : 0.0;
+            evals[static_cast<size_t>(p) * b + c] = (c < n) ? eord[static_cast<size_t>(p) * b + c] + ecore[p] : 0.0;
+    }
+    // Eigenvectors E = X C and residuals H E - e E in FP64.
+    if ((rc = combine<double, double, double>(X64, b, C, b, 0.0, E64, act_)) ||
+        (rc = combine<double, double, double>(AX64, b, C, b, 0.0, AE64, act_)))
+        return rc;
+    PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, eord.data(), sizeof(double) * P * b, cudaMemcpyHostToDevice, st_));
+    seg_residual_kernel<double><<<grid(N), 256, 0, st_>>>(AE64, E64, d_theta_, b, N, act_.view(), d_row0_, R64),
+        ::pyci_gpu::note_launch();
+    std::vector<double> RR;
+    if ((rc = gram<double>(R64, b, R64, b, RR)))
+        return rc;
+    double max_res = 0.0;
+    for (int p = 0; p < P; ++p)
+        for (int j = 0; j < std::min<int64_t>(b, ops_[p]->nrow); ++j)
+            max_res = std::max(max_res, std::sqrt(std::max(RR[(static_cast<size_t>(p) * b + j) * b + j], 0.0)));
+    if (evecs) {
+        for (int p = 0; p < P; ++p) {
+            if (!evecs[p])
+                continue;
+            for (int c = 0; c < b; ++c)
+                PYCI_CUDA_TRY(cudaMemcpyAsync(evecs[p] + static_cast<int64_t>(c) * ops_[p]->nrow,
+                                              E64 + static_cast<int64_t>(c) * N + row0_[p],
+                                              sizeof(double) * ops_[p]->nrow, cudaMemcpyDeviceToHost, st_));
+        }
     }
     PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+    if (iterations)
+        for (int p = 0; p < P; ++p)
+            iterations[p] = conv_iter[p];
     if (stats) {
         stats->iterations = iter + 1;
         stats->matvecs = matvecs_;
         stats->matvecs_fp64 = mixed_ ? static_cast<int64_t>(P) * b : matvecs_;
-        stats->restarts = 0;
+        stats->restarts = restarts;
         stats->refinements = 1;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         stats->seconds_spmm = spmm_ms_ * 1e-3;
-        stats->max_residual = 0.0;
+        stats->max_residual = max_res;
     }
     return PYCI_GPU_OK;
 }
@@ -789,7 +1098,7 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
 
 extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_csr *const *ops, int64_t n,
                                     int64_t maxiter, double tol, const double *ecore, int mode, double *evals,
-                                    pyci_gpu_solve_stats *stats) {
+                                    double *const *evecs, int64_t *iterations, pyci_gpu_solve_stats *stats) {
     if (!ctx || !ops || !ecore || !evals || nprob <= 0) {
         set_error("NULL argument or empty batch");
         return PYCI_GPU_EINVAL;
@@ -823,7 +1132,7 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
                 return rc;
         }
         Batch<float> bsolve(ctx, v, static_cast<int>(n), mmax, true);
-        return bsolve.run(iters, tol, ecore, evals, stats);
+        return bsolve.run(iters, tol, ecore, evals, evecs, iterations, stats);
     }
     for (auto *c : v)
         if (!c->vals && !(c->hi && c->lo)) {
@@ -831,5 +1140,5 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
             return PYCI_GPU_EINVAL;
         }
     Batch<double> bsolve(ctx, v, static_cast<int>(n), mmax, false);
-    return bsolve.run(iters, tol, ecore, evals, stats);
+    return bsolve.run(iters, tol, ecore, evals, evecs, iterations, stats);
 }

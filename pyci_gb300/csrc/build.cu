@@ -587,6 +587,235 @@ __global__ void __launch_bounds__(256) fill_kernel(BuildParams p, int64_t row0, 
         p.lower_len[row] = 0;
 }
 
+// Exc of a given kind and within-kind index (inverse of decode's layout).
+__device__ __forceinline__ Exc make_exc(const RowState &s, int type, int i1, int i2) {
+    Exc e{};
+    e.type = type;
+    const int qa = s.nv_a * (s.nv_a - 1) / 2, qb = s.nv_b * (s.nv_b - 1) / 2;
+    int i, k, x, y;
+    switch (type) {
+    case kSingleA:
+        e.sa_idx = i1;
+        e.ii = s.occ_a[i1 / s.nv_a];
+        e.jj = s.vir_a[i1 % s.nv_a];
+        break;
+    case kSingleB:
+        e.sb_idx = i1;
+        e.ii = s.occ_b[i1 / s.nv_b];
+        e.jj = s.vir_b[i1 % s.nv_b];
+        break;
+    case kDoubleAA:
+        e.q = i1;
+        decode_pair(i1 / qa, i, k);
+        decode_pair(i1 % qa, x, y);
+        e.ii = s.occ_a[i];
+        e.kk = s.occ_a[k];
+        e.jj = s.vir_a[x];
+        e.ll = s.vir_a[y];
+        break;
+    case kDoubleBB:
+        e.q = i1;
+        decode_pair(i1 / qb, i, k);
+        decode_pair(i1 % qb, x, y);
+        e.ii = s.occ_b[i];
+        e.kk = s.occ_b[k];
+        e.jj = s.vir_b[x];
+        e.ll = s.vir_b[y];
+        break;
+    default: // kDoubleAB
+        e.sa_idx = i1;
+        e.sb_idx = i2;
+        e.ii = s.occ_a[i1 / s.nv_a];
+        e.jj = s.vir_a[i1 % s.nv_a];
+        e.kk = s.occ_b[i2 / s.nv_b];
+        e.ll = s.vir_b[i2 % s.nv_b];
+        break;
+    }
+    return e;
+}
+
+// Exclusive prefix sum of v[0..n) in shared memory (n <= blockDim.x * 2).
+__device__ void block_exclusive_scan(int *v, int *tmp, int n) {
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+        tmp[t] = v[t];
+    __syncthreads();
+    for (int off = 1; off < n; off <<= 1) {
+        int a[2] = {0, 0};
+        int c = 0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x, ++c)
+            a[c] = (t >= off) ? tmp[t - off] : 0;
+        __syncthreads();
+        c = 0;
+        for (int t = threadIdx.x; t < n; t += blockDim.x, ++c)
+            tmp[t] += a[c];
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x)
+        v[t] = tmp[t] - v[t];
+    __syncthreads();
+}
+
+// Bitonic sort of n (power of two) int keys with int payloads.
+__device__ void block_sort_pairs(int *key, int *val, int n) {
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = ((lo & size) == 0);
+                const int klo = key[lo], khi = key[hi];
+                if ((klo > khi) == up) {
+                    key[lo] = khi;
+                    key[hi] = klo;
+                    const int v = val[lo];
+                    val[lo] = val[hi];
+                    val[hi] = v;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+constexpr int kSortedMax = 512; // max alpha (or beta) excitations + 1 per row for the sorted fill
+
+// Full-space FullCI row written directly in ascending column order.
+//
+// Columns are rank(a') * nbeta + rank(b'), so a row is the concatenation,
+// over the row's alpha excitations a' = {a} + singles + doubles sorted by
+// rank, of its beta partners sorted by rank: all of {b} + singles + doubles
+// for a' = a, {b} + singles for a single, {b} for a double.  Sorting the two
+// short excitation lists and a prefix sum over the alpha list place every
+// entry; no row-length sort is needed.  Only for builds that keep every
+// candidate (fresh full space, nrow = ncol = ndet).
+template<int NW>
+__global__ void __launch_bounds__(256) fill_fci_sorted_kernel(BuildParams p, int64_t row0) {
+    __shared__ RowState s;
+    __shared__ int akey[kSortedMax], aval[kSortedMax], bkey[kSortedMax], bval[kSortedMax];
+    __shared__ int b1key[kSortedMax], b1val[kSortedMax], off[kSortedMax], tmp[kSortedMax], flag[kSortedMax];
+    __shared__ double dval;
+    __shared__ int apos, bpos, nb1;
+    extern __shared__ __align__(16) unsigned char dyn[];
+    const int64_t row = row0 + blockIdx.x;
+    if (row >= p.nrow)
+        return;
+    const RowScratch sc = setup_scratch(p, dyn);
+    load_row<NW>(p, row, s);
+    fill_rank_cache<NW>(p, s, sc.binom, sc.cache);
+    const int sa = s.no_a * s.nv_a, sb = s.no_b * s.nv_b;
+    const int da = (s.no_a * (s.no_a - 1) / 2) * (s.nv_a * (s.nv_a - 1) / 2);
+    const int db = (s.no_b * (s.no_b - 1) / 2) * (s.nv_b * (s.nv_b - 1) / 2);
+    const int na = 1 + sa + da, nbb = 1 + sb + db;
+    int npad = 2;
+    while (npad < na || npad < nbb)
+        npad <<= 1;
+    const int64_t ra = row / p.nbeta, rb = row % p.nbeta;
+    __syncthreads();
+    // Excitation lists: payload = type * 2^20 + index (type 0 = the row's own string).
+    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+        if (t < na) {
+            akey[t] = (t == 0) ? static_cast<int>(ra) : (t <= sa ? sc.cache[t - 1] : sc.cache[sa + sb + (t - 1 - sa)]);
+            aval[t] = (t == 0) ? 0 : (t <= sa ? ((1 << 20) | (t - 1)) : ((2 << 20) | (t - 1 - sa)));
+        } else {
+            akey[t] = INT32_MAX;
+            aval[t] = 0;
+        }
+        if (t < nbb) {
+            bkey[t] = (t == 0) ? static_cast<int>(rb) : (t <= sb ? sc.cache[sa + t - 1] : sc.cache[sa + sb + da + (t - 1 - sb)]);
+            bval[t] = (t == 0) ? 0 : (t <= sb ? ((1 << 20) | (t - 1)) : ((2 << 20) | (t - 1 - sb)));
+        } else {
+            bkey[t] = INT32_MAX;
+            bval[t] = 0;
+        }
+    }
+    if (threadIdx.x == 0)
+        dval = diagonal(p, s);
+    __syncthreads();
+    block_sort_pairs(akey, aval, npad);
+    block_sort_pairs(bkey, bval, npad);
+    // Beta partners of an alpha single: {b} + singles, in sorted order.
+    for (int t = threadIdx.x; t < npad; t += blockDim.x)
+        flag[t] = (t < nbb && (bval[t] >> 20) <= 1) ? 1 : 0;
+    __syncthreads();
+    block_exclusive_scan(flag, tmp, npad);
+    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+        if (t < nbb && (bval[t] >> 20) <= 1) {
+            b1key[flag[t]] = bkey[t];
+            b1val[flag[t]] = bval[t];
+        }
+        if (t < nbb && bval[t] == 0)
+            bpos = t;
+        if (t < na && aval[t] == 0)
+            apos = t;
+    }
+    if (threadIdx.x == 0)
+        nb1 = 1 + sb;
+    // Group lengths along the sorted alpha list, then offsets.
+    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+        const int ty = aval[t] >> 20;
+        off[t] = (t < na) ? (ty == 0 ? nbb : (ty == 1 ? 1 + sb : 1)) : 0;
+    }
+    __syncthreads();
+    block_exclusive_scan(off, tmp, npad);
+    const int64_t start = p.rowptr[row];
+    const int len = static_cast<int>(p.rowptr[row + 1] - start);
+    if (threadIdx.x == 0) {
+        const int total = off[na - 1] + ((aval[na - 1] >> 20) == 0 ? nbb : ((aval[na - 1] >> 20) == 1 ? nb1 : 1));
+        if (total != len)
+            atomicExch(p.error, 4);
+        const int dpos = off[apos] + bpos;
+        if (p.lower_len)
+            p.lower_len[row] = dpos + 1;
+        p.diag[row] = dval;
+    }
+    for (int t = threadIdx.x; t < len; t += blockDim.x) {
+        // Group g: the last alpha position with off[g] <= t.
+        int lo = 0, hi = na - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int g = lo, qpos = t - off[g];
+        const int tya = aval[g] >> 20, ia = aval[g] & ((1 << 20) - 1);
+        int bk, bv;
+        if (tya == 0) {
+            bk = bkey[qpos];
+            bv = bval[qpos];
+        } else if (tya == 1) {
+            bk = b1key[qpos];
+            bv = b1val[qpos];
+        } else {
+            bk = static_cast<int>(rb);
+            bv = 0;
+        }
+        const int tyb = bv >> 20, ib = bv & ((1 << 20) - 1);
+        const int64_t col = static_cast<int64_t>(akey[g]) * p.nbeta + bk;
+        double val;
+        if (tya == 0 && tyb == 0) {
+            val = dval;
+        } else {
+            int type, i1 = 0, i2 = 0;
+            if (tya == 0) {
+                type = (tyb == 1) ? kSingleB : kDoubleBB;
+                i1 = ib;
+            } else if (tya == 1) {
+                type = (tyb == 0) ? kSingleA : kDoubleAB;
+                i1 = ia;
+                i2 = ib;
+            } else {
+                type = kDoubleAA;
+                i1 = ia;
+            }
+            val = exc_value<NW>(p, s, make_exc(s, type, i1, i2));
+        }
+        p.cols[start + t] = static_cast<int32_t>(col);
+        p.vals[start + t] = val;
+    }
+}
+
 // Insert every determinant index into the table (linear probing).
 template<int NWT>
 __global__ void table_insert_kernel(int32_t *slots, uint64_t mask, const uint64_t *dets,
@@ -922,7 +1151,8 @@ int pick_nw(int64_t nbasis) {
 }
 
 template<int NW>
-int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len) {
+int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len,
+              bool sorted_fci) {
     cudaStream_t st = ctx->stream;
     const int64_t chunk = 1 << 20; // rows per launch (grid.x limit is generous; keeps launches short)
     // Shared-memory scratch: rank cache + binomial table (see setup_scratch).
@@ -958,6 +1188,14 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
     p.vals = csr->vals;
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
+    if (sorted_fci) {
+        for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
+            const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
+            fill_fci_sorted_kernel<NW><<<static_cast<unsigned>(nb), 256, scratch, st>>>(p, r0), ::pyci_gpu::note_launch();
+        }
+        PYCI_CUDA_TRY(cudaGetLastError());
+        return PYCI_GPU_OK;
+    }
     const size_t smem = static_cast<size_t>(cap) * (sizeof(double) + sizeof(int32_t)) + scratch;
     if (smem > 48 * 1024) {
         if (smem > ctx->smem_optin) {
@@ -1215,10 +1453,14 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
     } else {
         const bool uniform = colex && legacy_nrow == 0 && csr->nrow == csr->ndet && csr->ncol == csr->ndet;
         const int64_t ulen = uniform ? ncand + 1 : 0;
+        const int64_t na = 1 + no_a * nv_a + (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
+        const int64_t nbb = 1 + no_b * nv_b + (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
+        const bool sorted_fci = uniform && kind == PYCI_WFN_FULLCI && p.ncache > 0 && na <= kSortedMax &&
+                                nbb <= kSortedMax && !(csr->flags & PYCI_BUILD_FORCE_HASH);
         switch (nw) {
-        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen); break;
-        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen); break;
-        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap), ulen); break;
+        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
+        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
+        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
         }
     }
     if (rc)

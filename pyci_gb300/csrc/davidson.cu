@@ -36,7 +36,6 @@
 
 namespace pyci_gpu {
 
-constexpr int kGramTile = 32;
 constexpr int kMaxGramP = 128;
 constexpr int kMaxQ = 8;
 
@@ -61,43 +60,86 @@ __global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, int kp
 // Width the SpMM reads with 8/16-byte vector gathers: 3 -> 4, 5..7 -> 8.
 inline int padded_width(int k) { return k == 3 ? 4 : (k > 4 && k < 8 ? 8 : k); }
 
-// Partial Gram products: partial[block][i * q + j] = sum over the block's rows
-// of A[i][r] * B[j][r], for p <= kMaxGramP, q <= kMaxQ.  Rows are staged in
-// shared memory tiles of kGramTile; each tile's products are summed in the
-// storage type and added to an FP64 accumulator.
-template<typename T>
-__global__ void __launch_bounds__(256) gram_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
-                                                   int q, int64_t N, double *__restrict__ partial) {
-    __shared__ T sa[kMaxGramP][kGramTile + 1];
-    __shared__ T sb[kMaxQ][kGramTile + 1];
-    const int pq = p * q;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const int64_t ntiles = (N + kGramTile - 1) / kGramTile;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const int64_t r0 = t * kGramTile;
-        for (int e = threadIdx.x; e < p * kGramTile; e += blockDim.x) {
-            const int i = e / kGramTile, c = e % kGramTile;
-            sa[i][c] = (r0 + c < N) ? A[i * N + r0 + c] : T(0);
+// Vectors per SpMM launch in the eigensolver: blocks wider than 4 run as
+// several products of at most 4 (a 5-vector block as 4 + 1 instead of one
+// product padded to 8), since the gather-bound product costs about as much
+// per gathered byte at any width.
+constexpr int kSpmmChunk = 4;
+
+// Row-streaming Gram product: block (x, y) sums A[i][r] * B[j][r] over a
+// grid-stride set of rows for i in [y * PI, y * PI + PI), j < q <= QC, with
+// a per-thread PI x QC register tile (one coalesced pass over the rows), then
+// reduces across the block; partial[x][i * q + j].  QC is the smallest of
+// 1, 2, 4, 8 that holds q, so the tile (and the register count) follows q.
+template<typename T, int PI, int QC>
+__global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
+                                                        int q, int64_t N, double *__restrict__ partial) {
+    const int i0 = blockIdx.y * PI;
+    const int ni = min(PI, p - i0);
+    T acc[PI][QC];
+#pragma unroll
+    for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            acc[ii][j] = T(0);
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        T bv[QC];
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            bv[j] = (j < q) ? B[j * N + r] : T(0);
+#pragma unroll
+        for (int ii = 0; ii < PI; ++ii) {
+            if (ii < ni) {
+                const T a = A[(i0 + ii) * N + r];
+#pragma unroll
+                for (int j = 0; j < QC; ++j)
+                    acc[ii][j] += a * bv[j];
+            }
         }
-        for (int e = threadIdx.x; e < q * kGramTile; e += blockDim.x) {
-            const int j = e / kGramTile, c = e % kGramTile;
-            sb[j][c] = (r0 + c < N) ? B[j * N + r0 + c] : T(0);
-        }
-        __syncthreads();
-        int slot = 0;
-        for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot) {
-            const int i = idx / q, j = idx % q;
-            T s = 0;
-#pragma unroll 8
-            for (int c = 0; c < kGramTile; ++c)
-                s += sa[i][c] * sb[j][c];
-            acc[slot] += static_cast<double>(s);
-        }
-        __syncthreads();
     }
-    int slot = 0;
-    for (int idx = threadIdx.x; idx < pq; idx += blockDim.x, ++slot)
-        partial[static_cast<int64_t>(blockIdx.x) * pq + idx] = acc[slot];
+    __shared__ double red[8][PI * QC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+        for (int j = 0; j < QC; ++j) {
+            double v = static_cast<double>(acc[ii][j]);
+            for (int o = 16; o > 0; o >>= 1)
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0)
+                red[warp][ii * QC + j] = v;
+        }
+    __syncthreads();
+    const int nwarps = blockDim.x >> 5;
+    for (int idx = threadIdx.x; idx < ni * q; idx += blockDim.x) {
+        const int ii = idx / q, j = idx % q;
+        double v = 0.0;
+        for (int w = 0; w < nwarps; ++w)
+            v += red[w][ii * QC + j];
+        partial[static_cast<int64_t>(blockIdx.x) * p * q + (i0 + ii) * q + j] = v;
+    }
+}
+
+// Launch gram_rows_kernel with the register tile that fits q (<= 8): rows
+// of A per block PI = 8 (4 when q > 4).  budget: blocks to aim for.  Returns
+// the number of partial sums per entry (blocks along x).
+template<typename T>
+unsigned launch_gram_rows(unsigned budget, cudaStream_t st, const T *A, int p, const T *B, int q, int64_t N,
+                          double *partial) {
+    const int pi = (q <= 4) ? 8 : 4;
+    const unsigned gy = static_cast<unsigned>((p + pi - 1) / pi);
+    const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(budget / gy, (N + 255) / 256)));
+    const dim3 g(nb, gy);
+    if (q <= 1)
+        gram_rows_kernel<T, 8, 1><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
+    else if (q <= 2)
+        gram_rows_kernel<T, 8, 2><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
+    else if (q <= 4)
+        gram_rows_kernel<T, 8, 4><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
+    else
+        gram_rows_kernel<T, 4, 8><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
+    return nb;
 }
 
 __global__ void reduce_partials_kernel(const double *__restrict__ partial, int nblocks, int pq,
@@ -203,6 +245,14 @@ __global__ void unit_kernel(T *V, int64_t N, const int64_t *idx, int k) {
             V[j * N + r] = (r == idx[j]) ? T(1) : T(0);
 }
 
+// v = e_idx + amp * noise(., col): one perturbed start vector.
+template<typename T>
+__global__ void guess_kernel(T *v, int64_t N, int64_t idx, double amp, int col) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        v[r] = static_cast<T>((r == idx ? 1.0 : 0.0) + amp * guess_noise(static_cast<uint64_t>(r), static_cast<uint64_t>(col)));
+}
+
 // ------------------------------------------------------------------------
 
 struct Timer {
@@ -257,9 +307,9 @@ private:
             const int pp = std::min(kMaxGramP, p - i0);
             for (int j0 = 0; j0 < q; j0 += kMaxQ) {
                 const int qq = std::min(kMaxQ, q - j0);
-                const unsigned nb = std::min<unsigned>(gram_blocks_, static_cast<unsigned>((N_ + kGramTile - 1) / kGramTile));
-                gram_kernel<U><<<nb, 256, 0, st_>>>(A + static_cast<int64_t>(i0) * N_, pp,
-                                                     B + static_cast<int64_t>(j0) * N_, qq, N_, d_partial_), ::pyci_gpu::note_launch();
+                const unsigned nb = launch_gram_rows<U>(gram_blocks_, st_, A + static_cast<int64_t>(i0) * N_, pp,
+                                                        B + static_cast<int64_t>(j0) * N_, qq, N_, d_partial_);
+                ::pyci_gpu::note_launch();
                 reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq, d_small_), ::pyci_gpu::note_launch();
                 std::vector<double> tmp(static_cast<size_t>(pp) * qq);
                 cudaError_t e = cudaMemcpyAsync(tmp.data(), d_small_, sizeof(double) * pp * qq,
@@ -303,8 +353,8 @@ private:
 
     // W[0..k) = H V[0..k) (storage precision of T; FP64 uses f64 values).
     int apply(const T *V, int k, T *W, int prec) {
-        for (int j0 = 0; j0 < k; j0 += kMaxQ) {
-            const int kk = std::min(kMaxQ, k - j0);
+        for (int j0 = 0; j0 < k; j0 += kSpmmChunk) {
+            const int kk = std::min(kSpmmChunk, k - j0);
             const int kp = padded_width(kk);
             pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_), ::pyci_gpu::note_launch();
             cudaEventRecord(ev0_, st_);
@@ -501,15 +551,14 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         knew = static_cast<int>(N);
     } else {
         // Unit vectors on the lowest diagonal elements (after c0, if given),
-        // topped up until the block holds b independent vectors.
+        // each with a small seeded component in every row, topped up until
+        // the block holds b independent vectors.
         std::vector<int64_t> order(N);
         std::iota(order.begin(), order.end(), 0);
         const int64_t nsort = std::min<int64_t>(N, 2 * b + 8);
         std::partial_sort(order.begin(), order.begin() + nsort, order.end(),
                           [&](int64_t x, int64_t y) { return diag[x] < diag[y] || (diag[x] == diag[y] && x < y); });
-        int64_t *d_idx;
-        if ((rc = alloc(&d_idx, 1)))
-            return rc;
+        const double amp = kGuessNoise / std::sqrt(static_cast<double>(N));
         int64_t next = 0;
         if (c0) {
             std::vector<T> hc(N);
@@ -522,10 +571,10 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         }
         while (knew < b && next < N) {
             const int64_t pick = (next < nsort) ? order[next] : next;
+            guess_kernel<T><<<grid(N), 256, 0, st_>>>(V + static_cast<int64_t>(knew) * N, N, pick, amp,
+                                                        static_cast<int>(next)),
+                ::pyci_gpu::note_launch();
             ++next;
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_idx, &pick, sizeof(int64_t), cudaMemcpyHostToDevice, st_));
-            unit_kernel<T><<<grid(N), 256, 0, st_>>>(V + static_cast<int64_t>(knew) * N, N, d_idx, 1), ::pyci_gpu::note_launch();
-            PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
             int got = 0;
             if ((rc = orthonormalize(V, knew, 1, got)))
                 return rc;
@@ -596,6 +645,11 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 todo.push_back(j);
             }
         }
+        // Corrections for at most nw roots per iteration, lowest first: the
+        // guard Ritz pairs beyond nw steer the subspace without widening the
+        // SpMM.
+        if (static_cast<int>(todo.size()) > nw)
+            todo.resize(nw);
         if (all) {
             if (!mixed_) {
                 converged = true;
@@ -628,8 +682,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                     return rc;
                 scale_kernel<double><<<grid(N), 256, 0, st_>>>(xj, N, 1.0 / std::sqrt(Gc[0])), ::pyci_gpu::note_launch();
             }
-            for (int j0 = 0; j0 < b; j0 += kMaxQ) {
-                const int kk = std::min(kMaxQ, b - j0);
+            for (int j0 = 0; j0 < b; j0 += kSpmmChunk) {
+                const int kk = std::min(kSpmmChunk, b - j0);
                 const int kp = padded_width(kk);
                 pack_kernel<double><<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, Xi64), ::pyci_gpu::note_launch();
                 cudaEventRecord(ev0_, st_);
@@ -677,6 +731,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                     todo.push_back(j);
                 }
             }
+            if (static_cast<int>(todo.size()) > nw)
+                todo.resize(nw);
             if (ok64 || refinements >= 8) {
                 converged = ok64;
                 final_theta = th64;
@@ -785,13 +841,18 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
                    double tol, double ecore, int mode, double *evals, double *evecs,
                    pyci_gpu_solve_stats *stats) {
     const int64_t N = csr->nrow;
-    // Block size: the n wanted roots plus PYCI_GPU_DAVIDSON_EXTRA buffer vectors
-    // (default 0), never more than N - 1.
-    int64_t extra = 0;
+    // Ritz pairs tracked: the n wanted roots plus PYCI_GPU_DAVIDSON_EXTRA
+    // guard pairs (default 1), never more than N - 1.  Convergence is tested
+    // on the n wanted roots only, and each iteration adds corrections for at
+    // most n roots.  Without a guard pair, a root whose start-vector overlap
+    // is small can be passed over: the n tracked pairs converge to the roots
+    // above it (seen on random FullCI Hamiltonians with nearly degenerate
+    // 4th and 5th roots).
+    int64_t extra = 1;
     if (const char *env = std::getenv("PYCI_GPU_DAVIDSON_EXTRA"))
         extra = std::max<int64_t>(0, std::atol(env));
     const int64_t b = std::max<int64_t>(n, std::min<int64_t>(n + extra, N - 1));
-    int64_t mmax = (ncv > 0) ? ncv : std::max<int64_t>(8 * b, 24);
+    int64_t mmax = (ncv > 0) ? ncv : std::max<int64_t>(8 * n, 24);
     mmax = std::max<int64_t>(mmax, 2 * b + 2);
     if (N <= std::max<int64_t>(64, 3 * n) || N <= mmax)
         mmax = std::max<int64_t>(mmax, N); // full space: exact Rayleigh-Ritz

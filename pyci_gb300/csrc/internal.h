@@ -88,3 +88,21 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
                    pyci_gpu_solve_stats *stats);
 
 int64_t host_binomial(int64_t n, int64_t k);
+
+// Seeded perturbation of the Davidson start vectors.  Unit vectors on the
+// lowest diagonal elements can all lie in one symmetry sector of H (e.g.
+// symmetric under alpha <-> beta exchange), and the sector of a skipped root
+// is then fed only by the corrections of roots that happen to share it: once
+// those converge, the skipped root is never found.  A small deterministic
+// component in every row (relative norm kGuessNoise / sqrt(3)) gives every
+// sector a start, as the reference's random Lanczos start vector does.
+constexpr double kGuessNoise = 1e-3;
+
+// Uniform in [-1, 1) from (row, column) via the splitmix64 finaliser.
+__host__ __device__ inline double guess_noise(uint64_t row, uint64_t col) {
+    uint64_t z = row * 0x9E3779B97F4A7C15ull + (col + 1) * 0xD1B54A32D192ED03ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return static_cast<double>(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}

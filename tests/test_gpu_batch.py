@@ -25,30 +25,68 @@ def ctx():
     c.close()
 
 
-def build_all(ctx):
+def dense_lowest(kind, n, nu, nd, one, two, nroot=4):
+    r"""The oracle's lowest eigenvalues by dense diagonalisation (no start vector)."""
+    k = {capi.WFN_FULLCI: O.FULLCI, capi.WFN_DOCI: O.DOCI}[kind]
+    dets = O.all_dets(k, n, nu, nd)
+    data, indices, indptr = O.build_csr(k, n, nu, nd, dets, one, two)
+    return np.linalg.eigvalsh(O.full_matrix(data, indices, indptr).toarray())[:nroot]
+
+
+def build_all(ctx, problems=PROBLEMS, core=True):
     from math import comb
     ops, ecore, ref = [], [], []
-    for kind, n, nu, nd, seed in PROBLEMS:
+    for kind, n, nu, nd, seed in problems:
         e, one, two = synthetic_integrals(n, seed)
-        e = 0.25 * seed  # a nonzero core energy per problem
+        if core:
+            e = 0.25 * seed  # a nonzero core energy per problem
         nd_ = comb(n, nu) * (comb(n, nd) if kind == capi.WFN_FULLCI else 1)
         csr = capi.Csr(ctx, kind, n, nu, nd, None, one, two, flags=capi.BUILD_FULL_COLEX, ndet=nd_)
         ops.append(csr)
         ecore.append(e)
-        ref.append(csr.solve(n=4, tol=1e-10, ecore=e)[0])
+        ref.append(dense_lowest(kind, n, nu, nd, one, two)[::-1] + e)
     return ops, np.array(ecore), np.array(ref)
 
 
 @pytest.mark.parametrize("mode, atol", [(capi.SOLVE_FP64, 1e-8), (capi.SOLVE_MIXED, 1e-6)])
-def test_batch_matches_single_solves(ctx, mode, atol):
+def test_batch_matches_dense_spectrum(ctx, mode, atol):
     ops, ecore, ref = build_all(ctx)
-    evals, stats = capi.batch_solve(ctx, ops, ecore, n=4, tol=1e-9 if mode == capi.SOLVE_FP64 else 1e-6, mode=mode)
+    evals, vecs, stats = capi.batch_solve(ctx, ops, ecore, n=4, tol=1e-9 if mode == capi.SOLVE_FP64 else 1e-6,
+                                          mode=mode, evecs=True)
     assert evals.shape == (len(ops), 4)
     for p in range(len(ops)):
         assert np.all(np.diff(evals[p]) <= 0)  # decreasing, like the single solve
         np.testing.assert_allclose(evals[p], ref[p], rtol=0, atol=atol)
+        # eigenvectors: unit norm, H v = (e - ecore) v
+        v = vecs[p]
+        np.testing.assert_allclose(np.linalg.norm(v, axis=1), 1.0, atol=1e-9)
+        for c in range(4):
+            r = ops[p].matvec(v[c]) - (evals[p][c] - ecore[p]) * v[c]
+            assert np.linalg.norm(r) < 1e-4
     assert stats["matvecs"] > 0
+    assert stats["max_residual"] < 1e-4
+    its = stats["per_problem_iterations"]
+    assert len(its) == len(ops) and min(its) >= 1 and max(its) <= stats["iterations"]
     for c in ops:
+        c.free()
+
+
+# Problems whose 4 lowest roots include spin-flip-antisymmetric states that
+# unit start vectors on the lowest diagonal elements reach only through the
+# corrections of one root: without the seeded start perturbation, block
+# Davidson converged to a higher root instead (errors of 0.02-0.05 Ha).
+SECTOR_CASES = [(capi.WFN_FULLCI, 8, 4, 4, 5042), (capi.WFN_FULLCI, 8, 3, 3, 5043),
+                (capi.WFN_FULLCI, 8, 2, 2, 5057), (capi.WFN_FULLCI, 8, 2, 2, 5058)]
+
+
+@pytest.mark.parametrize("mode", [capi.SOLVE_FP64, capi.SOLVE_MIXED])
+def test_no_skipped_roots(ctx, mode):
+    ops, ecore, ref = build_all(ctx, SECTOR_CASES, core=False)
+    evals, stats = capi.batch_solve(ctx, ops, ecore, n=4, tol=1e-6, mode=mode)
+    for p, c in enumerate(ops):
+        np.testing.assert_allclose(evals[p], ref[p], rtol=0, atol=1e-6)
+        single, _, _ = c.solve(n=4, tol=1e-6, ecore=ecore[p], mode=mode)
+        np.testing.assert_allclose(single, ref[p], rtol=0, atol=1e-6)
         c.free()
 
 
