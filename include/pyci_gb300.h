@@ -56,6 +56,10 @@ extern "C" {
 #define PYCI_PREC_FP64 0       /* values f64, x/y f64                                      */
 #define PYCI_PREC_FP32 1       /* values f32 (high part), x/y f32                          */
 #define PYCI_PREC_FP64_SPLIT 2 /* values f32 high + f32 low summed in f64, x/y f64         */
+#define PYCI_PREC_FP64_DF 3    /* values f32 high + low, x split the same way, FP32
+                                  arithmetic with double-float sums (~2^-44 relative):
+                                  x f32[ncol][2k] (each row's k high parts, then its k
+                                  low parts), y f64[nrow][k]; k = 1, 2 or 4            */
 
 typedef struct pyci_gpu_ctx pyci_gpu_ctx;
 typedef struct pyci_gpu_csr pyci_gpu_csr;
@@ -154,7 +158,8 @@ int pyci_gpu_csr_matvec_noalloc(const pyci_gpu_csr *csr, const double *x, double
 /* Y = H X on device buffers for k vectors stored interleaved ([ncol][k] and
  * [nrow][k], element (row, vector) at row*k + vector), on `stream` (a
  * cudaStream_t, or NULL for the context's stream).  precision PYCI_PREC_*;
- * FP32 and FP64_SPLIT need pyci_gpu_csr_prepare_mixed first.  Asynchronous.
+ * FP32, FP64_SPLIT and FP64_DF need pyci_gpu_csr_prepare_mixed first
+ * (FP64_DF uses its own operand layout, above).  Asynchronous.
  * The device form of perform_op, used by the eigensolver and benchmarks. */
 int pyci_gpu_csr_spmm_device(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x,
                              void *y, void *stream);

@@ -18,7 +18,7 @@ OK, EINVAL, ETYPE, ENOCONV, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5,
 WFN_DOCI, WFN_FULLCI, WFN_GENCI = 0, 1, 2
 BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH = 0x1, 0x2, 0x4
 SOLVE_FP64, SOLVE_MIXED = 0, 1
-PREC_FP64, PREC_FP32, PREC_FP64_SPLIT = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_FP64_SPLIT, PREC_FP64_DF = 0, 1, 2, 3
 
 # Every symbol the header declares.
 SYMBOLS = [

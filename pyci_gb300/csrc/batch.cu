@@ -147,6 +147,89 @@ __global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restri
     }
 }
 
+// Block-diagonal FP64-accurate product in FP32 arithmetic for the final
+// Rayleigh-Ritz step: y[r][0..4) = (hi + lo) x over problem rows, x split as
+// xs[r] = (4 high parts, 4 low parts); exact products via FMA and
+// double-float (TwoSum) sums, as the single-operator double-float SpMM.
+__device__ __forceinline__ void df_acc(float &s, float &c, float p) {
+    const float u = __fadd_rn(s, p);
+    const float z = __fadd_rn(u, -s);
+    const float d = __fadd_rn(__fadd_rn(s, -__fadd_rn(u, -z)), __fadd_rn(p, -z));
+    s = u;
+    c = __fadd_rn(c, d);
+}
+
+template<int LANES>
+__global__ void __launch_bounds__(256) batch_spmm_df_kernel(const BatchOp *__restrict__ ops, RowSet rs,
+                                                            const float *__restrict__ xs, double *__restrict__ y) {
+    constexpr int K = 4;
+    const int lane = threadIdx.x % LANES;
+    const int64_t group = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / LANES;
+    const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
+    const int nseg = *rs.count;
+    const int64_t total = rs.arow0[nseg];
+    for (int64_t c0 = group; c0 < total; c0 += ngroups) {
+        const int kk = find_segment(rs.arow0, nseg, c0);
+        const BatchOp op = ops[rs.aprob[kk]];
+        const int64_t lr = c0 - rs.arow0[kk];
+        const int64_t r = op.row0 + lr;
+        const int64_t start = op.rowptr[lr], end = op.rowptr[lr + 1];
+        const float *xb = xs + op.row0 * (2 * K);
+        float s[K], c[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            s[k] = c[k] = 0.0f;
+        for (int64_t e = start + lane; e < end; e += LANES) {
+            const int64_t col = __ldcs(op.cols + e);
+            const float vh = __ldcs(op.hi + e), vl = __ldcs(op.lo + e);
+            const float4 a = __ldg(reinterpret_cast<const float4 *>(xb + col * (2 * K)));
+            const float4 b = __ldg(reinterpret_cast<const float4 *>(xb + col * (2 * K)) + 1);
+            const float xh[K] = {a.x, a.y, a.z, a.w}, xl[K] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const float p = __fmul_rn(vh, xh[k]);
+                const float err = fmaf(vh, xh[k], -p);
+                const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
+                df_acc(s[k], c[k], p);
+                c[k] = __fadd_rn(c[k], t);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1) {
+                const float s2 = __shfl_xor_sync(0xffffffffu, s[k], o, LANES);
+                const float c2 = __shfl_xor_sync(0xffffffffu, c[k], o, LANES);
+                df_acc(s[k], c[k], s2);
+                c[k] = __fadd_rn(c[k], c2);
+            }
+        }
+        if (lane < K) {
+            double out = static_cast<double>(s[0]) + static_cast<double>(c[0]);
+#pragma unroll
+            for (int k = 1; k < K; ++k)
+                if (lane == k)
+                    out = static_cast<double>(s[k]) + static_cast<double>(c[k]);
+            y[r * K + lane] = out;
+        }
+    }
+}
+
+// xs[r] = (fl32(X[j][r]), j < 4; fl32(X[j][r] - fl32(X[j][r])), j < 4) for the subset's rows.
+__global__ void batch_pack_split_kernel(const double *__restrict__ X, int64_t N, RowSet rs,
+                                        const int64_t *__restrict__ row0, float *__restrict__ xs) {
+    for_rows(rs, row0, [&](int prob, int64_t r) {
+        (void)prob;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const double v = X[j * N + r];
+            const float h = static_cast<float>(v);
+            xs[r * 8 + j] = h;
+            xs[r * 8 + 4 + j] = static_cast<float>(v - static_cast<double>(h));
+        }
+    });
+}
+
 // Xi[r][j] = V[base[prob] + j][r], j < K, for the subset's rows.
 template<typename T, int K>
 __global__ void batch_pack_kernel(const T *__restrict__ V, int64_t N, const int *__restrict__ base, RowSet rs,
@@ -304,14 +387,23 @@ __global__ void seg_copy_kernel(const T *__restrict__ src, int ncols, int64_t N,
     });
 }
 
-// R[j][r] = AX[j][r] - theta[prob(r)][j] X[j][r]
+// R[j][r] = AX[j][r] - theta[prob(r)][j] X[j][r].  FP32 vectors: theta
+// split into FP32 high + low parts applied with two FMAs (no FP64
+// arithmetic, which is scarce on this GPU).
 template<typename T>
 __global__ void seg_residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const double *__restrict__ theta,
                                     int q, int64_t N, RowSet rs, const int64_t *__restrict__ row0, T *__restrict__ R) {
     for_rows(rs, row0, [&](int prob, int64_t r) {
-        for (int j = 0; j < q; ++j)
-            R[j * N + r] = static_cast<T>(static_cast<double>(AX[j * N + r]) -
-                                          theta[prob * q + j] * static_cast<double>(X[j * N + r]));
+        for (int j = 0; j < q; ++j) {
+            const double t = theta[prob * q + j];
+            if constexpr (sizeof(T) == 4) {
+                const float th = static_cast<float>(t), tl = static_cast<float>(t - static_cast<double>(th));
+                const float x = X[j * N + r];
+                R[j * N + r] = fmaf(-tl, x, fmaf(-th, x, AX[j * N + r]));
+            } else {
+                R[j * N + r] = AX[j * N + r] - t * X[j * N + r];
+            }
+        }
     });
 }
 
@@ -330,7 +422,10 @@ __global__ void seg_precondition_kernel(const T *__restrict__ R, const double *_
                 double den = theta[prob * nt + j] - d;
                 if (fabs(den) < 1e-8)
                     den = (den < 0.0) ? -1e-8 : 1e-8;
-                v = static_cast<T>(static_cast<double>(R[j * N + r]) / den);
+                if constexpr (sizeof(T) == 4)
+                    v = R[j * N + r] / static_cast<float>(den); // FP32 quotient
+                else
+                    v = R[j * N + r] / den;
             }
             out[c * N + r] = v;
         }
@@ -996,14 +1091,18 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
     {
         const RowSet rs = act_.view();
         const unsigned gr = grid(N);
-        batch_pack_kernel<double, 4><<<gr, 256, 0, st_>>>(X64, N, d_zero_, rs, d_row0_, Xi64), ::pyci_gpu::note_launch();
         const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ctx_->num_sms * 32, (N * 32 + 255) / 256));
-        if (mixed_ || !all_vals_)
-            batch_spmm_kernel<2, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi64, Yi64),
+        if (mixed_ || !all_vals_) {
+            // FP64-accurate products in FP32 arithmetic from high + low values.
+            float *xs = reinterpret_cast<float *>(Xi64); // [N][8] floats fit in [N][4] doubles
+            batch_pack_split_kernel<<<gr, 256, 0, st_>>>(X64, N, rs, d_row0_, xs), ::pyci_gpu::note_launch();
+            batch_spmm_df_kernel<32><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, xs, Yi64),
                 ::pyci_gpu::note_launch();
-        else
+        } else {
+            batch_pack_kernel<double, 4><<<gr, 256, 0, st_>>>(X64, N, d_zero_, rs, d_row0_, Xi64), ::pyci_gpu::note_launch();
             batch_spmm_kernel<0, 4, 32, double><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi64, Yi64),
                 ::pyci_gpu::note_launch();
+        }
         batch_unpack_kernel<double, 4><<<gr, 256, 0, st_>>>(Yi64, N, d_zero_, rs, d_row0_, AX64, nullptr),
             ::pyci_gpu::note_launch();
         matvecs_ += static_cast<int64_t>(P) * b;

@@ -94,6 +94,16 @@ int pyci_gpu_ctx_create(int device, pyci_gpu_ctx **out) {
         delete ctx;
         return cuda_status(e, "cudaStreamCreate");
     }
+    // Keep memory released by cudaFreeAsync in the device's stream-ordered
+    // pool rather than handing it back to the driver at every
+    // synchronisation: each solve allocates and frees gigabytes of workspace,
+    // and re-mapping it cost more than the solve's own kernels on large
+    // operators.  pyci_gpu_ctx_destroy trims the pool.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     *out = ctx;
     return PYCI_GPU_OK;
 }
@@ -104,6 +114,9 @@ int pyci_gpu_ctx_destroy(pyci_gpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamDestroy(ctx->stream);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess)
+        cudaMemPoolTrimTo(pool, 0);
     delete ctx;
     return PYCI_GPU_OK;
 }
@@ -404,6 +417,8 @@ int pyci_gpu_csr_spmm_device(const pyci_gpu_csr *csr, int precision, int64_t k, 
         return PYCI_GPU_EINVAL;
     }
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : csr->ctx->stream;
+    if (precision == PYCI_PREC_FP64_DF)
+        return csr_spmm_df(csr, static_cast<int>(k), static_cast<const float *>(x), static_cast<double *>(y), st);
     return csr_spmm(csr, precision, k, x, y, st);
 }
 

@@ -49,6 +49,19 @@ __global__ void pack_kernel(const T *__restrict__ V, int64_t N, int k, int kp, T
             Xi[r * kp + j] = (j < k) ? V[j * N + r] : T(0);
 }
 
+// xs[r][j] = fl32(V[j][r]), xs[r][K + j] = fl32(V[j][r] - xs[r][j]) for j < k,
+// zero for k <= j < K: the split operand of the double-float SpMM.
+__global__ void pack_split_kernel(const double *__restrict__ V, int64_t N, int k, int K, float *__restrict__ xs) {
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        for (int j = 0; j < K; ++j) {
+            const double v = (j < k) ? V[j * N + r] : 0.0;
+            const float h = static_cast<float>(v);
+            xs[r * 2 * K + j] = h;
+            xs[r * 2 * K + K + j] = static_cast<float>(v - static_cast<double>(h));
+        }
+}
+
 template<typename T>
 __global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, int kp, T *__restrict__ W) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
@@ -198,15 +211,39 @@ __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, 
 
 // R[j] = AX[j] - theta[j] X[j]; then, if precondition, R[j] /= (theta[j] - D)
 // with |theta - D| floored at 1e-8 (Davidson's diagonal preconditioner).
+// R[j] = AX[j] - theta[j] X[j].  FP32 vectors: theta is split into
+// theta_hi + theta_lo (both FP32) and applied with two FMAs, so the result
+// carries the FP32 rounding of AX and X only, with no FP64 arithmetic (which
+// is scarce on this GPU).
 template<typename T>
 __global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const double *__restrict__ theta,
                                 int q, int64_t N, T *__restrict__ R) {
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        for (int j = 0; j < q; ++j)
-            R[j * N + r] = static_cast<T>(static_cast<double>(AX[j * N + r]) - theta[j] * static_cast<double>(X[j * N + r]));
+    if constexpr (sizeof(T) == 4) {
+        float th_hi[kMaxQ], th_lo[kMaxQ];
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j) {
+            const double t = (j < q) ? theta[j] : 0.0;
+            th_hi[j] = static_cast<float>(t);
+            th_lo[j] = static_cast<float>(t - static_cast<double>(th_hi[j]));
+        }
+        for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+             r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+#pragma unroll
+            for (int j = 0; j < kMaxQ; ++j)
+                if (j < q) {
+                    const float x = X[j * N + r];
+                    R[j * N + r] = fmaf(-th_lo[j], x, fmaf(-th_hi[j], x, AX[j * N + r]));
+                }
+    } else {
+        for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+             r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+            for (int j = 0; j < q; ++j)
+                R[j * N + r] = AX[j * N + r] - theta[j] * X[j * N + r];
+    }
 }
 
+// out[j] = R[j] / (theta[j] - D) with |theta - D| floored at 1e-8 (Davidson's
+// diagonal preconditioner).  FP32 output: the quotient is taken in FP32.
 template<typename TI, typename TO>
 __global__ void precondition_kernel(const TI *__restrict__ R, const double *__restrict__ theta,
                                     const double *__restrict__ diag, int q, int64_t N, TO *__restrict__ out) {
@@ -217,7 +254,10 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
             double den = theta[j] - d;
             if (fabs(den) < 1e-8)
                 den = (den < 0.0) ? -1e-8 : 1e-8;
-            out[j * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
+            if constexpr (sizeof(TO) == 4)
+                out[j * N + r] = static_cast<float>(R[j * N + r]) / static_cast<float>(den);
+            else
+                out[j * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
         }
     }
 }
@@ -665,7 +705,9 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                     (rc = alloc(&Yi64, N * kMaxQ)))
                     return rc;
             }
-            if ((rc = combine<T, double, double>(V, m, Yb, b, 0.0, X64)))
+            // Accumulated in the storage precision: errors in the Ritz
+            // vectors enter the refined Rayleigh quotients only to second order.
+            if ((rc = combine<T, double, T>(V, m, Yb, b, 0.0, X64)))
                 return rc;
             // Orthonormalise X64 in FP64 (modified Gram-Schmidt, two passes).
             for (int j = 0; j < b; ++j) {
@@ -683,11 +725,14 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 scale_kernel<double><<<grid(N), 256, 0, st_>>>(xj, N, 1.0 / std::sqrt(Gc[0])), ::pyci_gpu::note_launch();
             }
             for (int j0 = 0; j0 < b; j0 += kSpmmChunk) {
+                // FP64-accurate product in FP32 arithmetic (double-float).
                 const int kk = std::min(kSpmmChunk, b - j0);
                 const int kp = padded_width(kk);
-                pack_kernel<double><<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, Xi64), ::pyci_gpu::note_launch();
+                float *xs = reinterpret_cast<float *>(Xi64); // [N][2 kp] floats fit in [N][kMaxQ] doubles
+                pack_split_kernel<<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, xs),
+                    ::pyci_gpu::note_launch();
                 cudaEventRecord(ev0_, st_);
-                if ((rc = csr_spmm(csr_, PYCI_PREC_FP64_SPLIT, kp, Xi64, Yi64, st_)))
+                if ((rc = csr_spmm_df(csr_, kp, xs, Yi64, st_)))
                     return rc;
                 cudaEventRecord(ev1_, st_);
                 unpack_kernel<double><<<grid(N), 256, 0, st_>>>(Yi64, N, kk, kp, AX64 + static_cast<int64_t>(j0) * N), ::pyci_gpu::note_launch();

@@ -43,7 +43,9 @@ struct pyci_gpu_csr {
     int spmm_lanes = 32;         // lanes per row suggested by the mean row length
     // SpMM tile variant chosen by the autotuner per (value kind, width k <= 8),
     // -1 until the first product with that pair.
-    mutable int tuned[3][9] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1},
+    // Kinds: FP64, FP32, FP64 from high + low, double-float from high + low.
+    mutable int tuned[4][9] = {{-1, -1, -1, -1, -1, -1, -1, -1, -1},
+                               {-1, -1, -1, -1, -1, -1, -1, -1, -1},
                                {-1, -1, -1, -1, -1, -1, -1, -1, -1},
                                {-1, -1, -1, -1, -1, -1, -1, -1, -1}};
     // GenCI in the reference's own row loop (see genci_ref_* in build.cu):
@@ -76,6 +78,9 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
                      int64_t legacy_ncol);
 int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, void *y,
              cudaStream_t stream);
+// y[N][K] = (hi + lo) x with FP32 arithmetic and double-float accumulation;
+// xs[N][2K] holds each row's FP32 high parts then low parts; K = 1, 2 or 4.
+int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t stream);
 void csr_release(pyci_gpu_csr *csr);
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
 int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,

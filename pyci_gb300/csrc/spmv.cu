@@ -23,7 +23,7 @@
 
 namespace pyci_gpu {
 
-enum ValueKind { kF64 = 0, kF32 = 1, kSplit = 2 };
+enum ValueKind { kF64 = 0, kF32 = 1, kSplit = 2, kSplitDF = 3 };
 
 template<int VK>
 struct Values;
@@ -364,9 +364,167 @@ __global__ void spmm_lower_kernel(int64_t nrow, const int64_t *rowptr, const int
     }
 }
 
+// FP64-accurate product with FP32 arithmetic only (this GPU's FP64 rate is
+// a small fraction of its FP32 rate).  Values are the exact high/low split
+// v = hi + lo; x arrives split the same way, row c of xs holding
+// xh[c][0..K) then xl[c][0..K).  Each term
+//   v x = hi xh + (hi xh - fl(hi xh)) + hi xl + lo xh  (+ lo xl, ~2^-48 |v x|)
+// is formed as p = fl(hi xh), its exact rounding error e = fma(hi, xh, -p),
+// and t = fma(hi, xl, fma(lo, xh, e)); p is added to a double-float sum
+// (s, c) with Knuth's TwoSum (6 FP32 additions, exact), and t to c.  The
+// result s + c is converted to FP64 once per row: relative error ~2^-44,
+// against ~2^-53 for FP64 arithmetic, far below what the FP64 refinement of
+// the eigensolver can resolve.  __fadd_rn / __fmul_rn keep the compiler from
+// fusing the error-free transformations into FMAs.
+__device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
+    const float u = __fadd_rn(s, p);
+    const float z = __fadd_rn(u, -s);
+    const float d = __fadd_rn(__fadd_rn(s, -__fadd_rn(u, -z)), __fadd_rn(p, -z));
+    s = u;
+    c = __fadd_rn(c, d);
+}
+
+template<int K, int LANES>
+__global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
+                                                      const int32_t *__restrict__ cols, const float *__restrict__ hi,
+                                                      const float *__restrict__ lo, const float *__restrict__ xs,
+                                                      double *__restrict__ y) {
+    const int lane = threadIdx.x % LANES;
+    const int64_t group = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / LANES;
+    const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
+    for (int64_t r = group; r < nrow; r += ngroups) {
+        const int64_t start = rowptr[r], end = rowptr[r + 1];
+        float s[K], c[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            s[k] = c[k] = 0.0f;
+        for (int64_t e = start + lane; e < end; e += LANES) {
+            const int64_t col = __ldcs(cols + e);
+            const float vh = __ldcs(hi + e), vl = __ldcs(lo + e);
+            const float *xr = xs + col * (2 * K);
+            float xh[K], xl[K];
+            if constexpr (K == 4) {
+                const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
+                const float4 b = __ldg(reinterpret_cast<const float4 *>(xr) + 1);
+                xh[0] = a.x, xh[1] = a.y, xh[2] = a.z, xh[3] = a.w;
+                xl[0] = b.x, xl[1] = b.y, xl[2] = b.z, xl[3] = b.w;
+            } else if constexpr (K == 2) {
+                const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
+                xh[0] = a.x, xh[1] = a.y;
+                xl[0] = a.z, xl[1] = a.w;
+            } else {
+                const float2 a = __ldg(reinterpret_cast<const float2 *>(xr));
+                xh[0] = a.x;
+                xl[0] = a.y;
+            }
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const float p = __fmul_rn(vh, xh[k]);
+                const float err = fmaf(vh, xh[k], -p);
+                const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
+                two_sum_acc(s[k], c[k], p);
+                c[k] = __fadd_rn(c[k], t);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1) {
+                const float s2 = __shfl_xor_sync(0xffffffffu, s[k], o, LANES);
+                const float c2 = __shfl_xor_sync(0xffffffffu, c[k], o, LANES);
+                two_sum_acc(s[k], c[k], s2);
+                c[k] = __fadd_rn(c[k], c2);
+            }
+        }
+        if (lane < K) {
+            double out = static_cast<double>(s[0]) + static_cast<double>(c[0]);
+#pragma unroll
+            for (int k = 1; k < K; ++k)
+                if (lane == k)
+                    out = static_cast<double>(s[k]) + static_cast<double>(c[k]);
+            y[r * K + lane] = out;
+        }
+    }
+}
+
+template<int K>
+void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
+    const int lanes = variant_lanes(v);
+    const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (csr->nrow * lanes + 255) / 256));
+    const unsigned g = static_cast<unsigned>(blocks);
+    if (lanes == 8)
+        spmm_df_kernel<K, 8><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
+    else if (lanes == 16)
+        spmm_df_kernel<K, 16><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
+    else
+        spmm_df_kernel<K, 32><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
+    ::pyci_gpu::note_launch();
+}
+
+inline void launch_df(int v, const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
+    if (K == 4)
+        launch_df_variant<4>(v, csr, xs, y, st);
+    else if (K == 2)
+        launch_df_variant<2>(v, csr, xs, y, st);
+    else
+        launch_df_variant<1>(v, csr, xs, y, st);
+}
+
 } // namespace pyci_gpu
 
 using namespace pyci_gpu;
+
+// y[N][K] = (hi + lo) x for one split block xs[N][2K] (K = 1, 2 or 4), FP32
+// arithmetic with double-float accumulation; lanes per row tuned on first use
+// (variants 2, 1, 0 = 32, 16, 8 lanes).
+int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
+    if (!csr->hi || !csr->lo) {
+        set_error("split product needs pyci_gpu_csr_prepare_mixed first");
+        return PYCI_GPU_EINVAL;
+    }
+    if (csr->lower_only || !(K == 1 || K == 2 || K == 4)) {
+        set_error("double-float product: unsupported operator layout or width %d", K);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    if (csr->nrow == 0)
+        return PYCI_GPU_OK;
+    int &choice = csr->tuned[kSplitDF][K];
+    if (choice < 0)
+        choice = tuning_cache_lookup(csr, kSplitDF, K);
+    if (choice < 0) {
+        if (!autotune_enabled() || csr->nnz < (1 << 20)) {
+            choice = heuristic_variant(csr);
+        } else {
+            cudaEvent_t a, b;
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            float best = 1e30f;
+            int best_v = heuristic_variant(csr);
+            for (int v = 0; v < 3; ++v) {
+                launch_df(v, csr, K, xs, y, st);
+                cudaEventRecord(a, st);
+                launch_df(v, csr, K, xs, y, st);
+                launch_df(v, csr, K, xs, y, st);
+                cudaEventRecord(b, st);
+                cudaEventSynchronize(b);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (ms < best) {
+                    best = ms;
+                    best_v = v;
+                }
+            }
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            choice = best_v;
+            tuning_cache_store(csr, kSplitDF, K, choice);
+        }
+    }
+    launch_df(choice, csr, K, xs, y, st);
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
 
 static int spmm_lower(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, void *y,
                       cudaStream_t st) {

@@ -164,6 +164,39 @@ def test_spmm_precisions_against_oracle(ctx):
     csr.free()
 
 
+def split_rows(X):
+    r"""[N][k] FP64 -> [N][2k] FP32: each row's high parts, then its low parts."""
+    hi = X.astype(np.float32)
+    lo = (X - hi.astype(np.float64)).astype(np.float32)
+    return np.ascontiguousarray(np.concatenate([hi, lo], axis=1))
+
+
+@pytest.mark.parametrize("nb, na", [(8, 4), (10, 4)])  # 10, 4: 26M entries, past the autotuning threshold
+def test_spmm_double_float_against_oracle(ctx, nb, na):
+    r"""PYCI_PREC_FP64_DF: FP32 arithmetic with double-float sums reproduces the
+    FP64 product to ~2^-44 relative."""
+    import torch
+    ecore, one, two = synthetic_integrals(nb, 1002)
+    dets = O.all_dets(O.FULLCI, nb, na, na)
+    ref = O.build_csr(O.FULLCI, nb, na, na, dets, one, two)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, na, na, dets, one, two, flags=capi.BUILD_FULL_COLEX)
+    csr.prepare_mixed(drop_fp64=True)
+    N = dets.shape[0]
+    rng = np.random.default_rng(6)
+    for k in (1, 2, 4):
+        X = rng.normal(size=(N, k))
+        Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
+        xs = torch.tensor(split_rows(X), device="cuda")
+        yd = torch.empty((N, k), dtype=torch.float64, device="cuda")
+        for _ in range(2):  # the first call may tune, the second uses the chosen variant
+            csr.spmm_device(capi.PREC_FP64_DF, k, xs.data_ptr(), yd.data_ptr(), None)
+            torch.cuda.synchronize()
+            np.testing.assert_allclose(yd.cpu().numpy(), Y_ref, rtol=1e-11, atol=1e-11 * np.abs(Y_ref).max())
+    with pytest.raises(capi.GpuError):
+        csr.spmm_device(capi.PREC_FP64_DF, 3, xs.data_ptr(), yd.data_ptr(), None)
+    csr.free()
+
+
 def test_add_all_dets_on_device(ctx):
     for kind, ok, n, nu, nd in [(capi.WFN_FULLCI, O.FULLCI, 8, 3, 2), (capi.WFN_DOCI, O.DOCI, 70, 2, 2),
                                 (capi.WFN_GENCI, O.GENCI, 12, 4, 0), (capi.WFN_FULLCI, O.FULLCI, 65, 2, 1)]:
