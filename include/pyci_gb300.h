@@ -175,7 +175,8 @@ int pyci_gpu_csr_prepare_mixed(pyci_gpu_csr *csr, int drop_fp64);
  *   ncv      maximum subspace dimension (-1: default)
  *   maxiter  maximum iterations (-1: default)
  *   tol      convergence: ||H x - theta x|| <= tol * max(eps^(2/3), |theta|) per root
- *   evals    f64[n]; evecs f64[n][nrow] (eigenvector per row)
+ *   evals    f64[n]; evecs f64[n][nrow] (eigenvector per row), or NULL to keep
+ *            the eigenvectors on the device only
  * Eigenpairs are returned in decreasing order of eigenvalue, as the reference
  * returns them.  Errors: EINVAL when n >= nrow (nrow > 1), ETYPE when
  * nrow != ncol or the operator is not symmetric, ENOCONV on no convergence. */

@@ -207,10 +207,12 @@ class Csr:
     def prepare_mixed(self, drop_fp64=False):
         check(lib().pyci_gpu_csr_prepare_mixed(self.handle, int(bool(drop_fp64))))
 
-    def solve(self, n=1, c0=None, ncv=-1, maxiter=-1, tol=1e-12, ecore=0.0, mode=SOLVE_FP64):
+    def solve(self, n=1, c0=None, ncv=-1, maxiter=-1, tol=1e-12, ecore=0.0, mode=SOLVE_FP64, evecs=True):
+        r"""(evals, evecs, stats); evecs is None when `evecs` is false (the
+        eigenvectors then stay on the device and are not copied out)."""
         nrow = self.shape()[0]
         evals = np.empty(n, dtype=np.float64)
-        evecs = np.empty((n, nrow), dtype=np.float64)
+        evecs = np.empty((n, nrow), dtype=np.float64) if evecs else None
         st = SolveStats()
         c0 = None if c0 is None else np.ascontiguousarray(c0, dtype=np.float64)
         check(lib().pyci_gpu_csr_solve(self.handle, n, _ptr(c0), ncv, maxiter, tol, ecore, mode, _ptr(evals),
