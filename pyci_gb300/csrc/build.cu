@@ -304,6 +304,12 @@ __device__ __forceinline__ int64_t exc_column(const BuildParams &p, const RowSta
     return column_of<NW>(p, a, b);
 }
 
+// phase * v for phase = +-1, as a sign-bit flip: bit-identical to the FP64
+// product and free of FP64 arithmetic (scarce on this GPU).
+__device__ __forceinline__ double apply_phase(int phase, double v) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (static_cast<long long>(phase < 0) << 63));
+}
+
 // Matrix element of an excitation, with the formulas and summation order of
 // add_row (pyci/src/sparseop.cpp:220-258 DOCI, 260-427 FullCI, 429-502 GenCI).
 template<int NW>
@@ -325,7 +331,7 @@ __device__ double exc_value(const BuildParams &p, const RowState &s, const Exc &
             const int k2 = s.occ_b[t];
             v1 += two_mo_at(two, n, ii, k2, jj, k2);
         }
-        return phase_single<NW>(s.ra, ii, jj) * v1;
+        return apply_phase(phase_single<NW>(s.ra, ii, jj), v1);
     }
     case kSingleB: {
         // 0-1 excitation
@@ -338,18 +344,18 @@ __device__ double exc_value(const BuildParams &p, const RowState &s, const Exc &
             const int k2 = s.occ_b[t];
             v1 += two_mo_at(two, n, ii, k2, jj, k2) - two_mo_at(two, n, ii, k2, k2, jj);
         }
-        return phase_single<NW>(s.rb, ii, jj) * v1;
+        return apply_phase(phase_single<NW>(s.rb, ii, jj), v1);
     }
     case kDoubleAA:
-        return phase_double<NW>(s.ra, ii, kk, jj, ll) *
-               (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+        return apply_phase(phase_double<NW>(s.ra, ii, kk, jj, ll),
+                           two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
     case kDoubleBB:
-        return phase_double<NW>(s.rb, ii, kk, jj, ll) *
-               (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
+        return apply_phase(phase_double<NW>(s.rb, ii, kk, jj, ll),
+                           two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj));
     default:
         // 1-1 excitation: alpha ii -> jj, beta kk -> ll
-        return (phase_single<NW>(s.ra, ii, jj) * phase_single<NW>(s.rb, kk, ll)) *
-               two_mo_at(two, n, ii, kk, jj, ll);
+        return apply_phase(phase_single<NW>(s.ra, ii, jj) * phase_single<NW>(s.rb, kk, ll),
+                           two_mo_at(two, n, ii, kk, jj, ll));
     }
 }
 
@@ -677,132 +683,237 @@ __device__ void block_sort_pairs(int *key, int *val, int n) {
     }
 }
 
-constexpr int kSortedMax = 512; // max alpha (or beta) excitations + 1 per row for the sorted fill
+constexpr int kSortedMax = 512; // max alpha (or beta) excitations + 1 per string for the table fill
 
-// Full-space FullCI row written directly in ascending column order.
+// Full-space FullCI rows written directly in ascending column order.
 //
 // Columns are rank(a') * nbeta + rank(b'), so a row is the concatenation,
 // over the row's alpha excitations a' = {a} + singles + doubles sorted by
 // rank, of its beta partners sorted by rank: all of {b} + singles + doubles
-// for a' = a, {b} + singles for a single, {b} for a double.  Sorting the two
-// short excitation lists and a prefix sum over the alpha list place every
-// entry; no row-length sort is needed.  Only for builds that keep every
+// for a' = a, {b} + singles for a single, {b} for a double.  The sorted lists
+// depend on one string only, so they are built once per string
+// (string_tables_kernel) rather than once per row: for 12 orbitals, 5 + 5
+// electrons, 792 strings serve 627,264 rows.  Only for builds that keep every
 // candidate (fresh full space, nrow = ncol = ndet).
+//
+// Per string s of one spin (arrays [nstr][npad]):
+//   key[s][i]     target string rank, ascending (INT32_MAX padding)
+//   val[s][i]     type << 20 | index within its kind (type 0: s itself,
+//                 1: single, 2: double; the index is the row's own
+//                 occupied/virtual enumeration, as in make_exc)
+//   off[s][i]     exclusive prefix of the number of beta partners of the
+//                 entries before i (alpha use)
+//   sub[s][c], subval[s][c]  the entries of type <= 1, in order (beta use)
+//   self[s]       position of s itself in key
+//   bits[s][w]    the string's occupation words (nw of them)
+struct StringTables {
+    int32_t *key, *val, *off, *sub, *subval, *self;
+    uint64_t *bits;
+    int npad, nw;
+};
+
+// One block per string of `spin` (0 alpha, 1 beta).  grp0 / grp1: beta
+// partners of the alpha string itself / of an alpha single (the beta list
+// length 1 + singles + doubles, and 1 + singles).  row_len: the uniform row
+// length, checked on alpha tables (error 4 on a mismatch).
 template<int NW>
-__global__ void __launch_bounds__(256) fill_fci_sorted_kernel(BuildParams p, int64_t row0) {
+__global__ void __launch_bounds__(256) string_tables_kernel(BuildParams p, int spin, StringTables T, int grp0,
+                                                            int grp1, int64_t row_len) {
     __shared__ RowState s;
-    __shared__ int akey[kSortedMax], aval[kSortedMax], bkey[kSortedMax], bval[kSortedMax];
-    __shared__ int b1key[kSortedMax], b1val[kSortedMax], off[kSortedMax], tmp[kSortedMax], flag[kSortedMax];
-    __shared__ double dval;
-    __shared__ int apos, bpos, nb1;
+    __shared__ int key[kSortedMax], val[kSortedMax], flag[kSortedMax], tmp[kSortedMax];
     extern __shared__ __align__(16) unsigned char dyn[];
-    const int64_t row = row0 + blockIdx.x;
-    if (row >= p.nrow)
-        return;
+    const int64_t str = blockIdx.x;
     const RowScratch sc = setup_scratch(p, dyn);
-    load_row<NW>(p, row, s);
+    load_row<NW>(p, spin == 0 ? str * p.nbeta : str, s);
     fill_rank_cache<NW>(p, s, sc.binom, sc.cache);
+    __syncthreads();
     const int sa = s.no_a * s.nv_a, sb = s.no_b * s.nv_b;
     const int da = (s.no_a * (s.no_a - 1) / 2) * (s.nv_a * (s.nv_a - 1) / 2);
-    const int db = (s.no_b * (s.no_b - 1) / 2) * (s.nv_b * (s.nv_b - 1) / 2);
-    const int na = 1 + sa + da, nbb = 1 + sb + db;
-    int npad = 2;
-    while (npad < na || npad < nbb)
-        npad <<= 1;
-    const int64_t ra = row / p.nbeta, rb = row % p.nbeta;
-    __syncthreads();
-    // Excitation lists: payload = type * 2^20 + index (type 0 = the row's own string).
+    const int n1 = spin == 0 ? sa : sb;
+    const int n2 = spin == 0 ? da : (s.no_b * (s.no_b - 1) / 2) * (s.nv_b * (s.nv_b - 1) / 2);
+    const int nl = 1 + n1 + n2, npad = T.npad;
+    // Rank cache layout: alpha singles, beta singles, alpha doubles, beta doubles.
+    const int s_off = spin == 0 ? 0 : sa, d_off = sa + sb + (spin == 0 ? 0 : da);
     for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-        if (t < na) {
-            akey[t] = (t == 0) ? static_cast<int>(ra) : (t <= sa ? sc.cache[t - 1] : sc.cache[sa + sb + (t - 1 - sa)]);
-            aval[t] = (t == 0) ? 0 : (t <= sa ? ((1 << 20) | (t - 1)) : ((2 << 20) | (t - 1 - sa)));
+        if (t < nl) {
+            key[t] = (t == 0) ? static_cast<int>(str) : (t <= n1 ? sc.cache[s_off + t - 1] : sc.cache[d_off + t - 1 - n1]);
+            val[t] = (t == 0) ? 0 : (t <= n1 ? ((1 << 20) | (t - 1)) : ((2 << 20) | (t - 1 - n1)));
         } else {
-            akey[t] = INT32_MAX;
-            aval[t] = 0;
-        }
-        if (t < nbb) {
-            bkey[t] = (t == 0) ? static_cast<int>(rb) : (t <= sb ? sc.cache[sa + t - 1] : sc.cache[sa + sb + da + (t - 1 - sb)]);
-            bval[t] = (t == 0) ? 0 : (t <= sb ? ((1 << 20) | (t - 1)) : ((2 << 20) | (t - 1 - sb)));
-        } else {
-            bkey[t] = INT32_MAX;
-            bval[t] = 0;
+            key[t] = INT32_MAX;
+            val[t] = 0;
         }
     }
-    if (threadIdx.x == 0)
-        dval = diagonal(p, s);
     __syncthreads();
-    block_sort_pairs(akey, aval, npad);
-    block_sort_pairs(bkey, bval, npad);
-    // Beta partners of an alpha single: {b} + singles, in sorted order.
+    block_sort_pairs(key, val, npad);
+    int32_t *K = T.key + str * npad, *V = T.val + str * npad, *O = T.off + str * npad;
+    int32_t *SK = T.sub + str * npad, *SV = T.subval + str * npad;
+    // Entries of type <= 1, compacted in order.
     for (int t = threadIdx.x; t < npad; t += blockDim.x)
-        flag[t] = (t < nbb && (bval[t] >> 20) <= 1) ? 1 : 0;
+        flag[t] = (t < nl && (val[t] >> 20) <= 1) ? 1 : 0;
     __syncthreads();
     block_exclusive_scan(flag, tmp, npad);
     for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-        if (t < nbb && (bval[t] >> 20) <= 1) {
-            b1key[flag[t]] = bkey[t];
-            b1val[flag[t]] = bval[t];
+        if (t < nl && (val[t] >> 20) <= 1) {
+            SK[flag[t]] = key[t];
+            SV[flag[t]] = val[t];
         }
-        if (t < nbb && bval[t] == 0)
-            bpos = t;
-        if (t < na && aval[t] == 0)
-            apos = t;
+        if (t < nl && val[t] == 0)
+            T.self[str] = t;
     }
-    if (threadIdx.x == 0)
-        nb1 = 1 + sb;
-    // Group lengths along the sorted alpha list, then offsets.
+    if (threadIdx.x < T.nw)
+        T.bits[str * T.nw + threadIdx.x] = spin == 0 ? s.ra[threadIdx.x] : s.rb[threadIdx.x];
+    __syncthreads();
+    // Beta-partner counts along the sorted list, then their exclusive prefix.
     for (int t = threadIdx.x; t < npad; t += blockDim.x) {
-        const int ty = aval[t] >> 20;
-        off[t] = (t < na) ? (ty == 0 ? nbb : (ty == 1 ? 1 + sb : 1)) : 0;
+        const int ty = val[t] >> 20;
+        flag[t] = (t < nl) ? (ty == 0 ? grp0 : (ty == 1 ? grp1 : 1)) : 0;
     }
     __syncthreads();
-    block_exclusive_scan(off, tmp, npad);
+    block_exclusive_scan(flag, tmp, npad);
+    for (int t = threadIdx.x; t < npad; t += blockDim.x) {
+        K[t] = key[t];
+        V[t] = val[t];
+        O[t] = flag[t];
+    }
+    if (threadIdx.x == 0 && spin == 0) {
+        const int ty = val[nl - 1] >> 20;
+        const int64_t total = flag[nl - 1] + (ty == 0 ? grp0 : (ty == 1 ? grp1 : 1));
+        if (total != row_len)
+            atomicExch(p.error, 4);
+    }
+}
+
+// Ascending occupied and virtual orbital lists of one string, built by a
+// warp: lane j tests orbital o0 + j, a ballot gives each list position.
+template<int NW>
+__device__ __forceinline__ void warp_lists(const uint64_t *bits, int nbasis, int16_t *occ, int16_t *vir, int &no,
+                                           int &nv) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int cno = 0, cnv = 0;
+    for (int o0 = 0; o0 < nbasis; o0 += 32) {
+        const int o = o0 + lane;
+        const bool valid = o < nbasis;
+        const bool in = valid && ((bits[o >> 6] >> (o & 63)) & 1ULL);
+        const unsigned mo = __ballot_sync(0xffffffffu, in), mv = __ballot_sync(0xffffffffu, valid && !in);
+        if (in && cno + __popc(mo & below) < kMaxOcc)
+            occ[cno + __popc(mo & below)] = static_cast<int16_t>(o);
+        else if (valid && !in && cnv + __popc(mv & below) < kMaxVir)
+            vir[cnv + __popc(mv & below)] = static_cast<int16_t>(o);
+        cno += __popc(mo);
+        cnv += __popc(mv);
+    }
+    no = cno;
+    nv = cnv;
+}
+
+// One warp per row (kFillRowsPerBlock rows per block), so nothing waits on a
+// block-wide barrier: the warp builds the row's occupation lists from the
+// string tables, computes the row's single-excitation values (O(nocc) sums
+// each) on all lanes but one and the diagonal on the last lane, then places
+// every entry from the row's alpha and beta tables (binary search of the
+// entry's alpha group) and writes columns and values in order.  Per-warp
+// shared memory: RowState, the alpha group offsets (na ints), the singles
+// (nsg doubles).
+constexpr int kFillRowsPerBlock = 8;
+constexpr int kTableMaxSingles = 2048; // alpha + beta singles per row (8 warps' shared memory stays < 160 KB)
+
+template<int NW>
+__global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int64_t row0, StringTables A,
+                                                              StringTables B, int na, int nsg) {
+    extern __shared__ __align__(16) unsigned char dyn[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t per_warp = (sizeof(RowState) + sizeof(double) * nsg + sizeof(int) * na + 15) & ~static_cast<size_t>(15);
+    unsigned char *mine = dyn + per_warp * warp;
+    RowState &s = *reinterpret_cast<RowState *>(mine);
+    double *sval = reinterpret_cast<double *>(mine + sizeof(RowState));
+    int *aoff = reinterpret_cast<int *>(mine + sizeof(RowState) + sizeof(double) * nsg);
+    const int64_t row = row0 + static_cast<int64_t>(blockIdx.x) * kFillRowsPerBlock + warp;
+    if (row >= p.nrow)
+        return;
+    const int64_t ra = row / p.nbeta, rb = row % p.nbeta;
+    if (lane < NW) {
+        s.ra[lane] = __ldg(A.bits + ra * NW + lane);
+        s.rb[lane] = __ldg(B.bits + rb * NW + lane);
+    }
+    __syncwarp();
+    {
+        int no, nv;
+        warp_lists<NW>(s.ra, p.nbasis, s.occ_a, s.vir_a, no, nv);
+        if (lane == 0) {
+            s.no_a = no;
+            s.nv_a = nv;
+        }
+        warp_lists<NW>(s.rb, p.nbasis, s.occ_b, s.vir_b, no, nv);
+        if (lane == 0) {
+            s.no_b = no;
+            s.nv_b = nv;
+        }
+    }
+    const int32_t *AK = A.key + ra * A.npad, *AV = A.val + ra * A.npad, *AO = A.off + ra * A.npad;
+    const int32_t *BK = B.key + rb * B.npad, *BV = B.val + rb * B.npad;
+    const int32_t *SK = B.sub + rb * B.npad, *SV = B.subval + rb * B.npad;
+    for (int t = lane; t < na; t += 32)
+        aoff[t] = __ldg(AO + t);
+    __syncwarp();
+    const int sa = s.no_a * s.nv_a;
+    for (int t = lane; t < nsg; t += 31) {
+        if (lane == 31)
+            break;
+        sval[t] = exc_value<NW>(p, s, t < sa ? make_exc(s, kSingleA, t, 0) : make_exc(s, kSingleB, t - sa, 0));
+    }
+    double dval = 0.0;
+    if (lane == 31)
+        dval = diagonal(p, s);
+    dval = __shfl_sync(0xffffffffu, dval, 31);
+    __syncwarp();
     const int64_t start = p.rowptr[row];
     const int len = static_cast<int>(p.rowptr[row + 1] - start);
-    if (threadIdx.x == 0) {
-        const int total = off[na - 1] + ((aval[na - 1] >> 20) == 0 ? nbb : ((aval[na - 1] >> 20) == 1 ? nb1 : 1));
-        if (total != len)
-            atomicExch(p.error, 4);
-        const int dpos = off[apos] + bpos;
+    if (lane == 0) {
         if (p.lower_len)
-            p.lower_len[row] = dpos + 1;
+            p.lower_len[row] = aoff[__ldg(A.self + ra)] + __ldg(B.self + rb) + 1;
         p.diag[row] = dval;
     }
-    for (int t = threadIdx.x; t < len; t += blockDim.x) {
-        // Group g: the last alpha position with off[g] <= t.
+    for (int t = lane; t < len; t += 32) {
+        // Alpha group g: the last position with aoff[g] <= t.
         int lo = 0, hi = na - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (off[mid] <= t)
+            if (aoff[mid] <= t)
                 lo = mid;
             else
                 hi = mid - 1;
         }
-        const int g = lo, qpos = t - off[g];
-        const int tya = aval[g] >> 20, ia = aval[g] & ((1 << 20) - 1);
+        const int g = lo, qpos = t - aoff[g];
+        const int av = __ldg(AV + g);
+        const int tya = av >> 20, ia = av & ((1 << 20) - 1);
         int bk, bv;
         if (tya == 0) {
-            bk = bkey[qpos];
-            bv = bval[qpos];
+            bk = __ldg(BK + qpos);
+            bv = __ldg(BV + qpos);
         } else if (tya == 1) {
-            bk = b1key[qpos];
-            bv = b1val[qpos];
+            bk = __ldg(SK + qpos);
+            bv = __ldg(SV + qpos);
         } else {
             bk = static_cast<int>(rb);
             bv = 0;
         }
         const int tyb = bv >> 20, ib = bv & ((1 << 20) - 1);
-        const int64_t col = static_cast<int64_t>(akey[g]) * p.nbeta + bk;
+        const int64_t col = static_cast<int64_t>(__ldg(AK + g)) * p.nbeta + bk;
         double val;
         if (tya == 0 && tyb == 0) {
             val = dval;
+        } else if (tya == 1 && tyb == 0) {
+            val = sval[ia];
+        } else if (tya == 0 && tyb == 1) {
+            val = sval[sa + ib];
         } else {
             int type, i1 = 0, i2 = 0;
             if (tya == 0) {
-                type = (tyb == 1) ? kSingleB : kDoubleBB;
+                type = kDoubleBB;
                 i1 = ib;
             } else if (tya == 1) {
-                type = (tyb == 0) ? kSingleA : kDoubleAB;
+                type = kDoubleAB;
                 i1 = ia;
                 i2 = ib;
             } else {
@@ -968,7 +1079,7 @@ __device__ void genci_ref_row(const BuildParams &p, int64_t idet, Emit emit) {
                         const int kk = occs[k];
                         v1 += two_mo_at(two, n, ii, kk, jj, kk) - two_mo_at(two, n, ii, kk, kk, jj);
                     }
-                    v = phase_single<NW>(rdet, ii, jj) * v1;
+                    v = apply_phase(phase_single<NW>(rdet, ii, jj), v1);
                 }
                 emit(jdet, v);
             }
@@ -979,8 +1090,8 @@ __device__ void genci_ref_row(const BuildParams &p, int64_t idet, Emit emit) {
                     excite_ref(det, kk, ll);
                     jdet = p.table.find<NW>(det);
                     if (keep_ref(p, idet, jdet))
-                        emit(jdet, VALUES ? phase_double<NW>(rdet, ii, kk, jj, ll) *
-                                                (two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj))
+                        emit(jdet, VALUES ? apply_phase(phase_double<NW>(rdet, ii, kk, jj, ll),
+                                                        two_mo_at(two, n, ii, kk, jj, ll) - two_mo_at(two, n, ii, kk, ll, jj))
                                           : 0.0);
                     excite_ref(det, ll, kk);
                 }
@@ -1189,10 +1300,75 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
     if (sorted_fci) {
-        for (int64_t r0 = 0; r0 < p.nrow; r0 += chunk) {
-            const int64_t nb = (p.nrow - r0 < chunk) ? p.nrow - r0 : chunk;
-            fill_fci_sorted_kernel<NW><<<static_cast<unsigned>(nb), 256, scratch, st>>>(p, r0), ::pyci_gpu::note_launch();
+        // Per-string tables (alpha and beta; one set when both spins have the
+        // same electron count), then the row fill.
+        const int64_t nstr_a = p.nrow / p.nbeta, nstr_b = p.nbeta;
+        const int no_a = static_cast<int>(p.nocc_up), no_b = static_cast<int>(p.nocc_dn);
+        const int nv_a = p.nbasis - no_a, nv_b = p.nbasis - no_b;
+        const int na = 1 + no_a * nv_a + (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
+        const int nbl = 1 + no_b * nv_b + (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
+        const int grp1 = 1 + no_b * nv_b;
+        auto pad = [](int n) {
+            int q = 2;
+            while (q < n)
+                q <<= 1;
+            return q;
+        };
+        const bool shared = (no_a == no_b);
+        StringTables TA{}, TB{};
+        TA.npad = pad(na);
+        TB.npad = pad(nbl);
+        TA.nw = TB.nw = NW;
+        std::vector<void *> mem;
+        auto make = [&](StringTables &T, int64_t nstr) -> int {
+            int32_t **arrs[] = {&T.key, &T.val, &T.off, &T.sub, &T.subval};
+            for (int32_t **a : arrs) {
+                PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(a), sizeof(int32_t) * nstr * T.npad, st));
+                mem.push_back(*a);
+            }
+            PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&T.self), sizeof(int32_t) * nstr, st));
+            mem.push_back(T.self);
+            PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&T.bits), sizeof(uint64_t) * nstr * NW, st));
+            mem.push_back(T.bits);
+            return PYCI_GPU_OK;
+        };
+        int rc = make(TA, nstr_a);
+        if (!rc && !shared)
+            rc = make(TB, nstr_b);
+        if (!shared && !rc) {
+            string_tables_kernel<NW><<<static_cast<unsigned>(nstr_a), 256, scratch, st>>>(p, 0, TA, nbl, grp1, uniform_len),
+                ::pyci_gpu::note_launch();
+            string_tables_kernel<NW><<<static_cast<unsigned>(nstr_b), 256, scratch, st>>>(p, 1, TB, nbl, grp1, uniform_len),
+                ::pyci_gpu::note_launch();
+        } else if (!rc) {
+            // Same string space for both spins: the alpha tables (offsets for
+            // alpha use, type <= 1 lists for beta use) serve both.
+            string_tables_kernel<NW><<<static_cast<unsigned>(nstr_a), 256, scratch, st>>>(p, 0, TA, nbl, grp1, uniform_len),
+                ::pyci_gpu::note_launch();
+            TB = TA;
         }
+        if (!rc) {
+            const int nsg = no_a * nv_a + no_b * nv_b;
+            const size_t per_warp = (sizeof(RowState) + sizeof(double) * nsg + sizeof(int) * na + 15) & ~static_cast<size_t>(15);
+            const size_t dsm = per_warp * kFillRowsPerBlock;
+            if (dsm > 48 * 1024) {
+                const cudaError_t e = cudaFuncSetAttribute(fill_fci_tables_kernel<NW>,
+                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dsm));
+                if (e != cudaSuccess)
+                    rc = cuda_status(e, "fill shared memory");
+            }
+            const int64_t rows_per_launch = chunk * kFillRowsPerBlock;
+            for (int64_t r0 = 0; !rc && r0 < p.nrow; r0 += rows_per_launch) {
+                const int64_t nr = (p.nrow - r0 < rows_per_launch) ? p.nrow - r0 : rows_per_launch;
+                const unsigned nb = static_cast<unsigned>((nr + kFillRowsPerBlock - 1) / kFillRowsPerBlock);
+                fill_fci_tables_kernel<NW><<<nb, 32 * kFillRowsPerBlock, dsm, st>>>(p, r0, TA, TB, na, nsg),
+                    ::pyci_gpu::note_launch();
+            }
+        }
+        for (void *m : mem)
+            cudaFreeAsync(m, st);
+        if (rc)
+            return rc;
         PYCI_CUDA_TRY(cudaGetLastError());
         return PYCI_GPU_OK;
     }
@@ -1456,7 +1632,8 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         const int64_t na = 1 + no_a * nv_a + (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
         const int64_t nbb = 1 + no_b * nv_b + (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
         const bool sorted_fci = uniform && kind == PYCI_WFN_FULLCI && p.ncache > 0 && na <= kSortedMax &&
-                                nbb <= kSortedMax && !(csr->flags & PYCI_BUILD_FORCE_HASH);
+                                nbb <= kSortedMax && no_a * nv_a + no_b * nv_b <= kTableMaxSingles &&
+                                !(csr->flags & PYCI_BUILD_FORCE_HASH);
         switch (nw) {
         case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
         case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
