@@ -80,7 +80,7 @@ def build_library(verbose=False):
         o = os.path.join(OBJDIR, src + ".o")
         objs.append(o)
         if _newer(o, [s] + headers + [__file__]):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-I" + INCLUDE, "-I" + CSRC, "-c", s, "-o", o])
     with concurrent.futures.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):
             if verbose and out.strip():

@@ -706,10 +706,18 @@ constexpr int kSortedMax = 512; // max alpha (or beta) excitations + 1 per strin
 //   sub[s][c], subval[s][c]  the entries of type <= 1, in order (beta use)
 //   self[s]       position of s itself in key
 //   bits[s][w]    the string's occupation words (nw of them)
+//   sdesc[s][i]   single i (in make_exc's enumeration): ii | jj << 8 | (phase < 0) << 16
+//   dval[s][q]    the same-spin double q's matrix element (one string only:
+//                 phase * (<ii kk|jj ll> - <ii kk|ll jj>), add_row's formula)
+//   gmap[s][t]    alpha use: the group (position in key) that row entry t
+//                 falls in, for t < glen (the uniform row length)
 struct StringTables {
-    int32_t *key, *val, *off, *sub, *subval, *self;
+    int32_t *key, *val, *off, *sub, *subval, *self, *sdesc;
+    uint16_t *gmap;
     uint64_t *bits;
-    int npad, nw;
+    double *dval;
+    int64_t glen;
+    int npad, nw, n1, n2;
 };
 
 // One block per string of `spin` (0 alpha, 1 beta).  grp0 / grp1: beta
@@ -762,6 +770,14 @@ __global__ void __launch_bounds__(256) string_tables_kernel(BuildParams p, int s
     }
     if (threadIdx.x < T.nw)
         T.bits[str * T.nw + threadIdx.x] = spin == 0 ? s.ra[threadIdx.x] : s.rb[threadIdx.x];
+    // Single descriptors and same-spin double values of this string.
+    for (int i = threadIdx.x; i < n1; i += blockDim.x) {
+        const Exc e = make_exc(s, spin == 0 ? kSingleA : kSingleB, i, 0);
+        const int ph = phase_single<NW>(spin == 0 ? s.ra : s.rb, e.ii, e.jj);
+        T.sdesc[str * T.n1 + i] = e.ii | (e.jj << 8) | ((ph < 0 ? 1 : 0) << 16);
+    }
+    for (int q = threadIdx.x; q < n2; q += blockDim.x)
+        T.dval[str * T.n2 + q] = exc_value<NW>(p, s, make_exc(s, spin == 0 ? kDoubleAA : kDoubleBB, q, 0));
     __syncthreads();
     // Beta-partner counts along the sorted list, then their exclusive prefix.
     for (int t = threadIdx.x; t < npad; t += blockDim.x) {
@@ -775,12 +791,71 @@ __global__ void __launch_bounds__(256) string_tables_kernel(BuildParams p, int s
         V[t] = val[t];
         O[t] = flag[t];
     }
+    if (T.gmap) {
+        // Entry -> group map for the alpha use of this string.
+        uint16_t *G = T.gmap + str * T.glen;
+        for (int g = threadIdx.x; g < nl; g += blockDim.x) {
+            const int ty = val[g] >> 20;
+            const int64_t e = min(static_cast<int64_t>(flag[g]) + (ty == 0 ? grp0 : (ty == 1 ? grp1 : 1)), T.glen);
+            for (int64_t t = flag[g]; t < e; ++t)
+                G[t] = static_cast<uint16_t>(g);
+        }
+    }
     if (threadIdx.x == 0 && spin == 0) {
         const int ty = val[nl - 1] >> 20;
         const int64_t total = flag[nl - 1] + (ty == 0 ? grp0 : (ty == 1 ? grp1 : 1));
         if (total != row_len)
             atomicExch(p.error, 4);
     }
+}
+
+// Next set bit at or above position `from` in an NW-word string (-1: none).
+template<int NW>
+__device__ __forceinline__ int next_bit(const uint64_t *w, int from) {
+#pragma unroll
+    for (int i = 0; i < NW; ++i) {
+        if (from >= 64 * (i + 1))
+            continue;
+        const int sh = from - 64 * i;
+        const uint64_t m = sh > 0 ? (w[i] >> sh) << sh : w[i];
+        if (m)
+            return 64 * i + __ffsll(static_cast<long long>(m)) - 1;
+    }
+    return -1;
+}
+
+// FullCI diagonal of every row, one thread per row, in diagonal()'s summation
+// order (occupied orbitals ascending, as add_row<FullCIWfn> sums them):
+// alpha i: h_ii, then (J - K) with each later alpha, then J with each beta;
+// then beta i: h_ii, then (J - K) with each later beta.
+template<int NW>
+__global__ void fci_diag_kernel(BuildParams p, StringTables A, StringTables B) {
+    const int64_t row = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (row >= p.nrow)
+        return;
+    const int64_t ra = row / p.nbeta, rb = row % p.nbeta;
+    uint64_t a[NW], b[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        a[w] = __ldg(A.bits + ra * NW + w);
+        b[w] = __ldg(B.bits + rb * NW + w);
+    }
+    const int n = p.nbasis;
+    const double *one = p.one_mo, *two = p.two_mo;
+    double v2 = 0.0;
+    for (int ii = next_bit<NW>(a, 0); ii >= 0; ii = next_bit<NW>(a, ii + 1)) {
+        v2 += __ldg(&one[(n + 1) * ii]);
+        for (int kk = next_bit<NW>(a, ii + 1); kk >= 0; kk = next_bit<NW>(a, kk + 1))
+            v2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
+        for (int kk = next_bit<NW>(b, 0); kk >= 0; kk = next_bit<NW>(b, kk + 1))
+            v2 += two_mo_at(two, n, ii, kk, ii, kk);
+    }
+    for (int ii = next_bit<NW>(b, 0); ii >= 0; ii = next_bit<NW>(b, ii + 1)) {
+        v2 += __ldg(&one[(n + 1) * ii]);
+        for (int kk = next_bit<NW>(b, ii + 1); kk >= 0; kk = next_bit<NW>(b, kk + 1))
+            v2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
+    }
+    p.diag[row] = v2;
 }
 
 // Ascending occupied and virtual orbital lists of one string, built by a
@@ -810,9 +885,11 @@ __device__ __forceinline__ void warp_lists(const uint64_t *bits, int nbasis, int
 // One warp per row (kFillRowsPerBlock rows per block), so nothing waits on a
 // block-wide barrier: the warp builds the row's occupation lists from the
 // string tables, computes the row's single-excitation values (O(nocc) sums
-// each) on all lanes but one and the diagonal on the last lane, then places
-// every entry from the row's alpha and beta tables (binary search of the
-// entry's alpha group) and writes columns and values in order.  Per-warp
+// each) on its lanes, then places every entry from the row's alpha and beta
+// tables (binary search of the entry's alpha group; same-spin doubles and
+// single descriptors precomputed per string) and writes columns and values
+// in order.  The diagonal comes from fci_diag_kernel (one thread per row).
+// Per-warp
 // shared memory: RowState, the alpha group offsets (na ints), the singles
 // (nsg doubles).
 constexpr int kFillRowsPerBlock = 8;
@@ -857,34 +934,19 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
         aoff[t] = __ldg(AO + t);
     __syncwarp();
     const int sa = s.no_a * s.nv_a;
-    for (int t = lane; t < nsg; t += 31) {
-        if (lane == 31)
-            break;
+    for (int t = lane; t < nsg; t += 32)
         sval[t] = exc_value<NW>(p, s, t < sa ? make_exc(s, kSingleA, t, 0) : make_exc(s, kSingleB, t - sa, 0));
-    }
-    double dval = 0.0;
-    if (lane == 31)
-        dval = diagonal(p, s);
-    dval = __shfl_sync(0xffffffffu, dval, 31);
+    const double dval = p.diag[row]; // fci_diag_kernel ran first
     __syncwarp();
     const int64_t start = p.rowptr[row];
     const int len = static_cast<int>(p.rowptr[row + 1] - start);
-    if (lane == 0) {
-        if (p.lower_len)
-            p.lower_len[row] = aoff[__ldg(A.self + ra)] + __ldg(B.self + rb) + 1;
-        p.diag[row] = dval;
-    }
+    if (lane == 0 && p.lower_len)
+        p.lower_len[row] = aoff[__ldg(A.self + ra)] + __ldg(B.self + rb) + 1;
+    const uint16_t *GM = A.gmap + ra * A.glen;
+    const bool idx32 = p.nbasis <= 215; // n^4 < 2^31: 32-bit integral offsets
+    const int nb = p.nbasis;
     for (int t = lane; t < len; t += 32) {
-        // Alpha group g: the last position with aoff[g] <= t.
-        int lo = 0, hi = na - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (aoff[mid] <= t)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        const int g = lo, qpos = t - aoff[g];
+        const int g = __ldg(GM + t), qpos = t - aoff[g];
         const int av = __ldg(AV + g);
         const int tya = av >> 20, ia = av & ((1 << 20) - 1);
         int bk, bv;
@@ -907,20 +969,17 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
             val = sval[ia];
         } else if (tya == 0 && tyb == 1) {
             val = sval[sa + ib];
+        } else if (tya == 0) {
+            val = __ldg(B.dval + rb * B.n2 + ib); // beta double
+        } else if (tya == 2) {
+            val = __ldg(A.dval + ra * A.n2 + ia); // alpha double
         } else {
-            int type, i1 = 0, i2 = 0;
-            if (tya == 0) {
-                type = kDoubleBB;
-                i1 = ib;
-            } else if (tya == 1) {
-                type = kDoubleAB;
-                i1 = ia;
-                i2 = ib;
-            } else {
-                type = kDoubleAA;
-                i1 = ia;
-            }
-            val = exc_value<NW>(p, s, make_exc(s, type, i1, i2));
+            // Opposite-spin double: alpha ii -> jj, beta kk -> ll.
+            const int da = __ldg(A.sdesc + ra * A.n1 + ia), db = __ldg(B.sdesc + rb * B.n1 + ib);
+            const int ii = da & 255, jj = (da >> 8) & 255, kk = db & 255, ll = (db >> 8) & 255;
+            const double g2 = idx32 ? __ldg(p.two_mo + (((ii * nb + kk) * nb + jj) * nb + ll))
+                                    : two_mo_at(p.two_mo, nb, ii, kk, jj, ll);
+            val = apply_phase(((da ^ db) >> 16) & 1 ? -1 : 1, g2);
         }
         p.cols[start + t] = static_cast<int32_t>(col);
         p.vals[start + t] = val;
@@ -1319,6 +1378,10 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
         TA.npad = pad(na);
         TB.npad = pad(nbl);
         TA.nw = TB.nw = NW;
+        TA.n1 = no_a * nv_a;
+        TA.n2 = (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
+        TB.n1 = no_b * nv_b;
+        TB.n2 = (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
         std::vector<void *> mem;
         auto make = [&](StringTables &T, int64_t nstr) -> int {
             int32_t **arrs[] = {&T.key, &T.val, &T.off, &T.sub, &T.subval};
@@ -1330,11 +1393,24 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
             mem.push_back(T.self);
             PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&T.bits), sizeof(uint64_t) * nstr * NW, st));
             mem.push_back(T.bits);
+            PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&T.sdesc), sizeof(int32_t) * nstr * std::max(T.n1, 1), st));
+            mem.push_back(T.sdesc);
+            PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&T.dval), sizeof(double) * nstr * std::max(T.n2, 1), st));
+            mem.push_back(T.dval);
             return PYCI_GPU_OK;
         };
         int rc = make(TA, nstr_a);
         if (!rc && !shared)
             rc = make(TB, nstr_b);
+        TA.glen = uniform_len;
+        if (!rc) {
+            const cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&TA.gmap),
+                                                  sizeof(uint16_t) * nstr_a * uniform_len, st);
+            if (e != cudaSuccess)
+                rc = cuda_status(e, "cudaMallocAsync (string tables)");
+            else
+                mem.push_back(TA.gmap);
+        }
         if (!shared && !rc) {
             string_tables_kernel<NW><<<static_cast<unsigned>(nstr_a), 256, scratch, st>>>(p, 0, TA, nbl, grp1, uniform_len),
                 ::pyci_gpu::note_launch();
@@ -1357,6 +1433,8 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
                 if (e != cudaSuccess)
                     rc = cuda_status(e, "fill shared memory");
             }
+            fci_diag_kernel<NW><<<static_cast<unsigned>((p.nrow + 255) / 256), 256, 0, st>>>(p, TA, TB),
+                ::pyci_gpu::note_launch();
             const int64_t rows_per_launch = chunk * kFillRowsPerBlock;
             for (int64_t r0 = 0; !rc && r0 < p.nrow; r0 += rows_per_launch) {
                 const int64_t nr = (p.nrow - r0 < rows_per_launch) ? p.nrow - r0 : rows_per_launch;
