@@ -87,7 +87,7 @@ def build_library(verbose=False):
                 print(out)
     lib = os.path.join(LIBDIR, LIBNAME)
     if _newer(lib, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"])
+        _run([NVCC] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-lpthread"])
     return lib
 
 

@@ -21,7 +21,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <thread>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -345,35 +347,50 @@ __global__ void seg_reduce_kernel(const double *__restrict__ partial, int pq, co
 }
 
 // out[obase[prob] + j][r] = beta * (same) + sum_{i < vlen[prob]} Y[prob][i * q + j] * V[i][r]
-// for the subset's rows (obase, vlen optional: 0 and p).
+// over the rows of the active tiles whose problem has mask[prob] != 0 (mask,
+// obase, vlen optional: all, 0 and p).  A block takes whole tiles, each
+// inside one problem, and stages that problem's coefficients in shared
+// memory once per tile.
 template<typename TV, typename TO, typename ACC>
 __global__ void __launch_bounds__(256) seg_combine_kernel(const TV *__restrict__ V, int p, int64_t N,
-                                                          const double *__restrict__ Y, int q, double beta, RowSet rs,
-                                                          const int64_t *__restrict__ row0,
-                                                          const int *__restrict__ vlen, const int *__restrict__ obase,
-                                                          TO *__restrict__ out) {
-    for_rows(rs, row0, [&](int prob, int64_t r) {
-        const double *Yp = Y + static_cast<int64_t>(prob) * p * q;
+                                                          const double *__restrict__ Y, int q, double beta,
+                                                          const int64_t *__restrict__ tile_lo,
+                                                          const int64_t *__restrict__ tile_hi,
+                                                          const int *__restrict__ tile_prob, int ntiles,
+                                                          const int *__restrict__ mask, const int *__restrict__ vlen,
+                                                          const int *__restrict__ obase, TO *__restrict__ out) {
+    __shared__ ACC sy[kSegMaxP * kSegMaxQ];
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int prob = tile_prob[t];
+        if (mask && !mask[prob])
+            continue;
         const int plim = vlen ? min(p, vlen[prob]) : p;
-        ACC acc[kSegMaxQ];
-#pragma unroll
-        for (int j = 0; j < kSegMaxQ; ++j)
-            acc[j] = 0;
-        for (int i = 0; i < plim; ++i) {
-            const ACC v = static_cast<ACC>(V[i * N + r]);
+        const double *Yp = Y + static_cast<int64_t>(prob) * p * q;
+        __syncthreads(); // the previous tile's coefficients are no longer read
+        for (int e = threadIdx.x; e < plim * q; e += blockDim.x)
+            sy[e] = static_cast<ACC>(Yp[e]);
+        __syncthreads();
+        const int64_t b0 = obase ? obase[prob] : 0;
+        for (int64_t r = tile_lo[t] + threadIdx.x; r < tile_hi[t]; r += blockDim.x) {
+            ACC acc[kSegMaxQ];
 #pragma unroll
             for (int j = 0; j < kSegMaxQ; ++j)
-                if (j < q)
-                    acc[j] += static_cast<ACC>(__ldg(&Yp[i * q + j])) * v;
-        }
-        const int64_t b0 = obase ? obase[prob] : 0;
+                acc[j] = 0;
+            for (int i = 0; i < plim; ++i) {
+                const ACC v = static_cast<ACC>(V[i * N + r]);
 #pragma unroll
-        for (int j = 0; j < kSegMaxQ; ++j)
-            if (j < q) {
-                TO *o = out + (b0 + j) * N + r;
-                *o = (beta == 0.0) ? static_cast<TO>(acc[j]) : static_cast<TO>(static_cast<ACC>(*o) + acc[j]);
+                for (int j = 0; j < kSegMaxQ; ++j)
+                    if (j < q)
+                        acc[j] += sy[i * q + j] * v;
             }
-    });
+#pragma unroll
+            for (int j = 0; j < kSegMaxQ; ++j)
+                if (j < q) {
+                    TO *o = out + (b0 + j) * N + r;
+                    *o = (beta == 0.0) ? static_cast<TO>(acc[j]) : static_cast<TO>(static_cast<ACC>(*o) + acc[j]);
+                }
+        }
+    }
 }
 
 // dst[j][r] = src[j][r], j < ncols, for the subset's rows.
@@ -458,6 +475,29 @@ __global__ void seg_guess_kernel(T *__restrict__ Tb, int b, int64_t N, RowSet rs
 using namespace pyci_gpu;
 
 namespace {
+
+// f(i) for i in [0, n) on up to 16 host threads (dynamic scheduling): the
+// per-problem Rayleigh-Ritz eigenproblems of one iteration are independent.
+template<typename F>
+void host_parallel_for(int n, F f) {
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int nt = std::min(n, static_cast<int>(std::min(16u, hw)));
+    if (nt <= 1 || n < 4) {
+        for (int i = 0; i < n; ++i)
+            f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    pool.reserve(nt);
+    for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+            for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1))
+                f(i);
+        });
+    for (auto &th : pool)
+        th.join();
+}
 
 // A RowSet in device memory plus its host mirror.
 struct DevRowSet {
@@ -617,20 +657,37 @@ private:
     }
 
     // out[obase + j] = beta out[obase + j] + sum_{i < vlen} Y[prob][i][j] V[i]
-    // (Y host: [P][p][q]) over the rows of rs.
+    // (Y host: [P][p][q]) over the rows of the active problems, or of those
+    // with mask[prob] != 0 (a device array) when mask is given.
     template<typename TV, typename TO, typename ACC>
-    int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out, const DevRowSet &rs,
-                const int *vlen = nullptr, const int *obase = nullptr) {
-        if (p > kSegMaxP * 4 || q > kSegMaxQ) {
-            set_error("batched combine: p = %d, q = %d beyond limits", p, q);
+    int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out,
+                const int *vlen = nullptr, const int *obase = nullptr, const int *mask = nullptr) {
+        if (p > kSegMaxP) {
+            set_error("batched combine: p = %d beyond limits", p);
             return PYCI_GPU_EUNSUPPORTED;
         }
-        if (rs.total == 0)
+        if (ntiles_ == 0)
             return PYCI_GPU_OK;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_coef_, Y.data(), sizeof(double) * Y.size(), cudaMemcpyHostToDevice, st_));
-        seg_combine_kernel<TV, TO, ACC><<<grid(rs.total), 256, 0, st_>>>(V, p, N_, d_coef_, q, beta, rs.view(), d_row0_,
-                                                                          vlen, obase, out),
-            ::pyci_gpu::note_launch();
+        // Output columns in chunks of kSegMaxQ.
+        for (int j0 = 0; j0 < q; j0 += kSegMaxQ) {
+            const int qq = std::min(kSegMaxQ, q - j0);
+            const double *coef = Y.data();
+            std::vector<double> sub;
+            if (qq != q) {
+                sub.resize(static_cast<size_t>(P_) * p * qq);
+                for (int pr = 0; pr < P_; ++pr)
+                    for (int i = 0; i < p; ++i)
+                        for (int j = 0; j < qq; ++j)
+                            sub[(static_cast<size_t>(pr) * p + i) * qq + j] = Y[(static_cast<size_t>(pr) * p + i) * q + j0 + j];
+                coef = sub.data();
+            }
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_coef_, coef, sizeof(double) * P_ * p * qq, cudaMemcpyHostToDevice, st_));
+            const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(ntiles_, ctx_->num_sms * 8)));
+            seg_combine_kernel<TV, TO, ACC><<<nb, 256, 0, st_>>>(V, p, N_, d_coef_, qq, beta, d_tile_lo_, d_tile_hi_,
+                                                                 d_tile_prob_, ntiles_, mask, vlen, obase,
+                                                                 out + static_cast<int64_t>(j0) * N_),
+                ::pyci_gpu::note_launch();
+        }
         return PYCI_GPU_OK;
     }
 
@@ -657,7 +714,7 @@ private:
     DevRowSet act_, sel_;
     int64_t *d_row0_ = nullptr, *d_tile_lo_ = nullptr, *d_tile_hi_ = nullptr;
     int *d_tile_begin_ = nullptr, *d_tile_prob_ = nullptr, *d_sel_ = nullptr, *d_base_ = nullptr, *d_len_ = nullptr;
-    int *d_zero_ = nullptr;
+    int *d_zero_ = nullptr, *d_mask_ = nullptr;
     double *d_partial_ = nullptr, *d_small_ = nullptr, *d_coef_ = nullptr, *d_theta_ = nullptr, *d_diag_ = nullptr;
     BatchOp *d_ops_ = nullptr;
     T *Tnew_ = nullptr, *Wnew_ = nullptr, *Xi_ = nullptr, *Yi_ = nullptr;
@@ -788,11 +845,11 @@ int Batch<T>::cholqr_block(std::vector<int> &use, T *tmp, T *V, std::vector<int>
                 knew[p] = c;
         }
         if (pass == 0) {
-            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, tmp, act_)))
+            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, tmp)))
                 return rc;
             src = tmp;
         } else {
-            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, V, act_, nullptr, d_base_)))
+            if ((rc = combine<T, T, T>(src, b, Y, b, 0.0, V, nullptr, d_base_)))
                 return rc;
         }
     }
@@ -822,7 +879,9 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         hops[p] = BatchOp{ops_[p]->rowptr, ops_[p]->cols, ops_[p]->vals, ops_[p]->hi, ops_[p]->lo, row0_[p], ops_[p]->nrow};
 
     T *V, *W, *X, *AX, *R, *Xk, *Wk, *Xfinal;
-    const int nkeep = std::min(kSegMaxQ, std::max(nt, std::min(mmax - b, 2 * nt)));
+    // Kept at a thick restart: the lowest 4 b Ritz vectors (16 for 4 roots),
+    // leaving room for a full block.
+    const int nkeep = std::max(nt, std::min(mmax - b, 4 * b));
     if ((rc = alloc(&V, static_cast<int64_t>(mmax) * N)) || (rc = alloc(&W, static_cast<int64_t>(mmax) * N)) ||
         (rc = alloc(&X, static_cast<int64_t>(nt) * N)) || (rc = alloc(&AX, static_cast<int64_t>(nt) * N)) ||
         (rc = alloc(&R, static_cast<int64_t>(nt) * N)) || (rc = alloc(&Xk, static_cast<int64_t>(nkeep) * N)) ||
@@ -832,7 +891,7 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         (rc = alloc(&d_tile_lo_, ntiles_all)) || (rc = alloc(&d_tile_hi_, ntiles_all)) ||
         (rc = alloc(&d_tile_prob_, ntiles_all)) || (rc = alloc(&d_tile_begin_, P + 1)) ||
         (rc = alloc(&d_sel_, P * b)) || (rc = alloc(&d_base_, P)) || (rc = alloc(&d_len_, P)) ||
-        (rc = alloc(&d_zero_, P)) || (rc = alloc(&d_partial_, ntiles_all * kSegMaxP * kSegMaxQ)) ||
+        (rc = alloc(&d_zero_, P)) || (rc = alloc(&d_mask_, P)) || (rc = alloc(&d_partial_, ntiles_all * kSegMaxP * kSegMaxQ)) ||
         (rc = alloc(&d_small_, static_cast<int64_t>(P) * kSegMaxP * kSegMaxQ)) ||
         (rc = alloc(&d_coef_, static_cast<int64_t>(P) * mmax * std::max(mmax, kSegMaxQ))) ||
         (rc = alloc(&d_theta_, static_cast<int64_t>(P) * nt)) || (rc = alloc(&d_diag_, N)) || (rc = alloc(&d_ops_, P)) ||
@@ -932,17 +991,18 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             if (active[p])
                 mrr = std::max(mrr, m[p]);
         std::vector<double> Yb(static_cast<size_t>(P) * mrr * nt, 0.0), Yk(static_cast<size_t>(P) * mrr * nkeep, 0.0);
-        for (int p = 0; p < P; ++p) {
+        std::vector<char> rr_failed(P, 0);
+        host_parallel_for(P, [&](int p) {
             if (!active[p])
-                continue;
+                return;
             const int mv = m[p];
             std::vector<double> Gm(static_cast<size_t>(mv) * mv), th, Y;
             for (int i = 0; i < mv; ++i)
                 for (int j = 0; j < mv; ++j)
                     Gm[static_cast<size_t>(i) * mv + j] = G[p][static_cast<size_t>(i) * mmax + j];
             if (!symmetric_eigen(mv, Gm, th, Y)) {
-                set_error("Rayleigh-Ritz eigensolver failed (problem %d)", p);
-                return PYCI_GPU_ENOCONV;
+                rr_failed[p] = 1;
+                return;
             }
             for (int j = 0; j < nt; ++j) {
                 theta_all[p * nt + j] = (j < mv) ? th[j] : 0.0;
@@ -953,9 +1013,14 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             for (int j = 0; j < std::min(nkeep, mv); ++j)
                 for (int i = 0; i < mv; ++i)
                     Yk[(static_cast<size_t>(p) * mrr + i) * nkeep + j] = Y[static_cast<size_t>(i) * mv + j];
-        }
-        if ((rc = upload_ints(d_len_, m)) || (rc = combine<T, T, T>(V, mrr, Yb, nt, 0.0, X, act_, d_len_)) ||
-            (rc = combine<T, T, T>(W, mrr, Yb, nt, 0.0, AX, act_, d_len_)))
+        });
+        for (int p = 0; p < P; ++p)
+            if (rr_failed[p]) {
+                set_error("Rayleigh-Ritz eigensolver failed (problem %d)", p);
+                return PYCI_GPU_ENOCONV;
+            }
+        if ((rc = upload_ints(d_len_, m)) || (rc = combine<T, T, T>(V, mrr, Yb, nt, 0.0, X, d_len_)) ||
+            (rc = combine<T, T, T>(W, mrr, Yb, nt, 0.0, AX, d_len_)))
             return rc;
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta_all.data(), sizeof(double) * P * nt, cudaMemcpyHostToDevice, st_));
         seg_residual_kernel<T><<<grid(act_.total), 256, 0, st_>>>(AX, X, d_theta_, nt, N, act_.view(), d_row0_, R),
@@ -1011,8 +1076,9 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
                 any_restart = true;
             }
         if (any_restart) {
-            if ((rc = set_rowset(sel_, rmask)) || (rc = combine<T, T, T>(V, mrr, Yk, nkeep, 0.0, Xk, sel_, d_len_)) ||
-                (rc = combine<T, T, T>(W, mrr, Yk, nkeep, 0.0, Wk, sel_, d_len_)))
+            if ((rc = set_rowset(sel_, rmask)) || (rc = upload_ints(d_mask_, rmask)) ||
+                (rc = combine<T, T, T>(V, mrr, Yk, nkeep, 0.0, Xk, d_len_, nullptr, d_mask_)) ||
+                (rc = combine<T, T, T>(W, mrr, Yk, nkeep, 0.0, Wk, d_len_, nullptr, d_mask_)))
                 return rc;
             seg_copy_kernel<T><<<grid(sel_.total), 256, 0, st_>>>(Xk, nkeep, N, sel_.view(), d_row0_, V),
                 ::pyci_gpu::note_launch();
@@ -1035,13 +1101,19 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         }
         // Corrections of the lowest unconverged roots (at most b per active
         // problem) into Tnew_.
+        // The block-diagonal product is always b wide, so a problem with fewer
+        // unconverged roots fills its block with the lowest converged ones.
         std::vector<int> sel(static_cast<size_t>(P) * b, -1);
         for (int p = 0; p < P; ++p) {
             int c = 0;
-            if (active[p])
+            if (active[p]) {
                 for (int j = 0; j < nt && c < b; ++j)
                     if (!conv[p * nt + j])
                         sel[p * b + c++] = j;
+                for (int j = 0; j < nt && c < b && j < m[p]; ++j)
+                    if (conv[p * nt + j] && m[p] < ops_[p]->nrow)
+                        sel[p * b + c++] = j;
+            }
             for (int cc = 0; cc < b; ++cc)
                 use[p * b + cc] = (sel[p * b + cc] >= 0) ? 1 : 0;
         }
@@ -1065,7 +1137,7 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
                     for (int i = 0; i < m[p]; ++i)
                         for (int j = 0; j < b; ++j)
                             C[(static_cast<size_t>(p) * mgs + i) * b + j] = -Gc[(static_cast<size_t>(p) * mgs + i) * b + j];
-            if ((rc = combine<T, T, T>(V, mgs, C, b, 1.0, Tnew_, act_, d_len_)))
+            if ((rc = combine<T, T, T>(V, mgs, C, b, 1.0, Tnew_, d_len_)))
                 return rc;
         }
         // Orthonormalise inside each block into the next slots.
@@ -1153,8 +1225,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             evals[static_cast<size_t>(p) * b + c] = (c < n) ? eord[static_cast<size_t>(p) * b + c] + ecore[p] : 0.0;
     }
     // Eigenvectors E = X C and residuals H E - e E in FP64.
-    if ((rc = combine<double, double, double>(X64, b, C, b, 0.0, E64, act_)) ||
-        (rc = combine<double, double, double>(AX64, b, C, b, 0.0, AE64, act_)))
+    if ((rc = combine<double, double, double>(X64, b, C, b, 0.0, E64)) ||
+        (rc = combine<double, double, double>(AX64, b, C, b, 0.0, AE64)))
         return rc;
     PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, eord.data(), sizeof(double) * P * b, cudaMemcpyHostToDevice, st_));
     seg_residual_kernel<double><<<grid(N), 256, 0, st_>>>(AE64, E64, d_theta_, b, N, act_.view(), d_row0_, R64),
@@ -1223,7 +1295,7 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
     }
     PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
     const int64_t iters = (maxiter > 0) ? maxiter : 1000;
-    const int mmax = 32;
+    const int mmax = 64; // per-problem subspace (restarts keep 16)
     if (mode == PYCI_SOLVE_MIXED) {
         for (auto *c : v) {
             int rc = csr_prepare_mixed_device(c, 0);

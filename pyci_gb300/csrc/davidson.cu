@@ -689,9 +689,19 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         }
         // Corrections for at most nw roots per iteration, lowest first: the
         // guard Ritz pairs beyond nw steer the subspace without widening the
-        // SpMM.
+        // SpMM.  In mixed precision a block with fewer unconverged roots is
+        // topped up with the lowest converged ones: the FP32 product is bound
+        // by streaming the matrix, so a narrower block saves little (2
+        // vectors cost ~3/4 of 4) and the extra directions keep improving the
+        // converged roots.  (The FP64 product's cost grows with the width.)
         if (static_cast<int>(todo.size()) > nw)
             todo.resize(nw);
+        if (mixed_ && !all && !full_space && static_cast<int>(todo.size()) < nw) {
+            for (int j = 0; j < b && static_cast<int>(todo.size()) < nw; ++j)
+                if (std::find(todo.begin(), todo.end(), j) == todo.end())
+                    todo.push_back(j);
+            std::sort(todo.begin(), todo.end());
+        }
         if (all) {
             if (!mixed_) {
                 converged = true;
@@ -699,20 +709,26 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 max_res = *std::max_element(rnorm.begin(), rnorm.begin() + nw);
                 break;
             }
-            // FP64 refinement of the Ritz block.
+            // FP64 refinement of the nw wanted Ritz vectors (the guard pairs
+            // only steer the FP32 subspace).
             ++refinements;
+            const int br = nw;
             if (!X64) {
-                if ((rc = alloc(&X64, static_cast<int64_t>(b) * N)) || (rc = alloc(&AX64, static_cast<int64_t>(b) * N)) ||
-                    (rc = alloc(&R64, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi64, N * kMaxQ)) ||
+                if ((rc = alloc(&X64, static_cast<int64_t>(br) * N)) || (rc = alloc(&AX64, static_cast<int64_t>(br) * N)) ||
+                    (rc = alloc(&R64, static_cast<int64_t>(br) * N)) || (rc = alloc(&Xi64, N * kMaxQ)) ||
                     (rc = alloc(&Yi64, N * kMaxQ)))
                     return rc;
             }
+            std::vector<double> Ybr(static_cast<size_t>(m) * br);
+            for (int i = 0; i < m; ++i)
+                for (int j = 0; j < br; ++j)
+                    Ybr[static_cast<size_t>(i) * br + j] = Yb[static_cast<size_t>(i) * b + j];
             // Accumulated in the storage precision: errors in the Ritz
             // vectors enter the refined Rayleigh quotients only to second order.
-            if ((rc = combine<T, double, T>(V, m, Yb, b, 0.0, X64)))
+            if ((rc = combine<T, double, T>(V, m, Ybr, br, 0.0, X64)))
                 return rc;
             // Orthonormalise X64 in FP64 (modified Gram-Schmidt, two passes).
-            for (int j = 0; j < b; ++j) {
+            for (int j = 0; j < br; ++j) {
                 double *xj = X64 + static_cast<int64_t>(j) * N;
                 for (int pass = 0; pass < 2 && j > 0; ++pass) {
                     if ((rc = gram<double>(X64, j, xj, 1, Gc)))
@@ -726,9 +742,9 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                     return rc;
                 scale_kernel<double><<<grid(N), 256, 0, st_>>>(xj, N, 1.0 / std::sqrt(Gc[0])), ::pyci_gpu::note_launch();
             }
-            for (int j0 = 0; j0 < b; j0 += kSpmmChunk) {
+            for (int j0 = 0; j0 < br; j0 += kSpmmChunk) {
                 // FP64-accurate product in FP32 arithmetic (double-float).
-                const int kk = std::min(kSpmmChunk, b - j0);
+                const int kk = std::min(kSpmmChunk, br - j0);
                 const int kp = padded_width(kk);
                 float *xs = reinterpret_cast<float *>(Xi64); // [N][2 kp] floats fit in [N][kMaxQ] doubles
                 pack_split_kernel<<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, xs),
@@ -746,40 +762,35 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 matvecs64_ += kk;
             }
             std::vector<double> G64, th64, Z;
-            if ((rc = gram<double>(X64, b, AX64, b, G64)))
+            if ((rc = gram<double>(X64, br, AX64, br, G64)))
                 return rc;
-            if (!symmetric_eigen(b, G64, th64, Z)) {
+            if (!symmetric_eigen(br, G64, th64, Z)) {
                 set_error("Rayleigh-Ritz eigensolver failed");
                 return PYCI_GPU_ENOCONV;
             }
-            // Rotate X64 and AX64 into the FP64 Ritz basis (via Xr/AXr scratch is
-            // not FP64 for mixed; use R64 as scratch).
-            if ((rc = combine<double, double, double>(X64, b, Z, b, 0.0, R64)))
+            // Rotate X64 and AX64 into the FP64 Ritz basis (R64 as scratch).
+            if ((rc = combine<double, double, double>(X64, br, Z, br, 0.0, R64)))
                 return rc;
-            PYCI_CUDA_TRY(cudaMemcpyAsync(X64, R64, sizeof(double) * b * N, cudaMemcpyDeviceToDevice, st_));
-            if ((rc = combine<double, double, double>(AX64, b, Z, b, 0.0, R64)))
+            PYCI_CUDA_TRY(cudaMemcpyAsync(X64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
+            if ((rc = combine<double, double, double>(AX64, br, Z, br, 0.0, R64)))
                 return rc;
-            PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * b * N, cudaMemcpyDeviceToDevice, st_));
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
-            residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, b, N, R64), ::pyci_gpu::note_launch();
+            PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * br, cudaMemcpyHostToDevice, st_));
+            residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, br, N, R64), ::pyci_gpu::note_launch();
             bool ok64 = true;
             todo.clear();
             max_res = 0.0;
-            for (int j = 0; j < b; ++j) {
-                if ((rc = gram<double>(R64 + static_cast<int64_t>(j) * N, 1, R64 + static_cast<int64_t>(j) * N, 1, Gc)))
-                    return rc;
-                const double r64 = std::sqrt(std::max(Gc[0], 0.0));
+            if ((rc = gram<double>(R64, br, R64, br, Gc)))
+                return rc;
+            for (int j = 0; j < br; ++j) {
+                const double r64 = std::sqrt(std::max(Gc[static_cast<size_t>(j) * br + j], 0.0));
                 const double thr = std::max(tol * std::max(eps23, std::fabs(th64[j])), 2.0 * mixed_floor);
-                if (j < nw)
-                    max_res = std::max(max_res, r64);
+                max_res = std::max(max_res, r64);
                 if (!(r64 <= thr)) {
-                    if (j < nw)
-                        ok64 = false;
+                    ok64 = false;
                     todo.push_back(j);
                 }
             }
-            if (static_cast<int>(todo.size()) > nw)
-                todo.resize(nw);
             if (ok64 || refinements >= 8) {
                 converged = ok64;
                 final_theta = th64;
@@ -787,18 +798,17 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             }
             // Seed the FP32 subspace with the FP64-preconditioned residuals.
             if (m + static_cast<int>(todo.size()) > mmax) {
-                // Collapse onto the FP64 Ritz vectors.
-                convert_kernel<double, T><<<grid(static_cast<int64_t>(b) * N), 256, 0, st_>>>(X64, V, static_cast<int64_t>(b) * N), ::pyci_gpu::note_launch();
-                convert_kernel<double, T><<<grid(static_cast<int64_t>(b) * N), 256, 0, st_>>>(AX64, W, static_cast<int64_t>(b) * N), ::pyci_gpu::note_launch();
-                // X64/AX64 are in the FP64 Ritz basis: the projected matrix is diag(th64).
+                // Collapse onto the b FP32 Ritz vectors of this iteration
+                // (projected matrix diag(theta)).
+                PYCI_CUDA_TRY(cudaMemcpyAsync(V, Xr, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
+                PYCI_CUDA_TRY(cudaMemcpyAsync(W, AXr, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
                 std::fill(G.begin(), G.end(), 0.0);
                 for (int i = 0; i < b; ++i)
-                    for (int j = 0; j < b; ++j)
-                        G[static_cast<size_t>(i) * mmax + j] = (i == j) ? th64[i] : 0.0;
+                    G[static_cast<size_t>(i) * mmax + i] = theta[i];
                 m = b;
                 ++restarts;
             }
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * br, cudaMemcpyHostToDevice, st_));
             int q = 0;
             for (int j : todo) {
                 precondition_kernel<double, T><<<grid(N), 256, 0, st_>>>(R64 + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
