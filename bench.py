@@ -467,8 +467,9 @@ def run_batch(args, world=1, rank=0, local=0):
 
 
 def run_profile_case(args):
-    r"""Profiling driver (for ncu): build one FCI operator and run its SpMM
-    kernels, or only mixed solves, with nothing else in the launch list."""
+    r"""Profiling driver (for ncu): build one FCI (or DOCI) operator and run
+    its SpMM kernels (FP32 k=4, FP64 k=1, double-float k=4), or only mixed
+    solves, with nothing else in the launch list."""
     import torch
     from pyci_gb300 import capi
     from pyci_gb300.synth import synthetic_integrals
@@ -489,9 +490,12 @@ def run_profile_case(args):
         y32 = torch.empty_like(x32)
         x64 = torch.randn((N, 1), dtype=torch.float64, device="cuda")
         y64 = torch.empty_like(x64)
+        xdf = torch.randn((N, 8), dtype=torch.float32, device="cuda")
+        ydf = torch.empty((N, 4), dtype=torch.float64, device="cuda")
         for _ in range(args.reps):
             csr.spmm_device(capi.PREC_FP32, 4, x32.data_ptr(), y32.data_ptr(), ctx.stream)
             csr.spmm_device(capi.PREC_FP64, 1, x64.data_ptr(), y64.data_ptr(), ctx.stream)
+            csr.spmm_device(capi.PREC_FP64_DF, 4, xdf.data_ptr(), ydf.data_ptr(), ctx.stream)
         torch.cuda.synchronize()
     else:
         for _ in range(args.reps):

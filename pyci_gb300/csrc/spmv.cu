@@ -384,7 +384,44 @@ __device__ __forceinline__ void two_sum_acc(float &s, float &c, float p) {
     c = __fadd_rn(c, d);
 }
 
-template<int K, int LANES>
+// Split operand row c: K high parts then K low parts.
+template<int K>
+__device__ __forceinline__ void load_split(const float *__restrict__ xs, int64_t col, float xh[K], float xl[K]) {
+    const float *xr = xs + col * (2 * K);
+    if constexpr (K == 4) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
+        const float4 b = __ldg(reinterpret_cast<const float4 *>(xr) + 1);
+        xh[0] = a.x, xh[1] = a.y, xh[2] = a.z, xh[3] = a.w;
+        xl[0] = b.x, xl[1] = b.y, xl[2] = b.z, xl[3] = b.w;
+    } else if constexpr (K == 2) {
+        const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
+        xh[0] = a.x, xh[1] = a.y;
+        xl[0] = a.z, xl[1] = a.w;
+    } else {
+        const float2 a = __ldg(reinterpret_cast<const float2 *>(xr));
+        xh[0] = a.x;
+        xl[0] = a.y;
+    }
+}
+
+// Adds (vh + vl) (xh + xl) to the double-float sums (s, c).
+template<int K>
+__device__ __forceinline__ void df_term(float vh, float vl, const float xh[K], const float xl[K], float s[K],
+                                        float c[K]) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float p = __fmul_rn(vh, xh[k]);
+        const float err = fmaf(vh, xh[k], -p);
+        const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
+        two_sum_acc(s[k], c[k], p);
+        c[k] = __fadd_rn(c[k], t);
+    }
+}
+
+// MAP 1: lane l takes entries l, l + LANES, ... of the row; MAP 0: each lane
+// takes 4 consecutive entries per step (16-byte loads of columns and of both
+// value halves), so four independent gathers are in flight per lane.
+template<int K, int LANES, int MAP>
 __global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
                                                       const int32_t *__restrict__ cols, const float *__restrict__ hi,
                                                       const float *__restrict__ lo, const float *__restrict__ xs,
@@ -394,36 +431,45 @@ __global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_
     const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
     for (int64_t r = group; r < nrow; r += ngroups) {
         const int64_t start = rowptr[r], end = rowptr[r + 1];
-        float s[K], c[K];
+        float s[K], c[K], xh[K], xl[K];
 #pragma unroll
         for (int k = 0; k < K; ++k)
             s[k] = c[k] = 0.0f;
-        for (int64_t e = start + lane; e < end; e += LANES) {
-            const int64_t col = __ldcs(cols + e);
-            const float vh = __ldcs(hi + e), vl = __ldcs(lo + e);
-            const float *xr = xs + col * (2 * K);
-            float xh[K], xl[K];
-            if constexpr (K == 4) {
-                const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
-                const float4 b = __ldg(reinterpret_cast<const float4 *>(xr) + 1);
-                xh[0] = a.x, xh[1] = a.y, xh[2] = a.z, xh[3] = a.w;
-                xl[0] = b.x, xl[1] = b.y, xl[2] = b.z, xl[3] = b.w;
-            } else if constexpr (K == 2) {
-                const float4 a = __ldg(reinterpret_cast<const float4 *>(xr));
-                xh[0] = a.x, xh[1] = a.y;
-                xl[0] = a.z, xl[1] = a.w;
-            } else {
-                const float2 a = __ldg(reinterpret_cast<const float2 *>(xr));
-                xh[0] = a.x;
-                xl[0] = a.y;
+        if constexpr (MAP == 1) {
+            for (int64_t e = start + lane; e < end; e += LANES) {
+                const int64_t col = __ldcs(cols + e);
+                const float vh = __ldcs(hi + e), vl = __ldcs(lo + e);
+                load_split<K>(xs, col, xh, xl);
+                df_term<K>(vh, vl, xh, xl, s, c);
             }
-#pragma unroll
-            for (int k = 0; k < K; ++k) {
-                const float p = __fmul_rn(vh, xh[k]);
-                const float err = fmaf(vh, xh[k], -p);
-                const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
-                two_sum_acc(s[k], c[k], p);
-                c[k] = __fadd_rn(c[k], t);
+        } else {
+            // Head: entries before the first 4-aligned index; body: 4 per lane
+            // per step; tail.
+            const int64_t a0 = min(end, (start + 3) & ~static_cast<int64_t>(3));
+            const int64_t a1 = max(a0, end & ~static_cast<int64_t>(3));
+            if (start + lane < a0) {
+                const int64_t e = start + lane;
+                load_split<K>(xs, __ldcs(cols + e), xh, xl);
+                df_term<K>(__ldcs(hi + e), __ldcs(lo + e), xh, xl, s, c);
+            }
+            for (int64_t e = a0 + 4 * lane; e < a1; e += 4 * LANES) {
+                const int4 c4 = __ldcs(reinterpret_cast<const int4 *>(cols + e));
+                const float4 h4 = __ldcs(reinterpret_cast<const float4 *>(hi + e));
+                const float4 l4 = __ldcs(reinterpret_cast<const float4 *>(lo + e));
+                float gh[4][K], gl[4][K];
+                load_split<K>(xs, c4.x, gh[0], gl[0]);
+                load_split<K>(xs, c4.y, gh[1], gl[1]);
+                load_split<K>(xs, c4.z, gh[2], gl[2]);
+                load_split<K>(xs, c4.w, gh[3], gl[3]);
+                df_term<K>(h4.x, l4.x, gh[0], gl[0], s, c);
+                df_term<K>(h4.y, l4.y, gh[1], gl[1], s, c);
+                df_term<K>(h4.z, l4.z, gh[2], gl[2], s, c);
+                df_term<K>(h4.w, l4.w, gh[3], gl[3], s, c);
+            }
+            if (a1 + lane < end) {
+                const int64_t e = a1 + lane;
+                load_split<K>(xs, __ldcs(cols + e), xh, xl);
+                df_term<K>(__ldcs(hi + e), __ldcs(lo + e), xh, xl, s, c);
             }
         }
 #pragma unroll
@@ -449,16 +495,19 @@ __global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_
 
 template<int K>
 void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
-    const int lanes = variant_lanes(v);
+    const int lanes = variant_lanes(v), map = variant_map(v);
     const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (csr->nrow * lanes + 255) / 256));
     const unsigned g = static_cast<unsigned>(blocks);
-    if (lanes == 8)
-        spmm_df_kernel<K, 8><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
-    else if (lanes == 16)
-        spmm_df_kernel<K, 16><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
-    else
-        spmm_df_kernel<K, 32><<<g, 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y);
+    const int64_t n = csr->nrow;
+    switch (lanes * 2 + map) {
+    case 16: spmm_df_kernel<K, 8, 0><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    case 17: spmm_df_kernel<K, 8, 1><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    case 32: spmm_df_kernel<K, 16, 0><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    case 33: spmm_df_kernel<K, 16, 1><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    case 64: spmm_df_kernel<K, 32, 0><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    default: spmm_df_kernel<K, 32, 1><<<g, 256, 0, st>>>(n, csr->rowptr, csr->cols, csr->hi, csr->lo, xs, y); break;
+    }
     ::pyci_gpu::note_launch();
 }
 
@@ -476,8 +525,8 @@ inline void launch_df(int v, const pyci_gpu_csr *csr, int K, const float *xs, do
 using namespace pyci_gpu;
 
 // y[N][K] = (hi + lo) x for one split block xs[N][2K] (K = 1, 2 or 4), FP32
-// arithmetic with double-float accumulation; lanes per row tuned on first use
-// (variants 2, 1, 0 = 32, 16, 8 lanes).
+// arithmetic with double-float accumulation; the tile variant (lanes per row x
+// entry mapping, as the other products) is tuned on first use.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
     if (!csr->hi || !csr->lo) {
         set_error("split product needs pyci_gpu_csr_prepare_mixed first");
@@ -501,7 +550,7 @@ int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cuda
             cudaEventCreate(&b);
             float best = 1e30f;
             int best_v = heuristic_variant(csr);
-            for (int v = 0; v < 3; ++v) {
+            for (int v = 0; v < kVariants; ++v) {
                 launch_df(v, csr, K, xs, y, st);
                 cudaEventRecord(a, st);
                 launch_df(v, csr, K, xs, y, st);
