@@ -602,12 +602,9 @@ private:
         return PYCI_GPU_OK;
     }
 
-    // Per-problem small integer table (e.g. subspace sizes) to the device.
-    int upload_ints(int *dst, const std::vector<int> &v) {
-        PYCI_CUDA_TRY(cudaMemcpyAsync(dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice, st_));
-        PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
-        return PYCI_GPU_OK;
-    }
+    // Per-problem small integer table (e.g. subspace sizes) to the device,
+    // asynchronously (pinned staging).
+    int upload_ints(int *dst, const std::vector<int> &v) { return ctx_->ring->upload(dst, v.data(), sizeof(int) * v.size(), st_); }
 
     // G[prob] (p x q, row-major) = A^T B over the active problems' rows; A
     // has p vectors (only the first alen[prob] are read when alen is given),
@@ -681,7 +678,9 @@ private:
                             sub[(static_cast<size_t>(pr) * p + i) * qq + j] = Y[(static_cast<size_t>(pr) * p + i) * q + j0 + j];
                 coef = sub.data();
             }
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_coef_, coef, sizeof(double) * P_ * p * qq, cudaMemcpyHostToDevice, st_));
+            int rc = ctx_->ring->upload(d_coef_, coef, sizeof(double) * P_ * p * qq, st_);
+            if (rc)
+                return rc;
             const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(ntiles_, ctx_->num_sms * 8)));
             seg_combine_kernel<TV, TO, ACC><<<nb, 256, 0, st_>>>(V, p, N_, d_coef_, qq, beta, d_tile_lo_, d_tile_hi_,
                                                                  d_tile_prob_, ntiles_, mask, vlen, obase,
@@ -1022,7 +1021,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         if ((rc = upload_ints(d_len_, m)) || (rc = combine<T, T, T>(V, mrr, Yb, nt, 0.0, X, d_len_)) ||
             (rc = combine<T, T, T>(W, mrr, Yb, nt, 0.0, AX, d_len_)))
             return rc;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta_all.data(), sizeof(double) * P * nt, cudaMemcpyHostToDevice, st_));
+        if ((rc = ctx_->ring->upload(d_theta_, theta_all.data(), sizeof(double) * P * nt, st_)))
+            return rc;
         seg_residual_kernel<T><<<grid(act_.total), 256, 0, st_>>>(AX, X, d_theta_, nt, N, act_.view(), d_row0_, R),
             ::pyci_gpu::note_launch();
         if ((rc = gram<T>(R, nt, R, nt, Gc)))
@@ -1117,7 +1117,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             for (int cc = 0; cc < b; ++cc)
                 use[p * b + cc] = (sel[p * b + cc] >= 0) ? 1 : 0;
         }
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_sel_, sel.data(), sizeof(int) * P * b, cudaMemcpyHostToDevice, st_));
+        if ((rc = ctx_->ring->upload(d_sel_, sel.data(), sizeof(int) * P * b, st_)))
+            return rc;
         seg_precondition_kernel<T><<<grid(act_.total), 256, 0, st_>>>(R, d_theta_, nt, d_sel_, d_diag_, b, N,
                                                                        act_.view(), d_row0_, Tnew_),
             ::pyci_gpu::note_launch();

@@ -104,6 +104,14 @@ int pyci_gpu_ctx_create(int device, pyci_gpu_ctx **out) {
         uint64_t keep = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
+    // Pinned staging for the solvers' coefficient uploads: 16 slots of 512 KB.
+    ctx->ring = new (std::nothrow) PinnedRing();
+    if (!ctx->ring || ctx->ring->init(16, 512 * 1024) != PYCI_GPU_OK) {
+        delete ctx->ring;
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return PYCI_GPU_ENOMEM;
+    }
     *out = ctx;
     return PYCI_GPU_OK;
 }
@@ -113,6 +121,7 @@ int pyci_gpu_ctx_destroy(pyci_gpu_ctx *ctx) {
         return PYCI_GPU_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    delete ctx->ring;
     cudaStreamDestroy(ctx->stream);
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess)

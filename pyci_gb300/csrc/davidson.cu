@@ -378,14 +378,12 @@ private:
                 for (int i = 0; i < pp; ++i)
                     for (int j = 0; j < qq; ++j)
                         sub[static_cast<size_t>(i) * qq + j] = Y[static_cast<size_t>(i0 + i) * q + j0 + j];
-                cudaError_t e = cudaMemcpyAsync(d_coef_, sub.data(), sizeof(double) * sub.size(),
-                                                cudaMemcpyHostToDevice, st_);
-                if (e != cudaSuccess)
-                    return cuda_status(e, "combine coefficients");
+                const int rc = csr_->ctx->ring->upload(d_coef_, sub.data(), sizeof(double) * sub.size(), st_);
+                if (rc)
+                    return rc;
                 combine_kernel<TV, TO, ACC><<<grid(N_), 256, 0, st_>>>(
                     V + static_cast<int64_t>(i0) * N_, pp, N_, d_coef_, qq, (i0 == 0) ? beta : 1.0,
                     out + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
-                // `sub` is pageable: cudaMemcpyAsync has staged it before returning.
             }
         }
         return PYCI_GPU_OK;
@@ -558,6 +556,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         return cuda_status(cudaGetLastError(), "cudaEventCreate");
     gram_blocks_ = static_cast<unsigned>(csr_->ctx->num_sms * 4);
 
+
     T *V, *W, *Xr, *AXr, *R;
     // Vectors kept at a thick restart; leaves room for a full new block.
     // Kept at a thick restart: the lowest max(4 nw, 2 b) Ritz vectors, leaving
@@ -668,7 +667,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 Yb[static_cast<size_t>(i) * b + j] = Y[static_cast<size_t>(i) * m + j];
         if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
             return rc;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+        if ((rc = csr_->ctx->ring->upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
+            return rc;
         residual_kernel<T><<<grid(N), 256, 0, st_>>>(AXr, Xr, d_theta_, b, N, R), ::pyci_gpu::note_launch();
         bool all = true;
         std::vector<int> todo;
@@ -775,7 +775,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if ((rc = combine<double, double, double>(AX64, br, Z, br, 0.0, R64)))
                 return rc;
             PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * br, cudaMemcpyHostToDevice, st_));
+            if ((rc = csr_->ctx->ring->upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
+                return rc;
             residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, br, N, R64), ::pyci_gpu::note_launch();
             bool ok64 = true;
             todo.clear();
@@ -808,7 +809,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 m = b;
                 ++restarts;
             }
-            PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, th64.data(), sizeof(double) * br, cudaMemcpyHostToDevice, st_));
+            if ((rc = csr_->ctx->ring->upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
+                return rc;
             int q = 0;
             for (int j : todo) {
                 precondition_kernel<double, T><<<grid(N), 256, 0, st_>>>(R64 + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
@@ -843,7 +845,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             ++restarts;
         }
         // Preconditioned residuals of the unconverged roots.
-        PYCI_CUDA_TRY(cudaMemcpyAsync(d_theta_, theta.data(), sizeof(double) * b, cudaMemcpyHostToDevice, st_));
+        if ((rc = csr_->ctx->ring->upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
+            return rc;
         int q = 0;
         for (int j : todo) {
             precondition_kernel<T, T><<<grid(N), 256, 0, st_>>>(R + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,

@@ -5,15 +5,21 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 #include <string>
+#include <vector>
 
 #include "pyci_gb300.h"
+
+class PinnedRing;
 
 struct pyci_gpu_ctx {
     int device = 0;
     int num_sms = 0;
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
+    PinnedRing *ring = nullptr; // pinned staging for small uploads (created with the context)
 };
 
 // Device-resident CSR of the CI Hamiltonian.
@@ -111,3 +117,55 @@ __host__ __device__ inline double guess_noise(uint64_t row, uint64_t col) {
     z ^= z >> 31;
     return static_cast<double>(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
+
+// Asynchronous host -> device uploads of small coefficient blocks through a
+// ring of pinned staging buffers.  A cudaMemcpyAsync from pageable memory
+// first synchronises the stream, which would stall the GPU once per upload;
+// from pinned memory it is queued like a kernel.  A slot is reused only after
+// the event recorded behind its previous copy has completed.
+class PinnedRing {
+public:
+    ~PinnedRing() {
+        for (size_t i = 0; i < buf_.size(); ++i) {
+            if (ev_[i]) {
+                cudaEventSynchronize(ev_[i]);
+                cudaEventDestroy(ev_[i]);
+            }
+            if (buf_[i])
+                cudaFreeHost(buf_[i]);
+        }
+    }
+    // nslot buffers of `bytes` each.
+    int init(int nslot, size_t bytes) {
+        bytes_ = bytes;
+        buf_.assign(nslot, nullptr);
+        ev_.assign(nslot, nullptr);
+        for (int i = 0; i < nslot; ++i) {
+            PYCI_CUDA_TRY(cudaMallocHost(&buf_[i], bytes));
+            PYCI_CUDA_TRY(cudaEventCreateWithFlags(&ev_[i], cudaEventDisableTiming));
+        }
+        return PYCI_GPU_OK;
+    }
+    // dst[0..n) = src[0..n) (bytes) on stream st, asynchronously.
+    int upload(void *dst, const void *src, size_t n, cudaStream_t st) {
+        std::lock_guard<std::mutex> lock(mu_);
+        if (buf_.empty() || n > bytes_) {
+            PYCI_CUDA_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st));
+            return PYCI_GPU_OK;
+        }
+        const int s = next_;
+        next_ = (next_ + 1) % static_cast<int>(buf_.size());
+        PYCI_CUDA_TRY(cudaEventSynchronize(ev_[s])); // its previous copy has been consumed
+        std::memcpy(buf_[s], src, n);
+        PYCI_CUDA_TRY(cudaMemcpyAsync(dst, buf_[s], n, cudaMemcpyHostToDevice, st));
+        PYCI_CUDA_TRY(cudaEventRecord(ev_[s], st));
+        return PYCI_GPU_OK;
+    }
+
+private:
+    std::vector<void *> buf_;
+    std::vector<cudaEvent_t> ev_;
+    size_t bytes_ = 0;
+    int next_ = 0;
+    std::mutex mu_;
+};
