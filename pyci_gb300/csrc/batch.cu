@@ -23,6 +23,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <thread>
 #include <cmath>
 #include <cstring>
@@ -476,6 +479,11 @@ using namespace pyci_gpu;
 
 namespace {
 
+// Tile-class tuning results shared by batches of the same shape in this
+// process: key = (value kind, class rows, class stored entries) -> lanes.
+std::mutex g_class_tune_mutex;
+std::map<std::tuple<int, int64_t, int64_t>, int> g_class_tune;
+
 // f(i) for i in [0, n) on up to 16 host threads (dynamic scheduling): the
 // per-problem Rayleigh-Ritz eigenproblems of one iteration are independent.
 template<typename F>
@@ -577,6 +585,13 @@ private:
         int rc;
         if ((rc = set_rowset(act_, mask)))
             return rc;
+        for (int c = 0; c < kClasses; ++c) {
+            std::vector<int> mc(P_, 0);
+            for (int p = 0; p < P_; ++p)
+                mc[p] = mask[p] && cls_of_[p] == c;
+            if ((rc = set_rowset(cls_[c], mc)))
+                return rc;
+        }
         std::vector<int64_t> tlo, thi;
         std::vector<int> tprob, tbeg(P_ + 1, 0);
         const int64_t tile = 8192;
@@ -691,8 +706,30 @@ private:
     }
 
     // W[m_p + j] = H V[m_p + j] (j < b) for every active problem, and the
-    // same products into Wnew_[j]; one graph replay (pack, SpMM, unpack).
+    // same products into Wnew_[j]; one graph replay (pack, one SpMM per tile
+    // class, unpack).
     int apply_block(int prec, T *V, T *W);
+
+    // Block-diagonal product Xi_ -> Yi_ over the rows of rs at `lanes` lanes
+    // per row.
+    void spmm_class(int prec, int lanes, const DevRowSet &rs) {
+        const int64_t rows = std::max<int64_t>(rs.total, 1);
+        const unsigned blocks = static_cast<unsigned>(
+            std::max<int64_t>(1, std::min<int64_t>(ctx_->num_sms * 32, (rows * lanes + 255) / 256)));
+        const RowSet v = rs.view();
+        if (prec == PYCI_PREC_FP32) {
+            if (lanes == 8)
+                batch_spmm_kernel<1, 4, 8, T><<<blocks, 256, 0, st_>>>(d_ops_, v, Xi_, Yi_);
+            else if (lanes == 16)
+                batch_spmm_kernel<1, 4, 16, T><<<blocks, 256, 0, st_>>>(d_ops_, v, Xi_, Yi_);
+            else
+                batch_spmm_kernel<1, 4, 32, T><<<blocks, 256, 0, st_>>>(d_ops_, v, Xi_, Yi_);
+        } else if (prec == PYCI_PREC_FP64_SPLIT) {
+            batch_spmm_kernel<2, 4, 32, T><<<blocks, 256, 0, st_>>>(d_ops_, v, Xi_, Yi_);
+        } else {
+            batch_spmm_kernel<0, 4, 32, T><<<blocks, 256, 0, st_>>>(d_ops_, v, Xi_, Yi_);
+        }
+    }
 
     // Two Cholesky-QR passes of the b vectors in Tnew_ inside each active
     // problem's block: columns with use == 0 are left out, dependent ones are
@@ -711,6 +748,14 @@ private:
     std::vector<void *> allocs_;
     std::vector<int64_t> row0_;
     DevRowSet act_, sel_;
+    // SpMM tile classes: problems grouped by mean row length (nominal 8, 16,
+    // 32 lanes per row); cls_[c] holds the active members of class c and
+    // cls_lanes_[c] the lanes per row the autotuner chose for it.
+    static constexpr int kClasses = 3;
+    DevRowSet cls_[kClasses];
+    std::vector<int> cls_of_;
+    int cls_lanes_[kClasses] = {8, 16, 32};
+    bool cls_tuned_ = false;
     int64_t *d_row0_ = nullptr, *d_tile_lo_ = nullptr, *d_tile_hi_ = nullptr;
     int *d_tile_begin_ = nullptr, *d_tile_prob_ = nullptr, *d_sel_ = nullptr, *d_base_ = nullptr, *d_len_ = nullptr;
     int *d_zero_ = nullptr, *d_mask_ = nullptr;
@@ -736,18 +781,59 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             cudaGraphExecDestroy(graph_exec_);
             graph_exec_ = nullptr;
         }
-        cudaGraph_t g;
-        PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         const RowSet rs = act_.view();
         const unsigned gr = grid(N_);
+        if (!cls_tuned_) {
+            // Autotuner: time each class's product at 8, 16 and 32 lanes per
+            // row (one warm-up + one timed launch each) and keep the fastest.
+            batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
+            cudaEvent_t ea, eb;
+            cudaEventCreate(&ea);
+            cudaEventCreate(&eb);
+            for (int c = 0; c < kClasses; ++c) {
+                if (cls_[c].total == 0)
+                    continue;
+                int64_t cls_nnz = 0;
+                for (int p : cls_[c].members)
+                    cls_nnz += ops_[p]->nnz;
+                const auto key = std::make_tuple(prec, cls_[c].total, cls_nnz);
+                {
+                    std::lock_guard<std::mutex> lock(g_class_tune_mutex);
+                    auto it = g_class_tune.find(key);
+                    if (it != g_class_tune.end()) {
+                        cls_lanes_[c] = it->second;
+                        continue;
+                    }
+                }
+                float best = 1e30f;
+                for (int lanes : {8, 16, 32}) {
+                    for (int rep = 0; rep < 2; ++rep) {
+                        if (rep == 1)
+                            cudaEventRecord(ea, st_);
+                        spmm_class(prec, lanes, cls_[c]);
+                        if (rep == 1)
+                            cudaEventRecord(eb, st_);
+                    }
+                    PYCI_CUDA_TRY(cudaEventSynchronize(eb));
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, ea, eb);
+                    if (ms < best) {
+                        best = ms;
+                        cls_lanes_[c] = lanes;
+                    }
+                }
+                std::lock_guard<std::mutex> lock(g_class_tune_mutex);
+                g_class_tune[key] = cls_lanes_[c];
+            }
+            cudaEventDestroy(ea);
+            cudaEventDestroy(eb);
+            cls_tuned_ = true;
+        }
+        cudaGraph_t g;
+        PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
-        const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ctx_->num_sms * 32, (N_ * 32 + 255) / 256));
-        if (prec == PYCI_PREC_FP32)
-            batch_spmm_kernel<1, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
-        else if (prec == PYCI_PREC_FP64_SPLIT)
-            batch_spmm_kernel<2, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
-        else
-            batch_spmm_kernel<0, 4, 32, T><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, Xi_, Yi_);
+        for (int c = 0; c < kClasses; ++c)
+            spmm_class(prec, cls_lanes_[c], cls_[c]);
         batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, d_base_, rs, d_row0_, W, Wnew_);
         cudaError_t e = cudaStreamEndCapture(st_, &g);
         if (e != cudaSuccess)
@@ -764,9 +850,8 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
     cudaEventCreate(&c);
     cudaEventRecord(a, st_);
     PYCI_CUDA_TRY(cudaGraphLaunch(graph_exec_, st_));
-    ::pyci_gpu::note_launch();
-    ::pyci_gpu::note_launch();
-    ::pyci_gpu::note_launch();
+    for (int i = 0; i < 2 + kClasses; ++i) // pack, one product per class, unpack
+        ::pyci_gpu::note_launch();
     cudaEventRecord(c, st_);
     PYCI_CUDA_TRY(cudaEventSynchronize(c));
     float ms = 0.0f;
@@ -894,7 +979,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         (rc = alloc(&d_small_, static_cast<int64_t>(P) * kSegMaxP * kSegMaxQ)) ||
         (rc = alloc(&d_coef_, static_cast<int64_t>(P) * mmax * std::max(mmax, kSegMaxQ))) ||
         (rc = alloc(&d_theta_, static_cast<int64_t>(P) * nt)) || (rc = alloc(&d_diag_, N)) || (rc = alloc(&d_ops_, P)) ||
-        (rc = alloc_rowset(act_)) || (rc = alloc_rowset(sel_)))
+        (rc = alloc_rowset(act_)) || (rc = alloc_rowset(sel_)) || (rc = alloc_rowset(cls_[0])) ||
+        (rc = alloc_rowset(cls_[1])) || (rc = alloc_rowset(cls_[2])))
         return rc;
     // Every vector buffer starts at zero, so slots a problem has not written
     // yet hold finite values wherever a kernel reads them.
@@ -910,6 +996,11 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
     for (int p = 0; p < P; ++p)
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_diag_ + row0_[p], ops_[p]->diag, sizeof(double) * ops_[p]->nrow,
                                       cudaMemcpyDeviceToDevice, st_));
+    cls_of_.assign(P, 0);
+    for (int p = 0; p < P; ++p) {
+        const double avg = ops_[p]->nrow ? static_cast<double>(ops_[p]->nnz) / ops_[p]->nrow : 0.0;
+        cls_of_[p] = avg >= 96 ? 2 : (avg >= 24 ? 1 : 0);
+    }
     std::vector<int> active(P, 1);
     if ((rc = set_active(active)))
         return rc;

@@ -312,10 +312,10 @@ public:
     ~Davidson() {
         for (void *p : allocs_)
             cudaFreeAsync(p, st_);
-        if (ev0_)
-            cudaEventDestroy(ev0_);
-        if (ev1_)
-            cudaEventDestroy(ev1_);
+        for (auto &pr : timers_) {
+            cudaEventDestroy(pr.first);
+            cudaEventDestroy(pr.second);
+        }
         cudaStreamSynchronize(st_);
     }
 
@@ -395,18 +395,12 @@ private:
             const int kk = std::min(kSpmmChunk, k - j0);
             const int kp = padded_width(kk);
             pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_), ::pyci_gpu::note_launch();
-            cudaEventRecord(ev0_, st_);
+            const size_t tk = timer_begin();
             int rc = csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
             if (rc)
                 return rc;
-            cudaEventRecord(ev1_, st_);
+            timer_end(tk);
             unpack_kernel<T><<<grid(N_), 256, 0, st_>>>(Yi_, N_, kk, kp, W + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
-            cudaError_t e = cudaEventSynchronize(ev1_);
-            if (e != cudaSuccess)
-                return cuda_status(e, "SpMM");
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, ev0_, ev1_);
-            spmm_ms_ += ms;
             matvecs_ += kk;
         }
         return PYCI_GPU_OK;
@@ -424,8 +418,27 @@ private:
     int64_t N_, nroot_, nwant_, mmax_;
     bool mixed_;
     std::vector<void *> allocs_;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
-    double spmm_ms_ = 0.0;
+    // SpMM timing: an event pair per product, read once at the end of the
+    // solve (no synchronisation per product).
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> timers_;
+    size_t timer_begin() {
+        std::pair<cudaEvent_t, cudaEvent_t> pr{nullptr, nullptr};
+        cudaEventCreate(&pr.first);
+        cudaEventCreate(&pr.second);
+        cudaEventRecord(pr.first, st_);
+        timers_.push_back(pr);
+        return timers_.size() - 1;
+    }
+    void timer_end(size_t k) { cudaEventRecord(timers_[k].second, st_); }
+    double timed_total_ms() {
+        double total = 0.0;
+        for (auto &pr : timers_) {
+            float ms = 0.0f;
+            if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+                total += ms;
+        }
+        return total;
+    }
     int64_t matvecs_ = 0, matvecs64_ = 0;
     unsigned gram_blocks_ = 1;
     T *Xi_ = nullptr, *Yi_ = nullptr, *Sb_ = nullptr;
@@ -435,55 +448,107 @@ private:
 template<typename T>
 int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
     // Block classical Gram-Schmidt against V[0..m) (two passes), then two
-    // Cholesky-QR passes inside the block: 4 small Gram products per call
-    // instead of one per vector.  A near-singular block falls back to the
-    // vector-by-vector path, which drops dependent directions.
+    // Cholesky-QR passes inside the block.  The block T sits right after
+    // V[0..m), so the second Gram-Schmidt pass's product [V T]^T T also gives
+    // T^T T; after that pass T'^T T' = T^T T - C2^T C2 (C2 = V^T T, small), so
+    // the first Cholesky-QR needs no product of its own and one combination
+    // applies both: 3 Gram products (host synchronisations) per call.  A
+    // near-singular block falls back to the vector-by-vector path, which drops
+    // dependent directions.
     T *Tb = V + static_cast<int64_t>(m) * N_;
     std::vector<double> C, S;
     int rc;
+    const double piv_tol = mixed_ ? 1e-6 : 1e-14;
+    // Cholesky S = L L^T and Linv = L^{-1}; false when S is not safely positive definite.
+    auto cholesky_inv = [&](const std::vector<double> &Sm, std::vector<double> &Linv) -> bool {
+        std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
+        for (int j = 0; j < k; ++j) {
+            double d = Sm[static_cast<size_t>(j) * k + j];
+            for (int t = 0; t < j; ++t)
+                d -= L[static_cast<size_t>(j) * k + t] * L[static_cast<size_t>(j) * k + t];
+            if (!(d > piv_tol * Sm[static_cast<size_t>(j) * k + j]) || !(d > 0.0))
+                return false;
+            L[static_cast<size_t>(j) * k + j] = std::sqrt(d);
+            for (int i = j + 1; i < k; ++i) {
+                double x = Sm[static_cast<size_t>(i) * k + j];
+                for (int t = 0; t < j; ++t)
+                    x -= L[static_cast<size_t>(i) * k + t] * L[static_cast<size_t>(j) * k + t];
+                L[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(j) * k + j];
+            }
+        }
+        Linv.assign(static_cast<size_t>(k) * k, 0.0);
+        for (int j = 0; j < k; ++j) {
+            Linv[static_cast<size_t>(j) * k + j] = 1.0 / L[static_cast<size_t>(j) * k + j];
+            for (int i = j + 1; i < k; ++i) {
+                double x = 0.0;
+                for (int t = j; t < i; ++t)
+                    x -= L[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(t) * k + j];
+                Linv[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(i) * k + i];
+            }
+        }
+        return true;
+    };
     if (k > 1 && k <= kMaxQ) {
-        for (int pass = 0; pass < 2 && m > 0; ++pass) {
+        bool ok = true;
+        int passes_left = 2; // Cholesky-QR passes still to do
+        if (m > 0) {
+            // Pass 1.
             if ((rc = gram<T>(V, m, Tb, k, C)))
                 return rc;
             for (double &c : C)
                 c = -c;
             if ((rc = combine<T, T, T>(V, m, C, k, 1.0, Tb)))
                 return rc;
+            // Pass 2 fused with the first Cholesky-QR.
+            if ((rc = gram<T>(V, m + k, Tb, k, C)))
+                return rc;
+            std::vector<double> Sm(static_cast<size_t>(k) * k);
+            double cmax = 0.0, smin = std::numeric_limits<double>::infinity();
+            for (int i = 0; i < k; ++i)
+                smin = std::min(smin, C[static_cast<size_t>(m + i) * k + i]);
+            for (size_t e = 0; e < static_cast<size_t>(m) * k; ++e)
+                cmax = std::max(cmax, std::fabs(C[e]));
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) {
+                    double x = C[static_cast<size_t>(m + i) * k + j];
+                    for (int t = 0; t < m; ++t)
+                        x -= C[static_cast<size_t>(t) * k + i] * C[static_cast<size_t>(t) * k + j];
+                    Sm[static_cast<size_t>(i) * k + j] = x;
+                }
+            std::vector<double> Linv;
+            if (smin > 0.0 && cmax * cmax <= 1e-4 * smin && cholesky_inv(Sm, Linv)) {
+                // new = (T - V C2) L^{-T}: rows i < m: -(C2 Linv^T)[i][j]; rows m + i: Linv[j][i].
+                std::vector<double> Y(static_cast<size_t>(m + k) * k, 0.0);
+                for (int i = 0; i < m; ++i)
+                    for (int j = 0; j < k; ++j) {
+                        double x = 0.0;
+                        for (int t = 0; t < k; ++t)
+                            x -= C[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(j) * k + t];
+                        Y[static_cast<size_t>(i) * k + j] = x;
+                    }
+                for (int i = 0; i < k; ++i)
+                    for (int j = 0; j < k; ++j)
+                        Y[static_cast<size_t>(m + i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
+                if ((rc = combine<T, T, T>(V, m + k, Y, k, 0.0, Sb_)))
+                    return rc;
+                PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
+                passes_left = 1;
+            } else {
+                // Plain second pass (the block was far from orthogonal to V).
+                for (size_t e = 0; e < static_cast<size_t>(m) * k; ++e)
+                    C[e] = -C[e];
+                C.resize(static_cast<size_t>(m) * k);
+                if ((rc = combine<T, T, T>(V, m, C, k, 1.0, Tb)))
+                    return rc;
+            }
         }
-        const double piv_tol = mixed_ ? 1e-6 : 1e-14;
-        bool ok = true;
-        for (int pass = 0; pass < 2 && ok; ++pass) {
+        for (int pass = 0; pass < passes_left && ok; ++pass) {
             if ((rc = gram<T>(Tb, k, Tb, k, S)))
                 return rc;
-            // S = L L^T; coefficients of T L^{-T}: column j = row j of L^{-1}.
-            std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
-            for (int j = 0; j < k && ok; ++j) {
-                double d = S[static_cast<size_t>(j) * k + j];
-                for (int t = 0; t < j; ++t)
-                    d -= L[static_cast<size_t>(j) * k + t] * L[static_cast<size_t>(j) * k + t];
-                if (!(d > piv_tol * S[static_cast<size_t>(j) * k + j]) || !(d > 0.0)) {
-                    ok = false;
-                    break;
-                }
-                L[static_cast<size_t>(j) * k + j] = std::sqrt(d);
-                for (int i = j + 1; i < k; ++i) {
-                    double x = S[static_cast<size_t>(i) * k + j];
-                    for (int t = 0; t < j; ++t)
-                        x -= L[static_cast<size_t>(i) * k + t] * L[static_cast<size_t>(j) * k + t];
-                    L[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(j) * k + j];
-                }
-            }
-            if (!ok)
+            std::vector<double> Linv;
+            if (!cholesky_inv(S, Linv)) {
+                ok = false;
                 break;
-            std::vector<double> Linv(static_cast<size_t>(k) * k, 0.0);
-            for (int j = 0; j < k; ++j) {
-                Linv[static_cast<size_t>(j) * k + j] = 1.0 / L[static_cast<size_t>(j) * k + j];
-                for (int i = j + 1; i < k; ++i) {
-                    double x = 0.0;
-                    for (int t = j; t < i; ++t)
-                        x -= L[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(t) * k + j];
-                    Linv[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(i) * k + i];
-                }
             }
             // new_j = sum_i Linv[j][i] T_i  ->  coefficient matrix Y[i][j] = Linv[j][i]
             std::vector<double> Y(static_cast<size_t>(k) * k);
@@ -552,8 +617,6 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     const bool full_space = (N <= mmax);
     const int prec = mixed_ ? PYCI_PREC_FP32 : PYCI_PREC_FP64;
     int rc;
-    if (cudaEventCreate(&ev0_) != cudaSuccess || cudaEventCreate(&ev1_) != cudaSuccess)
-        return cuda_status(cudaGetLastError(), "cudaEventCreate");
     gram_blocks_ = static_cast<unsigned>(csr_->ctx->num_sms * 4);
 
 
@@ -749,15 +812,11 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 float *xs = reinterpret_cast<float *>(Xi64); // [N][2 kp] floats fit in [N][kMaxQ] doubles
                 pack_split_kernel<<<grid(N), 256, 0, st_>>>(X64 + static_cast<int64_t>(j0) * N, N, kk, kp, xs),
                     ::pyci_gpu::note_launch();
-                cudaEventRecord(ev0_, st_);
+                const size_t tk = timer_begin();
                 if ((rc = csr_spmm_df(csr_, kp, xs, Yi64, st_)))
                     return rc;
-                cudaEventRecord(ev1_, st_);
+                timer_end(tk);
                 unpack_kernel<double><<<grid(N), 256, 0, st_>>>(Yi64, N, kk, kp, AX64 + static_cast<int64_t>(j0) * N), ::pyci_gpu::note_launch();
-                PYCI_CUDA_TRY(cudaEventSynchronize(ev1_));
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, ev0_, ev1_);
-                spmm_ms_ += ms;
                 matvecs_ += kk;
                 matvecs64_ += kk;
             }
@@ -887,7 +946,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         stats->restarts = restarts;
         stats->refinements = refinements;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-        stats->seconds_spmm = spmm_ms_ * 1e-3;
+        stats->seconds_spmm = timed_total_ms() * 1e-3;
         stats->max_residual = max_res;
     }
     return PYCI_GPU_OK;
