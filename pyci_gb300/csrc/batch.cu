@@ -184,9 +184,8 @@ __global__ void __launch_bounds__(256) batch_spmm_df_kernel(const BatchOp *__res
 #pragma unroll
         for (int k = 0; k < K; ++k)
             s[k] = c[k] = 0.0f;
-        for (int64_t e = start + lane; e < end; e += LANES) {
-            const int64_t col = __ldcs(op.cols + e);
-            const float vh = __ldcs(op.hi + e), vl = __ldcs(op.lo + e);
+        // One term: (vh + vl) (xh + xl) of column col into the double-float sums.
+        auto term = [&](int64_t col, float vh, float vl) {
             const float4 a = __ldg(reinterpret_cast<const float4 *>(xb + col * (2 * K)));
             const float4 b = __ldg(reinterpret_cast<const float4 *>(xb + col * (2 * K)) + 1);
             const float xh[K] = {a.x, a.y, a.z, a.w}, xl[K] = {b.x, b.y, b.z, b.w};
@@ -198,7 +197,24 @@ __global__ void __launch_bounds__(256) batch_spmm_df_kernel(const BatchOp *__res
                 df_acc(s[k], c[k], p);
                 c[k] = __fadd_rn(c[k], t);
             }
+        };
+        // Head up to a 4-aligned index, body of 4 entries per lane per step
+        // (16-byte loads of columns and both value halves), tail.
+        const int64_t a0 = min(end, (start + 3) & ~static_cast<int64_t>(3));
+        const int64_t a1 = max(a0, end & ~static_cast<int64_t>(3));
+        if (start + lane < a0)
+            term(__ldcs(op.cols + start + lane), __ldcs(op.hi + start + lane), __ldcs(op.lo + start + lane));
+        for (int64_t e = a0 + 4 * lane; e < a1; e += 4 * LANES) {
+            const int4 c4 = __ldcs(reinterpret_cast<const int4 *>(op.cols + e));
+            const float4 h4 = __ldcs(reinterpret_cast<const float4 *>(op.hi + e));
+            const float4 l4 = __ldcs(reinterpret_cast<const float4 *>(op.lo + e));
+            term(c4.x, h4.x, l4.x);
+            term(c4.y, h4.y, l4.y);
+            term(c4.z, h4.z, l4.z);
+            term(c4.w, h4.w, l4.w);
         }
+        if (a1 + lane < end)
+            term(__ldcs(op.cols + a1 + lane), __ldcs(op.hi + a1 + lane), __ldcs(op.lo + a1 + lane));
 #pragma unroll
         for (int k = 0; k < K; ++k) {
 #pragma unroll
@@ -1260,7 +1276,7 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
             // FP64-accurate products in FP32 arithmetic from high + low values.
             float *xs = reinterpret_cast<float *>(Xi64); // [N][8] floats fit in [N][4] doubles
             batch_pack_split_kernel<<<gr, 256, 0, st_>>>(X64, N, rs, d_row0_, xs), ::pyci_gpu::note_launch();
-            batch_spmm_df_kernel<32><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, xs, Yi64),
+            batch_spmm_df_kernel<16><<<static_cast<unsigned>(blocks), 256, 0, st_>>>(d_ops_, rs, xs, Yi64),
                 ::pyci_gpu::note_launch();
         } else {
             batch_pack_kernel<double, 4><<<gr, 256, 0, st_>>>(X64, N, d_zero_, rs, d_row0_, Xi64), ::pyci_gpu::note_launch();

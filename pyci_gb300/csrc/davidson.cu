@@ -459,7 +459,9 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
     std::vector<double> C, S;
     int rc;
     const double piv_tol = mixed_ ? 1e-6 : 1e-14;
-    // Cholesky S = L L^T and Linv = L^{-1}; false when S is not safely positive definite.
+    // Cholesky S = L L^T and Linv = L^{-1}; false when S is not safely positive
+    // definite.  kappa: (max L_jj / min L_jj)^2, a cheap estimate of cond(S).
+    double kappa = 0.0;
     auto cholesky_inv = [&](const std::vector<double> &Sm, std::vector<double> &Linv) -> bool {
         std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
         for (int j = 0; j < k; ++j) {
@@ -476,6 +478,12 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
                 L[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(j) * k + j];
             }
         }
+        double lmax = 0.0, lmin = std::numeric_limits<double>::infinity();
+        for (int j = 0; j < k; ++j) {
+            lmax = std::max(lmax, L[static_cast<size_t>(j) * k + j]);
+            lmin = std::min(lmin, L[static_cast<size_t>(j) * k + j]);
+        }
+        kappa = (lmax / lmin) * (lmax / lmin);
         Linv.assign(static_cast<size_t>(k) * k, 0.0);
         for (int j = 0; j < k; ++j) {
             Linv[static_cast<size_t>(j) * k + j] = 1.0 / L[static_cast<size_t>(j) * k + j];
@@ -532,7 +540,10 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
                 if ((rc = combine<T, T, T>(V, m + k, Y, k, 0.0, Sb_)))
                     return rc;
                 PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
-                passes_left = 1;
+                // A well-conditioned block is orthonormal to ~kappa * eps
+                // after one pass: skip the second (one product and one
+                // synchronisation fewer per iteration).
+                passes_left = (kappa < 10.0) ? 0 : 1;
             } else {
                 // Plain second pass (the block was far from orthogonal to V).
                 for (size_t e = 0; e < static_cast<size_t>(m) * k; ++e)
