@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["build.cu", "spmv.cu", "ops.cu", "davidson.cu", "batch.cu", "capi.cu", "noalloc.cu"]
 CPP_SOURCES = ["dense.cpp"]
-HEADERS = ["internal.h", "detops.cuh", "dense.h"]
+HEADERS = ["internal.h", "detops.cuh", "dense.h", "split_bits.h"]
 
 
 def _newer(target, deps):

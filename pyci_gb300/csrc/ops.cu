@@ -8,6 +8,7 @@
 
 #include "detops.cuh"
 #include "internal.h"
+#include "split_bits.h"
 
 namespace pyci_gpu {
 
@@ -75,14 +76,41 @@ __global__ void digest_kernel(int64_t nrow, const int64_t *rowptr, const int32_t
     }
 }
 
-__global__ void split_kernel(int64_t n, const double *v, float *hi, float *lo) {
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const double d = v[i];
-        const float h = static_cast<float>(d);
-        hi[i] = h;
-        lo[i] = static_cast<float>(d - static_cast<double>(h));
+// hi[i] = fl32(v[i]), lo[i] = fl32(v[i] - hi[i]) by integer arithmetic
+// (split_bits.h).  Each thread handles 4 x 2 values per step: four
+// independent 16-byte loads in flight before any arithmetic, 8-byte stores.
+__global__ void split_kernel(int64_t n, const double *__restrict__ v, float *__restrict__ hi, float *__restrict__ lo) {
+    constexpr int U = 4;
+    const int64_t n2 = n / 2;                 // double2 elements
+    const int64_t nb = n2 / U;                // full groups of U
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const double2 *v2 = reinterpret_cast<const double2 *>(v);
+    float2 *h2 = reinterpret_cast<float2 *>(hi), *l2 = reinterpret_cast<float2 *>(lo);
+    for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < nb; g += stride) {
+        double2 d[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            d[u] = __ldcs(v2 + g + u * nb);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            float2 h, l;
+            split_hi_lo(d[u].x, h.x, l.x);
+            split_hi_lo(d[u].y, h.y, l.y);
+            h2[g + u * nb] = h;
+            l2[g + u * nb] = l;
+        }
     }
+    // Leftover double2 elements and a final odd value.
+    for (int64_t i = U * nb + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n2; i += stride) {
+        const double2 d = v2[i];
+        float2 h, l;
+        split_hi_lo(d.x, h.x, l.x);
+        split_hi_lo(d.y, h.y, l.y);
+        h2[i] = h;
+        l2[i] = l;
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+        split_hi_lo(v[n - 1], hi[n - 1], lo[n - 1]);
 }
 
 // Colex unranking into an arbitrary number of words (pyci/src/common.cpp:139-153).
