@@ -824,6 +824,218 @@ __device__ __forceinline__ int next_bit(const uint64_t *w, int from) {
     return -1;
 }
 
+// Ascending occupied and virtual orbital lists of one string, built by a
+// warp: lane j tests orbital o0 + j, a ballot gives each list position.
+template<int NW>
+__device__ __forceinline__ void warp_lists(const uint64_t *bits, int nbasis, int16_t *occ, int16_t *vir, int &no,
+                                           int &nv) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int cno = 0, cnv = 0;
+    for (int o0 = 0; o0 < nbasis; o0 += 32) {
+        const int o = o0 + lane;
+        const bool valid = o < nbasis;
+        const bool in = valid && ((bits[o >> 6] >> (o & 63)) & 1ULL);
+        const unsigned mo = __ballot_sync(0xffffffffu, in), mv = __ballot_sync(0xffffffffu, valid && !in);
+        if (in && cno + __popc(mo & below) < kMaxOcc)
+            occ[cno + __popc(mo & below)] = static_cast<int16_t>(o);
+        else if (valid && !in && cnv + __popc(mv & below) < kMaxVir)
+            vir[cnv + __popc(mv & below)] = static_cast<int16_t>(o);
+        cno += __popc(mo);
+        cnv += __popc(mv);
+    }
+    no = cno;
+    nv = cnv;
+}
+
+// DOCI diagonal of every row of a full colex space, one thread per row, in
+// diagonal()'s summation order: for each occupied pair k (ascending),
+// v1 += v_kk, v2 += h_k, then v2 += w_kj for each later occupied j; the
+// element is v1 + 2 v2.
+template<int NW>
+__global__ void doci_diag_kernel(BuildParams p) {
+    const int64_t row = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (row >= p.nrow)
+        return;
+    uint64_t a[NW];
+    unrank_colex<NW>(row, p.nbasis, p.nocc_up, p.binom, p.ldk, a);
+    const int n = p.nbasis;
+    double v1 = 0.0, v2 = 0.0;
+    for (int k = next_bit<NW>(a, 0); k >= 0; k = next_bit<NW>(a, k + 1)) {
+        v1 += __ldg(&p.v[k * (n + 1)]);
+        v2 += __ldg(&p.h[k]);
+        for (int j = next_bit<NW>(a, k + 1); j >= 0; j = next_bit<NW>(a, j + 1))
+            v2 += __ldg(&p.w[k * n + j]);
+    }
+    p.diag[row] = v1 + v2 * 2;
+}
+
+// Inclusive prefix sum of v[0..n) in shared memory by one warp (32-wide
+// shuffle scans with a running carry).
+__device__ __forceinline__ void warp_inclusive_scan(int *v, int n) {
+    const int lane = threadIdx.x & 31;
+    int carry = 0;
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        int x = (i < n) ? v[i] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o)
+                x += y;
+        }
+        if (i < n)
+            v[i] = x + carry;
+        carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    __syncwarp();
+}
+
+// Full-space DOCI rows, one warp per row, each warp taking kDociRowsPerWarp
+// consecutive rows (8 warps per block), with no block-wide barriers after
+// the binomial table is staged.
+//
+// Colex order of same-size subsets is the numeric order of their bitmasks,
+// so the pair moves i -> a of a string s sort by 2^a - 2^i: first every move
+// with a < i, grouped by i descending and a ascending within a group; then s
+// itself (the diagonal); then every move with a > i, grouped by a ascending
+// and i descending within a group.  Prefix counts of the groups place any
+// output position directly: lanes walk the row's positions in order (no
+// sort, coalesced writes), rank each excited string (colex) and take its
+// element v_ia.  Later strings of a warp's run follow by Gosper's step (next
+// larger mask with the same popcount) for one-word strings.
+constexpr int kDociRowsPerWarp = 4;
+constexpr int kDociBinomSmem = 1024; // binomial-table entries staged in shared memory
+
+template<int NW>
+__global__ void __launch_bounds__(256) fill_doci_warp_kernel(BuildParams p, int64_t row0) {
+    __shared__ int16_t occ_s[8][kMaxOcc], vir_s[8][kMaxVir];
+    __shared__ int negc[8][kMaxOcc + 1], posc[8][kMaxVir + 1];
+    __shared__ int64_t binom_s[kDociBinomSmem];
+    const int nbin = (p.nbasis + 1) * p.ldk;
+    const bool bsm = nbin <= kDociBinomSmem;
+    if (bsm)
+        for (int t = threadIdx.x; t < nbin; t += blockDim.x)
+            binom_s[t] = p.binom[t];
+    __syncthreads();
+    const int64_t *binom = bsm ? binom_s : p.binom;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t first = row0 + (static_cast<int64_t>(blockIdx.x) * 8 + warp) * kDociRowsPerWarp;
+    const int n = p.nbasis;
+    int16_t *occ = occ_s[warp], *vir = vir_s[warp];
+    int *nc_ = negc[warp], *pc_ = posc[warp];
+    uint64_t bits[NW];
+    for (int rr = 0; rr < kDociRowsPerWarp; ++rr) {
+        const int64_t row = first + rr;
+        if (row >= p.nrow)
+            return;
+        if (rr == 0 || NW > 1) {
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                bits[w] = 0;
+            int64_t rank = row;
+            int pp = n - 1;
+            for (int j = p.nocc_up; j >= 1; --j) {
+                while (pp >= 0 && binom[pp * p.ldk + j] > rank)
+                    --pp;
+                if (pp < 0)
+                    break;
+                bits[pp >> 6] |= 1ULL << (pp & 63);
+                rank -= binom[pp * p.ldk + j];
+                --pp;
+            }
+        } else {
+            const uint64_t x = bits[0], c = x & (~x + 1), r = x + c;
+            bits[0] = (((r ^ x) >> 2) >> (__ffsll(static_cast<long long>(c)) - 1)) | r;
+        }
+        int no, nv;
+        __syncwarp();
+        warp_lists<NW>(bits, n, occ, vir, no, nv);
+        __syncwarp();
+        // Group sizes: a < i moves of occupied occ[no-1-j] (descending j order):
+        // virtuals below it = occ - index; a > i moves into vir[u]: occupied
+        // below it = vir - index.  Slot 0 holds the exclusive start.
+        for (int j = lane; j < no; j += 32) {
+            const int t = no - 1 - j;
+            nc_[j + 1] = occ[t] - t;
+        }
+        for (int u = lane; u < nv; u += 32)
+            pc_[u + 1] = vir[u] - u;
+        if (lane == 0)
+            nc_[0] = pc_[0] = 0;
+        __syncwarp();
+        warp_inclusive_scan(nc_ + 1, no);
+        warp_inclusive_scan(pc_ + 1, nv);
+        const int nneg = nc_[no];
+        const int64_t start = p.rowptr[row];
+        const int len = static_cast<int>(p.rowptr[row + 1] - start);
+        if (lane == 0) {
+            if (len != no * nv + 1)
+                atomicExch(p.error, 5);
+            if (p.lower_len)
+                p.lower_len[row] = nneg + 1;
+        }
+        for (int pos = lane; pos < len; pos += 32) {
+            int32_t col;
+            double val;
+            if (pos == nneg) {
+                col = static_cast<int32_t>(row);
+                val = p.diag[row]; // doci_diag_kernel ran first
+            } else {
+                int ii, aa;
+                if (pos < nneg) {
+                    int lo = 0, hi = no - 1; // last j with nc_[j] <= pos
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (nc_[mid] <= pos)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
+                    }
+                    ii = occ[no - 1 - lo];
+                    aa = vir[pos - nc_[lo]];
+                } else {
+                    const int q = pos - nneg - 1;
+                    int lo = 0, hi = nv - 1; // last u with pc_[u] <= q
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (pc_[mid] <= q)
+                            lo = mid;
+                        else
+                            hi = mid - 1;
+                    }
+                    aa = vir[lo];
+                    const int below = pc_[lo + 1] - pc_[lo]; // occupied below aa
+                    ii = occ[below - 1 - (q - pc_[lo])];
+                }
+                uint64_t d[NW];
+#pragma unroll
+                for (int w = 0; w < NW; ++w)
+                    d[w] = bits[w];
+                flip(d, ii);
+                flip(d, aa);
+                int64_t r = 0;
+                int cnt = 0;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    uint64_t x = d[w];
+                    while (x) {
+                        const int pb = __ffsll(static_cast<long long>(x)) - 1 + 64 * w;
+                        ++cnt;
+                        r += binom[pb * p.ldk + cnt];
+                        x &= x - 1;
+                    }
+                }
+                col = static_cast<int32_t>(r);
+                val = __ldg(&p.v[ii * n + aa]);
+            }
+            p.cols[start + pos] = col;
+            p.vals[start + pos] = val;
+        }
+        __syncwarp();
+    }
+}
+
 // FullCI diagonal of every row, one thread per row, in diagonal()'s summation
 // order (occupied orbitals ascending, as add_row<FullCIWfn> sums them):
 // alpha i: h_ii, then (J - K) with each later alpha, then J with each beta;
@@ -856,30 +1068,6 @@ __global__ void fci_diag_kernel(BuildParams p, StringTables A, StringTables B) {
             v2 += two_mo_at(two, n, ii, kk, ii, kk) - two_mo_at(two, n, ii, kk, kk, ii);
     }
     p.diag[row] = v2;
-}
-
-// Ascending occupied and virtual orbital lists of one string, built by a
-// warp: lane j tests orbital o0 + j, a ballot gives each list position.
-template<int NW>
-__device__ __forceinline__ void warp_lists(const uint64_t *bits, int nbasis, int16_t *occ, int16_t *vir, int &no,
-                                           int &nv) {
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    int cno = 0, cnv = 0;
-    for (int o0 = 0; o0 < nbasis; o0 += 32) {
-        const int o = o0 + lane;
-        const bool valid = o < nbasis;
-        const bool in = valid && ((bits[o >> 6] >> (o & 63)) & 1ULL);
-        const unsigned mo = __ballot_sync(0xffffffffu, in), mv = __ballot_sync(0xffffffffu, valid && !in);
-        if (in && cno + __popc(mo & below) < kMaxOcc)
-            occ[cno + __popc(mo & below)] = static_cast<int16_t>(o);
-        else if (valid && !in && cnv + __popc(mv & below) < kMaxVir)
-            vir[cnv + __popc(mv & below)] = static_cast<int16_t>(o);
-        cno += __popc(mo);
-        cnv += __popc(mv);
-    }
-    no = cno;
-    nv = cnv;
 }
 
 // One warp per row (kFillRowsPerBlock rows per block), so nothing waits on a
@@ -1322,7 +1510,7 @@ int pick_nw(int64_t nbasis) {
 
 template<int NW>
 int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len,
-              bool sorted_fci) {
+              bool sorted_fci, bool warp_doci) {
     cudaStream_t st = ctx->stream;
     const int64_t chunk = 1 << 20; // rows per launch (grid.x limit is generous; keeps launches short)
     // Shared-memory scratch: rank cache + binomial table (see setup_scratch).
@@ -1358,6 +1546,19 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
     p.vals = csr->vals;
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
+    if (warp_doci) {
+        // Full DOCI space: thread-per-row diagonal, then one warp per row.
+        doci_diag_kernel<NW><<<static_cast<unsigned>((p.nrow + 255) / 256), 256, 0, st>>>(p), ::pyci_gpu::note_launch();
+        const int64_t rows_per_block = 8 * kDociRowsPerWarp;
+        const int64_t rows_per_launch = static_cast<int64_t>(1) << 30;
+        for (int64_t r0 = 0; r0 < p.nrow; r0 += rows_per_launch) {
+            const int64_t nr = std::min<int64_t>(p.nrow - r0, rows_per_launch);
+            fill_doci_warp_kernel<NW><<<static_cast<unsigned>((nr + rows_per_block - 1) / rows_per_block), 256, 0, st>>>(p, r0),
+                ::pyci_gpu::note_launch();
+        }
+        PYCI_CUDA_TRY(cudaGetLastError());
+        return PYCI_GPU_OK;
+    }
     if (sorted_fci) {
         // Per-string tables (alpha and beta; one set when both spins have the
         // same electron count), then the row fill.
@@ -1709,13 +1910,15 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         const int64_t ulen = uniform ? ncand + 1 : 0;
         const int64_t na = 1 + no_a * nv_a + (no_a * (no_a - 1) / 2) * (nv_a * (nv_a - 1) / 2);
         const int64_t nbb = 1 + no_b * nv_b + (no_b * (no_b - 1) / 2) * (nv_b * (nv_b - 1) / 2);
+        const bool warp_doci = uniform && kind == PYCI_WFN_DOCI && no_a <= kMaxOcc && nv_a <= kMaxVir &&
+                               !(csr->flags & PYCI_BUILD_FORCE_HASH);
         const bool sorted_fci = uniform && kind == PYCI_WFN_FULLCI && p.ncache > 0 && na <= kSortedMax &&
                                 nbb <= kSortedMax && no_a * nv_a + no_b * nv_b <= kTableMaxSingles &&
                                 !(csr->flags & PYCI_BUILD_FORCE_HASH);
         switch (nw) {
-        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
-        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
-        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci); break;
+        case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci, warp_doci); break;
+        case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci, warp_doci); break;
+        default: rc = run_build<4>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci, warp_doci); break;
         }
     }
     if (rc)

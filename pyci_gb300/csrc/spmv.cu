@@ -199,6 +199,92 @@ __global__ void __launch_bounds__(256) spmm_kernel(int64_t nrow, const int64_t *
     }
 }
 
+// Column-blocked pass: only the entries of each row with c0 <= column < c1
+// (found by binary search; columns are sorted within a row), lanes strided
+// over them; y = (accumulate ? y : 0) + that part of H x.  Passes over
+// consecutive column blocks keep the gathered slice of x inside L2 when the
+// whole block of vectors does not fit.
+template<int VK, int K, int LANES, bool VEC>
+__global__ void __launch_bounds__(256) spmm_cb_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
+                                                      const int32_t *__restrict__ cols, Values<VK> vals,
+                                                      const typename Values<VK>::x_t *__restrict__ x, int64_t ldx,
+                                                      typename Values<VK>::x_t *__restrict__ y, int64_t ldy,
+                                                      int32_t c0, int32_t c1, bool accumulate) {
+    typedef typename Values<VK>::acc_t acc_t;
+    typedef typename Values<VK>::x_t x_t;
+    const int lane = threadIdx.x % LANES;
+    const int64_t group = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) / LANES;
+    const int64_t ngroups = (static_cast<int64_t>(gridDim.x) * blockDim.x) / LANES;
+    for (int64_t r = group; r < nrow; r += ngroups) {
+        const int64_t start = rowptr[r], end = rowptr[r + 1];
+        // First entry with column >= c (lower bound), for c = c0 and c1.
+        auto lower = [&](int32_t c) {
+            int64_t lo = start, hi = end;
+            while (lo < hi) {
+                const int64_t mid = (lo + hi) >> 1;
+                if (__ldg(cols + mid) < c)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            return lo;
+        };
+        const int64_t e0 = lower(c0), e1 = lower(c1);
+        acc_t acc[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            acc[k] = 0;
+        acc_t xv[K];
+#pragma unroll 4
+        for (int64_t e = e0 + lane; e < e1; e += LANES) {
+            const int64_t c = __ldcs(cols + e);
+            const acc_t v = vals.at(e);
+            load_x<VEC, K>(x + c * ldx, xv);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                acc[k] += v * xv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1)
+                acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o, LANES);
+        }
+        if (lane < K) {
+            acc_t out = acc[0];
+#pragma unroll
+            for (int k = 1; k < K; ++k)
+                if (lane == k)
+                    out = acc[k];
+            x_t *yo = y + r * ldy + lane;
+            *yo = accumulate ? static_cast<x_t>(static_cast<acc_t>(*yo) + out) : static_cast<x_t>(out);
+        }
+    }
+}
+
+template<int VK, int K, int LANES>
+void launch_cb(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y, int64_t ldy,
+               int nblk, cudaStream_t st) {
+    typedef typename Values<VK>::x_t x_t;
+    const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
+    const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (csr->nrow * LANES + 255) / 256));
+    const size_t rowbytes = static_cast<size_t>(ldx) * sizeof(x_t);
+    const size_t vbytes = (K * sizeof(x_t)) % 16 == 0 ? 16 : ((K * sizeof(x_t)) == 8 ? 8 : 0);
+    const bool vec = vbytes && (reinterpret_cast<uintptr_t>(x) % vbytes == 0) && (rowbytes % vbytes == 0);
+    for (int b = 0; b < nblk; ++b) {
+        const int32_t c0 = static_cast<int32_t>(csr->ncol * b / nblk), c1 = static_cast<int32_t>(csr->ncol * (b + 1) / nblk);
+        if (vec)
+            spmm_cb_kernel<VK, K, LANES, true><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+                csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx, static_cast<x_t *>(y), ldy,
+                c0, c1, b > 0);
+        else
+            spmm_cb_kernel<VK, K, LANES, false><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+                csr->nrow, csr->rowptr, csr->cols, vals, static_cast<const x_t *>(x), ldx, static_cast<x_t *>(y), ldy,
+                c0, c1, b > 0);
+        ::pyci_gpu::note_launch();
+    }
+}
+
 template<int VK, int K, int LANES, int MAP>
 void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                 int64_t ldy, cudaStream_t st) {
@@ -229,6 +315,17 @@ inline int variant_map(int v) { return v / 3; }
 template<int VK, int K>
 void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                     int64_t ldy, cudaStream_t st) {
+    const int nblk = v >> 4;
+    v &= 15;
+    if (nblk > 1) {
+        // Column-blocked passes (lane-strided entries) at the variant's lanes.
+        switch (variant_lanes(v)) {
+        case 8: launch_cb<VK, K, 8>(csr, vals, x, ldx, y, ldy, nblk, st); break;
+        case 16: launch_cb<VK, K, 16>(csr, vals, x, ldx, y, ldy, nblk, st); break;
+        default: launch_cb<VK, K, 32>(csr, vals, x, ldx, y, ldy, nblk, st); break;
+        }
+        return;
+    }
     constexpr bool kMapped = (K == 1 || K == 2 || K == 4 || K == 8);
     const int map = kMapped ? variant_map(v) : 0;
     switch (variant_lanes(v) * 2 + map) {
@@ -329,6 +426,26 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
                     if (ms < best) {
                         best = ms;
                         best_v = v;
+                    }
+                }
+                // Column blocks when the gathered block of vectors is larger
+                // than about half the L2 (126 MB on this GPU).
+                const double xbytes = static_cast<double>(csr->ncol) * K * sizeof(x_t);
+                if (xbytes > 48.0 * (1 << 20) && csr->ncol < INT32_MAX) {
+                    for (int nblk = 2; nblk <= 4; ++nblk) {
+                        const int v = best_v | (nblk << 4);
+                        launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                        cudaEventRecord(a, st);
+                        launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                        launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
+                        cudaEventRecord(b, st);
+                        cudaEventSynchronize(b);
+                        float ms = 0.0f;
+                        cudaEventElapsedTime(&ms, a, b);
+                        if (ms < best) {
+                            best = ms;
+                            best_v = v;
+                        }
                     }
                 }
                 cudaEventDestroy(a);
