@@ -164,6 +164,19 @@ int pyci_gpu_csr_matvec_noalloc(const pyci_gpu_csr *csr, const double *x, double
 int pyci_gpu_csr_spmm_device(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x,
                              void *y, void *stream);
 
+/* Gram product C = A^T B of FP32 vector blocks on the device, as the mixed-
+ * precision eigensolver forms it: A holds p vectors and B q vectors of N rows,
+ * vector-major (element (i, r) at i*N + r); C is f64[p][q] on the host.
+ * method PYCI_GRAM_CUDA_CORES: FP32 FMAs; PYCI_GRAM_TENSOR_CORES: tcgen05
+ * TF32 MMAs on high/low split operands (~2^-22 relative per product).  Partial
+ * sums are added in FP64.  Synchronous.  No counterpart in the reference
+ * (Spectra orthogonalises its Lanczos basis on the host); exposed so the two
+ * device paths can be checked against each other. */
+#define PYCI_GRAM_CUDA_CORES 0
+#define PYCI_GRAM_TENSOR_CORES 1
+int pyci_gpu_gram_device(pyci_gpu_ctx *ctx, int method, const float *A, int64_t p, const float *B, int64_t q,
+                         int64_t N, double *C);
+
 /* Derive the FP32 high/low value split used by the mixed-precision solve.
  * With drop_fp64 != 0 the FP64 values are freed afterwards (FP64 products then
  * use high + low, which reproduces every FP64 value to within 2^-48 relative). */

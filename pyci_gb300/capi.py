@@ -18,6 +18,7 @@ OK, EINVAL, ETYPE, ENOCONV, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5,
 WFN_DOCI, WFN_FULLCI, WFN_GENCI = 0, 1, 2
 BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH = 0x1, 0x2, 0x4
 SOLVE_FP64, SOLVE_MIXED = 0, 1
+GRAM_CUDA_CORES, GRAM_TENSOR_CORES = 0, 1
 PREC_FP64, PREC_FP32, PREC_FP64_SPLIT, PREC_FP64_DF = 0, 1, 2, 3
 
 # Every symbol the header declares.
@@ -27,6 +28,7 @@ SYMBOLS = [
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
+    "pyci_gpu_gram_device",
 ]
 
 
@@ -78,6 +80,7 @@ def lib():
                                             ctypes.POINTER(SolveStats)]),
             "pyci_gpu_csr_digest": (_int, [_p, _p, _p, _p, _p, _p]),
             "pyci_gpu_add_all_dets": (_int, [_p, _int, _i64, _i64, _i64, _p]),
+            "pyci_gpu_gram_device": (_int, [_p, _int, _p, _i64, _p, _i64, _i64, _p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -137,6 +140,12 @@ class Context:
         nw = ((nbasis + 63) // 64) * (2 if kind == WFN_FULLCI else 1)
         out = np.zeros((nd, nw), dtype=np.uint64)
         check(lib().pyci_gpu_add_all_dets(self.handle, kind, nbasis, nocc_up, nocc_dn, _ptr(out)))
+        return out
+
+    def gram_device(self, method, a_ptr, p, b_ptr, q, n):
+        r"""C = A^T B (f64[p][q], host) for FP32 device vector blocks A [p][n] and B [q][n]."""
+        out = np.zeros((p, q), dtype=np.float64)
+        check(lib().pyci_gpu_gram_device(self.handle, method, a_ptr, p, b_ptr, q, n, _ptr(out)))
         return out
 
 

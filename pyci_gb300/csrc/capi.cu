@@ -431,6 +431,23 @@ int pyci_gpu_csr_spmm_device(const pyci_gpu_csr *csr, int precision, int64_t k, 
     return csr_spmm(csr, precision, k, x, y, st);
 }
 
+int pyci_gpu_gram_device(pyci_gpu_ctx *ctx, int method, const float *A, int64_t p, const float *B, int64_t q,
+                         int64_t N, double *C) {
+    if (!ctx || !A || !B || !C) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    if (p < 0 || q < 0 || N < 0 || (method != PYCI_GRAM_CUDA_CORES && method != PYCI_GRAM_TENSOR_CORES)) {
+        set_error("invalid Gram product arguments (p=%lld, q=%lld, N=%lld, method=%d)", static_cast<long long>(p),
+                  static_cast<long long>(q), static_cast<long long>(N), method);
+        return PYCI_GPU_EINVAL;
+    }
+    if (p == 0 || q == 0)
+        return PYCI_GPU_OK;
+    PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    return pyci_gpu::gram_device(ctx, method, A, p, B, q, N, C);
+}
+
 int pyci_gpu_csr_prepare_mixed(pyci_gpu_csr *csr, int drop_fp64) {
     if (!csr) {
         set_error("NULL argument");

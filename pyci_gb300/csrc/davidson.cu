@@ -29,6 +29,7 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "dense.h"
@@ -38,6 +39,12 @@ namespace pyci_gpu {
 
 constexpr int kMaxGramP = 128;
 constexpr int kMaxQ = 8;
+// FP32 Gram products with at least this many A vectors run on the tensor
+// cores (gram_tc.cu); narrower ones on the CUDA cores, where the tensor-core
+// version is bound by its per-tile MMA latency (measured on 10.5M-row
+// vectors, q = 4: p = 64 1.18 ms vs 1.31 ms on CUDA cores, p = 128 (q = 8)
+// 2.0 vs 2.9 ms, but p = 32 0.93 vs 0.72 ms and p = 8 0.81 vs 0.30 ms).
+constexpr int kGramTcMinP = 48;
 
 // Xi[r * kp + j] = V[j * N + r] for j < k, 0 for k <= j < kp (padding to a
 // width the SpMM gathers with vector loads).
@@ -347,9 +354,20 @@ private:
             const int pp = std::min(kMaxGramP, p - i0);
             for (int j0 = 0; j0 < q; j0 += kMaxQ) {
                 const int qq = std::min(kMaxQ, q - j0);
-                const unsigned nb = launch_gram_rows<U>(gram_blocks_, st_, A + static_cast<int64_t>(i0) * N_, pp,
-                                                        B + static_cast<int64_t>(j0) * N_, qq, N_, d_partial_);
-                ::pyci_gpu::note_launch();
+                const U *Ai = A + static_cast<int64_t>(i0) * N_;
+                const U *Bj = B + static_cast<int64_t>(j0) * N_;
+                unsigned nb;
+                bool on_tc = false;
+                if constexpr (std::is_same<U, float>::value) {
+                    on_tc = gram_tc_enabled() && pp >= kGramTcMinP;
+                }
+                if (on_tc) {
+                    nb = launch_gram_tc(gram_blocks_, st_, reinterpret_cast<const float *>(Ai), pp,
+                                        reinterpret_cast<const float *>(Bj), qq, N_, d_partial_);
+                } else {
+                    nb = launch_gram_rows<U>(gram_blocks_, st_, Ai, pp, Bj, qq, N_, d_partial_);
+                    ::pyci_gpu::note_launch();
+                }
                 reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq, d_small_), ::pyci_gpu::note_launch();
                 std::vector<double> tmp(static_cast<size_t>(pp) * qq);
                 cudaError_t e = cudaMemcpyAsync(tmp.data(), d_small_, sizeof(double) * pp * qq,
@@ -359,6 +377,13 @@ private:
                 e = cudaStreamSynchronize(st_);
                 if (e != cudaSuccess)
                     return cuda_status(e, "gram");
+                if (on_tc) {
+                    for (double v : tmp)
+                        if (!std::isfinite(v) && gram_tc_error(true)) {
+                            set_error("tensor-core Gram product: MMA completion wait timed out");
+                            return PYCI_GPU_ECUDA;
+                        }
+                }
                 for (int i = 0; i < pp; ++i)
                     for (int j = 0; j < qq; ++j)
                         C[static_cast<size_t>(i0 + i) * q + j0 + j] = tmp[static_cast<size_t>(i) * qq + j];
@@ -961,6 +986,61 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         stats->max_residual = max_res;
     }
     return PYCI_GPU_OK;
+}
+
+bool gram_tc_enabled() {
+    static const bool on = [] {
+        const char *e = std::getenv("PYCI_GPU_GRAM");
+        return !(e && std::strcmp(e, "cuda") == 0);
+    }();
+    return on;
+}
+
+int gram_device(pyci_gpu_ctx *ctx, int method, const float *A, int64_t p, const float *B, int64_t q, int64_t N,
+                double *C) {
+    cudaStream_t st = ctx->stream;
+    const unsigned budget = static_cast<unsigned>(ctx->num_sms * 4);
+    double *partial = nullptr, *small = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(&partial, sizeof(double) * budget * kMaxGramP * kMaxQ, st));
+    PYCI_CUDA_TRY(cudaMallocAsync(&small, sizeof(double) * kMaxGramP * kMaxQ, st));
+    int rc = PYCI_GPU_OK;
+    std::vector<double> tmp(static_cast<size_t>(kMaxGramP) * kMaxQ);
+    for (int64_t i0 = 0; i0 < p && rc == PYCI_GPU_OK; i0 += kMaxGramP) {
+        const int pp = static_cast<int>(std::min<int64_t>(kMaxGramP, p - i0));
+        for (int64_t j0 = 0; j0 < q && rc == PYCI_GPU_OK; j0 += kMaxQ) {
+            const int qq = static_cast<int>(std::min<int64_t>(kMaxQ, q - j0));
+            const float *Ai = A + i0 * N, *Bj = B + j0 * N;
+            unsigned nb;
+            if (method == 1) {
+                nb = launch_gram_tc(budget, st, Ai, pp, Bj, qq, N, partial);
+            } else {
+                nb = launch_gram_rows<float>(budget, st, Ai, pp, Bj, qq, N, partial);
+                note_launch();
+            }
+            reduce_partials_kernel<<<pp * qq, 256, 0, st>>>(partial, nb, pp * qq, small), note_launch();
+            cudaError_t e = cudaMemcpyAsync(tmp.data(), small, sizeof(double) * pp * qq, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
+                rc = cuda_status(e, "Gram product");
+                break;
+            }
+            if (method == 1 && gram_tc_error(true)) {
+                set_error("tensor-core Gram product: MMA completion wait timed out");
+                rc = PYCI_GPU_ECUDA;
+                break;
+            }
+            for (int i = 0; i < pp; ++i)
+                for (int j = 0; j < qq; ++j)
+                    C[(i0 + i) * q + j0 + j] = tmp[static_cast<size_t>(i) * qq + j];
+        }
+    }
+    cudaFreeAsync(partial, st);
+    cudaFreeAsync(small, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc == PYCI_GPU_OK && e != cudaSuccess)
+        rc = cuda_status(e, "Gram product");
+    return rc;
 }
 
 } // namespace pyci_gpu

@@ -100,6 +100,24 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
 
 int64_t host_binomial(int64_t n, int64_t k);
 
+namespace pyci_gpu {
+// Tensor-core Gram partials (gram_tc.cu): partial[b][i * q + j] = sum over
+// the rows of CTA b of A[i][r] B[j][r], p <= 128, q <= 8, FP32 vectors with
+// N rows (vector-major).  Returns the number of CTAs (partials per entry).
+unsigned launch_gram_tc(unsigned budget, cudaStream_t st, const float *A, int p, const float *B, int q, int64_t N,
+                        double *partial);
+// Nonzero when a tensor-core Gram kernel gave up waiting for its MMAs
+// (its partials are then NaN); `clear` resets the flag.
+int gram_tc_error(bool clear);
+// Whether the FP32 Gram products use the tensor cores (PYCI_GPU_GRAM=cuda
+// selects the CUDA-core kernel instead).
+bool gram_tc_enabled();
+// C (host, p x q row-major) = A^T B for FP32 vectors on the device
+// (method 0: CUDA cores, 1: tensor cores); pyci_gpu_gram_device.
+int gram_device(pyci_gpu_ctx *ctx, int method, const float *A, int64_t p, const float *B, int64_t q, int64_t N,
+                double *C);
+} // namespace pyci_gpu
+
 // Seeded perturbation of the Davidson start vectors.  Unit vectors on the
 // lowest diagonal elements can all lie in one symmetry sector of H (e.g.
 // symmetric under alpha <-> beta exchange), and the sector of a skipped root
