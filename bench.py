@@ -475,6 +475,26 @@ def run_batch(args, world=1, rank=0, local=0):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_gram(args):
+    r"""Profiling driver (for ncu): FP32 Gram products C = A^T B of --gram P Q N
+    (random vectors, N rows), on the CUDA cores then on the tensor cores,
+    --reps times each; prints the mean wall time per call of each."""
+    import torch
+    from pyci_gb300 import capi
+    p, q, n = args.gram
+    ctx = capi.Context(0)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    a = torch.randn((p, n), device="cuda", generator=g)
+    b = torch.randn((q, n), device="cuda", generator=g)
+    out = {}
+    for method, name in ((capi.GRAM_CUDA_CORES, "cuda_cores"), (capi.GRAM_TENSOR_CORES, "tensor_cores")):
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            ctx.gram_device(method, a.data_ptr(), p, b.data_ptr(), q, n)
+        out[name + "_ms_per_call"] = (time.perf_counter() - t0) / args.reps * 1e3
+    print(json.dumps({"profile": "gram", "p": p, "q": q, "n": n, **out}))
+
+
 def run_profile_case(args):
     r"""Profiling driver (for ncu): build one FCI (or DOCI) operator and run
     its SpMM kernels (FP32 k=4, FP64 k=1, double-float k=4), or only mixed
@@ -482,6 +502,8 @@ def run_profile_case(args):
     import torch
     from pyci_gb300 import capi
     from pyci_gb300.synth import synthetic_integrals
+    if args.profile == "gram":
+        return run_profile_gram(args)
     nb, nu, nd = args.case
     ecore, one, two = synthetic_integrals(nb, 1000 + nb)
     from math import comb
@@ -519,8 +541,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU baseline sample")
-    ap.add_argument("--profile", choices=["spmm", "solve"], default=None,
-                    help="profiling driver: only SpMM launches, or only mixed solves, on --case")
+    ap.add_argument("--gram", type=int, nargs=3, default=[128, 8, 2 << 20], metavar=("P", "Q", "N"),
+                    help="shape of --profile gram")
+    ap.add_argument("--profile", choices=["spmm", "solve", "gram"], default=None,
+                    help="profiling driver: only SpMM launches, or only mixed solves, on --case; "
+                         "or only Gram products of shape --gram")
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--wfn", choices=["fullci", "doci"], default="fullci", help="wave function of --case")

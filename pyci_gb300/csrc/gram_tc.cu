@@ -23,17 +23,23 @@
 // the CUDA-core kernel).  The CTA's partial C is written as FP64; a second
 // kernel sums the partials over CTAs in FP64.
 //
-// Two loaders feed the same MMA stage.  When the vectors' rows are 16-byte
-// aligned (N % 4 == 0), gram_tma_kernel streams each tile of A and B into a
-// ring of shared-memory stages with TMA (cp.async.bulk.tensor, 128-byte
-// swizzle, zero fill past N; up to 16 tiles in flight per CTA), and the warps
-// split the landed tile into hi/lo operand tiles of the same swizzled layout
-// (conflict-free shared-memory reads and writes).  Otherwise gram_tc_kernel
-// loads each tile with plain coalesced loads into registers.
+// Two loaders feed the same MMA stage.  For wide A blocks (p >= 96) whose
+// rows are 16-byte aligned (N % 4 == 0), gram_tma_kernel streams each tile of
+// A and B into a ring of shared-memory stages with TMA (cp.async.bulk.tensor,
+// 128-byte swizzle, zero fill past N; up to 16 tiles in flight per CTA) and
+// double-buffers the operand tiles and accumulators, and the warps split the
+// landed tile into the hi/lo operand tiles (the swizzle makes both the reads
+// and the writes bank-conflict-free).  Otherwise gram_tc_kernel loads each
+// tile with plain coalesced loads into registers.
+//
+// Each MMA (128 x 16 x 8) does little work for its fixed cost, so for narrow
+// blocks the product is bound by MMA latency, not by HBM: the eigensolver
+// sends only its wide Gram products here and the rest to the CUDA-core kernel.
 //
 // The product reads every vector once and does (p x q) FMAs per row of 4(p+q)
-// bytes: it is HBM-bound like the CUDA-core version (gram_rows_kernel); the
-// tensor cores take the multiply-adds off the FMA pipes.
+// bytes, so at best it is HBM-bound like the CUDA-core version
+// (gram_rows_kernel); the tensor cores take the multiply-adds off the FMA
+// pipes.
 //
 // Waits on the MMA-completion mbarrier are bounded: on expiry the kernel
 // records an error in g_gram_tc_error, writes NaN partials (so the caller's
@@ -174,17 +180,6 @@ __device__ __forceinline__ void drain(uint32_t tmem, int warp, float acc[8]) {
     }
 }
 
-// Shared-memory matrix descriptor of a K-major operand in the 128-byte
-// swizzled layout (rows of 128 bytes, 8-row atoms of 1024 bytes, 16-byte
-// chunk c of row r stored at chunk c ^ (r % 8)): stride byte offset 1024
-// between atoms, leading byte offset unused (1), layout type 2 at bits 61-63.
-// A K-step of 8 TF32 values advances the start address by 32 bytes inside
-// the atom.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
-    return static_cast<uint64_t>((addr >> 4) & 0x3FFFu) | (1ull << 16) | (static_cast<uint64_t>(1024u >> 4) << 32) |
-           (1ull << 46) | (2ull << 61);
-}
-
 // One tile's MMAs (4 K-steps x 3 terms; lo.lo, ~2^-22 of a product, is
 // left out) into six accumulators of kN columns each, so that no MMA
 // waits on the one before it: region 4 + k/2 takes hi.hi of K-steps k, and
@@ -193,14 +188,10 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
 // commit of all of them to `bar`.  A chain of dependent accumulations would
 // expose the MMA latency on every step.
 
-template<bool SW128>
 __device__ __forceinline__ void issue_tile_mmas(uint32_t tmem, uint32_t sa_hi, uint32_t sa_lo, uint32_t sb_hi,
                                                 uint32_t sb_lo, uint32_t bar) {
-    auto d = [&](uint32_t a, int k) {
-        // 8 rows of K: 32 bytes inside a swizzled row, or 2 core matrices.
-        const uint32_t koff = SW128 ? static_cast<uint32_t>(k) * 32u : static_cast<uint32_t>(k) * 2u * kCoreK;
-        return SW128 ? smem_desc_sw128(a + koff) : smem_desc(a + koff);
-    };
+    // 8 rows of K = 2 core matrices.
+    auto d = [&](uint32_t a, int k) { return smem_desc(a + static_cast<uint32_t>(k) * 2u * kCoreK); };
     auto region = [&](int r) { return tmem + static_cast<uint32_t>(r * kN); };
 #pragma unroll
     for (int k = 0; k < kDepth / 8; ++k)
@@ -333,7 +324,7 @@ __global__ void __launch_bounds__(128) gram_tc_kernel(const float *__restrict__ 
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            issue_tile_mmas<false>(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), bar_addr);
+            issue_tile_mmas(tmem, smem_addr(a_hi), smem_addr(a_lo), smem_addr(b_hi), smem_addr(b_lo), bar_addr);
         }
     }
 
@@ -362,8 +353,9 @@ __global__ void __launch_bounds__(128) gram_tc_kernel(const float *__restrict__ 
 // it % 2 and accumulated into accumulator set it % 2 (columns 64 (it % 2) +
 // [0, 3 kN)), so its MMAs run while the warps split tile it + 1; tile it + 2
 // waits for them.  Dynamic shared memory: two sets of hi/lo operand tiles
-// (128-byte swizzled, 1024-aligned), then `stages` raw stages of stage_bytes
-// each (A's p x 32 box at 0, B's q x 32 box at b_off), as TMA lands them.
+// (no swizzle, 1024-aligned), then `stages` raw stages of stage_bytes each
+// (A's p x 32 box at 0, B's q x 32 box at b_off, 128-byte swizzled), as TMA
+// lands them.
 constexpr int kMaxStages = 16;
 constexpr uint32_t kTmaTmemCols = 256; // two accumulator sets of 128 columns
 
@@ -488,7 +480,7 @@ __global__ void __launch_bounds__(128) gram_tma_kernel(const __grid_constant__ C
         __syncthreads();
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            issue_tile_mmas<false>(tmem + static_cast<uint32_t>(b * 128), smem_addr(a_hi), smem_addr(a_lo),
+            issue_tile_mmas(tmem + static_cast<uint32_t>(b * 128), smem_addr(a_hi), smem_addr(a_lo),
                                   smem_addr(b_hi), smem_addr(b_lo), smem_addr(&mma_done[b]));
         }
     }
