@@ -55,6 +55,9 @@ def lib():
         L.orc_phase_single.argtypes = [_p, _i64, _i64]
         L.orc_phase_double.restype = ctypes.c_int
         L.orc_phase_double.argtypes = [_p, _i64, _i64, _i64, _i64]
+        L.orc_add_hci.restype = ctypes.c_int
+        L.orc_add_hci.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _i64, _p,
+                                  ctypes.POINTER(_i64)]
         _lib = L
     return _lib
 
@@ -156,3 +159,22 @@ def lowest_eigenvalues(data, indices, indptr, nroot=1, tol=1e-12):
     vals = spl.eigsh(op, k=nroot, which="SA", tol=tol, return_eigenvectors=False,
                      v0=np.random.default_rng(7).standard_normal(n), ncv=max(2 * nroot + 1, 20))
     return np.sort(vals)
+
+
+def add_hci(kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, eps):
+    r"""Determinants heat-bath CI adds to `dets` (uint64[nnew, nwords]), each
+    once, in first-occurrence order (pyci/src/hci.cpp:240-262)."""
+    L = lib()
+    dets = np.ascontiguousarray(dets, dtype=np.uint64)
+    coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+    one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+    two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+    n = _i64(0)
+    args = (kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets), _ptr(coeffs), _ptr(one_mo), _ptr(two_mo),
+            float(eps))
+    if L.orc_add_hci(*args, 0, None, ctypes.byref(n)):
+        raise RuntimeError("orc_add_hci failed")
+    out = np.zeros((n.value, dets.shape[1]), dtype=np.uint64)
+    if n.value and L.orc_add_hci(*args, n.value, _ptr(out), ctypes.byref(n)):
+        raise RuntimeError("orc_add_hci failed")
+    return out

@@ -15,6 +15,7 @@
 #include "pyci_oracle.h"
 
 #include <limits.h>
+#include <math.h>
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
@@ -728,4 +729,225 @@ void orc_spmv_general(int64_t nrow, const int64_t *indptr, const int64_t *indice
 void orc_spmv_sym_lower(int64_t nrow, const int64_t *indptr, const int64_t *indices,
                         const double *data, const double *x, double *y, int nthreads) {
     spmv_run(nrow, indptr, indices, data, x, y, nthreads, 1);
+}
+
+/* ---------------- heat-bath CI determinant selection ---------------- */
+
+typedef struct {
+    int64_t n, cap, nwords;
+    uint64_t *words;
+} candbuf;
+
+static int cand_push(candbuf *c, const uint64_t *d) {
+    if (c->n == c->cap) {
+        int64_t cap = c->cap ? 2 * c->cap : 1024;
+        uint64_t *w = realloc(c->words, sizeof(uint64_t) * cap * c->nwords);
+        if (!w)
+            return -1;
+        c->words = w;
+        c->cap = cap;
+    }
+    memcpy(c->words + c->n * c->nwords, d, sizeof(uint64_t) * c->nwords);
+    ++c->n;
+    return 0;
+}
+
+/* A candidate joins when |value| > eps / |c_i| and it is not a determinant of
+ * the wave function already (pyci/src/hci.cpp:37-41). */
+static int hci_try(const det_index *ix, candbuf *c, const uint64_t *d, double val, double eps_i) {
+    if (fabs(val) > eps_i && index_find(ix, d) == -1)
+        return cand_push(c, d);
+    return 0;
+}
+
+/* One determinant's candidates in the reference's loop order:
+ * DOCI pyci/src/hci.cpp:21-46, FullCI 48-183, GenCI 185-238 (the GenCI
+ * loop runs over 2 nbasis - nocc "virtuals", the true ones then orbital 0,
+ * exactly as add_row<GenCIWfn> does; ORC_GENCI uses the true virtuals). */
+static int hci_row(int kind, int64_t n1, int64_t nocc_up, int64_t nocc_dn, int64_t nword, const uint64_t *rdet,
+                   const double *one, const double *two, double eps_i, const det_index *ix, candbuf *c) {
+    const int64_t n2 = n1 * n1, n3 = n1 * n2;
+    uint64_t det[128];
+    int64_t occs[512], virs[8192];
+    int rc = 0;
+    if (kind == ORC_DOCI) {
+        memcpy(det, rdet, sizeof(uint64_t) * nword);
+        int64_t no = fill_occs(nword, rdet, occs), nv = fill_virs(nword, n1, rdet, virs);
+        for (int64_t i = 0; i < no && !rc; ++i) {
+            int64_t k = occs[i];
+            for (int64_t j = 0; j < nv && !rc; ++j) {
+                int64_t l = virs[j];
+                double val = TWO(k, k, l, l); /* SQuantOp::v (pyci/src/squantop.cpp:177) */
+                if (fabs(val) > eps_i) {
+                    excite(det, k, l);
+                    rc = hci_try(ix, c, det, val, eps_i);
+                    excite(det, l, k);
+                }
+            }
+        }
+        return rc;
+    }
+    if (kind == ORC_FULLCI) {
+        uint64_t *up = det, *dn = det + nword;
+        memcpy(det, rdet, sizeof(uint64_t) * 2 * nword);
+        int64_t ou[256], od[256], vu[256], vd[256];
+        int64_t nou = fill_occs(nword, rdet, ou), nod = fill_occs(nword, rdet + nword, od);
+        int64_t nvu = fill_virs(nword, n1, rdet, vu), nvd = fill_virs(nword, n1, rdet + nword, vd);
+        for (int64_t i = 0; i < nou && !rc; ++i) {
+            int64_t ii = ou[i];
+            for (int64_t j = 0; j < nvu && !rc; ++j) {
+                int64_t jj = vu[j];
+                excite(up, ii, jj);
+                double val = one[n1 * ii + jj];
+                for (int64_t k = 0; k < nou; ++k) {
+                    int64_t kk = ou[k];
+                    val += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                }
+                for (int64_t k = 0; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    val += TWO(ii, kk, jj, kk);
+                }
+                rc = hci_try(ix, c, det, val, eps_i);
+                for (int64_t k = 0; k < nod && !rc; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = 0; l < nvd && !rc; ++l) {
+                        int64_t ll = vd[l];
+                        val = TWO(ii, kk, jj, ll);
+                        if (fabs(val) > eps_i) {
+                            excite(dn, kk, ll);
+                            rc = hci_try(ix, c, det, val, eps_i);
+                            excite(dn, ll, kk);
+                        }
+                    }
+                }
+                for (int64_t k = i + 1; k < nou && !rc; ++k) {
+                    int64_t kk = ou[k];
+                    for (int64_t l = j + 1; l < nvu && !rc; ++l) {
+                        int64_t ll = vu[l];
+                        val = TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj);
+                        if (fabs(val) > eps_i) {
+                            excite(up, kk, ll);
+                            rc = hci_try(ix, c, det, val, eps_i);
+                            excite(up, ll, kk);
+                        }
+                    }
+                }
+                excite(up, jj, ii);
+            }
+        }
+        for (int64_t i = 0; i < nod && !rc; ++i) {
+            int64_t ii = od[i];
+            for (int64_t j = 0; j < nvd && !rc; ++j) {
+                int64_t jj = vd[j];
+                excite(dn, ii, jj);
+                double val = one[n1 * ii + jj];
+                for (int64_t k = 0; k < nou; ++k) {
+                    int64_t kk = ou[k];
+                    val += TWO(ii, kk, jj, kk);
+                }
+                for (int64_t k = 0; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    val += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                }
+                rc = hci_try(ix, c, det, val, eps_i);
+                for (int64_t k = i + 1; k < nod && !rc; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = j + 1; l < nvd && !rc; ++l) {
+                        int64_t ll = vd[l];
+                        val = TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj);
+                        if (fabs(val) > eps_i) {
+                            excite(dn, kk, ll);
+                            rc = hci_try(ix, c, det, val, eps_i);
+                            excite(dn, ll, kk);
+                        }
+                    }
+                }
+                excite(dn, jj, ii);
+            }
+        }
+        return rc;
+    }
+    /* GenCI */
+    memcpy(det, rdet, sizeof(uint64_t) * nword);
+    int64_t no = fill_occs(nword, rdet, occs), nv = fill_virs(nword, n1, rdet, virs);
+    if (kind == ORC_GENCI_REF) {
+        int64_t nv_ref = 2 * n1 - nocc_up - nocc_dn;
+        for (int64_t j = nv; j < nv_ref; ++j)
+            virs[j] = 0;
+        nv = nv_ref;
+    }
+    for (int64_t i = 0; i < no && !rc; ++i) {
+        int64_t ii = occs[i];
+        for (int64_t j = 0; j < nv && !rc; ++j) {
+            int64_t jj = virs[j];
+            excite(det, ii, jj);
+            double val = one[n1 * ii + jj];
+            for (int64_t k = 0; k < no; ++k) {
+                int64_t kk = occs[k];
+                val += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+            }
+            rc = hci_try(ix, c, det, val, eps_i);
+            for (int64_t k = i + 1; k < no && !rc; ++k) {
+                int64_t kk = occs[k];
+                for (int64_t l = j + 1; l < nv && !rc; ++l) {
+                    int64_t ll = virs[l];
+                    val = TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj);
+                    if (fabs(val) > eps_i) {
+                        excite(det, kk, ll);
+                        rc = hci_try(ix, c, det, val, eps_i);
+                        excite(det, ll, kk);
+                    }
+                }
+            }
+            excite(det, jj, ii);
+        }
+    }
+    return rc;
+}
+
+/* add_hci (pyci/src/hci.cpp:240-262): every determinant not yet in the wave
+ * function that some determinant i reaches by an excitation with
+ * |H_ji| > eps / |c_i|.  Each new determinant is listed once, at its first
+ * occurrence in the order (i ascending, the reference's loop order); the
+ * reference merges its per-thread results by iterating hash maps, so its
+ * order is that of its hash-map implementation while the set is the same. */
+int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                const double *coeffs, const double *one_mo, const double *two_mo, double eps, int64_t max_new,
+                uint64_t *out, int64_t *n_new) {
+    const int64_t nword = orc_nword(nbasis);
+    const int64_t nw = kind == ORC_FULLCI ? 2 * nword : nword;
+    if (nword > 64 || (kind == ORC_FULLCI && nword > 4))
+        return -2;
+    det_index ix;
+    if (index_build(&ix, ndet, nw, dets))
+        return -1;
+    candbuf c = {0, 0, nw, NULL};
+    int rc = 0;
+    for (int64_t i = 0; i < ndet && !rc; ++i) {
+        const double eps_i = eps / fabs(coeffs[i]);
+        rc = hci_row(kind, nbasis, nocc_up, nocc_dn, nword, dets + i * nw, one_mo, two_mo, eps_i, &ix, &c);
+    }
+    free(ix.slots);
+    if (rc) {
+        free(c.words);
+        return -1;
+    }
+    /* First occurrence of each candidate: the table keeps the first index. */
+    det_index cx;
+    if (index_build(&cx, c.n, nw, c.words)) {
+        free(c.words);
+        return -1;
+    }
+    int64_t m = 0;
+    for (int64_t i = 0; i < c.n; ++i) {
+        if (index_find(&cx, c.words + i * nw) != i)
+            continue;
+        if (out && m < max_new)
+            memcpy(out + m * nw, c.words + i * nw, sizeof(uint64_t) * nw);
+        ++m;
+    }
+    *n_new = m;
+    free(cx.slots);
+    free(c.words);
+    return 0;
 }

@@ -54,6 +54,15 @@ void orc_spmv_general(int64_t nrow, const int64_t *indptr, const int64_t *indice
 void orc_spmv_sym_lower(int64_t nrow, const int64_t *indptr, const int64_t *indices,
                         const double *data, const double *x, double *y, int nthreads);
 
+/* Heat-bath CI selection (add_hci): determinants not in dets[ndet] reached
+ * from some determinant i by an excitation with |H_ji| > eps / |coeffs[i]|,
+ * each once, in first-occurrence order.  Writes at most max_new of them to
+ * out (out may be NULL) and their total count to *n_new.  kind ORC_GENCI_REF
+ * follows the reference's GenCI loop (with its virtual-count quirk). */
+int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                const double *coeffs, const double *one_mo, const double *two_mo, double eps, int64_t max_new,
+                uint64_t *out, int64_t *n_new);
+
 #ifdef __cplusplus
 }
 #endif

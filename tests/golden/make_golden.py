@@ -3,7 +3,7 @@ r"""Generate the golden fixtures in tests/golden/ from the reference itself.
 Run in a container that has the reference source tree:
 
     make -C oracle ref port            # reference built against the shims + C oracle
-    python tests/golden/make_golden.py [--big]
+    python tests/golden/make_golden.py [--big | --only-big | --only-hci]
 
 Outputs (all committed):
   kat_<system>.npz      integrals of the FCIDUMP files the reference's known-answer
@@ -11,6 +11,8 @@ Outputs (all committed):
                         elements only, plus the tests' energies (kat.json)
   csr_<case>.npz        the reference's own CSR (data / indices / indptr) for small
                         synthetic cases, built by pyci.sparse_op of the reference
+  hci_<case>.npz        one heat-bath CI step of the reference (pyci.add_hci): input
+                        determinants and coefficients, and the set it added
   digests.json          order-independent digests of the reference CSR for the
                         larger synthetic workloads, and reference eigenvalues
 The reference is imported from oracle/_ref (the unchanged sources compiled
@@ -127,6 +129,63 @@ def csr_fixtures(pyci):
     return meta
 
 
+HCI_CASES = [
+    # name, kind, nbasis, nocc_up, nocc_dn, excitations of the input set, seed, eps
+    ("doci_10_4", "doci", 10, 4, 4, (0, 1), 21, 1e-3),
+    ("fci_7_3_2", "fullci", 7, 3, 2, (0, 1), 22, 1e-3),
+    ("genci_10_4", "genci", 10, 4, 0, (0, 1), 23, 1e-3),
+]
+
+
+def sorted_rows(a):
+    r"""Rows of a uint64 array in lexicographic order (an order-free set)."""
+    a = np.asarray(a, dtype=np.uint64).reshape(a.shape[0], -1)
+    if a.shape[0] == 0:
+        return a
+    return a[np.lexsort(a.T[::-1])]
+
+
+def hci_fixtures(pyci):
+    r"""One heat-bath CI step of the reference (pyci.add_hci) per case: the
+    input determinants and coefficients, and the determinants it added.  The
+    reference merges per-thread hash maps, so its order of the added
+    determinants is that of its hash map; the fixture keeps them as a sorted
+    set.  The last case starts from a solved be/cc-pVDZ FullCI(2,2) Hartree-Fock
+    determinant, as the reference's test_run_hci does."""
+    meta = []
+    cases = [(name, kind, n, nu, nd, exc, seed, eps, None) for name, kind, n, nu, nd, exc, seed, eps in HCI_CASES]
+    cases.append(("be_fci_hf", "fullci", None, 2, 2, None, None, 1e-4, "be_ccpvdz"))
+    for name, kind, n, nu, nd, exc, seed, eps, system in cases:
+        W = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn, "genci": pyci.genci_wfn}[kind]
+        if system is None:
+            ecore, one, two = synthetic_integrals(n, seed)
+            ham = pyci.secondquant_op(ecore, one, two)
+            wfn = W(n, nu, nd)
+            pyci.add_excitations(wfn, *exc)
+            coeffs = np.random.default_rng(seed).normal(size=len(wfn))
+            coeffs /= np.linalg.norm(coeffs)
+        else:
+            ham = pyci.secondquant_op(os.path.join(REFROOT, "pyci", "test", "data", system + ".fcidump"))
+            ecore, one, two = float(ham.ecore), np.asarray(ham.one_mo), np.asarray(ham.two_mo)
+            n = ham.nbasis
+            wfn = W(n, nu, nd)
+            wfn.add_hartreefock_det()
+            op = pyci.sparse_op(ham, wfn)
+            es, cs = op.solve(n=1, tol=1.0e-6)
+            coeffs = np.asarray(cs[0])
+        dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1).copy()
+        nadded = pyci.add_hci(ham, wfn, coeffs, eps=eps, nthread=1)
+        after = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
+        added = after[dets.shape[0]:]
+        keys, vals = pack_8fold(two)
+        np.savez_compressed(os.path.join(HERE, "hci_%s.npz" % name), dets=dets, coeffs=coeffs,
+                            added=sorted_rows(added), ecore=np.float64(ecore), one_mo=one, keys=keys, vals=vals)
+        meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd, "eps": eps,
+                     "seed": seed, "system": system, "ndet": int(dets.shape[0]), "nadded": int(nadded)})
+        print("hci", name, dets.shape[0], "->", nadded, flush=True)
+    return meta
+
+
 WORKLOADS = [
     # name, kind, nbasis, nocc, config index (seed 1000 + index), roots
     ("fci_8_4_4", "fullci", 8, (4, 4), 1, 4),
@@ -168,16 +227,21 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--big", action="store_true")
     ap.add_argument("--only-big", action="store_true")
+    ap.add_argument("--only-hci", action="store_true")
     args = ap.parse_args()
     import pyci  # the reference, from oracle/_ref
     path = os.path.join(HERE, "digests.json")
-    if args.only_big:
+    if args.only_hci:
+        with open(path) as f:
+            meta = json.load(f)
+        meta["hci_cases"] = hci_fixtures(pyci)
+    elif args.only_big:
         with open(path) as f:
             meta = json.load(f)
         meta["workloads"].update({k: v for k, v in workload_digests(pyci, True).items()
                                   if k in dict((w[0], 1) for w in BIG_WORKLOADS)})
     else:
-        meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci),
+        meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci), "hci_cases": hci_fixtures(pyci),
                 "workloads": workload_digests(pyci, args.big)}
     with open(path, "w") as f:
         json.dump(meta, f, indent=1)

@@ -92,3 +92,45 @@ def test_oracle_known_answer_energies(golden, kat):
     csr = O.build_csr(kind, n, k["occs"][0], k["occs"][1], dets, one, two)
     e = O.lowest_eigenvalues(*csr, nroot=1)[0] + ecore
     assert abs(e - k["energy"]) < 1e-9
+
+
+def load_hci_case(name):
+    from conftest import unpack_8fold
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "hci_%s.npz" % name))
+    one = np.ascontiguousarray(z["one_mo"])
+    return {k: z[k] for k in ("dets", "coeffs", "added")}, one, unpack_8fold(one, z["keys"], z["vals"])
+
+
+def sorted_rows(a):
+    return a[np.lexsort(a.T[::-1])] if len(a) else a
+
+
+def test_add_hci_matches_reference_sets(golden):
+    r"""One heat-bath CI step (pyci/src/hci.cpp) on every golden case: the set
+    of determinants the oracle adds equals the reference's, and each appears
+    once.  The GenCI case replays the reference's virtual-count quirk, which
+    adds determinants with one electron too few (reproduced, not fixed)."""
+    for m in golden["hci_cases"]:
+        z, one, two = load_hci_case(m["name"])
+        new = O.add_hci(KIND[m["wfn"]], one.shape[0], m["nocc_up"], m["nocc_dn"], z["dets"], z["coeffs"],
+                        one, two, m["eps"])
+        assert new.shape[0] == m["nadded"]
+        assert np.array_equal(sorted_rows(new), z["added"]), m["name"]
+        assert len({tuple(r) for r in new}) == new.shape[0]
+
+
+def test_add_hci_thresholds():
+    # eps = 0 adds exactly the determinants H connects to the start with a
+    # nonzero element (|H_ij| > 0); a zero coefficient (eps / |c| = inf) and a
+    # huge eps add none.
+    ecore, one, two = synthetic_integrals(6, 5)
+    dets = O.all_dets(O.FULLCI, 6, 2, 2)
+    hf = dets[:1]
+    every = O.add_hci(O.FULLCI, 6, 2, 2, hf, np.array([1.0]), one, two, 0.0)
+    data, indices, indptr = O.build_csr(O.FULLCI, 6, 2, 2, dets, one, two, symmetric=False)
+    cols, vals = indices[indptr[0]:indptr[1]], data[indptr[0]:indptr[1]]
+    connected = {tuple(dets[j]) for j, v in zip(cols, vals) if j != 0 and v != 0.0}
+    assert {tuple(r) for r in every} == connected
+    assert O.add_hci(O.FULLCI, 6, 2, 2, hf, np.array([0.0]), one, two, 1e-9).shape[0] == 0
+    assert O.add_hci(O.FULLCI, 6, 2, 2, hf, np.array([1.0]), one, two, 1e9).shape[0] == 0
