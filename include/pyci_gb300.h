@@ -233,6 +233,23 @@ int pyci_gpu_csr_digest(const pyci_gpu_csr *csr, uint64_t *pattern_sum, uint64_t
 int pyci_gpu_add_all_dets(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up,
                           int64_t nocc_dn, uint64_t *dets);
 
+/* One heat-bath CI selection step (add_hci, pyci/src/hci.cpp:240-262): the
+ * determinants not among dets[ndet] that some determinant i reaches by a
+ * single or double excitation with |H_ji| > eps / |coeffs[i]|, each once, in
+ * first-occurrence order (i ascending, then the reference's excitation
+ * order; the reference's own order follows its hash maps, its set is the
+ * same).  dets in the wave function's layout (uint64[ndet][nwords],
+ * nwords = ceil(nbasis / 64), doubled for FullCI); coeffs f64[ndet]; one_mo,
+ * two_mo as for pyci_gpu_csr_build.  flags: PYCI_BUILD_GENCI_EXACT (GenCI
+ * over the true virtual spin-orbitals; by default the reference's GenCI loop
+ * with its virtual-count quirk).  *n_new receives the number of new
+ * determinants; they are written to out only when out != NULL and
+ * *n_new <= max_new (otherwise call again with room for *n_new).  The caller
+ * appends them to its wave function. */
+int pyci_gpu_add_hci(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                     const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
+                     double eps, int flags, int64_t max_new, uint64_t *out, int64_t *n_new);
+
 #ifdef __cplusplus
 }
 #endif

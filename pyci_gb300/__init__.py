@@ -3,8 +3,9 @@ r"""pyci_gb300: PyCI's CI hot path on NVIDIA GB300 (sm_103a).
 Drop-in for the ``pyci`` names on the sparse-operator path
 (pyci/__init__.py:18-31): ``secondquant_op`` (alias ``hamiltonian``), the
 ``doci_wfn`` / ``fullci_wfn`` / ``genci_wfn`` wave functions, ``sparse_op``
-(CSR build, ``op(x)``, ``op.solve``), ``popcnt``, ``ctz``, thread-count
-helpers and ``add_excitations``.  The operator runs on the GPU through
+(CSR build, ``op(x)``, ``op.solve``, ``op.update``), ``add_hci`` (heat-bath
+CI selection), ``popcnt``, ``ctz``, thread-count helpers and
+``add_excitations``.  The operator runs on the GPU through
 ``libpyci_gb300.so``; importing works without a GPU, building an operator
 does not.
 
@@ -19,6 +20,7 @@ _HERE = _os.path.dirname(_os.path.abspath(__file__))
 try:
     from pyci_gb300._pyci import (  # noqa: F401
         __version__,
+        add_hci,
         c_double,
         c_long,
         c_ulong,
@@ -67,6 +69,7 @@ __all__ = [
     "popcnt",
     "ctz",
     "add_excitations",
+    "add_hci",
     "gpu_version",
     "LIBRARY_PATH",
 ]

@@ -28,7 +28,7 @@ SYMBOLS = [
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
-    "pyci_gpu_gram_device",
+    "pyci_gpu_gram_device", "pyci_gpu_add_hci",
 ]
 
 
@@ -81,6 +81,8 @@ def lib():
             "pyci_gpu_csr_digest": (_int, [_p, _p, _p, _p, _p, _p]),
             "pyci_gpu_add_all_dets": (_int, [_p, _int, _i64, _i64, _i64, _p]),
             "pyci_gpu_gram_device": (_int, [_p, _int, _p, _i64, _p, _i64, _i64, _p]),
+            "pyci_gpu_add_hci": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _int,
+                                        _i64, _p, ctypes.POINTER(_i64)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -141,6 +143,24 @@ class Context:
         out = np.zeros((nd, nw), dtype=np.uint64)
         check(lib().pyci_gpu_add_all_dets(self.handle, kind, nbasis, nocc_up, nocc_dn, _ptr(out)))
         return out
+
+    def add_hci(self, kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, eps, flags=0):
+        r"""New determinants of one heat-bath CI step (uint64[nnew, nwords]), first-occurrence order."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+        two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+        nw = dets.shape[1] if dets.ndim == 2 else ((nbasis + 63) // 64) * (2 if kind == WFN_FULLCI else 1)
+        n = _i64(0)
+        cap = max(4096, 4 * dets.shape[0])
+        while True:
+            out = np.zeros((cap, nw), dtype=np.uint64)
+            check(lib().pyci_gpu_add_hci(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
+                                         _ptr(coeffs), _ptr(one_mo), _ptr(two_mo), float(eps), flags, cap,
+                                         _ptr(out), ctypes.byref(n)))
+            if n.value <= cap:
+                return out[:n.value]
+            cap = n.value
 
     def gram_device(self, method, a_ptr, p, b_ptr, q, n):
         r"""C = A^T B (f64[p][q], host) for FP32 device vector blocks A [p][n] and B [q][n]."""

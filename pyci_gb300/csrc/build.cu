@@ -1479,6 +1479,38 @@ int device_exclusive_scan(const int64_t *counts, int64_t n, int64_t *out, cudaSt
     return PYCI_GPU_OK;
 }
 
+// Open-addressing table over ndet determinants of nwords (1, 2, 4 or 8)
+// words at d_dets: *slots (2^k >= 2 ndet int32 slots, from the stream's pool;
+// the caller frees it) and *mask = 2^k - 1.  Duplicates keep the smallest
+// index.  Table overflow sets *d_err = 2.
+int det_table_build(const uint64_t *d_dets, int64_t ndet, int nwords, cudaStream_t st, int *d_err,
+                    int32_t **slots_out, uint64_t *mask_out) {
+    uint64_t cap = 16;
+    while (cap < static_cast<uint64_t>(2 * ndet))
+        cap <<= 1;
+    int32_t *slots = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(&slots, sizeof(int32_t) * cap, st));
+    PYCI_CUDA_TRY(cudaMemsetAsync(slots, 0xff, sizeof(int32_t) * cap, st));
+    const unsigned blocks = static_cast<unsigned>((ndet + 255) / 256);
+    if (blocks) {
+        switch (nwords) {
+        case 1: table_insert_kernel<1><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, ndet, d_err); break;
+        case 2: table_insert_kernel<2><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, ndet, d_err); break;
+        case 4: table_insert_kernel<4><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, ndet, d_err); break;
+        case 8: table_insert_kernel<8><<<blocks, 256, 0, st>>>(slots, cap - 1, d_dets, ndet, d_err); break;
+        default:
+            cudaFreeAsync(slots, st);
+            set_error("unsupported determinant width");
+            return PYCI_GPU_EUNSUPPORTED;
+        }
+        ::pyci_gpu::note_launch();
+        PYCI_CUDA_TRY(cudaGetLastError());
+    }
+    *slots_out = slots;
+    *mask_out = cap - 1;
+    return PYCI_GPU_OK;
+}
+
 namespace {
 
 struct DeviceBuffers {

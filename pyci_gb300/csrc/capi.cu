@@ -525,4 +525,23 @@ int pyci_gpu_add_all_dets(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t n
     return add_all_dets_device(ctx, kind, nbasis, nocc_up, nocc_dn, dets);
 }
 
+int pyci_gpu_add_hci(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                     const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
+                     double eps, int flags, int64_t max_new, uint64_t *out, int64_t *n_new) {
+    if (!ctx || !n_new || !one_mo || !two_mo || (ndet > 0 && (!dets || !coeffs))) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    if (ndet < 0 || max_new < 0) {
+        set_error("negative determinant count");
+        return PYCI_GPU_EINVAL;
+    }
+    int rc = validate_wfn(kind, nbasis, nocc_up, nocc_dn);
+    if (rc)
+        return rc;
+    PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    return hci_select_device(ctx, kind, nbasis, nocc_up, nocc_dn, ndet, dets, coeffs, one_mo, two_mo, eps, flags,
+                             max_new, out, n_new);
+}
+
 } // extern "C"

@@ -621,6 +621,40 @@ struct GenCIWfn final : OneSpinWfn {
     }
 };
 
+// ---------------------------------------------------------------- heat-bath CI
+
+// add_hci (pyci/src/hci.cpp:240-262, binding pyci/src/binding.cpp:1147-1181):
+// one selection step on the device, then the new determinants are appended
+// to the wave function in first-occurrence order.  Returns how many were
+// added.  nthread is accepted for the reference's signature (the device
+// needs no host threads).
+long add_hci(const SQuantOp &ham, Wfn &wfn, Array<double> coeffs, double eps, int flags) {
+    if (ham.nbasis != wfn.nbasis)
+        throw std::invalid_argument("Hamiltonian and wave function have different nbasis");
+    if (coeffs.size() < wfn.ndet)
+        throw std::invalid_argument("coeffs has fewer entries than the wave function has determinants");
+    const long nw = wfn.words();
+    auto ctx = default_ctx();
+    int64_t cap = std::max<int64_t>(4096, 4 * wfn.ndet), n_new = 0;
+    std::vector<ulong_t> out;
+    for (;;) {
+        out.assign(static_cast<size_t>(cap * nw), 0);
+        {
+            py::gil_scoped_release nogil;
+            check(pyci_gpu_add_hci(ctx.get(), wfn.kind(), wfn.nbasis, wfn.nocc_up, wfn.nocc_dn, wfn.ndet,
+                                   wfn.ndet ? wfn.dets.data() : nullptr, coeffs.data(), ham.one_mo.data(),
+                                   ham.two_mo.data(), eps, flags, cap, out.data(), &n_new));
+        }
+        if (n_new <= cap)
+            break;
+        cap = n_new;
+    }
+    const long before = wfn.ndet;
+    for (int64_t i = 0; i < n_new; ++i)
+        wfn.add_det(&out[static_cast<size_t>(i * nw)]);
+    return wfn.ndet - before;
+}
+
 // ---------------------------------------------------------------- numpy views
 
 Array<ulong_t> one_det(const Wfn &w, long i, bool two) {
@@ -1174,6 +1208,16 @@ PYBIND11_MODULE(_pyci, m) {
     sp.def("indices", &SparseOp::indices);
     sp.def("indptr", &SparseOp::indptr);
 
+    m.def("add_hci", [](const SQuantOp &h, DOCIWfn &w, Array<double> c, double eps, long) {
+        return add_hci(h, w, c, eps, 0);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("eps") = 1.0e-5, py::arg("nthread") = -1);
+    m.def("add_hci", [](const SQuantOp &h, FullCIWfn &w, Array<double> c, double eps, long) {
+        return add_hci(h, w, c, eps, 0);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("eps") = 1.0e-5, py::arg("nthread") = -1);
+    m.def("add_hci", [](const SQuantOp &h, GenCIWfn &w, Array<double> c, double eps, long, bool exact) {
+        return add_hci(h, w, c, eps, exact ? PYCI_BUILD_GENCI_EXACT : 0);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("eps") = 1.0e-5, py::arg("nthread") = -1,
+        py::arg("genci_exact") = false);
     m.def("get_num_threads", []() { return g_threads; });
     m.def("set_num_threads", [](long n) { g_threads = std::max(1L, n); }, py::arg("n"));
     m.def("popcnt", [](Array<ulong_t> d) {

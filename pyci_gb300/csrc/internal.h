@@ -100,6 +100,16 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
 
 int64_t host_binomial(int64_t n, int64_t k);
 
+// Exclusive scan of counts[n] into out[n + 1] (out[n] = total) on `stream`.
+int device_exclusive_scan(const int64_t *counts, int64_t n, int64_t *out, cudaStream_t stream);
+// Device determinant hash table (build.cu): slots from the stream's pool.
+int det_table_build(const uint64_t *d_dets, int64_t ndet, int nwords, cudaStream_t st, int *d_err,
+                    int32_t **slots, uint64_t *mask);
+// Heat-bath CI selection on the device (hci.cu), pyci_gpu_add_hci.
+int hci_select_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                      const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
+                      double eps, int flags, int64_t max_new, uint64_t *out, int64_t *n_new);
+
 namespace pyci_gpu {
 // Tensor-core Gram partials (gram_tc.cu): partial[b][i * q + j] = sum over
 // the rows of CTA b of A[i][r] B[j][r], p <= 128, q <= 8, FP32 vectors with
