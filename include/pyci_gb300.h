@@ -250,6 +250,17 @@ int pyci_gpu_add_hci(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_u
                      const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
                      double eps, int flags, int64_t max_new, uint64_t *out, int64_t *n_new);
 
+/* One- and two-particle reduced density matrices of sum_i coeffs[i] |dets[i]>
+ * (compute_rdms, pyci/src/rdm.cpp:20-66 for DOCI, 269-530 for FullCI; binding
+ * pyci/src/binding.cpp:1208-1291).  dets in the wave function's layout
+ * (host), coeffs f64[ndet].  DOCI: rdm1 = d0 f64[n][n], rdm2 = d2 f64[n][n];
+ * FullCI: rdm1 = [aa, bb] f64[2][n][n], rdm2 = [aaaa, bbbb, abab]
+ * f64[3][n][n][n][n] (host).  Same terms as the reference, summed with FP64
+ * atomics (entries agree to rounding).  GenCI: EUNSUPPORTED (the reference's
+ * GenCI compute_rdms writes past its output arrays). */
+int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                          int64_t ndet, const uint64_t *dets, const double *coeffs, double *rdm1, double *rdm2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,8 @@ def lib():
         L.orc_phase_single.argtypes = [_p, _i64, _i64]
         L.orc_phase_double.restype = ctypes.c_int
         L.orc_phase_double.argtypes = [_p, _i64, _i64, _i64, _i64]
+        L.orc_compute_rdms.restype = ctypes.c_int
+        L.orc_compute_rdms.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]
         L.orc_add_hci.restype = ctypes.c_int
         L.orc_add_hci.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _i64, _p,
                                   ctypes.POINTER(_i64)]
@@ -178,3 +180,19 @@ def add_hci(kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, eps):
     if n.value and L.orc_add_hci(*args, n.value, _ptr(out), ctypes.byref(n)):
         raise RuntimeError("orc_add_hci failed")
     return out
+
+
+def compute_rdms(kind, nbasis, nocc_up, nocc_dn, dets, coeffs):
+    r"""(rdm1, rdm2) as pyci.compute_rdms returns them (pyci/src/rdm.cpp): DOCI
+    (d0, d2) [n, n] each; FullCI rdm1 [2, n, n], rdm2 [3, n, n, n, n]."""
+    L = lib()
+    dets = np.ascontiguousarray(dets, dtype=np.uint64)
+    coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+    n = nbasis
+    if kind == DOCI:
+        r1, r2 = np.zeros((n, n)), np.zeros((n, n))
+    else:
+        r1, r2 = np.zeros((2, n, n)), np.zeros((3, n, n, n, n))
+    if L.orc_compute_rdms(kind, n, nocc_up, nocc_dn, dets.shape[0], _ptr(dets), _ptr(coeffs), _ptr(r1), _ptr(r2)):
+        raise RuntimeError("orc_compute_rdms failed")
+    return r1, r2

@@ -951,3 +951,214 @@ int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int6
     free(c.words);
     return 0;
 }
+
+/* ---------------- reduced density matrices ---------------- */
+
+/* compute_rdms, pyci/src/rdm.cpp:20-66 (DOCI: rdm1 = d0, rdm2 = d2, both
+ * nbasis x nbasis) and 269-530 (FullCI: rdm1 = [aa, bb] (2 n^2), rdm2 =
+ * [aaaa, bbbb, abab] (3 n^4)).  Serial, in the reference's loop and
+ * summation order, so the sums are bit-identical to the reference's. */
+int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                     const double *coeffs, double *rdm1, double *rdm2) {
+    const int64_t nword = orc_nword(nbasis), n1 = nbasis, n2 = n1 * n1, n3 = n1 * n2, n4 = n2 * n2;
+    (void)nocc_up;
+    (void)nocc_dn;
+    if (kind != ORC_DOCI && kind != ORC_FULLCI)
+        return -2;
+    const int64_t nw = kind == ORC_FULLCI ? 2 * nword : nword;
+    if (nword > 4)
+        return -2;
+    det_index ix;
+    if (index_build(&ix, ndet, nw, dets))
+        return -1;
+    uint64_t det[8];
+    int64_t ou[256], od[256], vu[256], vd[256];
+    if (kind == ORC_DOCI) {
+        double *d0 = rdm1, *d2 = rdm2;
+        memset(d0, 0, sizeof(double) * n2);
+        memset(d2, 0, sizeof(double) * n2);
+        for (int64_t idet = 0; idet < ndet; ++idet) {
+            const uint64_t *rdet = dets + idet * nw;
+            memcpy(det, rdet, sizeof(uint64_t) * nw);
+            int64_t no = fill_occs(nword, rdet, ou), nv = fill_virs(nword, n1, rdet, vu);
+            const double val1 = coeffs[idet] * coeffs[idet];
+            for (int64_t i = 0; i < no; ++i) {
+                int64_t k = ou[i];
+                d0[k * (n1 + 1)] += val1;
+                for (int64_t j = i + 1; j < no; ++j) {
+                    int64_t l = ou[j];
+                    d2[n1 * k + l] += val1;
+                    d2[n1 * l + k] += val1;
+                }
+                for (int64_t j = 0; j < nv; ++j) {
+                    int64_t l = vu[j];
+                    excite(det, k, l);
+                    int64_t jdet = index_find(&ix, det);
+                    excite(det, l, k);
+                    if (jdet > idet) {
+                        const double val2 = coeffs[idet] * coeffs[jdet];
+                        d0[n1 * k + l] += val2;
+                        d0[n1 * l + k] += val2;
+                    }
+                }
+            }
+        }
+        free(ix.slots);
+        return 0;
+    }
+    double *aa = rdm1, *bb = rdm1 + n2;
+    double *aaaa = rdm2, *bbbb = rdm2 + n4, *abab = rdm2 + 2 * n4;
+    memset(rdm1, 0, sizeof(double) * 2 * n2);
+    memset(rdm2, 0, sizeof(double) * 3 * n4);
+#define R4(a, p, q, r, t) a[(p) * n3 + (q) * n2 + (r) * n1 + (t)]
+    for (int64_t idet = 0; idet < ndet; ++idet) {
+        const uint64_t *rup = dets + idet * nw, *rdn = rup + nword;
+        uint64_t *up = det, *dn = det + nword;
+        memcpy(det, rup, sizeof(uint64_t) * nw);
+        int64_t nou = fill_occs(nword, rup, ou), nod = fill_occs(nword, rdn, od);
+        int64_t nvu = fill_virs(nword, n1, rup, vu), nvd = fill_virs(nword, n1, rdn, vd);
+        const double val1 = coeffs[idet] * coeffs[idet];
+        for (int64_t i = 0; i < nou; ++i) {
+            int64_t ii = ou[i];
+            aa[(n1 + 1) * ii] += val1;
+            for (int64_t k = i + 1; k < nou; ++k) {
+                int64_t kk = ou[k];
+                R4(aaaa, ii, kk, ii, kk) += val1;
+                R4(aaaa, ii, kk, kk, ii) -= val1;
+                R4(aaaa, kk, ii, ii, kk) -= val1;
+                R4(aaaa, kk, ii, kk, ii) += val1;
+            }
+            for (int64_t k = 0; k < nod; ++k) {
+                int64_t kk = od[k];
+                R4(abab, ii, kk, ii, kk) += val1;
+            }
+            for (int64_t j = 0; j < nvu; ++j) {
+                int64_t jj = vu[j];
+                excite(up, ii, jj);
+                const int sign_up = orc_phase_single(rup, ii, jj);
+                int64_t jdet = index_find(&ix, det);
+                if (jdet > idet) {
+                    const double val2 = coeffs[idet] * coeffs[jdet] * sign_up;
+                    aa[ii * n1 + jj] += val2;
+                    aa[jj * n1 + ii] += val2;
+                    for (int64_t k = 0; k < nou; ++k) {
+                        if (i == k)
+                            continue;
+                        int64_t kk = ou[k];
+                        R4(aaaa, ii, kk, jj, kk) += val2;
+                        R4(aaaa, ii, kk, kk, jj) -= val2;
+                        R4(aaaa, kk, ii, kk, jj) += val2;
+                        R4(aaaa, kk, ii, jj, kk) -= val2;
+                        R4(aaaa, jj, kk, ii, kk) += val2;
+                        R4(aaaa, jj, kk, kk, ii) -= val2;
+                        R4(aaaa, kk, jj, ii, kk) -= val2;
+                        R4(aaaa, kk, jj, kk, ii) += val2;
+                    }
+                    for (int64_t k = 0; k < nod; ++k) {
+                        int64_t kk = od[k];
+                        R4(abab, ii, kk, jj, kk) += val2;
+                        R4(abab, jj, kk, ii, kk) += val2;
+                    }
+                }
+                for (int64_t k = 0; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = 0; l < nvd; ++l) {
+                        int64_t ll = vd[l];
+                        excite(dn, kk, ll);
+                        jdet = index_find(&ix, det);
+                        if (jdet > idet) {
+                            const double val2 = coeffs[idet] * coeffs[jdet] * sign_up * orc_phase_single(rdn, kk, ll);
+                            R4(abab, ii, kk, jj, ll) += val2;
+                            R4(abab, jj, ll, ii, kk) += val2;
+                        }
+                        excite(dn, ll, kk);
+                    }
+                }
+                for (int64_t k = i + 1; k < nou; ++k) {
+                    int64_t kk = ou[k];
+                    for (int64_t l = j + 1; l < nvu; ++l) {
+                        int64_t ll = vu[l];
+                        excite(up, kk, ll);
+                        jdet = index_find(&ix, det);
+                        if (jdet > idet) {
+                            const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_double(rup, ii, kk, jj, ll);
+                            R4(aaaa, ii, kk, jj, ll) += val2;
+                            R4(aaaa, ii, kk, ll, jj) -= val2;
+                            R4(aaaa, kk, ii, jj, ll) -= val2;
+                            R4(aaaa, kk, ii, ll, jj) += val2;
+                            R4(aaaa, jj, ll, ii, kk) += val2;
+                            R4(aaaa, jj, ll, kk, ii) -= val2;
+                            R4(aaaa, ll, jj, ii, kk) -= val2;
+                            R4(aaaa, ll, jj, kk, ii) += val2;
+                        }
+                        excite(up, ll, kk);
+                    }
+                }
+                excite(up, jj, ii);
+            }
+        }
+        for (int64_t i = 0; i < nod; ++i) {
+            int64_t ii = od[i];
+            bb[(n1 + 1) * ii] += val1;
+            for (int64_t k = i + 1; k < nod; ++k) {
+                int64_t kk = od[k];
+                R4(bbbb, ii, kk, ii, kk) += val1;
+                R4(bbbb, ii, kk, kk, ii) -= val1;
+                R4(bbbb, kk, ii, ii, kk) -= val1;
+                R4(bbbb, kk, ii, kk, ii) += val1;
+            }
+            for (int64_t j = 0; j < nvd; ++j) {
+                int64_t jj = vd[j];
+                excite(dn, ii, jj);
+                int64_t jdet = index_find(&ix, det);
+                if (jdet > idet) {
+                    const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_single(rdn, ii, jj);
+                    bb[ii * n1 + jj] += val2;
+                    bb[jj * n1 + ii] += val2;
+                    for (int64_t k = 0; k < nou; ++k) {
+                        int64_t kk = ou[k];
+                        R4(abab, kk, ii, kk, jj) += val2;
+                        R4(abab, kk, jj, kk, ii) += val2;
+                    }
+                    for (int64_t k = 0; k < nod; ++k) {
+                        if (i == k)
+                            continue;
+                        int64_t kk = od[k];
+                        R4(bbbb, ii, kk, jj, kk) += val2;
+                        R4(bbbb, ii, kk, kk, jj) -= val2;
+                        R4(bbbb, kk, ii, kk, jj) += val2;
+                        R4(bbbb, kk, ii, jj, kk) -= val2;
+                        R4(bbbb, jj, kk, ii, kk) += val2;
+                        R4(bbbb, jj, kk, kk, ii) -= val2;
+                        R4(bbbb, kk, jj, ii, kk) -= val2;
+                        R4(bbbb, kk, jj, kk, ii) += val2;
+                    }
+                }
+                for (int64_t k = i + 1; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = j + 1; l < nvd; ++l) {
+                        int64_t ll = vd[l];
+                        excite(dn, kk, ll);
+                        jdet = index_find(&ix, det);
+                        if (jdet > idet) {
+                            const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_double(rdn, ii, kk, jj, ll);
+                            R4(bbbb, ii, kk, jj, ll) += val2;
+                            R4(bbbb, ii, kk, ll, jj) -= val2;
+                            R4(bbbb, kk, ii, jj, ll) -= val2;
+                            R4(bbbb, kk, ii, ll, jj) += val2;
+                            R4(bbbb, jj, ll, ii, kk) += val2;
+                            R4(bbbb, ll, jj, ii, kk) -= val2;
+                            R4(bbbb, jj, ll, kk, ii) -= val2;
+                            R4(bbbb, ll, jj, kk, ii) += val2;
+                        }
+                        excite(dn, ll, kk);
+                    }
+                }
+                excite(dn, jj, ii);
+            }
+        }
+    }
+#undef R4
+    free(ix.slots);
+    return 0;
+}

@@ -63,6 +63,13 @@ int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int6
                 const double *coeffs, const double *one_mo, const double *two_mo, double eps, int64_t max_new,
                 uint64_t *out, int64_t *n_new);
 
+/* One- and two-particle RDMs of the wave function sum_i coeffs[i] |dets[i]>
+ * (compute_rdms): DOCI rdm1 = d0 [n][n], rdm2 = d2 [n][n]; FullCI rdm1 =
+ * [aa, bb] [2][n][n], rdm2 = [aaaa, bbbb, abab] [3][n][n][n][n].  Serial, in
+ * the reference's summation order. */
+int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                     const double *coeffs, double *rdm1, double *rdm2);
+
 #ifdef __cplusplus
 }
 #endif

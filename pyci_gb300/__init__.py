@@ -4,7 +4,8 @@ Drop-in for the ``pyci`` names on the sparse-operator path
 (pyci/__init__.py:18-31): ``secondquant_op`` (alias ``hamiltonian``), the
 ``doci_wfn`` / ``fullci_wfn`` / ``genci_wfn`` wave functions, ``sparse_op``
 (CSR build, ``op(x)``, ``op.solve``, ``op.update``), ``add_hci`` (heat-bath
-CI selection), ``popcnt``, ``ctz``, thread-count helpers and
+CI selection), ``compute_rdms`` (with ``spinize_rdms`` and
+``reduce_senzero_integrals``), ``popcnt``, ``ctz``, thread-count helpers and
 ``add_excitations``.  The operator runs on the GPU through
 ``libpyci_gb300.so``; importing works without a GPU, building an operator
 does not.
@@ -21,6 +22,7 @@ try:
     from pyci_gb300._pyci import (  # noqa: F401
         __version__,
         add_hci,
+        compute_rdms,
         c_double,
         c_long,
         c_ulong,
@@ -45,6 +47,7 @@ except ImportError as exc:  # pragma: no cover - exercised only on a broken buil
     ) from exc
 
 from pyci_gb300.excitation import add_excitations  # noqa: E402,F401
+from pyci_gb300.utility import reduce_senzero_integrals, spinize_rdms  # noqa: E402,F401
 
 hamiltonian = secondquant_op
 
@@ -70,6 +73,9 @@ __all__ = [
     "ctz",
     "add_excitations",
     "add_hci",
+    "compute_rdms",
+    "reduce_senzero_integrals",
+    "spinize_rdms",
     "gpu_version",
     "LIBRARY_PATH",
 ]

@@ -28,7 +28,7 @@ SYMBOLS = [
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
-    "pyci_gpu_gram_device", "pyci_gpu_add_hci",
+    "pyci_gpu_gram_device", "pyci_gpu_add_hci", "pyci_gpu_compute_rdms",
 ]
 
 
@@ -83,6 +83,7 @@ def lib():
             "pyci_gpu_gram_device": (_int, [_p, _int, _p, _i64, _p, _i64, _i64, _p]),
             "pyci_gpu_add_hci": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _int,
                                         _i64, _p, ctypes.POINTER(_i64)]),
+            "pyci_gpu_compute_rdms": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -161,6 +162,19 @@ class Context:
             if n.value <= cap:
                 return out[:n.value]
             cap = n.value
+
+    def compute_rdms(self, kind, nbasis, nocc_up, nocc_dn, dets, coeffs):
+        r"""(rdm1, rdm2) of a CI vector: DOCI (d0, d2) [n, n]; FullCI [2, n, n], [3, n, n, n, n]."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        n = nbasis
+        if kind == WFN_FULLCI:
+            r1, r2 = np.empty((2, n, n)), np.empty((3, n, n, n, n))
+        else:
+            r1, r2 = np.empty((n, n)), np.empty((n, n))
+        check(lib().pyci_gpu_compute_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
+                                          _ptr(coeffs), _ptr(r1), _ptr(r2)))
+        return r1, r2
 
     def gram_device(self, method, a_ptr, p, b_ptr, q, n):
         r"""C = A^T B (f64[p][q], host) for FP32 device vector blocks A [p][n] and B [q][n]."""

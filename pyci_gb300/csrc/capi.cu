@@ -544,4 +544,21 @@ int pyci_gpu_add_hci(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_u
                              max_new, out, n_new);
 }
 
+int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                          int64_t ndet, const uint64_t *dets, const double *coeffs, double *rdm1, double *rdm2) {
+    if (!ctx || !rdm1 || !rdm2 || (ndet > 0 && (!dets || !coeffs))) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    if (ndet < 0) {
+        set_error("negative determinant count");
+        return PYCI_GPU_EINVAL;
+    }
+    int rc = validate_wfn(kind, nbasis, nocc_up, nocc_dn);
+    if (rc)
+        return rc;
+    PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    return rdm_compute_device(ctx, kind, nbasis, ndet, dets, coeffs, rdm1, rdm2);
+}
+
 } // extern "C"

@@ -655,6 +655,26 @@ long add_hci(const SQuantOp &ham, Wfn &wfn, Array<double> coeffs, double eps, in
     return wfn.ndet - before;
 }
 
+// compute_rdms (pyci/src/rdm.cpp:1011-1055): DOCI (d0, d2), FullCI
+// (rdm1 [2, n, n], rdm2 [3, n, n, n, n]) on the device.
+py::tuple compute_rdms(const Wfn &wfn, Array<double> coeffs) {
+    if (coeffs.size() < wfn.ndet)
+        throw std::invalid_argument("coeffs has fewer entries than the wave function has determinants");
+    const long n = wfn.nbasis;
+    const bool fci = wfn.kind() == PYCI_WFN_FULLCI;
+    Array<double> r1 = fci ? Array<double>({2L, n, n}) : Array<double>({n, n});
+    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n}) : Array<double>({n, n});
+    auto ctx = default_ctx();
+    const double *c = coeffs.data();
+    double *p1 = r1.mutable_data(), *p2 = r2.mutable_data();
+    {
+        py::gil_scoped_release nogil;
+        check(pyci_gpu_compute_rdms(ctx.get(), wfn.kind(), wfn.nbasis, wfn.nocc_up, wfn.nocc_dn, wfn.ndet,
+                                    wfn.ndet ? wfn.dets.data() : nullptr, c, p1, p2));
+    }
+    return py::make_tuple(r1, r2);
+}
+
 // ---------------------------------------------------------------- numpy views
 
 Array<ulong_t> one_det(const Wfn &w, long i, bool two) {
@@ -1218,6 +1238,12 @@ PYBIND11_MODULE(_pyci, m) {
         return add_hci(h, w, c, eps, exact ? PYCI_BUILD_GENCI_EXACT : 0);
     }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("eps") = 1.0e-5, py::arg("nthread") = -1,
         py::arg("genci_exact") = false);
+    m.def("compute_rdms", [](const DOCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
+          py::arg("coeffs"));
+    m.def("compute_rdms", [](const FullCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
+          py::arg("coeffs"));
+    m.def("compute_rdms", [](const GenCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
+          py::arg("coeffs"));
     m.def("get_num_threads", []() { return g_threads; });
     m.def("set_num_threads", [](long n) { g_threads = std::max(1L, n); }, py::arg("n"));
     m.def("popcnt", [](Array<ulong_t> d) {

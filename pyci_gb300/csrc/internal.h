@@ -105,6 +105,9 @@ int device_exclusive_scan(const int64_t *counts, int64_t n, int64_t *out, cudaSt
 // Device determinant hash table (build.cu): slots from the stream's pool.
 int det_table_build(const uint64_t *d_dets, int64_t ndet, int nwords, cudaStream_t st, int *d_err,
                     int32_t **slots, uint64_t *mask);
+// Reduced density matrices on the device (rdm.cu), pyci_gpu_compute_rdms.
+int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet, const uint64_t *dets,
+                       const double *coeffs, double *rdm1, double *rdm2);
 // Heat-bath CI selection on the device (hci.cu), pyci_gpu_add_hci.
 int hci_select_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
                       const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,

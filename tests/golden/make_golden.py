@@ -3,7 +3,7 @@ r"""Generate the golden fixtures in tests/golden/ from the reference itself.
 Run in a container that has the reference source tree:
 
     make -C oracle ref port            # reference built against the shims + C oracle
-    python tests/golden/make_golden.py [--big | --only-big | --only-hci]
+    python tests/golden/make_golden.py [--big | --only-big | --only-hci | --only-rdm]
 
 Outputs (all committed):
   kat_<system>.npz      integrals of the FCIDUMP files the reference's known-answer
@@ -13,6 +13,8 @@ Outputs (all committed):
                         synthetic cases, built by pyci.sparse_op of the reference
   hci_<case>.npz        one heat-bath CI step of the reference (pyci.add_hci): input
                         determinants and coefficients, and the set it added
+  rdm_<case>.npz        the reference's pyci.compute_rdms (DOCI d0/d2, FullCI
+                        rdm1/rdm2) of seeded random coefficient vectors
   digests.json          order-independent digests of the reference CSR for the
                         larger synthetic workloads, and reference eigenvalues
 The reference is imported from oracle/_ref (the unchanged sources compiled
@@ -186,6 +188,40 @@ def hci_fixtures(pyci):
     return meta
 
 
+RDM_CASES = [
+    # name, kind, nbasis, nocc_up, nocc_dn, excitations of the set (None = all), seed
+    ("doci_10_4", "doci", 10, 4, 4, None, 51),
+    ("doci_12_5_cisd", "doci", 12, 5, 5, (0, 1, 2), 52),
+    ("fci_6_3_2", "fullci", 6, 3, 2, None, 53),
+    ("fci_7_3_3_cisd", "fullci", 7, 3, 3, (0, 1, 2), 54),
+]
+
+
+def rdm_fixtures(pyci):
+    r"""The reference's pyci.compute_rdms of seeded random (normalised)
+    coefficient vectors on full and CISD determinant sets, and its
+    pyci.spinize_rdms of them."""
+    meta = []
+    for name, kind, n, nu, nd, exc, seed in RDM_CASES:
+        W = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn}[kind]
+        wfn = W(n, nu, nd)
+        if exc is None:
+            wfn.add_all_dets()
+        else:
+            pyci.add_excitations(wfn, *exc)
+        coeffs = np.random.default_rng(seed).normal(size=len(wfn))
+        coeffs /= np.linalg.norm(coeffs)
+        rdm1, rdm2 = pyci.compute_rdms(wfn, coeffs)
+        spin1, spin2 = pyci.spinize_rdms(rdm1, rdm2)
+        dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
+        np.savez_compressed(os.path.join(HERE, "rdm_%s.npz" % name), dets=dets, coeffs=coeffs,
+                            rdm1=np.asarray(rdm1), rdm2=np.asarray(rdm2), spin1=spin1, spin2=spin2)
+        meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd, "seed": seed,
+                     "ndet": len(wfn)})
+        print("rdm", name, len(wfn), flush=True)
+    return meta
+
+
 WORKLOADS = [
     # name, kind, nbasis, nocc, config index (seed 1000 + index), roots
     ("fci_8_4_4", "fullci", 8, (4, 4), 1, 4),
@@ -228,13 +264,17 @@ def main():
     ap.add_argument("--big", action="store_true")
     ap.add_argument("--only-big", action="store_true")
     ap.add_argument("--only-hci", action="store_true")
+    ap.add_argument("--only-rdm", action="store_true")
     args = ap.parse_args()
     import pyci  # the reference, from oracle/_ref
     path = os.path.join(HERE, "digests.json")
-    if args.only_hci:
+    if args.only_hci or args.only_rdm:
         with open(path) as f:
             meta = json.load(f)
-        meta["hci_cases"] = hci_fixtures(pyci)
+        if args.only_hci:
+            meta["hci_cases"] = hci_fixtures(pyci)
+        if args.only_rdm:
+            meta["rdm_cases"] = rdm_fixtures(pyci)
     elif args.only_big:
         with open(path) as f:
             meta = json.load(f)
@@ -242,7 +282,7 @@ def main():
                                   if k in dict((w[0], 1) for w in BIG_WORKLOADS)})
     else:
         meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci), "hci_cases": hci_fixtures(pyci),
-                "workloads": workload_digests(pyci, args.big)}
+                "rdm_cases": rdm_fixtures(pyci), "workloads": workload_digests(pyci, args.big)}
     with open(path, "w") as f:
         json.dump(meta, f, indent=1)
 

@@ -134,3 +134,57 @@ def test_add_hci_thresholds():
     assert {tuple(r) for r in every} == connected
     assert O.add_hci(O.FULLCI, 6, 2, 2, hf, np.array([0.0]), one, two, 1e-9).shape[0] == 0
     assert O.add_hci(O.FULLCI, 6, 2, 2, hf, np.array([1.0]), one, two, 1e9).shape[0] == 0
+
+
+def load_rdm_case(name):
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "rdm_%s.npz" % name))
+    return {k: z[k] for k in z.files}
+
+
+def test_compute_rdms_bit_identical_to_reference(golden):
+    r"""The oracle's compute_rdms (pyci/src/rdm.cpp, reference summation order)
+    reproduces the reference's arrays exactly; spinize_rdms restated here
+    reproduces the reference's utility."""
+    from pyci_gb300.utility import spinize_rdms
+    for m in golden["rdm_cases"]:
+        z = load_rdm_case(m["name"])
+        r1, r2 = O.compute_rdms(KIND[m["wfn"]], m["nbasis"], m["nocc_up"], m["nocc_dn"], z["dets"], z["coeffs"])
+        assert np.array_equal(r1, z["rdm1"]) and np.array_equal(r2, z["rdm2"]), m["name"]
+        s1, s2 = spinize_rdms(z["rdm1"], z["rdm2"])
+        np.testing.assert_allclose(s1, z["spin1"], rtol=0, atol=1e-15)
+        np.testing.assert_allclose(s2, z["spin2"], rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("kind", ["doci", "fullci"])
+def test_rdm_energy_identities(kind):
+    r"""<c|H|c> from the RDMs equals the CSR quadratic form: DOCI through the
+    reduced seniority-zero integrals (pyci/utility.py:59-91), FullCI through
+    the spin-orbital RDMs and integrals."""
+    from pyci_gb300.utility import reduce_senzero_integrals, spinize_rdms
+    n, nu, nd = (8, 3, 3) if kind == "doci" else (6, 3, 2)
+    ecore, one, two = synthetic_integrals(n, 61)
+    dets = O.all_dets(KIND[kind], n, nu, nd)
+    c = np.random.default_rng(3).normal(size=dets.shape[0])
+    c /= np.linalg.norm(c)
+    csr = O.build_csr(KIND[kind], n, nu, nd, dets, one, two)
+    e_ref = c @ O.spmv(*csr, c)
+    r1, r2 = O.compute_rdms(KIND[kind], n, nu, nd, dets, c)
+    if kind == "doci":
+        assert np.trace(r1) == pytest.approx(nu, abs=1e-12)
+        assert np.sum(r2) == pytest.approx(nu * (nu - 1), abs=1e-12)
+        h, v, w = O.senzero(one, two)
+        k0, k2 = reduce_senzero_integrals(h, v, w, nu)
+        e = np.einsum("ij,ij", k0, r1) + np.einsum("ij,ij", k2, r2)
+    else:
+        s1, s2 = spinize_rdms(r1, r2)
+        # spin-orbital integrals (alpha block first), physicist's notation
+        o2 = np.kron(np.eye(2), one)
+        t2 = np.zeros((2 * n,) * 4)
+        for s in (0, n):
+            for t in (0, n):
+                t2[s:s + n, t:t + n, s:s + n, t:t + n] = two
+        # 1/2 <pq|rs> G_pqrs = 1/4 <pq||rs> G_pqrs for the antisymmetric G
+        e = np.einsum("ij,ij", o2, s1) + 0.5 * np.einsum("ijkl,ijkl", t2, s2)
+        assert np.allclose(s1, s1.T)
+    assert e == pytest.approx(e_ref, abs=1e-12)
