@@ -33,6 +33,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
+    "fci8": {"workload": "FullCI nbasis=8 4a4b (4900 dets), lowest root, synthetic seeded integrals",
+             "wfn": "fullci", "nbasis": 8, "nocc_up": 4, "nocc_dn": 4, "nroot": 1, "seed": 1001,
+             "golden": "fci_8_4_4",
+             "metric": "Davidson s/root at <=1 uHa (FP32-mixed), FCI(8o,8e) lowest root; SpMV GB/s"},
+    "doci24": {"workload": "DOCI nbasis=24 6 pairs (134596 dets), lowest root, tol 1e-8, synthetic seeded integrals",
+               "wfn": "doci", "nbasis": 24, "nocc_up": 6, "nocc_dn": 6, "nroot": 1, "seed": 1002, "tol": 1e-8,
+               "golden": "doci_24_6",
+               "metric": "Davidson s/root at <=1 uHa (FP32-mixed), DOCI(24o, 6 pairs) lowest root; SpMV GB/s"},
     "fci12": {"workload": "FullCI nbasis=12 5a5b (627264 dets), lowest 4 roots, synthetic seeded integrals",
               "wfn": "fullci", "nbasis": 12, "nocc_up": 5, "nocc_dn": 5, "nroot": 4, "seed": 1003,
               "golden": "fci_12_5_5",
@@ -167,9 +175,10 @@ def cpu_solve(nthreads):
     from pyci_gb300.synth import synthetic_integrals
     O.build()
     ecore, one, two = synthetic_integrals(WORKLOAD["nbasis"], WORKLOAD["seed"])
+    kind = O.FULLCI if WORKLOAD["wfn"] == "fullci" else O.DOCI
     t0 = time.perf_counter()
-    dets = O.all_dets(O.FULLCI, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"])
-    csr = O.build_csr(O.FULLCI, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"], dets, one, two,
+    dets = O.all_dets(kind, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"])
+    csr = O.build_csr(kind, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"], dets, one, two,
                       nthreads=nthreads)
     t1 = time.perf_counter()
     import scipy.sparse.linalg as spl
@@ -177,7 +186,7 @@ def cpu_solve(nthreads):
     op = spl.LinearOperator((n, n), matvec=lambda x: O.spmv(*csr, np.ravel(x), nthreads=nthreads),
                             dtype=np.float64)
     # Seeded random start, as the reference's Spectra solver starts from a random vector.
-    evals = spl.eigsh(op, k=WORKLOAD["nroot"], which="SA", tol=TOL, return_eigenvectors=False,
+    evals = spl.eigsh(op, k=WORKLOAD["nroot"], which="SA", tol=WORKLOAD.get("tol", TOL), return_eigenvectors=False,
                       v0=np.random.default_rng(7).standard_normal(n), ncv=2 * WORKLOAD["nroot"] + 12)
     t2 = time.perf_counter()
     return t2 - t0, t1 - t0, np.sort(evals) + ecore
@@ -232,10 +241,12 @@ def run_ours(args, world, rank, local):
     nrow, ncol, size, stored = csr.shape()
     csr.prepare_mixed()
 
+    tol = WORKLOAD.get("tol", TOL)
+
     def solve(mode):
         # Eigenvalues only: the device-resident metric does not copy the
         # eigenvectors out (the e2e number below does).
-        return csr.solve(n=nroot, tol=TOL, ecore=ecore, mode=mode, evecs=False)
+        return csr.solve(n=nroot, tol=tol, ecore=ecore, mode=mode, evecs=False)
 
     for _ in range(args.warmup):
         solve(capi.SOLVE_MIXED)
@@ -319,7 +330,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         op = pyci.sparse_op(ham, wfn)
-        es, cs = op.solve(n=nroot, tol=TOL, mode="mixed")
+        es, cs = op.solve(n=nroot, tol=tol, mode="mixed")
         t1 = time.perf_counter()
         del op
         if i > 0:  # first is a warm-up
@@ -330,25 +341,27 @@ def run_ours(args, world, rank, local):
 
     # ---- CPU baseline sample (rank 0 only, N = 1)
     cpu = None
-    if rank == 0 and world == 1 and not args.skip_cpu and fci:
+    if rank == 0 and world == 1 and not args.skip_cpu and (fci or ndet < 10**6):
         nthreads = os.cpu_count() or 1
         tcpu, tbuild, ev_cpu = cpu_solve(nthreads)
         cpu = {"value": tcpu / nroot, "unit": "s/root", "cores": nthreads, "kind": "port",
                "sample": "one full solve of the same workload: C oracle CSR build (%.1f s, %d threads) + "
-                         "ARPACK IRL on the oracle's threaded SpMV, tol %.0e" % (tbuild, nthreads, TOL)}
+                         "ARPACK IRL on the oracle's threaded SpMV, tol %.0e" % (tbuild, nthreads, tol)}
 
     if rank != 0:
         return
     errs = None
     if ref is not None:
-        errs = {"mixed_uHa": list(np.abs(np.sort(evals_mixed) - ecore - ref) * 1e6),
-                "fp64_uHa": list(np.abs(np.sort(evals64) - ecore - ref) * 1e6)}
+        errs = {"mixed_uHa": list(np.abs(np.sort(evals_mixed) - ecore - ref[:nroot]) * 1e6),
+                "fp64_uHa": list(np.abs(np.sort(evals64) - ecore - ref[:nroot]) * 1e6)}
     line = {
         "metric": METRIC, "value": value, "unit": "s/root", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic seeded integrals (seed %d)" % WORKLOAD["seed"],
         "config": {"workload": WORKLOAD["workload"], "ndet": N, "nnz_stored": stored, "nnz_reference": size,
-                   "roots": nroot, "tol": TOL, "l2": "matrix (GBs) >> 129 MB L2; no flush needed",
+                   "roots": nroot, "tol": tol,
+                   "l2": ("matrix (%.1f GB) >> 129 MB L2; no flush needed" % (bytes32 / 1e9)) if bytes32 > 2**28
+                   else "matrix (%.0f MB) fits in the 129 MB L2: SpMV figures are L2-resident" % (bytes32 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"s_per_root": fp64_spr, "iterations": st64["iterations"], "matvecs": st64["matvecs"]},
         "speedup_mixed_vs_fp64": fp64_spr / (ms_step / 1e3 / nroot),
@@ -475,6 +488,71 @@ def run_batch(args, world=1, rank=0, local=0):
     print(json.dumps(line), flush=True)
 
 
+def run_hci(args, world=1, rank=0, local=0):
+    r"""One heat-bath CI selection step (add_hci) on the 12-orbital FCI
+    Hamiltonian: the wave function is every determinant of the FP64 ground
+    state with |c| > 1e-4, in colex order, with those coefficients; the step
+    uses eps = 1e-5.  value = seconds per step through the C ABI (host arrays
+    in and out, as the reference's call); the same step of the CPU oracle
+    (a serial restatement of pyci/src/hci.cpp) is the baseline, and the two
+    results must be identical.  Independent replicas under torchrun."""
+    import torch
+    from math import comb
+    from pyci_gb300 import capi
+    from pyci_gb300.synth import synthetic_integrals
+    torch.cuda.set_device(local)
+    nb, na, nbeta, eps = 12, 5, 5, 1.0e-5
+    ctx = capi.Context(local)
+    ecore, one, two = synthetic_integrals(nb, 1003)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, na, nbeta, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                   ndet=comb(nb, na) * comb(nb, nbeta))
+    _, vecs, _ = csr.solve(n=1, tol=1e-8, ecore=ecore, mode=capi.SOLVE_FP64)
+    csr.free()
+    full = ctx.add_all_dets(capi.WFN_FULLCI, nb, na, nbeta)
+    keep = np.nonzero(np.abs(vecs[0]) > 1e-4)[0]
+    dets, coeffs = np.ascontiguousarray(full[keep]), np.ascontiguousarray(vecs[0][keep])
+    del full
+    for _ in range(args.warmup):
+        new = ctx.add_hci(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs, one, two, eps)
+    lib = capi.lib()
+    barrier(world)
+    launches0 = lib.pyci_gpu_kernel_launches()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            new = ctx.add_hci(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs, one, two, eps)
+            times.append(time.perf_counter() - t0)
+    launches = (lib.pyci_gpu_kernel_launches() - launches0) // args.steps
+    t_gpu = max_over_ranks(statistics.median(times), world)
+    if rank != 0:
+        return
+    line = {"metric": "heat-bath CI selection step (add_hci) seconds, FCI(12o,10e)", "value": t_gpu, "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_gpu * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded integrals (seed 1003)",
+            "config": {"workload": "add_hci on FCI nbasis=12 5a5b: determinants with |c| > 1e-4 in the FP64 "
+                                   "ground state, eps = 1e-5", "ndet_in": int(dets.shape[0]),
+                       "added": int(new.shape[0]), "parallelism": "replicas"},
+            "e2e": {"value": t_gpu, "unit": "s", "h2d_bytes_per_step": int(dets.nbytes + coeffs.nbytes + one.nbytes
+                                                                           + two.nbytes),
+                    "d2h_bytes_per_step": int(new.nbytes)},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    if not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        ref = O.add_hci(O.FULLCI, nb, na, nbeta, dets, coeffs, one, two, eps)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": t_cpu, "unit": "s", "cores": 1, "kind": "port",
+                                "sample": "the same step with the C oracle (serial restatement of pyci/src/hci.cpp; "
+                                          "the reference's add_hci runs PYCI_NUM_THREADS = 1 threads by default)"}
+        line["parity"] = "identical to the oracle" if np.array_equal(new, ref) else "MISMATCH vs the oracle"
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_gram(args):
     r"""Profiling driver (for ncu): FP32 Gram products C = A^T B of --gram P Q N
     (random vectors, N rows), on the CUDA cores then on the tensor cores,
@@ -549,9 +627,10 @@ def main():
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--wfn", choices=["fullci", "doci"], default="fullci", help="wave function of --case")
-    ap.add_argument("--workload", choices=["fci12", "doci32", "batch64"], default="fci12",
-                    help="fci12: the headline FCI(12o,10e) line; doci32: DOCI(32o, 8 pairs); "
-                         "batch64: the 64-problem batched solve")
+    ap.add_argument("--workload", choices=["fci12", "doci32", "fci8", "doci24", "batch64", "hci"], default="fci12",
+                    help="fci12: the headline FCI(12o,10e) line; doci32: DOCI(32o, 8 pairs); fci8 / doci24: the "
+                         "8-orbital FCI and 24-orbital DOCI cases; batch64: the 64-problem batched solve; "
+                         "hci: one heat-bath CI selection step")
     args = ap.parse_args()
     global WORKLOAD, METRIC
     if args.workload in WORKLOADS:
@@ -561,6 +640,17 @@ def main():
         run_profile_case(args)
         return
     world, rank, local = dist_init(args)
+    if args.workload == "hci":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference arm of this workload is the "
+                                  "cpu_baseline of the ours line (the same step with the CPU oracle)"}), flush=True)
+        else:
+            run_hci(args, world, rank, local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return
     if args.workload == "batch64":
         if args.impl == "reference":
             if rank == 0:
