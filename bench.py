@@ -553,6 +553,68 @@ def run_hci(args, world=1, rank=0, local=0):
     print(json.dumps(line), flush=True)
 
 
+def run_rdm(args, world=1, rank=0, local=0):
+    r"""compute_rdms of the FP64 ground state of the 10-orbital 5a5b FCI
+    Hamiltonian (63,504 determinants): rdm1 [2, 10, 10] and rdm2
+    [3, 10, 10, 10, 10].  value = seconds per call through the C ABI (host
+    arrays in and out, as the reference's call); the same call of the CPU
+    oracle (a serial restatement of pyci/src/rdm.cpp, as the reference runs it)
+    is the baseline, and the arrays must agree to 1e-12.  Replicas under
+    torchrun."""
+    import torch
+    from math import comb
+    from pyci_gb300 import capi
+    from pyci_gb300.synth import synthetic_integrals
+    torch.cuda.set_device(local)
+    nb, na, nbeta = 10, 5, 5
+    ctx = capi.Context(local)
+    ecore, one, two = synthetic_integrals(nb, 1000 + nb)
+    ndet = comb(nb, na) * comb(nb, nbeta)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, na, nbeta, None, one, two, flags=capi.BUILD_FULL_COLEX, ndet=ndet)
+    _, vecs, _ = csr.solve(n=1, tol=1e-8, ecore=ecore, mode=capi.SOLVE_FP64)
+    csr.free()
+    dets = ctx.add_all_dets(capi.WFN_FULLCI, nb, na, nbeta)
+    coeffs = np.ascontiguousarray(vecs[0])
+    for _ in range(args.warmup):
+        r1, r2 = ctx.compute_rdms(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs)
+    lib = capi.lib()
+    barrier(world)
+    launches0 = lib.pyci_gpu_kernel_launches()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r1, r2 = ctx.compute_rdms(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs)
+            times.append(time.perf_counter() - t0)
+    launches = (lib.pyci_gpu_kernel_launches() - launches0) // args.steps
+    t_gpu = max_over_ranks(statistics.median(times), world)
+    if rank != 0:
+        return
+    line = {"metric": "compute_rdms seconds, FCI(10o,10e) ground state", "value": t_gpu, "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_gpu * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded integrals (seed %d)" % (1000 + nb),
+            "config": {"workload": "compute_rdms of the FP64 ground state, FCI nbasis=10 5a5b (63504 dets)",
+                       "ndet": int(ndet), "parallelism": "replicas"},
+            "e2e": {"value": t_gpu, "unit": "s", "h2d_bytes_per_step": int(dets.nbytes + coeffs.nbytes),
+                    "d2h_bytes_per_step": int(r1.nbytes + r2.nbytes)},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    if not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        o1, o2 = O.compute_rdms(O.FULLCI, nb, na, nbeta, dets, coeffs)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": t_cpu, "unit": "s", "cores": 1, "kind": "port",
+                                "sample": "the same call with the C oracle (serial restatement of pyci/src/rdm.cpp, "
+                                          "which the reference runs on one thread)"}
+        diff = max(float(np.abs(r1 - o1).max()), float(np.abs(r2 - o2).max()))
+        line["parity"] = {"max_abs_diff_vs_oracle": diff, "ok": diff < 1e-12}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_gram(args):
     r"""Profiling driver (for ncu): FP32 Gram products C = A^T B of --gram P Q N
     (random vectors, N rows), on the CUDA cores then on the tensor cores,
@@ -627,10 +689,11 @@ def main():
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--wfn", choices=["fullci", "doci"], default="fullci", help="wave function of --case")
-    ap.add_argument("--workload", choices=["fci12", "doci32", "fci8", "doci24", "batch64", "hci"], default="fci12",
+    ap.add_argument("--workload", choices=["fci12", "doci32", "fci8", "doci24", "batch64", "hci", "rdm"],
+                    default="fci12",
                     help="fci12: the headline FCI(12o,10e) line; doci32: DOCI(32o, 8 pairs); fci8 / doci24: the "
                          "8-orbital FCI and 24-orbital DOCI cases; batch64: the 64-problem batched solve; "
-                         "hci: one heat-bath CI selection step")
+                         "hci: one heat-bath CI selection step; rdm: compute_rdms of a FCI ground state")
     args = ap.parse_args()
     global WORKLOAD, METRIC
     if args.workload in WORKLOADS:
@@ -640,13 +703,15 @@ def main():
         run_profile_case(args)
         return
     world, rank, local = dist_init(args)
-    if args.workload == "hci":
+    if args.workload in ("hci", "rdm"):
         if args.impl == "reference":
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the reference arm of this workload is the "
-                                  "cpu_baseline of the ours line (the same step with the CPU oracle)"}), flush=True)
-        else:
+                                  "cpu_baseline of the ours line (the same call with the CPU oracle)"}), flush=True)
+        elif args.workload == "hci":
             run_hci(args, world, rank, local)
+        else:
+            run_rdm(args, world, rank, local)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()

@@ -153,7 +153,7 @@ class Context:
         two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
         nw = dets.shape[1] if dets.ndim == 2 else ((nbasis + 63) // 64) * (2 if kind == WFN_FULLCI else 1)
         n = _i64(0)
-        cap = max(4096, 4 * dets.shape[0])
+        cap = max(1 << 16, 16 * dets.shape[0])  # a second call (full recount) only past this
         while True:
             out = np.zeros((cap, nw), dtype=np.uint64)
             check(lib().pyci_gpu_add_hci(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),

@@ -635,7 +635,9 @@ long add_hci(const SQuantOp &ham, Wfn &wfn, Array<double> coeffs, double eps, in
         throw std::invalid_argument("coeffs has fewer entries than the wave function has determinants");
     const long nw = wfn.words();
     auto ctx = default_ctx();
-    int64_t cap = std::max<int64_t>(4096, 4 * wfn.ndet), n_new = 0;
+    // A step adds at most ~(connections per determinant) x ndet; a buffer of
+    // 16 ndet avoids the second call (a full recount) in practice.
+    int64_t cap = std::max<int64_t>(1 << 16, 16 * wfn.ndet), n_new = 0;
     std::vector<ulong_t> out;
     for (;;) {
         out.assign(static_cast<size_t>(cap * nw), 0);
