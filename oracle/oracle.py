@@ -57,6 +57,9 @@ def lib():
         L.orc_phase_double.argtypes = [_p, _i64, _i64, _i64, _i64]
         L.orc_compute_rdms.restype = ctypes.c_int
         L.orc_compute_rdms.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]
+        L.orc_compute_enpt2.restype = ctypes.c_int
+        L.orc_compute_enpt2.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
         L.orc_add_hci.restype = ctypes.c_int
         L.orc_add_hci.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _i64, _p,
                                   ctypes.POINTER(_i64)]
@@ -196,3 +199,17 @@ def compute_rdms(kind, nbasis, nocc_up, nocc_dn, dets, coeffs):
     if L.orc_compute_rdms(kind, n, nocc_up, nocc_dn, dets.shape[0], _ptr(dets), _ptr(coeffs), _ptr(r1), _ptr(r2)):
         raise RuntimeError("orc_compute_rdms failed")
     return r1, r2
+
+
+def compute_enpt2(kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, energy, ecore, eps):
+    r"""Epstein-Nesbet second-order energy of pyci.compute_enpt2 (pyci/src/enpt2.cpp)."""
+    L = lib()
+    dets = np.ascontiguousarray(dets, dtype=np.uint64)
+    coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+    one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+    two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+    out = ctypes.c_double(0.0)
+    if L.orc_compute_enpt2(kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets), _ptr(coeffs), _ptr(one_mo),
+                           _ptr(two_mo), float(energy), float(ecore), float(eps), ctypes.byref(out)):
+        raise RuntimeError("orc_compute_enpt2 failed")
+    return out.value

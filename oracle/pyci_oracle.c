@@ -1162,3 +1162,215 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
     free(ix.slots);
     return 0;
 }
+
+/* ---------------- Epstein-Nesbet second-order correction ---------------- */
+
+typedef struct {
+    int64_t n, cap, nwords;
+    uint64_t *words;
+    double *val;
+} termbuf;
+
+static int term_push(termbuf *t, const uint64_t *d, double v) {
+    if (t->n == t->cap) {
+        int64_t cap = t->cap ? 2 * t->cap : 1024;
+        uint64_t *w = realloc(t->words, sizeof(uint64_t) * cap * t->nwords);
+        double *x = realloc(t->val, sizeof(double) * cap);
+        if (!w || !x) {
+            free(w ? w : t->words);
+            free(x ? x : t->val);
+            t->words = NULL;
+            t->val = NULL;
+            return -1;
+        }
+        t->words = w;
+        t->val = x;
+        t->cap = cap;
+    }
+    memcpy(t->words + t->n * t->nwords, d, sizeof(uint64_t) * t->nwords);
+    t->val[t->n++] = v;
+    return 0;
+}
+
+/* FullCI diagonal element of a determinant (compute_enpt2_thread_gather,
+ * pyci/src/enpt2.cpp:37-74): alpha terms with alpha-beta Coulomb, then beta. */
+static double fci_diag(int64_t nword, int64_t n1, const uint64_t *det, const double *one, const double *two) {
+    const int64_t n2 = n1 * n1, n3 = n1 * n2;
+    int64_t ou[256], od[256];
+    int64_t nou = fill_occs(nword, det, ou), nod = fill_occs(nword, det + nword, od);
+    double diag = 0.0;
+    for (int64_t i = 0; i < nou; ++i) {
+        int64_t j = ou[i];
+        diag += one[(n1 + 1) * j];
+        for (int64_t k = i + 1; k < nou; ++k) {
+            int64_t l = ou[k];
+            diag += TWO(j, l, j, l) - TWO(j, l, l, j);
+        }
+        for (int64_t k = 0; k < nod; ++k) {
+            int64_t l = od[k];
+            diag += TWO(j, l, j, l);
+        }
+    }
+    for (int64_t i = 0; i < nod; ++i) {
+        int64_t j = od[i];
+        diag += one[(n1 + 1) * j];
+        for (int64_t k = i + 1; k < nod; ++k) {
+            int64_t l = od[k];
+            diag += TWO(j, l, j, l) - TWO(j, l, l, j);
+        }
+    }
+    return diag;
+}
+
+/* compute_enpt2 (pyci/src/enpt2.cpp:76-197, 332-375) for FullCI
+ * determinants; DOCI runs through its FullCI image (alpha = beta string),
+ * as the reference does.  Every external determinant k reached from i with
+ * |H_ki| > eps / |c_i| collects H_ki c_i (phase included) in loop order;
+ * the result is energy + sum_k V_k^2 / (energy - ecore - H_kk). */
+int orc_compute_enpt2(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                      const double *coeffs, const double *one_mo, const double *two_mo, double energy, double ecore,
+                      double eps, double *result) {
+    const int64_t nword = orc_nword(nbasis), nw = 2 * nword, n1 = nbasis, n2 = n1 * n1, n3 = n1 * n2;
+    const double *one = one_mo, *two = two_mo;
+    (void)nocc_up;
+    (void)nocc_dn;
+    if ((kind != ORC_DOCI && kind != ORC_FULLCI) || nword > 4)
+        return -2;
+    uint64_t *fdets = malloc(sizeof(uint64_t) * (ndet ? ndet : 1) * nw);
+    if (!fdets)
+        return -1;
+    for (int64_t i = 0; i < ndet; ++i)
+        for (int64_t w = 0; w < nword; ++w) {
+            const uint64_t a = kind == ORC_DOCI ? dets[i * nword + w] : dets[i * nw + w];
+            const uint64_t b = kind == ORC_DOCI ? dets[i * nword + w] : dets[i * nw + nword + w];
+            fdets[i * nw + w] = a;
+            fdets[i * nw + nword + w] = b;
+        }
+    det_index ix;
+    if (index_build(&ix, ndet, nw, fdets)) {
+        free(fdets);
+        return -1;
+    }
+    termbuf t = {0, 0, nw, NULL, NULL};
+    int rc = 0;
+    uint64_t det[8];
+    int64_t ou[256], od[256], vu[256], vd[256];
+#define PUSH(v)                                                                                                        \
+    do {                                                                                                               \
+        if (index_find(&ix, det) == -1 && term_push(&t, det, (v)))                                                     \
+            rc = -1;                                                                                                   \
+    } while (0)
+    for (int64_t idet = 0; idet < ndet && !rc; ++idet) {
+        const uint64_t *rup = fdets + idet * nw, *rdn = rup + nword;
+        uint64_t *up = det, *dn = det + nword;
+        memcpy(det, rup, sizeof(uint64_t) * nw);
+        const double ci = coeffs[idet], eps_i = eps / fabs(ci);
+        int64_t nou = fill_occs(nword, rup, ou), nod = fill_occs(nword, rdn, od);
+        int64_t nvu = fill_virs(nword, n1, rup, vu), nvd = fill_virs(nword, n1, rdn, vd);
+        for (int64_t i = 0; i < nou && !rc; ++i) {
+            int64_t ii = ou[i];
+            for (int64_t j = 0; j < nvu && !rc; ++j) {
+                int64_t jj = vu[j];
+                excite(up, ii, jj);
+                const int sign_up = orc_phase_single(rup, ii, jj);
+                double val = one[n1 * ii + jj];
+                for (int64_t k = 0; k < nou; ++k) {
+                    int64_t kk = ou[k];
+                    val += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                }
+                for (int64_t k = 0; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    val += TWO(ii, kk, jj, kk);
+                }
+                if (fabs(val) > eps_i)
+                    PUSH(val * (sign_up * ci));
+                for (int64_t k = 0; k < nod && !rc; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = 0; l < nvd && !rc; ++l) {
+                        int64_t ll = vd[l];
+                        val = TWO(ii, kk, jj, ll);
+                        if (fabs(val) > eps_i) {
+                            excite(dn, kk, ll);
+                            PUSH(val * ((double)(sign_up * orc_phase_single(rdn, kk, ll)) * ci));
+                            excite(dn, ll, kk);
+                        }
+                    }
+                }
+                for (int64_t k = i + 1; k < nou && !rc; ++k) {
+                    int64_t kk = ou[k];
+                    for (int64_t l = j + 1; l < nvu && !rc; ++l) {
+                        int64_t ll = vu[l];
+                        val = TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj);
+                        if (fabs(val) > eps_i) {
+                            excite(up, kk, ll);
+                            PUSH(val * (orc_phase_double(rup, ii, kk, jj, ll) * ci));
+                            excite(up, ll, kk);
+                        }
+                    }
+                }
+                excite(up, jj, ii);
+            }
+        }
+        for (int64_t i = 0; i < nod && !rc; ++i) {
+            int64_t ii = od[i];
+            for (int64_t j = 0; j < nvd && !rc; ++j) {
+                int64_t jj = vd[j];
+                excite(dn, ii, jj);
+                double val = one[n1 * ii + jj];
+                for (int64_t k = 0; k < nou; ++k) {
+                    int64_t kk = ou[k];
+                    val += TWO(ii, kk, jj, kk);
+                }
+                for (int64_t k = 0; k < nod; ++k) {
+                    int64_t kk = od[k];
+                    val += TWO(ii, kk, jj, kk) - TWO(ii, kk, kk, jj);
+                }
+                if (fabs(val) > eps_i)
+                    PUSH(val * (orc_phase_single(rdn, ii, jj) * ci));
+                for (int64_t k = i + 1; k < nod && !rc; ++k) {
+                    int64_t kk = od[k];
+                    for (int64_t l = j + 1; l < nvd && !rc; ++l) {
+                        int64_t ll = vd[l];
+                        val = TWO(ii, kk, jj, ll) - TWO(ii, kk, ll, jj);
+                        if (fabs(val) > eps_i) {
+                            excite(dn, kk, ll);
+                            PUSH(val * (orc_phase_double(rdn, ii, kk, jj, ll) * ci));
+                            excite(dn, ll, kk);
+                        }
+                    }
+                }
+                excite(dn, jj, ii);
+            }
+        }
+    }
+#undef PUSH
+    free(ix.slots);
+    free(fdets);
+    if (rc) {
+        free(t.words);
+        free(t.val);
+        return -1;
+    }
+    /* Sum each determinant's contributions in loop order (the reference's
+     * per-thread order with one thread), then the correction. */
+    det_index cx;
+    if (index_build(&cx, t.n, nw, t.words)) {
+        free(t.words);
+        free(t.val);
+        return -1;
+    }
+    double *sum = calloc(t.n ? t.n : 1, sizeof(double));
+    for (int64_t c = 0; c < t.n; ++c)
+        sum[index_find(&cx, t.words + c * nw)] += t.val[c];
+    const double e = energy - ecore;
+    double correction = 0.0;
+    for (int64_t c = 0; c < t.n; ++c)
+        if (index_find(&cx, t.words + c * nw) == c)
+            correction += sum[c] * sum[c] / (e - fci_diag(nword, n1, t.words + c * nw, one, two));
+    *result = energy + correction;
+    free(sum);
+    free(cx.slots);
+    free(t.words);
+    free(t.val);
+    return 0;
+}

@@ -70,6 +70,14 @@ int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int6
 int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
                      const double *coeffs, double *rdm1, double *rdm2);
 
+/* Epstein-Nesbet second-order energy (compute_enpt2): energy + the sum over
+ * determinants k outside the wave function of V_k^2 / (energy - ecore - H_kk),
+ * V_k = sum of H_ki c_i over |H_ki| > eps / |c_i|.  DOCI through its FullCI
+ * image.  Writes the energy to *result. */
+int orc_compute_enpt2(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                      const double *coeffs, const double *one_mo, const double *two_mo, double energy, double ecore,
+                      double eps, double *result);
+
 #ifdef __cplusplus
 }
 #endif

@@ -3,7 +3,7 @@ r"""Generate the golden fixtures in tests/golden/ from the reference itself.
 Run in a container that has the reference source tree:
 
     make -C oracle ref port            # reference built against the shims + C oracle
-    python tests/golden/make_golden.py [--big | --only-big | --only-hci | --only-rdm]
+    python tests/golden/make_golden.py [--big | --only-big | --only-hci | --only-rdm | --only-enpt2]
 
 Outputs (all committed):
   kat_<system>.npz      integrals of the FCIDUMP files the reference's known-answer
@@ -15,6 +15,7 @@ Outputs (all committed):
                         determinants and coefficients, and the set it added
   rdm_<case>.npz        the reference's pyci.compute_rdms (DOCI d0/d2, FullCI
                         rdm1/rdm2) of seeded random coefficient vectors
+  enpt2_<case>.npz      the reference's pyci.compute_enpt2 of a solved ground state
   digests.json          order-independent digests of the reference CSR for the
                         larger synthetic workloads, and reference eigenvalues
 The reference is imported from oracle/_ref (the unchanged sources compiled
@@ -222,6 +223,47 @@ def rdm_fixtures(pyci):
     return meta
 
 
+ENPT2_CASES = [
+    # name, kind, nbasis, nocc_up, nocc_dn, excitations of the set, seed, eps
+    ("doci_10_4", "doci", 10, 4, 4, (0, 1), 71, 1e-4),
+    ("fci_7_3_2", "fullci", 7, 3, 2, (0, 1), 72, 1e-5),
+    ("fci_8_3_3", "fullci", 8, 3, 3, (0, 1, 2), 73, 1e-3),
+]
+# pyci/test/test_routines.py:473-491 (test_enpt2): system, wave function,
+# occupations and the expected ENPT2 energy (the cases whose data files exist).
+ENPT2_KATS = [
+    ("li2_ccpvdz", "doci", (3, 3), -14.90042952400693),
+    ("be_ccpvdz", "doci", (2, 2), -14.61920612157886),
+    ("be_ccpvdz", "fullci", (2, 2), -14.61740346031583),
+    ("h2o_ccpvdz", "doci", (5, 5), -76.04227376501808),
+]
+
+
+def enpt2_fixtures(pyci):
+    r"""The reference's pyci.compute_enpt2 (one thread) on the ground state of
+    seeded synthetic Hamiltonians over CISD-like sets, and the known answers of
+    its own test_enpt2."""
+    meta = []
+    for name, kind, n, nu, nd, exc, seed, eps in ENPT2_CASES:
+        ecore, one, two = synthetic_integrals(n, seed)
+        ham = pyci.secondquant_op(ecore, one, two)
+        wfn = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn}[kind](n, nu, nd)
+        pyci.add_excitations(wfn, *exc)
+        op = pyci.sparse_op(ham, wfn)
+        es, cs = op.solve(n=1, tol=1e-12)
+        e2 = pyci.compute_enpt2(ham, wfn, cs[0], es[0], eps, nthread=1)
+        dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
+        keys, vals = pack_8fold(two)
+        np.savez_compressed(os.path.join(HERE, "enpt2_%s.npz" % name), dets=dets, coeffs=np.asarray(cs[0]),
+                            energy=np.float64(es[0]), result=np.float64(e2), ecore=np.float64(ecore), one_mo=one,
+                            keys=keys, vals=vals)
+        meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd, "seed": seed, "eps": eps,
+                     "ndet": len(wfn), "energy": float(es[0]), "enpt2": float(e2)})
+        print("enpt2", name, len(wfn), es[0], e2, flush=True)
+    kats = [{"system": s, "wfn": w, "occs": list(o), "enpt2": e} for s, w, o, e in ENPT2_KATS]
+    return meta, kats
+
+
 WORKLOADS = [
     # name, kind, nbasis, nocc, config index (seed 1000 + index), roots
     ("fci_8_4_4", "fullci", 8, (4, 4), 1, 4),
@@ -265,12 +307,15 @@ def main():
     ap.add_argument("--only-big", action="store_true")
     ap.add_argument("--only-hci", action="store_true")
     ap.add_argument("--only-rdm", action="store_true")
+    ap.add_argument("--only-enpt2", action="store_true")
     args = ap.parse_args()
     import pyci  # the reference, from oracle/_ref
     path = os.path.join(HERE, "digests.json")
-    if args.only_hci or args.only_rdm:
+    if args.only_hci or args.only_rdm or args.only_enpt2:
         with open(path) as f:
             meta = json.load(f)
+        if args.only_enpt2:
+            meta["enpt2_cases"], meta["enpt2_kats"] = enpt2_fixtures(pyci)
         if args.only_hci:
             meta["hci_cases"] = hci_fixtures(pyci)
         if args.only_rdm:
@@ -281,8 +326,10 @@ def main():
         meta["workloads"].update({k: v for k, v in workload_digests(pyci, True).items()
                                   if k in dict((w[0], 1) for w in BIG_WORKLOADS)})
     else:
+        enpt2_cases, enpt2_kats = enpt2_fixtures(pyci)
         meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci), "hci_cases": hci_fixtures(pyci),
-                "rdm_cases": rdm_fixtures(pyci), "workloads": workload_digests(pyci, args.big)}
+                "rdm_cases": rdm_fixtures(pyci), "enpt2_cases": enpt2_cases, "enpt2_kats": enpt2_kats,
+                "workloads": workload_digests(pyci, args.big)}
     with open(path, "w") as f:
         json.dump(meta, f, indent=1)
 

@@ -188,3 +188,36 @@ def test_rdm_energy_identities(kind):
         e = np.einsum("ij,ij", o2, s1) + 0.5 * np.einsum("ijkl,ijkl", t2, s2)
         assert np.allclose(s1, s1.T)
     assert e == pytest.approx(e_ref, abs=1e-12)
+
+
+def test_compute_enpt2_matches_reference(golden):
+    from conftest import unpack_8fold
+    import os
+    for m in golden["enpt2_cases"]:
+        z = np.load(os.path.join(os.path.dirname(__file__), "golden", "enpt2_%s.npz" % m["name"]))
+        one = np.ascontiguousarray(z["one_mo"])
+        two = unpack_8fold(one, z["keys"], z["vals"])
+        r = O.compute_enpt2(KIND[m["wfn"]], m["nbasis"], m["nocc_up"], m["nocc_dn"], z["dets"], z["coeffs"], one, two,
+                            float(z["energy"]), float(z["ecore"]), m["eps"])
+        # Same terms; the final sum runs in another order than the reference's hash map.
+        assert r == pytest.approx(float(z["result"]), rel=0, abs=1e-13 * abs(float(z["result"])))
+
+
+@pytest.mark.parametrize("i", [0, 1, 2])
+def test_compute_enpt2_known_answers(golden, i):
+    r"""pyci/test/test_routines.py:473-491 (test_enpt2) with the oracle: CISD-like
+    set, FP64 ground state, eps = 1e-4, against the test's published values
+    (the 42,504-determinant water case runs on the GPU only)."""
+    import pyci_gb300 as pyci
+    k = golden["enpt2_kats"][i]
+    ecore, one, two = load_kat(k["system"])
+    n = one.shape[0]
+    wfn = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn}[k["wfn"]](n, *k["occs"])
+    pyci.add_excitations(wfn, *range(0, max(wfn.nocc - 1, 1)))
+    dets = np.asarray(wfn.to_det_array()).reshape(len(wfn), -1)
+    data, indices, indptr = O.build_csr(KIND[k["wfn"]], n, k["occs"][0], k["occs"][1], dets, one, two)
+    H = O.full_matrix(data, indices, indptr).toarray()
+    w, v = np.linalg.eigh(H)
+    e = O.compute_enpt2(KIND[k["wfn"]], n, k["occs"][0], k["occs"][1], dets, v[:, 0], one, two, w[0] + ecore, ecore,
+                        1.0e-4)
+    np.testing.assert_allclose(e, k["enpt2"], rtol=1e-7)
