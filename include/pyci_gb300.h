@@ -250,6 +250,18 @@ int pyci_gpu_add_hci(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_u
                      const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
                      double eps, int flags, int64_t max_new, uint64_t *out, int64_t *n_new);
 
+/* Epstein-Nesbet second-order energy (compute_enpt2, pyci/src/enpt2.cpp:332-375;
+ * binding pyci/src/binding.cpp:1344-1375): energy + sum over determinants k
+ * outside the wave function of V_k^2 / (energy - ecore - H_kk), where V_k sums
+ * H_ki coeffs[i] over the excitations with |H_ki| > eps / |coeffs[i]| (the
+ * selection of add_hci).  DOCI runs through its FullCI image, as the
+ * reference does; GenCI is EUNSUPPORTED.  V_k is summed with FP64 atomics (the
+ * reference sums in loop order), so results agree to rounding.  Writes the
+ * energy to *result. */
+int pyci_gpu_compute_enpt2(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                           int64_t ndet, const uint64_t *dets, const double *coeffs, const double *one_mo,
+                           const double *two_mo, double energy, double ecore, double eps, double *result);
+
 /* One- and two-particle reduced density matrices of sum_i coeffs[i] |dets[i]>
  * (compute_rdms, pyci/src/rdm.cpp:20-66 for DOCI, 269-530 for FullCI; binding
  * pyci/src/binding.cpp:1208-1291).  dets in the wave function's layout

@@ -5,7 +5,7 @@ Drop-in for the ``pyci`` names on the sparse-operator path
 ``doci_wfn`` / ``fullci_wfn`` / ``genci_wfn`` wave functions, ``sparse_op``
 (CSR build, ``op(x)``, ``op.solve``, ``op.update``), ``add_hci`` (heat-bath
 CI selection), ``compute_rdms`` (with ``spinize_rdms`` and
-``reduce_senzero_integrals``), ``popcnt``, ``ctz``, thread-count helpers and
+``reduce_senzero_integrals``), ``compute_enpt2``, ``popcnt``, ``ctz``, thread-count helpers and
 ``add_excitations``.  The operator runs on the GPU through
 ``libpyci_gb300.so``; importing works without a GPU, building an operator
 does not.
@@ -22,6 +22,7 @@ try:
     from pyci_gb300._pyci import (  # noqa: F401
         __version__,
         add_hci,
+        compute_enpt2,
         compute_rdms,
         c_double,
         c_long,
@@ -73,6 +74,7 @@ __all__ = [
     "ctz",
     "add_excitations",
     "add_hci",
+    "compute_enpt2",
     "compute_rdms",
     "reduce_senzero_integrals",
     "spinize_rdms",

@@ -28,7 +28,7 @@ SYMBOLS = [
     "pyci_gpu_csr_clone", "pyci_gpu_csr_shape", "pyci_gpu_csr_export", "pyci_gpu_csr_get_element",
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
-    "pyci_gpu_gram_device", "pyci_gpu_add_hci", "pyci_gpu_compute_rdms",
+    "pyci_gpu_gram_device", "pyci_gpu_add_hci", "pyci_gpu_compute_rdms", "pyci_gpu_compute_enpt2",
 ]
 
 
@@ -84,6 +84,8 @@ def lib():
             "pyci_gpu_add_hci": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _int,
                                         _i64, _p, ctypes.POINTER(_i64)]),
             "pyci_gpu_compute_rdms": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]),
+            "pyci_gpu_compute_enpt2": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double,
+                                              ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -175,6 +177,18 @@ class Context:
         check(lib().pyci_gpu_compute_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
                                           _ptr(coeffs), _ptr(r1), _ptr(r2)))
         return r1, r2
+
+    def compute_enpt2(self, kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, energy, ecore, eps):
+        r"""Epstein-Nesbet second-order energy (energy + correction)."""
+        dets = np.ascontiguousarray(dets, dtype=np.uint64)
+        coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
+        one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+        two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+        out = ctypes.c_double(0.0)
+        check(lib().pyci_gpu_compute_enpt2(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
+                                           _ptr(coeffs), _ptr(one_mo), _ptr(two_mo), float(energy), float(ecore),
+                                           float(eps), ctypes.byref(out)))
+        return out.value
 
     def gram_device(self, method, a_ptr, p, b_ptr, q, n):
         r"""C = A^T B (f64[p][q], host) for FP32 device vector blocks A [p][n] and B [q][n]."""

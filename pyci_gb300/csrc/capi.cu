@@ -561,4 +561,23 @@ int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t n
     return rdm_compute_device(ctx, kind, nbasis, ndet, dets, coeffs, rdm1, rdm2);
 }
 
+int pyci_gpu_compute_enpt2(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                           int64_t ndet, const uint64_t *dets, const double *coeffs, const double *one_mo,
+                           const double *two_mo, double energy, double ecore, double eps, double *result) {
+    if (!ctx || !result || !one_mo || !two_mo || (ndet > 0 && (!dets || !coeffs))) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    if (ndet < 0) {
+        set_error("negative determinant count");
+        return PYCI_GPU_EINVAL;
+    }
+    int rc = validate_wfn(kind, nbasis, nocc_up, nocc_dn);
+    if (rc)
+        return rc;
+    PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    return enpt2_device(ctx, kind, nbasis, nocc_up, nocc_dn, ndet, dets, coeffs, one_mo, two_mo, energy, ecore, eps,
+                        result);
+}
+
 } // extern "C"

@@ -677,6 +677,26 @@ py::tuple compute_rdms(const Wfn &wfn, Array<double> coeffs) {
     return py::make_tuple(r1, r2);
 }
 
+// compute_enpt2 (pyci/src/enpt2.cpp:332-375, binding pyci/src/binding.cpp:1344-1375):
+// Epstein-Nesbet second-order energy on the device.  nthread is accepted for
+// the reference's signature.
+double compute_enpt2(const SQuantOp &ham, const Wfn &wfn, Array<double> coeffs, double energy, double eps) {
+    if (ham.nbasis != wfn.nbasis)
+        throw std::invalid_argument("Hamiltonian and wave function have different nbasis");
+    if (coeffs.size() < wfn.ndet)
+        throw std::invalid_argument("coeffs has fewer entries than the wave function has determinants");
+    auto ctx = default_ctx();
+    double out = 0.0;
+    const double *c = coeffs.data();
+    {
+        py::gil_scoped_release nogil;
+        check(pyci_gpu_compute_enpt2(ctx.get(), wfn.kind(), wfn.nbasis, wfn.nocc_up, wfn.nocc_dn, wfn.ndet,
+                                     wfn.ndet ? wfn.dets.data() : nullptr, c, ham.one_mo.data(), ham.two_mo.data(),
+                                     energy, ham.ecore, eps, &out));
+    }
+    return out;
+}
+
 // ---------------------------------------------------------------- numpy views
 
 Array<ulong_t> one_det(const Wfn &w, long i, bool two) {
@@ -1246,6 +1266,18 @@ PYBIND11_MODULE(_pyci, m) {
           py::arg("coeffs"));
     m.def("compute_rdms", [](const GenCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
           py::arg("coeffs"));
+    m.def("compute_enpt2", [](const SQuantOp &h, const DOCIWfn &w, Array<double> c, double e, double eps, long) {
+        return compute_enpt2(h, w, c, e, eps);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("energy"), py::arg("eps") = 1.0e-5,
+          py::arg("nthread") = -1);
+    m.def("compute_enpt2", [](const SQuantOp &h, const FullCIWfn &w, Array<double> c, double e, double eps, long) {
+        return compute_enpt2(h, w, c, e, eps);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("energy"), py::arg("eps") = 1.0e-5,
+          py::arg("nthread") = -1);
+    m.def("compute_enpt2", [](const SQuantOp &h, const GenCIWfn &w, Array<double> c, double e, double eps, long) {
+        return compute_enpt2(h, w, c, e, eps);
+    }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("energy"), py::arg("eps") = 1.0e-5,
+          py::arg("nthread") = -1);
     m.def("get_num_threads", []() { return g_threads; });
     m.def("set_num_threads", [](long n) { g_threads = std::max(1L, n); }, py::arg("n"));
     m.def("popcnt", [](Array<ulong_t> d) {

@@ -108,6 +108,10 @@ int det_table_build(const uint64_t *d_dets, int64_t ndet, int nwords, cudaStream
 // Reduced density matrices on the device (rdm.cu), pyci_gpu_compute_rdms.
 int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet, const uint64_t *dets,
                        const double *coeffs, double *rdm1, double *rdm2);
+// Epstein-Nesbet second-order energy on the device (hci.cu), pyci_gpu_compute_enpt2.
+int enpt2_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                 const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo, double energy,
+                 double ecore, double eps, double *result);
 // Heat-bath CI selection on the device (hci.cu), pyci_gpu_add_hci.
 int hci_select_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
                       const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo,
