@@ -615,6 +615,77 @@ def run_rdm(args, world=1, rank=0, local=0):
     print(json.dumps(line), flush=True)
 
 
+def run_enpt2(args, world=1, rank=0, local=0):
+    r"""compute_enpt2 on the 12-orbital 5a5b FCI Hamiltonian: the wave
+    function is every determinant with |c| > 1e-4 in the full-space FP64
+    ground state (colex order), solved in that subspace (FP64); the external
+    space is the rest of the FCI space, eps = 1e-6.  value = seconds per call
+    through the C ABI (host arrays in and out); the same call of the CPU oracle
+    (serial restatement of pyci/src/enpt2.cpp, as the reference runs it with
+    one thread) is the baseline, and the energies must agree to 1e-10 of the
+    correction.  Replicas under torchrun."""
+    import torch
+    from math import comb
+    import pyci_gb300 as pyci
+    from pyci_gb300 import capi
+    from pyci_gb300.synth import synthetic_integrals
+    torch.cuda.set_device(local)
+    nb, na, nbeta, eps = 12, 5, 5, 1.0e-6
+    ctx = capi.Context(local)
+    ecore, one, two = synthetic_integrals(nb, 1003)
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, nb, na, nbeta, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                   ndet=comb(nb, na) * comb(nb, nbeta))
+    _, vecs, _ = csr.solve(n=1, tol=1e-8, ecore=ecore, mode=capi.SOLVE_FP64)
+    csr.free()
+    full = ctx.add_all_dets(capi.WFN_FULLCI, nb, na, nbeta)
+    dets = np.ascontiguousarray(full[np.nonzero(np.abs(vecs[0]) > 1e-4)[0]])
+    del full
+    sub = capi.Csr(ctx, capi.WFN_FULLCI, nb, na, nbeta, dets, one, two)
+    ev, cv, _ = sub.solve(n=1, tol=1e-10, ecore=ecore, mode=capi.SOLVE_FP64)
+    sub.free()
+    energy, coeffs = float(ev[0]), np.ascontiguousarray(cv[0])
+    for _ in range(args.warmup):
+        e2 = ctx.compute_enpt2(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs, one, two, energy, ecore, eps)
+    lib = capi.lib()
+    barrier(world)
+    launches0 = lib.pyci_gpu_kernel_launches()
+    times = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2 = ctx.compute_enpt2(capi.WFN_FULLCI, nb, na, nbeta, dets, coeffs, one, two, energy, ecore, eps)
+            times.append(time.perf_counter() - t0)
+    launches = (lib.pyci_gpu_kernel_launches() - launches0) // args.steps
+    t_gpu = max_over_ranks(statistics.median(times), world)
+    if rank != 0:
+        return
+    line = {"metric": "compute_enpt2 seconds, FCI(12o,10e) selected space", "value": t_gpu, "unit": "s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_gpu * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded integrals (seed 1003)",
+            "config": {"workload": "compute_enpt2 on FCI nbasis=12 5a5b: determinants with |c| > 1e-4 in the "
+                                   "ground state, their subspace ground state, eps = 1e-6",
+                       "ndet": int(dets.shape[0]), "energy": energy, "enpt2_energy": e2, "parallelism": "replicas"},
+            "e2e": {"value": t_gpu, "unit": "s", "h2d_bytes_per_step": int(dets.nbytes + coeffs.nbytes + one.nbytes
+                                                                           + two.nbytes),
+                    "d2h_bytes_per_step": 8},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    if not args.skip_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        O.build()
+        t0 = time.perf_counter()
+        e_ref = O.compute_enpt2(O.FULLCI, nb, na, nbeta, dets, coeffs, one, two, energy, ecore, eps)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": t_cpu, "unit": "s", "cores": 1, "kind": "port",
+                                "sample": "the same call with the C oracle (serial restatement of pyci/src/enpt2.cpp; "
+                                          "the reference runs PYCI_NUM_THREADS = 1 threads by default)"}
+        line["parity"] = {"oracle_energy": e_ref, "abs_diff": abs(e2 - e_ref),
+                          "ok": abs(e2 - e_ref) <= 1e-10 * abs(e_ref - energy)}
+    print(json.dumps(line), flush=True)
+
+
 def run_profile_gram(args):
     r"""Profiling driver (for ncu): FP32 Gram products C = A^T B of --gram P Q N
     (random vectors, N rows), on the CUDA cores then on the tensor cores,
@@ -689,11 +760,12 @@ def main():
     ap.add_argument("--case", type=int, nargs=3, default=[11, 5, 5], metavar=("NBASIS", "NALPHA", "NBETA"))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--wfn", choices=["fullci", "doci"], default="fullci", help="wave function of --case")
-    ap.add_argument("--workload", choices=["fci12", "doci32", "fci8", "doci24", "batch64", "hci", "rdm"],
+    ap.add_argument("--workload", choices=["fci12", "doci32", "fci8", "doci24", "batch64", "hci", "rdm", "enpt2"],
                     default="fci12",
                     help="fci12: the headline FCI(12o,10e) line; doci32: DOCI(32o, 8 pairs); fci8 / doci24: the "
                          "8-orbital FCI and 24-orbital DOCI cases; batch64: the 64-problem batched solve; "
-                         "hci: one heat-bath CI selection step; rdm: compute_rdms of a FCI ground state")
+                         "hci: one heat-bath CI selection step; rdm: compute_rdms of a FCI ground state; "
+                         "enpt2: compute_enpt2 of a selected FCI space")
     args = ap.parse_args()
     global WORKLOAD, METRIC
     if args.workload in WORKLOADS:
@@ -703,15 +775,17 @@ def main():
         run_profile_case(args)
         return
     world, rank, local = dist_init(args)
-    if args.workload in ("hci", "rdm"):
+    if args.workload in ("hci", "rdm", "enpt2"):
         if args.impl == "reference":
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the reference arm of this workload is the "
                                   "cpu_baseline of the ours line (the same call with the CPU oracle)"}), flush=True)
         elif args.workload == "hci":
             run_hci(args, world, rank, local)
-        else:
+        elif args.workload == "rdm":
             run_rdm(args, world, rank, local)
+        else:
+            run_enpt2(args, world, rank, local)
         if world > 1:
             import torch.distributed as dist
             dist.destroy_process_group()
