@@ -273,6 +273,16 @@ int pyci_gpu_compute_enpt2(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t 
 int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                           int64_t ndet, const uint64_t *dets, const double *coeffs, double *rdm1, double *rdm2);
 
+/* Transition RDMs between sum_i coeffs1[i] |dets1[i]> and sum_j coeffs2[j]
+ * |dets2[j]> (compute_transition_rdms, pyci/src/rdm.cpp:634-902; binding
+ * pyci/src/binding.cpp:1293-1340): same layouts as pyci_gpu_compute_rdms;
+ * the reference's terms (each excitation of a determinant of 1 found in 2,
+ * without the transposed partners), summed with FP64 atomics.  DOCI and
+ * FullCI; GenCI is EUNSUPPORTED. */
+int pyci_gpu_compute_transition_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                                     int64_t ndet1, const uint64_t *dets1, const double *coeffs1, int64_t ndet2,
+                                     const uint64_t *dets2, const double *coeffs2, double *rdm1, double *rdm2);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,9 @@ def lib():
         L.orc_phase_single.argtypes = [_p, _i64, _i64]
         L.orc_phase_double.restype = ctypes.c_int
         L.orc_phase_double.argtypes = [_p, _i64, _i64, _i64, _i64]
+        L.orc_compute_transition_rdms.restype = ctypes.c_int
+        L.orc_compute_transition_rdms.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _i64, _p, _p, _p,
+                                                  _p]
         L.orc_compute_rdms.restype = ctypes.c_int
         L.orc_compute_rdms.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]
         L.orc_compute_enpt2.restype = ctypes.c_int
@@ -213,3 +216,21 @@ def compute_enpt2(kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, 
                            _ptr(two_mo), float(energy), float(ecore), float(eps), ctypes.byref(out)):
         raise RuntimeError("orc_compute_enpt2 failed")
     return out.value
+
+
+def compute_transition_rdms(kind, nbasis, nocc_up, nocc_dn, dets1, coeffs1, dets2, coeffs2):
+    r"""(rdm1, rdm2) as pyci.compute_transition_rdms returns them (pyci/src/rdm.cpp:634-902)."""
+    L = lib()
+    dets1 = np.ascontiguousarray(dets1, dtype=np.uint64)
+    dets2 = np.ascontiguousarray(dets2, dtype=np.uint64)
+    coeffs1 = np.ascontiguousarray(coeffs1, dtype=np.float64)
+    coeffs2 = np.ascontiguousarray(coeffs2, dtype=np.float64)
+    n = nbasis
+    if kind == DOCI:
+        r1, r2 = np.zeros((n, n)), np.zeros((n, n))
+    else:
+        r1, r2 = np.zeros((2, n, n)), np.zeros((3, n, n, n, n))
+    if L.orc_compute_transition_rdms(kind, n, nocc_up, nocc_dn, dets1.shape[0], _ptr(dets1), _ptr(coeffs1),
+                                     dets2.shape[0], _ptr(dets2), _ptr(coeffs2), _ptr(r1), _ptr(r2)):
+        raise RuntimeError("orc_compute_transition_rdms failed")
+    return r1, r2

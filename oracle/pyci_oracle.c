@@ -956,21 +956,24 @@ int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int6
 
 /* compute_rdms, pyci/src/rdm.cpp:20-66 (DOCI: rdm1 = d0, rdm2 = d2, both
  * nbasis x nbasis) and 269-530 (FullCI: rdm1 = [aa, bb] (2 n^2), rdm2 =
- * [aaaa, bbbb, abab] (3 n^4)).  Serial, in the reference's loop and
+ * [aaaa, bbbb, abab] (3 n^4)); with tr, compute_transition_rdms
+ * (pyci/src/rdm.cpp:634-902): determinants of wavefunction 1 against the
+ * index of wavefunction 2, every excitation found in 2 (not only j > i), and
+ * no transposed partner terms.  Serial, in the reference's loop and
  * summation order, so the sums are bit-identical to the reference's. */
-int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
-                     const double *coeffs, double *rdm1, double *rdm2) {
+static int rdms_core(int kind, int64_t nbasis, int64_t ndet, const uint64_t *dets, const double *coeffs,
+                     int64_t ndet2, const uint64_t *dets2, const double *coeffs2, int tr, double *rdm1,
+                     double *rdm2) {
     const int64_t nword = orc_nword(nbasis), n1 = nbasis, n2 = n1 * n1, n3 = n1 * n2, n4 = n2 * n2;
-    (void)nocc_up;
-    (void)nocc_dn;
     if (kind != ORC_DOCI && kind != ORC_FULLCI)
         return -2;
     const int64_t nw = kind == ORC_FULLCI ? 2 * nword : nword;
     if (nword > 4)
         return -2;
     det_index ix;
-    if (index_build(&ix, ndet, nw, dets))
+    if (index_build(&ix, ndet2, nw, dets2))
         return -1;
+#define FOUND(j) (tr ? (j) != -1 : (j) > idet)
     uint64_t det[8];
     int64_t ou[256], od[256], vu[256], vd[256];
     if (kind == ORC_DOCI) {
@@ -981,7 +984,8 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
             const uint64_t *rdet = dets + idet * nw;
             memcpy(det, rdet, sizeof(uint64_t) * nw);
             int64_t no = fill_occs(nword, rdet, ou), nv = fill_virs(nword, n1, rdet, vu);
-            const double val1 = coeffs[idet] * coeffs[idet];
+            int64_t self = tr ? index_find(&ix, det) : idet;
+            const double val1 = self != -1 ? coeffs[idet] * coeffs2[self] : 0.;
             for (int64_t i = 0; i < no; ++i) {
                 int64_t k = ou[i];
                 d0[k * (n1 + 1)] += val1;
@@ -995,10 +999,11 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                     excite(det, k, l);
                     int64_t jdet = index_find(&ix, det);
                     excite(det, l, k);
-                    if (jdet > idet) {
-                        const double val2 = coeffs[idet] * coeffs[jdet];
+                    if (FOUND(jdet)) {
+                        const double val2 = coeffs[idet] * coeffs2[jdet];
                         d0[n1 * k + l] += val2;
-                        d0[n1 * l + k] += val2;
+                        if (!tr)
+                            d0[n1 * l + k] += val2;
                     }
                 }
             }
@@ -1017,7 +1022,8 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
         memcpy(det, rup, sizeof(uint64_t) * nw);
         int64_t nou = fill_occs(nword, rup, ou), nod = fill_occs(nword, rdn, od);
         int64_t nvu = fill_virs(nword, n1, rup, vu), nvd = fill_virs(nword, n1, rdn, vd);
-        const double val1 = coeffs[idet] * coeffs[idet];
+        int64_t self = tr ? index_find(&ix, det) : idet;
+        const double val1 = self != -1 ? coeffs[idet] * coeffs2[self] : 0.;
         for (int64_t i = 0; i < nou; ++i) {
             int64_t ii = ou[i];
             aa[(n1 + 1) * ii] += val1;
@@ -1037,10 +1043,11 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                 excite(up, ii, jj);
                 const int sign_up = orc_phase_single(rup, ii, jj);
                 int64_t jdet = index_find(&ix, det);
-                if (jdet > idet) {
-                    const double val2 = coeffs[idet] * coeffs[jdet] * sign_up;
+                if (FOUND(jdet)) {
+                    const double val2 = coeffs[idet] * coeffs2[jdet] * sign_up;
                     aa[ii * n1 + jj] += val2;
-                    aa[jj * n1 + ii] += val2;
+                    if (!tr)
+                        aa[jj * n1 + ii] += val2;
                     for (int64_t k = 0; k < nou; ++k) {
                         if (i == k)
                             continue;
@@ -1049,15 +1056,18 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                         R4(aaaa, ii, kk, kk, jj) -= val2;
                         R4(aaaa, kk, ii, kk, jj) += val2;
                         R4(aaaa, kk, ii, jj, kk) -= val2;
-                        R4(aaaa, jj, kk, ii, kk) += val2;
-                        R4(aaaa, jj, kk, kk, ii) -= val2;
-                        R4(aaaa, kk, jj, ii, kk) -= val2;
-                        R4(aaaa, kk, jj, kk, ii) += val2;
+                        if (!tr) {
+                            R4(aaaa, jj, kk, ii, kk) += val2;
+                            R4(aaaa, jj, kk, kk, ii) -= val2;
+                            R4(aaaa, kk, jj, ii, kk) -= val2;
+                            R4(aaaa, kk, jj, kk, ii) += val2;
+                        }
                     }
                     for (int64_t k = 0; k < nod; ++k) {
                         int64_t kk = od[k];
                         R4(abab, ii, kk, jj, kk) += val2;
-                        R4(abab, jj, kk, ii, kk) += val2;
+                        if (!tr)
+                            R4(abab, jj, kk, ii, kk) += val2;
                     }
                 }
                 for (int64_t k = 0; k < nod; ++k) {
@@ -1066,10 +1076,11 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                         int64_t ll = vd[l];
                         excite(dn, kk, ll);
                         jdet = index_find(&ix, det);
-                        if (jdet > idet) {
-                            const double val2 = coeffs[idet] * coeffs[jdet] * sign_up * orc_phase_single(rdn, kk, ll);
+                        if (FOUND(jdet)) {
+                            const double val2 = coeffs[idet] * coeffs2[jdet] * sign_up * orc_phase_single(rdn, kk, ll);
                             R4(abab, ii, kk, jj, ll) += val2;
-                            R4(abab, jj, ll, ii, kk) += val2;
+                            if (!tr)
+                                R4(abab, jj, ll, ii, kk) += val2;
                         }
                         excite(dn, ll, kk);
                     }
@@ -1080,16 +1091,18 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                         int64_t ll = vu[l];
                         excite(up, kk, ll);
                         jdet = index_find(&ix, det);
-                        if (jdet > idet) {
-                            const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_double(rup, ii, kk, jj, ll);
+                        if (FOUND(jdet)) {
+                            const double val2 = coeffs[idet] * coeffs2[jdet] * orc_phase_double(rup, ii, kk, jj, ll);
                             R4(aaaa, ii, kk, jj, ll) += val2;
                             R4(aaaa, ii, kk, ll, jj) -= val2;
                             R4(aaaa, kk, ii, jj, ll) -= val2;
                             R4(aaaa, kk, ii, ll, jj) += val2;
-                            R4(aaaa, jj, ll, ii, kk) += val2;
-                            R4(aaaa, jj, ll, kk, ii) -= val2;
-                            R4(aaaa, ll, jj, ii, kk) -= val2;
-                            R4(aaaa, ll, jj, kk, ii) += val2;
+                            if (!tr) {
+                                R4(aaaa, jj, ll, ii, kk) += val2;
+                                R4(aaaa, jj, ll, kk, ii) -= val2;
+                                R4(aaaa, ll, jj, ii, kk) -= val2;
+                                R4(aaaa, ll, jj, kk, ii) += val2;
+                            }
                         }
                         excite(up, ll, kk);
                     }
@@ -1111,14 +1124,16 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                 int64_t jj = vd[j];
                 excite(dn, ii, jj);
                 int64_t jdet = index_find(&ix, det);
-                if (jdet > idet) {
-                    const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_single(rdn, ii, jj);
+                if (FOUND(jdet)) {
+                    const double val2 = coeffs[idet] * coeffs2[jdet] * orc_phase_single(rdn, ii, jj);
                     bb[ii * n1 + jj] += val2;
-                    bb[jj * n1 + ii] += val2;
+                    if (!tr)
+                        bb[jj * n1 + ii] += val2;
                     for (int64_t k = 0; k < nou; ++k) {
                         int64_t kk = ou[k];
                         R4(abab, kk, ii, kk, jj) += val2;
-                        R4(abab, kk, jj, kk, ii) += val2;
+                        if (!tr)
+                            R4(abab, kk, jj, kk, ii) += val2;
                     }
                     for (int64_t k = 0; k < nod; ++k) {
                         if (i == k)
@@ -1128,10 +1143,12 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                         R4(bbbb, ii, kk, kk, jj) -= val2;
                         R4(bbbb, kk, ii, kk, jj) += val2;
                         R4(bbbb, kk, ii, jj, kk) -= val2;
-                        R4(bbbb, jj, kk, ii, kk) += val2;
-                        R4(bbbb, jj, kk, kk, ii) -= val2;
-                        R4(bbbb, kk, jj, ii, kk) -= val2;
-                        R4(bbbb, kk, jj, kk, ii) += val2;
+                        if (!tr) {
+                            R4(bbbb, jj, kk, ii, kk) += val2;
+                            R4(bbbb, jj, kk, kk, ii) -= val2;
+                            R4(bbbb, kk, jj, ii, kk) -= val2;
+                            R4(bbbb, kk, jj, kk, ii) += val2;
+                        }
                     }
                 }
                 for (int64_t k = i + 1; k < nod; ++k) {
@@ -1140,16 +1157,18 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                         int64_t ll = vd[l];
                         excite(dn, kk, ll);
                         jdet = index_find(&ix, det);
-                        if (jdet > idet) {
-                            const double val2 = coeffs[idet] * coeffs[jdet] * orc_phase_double(rdn, ii, kk, jj, ll);
+                        if (FOUND(jdet)) {
+                            const double val2 = coeffs[idet] * coeffs2[jdet] * orc_phase_double(rdn, ii, kk, jj, ll);
                             R4(bbbb, ii, kk, jj, ll) += val2;
                             R4(bbbb, ii, kk, ll, jj) -= val2;
                             R4(bbbb, kk, ii, jj, ll) -= val2;
                             R4(bbbb, kk, ii, ll, jj) += val2;
-                            R4(bbbb, jj, ll, ii, kk) += val2;
-                            R4(bbbb, ll, jj, ii, kk) -= val2;
-                            R4(bbbb, jj, ll, kk, ii) -= val2;
-                            R4(bbbb, ll, jj, kk, ii) += val2;
+                            if (!tr) {
+                                R4(bbbb, jj, ll, ii, kk) += val2;
+                                R4(bbbb, ll, jj, ii, kk) -= val2;
+                                R4(bbbb, jj, ll, kk, ii) -= val2;
+                                R4(bbbb, ll, jj, kk, ii) += val2;
+                            }
                         }
                         excite(dn, ll, kk);
                     }
@@ -1159,8 +1178,24 @@ int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
         }
     }
 #undef R4
+#undef FOUND
     free(ix.slots);
     return 0;
+}
+
+int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
+                     const double *coeffs, double *rdm1, double *rdm2) {
+    (void)nocc_up;
+    (void)nocc_dn;
+    return rdms_core(kind, nbasis, ndet, dets, coeffs, ndet, dets, coeffs, 0, rdm1, rdm2);
+}
+
+int orc_compute_transition_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet1,
+                                const uint64_t *dets1, const double *coeffs1, int64_t ndet2, const uint64_t *dets2,
+                                const double *coeffs2, double *rdm1, double *rdm2) {
+    (void)nocc_up;
+    (void)nocc_dn;
+    return rdms_core(kind, nbasis, ndet1, dets1, coeffs1, ndet2, dets2, coeffs2, 1, rdm1, rdm2);
 }
 
 /* ---------------- Epstein-Nesbet second-order correction ---------------- */

@@ -69,6 +69,10 @@ int orc_add_hci(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int6
  * the reference's summation order. */
 int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
                      const double *coeffs, double *rdm1, double *rdm2);
+/* Transition RDMs <Psi_1| ... |Psi_2> (compute_transition_rdms), same layouts. */
+int orc_compute_transition_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet1,
+                                const uint64_t *dets1, const double *coeffs1, int64_t ndet2, const uint64_t *dets2,
+                                const double *coeffs2, double *rdm1, double *rdm2);
 
 /* Epstein-Nesbet second-order energy (compute_enpt2): energy + the sum over
  * determinants k outside the wave function of V_k^2 / (energy - ecore - H_kk),

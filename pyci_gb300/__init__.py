@@ -4,7 +4,7 @@ Drop-in for the ``pyci`` names on the sparse-operator path
 (pyci/__init__.py:18-31): ``secondquant_op`` (alias ``hamiltonian``), the
 ``doci_wfn`` / ``fullci_wfn`` / ``genci_wfn`` wave functions, ``sparse_op``
 (CSR build, ``op(x)``, ``op.solve``, ``op.update``), ``add_hci`` (heat-bath
-CI selection), ``compute_rdms`` (with ``spinize_rdms`` and
+CI selection), ``compute_rdms`` / ``compute_transition_rdms`` (with ``spinize_rdms`` and
 ``reduce_senzero_integrals``), ``compute_enpt2``, ``popcnt``, ``ctz``, thread-count helpers and
 ``add_excitations``.  The operator runs on the GPU through
 ``libpyci_gb300.so``; importing works without a GPU, building an operator
@@ -24,6 +24,7 @@ try:
         add_hci,
         compute_enpt2,
         compute_rdms,
+        compute_transition_rdms,
         c_double,
         c_long,
         c_ulong,
@@ -76,6 +77,7 @@ __all__ = [
     "add_hci",
     "compute_enpt2",
     "compute_rdms",
+    "compute_transition_rdms",
     "reduce_senzero_integrals",
     "spinize_rdms",
     "gpu_version",

@@ -29,6 +29,7 @@ SYMBOLS = [
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
     "pyci_gpu_gram_device", "pyci_gpu_add_hci", "pyci_gpu_compute_rdms", "pyci_gpu_compute_enpt2",
+    "pyci_gpu_compute_transition_rdms",
 ]
 
 
@@ -84,6 +85,8 @@ def lib():
             "pyci_gpu_add_hci": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _int,
                                         _i64, _p, ctypes.POINTER(_i64)]),
             "pyci_gpu_compute_rdms": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p]),
+            "pyci_gpu_compute_transition_rdms": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _i64, _p, _p, _p,
+                                                        _p]),
             "pyci_gpu_compute_enpt2": (_int, [_p, _int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double,
                                               ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
         }
@@ -176,6 +179,22 @@ class Context:
             r1, r2 = np.empty((n, n)), np.empty((n, n))
         check(lib().pyci_gpu_compute_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
                                           _ptr(coeffs), _ptr(r1), _ptr(r2)))
+        return r1, r2
+
+    def compute_transition_rdms(self, kind, nbasis, nocc_up, nocc_dn, dets1, coeffs1, dets2, coeffs2):
+        r"""Transition (rdm1, rdm2) between two wave functions, same layouts as compute_rdms."""
+        dets1 = np.ascontiguousarray(dets1, dtype=np.uint64)
+        dets2 = np.ascontiguousarray(dets2, dtype=np.uint64)
+        coeffs1 = np.ascontiguousarray(coeffs1, dtype=np.float64)
+        coeffs2 = np.ascontiguousarray(coeffs2, dtype=np.float64)
+        n = nbasis
+        if kind == WFN_FULLCI:
+            r1, r2 = np.empty((2, n, n)), np.empty((3, n, n, n, n))
+        else:
+            r1, r2 = np.empty((n, n)), np.empty((n, n))
+        check(lib().pyci_gpu_compute_transition_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets1.shape[0],
+                                                     _ptr(dets1), _ptr(coeffs1), dets2.shape[0], _ptr(dets2),
+                                                     _ptr(coeffs2), _ptr(r1), _ptr(r2)))
         return r1, r2
 
     def compute_enpt2(self, kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, energy, ecore, eps):

@@ -558,7 +558,27 @@ int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t n
     if (rc)
         return rc;
     PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
-    return rdm_compute_device(ctx, kind, nbasis, ndet, dets, coeffs, rdm1, rdm2);
+    return rdm_compute_device(ctx, kind, nbasis, ndet, dets, coeffs, 0, nullptr, nullptr, rdm1, rdm2);
+}
+
+int pyci_gpu_compute_transition_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
+                                     int64_t ndet1, const uint64_t *dets1, const double *coeffs1, int64_t ndet2,
+                                     const uint64_t *dets2, const double *coeffs2, double *rdm1, double *rdm2) {
+    if (!ctx || !rdm1 || !rdm2 || (ndet1 > 0 && (!dets1 || !coeffs1)) || (ndet2 > 0 && (!dets2 || !coeffs2))) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    if (ndet1 < 0 || ndet2 < 0) {
+        set_error("negative determinant count");
+        return PYCI_GPU_EINVAL;
+    }
+    int rc = validate_wfn(kind, nbasis, nocc_up, nocc_dn);
+    if (rc)
+        return rc;
+    PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    static const uint64_t empty = 0;
+    return rdm_compute_device(ctx, kind, nbasis, ndet1, dets1, coeffs1, ndet2, dets2 ? dets2 : &empty, coeffs2, rdm1,
+                              rdm2);
 }
 
 int pyci_gpu_compute_enpt2(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,

@@ -697,6 +697,29 @@ double compute_enpt2(const SQuantOp &ham, const Wfn &wfn, Array<double> coeffs, 
     return out;
 }
 
+// compute_transition_rdms (pyci/src/rdm.cpp:634-902, 1057-1080): same
+// layouts as compute_rdms, between two wave functions of the same space.
+py::tuple compute_transition_rdms(const Wfn &w1, const Wfn &w2, Array<double> c1, Array<double> c2) {
+    if (w1.kind() != w2.kind() || w1.nbasis != w2.nbasis || w1.nocc_up != w2.nocc_up || w1.nocc_dn != w2.nocc_dn)
+        throw std::invalid_argument("the two wave functions describe different spaces");
+    if (c1.size() < w1.ndet || c2.size() < w2.ndet)
+        throw std::invalid_argument("a coefficient vector has fewer entries than its wave function has determinants");
+    const long n = w1.nbasis;
+    const bool fci = w1.kind() == PYCI_WFN_FULLCI;
+    Array<double> r1 = fci ? Array<double>({2L, n, n}) : Array<double>({n, n});
+    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n}) : Array<double>({n, n});
+    auto ctx = default_ctx();
+    const double *p1c = c1.data(), *p2c = c2.data();
+    double *p1 = r1.mutable_data(), *p2 = r2.mutable_data();
+    {
+        py::gil_scoped_release nogil;
+        check(pyci_gpu_compute_transition_rdms(ctx.get(), w1.kind(), n, w1.nocc_up, w1.nocc_dn, w1.ndet,
+                                               w1.ndet ? w1.dets.data() : nullptr, p1c, w2.ndet,
+                                               w2.ndet ? w2.dets.data() : nullptr, p2c, p1, p2));
+    }
+    return py::make_tuple(r1, r2);
+}
+
 // ---------------------------------------------------------------- numpy views
 
 Array<ulong_t> one_det(const Wfn &w, long i, bool two) {
@@ -1278,6 +1301,15 @@ PYBIND11_MODULE(_pyci, m) {
         return compute_enpt2(h, w, c, e, eps);
     }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("energy"), py::arg("eps") = 1.0e-5,
           py::arg("nthread") = -1);
+    m.def("compute_transition_rdms", [](const DOCIWfn &w1, const DOCIWfn &w2, Array<double> c1, Array<double> c2) {
+        return compute_transition_rdms(w1, w2, c1, c2);
+    }, py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"));
+    m.def("compute_transition_rdms", [](const FullCIWfn &w1, const FullCIWfn &w2, Array<double> c1, Array<double> c2) {
+        return compute_transition_rdms(w1, w2, c1, c2);
+    }, py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"));
+    m.def("compute_transition_rdms", [](const GenCIWfn &w1, const GenCIWfn &w2, Array<double> c1, Array<double> c2) {
+        return compute_transition_rdms(w1, w2, c1, c2);
+    }, py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"));
     m.def("get_num_threads", []() { return g_threads; });
     m.def("set_num_threads", [](long n) { g_threads = std::max(1L, n); }, py::arg("n"));
     m.def("popcnt", [](Array<ulong_t> d) {

@@ -106,8 +106,11 @@ int device_exclusive_scan(const int64_t *counts, int64_t n, int64_t *out, cudaSt
 int det_table_build(const uint64_t *d_dets, int64_t ndet, int nwords, cudaStream_t st, int *d_err,
                     int32_t **slots, uint64_t *mask);
 // Reduced density matrices on the device (rdm.cu), pyci_gpu_compute_rdms.
+// dets2 == NULL: RDMs of (dets, coeffs); otherwise transition RDMs against
+// (dets2, coeffs2).
 int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet, const uint64_t *dets,
-                       const double *coeffs, double *rdm1, double *rdm2);
+                       const double *coeffs, int64_t ndet2, const uint64_t *dets2, const double *coeffs2,
+                       double *rdm1, double *rdm2);
 // Epstein-Nesbet second-order energy on the device (hci.cu), pyci_gpu_compute_enpt2.
 int enpt2_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
                  const uint64_t *dets, const double *coeffs, const double *one_mo, const double *two_mo, double energy,

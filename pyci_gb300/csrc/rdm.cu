@@ -10,6 +10,11 @@
 // each term's value are the reference's; only the order of the FP64 sums
 // differs (atomics), so entries agree to rounding (~1e-16 relative).
 //
+// Transition RDMs (compute_transition_rdms, pyci/src/rdm.cpp:634-902) run
+// the same loops over wave function 1 with lookups in wave function 2: the
+// diagonal terms use c1_i c2_(i in 2), every excitation found in 2 counts
+// (not only j > i), and the transposed partner terms are not added.
+//
 // Layouts (as pyci.compute_rdms returns them): DOCI d0 = rdm1 [n][n],
 // d2 = rdm2 [n][n]; FullCI rdm1 = [aa, bb] [2][n][n], rdm2 = [aaaa, bbbb,
 // abab] [3][n][n][n][n].
@@ -30,13 +35,14 @@ struct RdmParams {
     int64_t ndet;
     const uint64_t *dets;
     const double *coeffs;
-    DetTable table;
+    DetTable table;          // lookups: wave function 2 (the wave function itself unless transition)
+    const double *coeffs2;   // coefficients of the table's wave function
     double *rdm1, *rdm2;
 };
 
 __device__ __forceinline__ void add(double *a, int64_t idx, double v) { atomicAdd(a + idx, v); }
 
-template<int NW, int NWD>
+template<int NW, int NWD, bool TR>
 __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
     const int64_t idet = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     if (idet >= p.ndet)
@@ -47,8 +53,11 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
     for (int w = 0; w < NWD; ++w)
         det[w] = rdet[w] = p.dets[idet * NWD + w];
     const double ci = p.coeffs[idet];
-    const double val1 = ci * ci;
     auto find = [&]() { return p.table.find<NWD>(det); };
+    const int64_t self = TR ? find() : idet;
+    const double val1 = self != -1 ? ci * p.coeffs2[self] : 0.0;
+    // The reference's partner test: j > i for the RDMs, found for transition RDMs.
+    auto hit = [&](int64_t j) { return TR ? j != -1 : j > idet; };
     auto flip = [&](uint64_t *d, int a) { d[a >> 6] ^= 1ULL << (a & 63); };
     if (p.kind == PYCI_WFN_DOCI) {
         // pyci/src/rdm.cpp:33-64.
@@ -70,10 +79,11 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
                 const int64_t jdet = find();
                 flip(det, l);
                 flip(det, k);
-                if (jdet > idet) {
-                    const double val2 = ci * p.coeffs[jdet];
+                if (hit(jdet)) {
+                    const double val2 = ci * p.coeffs2[jdet];
                     add(d0, n1 * k + l, val2);
-                    add(d0, n1 * l + k, val2);
+                    if (!TR)
+                        add(d0, n1 * l + k, val2);
                 }
             }
         }
@@ -116,10 +126,11 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
                 flip(mine, jj);
                 const double sign = phase_single<NW>(rmine, ii, jj);
                 int64_t jdet = find();
-                if (jdet > idet) {
-                    const double val2 = ci * p.coeffs[jdet] * sign;
+                if (hit(jdet)) {
+                    const double val2 = ci * p.coeffs2[jdet] * sign;
                     add(one, ii * n1 + jj, val2);
-                    add(one, jj * n1 + ii, val2);
+                    if (!TR)
+                        add(one, jj * n1 + ii, val2);
                     for (int k = 0; k < no; ++k) {
                         if (k == i)
                             continue;
@@ -128,19 +139,23 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
                         add(same, at(ii, kk, kk, jj), -val2);
                         add(same, at(kk, ii, kk, jj), val2);
                         add(same, at(kk, ii, jj, kk), -val2);
-                        add(same, at(jj, kk, ii, kk), val2);
-                        add(same, at(jj, kk, kk, ii), -val2);
-                        add(same, at(kk, jj, ii, kk), -val2);
-                        add(same, at(kk, jj, kk, ii), val2);
+                        if (!TR) {
+                            add(same, at(jj, kk, ii, kk), val2);
+                            add(same, at(jj, kk, kk, ii), -val2);
+                            add(same, at(kk, jj, ii, kk), -val2);
+                            add(same, at(kk, jj, kk, ii), val2);
+                        }
                     }
                     for (int k = 0; k < nother; ++k) {
                         const int kk = oo[k];
                         if (s == 0) {
                             add(abab, at(ii, kk, jj, kk), val2);
-                            add(abab, at(jj, kk, ii, kk), val2);
+                            if (!TR)
+                                add(abab, at(jj, kk, ii, kk), val2);
                         } else {
                             add(abab, at(kk, ii, kk, jj), val2);
-                            add(abab, at(kk, jj, kk, ii), val2);
+                            if (!TR)
+                                add(abab, at(kk, jj, kk, ii), val2);
                         }
                     }
                 }
@@ -153,10 +168,11 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
                             flip(dn, kk);
                             flip(dn, ll);
                             jdet = find();
-                            if (jdet > idet) {
-                                const double val2 = ci * p.coeffs[jdet] * sign * phase_single<NW>(rdn, kk, ll);
+                            if (hit(jdet)) {
+                                const double val2 = ci * p.coeffs2[jdet] * sign * phase_single<NW>(rdn, kk, ll);
                                 add(abab, at(ii, kk, jj, ll), val2);
-                                add(abab, at(jj, ll, ii, kk), val2);
+                                if (!TR)
+                                    add(abab, at(jj, ll, ii, kk), val2);
                             }
                             flip(dn, ll);
                             flip(dn, kk);
@@ -170,16 +186,18 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
                         flip(mine, kk);
                         flip(mine, ll);
                         jdet = find();
-                        if (jdet > idet) {
-                            const double val2 = ci * p.coeffs[jdet] * phase_double<NW>(rmine, ii, kk, jj, ll);
+                        if (hit(jdet)) {
+                            const double val2 = ci * p.coeffs2[jdet] * phase_double<NW>(rmine, ii, kk, jj, ll);
                             add(same, at(ii, kk, jj, ll), val2);
                             add(same, at(ii, kk, ll, jj), -val2);
                             add(same, at(kk, ii, jj, ll), -val2);
                             add(same, at(kk, ii, ll, jj), val2);
-                            add(same, at(jj, ll, ii, kk), val2);
-                            add(same, at(jj, ll, kk, ii), -val2);
-                            add(same, at(ll, jj, ii, kk), -val2);
-                            add(same, at(ll, jj, kk, ii), val2);
+                            if (!TR) {
+                                add(same, at(jj, ll, ii, kk), val2);
+                                add(same, at(jj, ll, kk, ii), -val2);
+                                add(same, at(ll, jj, ii, kk), -val2);
+                                add(same, at(ll, jj, kk, ii), val2);
+                            }
                         }
                         flip(mine, ll);
                         flip(mine, kk);
@@ -192,6 +210,26 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
     }
 }
 
+template<bool TR>
+void launch_rdm(int nwd, int kind, unsigned blocks, cudaStream_t st, const RdmParams &p) {
+    switch (nwd) {
+    case 1: rdm_kernel<1, 1, TR><<<blocks, 128, 0, st>>>(p); break;
+    case 2:
+        if (kind == PYCI_WFN_FULLCI)
+            rdm_kernel<1, 2, TR><<<blocks, 128, 0, st>>>(p);
+        else
+            rdm_kernel<2, 2, TR><<<blocks, 128, 0, st>>>(p);
+        break;
+    case 4:
+        if (kind == PYCI_WFN_FULLCI)
+            rdm_kernel<2, 4, TR><<<blocks, 128, 0, st>>>(p);
+        else
+            rdm_kernel<4, 4, TR><<<blocks, 128, 0, st>>>(p);
+        break;
+    default: rdm_kernel<4, 8, TR><<<blocks, 128, 0, st>>>(p); break;
+    }
+}
+
 } // namespace
 
 } // namespace pyci_gpu
@@ -199,7 +237,9 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
 using namespace pyci_gpu;
 
 int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet, const uint64_t *dets,
-                       const double *coeffs, double *rdm1, double *rdm2) {
+                       const double *coeffs, int64_t ndet2, const uint64_t *dets2, const double *coeffs2,
+                       double *rdm1, double *rdm2) {
+    const bool tr = dets2 != nullptr;
     cudaStream_t st = ctx->stream;
     const int64_t n = nbasis;
     const int nw = n <= 64 ? 1 : (n <= 128 ? 2 : (n <= 256 ? 4 : 0));
@@ -211,7 +251,7 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
         set_error("compute_rdms on the GPU supports DOCI and FullCI wave functions");
         return PYCI_GPU_EUNSUPPORTED;
     }
-    if (ndet >= INT32_MAX) {
+    if (ndet >= INT32_MAX || ndet2 >= INT32_MAX) {
         set_error("more than 2^31 - 1 determinants is not supported");
         return PYCI_GPU_EUNSUPPORTED;
     }
@@ -233,17 +273,22 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
             bufs.push_back(*p);
         return e;
     };
-    std::vector<uint64_t> packed(static_cast<size_t>(ndet) * nwd, 0ULL);
-    for (int64_t i = 0; i < ndet; ++i)
+    // Determinants of both wave functions (the second only for transition
+    // RDMs), repacked to nw words per string.
+    const int64_t nall = ndet + (tr ? ndet2 : 0);
+    std::vector<uint64_t> packed(static_cast<size_t>(nall) * nwd, 0ULL);
+    for (int64_t i = 0; i < nall; ++i) {
+        const uint64_t *src = i < ndet ? dets + i * nstr * host_nword : dets2 + (i - ndet) * nstr * host_nword;
         for (int s = 0; s < nstr; ++s)
             for (int64_t w = 0; w < host_nword; ++w)
-                packed[i * nwd + s * nw + w] = dets[(i * nstr + s) * host_nword + w];
+                packed[i * nwd + s * nw + w] = src[s * host_nword + w];
+    }
     uint64_t *d_dets = nullptr;
     double *d_coef = nullptr, *d_r1 = nullptr, *d_r2 = nullptr;
     int *d_err = nullptr;
     cudaError_t e = cudaSuccess;
     if ((e = alloc(reinterpret_cast<void **>(&d_dets), sizeof(uint64_t) * packed.size())) != cudaSuccess ||
-        (e = alloc(reinterpret_cast<void **>(&d_coef), sizeof(double) * ndet)) != cudaSuccess ||
+        (e = alloc(reinterpret_cast<void **>(&d_coef), sizeof(double) * nall)) != cudaSuccess ||
         (e = alloc(reinterpret_cast<void **>(&d_r1), sizeof(double) * len1)) != cudaSuccess ||
         (e = alloc(reinterpret_cast<void **>(&d_r2), sizeof(double) * len2)) != cudaSuccess ||
         (e = alloc(reinterpret_cast<void **>(&d_err), sizeof(int))) != cudaSuccess) {
@@ -257,13 +302,19 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
         if ((e = cudaMemcpyAsync(d_dets, packed.data(), sizeof(uint64_t) * packed.size(), cudaMemcpyHostToDevice,
                                  st)) != cudaSuccess ||
             (e = cudaMemcpyAsync(d_coef, coeffs, sizeof(double) * ndet, cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+            (tr && ndet2 > 0 &&
+             (e = cudaMemcpyAsync(d_coef + ndet, coeffs2, sizeof(double) * ndet2, cudaMemcpyHostToDevice, st)) !=
+                 cudaSuccess) ||
             (e = cudaMemsetAsync(d_r1, 0, sizeof(double) * len1, st)) != cudaSuccess ||
             (e = cudaMemsetAsync(d_r2, 0, sizeof(double) * len2, st)) != cudaSuccess ||
             (e = cudaMemsetAsync(d_err, 0, sizeof(int), st)) != cudaSuccess) {
             rc = cuda_status(e, "RDM upload");
             break;
         }
-        if ((rc = det_table_build(d_dets, ndet, nwd, st, d_err, &slots, &mask)))
+        // The lookup table covers wave function 2 (itself unless transition).
+        const uint64_t *tdets = tr ? d_dets + ndet * nwd : d_dets;
+        const int64_t tndet = tr ? ndet2 : ndet;
+        if ((rc = det_table_build(tdets, tndet, nwd, st, d_err, &slots, &mask)))
             break;
         bufs.push_back(slots);
         RdmParams p{};
@@ -272,27 +323,16 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
         p.ndet = ndet;
         p.dets = d_dets;
         p.coeffs = d_coef;
-        p.table = DetTable{slots, d_dets, mask, nwd};
+        p.table = DetTable{slots, tdets, mask, nwd};
+        p.coeffs2 = tr ? d_coef + ndet : d_coef;
         p.rdm1 = d_r1;
         p.rdm2 = d_r2;
         const unsigned blocks = static_cast<unsigned>((ndet + 127) / 128);
         if (blocks) {
-            switch (nwd) {
-            case 1: rdm_kernel<1, 1><<<blocks, 128, 0, st>>>(p); break;
-            case 2:
-                if (kind == PYCI_WFN_FULLCI)
-                    rdm_kernel<1, 2><<<blocks, 128, 0, st>>>(p);
-                else
-                    rdm_kernel<2, 2><<<blocks, 128, 0, st>>>(p);
-                break;
-            case 4:
-                if (kind == PYCI_WFN_FULLCI)
-                    rdm_kernel<2, 4><<<blocks, 128, 0, st>>>(p);
-                else
-                    rdm_kernel<4, 4><<<blocks, 128, 0, st>>>(p);
-                break;
-            default: rdm_kernel<4, 8><<<blocks, 128, 0, st>>>(p); break;
-            }
+            if (tr)
+                launch_rdm<true>(nwd, kind, blocks, st, p);
+            else
+                launch_rdm<false>(nwd, kind, blocks, st, p);
             note_launch();
             if ((e = cudaGetLastError()) != cudaSuccess) {
                 rc = cuda_status(e, "RDM kernel");

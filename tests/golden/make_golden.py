@@ -3,7 +3,7 @@ r"""Generate the golden fixtures in tests/golden/ from the reference itself.
 Run in a container that has the reference source tree:
 
     make -C oracle ref port            # reference built against the shims + C oracle
-    python tests/golden/make_golden.py [--big | --only-big | --only-hci | --only-rdm | --only-enpt2]
+    python tests/golden/make_golden.py [--big | --only-big | --only-hci | --only-rdm | --only-enpt2 | --only-trdm]
 
 Outputs (all committed):
   kat_<system>.npz      integrals of the FCIDUMP files the reference's known-answer
@@ -15,6 +15,7 @@ Outputs (all committed):
                         determinants and coefficients, and the set it added
   rdm_<case>.npz        the reference's pyci.compute_rdms (DOCI d0/d2, FullCI
                         rdm1/rdm2) of seeded random coefficient vectors
+  trdm_<case>.npz       the reference's pyci.compute_transition_rdms of two sets
   enpt2_<case>.npz      the reference's pyci.compute_enpt2 of a solved ground state
   digests.json          order-independent digests of the reference CSR for the
                         larger synthetic workloads, and reference eigenvalues
@@ -223,6 +224,43 @@ def rdm_fixtures(pyci):
     return meta
 
 
+TRDM_CASES = [
+    # name, kind, nbasis, nocc_up, nocc_dn, excitations of wave function 1 (None = all),
+    # of wave function 2, seed
+    ("doci_10_4", "doci", 10, 4, 4, (0, 1, 2), None, 61),
+    ("fci_6_3_2", "fullci", 6, 3, 2, (0, 1), None, 62),
+    ("fci_7_3_3", "fullci", 7, 3, 3, None, (0, 1, 2), 63),
+]
+
+
+def trdm_fixtures(pyci):
+    r"""The reference's pyci.compute_transition_rdms between two wave functions
+    (different determinant sets) with seeded random coefficient vectors."""
+    meta = []
+    for name, kind, n, nu, nd, exc1, exc2, seed in TRDM_CASES:
+        W = {"doci": pyci.doci_wfn, "fullci": pyci.fullci_wfn}[kind]
+        wfns = []
+        for exc in (exc1, exc2):
+            w = W(n, nu, nd)
+            if exc is None:
+                w.add_all_dets()
+            else:
+                pyci.add_excitations(w, *exc)
+            wfns.append(w)
+        rng = np.random.default_rng(seed)
+        c1 = rng.normal(size=len(wfns[0]))
+        c2 = rng.normal(size=len(wfns[1]))
+        rdm1, rdm2 = pyci.compute_transition_rdms(wfns[0], wfns[1], c1, c2)
+        d1 = np.asarray(wfns[0].to_det_array()).reshape(len(wfns[0]), -1)
+        d2 = np.asarray(wfns[1].to_det_array()).reshape(len(wfns[1]), -1)
+        np.savez_compressed(os.path.join(HERE, "trdm_%s.npz" % name), dets1=d1, coeffs1=c1, dets2=d2, coeffs2=c2,
+                            rdm1=np.asarray(rdm1), rdm2=np.asarray(rdm2))
+        meta.append({"name": name, "wfn": kind, "nbasis": n, "nocc_up": nu, "nocc_dn": nd, "seed": seed,
+                     "ndet1": len(wfns[0]), "ndet2": len(wfns[1])})
+        print("trdm", name, len(wfns[0]), len(wfns[1]), flush=True)
+    return meta
+
+
 ENPT2_CASES = [
     # name, kind, nbasis, nocc_up, nocc_dn, excitations of the set, seed, eps
     ("doci_10_4", "doci", 10, 4, 4, (0, 1), 71, 1e-4),
@@ -308,12 +346,15 @@ def main():
     ap.add_argument("--only-hci", action="store_true")
     ap.add_argument("--only-rdm", action="store_true")
     ap.add_argument("--only-enpt2", action="store_true")
+    ap.add_argument("--only-trdm", action="store_true")
     args = ap.parse_args()
     import pyci  # the reference, from oracle/_ref
     path = os.path.join(HERE, "digests.json")
-    if args.only_hci or args.only_rdm or args.only_enpt2:
+    if args.only_hci or args.only_rdm or args.only_enpt2 or args.only_trdm:
         with open(path) as f:
             meta = json.load(f)
+        if args.only_trdm:
+            meta["trdm_cases"] = trdm_fixtures(pyci)
         if args.only_enpt2:
             meta["enpt2_cases"], meta["enpt2_kats"] = enpt2_fixtures(pyci)
         if args.only_hci:
@@ -328,7 +369,8 @@ def main():
     else:
         enpt2_cases, enpt2_kats = enpt2_fixtures(pyci)
         meta = {"kats": kat_fixtures(pyci), "csr_cases": csr_fixtures(pyci), "hci_cases": hci_fixtures(pyci),
-                "rdm_cases": rdm_fixtures(pyci), "enpt2_cases": enpt2_cases, "enpt2_kats": enpt2_kats,
+                "rdm_cases": rdm_fixtures(pyci), "trdm_cases": trdm_fixtures(pyci), "enpt2_cases": enpt2_cases,
+                "enpt2_kats": enpt2_kats,
                 "workloads": workload_digests(pyci, args.big)}
     with open(path, "w") as f:
         json.dump(meta, f, indent=1)

@@ -96,3 +96,45 @@ def test_compute_rdms_rejects_genci(ctx):
     dets = O.all_dets(O.GENCI, 6, 3, 0)
     with pytest.raises(capi.GpuError):
         ctx.compute_rdms(capi.WFN_GENCI, 6, 3, 0, dets, np.ones(dets.shape[0]))
+
+
+def test_transition_rdms_match_reference(ctx, golden):
+    for m in golden["trdm_cases"]:
+        z = np.load(os.path.join(os.path.dirname(__file__), "golden", "trdm_%s.npz" % m["name"]))
+        r1, r2 = ctx.compute_transition_rdms(GPU[m["wfn"]], m["nbasis"], m["nocc_up"], m["nocc_dn"], z["dets1"],
+                                             z["coeffs1"], z["dets2"], z["coeffs2"])
+        scale = max(1.0, float(np.abs(z["rdm2"]).max()))
+        npt.assert_allclose(r1, z["rdm1"], rtol=0, atol=1e-13 * scale)
+        npt.assert_allclose(r2, z["rdm2"], rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("kind,n,nu,nd", [("fullci", 9, 3, 3), ("doci", 70, 3, 3)])
+def test_transition_rdms_match_oracle(ctx, kind, n, nu, nd):
+    full = O.all_dets(ORC[kind], n, nu, nd)
+    rng = np.random.default_rng(n + 1)
+    d1 = full[np.sort(rng.choice(full.shape[0], size=min(8000, full.shape[0] // 2), replace=False))]
+    d2 = full[np.sort(rng.choice(full.shape[0], size=min(8000, full.shape[0] // 2), replace=False))]
+    c1, c2 = rng.normal(size=d1.shape[0]), rng.normal(size=d2.shape[0])
+    c1 /= np.linalg.norm(c1)
+    c2 /= np.linalg.norm(c2)
+    r1, r2 = ctx.compute_transition_rdms(GPU[kind], n, nu, nd, d1, c1, d2, c2)
+    o1, o2 = O.compute_transition_rdms(ORC[kind], n, nu, nd, d1, c1, d2, c2)
+    npt.assert_allclose(r1, o1, rtol=0, atol=1e-12)
+    npt.assert_allclose(r2, o2, rtol=0, atol=1e-12)
+
+
+def test_transition_rdms_drop_in(golden):
+    # Between the two lowest states of be/cc-pVDZ FullCI(2,2): the transition
+    # 1-RDM traces to <Psi_1|Psi_2> * N = 0; with itself it equals compute_rdms.
+    k = next(k for k in golden["kats"] if k["wfn"] == "fullci")
+    ham = pyci.secondquant_op(*load_kat(k["system"]))
+    wfn = pyci.fullci_wfn(ham.nbasis, *k["occs"])
+    wfn.add_all_dets()
+    op = pyci.sparse_op(ham, wfn)
+    es, cs = op.solve(n=2, tol=1e-10)
+    t1, t2 = pyci.compute_transition_rdms(wfn, wfn, cs[0], cs[1])
+    assert abs(np.trace(t1[0]) + np.trace(t1[1])) < 1e-8
+    s1, s2 = pyci.compute_transition_rdms(wfn, wfn, cs[0], cs[0])
+    r1, r2 = pyci.compute_rdms(wfn, cs[0])
+    npt.assert_allclose(s1, r1, rtol=0, atol=1e-12)
+    npt.assert_allclose(s2, r2, rtol=0, atol=1e-12)

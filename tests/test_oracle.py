@@ -221,3 +221,25 @@ def test_compute_enpt2_known_answers(golden, i):
     e = O.compute_enpt2(KIND[k["wfn"]], n, k["occs"][0], k["occs"][1], dets, v[:, 0], one, two, w[0] + ecore, ecore,
                         1.0e-4)
     np.testing.assert_allclose(e, k["enpt2"], rtol=1e-7)
+
+
+def test_transition_rdms_match_reference(golden):
+    import os
+    for m in golden["trdm_cases"]:
+        z = np.load(os.path.join(os.path.dirname(__file__), "golden", "trdm_%s.npz" % m["name"]))
+        r1, r2 = O.compute_transition_rdms(KIND[m["wfn"]], m["nbasis"], m["nocc_up"], m["nocc_dn"], z["dets1"],
+                                           z["coeffs1"], z["dets2"], z["coeffs2"])
+        assert np.array_equal(r1, z["rdm1"]) and np.array_equal(r2, z["rdm2"]), m["name"]
+
+
+@pytest.mark.parametrize("kind", ["doci", "fullci"])
+def test_transition_rdms_of_a_state_with_itself(kind):
+    # <Psi|...|Psi> through the transition loops (every excitation, no
+    # partner terms) sums the same terms as compute_rdms.
+    n, nu, nd = (9, 3, 3) if kind == "doci" else (6, 3, 2)
+    dets = O.all_dets(KIND[kind], n, nu, nd)
+    c = np.random.default_rng(4).normal(size=dets.shape[0])
+    t1, t2 = O.compute_transition_rdms(KIND[kind], n, nu, nd, dets, c, dets, c)
+    r1, r2 = O.compute_rdms(KIND[kind], n, nu, nd, dets, c)
+    np.testing.assert_allclose(t1, r1, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(t2, r2, rtol=0, atol=1e-12)
