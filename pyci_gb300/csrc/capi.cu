@@ -41,7 +41,8 @@ void csr_release(pyci_gpu_csr *csr) {
     if (!csr || !csr->ctx)
         return;
     cudaStream_t st = csr->ctx->stream;
-    void *ptrs[] = {csr->rowptr, csr->cols, csr->vals, csr->hi, csr->lo, csr->lower_len, csr->ref_rowptr, csr->diag};
+    void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
+                    csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals};
     for (void *p : ptrs)
         if (p)
             cudaFreeAsync(p, st);
@@ -53,6 +54,10 @@ void csr_release(pyci_gpu_csr *csr) {
     csr->lower_len = nullptr;
     csr->ref_rowptr = nullptr;
     csr->diag = nullptr;
+    csr->sell_off = nullptr;
+    csr->sell_cols = nullptr;
+    csr->sell_vals = nullptr;
+    csr->nslice = csr->sell_nnz = 0;
 }
 
 extern "C" {
@@ -231,6 +236,10 @@ int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
     next.lower_len = nullptr;
     next.ref_rowptr = nullptr;
     next.diag = nullptr;
+    next.sell_off = nullptr;
+    next.sell_cols = nullptr;
+    next.sell_vals = nullptr;
+    next.nslice = next.sell_nnz = 0;
     next.flags = flags;
     next.ndet = ndet;
     next.nrow = ndet;
@@ -279,6 +288,9 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     c->lower_len = nullptr;
     c->ref_rowptr = nullptr;
     c->diag = nullptr;
+    c->sell_off = nullptr;
+    c->sell_cols = nullptr;
+    c->sell_vals = nullptr;
     struct Item {
         void *src;
         void **dst;
@@ -292,6 +304,9 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         {csr->lower_len, reinterpret_cast<void **>(&c->lower_len), sizeof(int32_t) * csr->nrow},
         {csr->ref_rowptr, reinterpret_cast<void **>(&c->ref_rowptr), sizeof(int64_t) * (csr->nrow + 1)},
         {csr->diag, reinterpret_cast<void **>(&c->diag), sizeof(double) * csr->nrow},
+        {csr->sell_off, reinterpret_cast<void **>(&c->sell_off), sizeof(int64_t) * (csr->nslice + 1)},
+        {csr->sell_cols, reinterpret_cast<void **>(&c->sell_cols), sizeof(int32_t) * csr->sell_nnz},
+        {csr->sell_vals, reinterpret_cast<void **>(&c->sell_vals), sizeof(float) * csr->sell_nnz},
     };
     for (auto &it : items) {
         if (!it.src)

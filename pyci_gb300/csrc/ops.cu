@@ -130,6 +130,46 @@ __device__ void unrank_words(int64_t rank, int nbasis, int nocc, const int64_t *
     }
 }
 
+// SELL-32 slice sizes: len[s] = 32 x (longest row of rows 32 s .. 32 s + 31).
+__global__ void sell_sizes_kernel(int64_t nrow, const int64_t *__restrict__ rowptr, int64_t nslice,
+                                  int64_t *__restrict__ len) {
+    for (int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; s < nslice;
+         s += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int64_t longest = 0;
+        const int64_t r1 = min(nrow, 32 * s + 32);
+        for (int64_t r = 32 * s; r < r1; ++r)
+            longest = max(longest, rowptr[r + 1] - rowptr[r]);
+        len[s] = 32 * longest;
+    }
+}
+
+// One warp per slice: lane l copies row 32 s + l's columns and FP32 values
+// to positions off[s] + 32 j + l; past the row's end it repeats the row's
+// last column with a zero value (a valid column near the lane's others).
+__global__ void sell_fill_kernel(int64_t nrow, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
+                                 const float *__restrict__ hi, int64_t nslice, const int64_t *__restrict__ off,
+                                 int32_t *__restrict__ scols, float *__restrict__ svals) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
+        const int64_t r = 32 * s + lane;
+        const int64_t start = r < nrow ? rowptr[r] : 0, len = r < nrow ? rowptr[r + 1] - start : 0;
+        const int64_t o = off[s], L = (off[s + 1] - o) >> 5;
+        int32_t last = len > 0 ? cols[start] : 0;
+        for (int64_t j = 0; j < L; ++j) {
+            int32_t c = last;
+            float v = 0.0f;
+            if (j < len) {
+                c = __ldg(cols + start + j);
+                v = __ldg(hi + start + j);
+                last = c;
+            }
+            scols[o + 32 * j + lane] = c;
+            svals[o + 32 * j + lane] = v;
+        }
+    }
+}
+
 __global__ void all_dets_kernel(int64_t ndet, int two_spin, int64_t nbeta, int nbasis, int nocc_up,
                                 int nocc_dn, const int64_t *binom, int ldk, int nword,
                                 uint64_t *dets) {
@@ -241,6 +281,57 @@ int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, d
     return PYCI_GPU_OK;
 }
 
+// SELL-32 copy of the FP32 operator (see pyci_gpu_csr::sell_*), built when
+// the slices' padding adds at most 1/16 to the stored entries (full FullCI
+// and DOCI spaces have equal rows: no padding).  Skipped silently otherwise;
+// the SpMM autotuner then never sees the variant.
+static int sell_build(pyci_gpu_csr *csr) {
+    cudaStream_t st = csr->ctx->stream;
+    if (csr->lower_only || csr->nnz == 0 || csr->ncol == 0 || csr->nrow == 0 || csr->sell_cols)
+        return PYCI_GPU_OK;
+    const int64_t nslice = (csr->nrow + 31) / 32;
+    int64_t *len = nullptr, *off = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&len), sizeof(int64_t) * nslice, st));
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&off), sizeof(int64_t) * (nslice + 1), st));
+    sell_sizes_kernel<<<grid_for(csr->ctx, nslice, 256), 256, 0, st>>>(csr->nrow, csr->rowptr, nslice, len),
+        ::pyci_gpu::note_launch();
+    int rc = device_exclusive_scan(len, nslice, off, st);
+    int64_t total = 0;
+    if (rc == PYCI_GPU_OK) {
+        cudaError_t e = cudaMemcpyAsync(&total, off + nslice, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            rc = cuda_status(e, "SELL sizes");
+    }
+    cudaFreeAsync(len, st);
+    if (rc != PYCI_GPU_OK || total > csr->nnz + csr->nnz / 16) {
+        cudaFreeAsync(off, st);
+        return rc;
+    }
+    int32_t *scols = nullptr;
+    float *svals = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&scols), sizeof(int32_t) * total, st) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void **>(&svals), sizeof(float) * total, st) != cudaSuccess) {
+        // Out of device memory: the CSR kernels serve the FP32 product.
+        cudaGetLastError();
+        if (scols)
+            cudaFreeAsync(scols, st);
+        cudaFreeAsync(off, st);
+        return PYCI_GPU_OK;
+    }
+    sell_fill_kernel<<<grid_for(csr->ctx, nslice * 32, 256), 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi,
+                                                                           nslice, off, scols, svals),
+        ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    csr->nslice = nslice;
+    csr->sell_nnz = total;
+    csr->sell_off = off;
+    csr->sell_cols = scols;
+    csr->sell_vals = svals;
+    return PYCI_GPU_OK;
+}
+
 int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
     cudaStream_t st = csr->ctx->stream;
     if (!csr->hi) {
@@ -255,6 +346,9 @@ int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
             split_kernel<<<grid_for(csr->ctx, csr->nnz, 256), 256, 0, st>>>(csr->nnz, csr->vals,
                                                                            csr->hi, csr->lo), ::pyci_gpu::note_launch();
         PYCI_CUDA_TRY(cudaGetLastError());
+        int rc = sell_build(csr);
+        if (rc)
+            return rc;
     }
     if (drop_fp64 && csr->vals) {
         PYCI_CUDA_TRY(cudaFreeAsync(csr->vals, st));

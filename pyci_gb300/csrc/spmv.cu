@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -262,6 +263,82 @@ __global__ void __launch_bounds__(256) spmm_cb_kernel(int64_t nrow, const int64_
     }
 }
 
+// FP32 product on the SELL-32 copy: one warp per slice of 32 rows, lane l
+// owns row 32 s + l and walks it in lockstep with the warp (entry j of all 32
+// rows is one coalesced 128-byte load of columns and one of values).  The
+// slice's rows share their column blocks of x (consecutive FCI / DOCI rows
+// differ in the low orbitals), so a warp's 32 gathers touch far fewer cache
+// lines than the 32 gathers of one CSR row.  Each lane sums its row in order;
+// no reduction across lanes.
+template<int K, bool VEC>
+__global__ void __launch_bounds__(256) spmm_sell_kernel(int64_t nrow, int64_t nslice, const int64_t *__restrict__ off,
+                                                        const int32_t *__restrict__ cols,
+                                                        const float *__restrict__ vals, const float *__restrict__ x,
+                                                        int64_t ldx, float *__restrict__ y, int64_t ldy) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
+        const int64_t o = off[s];
+        const int64_t L = (off[s + 1] - o) >> 5;
+        const int32_t *cp = cols + o + lane;
+        const float *vp = vals + o + lane;
+        float acc[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            acc[k] = 0.0f;
+        float xv[K];
+        int64_t j = 0;
+        for (; j + 4 <= L; j += 4) {
+            int32_t c[4];
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                c[u] = __ldcs(cp + 32 * (j + u));
+                v[u] = __ldcs(vp + 32 * (j + u));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                load_x<VEC, K>(x + static_cast<int64_t>(c[u]) * ldx, xv);
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    acc[k] += v[u] * xv[k];
+            }
+        }
+        for (; j < L; ++j) {
+            const int32_t c = __ldcs(cp + 32 * j);
+            const float v = __ldcs(vp + 32 * j);
+            load_x<VEC, K>(x + static_cast<int64_t>(c) * ldx, xv);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                acc[k] += v * xv[k];
+        }
+        const int64_t r = 32 * s + lane;
+        if (r < nrow) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                y[r * ldy + k] = acc[k];
+        }
+    }
+}
+
+template<int K>
+void launch_sell(const pyci_gpu_csr *csr, const void *x, int64_t ldx, void *y, int64_t ldy, cudaStream_t st) {
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice * 32 + 255) / 256));
+    const size_t rowbytes = static_cast<size_t>(ldx) * sizeof(float);
+    const size_t vbytes = (K * sizeof(float)) % 16 == 0 ? 16 : ((K * sizeof(float)) == 8 ? 8 : 0);
+    const bool vec = vbytes && (reinterpret_cast<uintptr_t>(x) % vbytes == 0) && (rowbytes % vbytes == 0);
+    if (vec)
+        spmm_sell_kernel<K, true><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+            csr->nrow, csr->nslice, csr->sell_off, csr->sell_cols, csr->sell_vals, static_cast<const float *>(x), ldx,
+            static_cast<float *>(y), ldy);
+    else
+        spmm_sell_kernel<K, false><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+            csr->nrow, csr->nslice, csr->sell_off, csr->sell_cols, csr->sell_vals, static_cast<const float *>(x), ldx,
+            static_cast<float *>(y), ldy);
+    ::pyci_gpu::note_launch();
+}
+
 template<int VK, int K, int LANES>
 void launch_cb(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y, int64_t ldy,
                int nblk, cudaStream_t st) {
@@ -307,14 +384,29 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
             static_cast<x_t *>(y), ldy), ::pyci_gpu::note_launch();
 }
 
-// Tile variants: lanes per row (8, 16, 32) x entry mapping (0, 1).
+// Tile variants: lanes per row (8, 16, 32) x entry mapping (0, 1); and, for
+// the FP32 values of an operator that has one, the SELL-32 copy.
 constexpr int kVariants = 6;
+constexpr int kSellVariant = 0x100;
 inline int variant_lanes(int v) { return v % 3 == 0 ? 8 : (v % 3 == 1 ? 16 : 32); }
 inline int variant_map(int v) { return v / 3; }
+
+inline int heuristic_variant(const pyci_gpu_csr *csr);
 
 template<int VK, int K>
 void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                     int64_t ldy, cudaStream_t st) {
+    if (v == kSellVariant) {
+        if constexpr (VK == kF32) {
+            if (csr->sell_cols) {
+                launch_sell<K>(csr, x, ldx, y, ldy, st);
+                return;
+            }
+        }
+        // A cached choice from an operator of the same shape that had the
+        // SELL copy: this one runs the row-length heuristic instead.
+        v = heuristic_variant(csr);
+    }
     const int nblk = v >> 4;
     v &= 15;
     if (nblk > 1) {
@@ -390,6 +482,20 @@ bool autotune_enabled() {
     return on;
 }
 
+// PYCI_GPU_SPMM=sell or =csr pins the FP32 product of operators built after
+// it is set to the SELL-32 copy or to the CSR heuristic (read when an
+// operator makes its first product, so a process can compare the two).
+int forced_f32_variant(const pyci_gpu_csr *csr) {
+    const char *e = std::getenv("PYCI_GPU_SPMM");
+    if (!e)
+        return -1;
+    if (!std::strcmp(e, "sell"))
+        return csr->sell_cols ? kSellVariant : heuristic_variant(csr);
+    if (!std::strcmp(e, "csr"))
+        return heuristic_variant(csr);
+    return -1;
+}
+
 // Autotuner: the first product of an operator for a (precision, width) pair
 // times every tile variant (one warm-up + two timed launches each, CUDA
 // events on the caller's stream) and keeps the fastest for later calls.
@@ -403,6 +509,8 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
         const void *xs = static_cast<const x_t *>(x) + j0;
         void *ys = static_cast<x_t *>(y) + j0;
         int &choice = csr->tuned[VK][K];
+        if (choice < 0 && VK == kF32)
+            choice = forced_f32_variant(csr);
         if (choice < 0)
             choice = tuning_cache_lookup(csr, VK, K);
         if (choice < 0) {
@@ -428,12 +536,28 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
                         best_v = v;
                     }
                 }
+                const int best_csr = best_v;
+                // The SELL-32 copy (FP32 values only).
+                if (VK == kF32 && csr->sell_cols) {
+                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(a, st);
+                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
+                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(b, st);
+                    cudaEventSynchronize(b);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (ms < best) {
+                        best = ms;
+                        best_v = kSellVariant;
+                    }
+                }
                 // Column blocks when the gathered block of vectors is larger
                 // than about half the L2 (126 MB on this GPU).
                 const double xbytes = static_cast<double>(csr->ncol) * K * sizeof(x_t);
                 if (xbytes > 48.0 * (1 << 20) && csr->ncol < INT32_MAX) {
                     for (int nblk = 2; nblk <= 4; ++nblk) {
-                        const int v = best_v | (nblk << 4);
+                        const int v = best_csr | (nblk << 4);
                         launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);
                         cudaEventRecord(a, st);
                         launch_k<VK>(v, csr, vals, K, xs, k, ys, k, st);

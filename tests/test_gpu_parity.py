@@ -164,6 +164,40 @@ def test_spmm_precisions_against_oracle(ctx):
     csr.free()
 
 
+@pytest.mark.parametrize("kind,n,nu,nd", [("fullci", 8, 4, 4), ("doci", 16, 6, 6), ("fullci", 9, 4, 2)])
+def test_spmm_fp32_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
+    r"""The FP32 product on the SELL-32 copy (pinned with PYCI_GPU_SPMM=sell)
+    and on the CSR kernels (=csr) against the oracle's FP64 product; row
+    counts that leave a partial last slice of 32 rows."""
+    import torch
+    ecore, one, two = synthetic_integrals(n, 1003)
+    dets = O.all_dets(OKIND[kind], n, nu, nd)
+    ref = O.build_csr(OKIND[kind], n, nu, nd, dets, one, two)
+    N = dets.shape[0]
+    rng = np.random.default_rng(8)
+    out = {}
+    for mode in ("sell", "csr"):
+        monkeypatch.setenv("PYCI_GPU_SPMM", mode)
+        csr = capi.Csr(ctx, WFN[kind], n, nu, nd, dets, one, two, flags=capi.BUILD_FULL_COLEX)
+        csr.prepare_mixed(drop_fp64=True)
+        for k in (1, 2, 3, 4, 8, 11):
+            X = rng.normal(size=(N, k)) if mode == "sell" else out[("x", k)]
+            xf = torch.tensor(X, dtype=torch.float32, device="cuda")
+            yf = torch.empty((N, k), dtype=torch.float32, device="cuda")
+            csr.spmm_device(capi.PREC_FP32, k, xf.data_ptr(), yf.data_ptr(), None)
+            torch.cuda.synchronize()
+            out[("x", k)] = X
+            out[(mode, k)] = yf.cpu().numpy().astype(np.float64)
+        csr.free()
+    for k in (1, 2, 3, 4, 8, 11):
+        X = out[("x", k)].astype(np.float32).astype(np.float64)
+        Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
+        scale = np.abs(Y_ref).max()
+        for mode in ("sell", "csr"):
+            # FP32 values and accumulation: relative error ~ sqrt(row length) * 2^-24
+            assert np.abs(out[(mode, k)] - Y_ref).max() / scale < 1e-5, (mode, k)
+
+
 def split_rows(X):
     r"""[N][k] FP64 -> [N][2k] FP32: each row's high parts, then its low parts."""
     hi = X.astype(np.float32)
