@@ -73,6 +73,8 @@ typedef struct pyci_gpu_solve_stats {
     double seconds;       /* wall time inside the solve                           */
     double seconds_spmm;  /* device time of the SpMM launches (CUDA events)       */
     double max_residual;  /* final max over roots of ||H x - theta x||, FP64      */
+    int64_t host_syncs;   /* stream synchronisations (device -> host round trips) */
+    double seconds_wait;  /* wall time the host spent blocked in them             */
 } pyci_gpu_solve_stats;
 
 /* Thread-local message of the last failure of the calling thread. */

@@ -37,7 +37,8 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("matvecs", ctypes.c_int64),
                 ("matvecs_fp64", ctypes.c_int64), ("restarts", ctypes.c_int64),
                 ("refinements", ctypes.c_int64), ("seconds", ctypes.c_double),
-                ("seconds_spmm", ctypes.c_double), ("max_residual", ctypes.c_double)]
+                ("seconds_spmm", ctypes.c_double), ("max_residual", ctypes.c_double),
+                ("host_syncs", ctypes.c_int64), ("seconds_wait", ctypes.c_double)]
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}

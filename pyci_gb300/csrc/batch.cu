@@ -1369,6 +1369,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         stats->seconds_spmm = spmm_ms_ * 1e-3;
         stats->max_residual = max_res;
+        stats->host_syncs = 0; // not counted by the batched solver
+        stats->seconds_wait = 0.0;
     }
     return PYCI_GPU_OK;
 }

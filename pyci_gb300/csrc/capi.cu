@@ -42,7 +42,8 @@ void csr_release(pyci_gpu_csr *csr) {
         return;
     cudaStream_t st = csr->ctx->stream;
     void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
-                    csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals};
+                    csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals,
+                    csr->sell_lo};
     for (void *p : ptrs)
         if (p)
             cudaFreeAsync(p, st);
@@ -57,6 +58,7 @@ void csr_release(pyci_gpu_csr *csr) {
     csr->sell_off = nullptr;
     csr->sell_cols = nullptr;
     csr->sell_vals = nullptr;
+    csr->sell_lo = nullptr;
     csr->nslice = csr->sell_nnz = 0;
 }
 
@@ -239,6 +241,7 @@ int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
     next.sell_off = nullptr;
     next.sell_cols = nullptr;
     next.sell_vals = nullptr;
+    next.sell_lo = nullptr;
     next.nslice = next.sell_nnz = 0;
     next.flags = flags;
     next.ndet = ndet;
@@ -291,6 +294,7 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     c->sell_off = nullptr;
     c->sell_cols = nullptr;
     c->sell_vals = nullptr;
+    c->sell_lo = nullptr;
     struct Item {
         void *src;
         void **dst;
@@ -307,6 +311,7 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         {csr->sell_off, reinterpret_cast<void **>(&c->sell_off), sizeof(int64_t) * (csr->nslice + 1)},
         {csr->sell_cols, reinterpret_cast<void **>(&c->sell_cols), sizeof(int32_t) * csr->sell_nnz},
         {csr->sell_vals, reinterpret_cast<void **>(&c->sell_vals), sizeof(float) * csr->sell_nnz},
+        {csr->sell_lo, reinterpret_cast<void **>(&c->sell_lo), sizeof(float) * csr->sell_nnz},
     };
     for (auto &it : items) {
         if (!it.src)

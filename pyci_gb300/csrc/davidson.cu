@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
@@ -86,12 +87,48 @@ inline int padded_width(int k) { return k == 3 ? 4 : (k > 4 && k < 8 ? 8 : k); }
 // per gathered byte at any width.
 constexpr int kSpmmChunk = 4;
 
+// R consecutive entries of a vector from one 16-byte load (R = 16 /
+// sizeof(T)), or one entry (R = 1).
+template<typename T, int R>
+__device__ __forceinline__ void load_rows(const T *__restrict__ p, T (&v)[R]) {
+    if constexpr (R == 1) {
+        v[0] = p[0];
+    } else if constexpr (sizeof(T) == 4) {
+        static_assert(R == 4, "four floats per 16-byte load");
+        const float4 w = *reinterpret_cast<const float4 *>(p);
+        v[0] = w.x, v[1] = w.y, v[2] = w.z, v[3] = w.w;
+    } else {
+        static_assert(R == 2, "two doubles per 16-byte load");
+        const double2 w = *reinterpret_cast<const double2 *>(p);
+        v[0] = w.x, v[1] = w.y;
+    }
+}
+
+// Stores R consecutive entries (R = 1, or 16 / sizeof(TV) of the input
+// vectors: one 16-byte store per 4 floats or per 2 doubles).
+template<typename T, int R>
+__device__ __forceinline__ void store_rows(T *__restrict__ p, const T (&v)[R]) {
+    if constexpr (R == 1) {
+        p[0] = v[0];
+    } else if constexpr (sizeof(T) == 4) {
+        static_assert(R == 4, "four floats per 16-byte store");
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int t = 0; t < R; t += 2)
+            *reinterpret_cast<double2 *>(p + t) = make_double2(v[t], v[t + 1]);
+    }
+}
+
 // Row-streaming Gram product: block (x, y) sums A[i][r] * B[j][r] over a
 // grid-stride set of rows for i in [y * PI, y * PI + PI), j < q <= QC, with
 // a per-thread PI x QC register tile (one coalesced pass over the rows), then
 // reduces across the block; partial[x][i * q + j].  QC is the smallest of
 // 1, 2, 4, 8 that holds q, so the tile (and the register count) follows q.
-template<typename T, int PI, int QC>
+// R > 1: each thread step takes R consecutive rows with 16-byte loads (N a
+// multiple of R, vectors 16-byte aligned), R times the bytes in flight per
+// load instruction of the one-row form.
+template<typename T, int PI, int QC, int R>
 __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
                                                         int q, int64_t N, double *__restrict__ partial) {
     const int i0 = blockIdx.y * PI;
@@ -102,19 +139,31 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
 #pragma unroll
         for (int j = 0; j < QC; ++j)
             acc[ii][j] = T(0);
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        T bv[QC];
+    const int64_t nu = N / R;
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
+         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = u * R;
+        T bv[QC][R];
 #pragma unroll
-        for (int j = 0; j < QC; ++j)
-            bv[j] = (j < q) ? B[j * N + r] : T(0);
+        for (int j = 0; j < QC; ++j) {
+            if (j < q) {
+                load_rows<T, R>(B + j * N + r, bv[j]);
+            } else {
+#pragma unroll
+                for (int t = 0; t < R; ++t)
+                    bv[j][t] = T(0);
+            }
+        }
 #pragma unroll
         for (int ii = 0; ii < PI; ++ii) {
             if (ii < ni) {
-                const T a = A[(i0 + ii) * N + r];
+                T a[R];
+                load_rows<T, R>(A + (i0 + ii) * N + r, a);
 #pragma unroll
                 for (int j = 0; j < QC; ++j)
-                    acc[ii][j] += a * bv[j];
+#pragma unroll
+                    for (int t = 0; t < R; ++t)
+                        acc[ii][j] += a[t] * bv[j][t];
             }
         }
     }
@@ -144,22 +193,48 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
 // Launch gram_rows_kernel with the register tile that fits q (<= 8): rows
 // of A per block PI = 8 (4 when q > 4).  budget: blocks to aim for.  Returns
 // the number of partial sums per entry (blocks along x).
+// One wave of blocks: the grid holds at most as many blocks as are resident
+// at once (occupancy of the instantiation, at most 4 per SM), so no block
+// runs in a second, partly idle wave.  budget = 4 blocks per SM; partial
+// holds budget blocks' sums.
+template<typename T, int PI, int QC, int R>
+unsigned launch_gram_tile(unsigned budget, cudaStream_t st, const T *A, int p, const T *B, int q, int64_t N,
+                          double *partial) {
+    static const int per_sm = [] {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gram_rows_kernel<T, PI, QC, R>, 256, 0) != cudaSuccess)
+            n = 1;
+        return std::max(1, std::min(4, n));
+    }();
+    const int64_t wave = static_cast<int64_t>(budget / 4) * per_sm;
+    const unsigned gy = static_cast<unsigned>((p + PI - 1) / PI);
+    const unsigned nb = static_cast<unsigned>(
+        std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(1, wave / gy), (N / R + 255) / 256)));
+    gram_rows_kernel<T, PI, QC, R><<<dim3(nb, gy), 256, 0, st>>>(A, p, B, q, N, partial);
+    return nb;
+}
+
+template<typename T, int R>
+unsigned launch_gram_rows_r(unsigned budget, cudaStream_t st, const T *A, int p, const T *B, int q, int64_t N,
+                            double *partial) {
+    if (q <= 1)
+        return launch_gram_tile<T, 8, 1, R>(budget, st, A, p, B, q, N, partial);
+    if (q <= 2)
+        return launch_gram_tile<T, 8, 2, R>(budget, st, A, p, B, q, N, partial);
+    if (q <= 4)
+        return launch_gram_tile<T, 8, 4, R>(budget, st, A, p, B, q, N, partial);
+    return launch_gram_tile<T, 4, 8, R>(budget, st, A, p, B, q, N, partial);
+}
+
+// 16-byte row loads when N is a multiple of 16 / sizeof(T) and both vector
+// sets start on 16-byte boundaries (every vector then does).
 template<typename T>
 unsigned launch_gram_rows(unsigned budget, cudaStream_t st, const T *A, int p, const T *B, int q, int64_t N,
                           double *partial) {
-    const int pi = (q <= 4) ? 8 : 4;
-    const unsigned gy = static_cast<unsigned>((p + pi - 1) / pi);
-    const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(budget / gy, (N + 255) / 256)));
-    const dim3 g(nb, gy);
-    if (q <= 1)
-        gram_rows_kernel<T, 8, 1><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
-    else if (q <= 2)
-        gram_rows_kernel<T, 8, 2><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
-    else if (q <= 4)
-        gram_rows_kernel<T, 8, 4><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
-    else
-        gram_rows_kernel<T, 4, 8><<<g, 256, 0, st>>>(A, p, B, q, N, partial);
-    return nb;
+    constexpr int R = 16 / sizeof(T);
+    if (N % R == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0 && reinterpret_cast<uintptr_t>(B) % 16 == 0)
+        return launch_gram_rows_r<T, R>(budget, st, A, p, B, q, N, partial);
+    return launch_gram_rows_r<T, 1>(budget, st, A, p, B, q, N, partial);
 }
 
 __global__ void reduce_partials_kernel(const double *__restrict__ partial, int nblocks, int pq,
@@ -184,8 +259,10 @@ __global__ void reduce_partials_kernel(const double *__restrict__ partial, int n
 }
 
 // out[j][r] = beta * out[j][r] + sum_{i < p} Y[i * q + j] * V[i][r]
-// (accumulated in ACC; q <= kMaxQ).
-template<typename TV, typename TO, typename ACC>
+// (accumulated in ACC; q <= kMaxQ).  R > 1: R consecutive rows per thread
+// step with 16-byte loads and stores (N a multiple of R, 16-byte aligned
+// vectors); R = 1 otherwise.
+template<typename TV, typename TO, typename ACC, int R>
 __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, int p, int64_t N,
                                                       const double *__restrict__ Y, int q,
                                                       double beta, TO *__restrict__ out) {
@@ -193,25 +270,43 @@ __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, 
     for (int e = threadIdx.x; e < p * q; e += blockDim.x)
         sy[e] = static_cast<ACC>(Y[e]);
     __syncthreads();
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        ACC acc[kMaxQ];
+    const int64_t nu = N / R;
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
+         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = u * R;
+        ACC acc[kMaxQ][R];
 #pragma unroll
         for (int j = 0; j < kMaxQ; ++j)
-            acc[j] = 0;
+#pragma unroll
+            for (int t = 0; t < R; ++t)
+                acc[j][t] = 0;
         for (int i = 0; i < p; ++i) {
-            const ACC v = static_cast<ACC>(V[i * N + r]);
+            TV v[R];
+            load_rows<TV, R>(V + i * N + r, v);
 #pragma unroll
             for (int j = 0; j < kMaxQ; ++j)
-                if (j < q)
-                    acc[j] += sy[i * q + j] * v;
+                if (j < q) {
+                    const ACC y = sy[i * q + j];
+#pragma unroll
+                    for (int t = 0; t < R; ++t)
+                        acc[j][t] += y * static_cast<ACC>(v[t]);
+                }
         }
 #pragma unroll
         for (int j = 0; j < kMaxQ; ++j)
             if (j < q) {
                 TO *o = out + j * N + r;
-                *o = (beta == 0.0) ? static_cast<TO>(acc[j])
-                                   : static_cast<TO>(static_cast<ACC>(beta) * static_cast<ACC>(*o) + acc[j]);
+                TO w[R];
+                if (beta == 0.0) {
+#pragma unroll
+                    for (int t = 0; t < R; ++t)
+                        w[t] = static_cast<TO>(acc[j][t]);
+                } else {
+#pragma unroll
+                    for (int t = 0; t < R; ++t)
+                        w[t] = static_cast<TO>(static_cast<ACC>(beta) * static_cast<ACC>(o[t]) + acc[j][t]);
+                }
+                store_rows<TO, R>(o, w);
             }
     }
 }
@@ -324,6 +419,8 @@ public:
             cudaEventDestroy(pr.second);
         }
         cudaStreamSynchronize(st_);
+        if (h_small_)
+            cudaFreeHost(h_small_);
     }
 
     int run(const double *c0, int64_t maxiter, double tol, double ecore, double *evals, double *evecs,
@@ -369,17 +466,23 @@ private:
                     ::pyci_gpu::note_launch();
                 }
                 reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq, d_small_), ::pyci_gpu::note_launch();
-                std::vector<double> tmp(static_cast<size_t>(pp) * qq);
-                cudaError_t e = cudaMemcpyAsync(tmp.data(), d_small_, sizeof(double) * pp * qq,
+                // Read back through the pinned buffer: one DMA, then one
+                // synchronisation (a pageable copy would block inside the
+                // copy call instead).
+                const auto t0 = std::chrono::steady_clock::now();
+                cudaError_t e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pp * qq,
                                                 cudaMemcpyDeviceToHost, st_);
                 if (e != cudaSuccess)
                     return cuda_status(e, "gram copy");
                 e = cudaStreamSynchronize(st_);
+                wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+                ++syncs_;
                 if (e != cudaSuccess)
                     return cuda_status(e, "gram");
+                const double *tmp = h_small_;
                 if (on_tc) {
-                    for (double v : tmp)
-                        if (!std::isfinite(v) && gram_tc_error(true)) {
+                    for (int e2 = 0; e2 < pp * qq; ++e2)
+                        if (!std::isfinite(tmp[e2]) && gram_tc_error(true)) {
                             set_error("tensor-core Gram product: MMA completion wait timed out");
                             return PYCI_GPU_ECUDA;
                         }
@@ -403,12 +506,19 @@ private:
                 for (int i = 0; i < pp; ++i)
                     for (int j = 0; j < qq; ++j)
                         sub[static_cast<size_t>(i) * qq + j] = Y[static_cast<size_t>(i0 + i) * q + j0 + j];
-                const int rc = csr_->ctx->ring->upload(d_coef_, sub.data(), sizeof(double) * sub.size(), st_);
+                const int rc = upload(d_coef_, sub.data(), sizeof(double) * sub.size(), st_);
                 if (rc)
                     return rc;
-                combine_kernel<TV, TO, ACC><<<grid(N_), 256, 0, st_>>>(
-                    V + static_cast<int64_t>(i0) * N_, pp, N_, d_coef_, qq, (i0 == 0) ? beta : 1.0,
-                    out + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
+                const TV *Vi = V + static_cast<int64_t>(i0) * N_;
+                TO *Oj = out + static_cast<int64_t>(j0) * N_;
+                const double bt = (i0 == 0) ? beta : 1.0;
+                constexpr int R = 16 / sizeof(TV);
+                if (N_ % R == 0 && reinterpret_cast<uintptr_t>(Vi) % 16 == 0 &&
+                    reinterpret_cast<uintptr_t>(Oj) % 16 == 0)
+                    combine_kernel<TV, TO, ACC, R><<<grid(N_ / R), 256, 0, st_>>>(Vi, pp, N_, d_coef_, qq, bt, Oj);
+                else
+                    combine_kernel<TV, TO, ACC, 1><<<grid(N_), 256, 0, st_>>>(Vi, pp, N_, d_coef_, qq, bt, Oj);
+                ::pyci_gpu::note_launch();
             }
         }
         return PYCI_GPU_OK;
@@ -463,6 +573,31 @@ private:
                 total += ms;
         }
         return total;
+    }
+    // Host-side synchronisation with the stream, counted and timed.
+    cudaError_t wait() {
+        const auto t0 = std::chrono::steady_clock::now();
+        const cudaError_t e = cudaStreamSynchronize(st_);
+        wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        ++syncs_;
+        return e;
+    }
+    int64_t syncs_ = 0;
+    double wait_s_ = 0.0, upload_s_ = 0.0, eig_s_ = 0.0;
+    double *h_small_ = nullptr; // pinned [kMaxGramP * kMaxQ]
+    // Host -> device copy of small coefficient blocks through the context's
+    // pinned ring (which may wait for a slot's previous copy).
+    int upload(void *dst, const void *src, size_t n, cudaStream_t st) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const int rc = csr_->ctx->ring->upload(dst, src, n, st);
+        upload_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return rc;
+    }
+    bool eig(int m, const std::vector<double> &a, std::vector<double> &w, std::vector<double> &z) {
+        const auto t0 = std::chrono::steady_clock::now();
+        const bool ok = symmetric_eigen(m, a, w, z);
+        eig_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return ok;
     }
     int64_t matvecs_ = 0, matvecs64_ = 0;
     unsigned gram_blocks_ = 1;
@@ -669,12 +804,13 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         (rc = alloc(&d_small_, kMaxGramP * kMaxQ)) || (rc = alloc(&d_coef_, kMaxGramP * kMaxQ)) ||
         (rc = alloc(&d_theta_, std::max(mmax, b))))
         return rc;
+    PYCI_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&h_small_), sizeof(double) * kMaxGramP * kMaxQ));
     double *d_diag = csr_->diag;
 
     // Diagonal on the host for the initial guess.
     std::vector<double> diag(N);
     PYCI_CUDA_TRY(cudaMemcpyAsync(diag.data(), d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
-    PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+    PYCI_CUDA_TRY(wait());
 
     // Initial block.
     int m = 0, knew = 0;
@@ -687,7 +823,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_idx, idx.data(), sizeof(int64_t) * N, cudaMemcpyHostToDevice, st_));
         for (int64_t j0 = 0; j0 < N; j0 += 64)
             unit_kernel<T><<<grid(N), 256, 0, st_>>>(V + j0 * N, N, d_idx + j0, static_cast<int>(std::min<int64_t>(64, N - j0))), ::pyci_gpu::note_launch();
-        PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+        PYCI_CUDA_TRY(wait());
         knew = static_cast<int>(N);
     } else {
         // Unit vectors on the lowest diagonal elements (after c0, if given),
@@ -705,7 +841,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             for (int64_t r = 0; r < N; ++r)
                 hc[r] = static_cast<T>(c0[r]);
             PYCI_CUDA_TRY(cudaMemcpyAsync(V, hc.data(), sizeof(T) * N, cudaMemcpyHostToDevice, st_));
-            PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+            PYCI_CUDA_TRY(wait());
             if ((rc = orthonormalize(V, 0, 1, knew)))
                 return rc;
         }
@@ -755,7 +891,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         for (int i = 0; i < m; ++i)
             for (int j = 0; j < m; ++j)
                 Gm[static_cast<size_t>(i) * m + j] = G[static_cast<size_t>(i) * mmax + j];
-        if (!symmetric_eigen(m, Gm, theta, Y)) {
+        if (!eig(m, Gm, theta, Y)) {
             set_error("Rayleigh-Ritz eigensolver failed");
             return PYCI_GPU_ENOCONV;
         }
@@ -766,7 +902,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 Yb[static_cast<size_t>(i) * b + j] = Y[static_cast<size_t>(i) * m + j];
         if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
             return rc;
-        if ((rc = csr_->ctx->ring->upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
+        if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
             return rc;
         residual_kernel<T><<<grid(N), 256, 0, st_>>>(AXr, Xr, d_theta_, b, N, R), ::pyci_gpu::note_launch();
         bool all = true;
@@ -859,7 +995,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             std::vector<double> G64, th64, Z;
             if ((rc = gram<double>(X64, br, AX64, br, G64)))
                 return rc;
-            if (!symmetric_eigen(br, G64, th64, Z)) {
+            if (!eig(br, G64, th64, Z)) {
                 set_error("Rayleigh-Ritz eigensolver failed");
                 return PYCI_GPU_ENOCONV;
             }
@@ -870,7 +1006,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if ((rc = combine<double, double, double>(AX64, br, Z, br, 0.0, R64)))
                 return rc;
             PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
-            if ((rc = csr_->ctx->ring->upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
+            if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
                 return rc;
             residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, br, N, R64), ::pyci_gpu::note_launch();
             bool ok64 = true;
@@ -904,7 +1040,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 m = b;
                 ++restarts;
             }
-            if ((rc = csr_->ctx->ring->upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
+            if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
                 return rc;
             int q = 0;
             for (int j : todo) {
@@ -940,7 +1076,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             ++restarts;
         }
         // Preconditioned residuals of the unconverged roots.
-        if ((rc = csr_->ctx->ring->upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
+        if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
             return rc;
         int q = 0;
         for (int j : todo) {
@@ -974,7 +1110,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             }
         }
     }
-    PYCI_CUDA_TRY(cudaStreamSynchronize(st_));
+    PYCI_CUDA_TRY(wait());
     if (stats) {
         stats->iterations = iter + 1;
         stats->matvecs = matvecs_;
@@ -984,7 +1120,16 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
         stats->seconds_spmm = timed_total_ms() * 1e-3;
         stats->max_residual = max_res;
+        stats->host_syncs = syncs_;
+        stats->seconds_wait = wait_s_;
     }
+    // PYCI_GPU_SOLVE_TRACE: one line per solve on stderr with the host-side
+    // breakdown (blocked in read-backs, coefficient uploads, Rayleigh-Ritz).
+    if (std::getenv("PYCI_GPU_SOLVE_TRACE"))
+        std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), upload %.3f ms, eig %.3f ms, iters %lld\n",
+                     std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() * 1e3,
+                     timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), upload_s_ * 1e3, eig_s_ * 1e3,
+                     static_cast<long long>(iter + 1));
     return PYCI_GPU_OK;
 }
 

@@ -936,6 +936,8 @@ struct SparseOp {
         d["refinements"] = st.refinements;
         d["seconds"] = st.seconds;
         d["seconds_spmm"] = st.seconds_spmm;
+        d["host_syncs"] = st.host_syncs;
+        d["seconds_wait"] = st.seconds_wait;
         d["max_residual"] = st.max_residual;
         d["mode"] = mode;
         last_stats = d;

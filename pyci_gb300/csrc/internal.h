@@ -58,8 +58,8 @@ struct pyci_gpu_csr {
     // only the reference's layout is stored; a symmetric product then
     // scatters the transpose with atomics.
     bool lower_only = false;
-    // SELL-32 copy of the FP32 (high-part) operator, built with the mixed-
-    // precision split when rows within each 32-row slice have (nearly) equal
+    // SELL-32 copy of the split operator (high and low FP32 parts), built
+    // with the mixed-precision split when rows within each 32-row slice have (nearly) equal
     // lengths: entry j of slice s, lane l (row 32 s + l) at sell_off[s] + 32 j
     // + l; shorter rows padded with zero values.  One lane per row walks its
     // row while the warp's 32 rows share column blocks of x (consecutive FCI
@@ -69,7 +69,8 @@ struct pyci_gpu_csr {
     int64_t sell_nnz = 0;
     int64_t *sell_off = nullptr;  // [nslice + 1], multiples of 32
     int32_t *sell_cols = nullptr; // [sell_nnz]
-    float *sell_vals = nullptr;   // [sell_nnz]
+    float *sell_vals = nullptr;   // [sell_nnz] high parts
+    float *sell_lo = nullptr;     // [sell_nnz] low parts
 };
 
 namespace pyci_gpu {

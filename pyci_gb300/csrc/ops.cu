@@ -143,12 +143,13 @@ __global__ void sell_sizes_kernel(int64_t nrow, const int64_t *__restrict__ rowp
     }
 }
 
-// One warp per slice: lane l copies row 32 s + l's columns and FP32 values
-// to positions off[s] + 32 j + l; past the row's end it repeats the row's
-// last column with a zero value (a valid column near the lane's others).
+// One warp per slice: lane l copies row 32 s + l's columns and FP32 value
+// halves to positions off[s] + 32 j + l; past the row's end it repeats the
+// row's last column with zero values (a valid column near the lane's others).
 __global__ void sell_fill_kernel(int64_t nrow, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
-                                 const float *__restrict__ hi, int64_t nslice, const int64_t *__restrict__ off,
-                                 int32_t *__restrict__ scols, float *__restrict__ svals) {
+                                 const float *__restrict__ hi, const float *__restrict__ lo, int64_t nslice,
+                                 const int64_t *__restrict__ off, int32_t *__restrict__ scols,
+                                 float *__restrict__ svals, float *__restrict__ slo) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
@@ -158,14 +159,16 @@ __global__ void sell_fill_kernel(int64_t nrow, const int64_t *__restrict__ rowpt
         int32_t last = len > 0 ? cols[start] : 0;
         for (int64_t j = 0; j < L; ++j) {
             int32_t c = last;
-            float v = 0.0f;
+            float v = 0.0f, w = 0.0f;
             if (j < len) {
                 c = __ldg(cols + start + j);
                 v = __ldg(hi + start + j);
+                w = __ldg(lo + start + j);
                 last = c;
             }
             scols[o + 32 * j + lane] = c;
             svals[o + 32 * j + lane] = v;
+            slo[o + 32 * j + lane] = w;
         }
     }
 }
@@ -281,7 +284,7 @@ int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, d
     return PYCI_GPU_OK;
 }
 
-// SELL-32 copy of the FP32 operator (see pyci_gpu_csr::sell_*), built when
+// SELL-32 copy of the split operator (see pyci_gpu_csr::sell_*), built when
 // the slices' padding adds at most 1/16 to the stored entries (full FullCI
 // and DOCI spaces have equal rows: no padding).  Skipped silently otherwise;
 // the SpMM autotuner then never sees the variant.
@@ -310,18 +313,21 @@ static int sell_build(pyci_gpu_csr *csr) {
         return rc;
     }
     int32_t *scols = nullptr;
-    float *svals = nullptr;
+    float *svals = nullptr, *slo = nullptr;
     if (cudaMallocAsync(reinterpret_cast<void **>(&scols), sizeof(int32_t) * total, st) != cudaSuccess ||
-        cudaMallocAsync(reinterpret_cast<void **>(&svals), sizeof(float) * total, st) != cudaSuccess) {
-        // Out of device memory: the CSR kernels serve the FP32 product.
+        cudaMallocAsync(reinterpret_cast<void **>(&svals), sizeof(float) * total, st) != cudaSuccess ||
+        cudaMallocAsync(reinterpret_cast<void **>(&slo), sizeof(float) * total, st) != cudaSuccess) {
+        // Out of device memory: the CSR kernels serve the split products.
         cudaGetLastError();
         if (scols)
             cudaFreeAsync(scols, st);
+        if (svals)
+            cudaFreeAsync(svals, st);
         cudaFreeAsync(off, st);
         return PYCI_GPU_OK;
     }
     sell_fill_kernel<<<grid_for(csr->ctx, nslice * 32, 256), 256, 0, st>>>(csr->nrow, csr->rowptr, csr->cols, csr->hi,
-                                                                           nslice, off, scols, svals),
+                                                                           csr->lo, nslice, off, scols, svals, slo),
         ::pyci_gpu::note_launch();
     PYCI_CUDA_TRY(cudaGetLastError());
     csr->nslice = nslice;
@@ -329,6 +335,7 @@ static int sell_build(pyci_gpu_csr *csr) {
     csr->sell_off = off;
     csr->sell_cols = scols;
     csr->sell_vals = svals;
+    csr->sell_lo = slo;
     return PYCI_GPU_OK;
 }
 

@@ -482,10 +482,11 @@ bool autotune_enabled() {
     return on;
 }
 
-// PYCI_GPU_SPMM=sell or =csr pins the FP32 product of operators built after
-// it is set to the SELL-32 copy or to the CSR heuristic (read when an
-// operator makes its first product, so a process can compare the two).
-int forced_f32_variant(const pyci_gpu_csr *csr) {
+// PYCI_GPU_SPMM=sell or =csr pins the FP32 and double-float products of
+// operators built after it is set to the SELL-32 copy or to the CSR
+// heuristic (read when an operator makes its first product of a kind, so a
+// process can compare the two).
+int forced_sell_variant(const pyci_gpu_csr *csr) {
     const char *e = std::getenv("PYCI_GPU_SPMM");
     if (!e)
         return -1;
@@ -510,7 +511,7 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
         void *ys = static_cast<x_t *>(y) + j0;
         int &choice = csr->tuned[VK][K];
         if (choice < 0 && VK == kF32)
-            choice = forced_f32_variant(csr);
+            choice = forced_sell_variant(csr);
         if (choice < 0)
             choice = tuning_cache_lookup(csr, VK, K);
         if (choice < 0) {
@@ -734,8 +735,64 @@ __global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_
     }
 }
 
+// Double-float product on the SELL-32 copy: lane l of the slice's warp owns
+// row 32 s + l (as spmm_sell_kernel) and keeps its own double-float sums, so
+// no cross-lane combination is needed.
+template<int K>
+__global__ void __launch_bounds__(256) spmm_df_sell_kernel(int64_t nrow, int64_t nslice,
+                                                           const int64_t *__restrict__ off,
+                                                           const int32_t *__restrict__ cols,
+                                                           const float *__restrict__ hi, const float *__restrict__ lo,
+                                                           const float *__restrict__ xs, double *__restrict__ y) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
+        const int64_t o = off[s];
+        const int64_t L = (off[s + 1] - o) >> 5;
+        const int32_t *cp = cols + o + lane;
+        const float *hp = hi + o + lane;
+        const float *lp = lo + o + lane;
+        float sm[K], cm[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            sm[k] = cm[k] = 0.0f;
+        int64_t j = 0;
+        for (; j + 2 <= L; j += 2) {
+            const int32_t c0 = __ldcs(cp + 32 * j), c1 = __ldcs(cp + 32 * (j + 1));
+            const float h0 = __ldcs(hp + 32 * j), h1 = __ldcs(hp + 32 * (j + 1));
+            const float l0 = __ldcs(lp + 32 * j), l1 = __ldcs(lp + 32 * (j + 1));
+            float xh0[K], xl0[K], xh1[K], xl1[K];
+            load_split<K>(xs, c0, xh0, xl0);
+            load_split<K>(xs, c1, xh1, xl1);
+            df_term<K>(h0, l0, xh0, xl0, sm, cm);
+            df_term<K>(h1, l1, xh1, xl1, sm, cm);
+        }
+        if (j < L) {
+            float xh[K], xl[K];
+            load_split<K>(xs, __ldcs(cp + 32 * j), xh, xl);
+            df_term<K>(__ldcs(hp + 32 * j), __ldcs(lp + 32 * j), xh, xl, sm, cm);
+        }
+        const int64_t r = 32 * s + lane;
+        if (r < nrow) {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                y[r * K + k] = static_cast<double>(sm[k]) + static_cast<double>(cm[k]);
+        }
+    }
+}
+
 template<int K>
 void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
+    if (v == kSellVariant && csr->sell_lo) {
+        const int64_t blocks = std::max<int64_t>(
+            1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice * 32 + 255) / 256));
+        spmm_df_sell_kernel<K><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+            csr->nrow, csr->nslice, csr->sell_off, csr->sell_cols, csr->sell_vals, csr->sell_lo, xs, y);
+        ::pyci_gpu::note_launch();
+        return;
+    }
+    if (v == kSellVariant)
+        v = heuristic_variant(csr);
     const int lanes = variant_lanes(v), map = variant_map(v);
     const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;
     const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(max_blocks, (csr->nrow * lanes + 255) / 256));
@@ -781,6 +838,8 @@ int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cuda
         return PYCI_GPU_OK;
     int &choice = csr->tuned[kSplitDF][K];
     if (choice < 0)
+        choice = forced_sell_variant(csr);
+    if (choice < 0)
         choice = tuning_cache_lookup(csr, kSplitDF, K);
     if (choice < 0) {
         if (!autotune_enabled() || csr->nnz < (1 << 20)) {
@@ -803,6 +862,20 @@ int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cuda
                 if (ms < best) {
                     best = ms;
                     best_v = v;
+                }
+            }
+            if (csr->sell_lo) {
+                launch_df(kSellVariant, csr, K, xs, y, st);
+                cudaEventRecord(a, st);
+                launch_df(kSellVariant, csr, K, xs, y, st);
+                launch_df(kSellVariant, csr, K, xs, y, st);
+                cudaEventRecord(b, st);
+                cudaEventSynchronize(b);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (ms < best) {
+                    best = ms;
+                    best_v = kSellVariant;
                 }
             }
             cudaEventDestroy(a);

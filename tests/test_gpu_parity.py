@@ -165,10 +165,10 @@ def test_spmm_precisions_against_oracle(ctx):
 
 
 @pytest.mark.parametrize("kind,n,nu,nd", [("fullci", 8, 4, 4), ("doci", 16, 6, 6), ("fullci", 9, 4, 2)])
-def test_spmm_fp32_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
-    r"""The FP32 product on the SELL-32 copy (pinned with PYCI_GPU_SPMM=sell)
-    and on the CSR kernels (=csr) against the oracle's FP64 product; row
-    counts that leave a partial last slice of 32 rows."""
+def test_spmm_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
+    r"""The FP32 and double-float products on the SELL-32 copy (pinned with
+    PYCI_GPU_SPMM=sell) and on the CSR kernels (=csr) against the oracle's
+    FP64 product; row counts that leave a partial last slice of 32 rows."""
     import torch
     ecore, one, two = synthetic_integrals(n, 1003)
     dets = O.all_dets(OKIND[kind], n, nu, nd)
@@ -188,6 +188,13 @@ def test_spmm_fp32_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
             torch.cuda.synchronize()
             out[("x", k)] = X
             out[(mode, k)] = yf.cpu().numpy().astype(np.float64)
+        for k in (1, 2, 4):
+            X = out[("x", k)]
+            xs = torch.tensor(split_rows(X), device="cuda")
+            yd = torch.empty((N, k), dtype=torch.float64, device="cuda")
+            csr.spmm_device(capi.PREC_FP64_DF, k, xs.data_ptr(), yd.data_ptr(), None)
+            torch.cuda.synchronize()
+            out[(mode, "df", k)] = yd.cpu().numpy()
         csr.free()
     for k in (1, 2, 3, 4, 8, 11):
         X = out[("x", k)].astype(np.float32).astype(np.float64)
@@ -196,6 +203,12 @@ def test_spmm_fp32_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
         for mode in ("sell", "csr"):
             # FP32 values and accumulation: relative error ~ sqrt(row length) * 2^-24
             assert np.abs(out[(mode, k)] - Y_ref).max() / scale < 1e-5, (mode, k)
+    for k in (1, 2, 4):
+        X = out[("x", k)]
+        Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
+        for mode in ("sell", "csr"):
+            # double-float sums: ~2^-44 relative
+            np.testing.assert_allclose(out[(mode, "df", k)], Y_ref, rtol=1e-11, atol=1e-11 * np.abs(Y_ref).max())
 
 
 def split_rows(X):
