@@ -52,12 +52,13 @@ WORKLOADS = {
 }
 WORKLOAD = WORKLOADS["fci12"]
 METRIC = WORKLOAD["metric"]
-# DRAM bytes moved per algorithmic byte by the FP32 k = 4 SpMM, from one ncu
-# capture of the same kernel on the 11-orbital 5a5b operator (2.214 GB moved for
-# 2.162 GB algorithmic; profiles/spmm_fci11_5a5b_ncu_full.md).  Both operators
-# stream the matrix once per launch with the x block in L2, so traffic scales
-# with the entries processed.
-TRAFFIC_PER_ALGORITHMIC_BYTE = 1.024
+# DRAM bytes moved per algorithmic byte by the FP32 k = 4 SpMM (SELL-32 kernel),
+# from one ncu capture of the same kernel on the 11-orbital 5a5b operator
+# (2.1617 GB moved for 2.1621 GB algorithmic;
+# profiles/spmm_sell_fci11_5a5b_ncu_full.md).  Both operators stream the matrix
+# once per launch with the x block in L2, so traffic scales with the entries
+# processed.
+TRAFFIC_PER_ALGORITHMIC_BYTE = 1.000
 TOL = 1.0e-6  # residual <= 1e-6 * |E| (~1e-5 Ha): eigenvalues converge quadratically, well inside 1 uHa
 
 
@@ -379,9 +380,10 @@ def run_ours(args, world, rank, local):
                      "traffic": int(bytes32 * TRAFFIC_PER_ALGORITHMIC_BYTE) if fci else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel on "
                                        "FullCI 11o 5a5b, scaled by entries processed "
-                                       "(profiles/spmm_fci11_5a5b_ncu_full.md)" if fci else None,
+                                       "(profiles/spmm_sell_fci11_5a5b_ncu_full.md)" if fci else None,
                      "peak_source": peak_kind, "peak_note": "of measured" if peak_kind == "measured" else "of fallback",
-                     "kernel": "spmm_kernel<FP32, K=4> (tuned variant)", "algorithmic_bytes": bytes32},
+                     "kernel": "FP32 k=4 SpMM, autotuned: spmm_sell_kernel (SELL-32, 4 or 1 warps per slice) "
+                               "or a CSR spmm_kernel tile", "algorithmic_bytes": bytes32},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_spr, "unit": "s/root", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -584,6 +584,7 @@ private:
     }
     int64_t syncs_ = 0;
     double wait_s_ = 0.0, upload_s_ = 0.0, eig_s_ = 0.0;
+    const bool trace_ = std::getenv("PYCI_GPU_SOLVE_TRACE") != nullptr;
     double *h_small_ = nullptr; // pinned [kMaxGramP * kMaxQ]
     // Host -> device copy of small coefficient blocks through the context's
     // pinned ring (which may wait for a slot's previous copy).
@@ -864,6 +865,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
 
     std::vector<double> G(static_cast<size_t>(mmax) * mmax, 0.0), theta, Y, Gc;
     std::vector<double> rnorm(b, 0.0);
+    // Previous iteration's FP32 residual norms (mixed mode's stall test).
+    std::vector<double> rprev(b, std::numeric_limits<double>::infinity());
     const double eps23 = std::pow(std::numeric_limits<double>::epsilon(), 2.0 / 3.0);
     const double mixed_floor = 1e-5;
     int64_t iter = 0, restarts = 0, refinements = 0;
@@ -916,7 +919,14 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 thr = std::max(thr, mixed_floor);
             if (full_space)
                 thr = std::numeric_limits<double>::infinity();
-            if (!(rnorm[j] <= thr)) {
+            // Mixed mode: a residual within 2x of the threshold that fell by
+            // less than 30 % since the last iteration sits on the FP32
+            // rounding floor of H x (~1e-6 |theta|); more FP32 iterations
+            // cannot lower it, so the root goes to the FP64 refinement, whose
+            // own test decides.
+            const bool stalled = mixed_ && rnorm[j] <= 2.0 * thr && rnorm[j] > 0.7 * rprev[j];
+            rprev[j] = rnorm[j];
+            if (!(rnorm[j] <= thr) && !stalled) {
                 if (j < nw)
                     all = false;
                 todo.push_back(j);
@@ -929,6 +939,13 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         // by streaming the matrix, so a narrower block saves little (2
         // vectors cost ~3/4 of 4) and the extra directions keep improving the
         // converged roots.  (The FP64 product's cost grows with the width.)
+        if (trace_) {
+            double rmax = 0.0;
+            for (int j = 0; j < nw; ++j)
+                rmax = std::max(rmax, rnorm[j]);
+            std::fprintf(stderr, "  iter %lld m %d max_res(wanted) %.3e unconverged %d\n", static_cast<long long>(iter), m,
+                         rmax, static_cast<int>(todo.size()));
+        }
         if (static_cast<int>(todo.size()) > nw)
             todo.resize(nw);
         if (mixed_ && !all && !full_space && static_cast<int>(todo.size()) < nw) {
@@ -1023,6 +1040,9 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                     todo.push_back(j);
                 }
             }
+            if (trace_)
+                std::fprintf(stderr, "  refinement %lld max_res64 %.3e %s\n", static_cast<long long>(refinements), max_res,
+                             ok64 ? "converged" : "continue");
             if (ok64 || refinements >= 8) {
                 converged = ok64;
                 final_theta = th64;
@@ -1125,7 +1145,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     }
     // PYCI_GPU_SOLVE_TRACE: one line per solve on stderr with the host-side
     // breakdown (blocked in read-backs, coefficient uploads, Rayleigh-Ritz).
-    if (std::getenv("PYCI_GPU_SOLVE_TRACE"))
+    if (trace_)
         std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), upload %.3f ms, eig %.3f ms, iters %lld\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() * 1e3,
                      timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), upload_s_ * 1e3, eig_s_ * 1e3,

@@ -263,80 +263,140 @@ __global__ void __launch_bounds__(256) spmm_cb_kernel(int64_t nrow, const int64_
     }
 }
 
-// FP32 product on the SELL-32 copy: one warp per slice of 32 rows, lane l
-// owns row 32 s + l and walks it in lockstep with the warp (entry j of all 32
-// rows is one coalesced 128-byte load of columns and one of values).  The
-// slice's rows share their column blocks of x (consecutive FCI / DOCI rows
-// differ in the low orbitals), so a warp's 32 gathers touch far fewer cache
-// lines than the 32 gathers of one CSR row.  Each lane sums its row in order;
-// no reduction across lanes.
-template<int K, bool VEC>
+// FP32 product on the SELL-32 copy.  A block of 8 warps takes 8 / SPLIT
+// slices of 32 rows; the SPLIT warps of a slice split its entries into
+// SPLIT consecutive ranges, and lane l of each walks row 32 s + l over its
+// range (entry j of the 32 rows is one coalesced 128-byte load of columns
+// and one of values).
+// The slice's rows share their column blocks of x (consecutive FCI / DOCI
+// rows differ in the low orbitals), so a warp's 32 gathers touch far fewer
+// cache lines than the 32 gathers of one CSR row.  The next U entries'
+// columns and values are loaded before the current U are gathered, so the
+// matrix stream and the gathers overlap within a warp.  The SPLIT partial
+// sums of a row are added in a fixed order through shared memory
+// (deterministic).  SPLIT = 4 keeps the last wave of blocks short when x
+// fits in L2; SPLIT = 1 keeps a slice's gathers close together in time,
+// which matters when x does not fit (the autotuner picks).
+template<int K, bool VEC, int SPLIT>
 __global__ void __launch_bounds__(256) spmm_sell_kernel(int64_t nrow, int64_t nslice, const int64_t *__restrict__ off,
                                                         const int32_t *__restrict__ cols,
                                                         const float *__restrict__ vals, const float *__restrict__ x,
                                                         int64_t ldx, float *__restrict__ y, int64_t ldy) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
-        const int64_t o = off[s];
-        const int64_t L = (off[s + 1] - o) >> 5;
-        const int32_t *cp = cols + o + lane;
-        const float *vp = vals + o + lane;
+    constexpr int U = 4;
+    __shared__ float part[8][K][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int kPer = 8 / SPLIT; // slices per block step
+    const int q = warp % SPLIT;
+    for (int64_t grp = blockIdx.x; kPer * grp < nslice; grp += gridDim.x) {
+        const int64_t s = kPer * grp + warp / SPLIT;
         float acc[K];
 #pragma unroll
         for (int k = 0; k < K; ++k)
             acc[k] = 0.0f;
-        float xv[K];
-        int64_t j = 0;
-        for (; j + 4 <= L; j += 4) {
-            int32_t c[4];
-            float v[4];
+        if (s < nslice) {
+            const int64_t o = off[s];
+            const int64_t L = (off[s + 1] - o) >> 5;
+            const int64_t Lq = (L + SPLIT - 1) / SPLIT;
+            const int64_t j0 = min(L, q * Lq), j1 = min(L, j0 + Lq);
+            const int32_t *cp = cols + o + lane;
+            const float *vp = vals + o + lane;
+            float xv[K];
+            int64_t j = j0;
+            if (j + U <= j1) {
+                int32_t c[U];
+                float v[U];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                c[u] = __ldcs(cp + 32 * (j + u));
-                v[u] = __ldcs(vp + 32 * (j + u));
+                for (int u = 0; u < U; ++u) {
+                    c[u] = __ldcs(cp + 32 * (j + u));
+                    v[u] = __ldcs(vp + 32 * (j + u));
+                }
+                for (; j + 2 * U <= j1; j += U) {
+                    int32_t cn[U];
+                    float vn[U];
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        cn[u] = __ldcs(cp + 32 * (j + U + u));
+                        vn[u] = __ldcs(vp + 32 * (j + U + u));
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        load_x<VEC, K>(x + static_cast<int64_t>(c[u]) * ldx, xv);
+#pragma unroll
+                        for (int k = 0; k < K; ++k)
+                            acc[k] += v[u] * xv[k];
+                    }
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        c[u] = cn[u];
+                        v[u] = vn[u];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    load_x<VEC, K>(x + static_cast<int64_t>(c[u]) * ldx, xv);
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        acc[k] += v[u] * xv[k];
+                }
+                j += U;
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                load_x<VEC, K>(x + static_cast<int64_t>(c[u]) * ldx, xv);
+            for (; j < j1; ++j) {
+                const int32_t c = __ldcs(cp + 32 * j);
+                const float v = __ldcs(vp + 32 * j);
+                load_x<VEC, K>(x + static_cast<int64_t>(c) * ldx, xv);
 #pragma unroll
                 for (int k = 0; k < K; ++k)
-                    acc[k] += v[u] * xv[k];
+                    acc[k] += v * xv[k];
             }
         }
-        for (; j < L; ++j) {
-            const int32_t c = __ldcs(cp + 32 * j);
-            const float v = __ldcs(vp + 32 * j);
-            load_x<VEC, K>(x + static_cast<int64_t>(c) * ldx, xv);
 #pragma unroll
-            for (int k = 0; k < K; ++k)
-                acc[k] += v * xv[k];
-        }
-        const int64_t r = 32 * s + lane;
-        if (r < nrow) {
+        for (int k = 0; k < K; ++k)
+            part[warp][k][lane] = acc[k];
+        __syncthreads();
+        if (q == 0 && s < nslice) {
+            const int64_t r = 32 * s + lane;
+            if (r < nrow) {
 #pragma unroll
-            for (int k = 0; k < K; ++k)
-                y[r * ldy + k] = acc[k];
+                for (int k = 0; k < K; ++k) {
+                    float t = part[warp][k][lane];
+#pragma unroll
+                    for (int w = 1; w < SPLIT; ++w)
+                        t += part[warp + w][k][lane];
+                    y[r * ldy + k] = t;
+                }
+            }
         }
+        __syncthreads();
     }
 }
 
-template<int K>
-void launch_sell(const pyci_gpu_csr *csr, const void *x, int64_t ldx, void *y, int64_t ldy, cudaStream_t st) {
+template<int K, int SPLIT>
+void launch_sell_split(const pyci_gpu_csr *csr, const void *x, int64_t ldx, void *y, int64_t ldy, cudaStream_t st) {
+    constexpr int kPer = 8 / SPLIT;
     const int64_t blocks = std::max<int64_t>(
-        1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice * 32 + 255) / 256));
+        1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice + kPer - 1) / kPer));
     const size_t rowbytes = static_cast<size_t>(ldx) * sizeof(float);
     const size_t vbytes = (K * sizeof(float)) % 16 == 0 ? 16 : ((K * sizeof(float)) == 8 ? 8 : 0);
     const bool vec = vbytes && (reinterpret_cast<uintptr_t>(x) % vbytes == 0) && (rowbytes % vbytes == 0);
     if (vec)
-        spmm_sell_kernel<K, true><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+        spmm_sell_kernel<K, true, SPLIT><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
             csr->nrow, csr->nslice, csr->sell_off, csr->sell_cols, csr->sell_vals, static_cast<const float *>(x), ldx,
             static_cast<float *>(y), ldy);
     else
-        spmm_sell_kernel<K, false><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
+        spmm_sell_kernel<K, false, SPLIT><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
             csr->nrow, csr->nslice, csr->sell_off, csr->sell_cols, csr->sell_vals, static_cast<const float *>(x), ldx,
             static_cast<float *>(y), ldy);
     ::pyci_gpu::note_launch();
+}
+
+// sub 0: 4 warps per slice; sub 1: one warp per slice.
+template<int K>
+void launch_sell(int sub, const pyci_gpu_csr *csr, const void *x, int64_t ldx, void *y, int64_t ldy,
+                 cudaStream_t st) {
+    if (sub == 1)
+        launch_sell_split<K, 1>(csr, x, ldx, y, ldy, st);
+    else
+        launch_sell_split<K, 4>(csr, x, ldx, y, ldy, st);
 }
 
 template<int VK, int K, int LANES>
@@ -387,7 +447,7 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
 // Tile variants: lanes per row (8, 16, 32) x entry mapping (0, 1); and, for
 // the FP32 values of an operator that has one, the SELL-32 copy.
 constexpr int kVariants = 6;
-constexpr int kSellVariant = 0x100;
+constexpr int kSellVariant = 0x100; // FP32: + 0 (4 warps per slice) or + 1 (one warp)
 inline int variant_lanes(int v) { return v % 3 == 0 ? 8 : (v % 3 == 1 ? 16 : 32); }
 inline int variant_map(int v) { return v / 3; }
 
@@ -396,10 +456,10 @@ inline int heuristic_variant(const pyci_gpu_csr *csr);
 template<int VK, int K>
 void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                     int64_t ldy, cudaStream_t st) {
-    if (v == kSellVariant) {
+    if (v == kSellVariant || v == kSellVariant + 1) {
         if constexpr (VK == kF32) {
             if (csr->sell_cols) {
-                launch_sell<K>(csr, x, ldx, y, ldy, st);
+                launch_sell<K>(v - kSellVariant, csr, x, ldx, y, ldy, st);
                 return;
             }
         }
@@ -482,16 +542,18 @@ bool autotune_enabled() {
     return on;
 }
 
-// PYCI_GPU_SPMM=sell or =csr pins the FP32 and double-float products of
-// operators built after it is set to the SELL-32 copy or to the CSR
-// heuristic (read when an operator makes its first product of a kind, so a
-// process can compare the two).
+// PYCI_GPU_SPMM=sell, =sell1 or =csr pins the FP32 and double-float
+// products of operators built after it is set to the SELL-32 copy (FP32: 4
+// warps or one warp per slice) or to the CSR heuristic (read when an
+// operator makes its first product of a kind, so a process can compare them).
 int forced_sell_variant(const pyci_gpu_csr *csr) {
     const char *e = std::getenv("PYCI_GPU_SPMM");
     if (!e)
         return -1;
     if (!std::strcmp(e, "sell"))
         return csr->sell_cols ? kSellVariant : heuristic_variant(csr);
+    if (!std::strcmp(e, "sell1"))
+        return csr->sell_cols ? kSellVariant + 1 : heuristic_variant(csr);
     if (!std::strcmp(e, "csr"))
         return heuristic_variant(csr);
     return -1;
@@ -538,19 +600,19 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
                     }
                 }
                 const int best_csr = best_v;
-                // The SELL-32 copy (FP32 values only).
-                if (VK == kF32 && csr->sell_cols) {
-                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
+                // The SELL-32 copy (FP32 values only), both splits.
+                for (int sv = kSellVariant; VK == kF32 && csr->sell_cols && sv <= kSellVariant + 1; ++sv) {
+                    launch_k<VK>(sv, csr, vals, K, xs, k, ys, k, st);
                     cudaEventRecord(a, st);
-                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
-                    launch_k<VK>(kSellVariant, csr, vals, K, xs, k, ys, k, st);
+                    launch_k<VK>(sv, csr, vals, K, xs, k, ys, k, st);
+                    launch_k<VK>(sv, csr, vals, K, xs, k, ys, k, st);
                     cudaEventRecord(b, st);
                     cudaEventSynchronize(b);
                     float ms = 0.0f;
                     cudaEventElapsedTime(&ms, a, b);
                     if (ms < best) {
                         best = ms;
-                        best_v = kSellVariant;
+                        best_v = sv;
                     }
                 }
                 // Column blocks when the gathered block of vectors is larger
@@ -736,7 +798,7 @@ __global__ void __launch_bounds__(256) spmm_df_kernel(int64_t nrow, const int64_
 }
 
 // Double-float product on the SELL-32 copy: lane l of the slice's warp owns
-// row 32 s + l (as spmm_sell_kernel) and keeps its own double-float sums, so
+// row 32 s + l over the whole row and keeps its own double-float sums, so
 // no cross-lane combination is needed.
 template<int K>
 __global__ void __launch_bounds__(256) spmm_df_sell_kernel(int64_t nrow, int64_t nslice,
@@ -783,7 +845,7 @@ __global__ void __launch_bounds__(256) spmm_df_sell_kernel(int64_t nrow, int64_t
 
 template<int K>
 void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
-    if (v == kSellVariant && csr->sell_lo) {
+    if (v >= kSellVariant && csr->sell_lo) {
         const int64_t blocks = std::max<int64_t>(
             1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice * 32 + 255) / 256));
         spmm_df_sell_kernel<K><<<static_cast<unsigned>(blocks), 256, 0, st>>>(
@@ -791,7 +853,7 @@ void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *
         ::pyci_gpu::note_launch();
         return;
     }
-    if (v == kSellVariant)
+    if (v >= kSellVariant)
         v = heuristic_variant(csr);
     const int lanes = variant_lanes(v), map = variant_map(v);
     const int64_t max_blocks = static_cast<int64_t>(csr->ctx->num_sms) * 8 * 4;

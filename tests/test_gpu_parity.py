@@ -167,8 +167,9 @@ def test_spmm_precisions_against_oracle(ctx):
 @pytest.mark.parametrize("kind,n,nu,nd", [("fullci", 8, 4, 4), ("doci", 16, 6, 6), ("fullci", 9, 4, 2)])
 def test_spmm_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
     r"""The FP32 and double-float products on the SELL-32 copy (pinned with
-    PYCI_GPU_SPMM=sell) and on the CSR kernels (=csr) against the oracle's
-    FP64 product; row counts that leave a partial last slice of 32 rows."""
+    PYCI_GPU_SPMM=sell or =sell1) and on the CSR kernels (=csr) against the
+    oracle's FP64 product; row counts that leave a partial last slice of 32
+    rows."""
     import torch
     ecore, one, two = synthetic_integrals(n, 1003)
     dets = O.all_dets(OKIND[kind], n, nu, nd)
@@ -176,7 +177,7 @@ def test_spmm_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
     N = dets.shape[0]
     rng = np.random.default_rng(8)
     out = {}
-    for mode in ("sell", "csr"):
+    for mode in ("sell", "sell1", "csr"):
         monkeypatch.setenv("PYCI_GPU_SPMM", mode)
         csr = capi.Csr(ctx, WFN[kind], n, nu, nd, dets, one, two, flags=capi.BUILD_FULL_COLEX)
         csr.prepare_mixed(drop_fp64=True)
@@ -200,13 +201,13 @@ def test_spmm_sell_against_oracle(ctx, monkeypatch, kind, n, nu, nd):
         X = out[("x", k)].astype(np.float32).astype(np.float64)
         Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
         scale = np.abs(Y_ref).max()
-        for mode in ("sell", "csr"):
+        for mode in ("sell", "sell1", "csr"):
             # FP32 values and accumulation: relative error ~ sqrt(row length) * 2^-24
             assert np.abs(out[(mode, k)] - Y_ref).max() / scale < 1e-5, (mode, k)
     for k in (1, 2, 4):
         X = out[("x", k)]
         Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(k)], axis=1)
-        for mode in ("sell", "csr"):
+        for mode in ("sell", "sell1", "csr"):
             # double-float sums: ~2^-44 relative
             np.testing.assert_allclose(out[(mode, "df", k)], Y_ref, rtol=1e-11, atol=1e-11 * np.abs(Y_ref).max())
 
