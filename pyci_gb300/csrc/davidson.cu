@@ -169,15 +169,20 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
     }
     __shared__ double red[8][PI * QC];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Warp sums in T (FP32 for FP32 vectors: this GPU's FP64 add rate is a
+    // small fraction of its FP32 rate, and 5 levels of FP64 adds on every
+    // accumulator cost as much as the row pass of a short product); FP64
+    // from the cross-warp sum on.
 #pragma unroll
     for (int ii = 0; ii < PI; ++ii)
 #pragma unroll
         for (int j = 0; j < QC; ++j) {
-            double v = static_cast<double>(acc[ii][j]);
+            T v = acc[ii][j];
+#pragma unroll
             for (int o = 16; o > 0; o >>= 1)
                 v += __shfl_xor_sync(0xffffffffu, v, o);
             if (lane == 0)
-                red[warp][ii * QC + j] = v;
+                red[warp][ii * QC + j] = static_cast<double>(v);
         }
     __syncthreads();
     const int nwarps = blockDim.x >> 5;
@@ -280,6 +285,9 @@ __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, 
 #pragma unroll
             for (int t = 0; t < R; ++t)
                 acc[j][t] = 0;
+        // Unrolled so several vectors' loads are in flight per thread (a
+        // thread often handles a single row step).
+#pragma unroll 8
         for (int i = 0; i < p; ++i) {
             TV v[R];
             load_rows<TV, R>(V + i * N + r, v);
@@ -344,24 +352,41 @@ __global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ 
     }
 }
 
-// out[j] = R[j] / (theta[j] - D) with |theta - D| floored at 1e-8 (Davidson's
-// diagonal preconditioner).  FP32 output: the quotient is taken in FP32.
+// Residual columns to precondition (at most kMaxQ), passed by value.
+struct Cols {
+    int n;
+    int src[kMaxQ];
+};
+
+// out[c] = R[j] / (theta[j] - D) for j = cols.src[c], with |theta - D|
+// floored at 1e-8 (Davidson's diagonal preconditioner); one launch for the
+// whole block of corrections.  FP32 output: the quotient is taken in FP32.
 template<typename TI, typename TO>
 __global__ void precondition_kernel(const TI *__restrict__ R, const double *__restrict__ theta,
-                                    const double *__restrict__ diag, int q, int64_t N, TO *__restrict__ out) {
+                                    const double *__restrict__ diag, Cols cols, int64_t N, TO *__restrict__ out) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const double d = diag[r];
-        for (int j = 0; j < q; ++j) {
+        for (int c = 0; c < cols.n; ++c) {
+            const int j = cols.src[c];
             double den = theta[j] - d;
             if (fabs(den) < 1e-8)
                 den = (den < 0.0) ? -1e-8 : 1e-8;
             if constexpr (sizeof(TO) == 4)
-                out[j * N + r] = static_cast<float>(R[j * N + r]) / static_cast<float>(den);
+                out[c * N + r] = static_cast<float>(R[j * N + r]) / static_cast<float>(den);
             else
-                out[j * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
+                out[c * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
         }
     }
+}
+
+// Columns todo[c0 .. c0 + kMaxQ) of a correction list.
+inline Cols make_cols(const std::vector<int> &todo, size_t c0) {
+    Cols c{};
+    c.n = static_cast<int>(std::min<size_t>(kMaxQ, todo.size() - c0));
+    for (int i = 0; i < c.n; ++i)
+        c.src[i] = todo[c0 + i];
+    return c;
 }
 
 template<typename T>
@@ -539,6 +564,28 @@ private:
             matvecs_ += kk;
         }
         return PYCI_GPU_OK;
+    }
+
+    // R[j] = AX[j] - theta[j] X[j] for j < q (theta in d_theta_), in
+    // launches of at most kMaxQ columns.
+    template<typename U>
+    void residuals(const U *AX, const U *X, int q, U *R) {
+        for (int j0 = 0; j0 < q; j0 += kMaxQ) {
+            const int64_t o = static_cast<int64_t>(j0) * N_;
+            residual_kernel<U><<<grid(N_), 256, 0, st_>>>(AX + o, X + o, d_theta_ + j0, std::min(kMaxQ, q - j0), N_,
+                                                          R + o),
+                ::pyci_gpu::note_launch();
+        }
+    }
+
+    // out[c] = preconditioned R[todo[c]] (theta in d_theta_), in launches of
+    // at most kMaxQ columns.
+    template<typename U>
+    void precondition(const U *R, const double *diag, const std::vector<int> &todo, T *out) {
+        for (size_t c0 = 0; c0 < todo.size(); c0 += kMaxQ)
+            precondition_kernel<U, T><<<grid(N_), 256, 0, st_>>>(R, d_theta_, diag, make_cols(todo, c0), N_,
+                                                                  out + static_cast<int64_t>(c0) * N_),
+                ::pyci_gpu::note_launch();
     }
 
     // Orthonormalise vectors V[m..m+k) against V[0..m) and each other;
@@ -907,7 +954,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             return rc;
         if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
             return rc;
-        residual_kernel<T><<<grid(N), 256, 0, st_>>>(AXr, Xr, d_theta_, b, N, R), ::pyci_gpu::note_launch();
+        residuals<T>(AXr, Xr, b, R);
         bool all = true;
         std::vector<int> todo;
         if ((rc = gram<T>(R, b, R, b, Gc)))
@@ -1025,7 +1072,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
             if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
                 return rc;
-            residual_kernel<double><<<grid(N), 256, 0, st_>>>(AX64, X64, d_theta_, br, N, R64), ::pyci_gpu::note_launch();
+            residuals<double>(AX64, X64, br, R64);
             bool ok64 = true;
             todo.clear();
             max_res = 0.0;
@@ -1062,12 +1109,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             }
             if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
                 return rc;
-            int q = 0;
-            for (int j : todo) {
-                precondition_kernel<double, T><<<grid(N), 256, 0, st_>>>(R64 + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
-                                                                        V + static_cast<int64_t>(m + q) * N), ::pyci_gpu::note_launch();
-                ++q;
-            }
+            const int q = static_cast<int>(todo.size());
+            precondition<double>(R64, d_diag, todo, V + static_cast<int64_t>(m) * N);
             if ((rc = orthonormalize(V, m, q, knew)))
                 return rc;
             continue;
@@ -1098,12 +1141,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         // Preconditioned residuals of the unconverged roots.
         if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
             return rc;
-        int q = 0;
-        for (int j : todo) {
-            precondition_kernel<T, T><<<grid(N), 256, 0, st_>>>(R + static_cast<int64_t>(j) * N, d_theta_ + j, d_diag, 1, N,
-                                                               V + static_cast<int64_t>(m + q) * N), ::pyci_gpu::note_launch();
-            ++q;
-        }
+        const int q = static_cast<int>(todo.size());
+        precondition<T>(R, d_diag, todo, V + static_cast<int64_t>(m) * N);
         if ((rc = orthonormalize(V, m, q, knew)))
             return rc;
         if (knew == 0) {

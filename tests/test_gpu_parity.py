@@ -123,6 +123,28 @@ def test_workload_digest_and_eigenvalues(ctx, golden, name):
     csr.free()
 
 
+@pytest.mark.parametrize("nroot", [9, 12])
+def test_many_roots_against_dense_eigenvalues(ctx, nroot):
+    r"""More wanted roots than one launch's column limit (8): residuals,
+    preconditioned corrections and products run in several launches per
+    block.  FullCI 7o 3a3b (1,225 determinants) against numpy's dense
+    eigenvalues, both precision modes."""
+    ecore, one, two = synthetic_integrals(7, 1005)
+    dets = O.all_dets(O.FULLCI, 7, 3, 3)
+    ref = O.build_csr(O.FULLCI, 7, 3, 3, dets, one, two)
+    N = dets.shape[0]
+    H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
+    exact = np.linalg.eigvalsh(0.5 * (H + H.T))[:nroot]
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, 7, 3, 3, dets, one, two, flags=capi.BUILD_FULL_COLEX)
+    for mode in (capi.SOLVE_FP64, capi.SOLVE_MIXED):
+        evals, evecs, st = csr.solve(n=nroot, tol=1e-8 if mode == capi.SOLVE_FP64 else 1e-6, mode=mode)
+        err = np.abs(np.sort(evals) - exact)
+        assert err.max() < 1e-6, (mode, err)
+        for k in range(nroot):
+            assert np.linalg.norm(evecs[k]) == pytest.approx(1.0, abs=1e-6)
+    csr.free()
+
+
 @pytest.mark.parametrize("kat", [0, 1, 2, 3])
 def test_known_answer_energies(ctx, golden, kat):
     # pyci/test/test_routines.py:37-54 with the reference's solve(n=1, ncv=30, tol=1e-6).
