@@ -143,32 +143,65 @@ __global__ void sell_sizes_kernel(int64_t nrow, const int64_t *__restrict__ rowp
     }
 }
 
-// One warp per slice: lane l copies row 32 s + l's columns and FP32 value
-// halves to positions off[s] + 32 j + l; past the row's end it repeats the
-// row's last column with zero values (a valid column near the lane's others).
-__global__ void sell_fill_kernel(int64_t nrow, const int64_t *__restrict__ rowptr, const int32_t *__restrict__ cols,
-                                 const float *__restrict__ hi, const float *__restrict__ lo, int64_t nslice,
-                                 const int64_t *__restrict__ off, int32_t *__restrict__ scols,
-                                 float *__restrict__ svals, float *__restrict__ slo) {
-    const int lane = threadIdx.x & 31;
+// One warp per slice, in chunks of 32 entries: the warp loads entries
+// j .. j + 31 of each of the slice's 32 rows (one coalesced 128-byte load per
+// row and array) into a shared-memory tile, then writes position j' of all 32
+// rows as one coalesced 128-byte store (off[s] + 32 j' + l for row 32 s + l),
+// for the columns and both FP32 value halves.  Past a row's end the row's
+// last column is repeated with zero values (a valid column near the lane's
+// others); rows past nrow use column 0.
+__global__ void __launch_bounds__(256) sell_fill_kernel(int64_t nrow, const int64_t *__restrict__ rowptr,
+                                                        const int32_t *__restrict__ cols,
+                                                        const float *__restrict__ hi, const float *__restrict__ lo,
+                                                        int64_t nslice, const int64_t *__restrict__ off,
+                                                        int32_t *__restrict__ scols, float *__restrict__ svals,
+                                                        float *__restrict__ slo) {
+    __shared__ uint32_t tile[8][32][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; s < nslice; s += nwarps) {
         const int64_t r = 32 * s + lane;
-        const int64_t start = r < nrow ? rowptr[r] : 0, len = r < nrow ? rowptr[r + 1] - start : 0;
+        const int64_t start = r < nrow ? rowptr[r] : 0;
+        const int64_t len = r < nrow ? rowptr[r + 1] - start : 0;
+        const int32_t last = len > 0 ? cols[start + len - 1] : 0;
         const int64_t o = off[s], L = (off[s + 1] - o) >> 5;
-        int32_t last = len > 0 ? cols[start] : 0;
-        for (int64_t j = 0; j < L; ++j) {
-            int32_t c = last;
-            float v = 0.0f, w = 0.0f;
-            if (j < len) {
-                c = __ldg(cols + start + j);
-                v = __ldg(hi + start + j);
-                w = __ldg(lo + start + j);
-                last = c;
+        for (int64_t j = 0; j < L; j += 32) {
+            for (int a = 0; a < 3; ++a) {
+                // 8 rows' loads in flight before their shared-memory stores.
+                for (int r8 = 0; r8 < 32; r8 += 8) {
+                    uint32_t v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int rr = r8 + u;
+                        const int64_t st = __shfl_sync(0xffffffffu, start, rr);
+                        const int64_t ln = __shfl_sync(0xffffffffu, len, rr);
+                        const int32_t lc = __shfl_sync(0xffffffffu, last, rr);
+                        const int64_t e = j + lane;
+                        if (a == 0)
+                            v[u] = static_cast<uint32_t>(e < ln ? __ldcs(cols + st + e) : lc);
+                        else if (a == 1)
+                            v[u] = e < ln ? __float_as_uint(__ldcs(hi + st + e)) : 0u;
+                        else
+                            v[u] = e < ln ? __float_as_uint(__ldcs(lo + st + e)) : 0u;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        tile[warp][r8 + u][lane] = v[u];
+                }
+                __syncwarp();
+                const int64_t n = (L - j < 32) ? (L - j) : 32;
+                for (int jj = 0; jj < n; ++jj) {
+                    const uint32_t v = tile[warp][lane][jj];
+                    const int64_t at = o + 32 * (j + jj) + lane;
+                    if (a == 0)
+                        scols[at] = static_cast<int32_t>(v);
+                    else if (a == 1)
+                        svals[at] = __uint_as_float(v);
+                    else
+                        slo[at] = __uint_as_float(v);
+                }
+                __syncwarp();
             }
-            scols[o + 32 * j + lane] = c;
-            svals[o + 32 * j + lane] = v;
-            slo[o + 32 * j + lane] = w;
         }
     }
 }
