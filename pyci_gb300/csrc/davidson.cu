@@ -263,18 +263,24 @@ __global__ void reduce_partials_kernel(const double *__restrict__ partial, int n
     }
 }
 
+// Coefficients of one combination launch (p x q <= kMaxGramP x kMaxQ,
+// row-major), passed as a kernel parameter: no host -> device copy in the
+// stream between the kernels (4 KB for FP32, 8 KB for FP64 accumulation).
+template<typename ACC>
+struct CoefBlock {
+    ACC y[kMaxGramP * kMaxQ];
+};
+
 // out[j][r] = beta * out[j][r] + sum_{i < p} Y[i * q + j] * V[i][r]
 // (accumulated in ACC; q <= kMaxQ).  R > 1: R consecutive rows per thread
 // step with 16-byte loads and stores (N a multiple of R, 16-byte aligned
-// vectors); R = 1 otherwise.
+// vectors); R = 1 otherwise.  Y is read from the parameter bank with
+// warp-uniform indices (broadcast).
 template<typename TV, typename TO, typename ACC, int R>
 __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, int p, int64_t N,
-                                                      const double *__restrict__ Y, int q,
+                                                      const __grid_constant__ CoefBlock<ACC> Y, int q,
                                                       double beta, TO *__restrict__ out) {
-    __shared__ ACC sy[kMaxGramP * kMaxQ];
-    for (int e = threadIdx.x; e < p * q; e += blockDim.x)
-        sy[e] = static_cast<ACC>(Y[e]);
-    __syncthreads();
+    const ACC *sy = Y.y;
     const int64_t nu = N / R;
     for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
          u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -325,9 +331,15 @@ __global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, 
 // theta_hi + theta_lo (both FP32) and applied with two FMAs, so the result
 // carries the FP32 rounding of AX and X only, with no FP64 arithmetic (which
 // is scarce on this GPU).
+// Ritz values of one launch (at most kMaxQ), passed as a kernel parameter.
+struct Theta {
+    double t[kMaxQ];
+};
+
 template<typename T>
-__global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const double *__restrict__ theta,
+__global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ X, const __grid_constant__ Theta th,
                                 int q, int64_t N, T *__restrict__ R) {
+    const double *theta = th.t;
     if constexpr (sizeof(T) == 4) {
         float th_hi[kMaxQ], th_lo[kMaxQ];
 #pragma unroll
@@ -352,24 +364,26 @@ __global__ void residual_kernel(const T *__restrict__ AX, const T *__restrict__ 
     }
 }
 
-// Residual columns to precondition (at most kMaxQ), passed by value.
+// Residual columns to precondition (at most kMaxQ) with their Ritz values,
+// passed by value.
 struct Cols {
     int n;
     int src[kMaxQ];
+    double theta[kMaxQ];
 };
 
 // out[c] = R[j] / (theta[j] - D) for j = cols.src[c], with |theta - D|
 // floored at 1e-8 (Davidson's diagonal preconditioner); one launch for the
 // whole block of corrections.  FP32 output: the quotient is taken in FP32.
 template<typename TI, typename TO>
-__global__ void precondition_kernel(const TI *__restrict__ R, const double *__restrict__ theta,
-                                    const double *__restrict__ diag, Cols cols, int64_t N, TO *__restrict__ out) {
+__global__ void precondition_kernel(const TI *__restrict__ R, const double *__restrict__ diag,
+                                    const __grid_constant__ Cols cols, int64_t N, TO *__restrict__ out) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const double d = diag[r];
         for (int c = 0; c < cols.n; ++c) {
             const int j = cols.src[c];
-            double den = theta[j] - d;
+            double den = cols.theta[c] - d;
             if (fabs(den) < 1e-8)
                 den = (den < 0.0) ? -1e-8 : 1e-8;
             if constexpr (sizeof(TO) == 4)
@@ -380,12 +394,14 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
     }
 }
 
-// Columns todo[c0 .. c0 + kMaxQ) of a correction list.
-inline Cols make_cols(const std::vector<int> &todo, size_t c0) {
+// Columns todo[c0 .. c0 + kMaxQ) of a correction list, with their Ritz values.
+inline Cols make_cols(const std::vector<int> &todo, size_t c0, const std::vector<double> &theta) {
     Cols c{};
     c.n = static_cast<int>(std::min<size_t>(kMaxQ, todo.size() - c0));
-    for (int i = 0; i < c.n; ++i)
+    for (int i = 0; i < c.n; ++i) {
         c.src[i] = todo[c0 + i];
+        c.theta[i] = theta[todo[c0 + i]];
+    }
     return c;
 }
 
@@ -490,13 +506,18 @@ private:
                     nb = launch_gram_rows<U>(gram_blocks_, st_, Ai, pp, Bj, qq, N_, d_partial_);
                     ::pyci_gpu::note_launch();
                 }
-                reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq, d_small_), ::pyci_gpu::note_launch();
-                // Read back through the pinned buffer: one DMA, then one
-                // synchronisation (a pageable copy would block inside the
-                // copy call instead).
+                // Sums straight into the mapped pinned buffer when the
+                // device can write host memory (no copy in the stream).
+                reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq,
+                                                                 d_mapped_ ? d_mapped_ : d_small_),
+                    ::pyci_gpu::note_launch();
+                // Otherwise read back through the pinned buffer: one DMA,
+                // then one synchronisation (a pageable copy would block
+                // inside the copy call instead).
                 const auto t0 = std::chrono::steady_clock::now();
-                cudaError_t e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pp * qq,
-                                                cudaMemcpyDeviceToHost, st_);
+                cudaError_t e = cudaSuccess;
+                if (!d_mapped_)
+                    e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pp * qq, cudaMemcpyDeviceToHost, st_);
                 if (e != cudaSuccess)
                     return cuda_status(e, "gram copy");
                 e = cudaStreamSynchronize(st_);
@@ -527,22 +548,19 @@ private:
             const int qq = std::min(kMaxQ, q - j0);
             for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
                 const int pp = std::min(kMaxGramP, p - i0);
-                std::vector<double> sub(static_cast<size_t>(pp) * qq);
+                CoefBlock<ACC> sub;
                 for (int i = 0; i < pp; ++i)
                     for (int j = 0; j < qq; ++j)
-                        sub[static_cast<size_t>(i) * qq + j] = Y[static_cast<size_t>(i0 + i) * q + j0 + j];
-                const int rc = upload(d_coef_, sub.data(), sizeof(double) * sub.size(), st_);
-                if (rc)
-                    return rc;
+                        sub.y[i * qq + j] = static_cast<ACC>(Y[static_cast<size_t>(i0 + i) * q + j0 + j]);
                 const TV *Vi = V + static_cast<int64_t>(i0) * N_;
                 TO *Oj = out + static_cast<int64_t>(j0) * N_;
                 const double bt = (i0 == 0) ? beta : 1.0;
                 constexpr int R = 16 / sizeof(TV);
                 if (N_ % R == 0 && reinterpret_cast<uintptr_t>(Vi) % 16 == 0 &&
                     reinterpret_cast<uintptr_t>(Oj) % 16 == 0)
-                    combine_kernel<TV, TO, ACC, R><<<grid(N_ / R), 256, 0, st_>>>(Vi, pp, N_, d_coef_, qq, bt, Oj);
+                    combine_kernel<TV, TO, ACC, R><<<grid(N_ / R), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
                 else
-                    combine_kernel<TV, TO, ACC, 1><<<grid(N_), 256, 0, st_>>>(Vi, pp, N_, d_coef_, qq, bt, Oj);
+                    combine_kernel<TV, TO, ACC, 1><<<grid(N_), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
                 ::pyci_gpu::note_launch();
             }
         }
@@ -566,24 +584,27 @@ private:
         return PYCI_GPU_OK;
     }
 
-    // R[j] = AX[j] - theta[j] X[j] for j < q (theta in d_theta_), in
-    // launches of at most kMaxQ columns.
+    // R[j] = AX[j] - theta[j] X[j] for j < q, in launches of at most kMaxQ
+    // columns.
     template<typename U>
-    void residuals(const U *AX, const U *X, int q, U *R) {
+    void residuals(const U *AX, const U *X, int q, const std::vector<double> &theta, U *R) {
         for (int j0 = 0; j0 < q; j0 += kMaxQ) {
             const int64_t o = static_cast<int64_t>(j0) * N_;
-            residual_kernel<U><<<grid(N_), 256, 0, st_>>>(AX + o, X + o, d_theta_ + j0, std::min(kMaxQ, q - j0), N_,
-                                                          R + o),
-                ::pyci_gpu::note_launch();
+            const int qq = std::min(kMaxQ, q - j0);
+            Theta th{};
+            for (int j = 0; j < qq; ++j)
+                th.t[j] = theta[j0 + j];
+            residual_kernel<U><<<grid(N_), 256, 0, st_>>>(AX + o, X + o, th, qq, N_, R + o), ::pyci_gpu::note_launch();
         }
     }
 
-    // out[c] = preconditioned R[todo[c]] (theta in d_theta_), in launches of
-    // at most kMaxQ columns.
+    // out[c] = preconditioned R[todo[c]] (Ritz value theta[todo[c]]), in
+    // launches of at most kMaxQ columns.
     template<typename U>
-    void precondition(const U *R, const double *diag, const std::vector<int> &todo, T *out) {
+    void precondition(const U *R, const double *diag, const std::vector<int> &todo, const std::vector<double> &theta,
+                      T *out) {
         for (size_t c0 = 0; c0 < todo.size(); c0 += kMaxQ)
-            precondition_kernel<U, T><<<grid(N_), 256, 0, st_>>>(R, d_theta_, diag, make_cols(todo, c0), N_,
+            precondition_kernel<U, T><<<grid(N_), 256, 0, st_>>>(R, diag, make_cols(todo, c0, theta), N_,
                                                                   out + static_cast<int64_t>(c0) * N_),
                 ::pyci_gpu::note_launch();
     }
@@ -630,17 +651,10 @@ private:
         return e;
     }
     int64_t syncs_ = 0;
-    double wait_s_ = 0.0, upload_s_ = 0.0, eig_s_ = 0.0;
+    double wait_s_ = 0.0, eig_s_ = 0.0;
     const bool trace_ = std::getenv("PYCI_GPU_SOLVE_TRACE") != nullptr;
-    double *h_small_ = nullptr; // pinned [kMaxGramP * kMaxQ]
-    // Host -> device copy of small coefficient blocks through the context's
-    // pinned ring (which may wait for a slot's previous copy).
-    int upload(void *dst, const void *src, size_t n, cudaStream_t st) {
-        const auto t0 = std::chrono::steady_clock::now();
-        const int rc = csr_->ctx->ring->upload(dst, src, n, st);
-        upload_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        return rc;
-    }
+    double *h_small_ = nullptr;  // pinned [kMaxGramP * kMaxQ]
+    double *d_mapped_ = nullptr; // device alias of h_small_ (mapped), or null
     bool eig(int m, const std::vector<double> &a, std::vector<double> &w, std::vector<double> &z) {
         const auto t0 = std::chrono::steady_clock::now();
         const bool ok = symmetric_eigen(m, a, w, z);
@@ -650,7 +664,7 @@ private:
     int64_t matvecs_ = 0, matvecs64_ = 0;
     unsigned gram_blocks_ = 1;
     T *Xi_ = nullptr, *Yi_ = nullptr, *Sb_ = nullptr;
-    double *d_partial_ = nullptr, *d_small_ = nullptr, *d_coef_ = nullptr, *d_theta_ = nullptr;
+    double *d_partial_ = nullptr, *d_small_ = nullptr;
 };
 
 template<typename T>
@@ -849,10 +863,18 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         (rc = alloc(&AXr, static_cast<int64_t>(std::max(nkeep_max, b)) * N)) ||
         (rc = alloc(&R, static_cast<int64_t>(b) * N)) || (rc = alloc(&Xi_, N * kMaxQ)) ||
         (rc = alloc(&Yi_, N * kMaxQ)) || (rc = alloc(&Sb_, N * kMaxQ)) || (rc = alloc(&d_partial_, static_cast<int64_t>(gram_blocks_) * kMaxGramP * kMaxQ)) ||
-        (rc = alloc(&d_small_, kMaxGramP * kMaxQ)) || (rc = alloc(&d_coef_, kMaxGramP * kMaxQ)) ||
-        (rc = alloc(&d_theta_, std::max(mmax, b))))
+        (rc = alloc(&d_small_, kMaxGramP * kMaxQ)))
         return rc;
-    PYCI_CUDA_TRY(cudaMallocHost(reinterpret_cast<void **>(&h_small_), sizeof(double) * kMaxGramP * kMaxQ));
+    PYCI_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(&h_small_), sizeof(double) * kMaxGramP * kMaxQ,
+                                cudaHostAllocMapped));
+    {
+        int can_map = 0;
+        cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, csr_->ctx->device);
+        void *dp = nullptr;
+        if (can_map && cudaHostGetDevicePointer(&dp, h_small_, 0) == cudaSuccess)
+            d_mapped_ = static_cast<double *>(dp);
+        cudaGetLastError();
+    }
     double *d_diag = csr_->diag;
 
     // Diagonal on the host for the initial guess.
@@ -952,9 +974,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 Yb[static_cast<size_t>(i) * b + j] = Y[static_cast<size_t>(i) * m + j];
         if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
             return rc;
-        if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
-            return rc;
-        residuals<T>(AXr, Xr, b, R);
+        residuals<T>(AXr, Xr, b, theta, R);
         bool all = true;
         std::vector<int> todo;
         if ((rc = gram<T>(R, b, R, b, Gc)))
@@ -1070,9 +1090,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if ((rc = combine<double, double, double>(AX64, br, Z, br, 0.0, R64)))
                 return rc;
             PYCI_CUDA_TRY(cudaMemcpyAsync(AX64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
-            if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
-                return rc;
-            residuals<double>(AX64, X64, br, R64);
+            residuals<double>(AX64, X64, br, th64, R64);
             bool ok64 = true;
             todo.clear();
             max_res = 0.0;
@@ -1107,10 +1125,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
                 m = b;
                 ++restarts;
             }
-            if ((rc = upload(d_theta_, th64.data(), sizeof(double) * br, st_)))
-                return rc;
             const int q = static_cast<int>(todo.size());
-            precondition<double>(R64, d_diag, todo, V + static_cast<int64_t>(m) * N);
+            precondition<double>(R64, d_diag, todo, th64, V + static_cast<int64_t>(m) * N);
             if ((rc = orthonormalize(V, m, q, knew)))
                 return rc;
             continue;
@@ -1139,10 +1155,8 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             ++restarts;
         }
         // Preconditioned residuals of the unconverged roots.
-        if ((rc = upload(d_theta_, theta.data(), sizeof(double) * b, st_)))
-            return rc;
         const int q = static_cast<int>(todo.size());
-        precondition<T>(R, d_diag, todo, V + static_cast<int64_t>(m) * N);
+        precondition<T>(R, d_diag, todo, theta, V + static_cast<int64_t>(m) * N);
         if ((rc = orthonormalize(V, m, q, knew)))
             return rc;
         if (knew == 0) {
@@ -1183,11 +1197,11 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         stats->seconds_wait = wait_s_;
     }
     // PYCI_GPU_SOLVE_TRACE: one line per solve on stderr with the host-side
-    // breakdown (blocked in read-backs, coefficient uploads, Rayleigh-Ritz).
+    // breakdown (blocked in read-backs, Rayleigh-Ritz).
     if (trace_)
-        std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), upload %.3f ms, eig %.3f ms, iters %lld\n",
+        std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), eig %.3f ms, iters %lld\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() * 1e3,
-                     timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), upload_s_ * 1e3, eig_s_ * 1e3,
+                     timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), eig_s_ * 1e3,
                      static_cast<long long>(iter + 1));
     return PYCI_GPU_OK;
 }
