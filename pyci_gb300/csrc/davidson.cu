@@ -394,6 +394,38 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
     }
 }
 
+// L^{-1} (row-major, lower) for the Cholesky factor S = L L^T of a k x k
+// symmetric matrix (row-major); false when a pivot is not above tol times its
+// diagonal entry (S not safely positive definite).
+inline bool cholesky_inverse(const std::vector<double> &S, int k, double tol, std::vector<double> &Linv) {
+    std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
+    for (int j = 0; j < k; ++j) {
+        double d = S[static_cast<size_t>(j) * k + j];
+        for (int t = 0; t < j; ++t)
+            d -= L[static_cast<size_t>(j) * k + t] * L[static_cast<size_t>(j) * k + t];
+        if (!(d > tol * S[static_cast<size_t>(j) * k + j]) || !(d > 0.0))
+            return false;
+        L[static_cast<size_t>(j) * k + j] = std::sqrt(d);
+        for (int i = j + 1; i < k; ++i) {
+            double x = S[static_cast<size_t>(i) * k + j];
+            for (int t = 0; t < j; ++t)
+                x -= L[static_cast<size_t>(i) * k + t] * L[static_cast<size_t>(j) * k + t];
+            L[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(j) * k + j];
+        }
+    }
+    Linv.assign(static_cast<size_t>(k) * k, 0.0);
+    for (int j = 0; j < k; ++j) {
+        Linv[static_cast<size_t>(j) * k + j] = 1.0 / L[static_cast<size_t>(j) * k + j];
+        for (int i = j + 1; i < k; ++i) {
+            double x = 0.0;
+            for (int t = j; t < i; ++t)
+                x -= L[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(t) * k + j];
+            Linv[static_cast<size_t>(i) * k + j] = x / L[static_cast<size_t>(i) * k + i];
+        }
+    }
+    return true;
+}
+
 // Columns todo[c0 .. c0 + kMaxQ) of a correction list, with their Ritz values.
 inline Cols make_cols(const std::vector<int> &todo, size_t c0, const std::vector<double> &theta) {
     Cols c{};
@@ -569,8 +601,12 @@ private:
 
     // W[0..k) = H V[0..k) (storage precision of T; FP64 uses f64 values).
     int apply(const T *V, int k, T *W, int prec) {
-        for (int j0 = 0; j0 < k; j0 += kSpmmChunk) {
-            const int kk = std::min(kSpmmChunk, k - j0);
+        // On the SELL-32 copy the FP32 product streams the matrix once per
+        // launch and is bound by that stream, so up to 8 vectors share one
+        // launch (a 5-vector block as one product padded to 8, not 4 + 1).
+        const int chunk = (prec == PYCI_PREC_FP32 && csr_->sell_cols) ? kMaxQ : kSpmmChunk;
+        for (int j0 = 0; j0 < k; j0 += chunk) {
+            const int kk = std::min(chunk, k - j0);
             const int kp = padded_width(kk);
             pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_), ::pyci_gpu::note_launch();
             const size_t tk = timer_begin();
@@ -1046,8 +1082,28 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             // vectors enter the refined Rayleigh quotients only to second order.
             if ((rc = combine<T, double, T>(V, m, Ybr, br, 0.0, X64)))
                 return rc;
-            // Orthonormalise X64 in FP64 (modified Gram-Schmidt, two passes).
-            for (int j = 0; j < br; ++j) {
+            // Orthonormalise X64 in FP64: Cholesky QR twice (the Ritz vectors
+            // of the FP32 subspace are orthonormal to ~1e-7, so X^T X is
+            // close to I; 2 host round trips); vector-by-vector Gram-Schmidt
+            // if X^T X is not safely positive definite.
+            bool cholqr_ok = br > 1;
+            for (int pass = 0; pass < 2 && cholqr_ok; ++pass) {
+                if ((rc = gram<double>(X64, br, X64, br, Gc)))
+                    return rc;
+                std::vector<double> Linv;
+                if (!cholesky_inverse(Gc, br, 1e-8, Linv)) {
+                    cholqr_ok = false;
+                    break;
+                }
+                std::vector<double> Yc(static_cast<size_t>(br) * br);
+                for (int i = 0; i < br; ++i)
+                    for (int j = 0; j < br; ++j)
+                        Yc[static_cast<size_t>(i) * br + j] = Linv[static_cast<size_t>(j) * br + i];
+                if ((rc = combine<double, double, double>(X64, br, Yc, br, 0.0, R64)))
+                    return rc;
+                PYCI_CUDA_TRY(cudaMemcpyAsync(X64, R64, sizeof(double) * br * N, cudaMemcpyDeviceToDevice, st_));
+            }
+            for (int j = 0; j < br && !cholqr_ok; ++j) {
                 double *xj = X64 + static_cast<int64_t>(j) * N;
                 for (int pass = 0; pass < 2 && j > 0; ++pass) {
                     if ((rc = gram<double>(X64, j, xj, 1, Gc)))
