@@ -106,3 +106,27 @@ def test_host_module_argument_errors_without_a_gpu():
     ham7 = pyci.secondquant_op(*synthetic_integrals(7, 3))
     with pytest.raises(ValueError):
         pyci.add_hci(ham7, wfn, np.ones(len(wfn)))  # Hamiltonian of another basis
+
+
+def test_solve_stats_layout_matches_the_header(tmp_path):
+    r"""The ctypes mirror of pyci_gpu_solve_stats has the C struct's field
+    offsets and size (compiled against include/pyci_gb300.h with the host C
+    compiler)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in capi.SolveStats._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"pyci_gb300.h\"\nint main(void) {\n"
+                   + "".join('    printf("%%s %%zu\\n", "%s", offsetof(pyci_gpu_solve_stats, %s));\n' % (f, f)
+                             for f in fields)
+                   + '    printf("sizeof %zu\\n", sizeof(pyci_gpu_solve_stats));\n    return 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                        text=True).stdout.splitlines())
+    for f in fields:
+        assert int(out[f]) == getattr(capi.SolveStats, f).offset, f
+    assert int(out["sizeof"]) == ctypes.sizeof(capi.SolveStats)
