@@ -321,3 +321,37 @@ def test_clone_is_deep(ctx):
     for x, y in zip(da, db):
         assert np.array_equal(x, y)
     b.free()
+
+
+def test_clone_keeps_the_sell_copy(ctx, monkeypatch):
+    r"""A clone of a prepared operator carries its SELL-32 copy: the clone's
+    FP32 and double-float products (pinned to the SELL kernels) equal the
+    original's, after the original is freed."""
+    import ctypes
+
+    import torch
+    ecore, one, two = synthetic_integrals(8, 1006)
+    dets = O.all_dets(O.FULLCI, 8, 4, 3)
+    monkeypatch.setenv("PYCI_GPU_SPMM", "sell")
+    a = capi.Csr(ctx, capi.WFN_FULLCI, 8, 4, 3, dets, one, two, flags=capi.BUILD_FULL_COLEX)
+    a.prepare_mixed(drop_fp64=True)
+    out = ctypes.c_void_p()
+    capi.check(capi.lib().pyci_gpu_csr_clone(a.handle, ctypes.byref(out)))
+    b = capi.Csr.__new__(capi.Csr)
+    b.handle = out
+    N = dets.shape[0]
+    X = np.random.default_rng(9).normal(size=(N, 4))
+    xf = torch.tensor(X, dtype=torch.float32, device="cuda")
+    xs = torch.tensor(split_rows(X), device="cuda")
+    res = []
+    for op in (a, b):
+        yf = torch.empty((N, 4), dtype=torch.float32, device="cuda")
+        yd = torch.empty((N, 4), dtype=torch.float64, device="cuda")
+        op.spmm_device(capi.PREC_FP32, 4, xf.data_ptr(), yf.data_ptr(), None)
+        op.spmm_device(capi.PREC_FP64_DF, 4, xs.data_ptr(), yd.data_ptr(), None)
+        torch.cuda.synchronize()
+        res.append((yf.cpu().numpy(), yd.cpu().numpy()))
+        if op is a:
+            a.free()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    b.free()
