@@ -1,0 +1,115 @@
+r"""Reduced density matrices from their definition, on the CPU: for small
+FullCI and DOCI wave functions the spin-orbital RDMs
+
+    gamma[p, q] = <Psi| a+_p a_q |Psi>,
+    Gamma[p, q, r, s] = <Psi| a+_p a+_q a_s a_r |Psi>,
+
+are formed by applying creation and annihilation operators to every
+determinant (Jordan-Wigner signs, spin orbitals alpha 0..n-1 then beta
+n..2n-1), and compared with the oracle's compute_rdms followed by the
+package's spinize_rdms (the reference's pyci.spinize_rdms convention, pinned
+by its tests on FullCI(2, 1α1β) and FullCI(3, 2α1β) with coefficients
+sqrt(1..N), pyci/test/test_routines.py:494-800).  This checks the oracle's
+restatement and the host-side spinization independently of the reference's
+code; the GPU RDMs equal the oracle's (GPU tests)."""
+
+import itertools
+
+import numpy as np
+import numpy.testing as npt
+import pytest
+
+import oracle as O
+import pyci_gb300 as pyci
+
+
+def spin_orbitals(kind, det, n):
+    r"""Occupied spin orbitals of one determinant row of the oracle's array."""
+    words = [int(w) for w in det]
+    if kind == O.FULLCI:
+        nw = len(words) // 2
+        alpha = sum(w << (64 * i) for i, w in enumerate(words[:nw]))
+        beta = sum(w << (64 * i) for i, w in enumerate(words[nw:]))
+    else:  # DOCI: one mask of doubly occupied orbitals
+        alpha = beta = sum(w << (64 * i) for i, w in enumerate(words))
+    occ = [p for p in range(n) if alpha >> p & 1] + [n + p for p in range(n) if beta >> p & 1]
+    return tuple(occ)
+
+
+def annihilate(state, p):
+    r"""a_p |state> for a sorted occupation tuple: (sign, state) or None."""
+    if p not in state:
+        return None
+    k = state.index(p)
+    return (-1) ** k, state[:k] + state[k + 1:]
+
+
+def create(state, p):
+    if p in state:
+        return None
+    k = sum(1 for q in state if q < p)
+    return (-1) ** k, state[:k] + (p,) + state[k:]
+
+
+def apply(ops, state):
+    r"""Apply operators right to left: ops = [(op, index), ...] in written order."""
+    sign = 1
+    for op, p in reversed(ops):
+        r = op(state, p)
+        if r is None:
+            return None
+        s, state = r
+        sign *= s
+    return sign, state
+
+
+def brute_force_rdms(kind, n, dets, coeffs):
+    states = [spin_orbitals(kind, d, n) for d in dets]
+    index = {s: i for i, s in enumerate(states)}
+    m = 2 * n
+    g1 = np.zeros((m, m))
+    g2 = np.zeros((m, m, m, m))
+    for j, sj in enumerate(states):
+        cj = coeffs[j]
+        if cj == 0.0:
+            continue
+        for p, q in itertools.product(range(m), repeat=2):
+            r = apply([(create, p), (annihilate, q)], sj)
+            if r is not None and r[1] in index:
+                g1[p, q] += coeffs[index[r[1]]] * r[0] * cj
+        for p, q, r_, s in itertools.product(range(m), repeat=4):
+            r = apply([(create, p), (create, q), (annihilate, s), (annihilate, r_)], sj)
+            if r is not None and r[1] in index:
+                g2[p, q, r_, s] += coeffs[index[r[1]]] * r[0] * cj
+    return g1, g2
+
+
+CASES = [
+    # (kind, nbasis, nocc_up, nocc_dn, coefficient pattern)
+    (O.FULLCI, 2, 1, 1, "sqrt"),
+    (O.FULLCI, 3, 2, 1, "sqrt"),
+    (O.FULLCI, 4, 2, 2, "random"),
+    (O.FULLCI, 4, 3, 1, "random"),
+    (O.DOCI, 4, 2, 2, "random"),
+    (O.DOCI, 5, 2, 2, "sqrt"),
+]
+
+
+@pytest.mark.parametrize("kind,n,nu,nd,pattern", CASES)
+def test_spinized_rdms_equal_their_definition(kind, n, nu, nd, pattern):
+    dets = O.all_dets(kind, n, nu, nd)
+    N = dets.shape[0]
+    if pattern == "sqrt":
+        c = np.sqrt(np.arange(1.0, N + 1.0))
+    else:
+        c = np.random.default_rng(n * 10 + nu).normal(size=N)
+    c /= np.linalg.norm(c)
+    d1, d2 = O.compute_rdms(kind, n, nu, nd, dets, c)
+    rdm1, rdm2 = pyci.spinize_rdms(d1, d2)
+    g1, g2 = brute_force_rdms(kind, n, dets, c)
+    npt.assert_allclose(rdm1, g1, rtol=0, atol=1e-13)
+    npt.assert_allclose(rdm2, g2, rtol=0, atol=1e-13)
+    # Traces: N electrons, N (N - 1) pairs.
+    ne = nu + nd
+    assert np.trace(rdm1) == pytest.approx(ne, abs=1e-12)
+    assert np.einsum("pqpq", rdm2) == pytest.approx(ne * (ne - 1), abs=1e-12)
