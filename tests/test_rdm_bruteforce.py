@@ -9,9 +9,10 @@ determinant (Jordan-Wigner signs, spin orbitals alpha 0..n-1 then beta
 n..2n-1), and compared with the oracle's compute_rdms followed by the
 package's spinize_rdms (the reference's pyci.spinize_rdms convention, pinned
 by its tests on FullCI(2, 1α1β) and FullCI(3, 2α1β) with coefficients
-sqrt(1..N), pyci/test/test_routines.py:494-800).  This checks the oracle's
-restatement and the host-side spinization independently of the reference's
-code; the GPU RDMs equal the oracle's (GPU tests)."""
+sqrt(1..N), pyci/test/test_routines.py:494-800).  Transition RDMs are
+<Psi_1| ... |Psi_2> with the first wave function as the bra.  This checks the
+oracle's restatement and the host-side spinization independently of the
+reference's code; the GPU RDMs equal the oracle's (GPU tests)."""
 
 import itertools
 
@@ -113,3 +114,39 @@ def test_spinized_rdms_equal_their_definition(kind, n, nu, nd, pattern):
     ne = nu + nd
     assert np.trace(rdm1) == pytest.approx(ne, abs=1e-12)
     assert np.einsum("pqpq", rdm2) == pytest.approx(ne * (ne - 1), abs=1e-12)
+
+
+def brute_force_transition_rdms(kind, n, dets1, c1, dets2, c2):
+    r"""<Psi_1| a+_p a_q |Psi_2> and <Psi_1| a+_p a+_q a_s a_r |Psi_2>."""
+    bra = {spin_orbitals(kind, d, n): c1[i] for i, d in enumerate(dets1)}
+    m = 2 * n
+    g1 = np.zeros((m, m))
+    g2 = np.zeros((m, m, m, m))
+    for j, d in enumerate(dets2):
+        sj, cj = spin_orbitals(kind, d, n), c2[j]
+        for p, q in itertools.product(range(m), repeat=2):
+            r = apply([(create, p), (annihilate, q)], sj)
+            if r is not None and r[1] in bra:
+                g1[p, q] += bra[r[1]] * r[0] * cj
+        for p, q, r_, s in itertools.product(range(m), repeat=4):
+            r = apply([(create, p), (create, q), (annihilate, s), (annihilate, r_)], sj)
+            if r is not None and r[1] in bra:
+                g2[p, q, r_, s] += bra[r[1]] * r[0] * cj
+    return g1, g2
+
+
+@pytest.mark.parametrize("n,nu,nd", [(3, 2, 1), (4, 2, 2)])
+def test_spinized_fullci_transition_rdms_equal_their_definition(n, nu, nd):
+    dets = O.all_dets(O.FULLCI, n, nu, nd)
+    N = dets.shape[0]
+    rng = np.random.default_rng(n)
+    c1, c2 = rng.normal(size=N), rng.normal(size=N)
+    c1 /= np.linalg.norm(c1)
+    c2 /= np.linalg.norm(c2)
+    # A proper subset on one side: excitations that leave it are dropped.
+    keep = np.sort(rng.choice(N, size=N - 2, replace=False))
+    d1, d2 = O.compute_transition_rdms(O.FULLCI, n, nu, nd, dets[keep], c1[keep], dets, c2)
+    t1, t2 = pyci.spinize_rdms(d1, d2)
+    g1, g2 = brute_force_transition_rdms(O.FULLCI, n, dets[keep], c1[keep], dets, c2)
+    npt.assert_allclose(t1, g1, rtol=0, atol=1e-13)
+    npt.assert_allclose(t2, g2, rtol=0, atol=1e-13)
