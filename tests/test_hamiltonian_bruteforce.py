@@ -1,0 +1,56 @@
+r"""The CI Hamiltonian from second quantization, on the CPU: for small FullCI
+and DOCI spaces every matrix element <Phi_i| H |Phi_j> of
+
+    H = sum_PQ h_PQ a+_P a_Q + 1/2 sum_PQRS <PQ|RS> a+_P a+_Q a_S a_R
+
+(spin orbitals alpha 0..n-1 then beta n..2n-1; <PQ|RS> = <pq|rs> when P, R
+and Q, S have equal spins, physicist's integrals as pyci's two_mo) is formed
+by applying the operators to every determinant, and compared with the
+oracle's CSR, which is bit-identical to the reference's sparse_op
+(pyci/src/sparseop.cpp add_row).  A DOCI space gets the projection of the
+same H onto its paired determinants.  This pins the Slater-Condon rules,
+phases and orbital orderings independently of the reference's code."""
+
+import itertools
+
+import numpy as np
+import pytest
+
+import oracle as O
+from pyci_gb300.synth import synthetic_integrals
+from test_rdm_bruteforce import annihilate, apply, create, spin_orbitals
+
+
+def second_quantized_matrix(kind, n, dets, one, two):
+    states = [spin_orbitals(kind, d, n) for d in dets]
+    index = {s: i for i, s in enumerate(states)}
+    m = 2 * n
+    spin = [p // n for p in range(m)]
+    orb = [p % n for p in range(m)]
+    H = np.zeros((len(states), len(states)))
+    for j, sj in enumerate(states):
+        for P, Q in itertools.product(range(m), repeat=2):
+            if spin[P] != spin[Q]:
+                continue
+            r = apply([(create, P), (annihilate, Q)], sj)
+            if r is not None and r[1] in index:
+                H[index[r[1]], j] += r[0] * one[orb[P], orb[Q]]
+        for P, Q, R, S in itertools.product(range(m), repeat=4):
+            if spin[P] != spin[R] or spin[Q] != spin[S]:
+                continue
+            r = apply([(create, P), (create, Q), (annihilate, S), (annihilate, R)], sj)
+            if r is not None and r[1] in index:
+                H[index[r[1]], j] += 0.5 * r[0] * two[orb[P], orb[Q], orb[R], orb[S]]
+    return H
+
+
+@pytest.mark.parametrize("kind,n,nu,nd", [(O.FULLCI, 4, 2, 2), (O.FULLCI, 4, 3, 1), (O.FULLCI, 3, 2, 0),
+                                          (O.DOCI, 5, 2, 2), (O.DOCI, 4, 1, 1)])
+def test_csr_equals_second_quantized_hamiltonian(kind, n, nu, nd):
+    ecore, one, two = synthetic_integrals(n, 90 + n)
+    dets = O.all_dets(kind, n, nu, nd)
+    N = dets.shape[0]
+    ref = O.build_csr(kind, n, nu, nd, dets, one, two)
+    H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
+    H2 = second_quantized_matrix(kind, n, dets, one, two)
+    np.testing.assert_allclose(H, H2, rtol=0, atol=1e-12 * np.abs(H2).max())
