@@ -54,3 +54,32 @@ def test_csr_equals_second_quantized_hamiltonian(kind, n, nu, nd):
     H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
     H2 = second_quantized_matrix(kind, n, dets, one, two)
     np.testing.assert_allclose(H, H2, rtol=0, atol=1e-12 * np.abs(H2).max())
+
+
+@pytest.mark.parametrize("n,nocc", [(6, 3), (7, 2)])
+def test_genci_csr_equals_spinless_second_quantized_hamiltonian(n, nocc):
+    r"""GenCI determinants are sets of nocc occupied spin-orbitals out of n,
+    with the integrals given over those spin-orbitals (no spin blocks).  The
+    oracle's Slater-Condon form (kind GENCI; the GPU build with
+    PYCI_BUILD_GENCI_EXACT) equals the operator-algebra matrix.  The
+    reference's own GenCI row loop, reproduced as kind GENCI_REF and by the
+    GPU's default GenCI build, differs from it: it walks 2 n - nocc virtual
+    entries where n - nocc exist."""
+    ecore, one, two = synthetic_integrals(n, 95 + n)
+    dets = O.all_dets(O.GENCI, n, nocc, 0)
+    N = dets.shape[0]
+    states = [tuple(p for p in range(n) if int(d[0]) >> p & 1) for d in dets]
+    index = {s: i for i, s in enumerate(states)}
+    H2 = np.zeros((N, N))
+    for j, sj in enumerate(states):
+        for P, Q in itertools.product(range(n), repeat=2):
+            r = apply([(create, P), (annihilate, Q)], sj)
+            if r is not None and r[1] in index:
+                H2[index[r[1]], j] += r[0] * one[P, Q]
+        for P, Q, R, S in itertools.product(range(n), repeat=4):
+            r = apply([(create, P), (create, Q), (annihilate, S), (annihilate, R)], sj)
+            if r is not None and r[1] in index:
+                H2[index[r[1]], j] += 0.5 * r[0] * two[P, Q, R, S]
+    ref = O.build_csr(O.GENCI, n, nocc, 0, dets, one, two)
+    H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
+    np.testing.assert_allclose(H, H2, rtol=0, atol=1e-12 * np.abs(H2).max())
