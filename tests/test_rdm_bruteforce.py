@@ -150,3 +150,32 @@ def test_spinized_fullci_transition_rdms_equal_their_definition(n, nu, nd):
     g1, g2 = brute_force_transition_rdms(O.FULLCI, n, dets[keep], c1[keep], dets, c2)
     npt.assert_allclose(t1, g1, rtol=0, atol=1e-13)
     npt.assert_allclose(t2, g2, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("n,npair", [(6, 3), (8, 2)])
+def test_reduced_senzero_integrals_give_the_doci_energy(n, npair):
+    r"""E = ecore + sum(rv * d0) + sum(rw * d2) for a DOCI eigenvector, with
+    (rv, rw) from reduce_senzero_integrals(h, v, w, npair) and (d0, d2) from
+    the oracle's compute_rdms (pyci/utility.py:59-91; the reference's
+    test_compute_rdms energy check).  h, v, w are the seniority-zero integrals
+    h_p = <p|h|p>, v_pq = <pp|qq>, w_pq = 2 <pq|pq> - <pq|qp>."""
+    from pyci_gb300.synth import synthetic_integrals
+    ecore, one, two = synthetic_integrals(n, 60 + n)
+    dets = O.all_dets(O.DOCI, n, npair, npair)
+    N = dets.shape[0]
+    ref = O.build_csr(O.DOCI, n, npair, npair, dets, one, two)
+    H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
+    w_, v_ = np.linalg.eigh(H)
+    c = v_[:, 0]
+    d0, d2 = O.compute_rdms(O.DOCI, n, npair, npair, dets, c)
+    idx = np.arange(n)
+    h = one[idx, idx]
+    v = two[idx[:, None], idx[:, None], idx[None, :], idx[None, :]]
+    w = 2.0 * two[idx[:, None], idx[None, :], idx[:, None], idx[None, :]] \
+        - two[idx[:, None], idx[None, :], idx[None, :], idx[:, None]]
+    # The host module's secondquant_op derives the same seniority-zero integrals.
+    ham = pyci.secondquant_op(ecore, one, two)
+    assert np.array_equal(ham.h, h) and np.array_equal(ham.v, v) and np.array_equal(ham.w, w)
+    rv, rw = pyci.reduce_senzero_integrals(ham.h, ham.v, ham.w, npair)
+    energy = ecore + np.sum(rv * d0) + np.sum(rw * d2)
+    assert energy == pytest.approx(w_[0] + ecore, abs=1e-10)
