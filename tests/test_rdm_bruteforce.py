@@ -179,3 +179,19 @@ def test_reduced_senzero_integrals_give_the_doci_energy(n, npair):
     rv, rw = pyci.reduce_senzero_integrals(ham.h, ham.v, ham.w, npair)
     energy = ecore + np.sum(rv * d0) + np.sum(rw * d2)
     assert energy == pytest.approx(w_[0] + ecore, abs=1e-10)
+
+
+@pytest.mark.parametrize("n,npair", [(5, 2), (6, 3)])
+def test_spinized_doci_transition_rdms_equal_their_definition(n, npair):
+    dets = O.all_dets(O.DOCI, n, npair, npair)
+    N = dets.shape[0]
+    rng = np.random.default_rng(10 * n + npair)
+    c1, c2 = rng.normal(size=N), rng.normal(size=N)
+    c1 /= np.linalg.norm(c1)
+    c2 /= np.linalg.norm(c2)
+    keep = np.sort(rng.choice(N, size=N - 3, replace=False))
+    d1, d2 = O.compute_transition_rdms(O.DOCI, n, npair, npair, dets[keep], c1[keep], dets, c2)
+    t1, t2 = pyci.spinize_rdms(d1, d2)
+    g1, g2 = brute_force_transition_rdms(O.DOCI, n, dets[keep], c1[keep], dets, c2)
+    npt.assert_allclose(t1, g1, rtol=0, atol=1e-13)
+    npt.assert_allclose(t2, g2, rtol=0, atol=1e-13)
