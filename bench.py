@@ -53,11 +53,10 @@ WORKLOADS = {
 WORKLOAD = WORKLOADS["fci12"]
 METRIC = WORKLOAD["metric"]
 # DRAM bytes moved per algorithmic byte by the FP32 k = 4 SpMM (SELL-32 kernel),
-# from one ncu capture of the same kernel on the 11-orbital 5a5b operator
-# (2.1617 GB moved for 2.1621 GB algorithmic;
-# profiles/spmm_sell_fci11_5a5b_ncu_full.md).  Both operators stream the matrix
-# once per launch with the x block in L2, so traffic scales with the entries
-# processed.
+# from one ncu capture of the same kernel on the 11-orbital 5a5b FullCI
+# operator (2.1617 GB moved for 2.1621 GB algorithmic).  Both operators stream
+# the matrix once per launch with the x block in L2, so traffic scales with the
+# entries processed.
 TRAFFIC_PER_ALGORITHMIC_BYTE = 1.000
 TOL = 1.0e-6  # residual <= 1e-6 * |E| (~1e-5 Ha): eigenvalues converge quadratically, well inside 1 uHa
 
@@ -169,50 +168,141 @@ def reference_eigenvalues():
         return None
 
 
-def cpu_solve(nthreads):
-    r"""One full CPU solve of the workload with the oracle; returns (seconds, evals)."""
+def load_synth():
+    r"""The synthetic-integral recipe (pyci_gb300/synth.py, pure numpy) loaded
+    by path, so that the CPU arm never imports the pyci_gb300 package (whose
+    __init__ loads the GPU library and the host module)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pyci_gb300_synth", os.path.join(ROOT, "pyci_gb300", "synth.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.synthetic_integrals
+
+
+def load_oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    from pyci_gb300.synth import synthetic_integrals
     O.build()
+    return O
+
+
+def workload_config(ndet, stored, size, world):
+    r"""The `config` object of both arms: the workload, its sizes (stored =
+    both triangles, as the GPU keeps them; reference = the reference's lower
+    layout), roots, tolerance, L2 note and parallelism."""
+    bytes32 = stored * (4 + 4) + (ndet + 1) * 8 + 2 * ndet * WORKLOAD["nroot"] * 4
+    return {"workload": WORKLOAD["workload"], "ndet": int(ndet), "nnz_stored": int(stored),
+            "nnz_reference": int(size), "roots": WORKLOAD["nroot"], "tol": WORKLOAD.get("tol", TOL),
+            "l2": ("matrix (%.1f GB) >> 129 MB L2; no flush needed" % (bytes32 / 1e9)) if bytes32 > 2**28
+            else "matrix (%.0f MB) fits in the 129 MB L2: SpMV figures are L2-resident" % (bytes32 / 1e6),
+            "parallelism": "replicas" if world > 1 else "single GPU"}
+
+
+def cpu_problem(O):
+    synthetic_integrals = load_synth()
     ecore, one, two = synthetic_integrals(WORKLOAD["nbasis"], WORKLOAD["seed"])
     kind = O.FULLCI if WORKLOAD["wfn"] == "fullci" else O.DOCI
+    return kind, ecore, one, two
+
+
+def arpack(O, csr, nthreads, counter=None):
+    r"""ARPACK's implicitly restarted Lanczos (the algorithm of Spectra's
+    SymEigsSolver, with the reference's ncv = max(2 n + 1, 20)) on the
+    oracle's threaded self-adjoint SpMV, from a seeded random start (the
+    reference's solver starts from a random vector)."""
+    import scipy.sparse.linalg as spl
+    n = csr[2].shape[0] - 1
+    nroot = WORKLOAD["nroot"]
+
+    def mv(x):
+        if counter is not None:
+            counter[0] += 1
+        return O.spmv(*csr, np.ravel(x), nthreads=nthreads)
+
+    op = spl.LinearOperator((n, n), matvec=mv, dtype=np.float64)
+    evals = spl.eigsh(op, k=nroot, which="SA", tol=WORKLOAD.get("tol", TOL), return_eigenvectors=False,
+                      v0=np.random.default_rng(7).standard_normal(n), ncv=max(2 * nroot + 1, 20))
+    return np.sort(evals)
+
+
+def cpu_solve(nthreads):
+    r"""One full CPU solve of the workload with the oracle; returns
+    (seconds, build seconds, eigenvalues)."""
+    O = load_oracle()
+    kind, ecore, one, two = cpu_problem(O)
     t0 = time.perf_counter()
     dets = O.all_dets(kind, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"])
     csr = O.build_csr(kind, WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"], dets, one, two,
                       nthreads=nthreads)
     t1 = time.perf_counter()
-    import scipy.sparse.linalg as spl
-    n = csr[2].shape[0] - 1
-    op = spl.LinearOperator((n, n), matvec=lambda x: O.spmv(*csr, np.ravel(x), nthreads=nthreads),
-                            dtype=np.float64)
-    # Seeded random start, as the reference's Spectra solver starts from a random vector.
-    evals = spl.eigsh(op, k=WORKLOAD["nroot"], which="SA", tol=WORKLOAD.get("tol", TOL), return_eigenvectors=False,
-                      v0=np.random.default_rng(7).standard_normal(n), ncv=2 * WORKLOAD["nroot"] + 12)
+    evals = arpack(O, csr, nthreads)
     t2 = time.perf_counter()
-    return t2 - t0, t1 - t0, np.sort(evals) + ecore
+    return t2 - t0, t1 - t0, evals + ecore
 
 
 def run_reference(args, world, rank):
+    r"""The reference algorithm on the host cores, in bounded samples.
+
+    Preparation (untimed): the oracle builds the whole operator once and
+    ARPACK solves it once, which gives the solve's SpMV count M.  The work of
+    one full solve is then cut into K equal samples, one per timed step:
+    step s builds rows [s N / K, (s + 1) N / K) of the operator (count and
+    fill passes, all threads) and applies the whole operator M / K times.
+    The K steps together are the build plus every product of one solve, so
+    value = (sum of the K step times) / roots.  ARPACK's own dense work
+    between products is not in the samples (it favours the CPU figure).
+    Only rank 0 works; the other ranks exit without work."""
     if rank != 0:
         return
     nthreads = os.cpu_count() or 1
-    for _ in range(args.warmup if args.warmup <= 1 else 1):
-        cpu_solve(nthreads)
+    O = load_oracle()
+    kind, ecore, one, two = cpu_problem(O)
+    nb, nu, nd = WORKLOAD["nbasis"], WORKLOAD["nocc_up"], WORKLOAD["nocc_dn"]
+    nroot = WORKLOAD["nroot"]
+    dets = O.all_dets(kind, nb, nu, nd)
+    n = dets.shape[0]
+    t0 = time.perf_counter()
+    csr = O.build_csr(kind, nb, nu, nd, dets, one, two, nthreads=nthreads)
+    t_build_full = time.perf_counter() - t0
+    size = int(csr[2][-1])
+    count = [0]
+    t0 = time.perf_counter()
+    evals = arpack(O, csr, nthreads, count)
+    t_solve_full = time.perf_counter() - t0
+    nmv = count[0]
+    hvw = O.senzero(one, two)
+    x = np.random.default_rng(11).standard_normal(n)
+    K = max(1, args.steps)
+
+    def sample(s):
+        r0, r1 = s * n // K, (s + 1) * n // K
+        O.build_csr_rows(kind, nb, nu, nd, dets, one, two, r0, r1, nthreads=nthreads, h_v_w=hvw)
+        for _ in range(nmv * (s + 1) // K - nmv * s // K):
+            O.spmv(*csr, x, nthreads=nthreads)
+
+    for w in range(args.warmup):
+        sample(w % K)
     times = []
-    for _ in range(args.steps):
-        t, tb, ev = cpu_solve(nthreads)
-        times.append(t)
-    spr = statistics.median(times) / WORKLOAD["nroot"]
+    for s in range(K):
+        t0 = time.perf_counter()
+        sample(s)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    spr = total / nroot
     line = {"impl": "reference", "metric": METRIC, "value": spr, "unit": "s/root", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / K,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic seeded integrals", "config": {k: WORKLOAD[k] for k in ("workload",)},
+            "data": "synthetic seeded integrals (seed %d)" % WORKLOAD["seed"],
+            "config": workload_config(n, 2 * size - n, size, world),
             "cpu_baseline": {"value": spr, "unit": "s/root", "cores": nthreads, "kind": "port",
-                             "sample": "full workload per step: C oracle CSR build (restating "
-                                       "pyci/src/sparseop.cpp, %d threads) + ARPACK IRL on the oracle's "
-                                       "threaded SpMV, tol %.0e" % (nthreads, TOL)},
-            "e2e": {"value": spr, "unit": "s/root", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+                             "sample": "one full solve cut into %d samples, one per step: step s builds 1/%d of the "
+                                       "rows with the C oracle (restating pyci/src/sparseop.cpp, %d threads) and "
+                                       "applies the whole operator %d/%d of the %d times ARPACK's implicitly "
+                                       "restarted Lanczos needed (tol %.0e); value = sum of the step times / %d "
+                                       "roots" % (K, K, nthreads, 1, K, nmv, WORKLOAD.get("tol", TOL), nroot)},
+            "e2e": {"value": spr, "unit": "s/root", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "preparation": {"full_build_seconds": t_build_full, "full_arpack_seconds": t_solve_full,
+                            "arpack_products": nmv, "eigenvalues": list(evals + ecore)}}
     print(json.dumps(line), flush=True)
 
 
@@ -342,7 +432,7 @@ def run_ours(args, world, rank, local):
 
     # ---- CPU baseline sample (rank 0 only, N = 1)
     cpu = None
-    if rank == 0 and world == 1 and not args.skip_cpu and (fci or ndet < 10**6):
+    if rank == 0 and world == 1 and not args.skip_cpu:
         nthreads = os.cpu_count() or 1
         tcpu, tbuild, ev_cpu = cpu_solve(nthreads)
         cpu = {"value": tcpu / nroot, "unit": "s/root", "cores": nthreads, "kind": "port",
@@ -359,11 +449,7 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": value, "unit": "s/root", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic seeded integrals (seed %d)" % WORKLOAD["seed"],
-        "config": {"workload": WORKLOAD["workload"], "ndet": N, "nnz_stored": stored, "nnz_reference": size,
-                   "roots": nroot, "tol": tol,
-                   "l2": ("matrix (%.1f GB) >> 129 MB L2; no flush needed" % (bytes32 / 1e9)) if bytes32 > 2**28
-                   else "matrix (%.0f MB) fits in the 129 MB L2: SpMV figures are L2-resident" % (bytes32 / 1e6),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": workload_config(N, stored, size, world),
         "fp64": {"s_per_root": fp64_spr, "iterations": st64["iterations"], "matvecs": st64["matvecs"]},
         "speedup_mixed_vs_fp64": fp64_spr / (ms_step / 1e3 / nroot),
         "mixed": {"iterations": stats[-1]["iterations"], "matvecs": stats[-1]["matvecs"],
@@ -379,8 +465,7 @@ def run_ours(args, world, rank, local):
         "roofline": {"bound": "hbm", "achieved": gbs32, "peak": hbm, "unit": "GB/s", "frac": gbs32 / hbm,
                      "traffic": int(bytes32 * TRAFFIC_PER_ALGORITHMIC_BYTE) if fci else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel on "
-                                       "FullCI 11o 5a5b, scaled by entries processed "
-                                       "(profiles/spmm_sell_fci11_5a5b_ncu_full.md)" if fci else None,
+                                       "FullCI 11o 5a5b, scaled by entries processed" if fci else None,
                      "peak_source": peak_kind, "peak_note": "of measured" if peak_kind == "measured" else "of fallback",
                      "kernel": "FP32 k=4 SpMM, autotuned: spmm_sell_kernel (SELL-32, 4 or 1 warps per slice) "
                                "or a CSR spmm_kernel tile", "algorithmic_bytes": bytes32},

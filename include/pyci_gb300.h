@@ -146,15 +146,16 @@ int pyci_gpu_csr_matvec(const pyci_gpu_csr *csr, const double *x, double *y);
 
 /* y[nrow] = H x[ncol] in FP64 like pyci_gpu_csr_matvec, but without allocating
  * any device memory: x and y are staged in two fixed device arrays of
- * PYCI_GPU_NOALLOC_MAX_ROWS doubles each that the library keeps on every GPU
- * it is loaded on.  No counterpart in the reference (whose product runs on
- * the host); it is for callers that cannot allocate device memory -- a host
- * that gives the whole GPU to its own memory arena, code inside a CUDA-graph
- * stream capture, loops that cannot take an allocation's implicit
- * synchronisation.  Returns PYCI_GPU_EINVAL when nrow or ncol exceeds the
- * maximum.  The first call on a device looks up the arrays' addresses; make
- * it before any stream capture.  All calls on a device share the arrays:
- * calls that overlap on the GPU race, so serialise them. */
+ * PYCI_GPU_NOALLOC_MAX_ROWS doubles each (16 MiB together) that the library
+ * keeps on every GPU it is loaded on until the process exits.  No counterpart
+ * in the reference (whose product runs on the host); it is for callers that
+ * cannot let a library allocate device memory while they run -- a host whose
+ * own allocator has reserved the GPU's memory, or one that must know the
+ * library's device footprint in advance.  Returns PYCI_GPU_EINVAL when nrow
+ * or ncol exceeds the maximum.  The first call on a device looks up the
+ * arrays' device addresses (once per device); make it before any stream
+ * capture.  All calls on a device share the arrays: calls that overlap on the
+ * GPU race, so serialise them.  Synchronous, like pyci_gpu_csr_matvec. */
 int pyci_gpu_csr_matvec_noalloc(const pyci_gpu_csr *csr, const double *x, double *y);
 
 /* Y = H X on device buffers for k vectors stored interleaved ([ncol][k] and

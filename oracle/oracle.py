@@ -48,6 +48,12 @@ def lib():
         L.orc_csr_fill.restype = ctypes.c_int
         L.orc_csr_fill.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _i64, _i64,
                                    ctypes.c_int, _p, _p, _p, _p, _p, ctypes.c_int, _p, _p, _p]
+        L.orc_csr_count_rows.restype = ctypes.c_int
+        L.orc_csr_count_rows.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _i64, _i64, _i64,
+                                         ctypes.c_int, ctypes.c_int, _p]
+        L.orc_csr_fill_rows.restype = ctypes.c_int
+        L.orc_csr_fill_rows.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _i64, _i64, _i64,
+                                        ctypes.c_int, _p, _p, _p, _p, _p, ctypes.c_int, _p, _p, _p]
         for f in (L.orc_spmv_general, L.orc_spmv_sym_lower):
             f.restype = None
             f.argtypes = [_i64, _p, _p, _p, _p, _p, ctypes.c_int]
@@ -122,6 +128,30 @@ def build_csr(kind, nbasis, nocc_up, nocc_dn, dets, one_mo, two_mo, nrow=-1, nco
     if L.orc_csr_fill(*args, _ptr(one_mo), _ptr(two_mo), _ptr(h), _ptr(v), _ptr(w), nthreads,
                       _ptr(indptr), _ptr(indices), _ptr(data)):
         raise RuntimeError("orc_csr_fill failed")
+    return data, indices, indptr
+
+
+def build_csr_rows(kind, nbasis, nocc_up, nocc_dn, dets, one_mo, two_mo, row0, row1, ncol=-1,
+                   symmetric=True, nthreads=None, h_v_w=None):
+    r"""Rows [row0, row1) of build_csr's CSR (indptr local to the range)."""
+    L = lib()
+    dets = np.ascontiguousarray(dets, dtype=np.uint64)
+    ndet = dets.shape[0]
+    ncol = ndet if ncol < 0 else ncol
+    nthreads = nthreads or os.cpu_count() or 1
+    one_mo = np.ascontiguousarray(one_mo, dtype=np.float64)
+    two_mo = np.ascontiguousarray(two_mo, dtype=np.float64)
+    h, v, w = h_v_w if h_v_w is not None else senzero(one_mo, two_mo)
+    indptr = np.zeros(row1 - row0 + 1, dtype=np.int64)
+    args = (kind, nbasis, nocc_up, nocc_dn, ndet, _ptr(dets), row0, row1, ncol, int(bool(symmetric)))
+    if L.orc_csr_count_rows(*args, nthreads, _ptr(indptr)):
+        raise RuntimeError("orc_csr_count_rows failed")
+    nnz = int(indptr[-1])
+    indices = np.empty(nnz, dtype=np.int64)
+    data = np.empty(nnz, dtype=np.float64)
+    if L.orc_csr_fill_rows(*args, _ptr(one_mo), _ptr(two_mo), _ptr(h), _ptr(v), _ptr(w), nthreads,
+                           _ptr(indptr), _ptr(indices), _ptr(data)):
+        raise RuntimeError("orc_csr_fill_rows failed")
     return data, indices, indptr
 
 

@@ -272,6 +272,7 @@ typedef struct {
     double *data;
     det_index ix;
     int nthreads;
+    int64_t row0; /* first row of the range [row0, nrow); counts/indptr are indexed from it */
 } job;
 
 typedef struct {
@@ -559,7 +560,7 @@ static void *worker(void *p) {
     job *jb = wa->jb;
     rowbuf rb = {0, 0, NULL, NULL};
     const int64_t chunk = 64;
-    for (int64_t start = (int64_t)wa->tid * chunk; start < jb->nrow;
+    for (int64_t start = jb->row0 + (int64_t)wa->tid * chunk; start < jb->nrow;
          start += (int64_t)jb->nthreads * chunk) {
         int64_t end = start + chunk < jb->nrow ? start + chunk : jb->nrow;
         for (int64_t idet = start; idet < end; ++idet) {
@@ -571,10 +572,10 @@ static void *worker(void *p) {
             else
                 row_genci(jb, idet, &rb, wa->values);
             if (!wa->values) {
-                jb->counts[idet] = rb.n;
+                jb->counts[idet - jb->row0] = rb.n;
             } else {
                 sort_row(&rb);
-                int64_t off = jb->indptr[idet];
+                int64_t off = jb->indptr[idet - jb->row0];
                 memcpy(jb->indices + off, rb.col, sizeof(int64_t) * rb.n);
                 memcpy(jb->data + off, rb.val, sizeof(double) * rb.n);
             }
@@ -652,6 +653,50 @@ int orc_csr_fill(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int
     job jb;
     if (job_init(&jb, kind, nbasis, nocc_up, nocc_dn, ndet, dets, nrow, ncol, symmetric, nthreads))
         return -1;
+    jb.one_mo = one_mo;
+    jb.two_mo = two_mo;
+    jb.h = h;
+    jb.v = v;
+    jb.w = w;
+    jb.indptr = indptr;
+    jb.indices = indices;
+    jb.data = data;
+    int rc = run(&jb, 1);
+    free(jb.ix.slots);
+    return rc;
+}
+
+/* Rows [row0, row1) of the same CSR: the count and fill passes of
+ * orc_csr_count / orc_csr_fill restricted to a row range, with indptr local
+ * to the range (indptr[0] = 0, row0 + r at indptr[r]).  The timed CPU
+ * baseline builds one slice of a large operator per sample with these. */
+int orc_csr_count_rows(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                       const uint64_t *dets, int64_t row0, int64_t row1, int64_t ncol, int symmetric,
+                       int nthreads, int64_t *indptr) {
+    job jb;
+    if (row0 < 0 || row0 > row1 ||
+        job_init(&jb, kind, nbasis, nocc_up, nocc_dn, ndet, dets, row1, ncol, symmetric, nthreads))
+        return -1;
+    jb.row0 = row0;
+    jb.counts = indptr + 1;
+    int rc = run(&jb, 0);
+    free(jb.ix.slots);
+    indptr[0] = 0;
+    for (int64_t i = 0; i < row1 - row0; ++i)
+        indptr[i + 1] += indptr[i];
+    return rc;
+}
+
+int orc_csr_fill_rows(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                      const uint64_t *dets, int64_t row0, int64_t row1, int64_t ncol, int symmetric,
+                      const double *one_mo, const double *two_mo, const double *h, const double *v,
+                      const double *w, int nthreads, const int64_t *indptr, int64_t *indices,
+                      double *data) {
+    job jb;
+    if (row0 < 0 || row0 > row1 ||
+        job_init(&jb, kind, nbasis, nocc_up, nocc_dn, ndet, dets, row1, ncol, symmetric, nthreads))
+        return -1;
+    jb.row0 = row0;
     jb.one_mo = one_mo;
     jb.two_mo = two_mo;
     jb.h = h;

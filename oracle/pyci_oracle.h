@@ -47,6 +47,17 @@ int orc_csr_fill(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int
                  const double *w, int nthreads, const int64_t *indptr, int64_t *indices,
                  double *data);
 
+/* The same two passes for rows [row0, row1) only; indptr is local to the
+ * range (row1 - row0 + 1 entries, indptr[0] = 0). */
+int orc_csr_count_rows(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                       const uint64_t *dets, int64_t row0, int64_t row1, int64_t ncol, int symmetric,
+                       int nthreads, int64_t *indptr);
+int orc_csr_fill_rows(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet,
+                      const uint64_t *dets, int64_t row0, int64_t row1, int64_t ncol, int symmetric,
+                      const double *one_mo, const double *two_mo, const double *h, const double *v,
+                      const double *w, int nthreads, const int64_t *indptr, int64_t *indices,
+                      double *data);
+
 /* y = A x for a general CSR matrix. */
 void orc_spmv_general(int64_t nrow, const int64_t *indptr, const int64_t *indices,
                       const double *data, const double *x, double *y, int nthreads);

@@ -1,13 +1,16 @@
 // op(x) without any device allocation: pyci_gpu_csr_matvec_noalloc.
 //
-// pyci_gpu_csr_matvec stages x and y in device buffers it allocates per call.
-// Some callers cannot allocate device memory on the way: a host application
-// that hands the whole GPU to its own memory arena (cudaMalloc would fail or
-// fragment it), code running under a CUDA-graph stream capture (where
-// cudaMalloc is not a capturable operation), and latency-bound loops that
-// cannot afford the implicit synchronisation of allocation.  This variant
-// stages x and y in two file-scope device arrays instead, so it allocates
-// nothing; the operator's own CSR arrays are already resident.
+// pyci_gpu_csr_matvec stages x and y in device buffers it takes from the
+// device's stream-ordered memory pool on every call.  Some callers cannot let
+// a library allocate device memory while they run: a host application whose
+// own allocator (an arena or pool it manages itself) has reserved the GPU's
+// memory up front, so that an allocation made on its behalf fails or eats
+// into memory the application has planned for; or a deployment that must
+// know the library's whole device footprint before it starts.  This variant
+// stages x and y in two file-scope device arrays instead, so a call allocates
+// nothing; the operator's own arrays were allocated when it was built.  Like
+// the allocating call it copies x from and y to host memory and waits for
+// its stream before returning.
 //
 // Limits and sharing rules (also in include/pyci_gb300.h):
 //   * nrow and ncol must each be <= PYCI_GPU_NOALLOC_MAX_ROWS (2^20): the

@@ -36,7 +36,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REFROOT = os.environ.get("PYCI_REFERENCE", "/root/reference")
+REFROOT = os.environ.get("PYCI_REFERENCE", "")
+if not os.path.isdir(os.path.join(REFROOT, "pyci", "src")):
+    sys.exit("set PYCI_REFERENCE to the reference source tree (the one oracle/_ref was built from)")
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))

@@ -66,6 +66,22 @@ def test_oracle_csr_matches_reference(golden, case):
     np.testing.assert_allclose(y, ref["y"], rtol=1e-12, atol=1e-12)
 
 
+@pytest.mark.parametrize("kind,nb,nu,nd", [(O.FULLCI, 7, 3, 2), (O.DOCI, 10, 4, 4)])
+def test_oracle_row_range_build_concatenates_to_the_full_build(kind, nb, nu, nd):
+    # The CPU baseline builds a large operator in row slices; the slices must
+    # be exactly the rows of the whole build.
+    ecore, one, two = synthetic_integrals(nb, 17)
+    dets = O.all_dets(kind, nb, nu, nd)
+    data, indices, indptr = O.build_csr(kind, nb, nu, nd, dets, one, two)
+    n = dets.shape[0]
+    cuts = [0, 1, n // 3, n // 3, n - 5, n]
+    for r0, r1 in zip(cuts[:-1], cuts[1:]):
+        d, i, p = O.build_csr_rows(kind, nb, nu, nd, dets, one, two, r0, r1, nthreads=3)
+        assert np.array_equal(p, indptr[r0:r1 + 1] - indptr[r0])
+        assert np.array_equal(i, indices[indptr[r0]:indptr[r1]])
+        assert np.array_equal(d, data[indptr[r0]:indptr[r1]])
+
+
 @pytest.mark.parametrize("name", ["fci_8_4_4", "doci_24_6"])
 def test_oracle_workload_digest(golden, name):
     from digest import digest

@@ -1,10 +1,12 @@
 r"""op(x) through pyci_gpu_csr_matvec_noalloc, the entry point that stages x and
-y in the library's fixed device arrays instead of allocating device memory
-(for callers that cannot allocate: a host that owns the GPU's memory through
-its own arena, code under CUDA-graph stream capture, loops that cannot take
-an allocation's synchronisation).  Its output must match the allocating
-pyci_gpu_csr_matvec on consecutive calls, and sizes past the arrays' limit
-must be rejected.  Collected last on purpose."""
+y in the library's fixed device arrays instead of allocating device memory.
+It serves callers that cannot let a library allocate device memory while
+they run (a host whose own allocator has reserved the GPU's memory, or one
+that must know the library's device footprint in advance).  Its output must
+match the allocating pyci_gpu_csr_matvec on consecutive calls, a warm call
+must leave the device's free memory unchanged, and sizes past the arrays'
+limit must be rejected.  Collected last on purpose: if it fails, a run that
+stops at the first failure has already run every other test."""
 
 import numpy as np
 import pytest
@@ -38,6 +40,33 @@ def test_noalloc_matches_allocating_matvec(ctx, golden, case):
         y_noalloc = csr.matvec_noalloc(x)
         np.testing.assert_allclose(y_noalloc, y_alloc, rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(csr.matvec_noalloc(ref["x"]), ref["y"], rtol=1e-12, atol=1e-11)
+    csr.free()
+
+
+def _free_device_memory():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info(0)[0]
+
+
+def test_noalloc_allocates_no_device_memory(ctx):
+    # After a warm call (kernels loaded, product variant chosen), further calls
+    # must not change the device's free memory; the allocating matvec, by
+    # contrast, takes its x and y buffers from the device's memory pool.
+    from math import comb
+    from pyci_gb300.synth import synthetic_integrals
+    ecore, one, two = synthetic_integrals(10, 1010)
+    n = comb(10, 5) ** 2
+    csr = capi.Csr(ctx, capi.WFN_FULLCI, 10, 5, 5, None, one, two, flags=capi.BUILD_FULL_COLEX, ndet=n)
+    x = np.random.default_rng(5).normal(size=n)
+    y_ref = csr.matvec(x)
+    csr.matvec_noalloc(x)  # warm call
+    before = _free_device_memory()
+    for _ in range(3):
+        y = csr.matvec_noalloc(x)
+    after = _free_device_memory()
+    assert after == before, "free device memory changed by %d bytes" % (before - after)
+    np.testing.assert_allclose(y, y_ref, rtol=1e-12, atol=1e-12)
     csr.free()
 
 
