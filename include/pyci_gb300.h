@@ -219,6 +219,28 @@ int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_csr *const *
                          int64_t maxiter, double tol, const double *ecore, int mode, double *evals,
                          double *const *evecs, int64_t *iterations, pyci_gpu_solve_stats *stats);
 
+/* Storage forms an operator holds on the device (bit flags, diagnostic; no
+ * counterpart in the reference, whose operator is one host CSR):
+ * PYCI_STORE_FP64 FP64 CSR values, PYCI_STORE_SPLIT the exact FP32 high/low
+ * split in CSR order, PYCI_STORE_SELL the SELL-32 copy of the split,
+ * PYCI_STORE_IMPLICIT the implicit-column form of a full FullCI space
+ * (columns derived from per-string tables, values only). */
+#define PYCI_STORE_FP64 0x1
+#define PYCI_STORE_SPLIT 0x2
+#define PYCI_STORE_SELL 0x4
+#define PYCI_STORE_IMPLICIT 0x8
+int pyci_gpu_csr_storage(const pyci_gpu_csr *csr, int *flags);
+
+/* Kernel form the autotuner chose for the products of `precision` at width k
+ * (diagnostic for benchmarks; no counterpart in the reference):
+ * PYCI_FORM_CSR, PYCI_FORM_SELL, PYCI_FORM_IMPLICIT, or PYCI_FORM_UNTUNED
+ * before the operator's first such product. */
+#define PYCI_FORM_UNTUNED (-1)
+#define PYCI_FORM_CSR 0
+#define PYCI_FORM_SELL 1
+#define PYCI_FORM_IMPLICIT 2
+int pyci_gpu_csr_product_form(const pyci_gpu_csr *csr, int precision, int64_t k, int *form);
+
 /* Order-independent digest of the reference-layout CSR, for checking
  * full-size builds against a digest computed from the reference's arrays:
  *   pattern_sum = sum over stored (i, j) of mix64(i * 2^32 + j)  (mod 2^64)
@@ -271,8 +293,11 @@ int pyci_gpu_compute_enpt2(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t 
  * (host), coeffs f64[ndet].  DOCI: rdm1 = d0 f64[n][n], rdm2 = d2 f64[n][n];
  * FullCI: rdm1 = [aa, bb] f64[2][n][n], rdm2 = [aaaa, bbbb, abab]
  * f64[3][n][n][n][n] (host).  Same terms as the reference, summed with FP64
- * atomics (entries agree to rounding).  GenCI: EUNSUPPORTED (the reference's
- * GenCI compute_rdms writes past its output arrays). */
+ * atomics (entries agree to rounding).  GenCI: the spin-orbital RDMs from
+ * their definition, rdm1[p][q] = <a+_p a_q> f64[n][n] and rdm2[p][q][r][s] =
+ * <a+_p a+_q a_s a_r> f64[n][n][n][n] (the reference's GenCI compute_rdms,
+ * pyci/src/rdm.cpp:532-632, writes past its output arrays, so its result is
+ * undefined and is not reproduced). */
 int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                           int64_t ndet, const uint64_t *dets, const double *coeffs, double *rdm1, double *rdm2);
 
@@ -280,8 +305,9 @@ int pyci_gpu_compute_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t n
  * |dets2[j]> (compute_transition_rdms, pyci/src/rdm.cpp:634-902; binding
  * pyci/src/binding.cpp:1293-1340): same layouts as pyci_gpu_compute_rdms;
  * the reference's terms (each excitation of a determinant of 1 found in 2,
- * without the transposed partners), summed with FP64 atomics.  DOCI and
- * FullCI; GenCI is EUNSUPPORTED. */
+ * without the transposed partners), summed with FP64 atomics.  GenCI: the
+ * definition-based spin-orbital forms above, <1| ... |2> with wave function 1
+ * as the bra. */
 int pyci_gpu_compute_transition_rdms(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn,
                                      int64_t ndet1, const uint64_t *dets1, const double *coeffs1, int64_t ndet2,
                                      const uint64_t *dets2, const double *coeffs2, double *rdm1, double *rdm2);

@@ -69,6 +69,8 @@ def lib():
         L.orc_compute_enpt2.restype = ctypes.c_int
         L.orc_compute_enpt2.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+        L.orc_compute_rdms_genci.restype = ctypes.c_int
+        L.orc_compute_rdms_genci.argtypes = [_i64, _i64, _p, _p, _i64, _p, _p, _p, _p]
         L.orc_add_hci.restype = ctypes.c_int
         L.orc_add_hci.argtypes = [ctypes.c_int, _i64, _i64, _i64, _i64, _p, _p, _p, _p, ctypes.c_double, _i64, _p,
                                   ctypes.POINTER(_i64)]
@@ -246,6 +248,23 @@ def compute_enpt2(kind, nbasis, nocc_up, nocc_dn, dets, coeffs, one_mo, two_mo, 
                            _ptr(two_mo), float(energy), float(ecore), float(eps), ctypes.byref(out)):
         raise RuntimeError("orc_compute_enpt2 failed")
     return out.value
+
+
+def compute_rdms_genci(nbasis, dets1, coeffs1, dets2=None, coeffs2=None):
+    r"""Spin-orbital (rdm1 [n][n], rdm2 [n][n][n][n]) of a GenCI wave function
+    from their definition, <1| a+_p a_q |2> and <1| a+_p a+_q a_s a_r |2>
+    (the wave function itself when the second is omitted)."""
+    L = lib()
+    dets1 = np.ascontiguousarray(dets1, dtype=np.uint64)
+    coeffs1 = np.ascontiguousarray(coeffs1, dtype=np.float64)
+    dets2 = dets1 if dets2 is None else np.ascontiguousarray(dets2, dtype=np.uint64)
+    coeffs2 = coeffs1 if coeffs2 is None else np.ascontiguousarray(coeffs2, dtype=np.float64)
+    n = nbasis
+    r1, r2 = np.zeros((n, n)), np.zeros((n, n, n, n))
+    if L.orc_compute_rdms_genci(n, dets1.shape[0], _ptr(dets1), _ptr(coeffs1), dets2.shape[0], _ptr(dets2),
+                                _ptr(coeffs2), _ptr(r1), _ptr(r2)):
+        raise RuntimeError("orc_compute_rdms_genci failed")
+    return r1, r2
 
 
 def compute_transition_rdms(kind, nbasis, nocc_up, nocc_dn, dets1, coeffs1, dets2, coeffs2):

@@ -1228,6 +1228,118 @@ static int rdms_core(int kind, int64_t nbasis, int64_t ndet, const uint64_t *det
     return 0;
 }
 
+/* Spin-orbital RDMs of a GenCI wave function from their definition (no
+ * reference counterpart: the reference's GenCI compute_rdms,
+ * pyci/src/rdm.cpp:532-632, writes past its output arrays and repeats index
+ * factors, so its result is undefined):
+ *   rdm1[p][q] = sum_IJ c1_I c2_J <I| a+_p a_q |J>,
+ *   rdm2[p][q][r][s] = sum_IJ c1_I c2_J <I| a+_p a+_q a_s a_r |J>,
+ * n = nbasis spin orbitals; (dets1, c1) the bra, (dets2, c2) the ket (the
+ * same wave function for compute_rdms).  Ket-driven: every determinant J of
+ * the ket, each of its diagonal, single and double excitations I found in
+ * the bra, with the sign of the operator string applied to J (occupied
+ * orbitals below each acted orbital) and all antisymmetric images. */
+
+/* (-1)^(number of occupied orbitals below p). */
+static int below_sign(const uint64_t *d, int64_t p) {
+    int c = 0;
+    for (int64_t w = 0; w < (p >> 6); ++w)
+        c += __builtin_popcountll(d[w]);
+    const uint64_t m = (p & 63) ? (d[p >> 6] & ((1ULL << (p & 63)) - 1)) : 0;
+    c += __builtin_popcountll(m);
+    return (c & 1) ? -1 : 1;
+}
+
+static void flip_bit(uint64_t *d, int64_t p) { d[p >> 6] ^= 1ULL << (p & 63); }
+
+int orc_compute_rdms_genci(int64_t nbasis, int64_t ndet1, const uint64_t *dets1, const double *c1, int64_t ndet2,
+                           const uint64_t *dets2, const double *c2, double *rdm1, double *rdm2) {
+    const int64_t nword = orc_nword(nbasis), n1 = nbasis, n2 = n1 * n1, n3 = n1 * n2, n4 = n2 * n2;
+    if (nword > 4)
+        return -2;
+    det_index ix;
+    if (index_build(&ix, ndet1, nword, dets1))
+        return -1;
+    memset(rdm1, 0, sizeof(double) * n2);
+    memset(rdm2, 0, sizeof(double) * n4);
+    uint64_t det[4];
+    int64_t occ[256], vir[256];
+    for (int64_t jdet = 0; jdet < ndet2; ++jdet) {
+        const uint64_t *kdet = dets2 + jdet * nword;
+        const double cj = c2[jdet];
+        const int64_t no = fill_occs(nword, kdet, occ), nv = fill_virs(nword, n1, kdet, vir);
+        memcpy(det, kdet, sizeof(uint64_t) * nword);
+        int64_t idet = index_find(&ix, det);
+        if (idet != -1) {
+            const double v = c1[idet] * cj;
+            for (int64_t x = 0; x < no; ++x) {
+                const int64_t p = occ[x];
+                rdm1[p * (n1 + 1)] += v;
+                for (int64_t y = 0; y < no; ++y) {
+                    const int64_t q = occ[y];
+                    if (q == p)
+                        continue;
+                    rdm2[p * n3 + q * n2 + p * n1 + q] += v;
+                    rdm2[p * n3 + q * n2 + q * n1 + p] -= v;
+                }
+            }
+        }
+        for (int64_t x = 0; x < no; ++x) {
+            const int64_t i = occ[x];
+            for (int64_t y = 0; y < nv; ++y) {
+                const int64_t a = vir[y];
+                /* single: a+_a a_i J */
+                int sg = below_sign(det, i);
+                flip_bit(det, i);
+                sg *= below_sign(det, a);
+                flip_bit(det, a);
+                idet = index_find(&ix, det);
+                if (idet != -1) {
+                    const double v = c1[idet] * cj * sg;
+                    rdm1[a * n1 + i] += v;
+                    for (int64_t z = 0; z < no; ++z) {
+                        const int64_t k = occ[z];
+                        if (k == i)
+                            continue;
+                        rdm2[a * n3 + k * n2 + i * n1 + k] += v;
+                        rdm2[k * n3 + a * n2 + i * n1 + k] -= v;
+                        rdm2[a * n3 + k * n2 + k * n1 + i] -= v;
+                        rdm2[k * n3 + a * n2 + k * n1 + i] += v;
+                    }
+                }
+                flip_bit(det, a);
+                flip_bit(det, i);
+            }
+        }
+        /* doubles: a+_a a+_b a_j a_i J, i < j occupied, a < b virtual */
+        for (int64_t x = 0; x < no; ++x)
+            for (int64_t x2 = x + 1; x2 < no; ++x2)
+                for (int64_t y = 0; y < nv; ++y)
+                    for (int64_t y2 = y + 1; y2 < nv; ++y2) {
+                        const int64_t i = occ[x], j = occ[x2], a = vir[y], b = vir[y2];
+                        int sg = below_sign(det, i);
+                        flip_bit(det, i);
+                        sg *= below_sign(det, j);
+                        flip_bit(det, j);
+                        sg *= below_sign(det, b);
+                        flip_bit(det, b);
+                        sg *= below_sign(det, a);
+                        flip_bit(det, a);
+                        idet = index_find(&ix, det);
+                        if (idet != -1) {
+                            const double v = c1[idet] * cj * sg;
+                            rdm2[a * n3 + b * n2 + i * n1 + j] += v;
+                            rdm2[b * n3 + a * n2 + i * n1 + j] -= v;
+                            rdm2[a * n3 + b * n2 + j * n1 + i] -= v;
+                            rdm2[b * n3 + a * n2 + j * n1 + i] += v;
+                        }
+                        memcpy(det, kdet, sizeof(uint64_t) * nword);
+                    }
+    }
+    free(ix.slots);
+    return 0;
+}
+
 int orc_compute_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64_t nocc_dn, int64_t ndet, const uint64_t *dets,
                      const double *coeffs, double *rdm1, double *rdm2) {
     (void)nocc_up;

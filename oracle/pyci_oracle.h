@@ -85,6 +85,13 @@ int orc_compute_transition_rdms(int kind, int64_t nbasis, int64_t nocc_up, int64
                                 const uint64_t *dets1, const double *coeffs1, int64_t ndet2, const uint64_t *dets2,
                                 const double *coeffs2, double *rdm1, double *rdm2);
 
+/* Spin-orbital RDMs of a GenCI wave function from their definition:
+ * rdm1[p][q] = <1| a+_p a_q |2>, rdm2[p][q][r][s] = <1| a+_p a+_q a_s a_r |2>
+ * over nbasis spin orbitals (rdm1 n^2, rdm2 n^4); bra (dets1, c1), ket
+ * (dets2, c2), the same wave function for compute_rdms. */
+int orc_compute_rdms_genci(int64_t nbasis, int64_t ndet1, const uint64_t *dets1, const double *c1, int64_t ndet2,
+                           const uint64_t *dets2, const double *c2, double *rdm1, double *rdm2);
+
 /* Epstein-Nesbet second-order energy (compute_enpt2): energy + the sum over
  * determinants k outside the wave function of V_k^2 / (energy - ecore - H_kk),
  * V_k = sum of H_ki c_i over |H_ki| > eps / |c_i|.  DOCI through its FullCI

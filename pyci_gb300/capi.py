@@ -20,6 +20,8 @@ BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH = 0x1, 0x2, 0x4
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 GRAM_CUDA_CORES, GRAM_TENSOR_CORES = 0, 1
 PREC_FP64, PREC_FP32, PREC_FP64_SPLIT, PREC_FP64_DF = 0, 1, 2, 3
+STORE_FP64, STORE_SPLIT, STORE_SELL, STORE_IMPLICIT = 0x1, 0x2, 0x4, 0x8
+FORM_UNTUNED, FORM_CSR, FORM_SELL, FORM_IMPLICIT = -1, 0, 1, 2
 
 # Every symbol the header declares.
 SYMBOLS = [
@@ -29,7 +31,7 @@ SYMBOLS = [
     "pyci_gpu_csr_matvec", "pyci_gpu_csr_matvec_noalloc", "pyci_gpu_csr_spmm_device", "pyci_gpu_csr_prepare_mixed",
     "pyci_gpu_csr_solve", "pyci_gpu_batch_solve", "pyci_gpu_csr_digest", "pyci_gpu_add_all_dets",
     "pyci_gpu_gram_device", "pyci_gpu_add_hci", "pyci_gpu_compute_rdms", "pyci_gpu_compute_enpt2",
-    "pyci_gpu_compute_transition_rdms",
+    "pyci_gpu_compute_transition_rdms", "pyci_gpu_csr_storage", "pyci_gpu_csr_product_form",
 ]
 
 
@@ -70,6 +72,8 @@ def lib():
             "pyci_gpu_csr_free": (_int, [_p]),
             "pyci_gpu_csr_clone": (_int, [_p, ctypes.POINTER(_p)]),
             "pyci_gpu_csr_shape": (_int, [_p, _p, _p, _p, _p]),
+            "pyci_gpu_csr_storage": (_int, [_p, ctypes.POINTER(_int)]),
+            "pyci_gpu_csr_product_form": (_int, [_p, _int, _i64, ctypes.POINTER(_int)]),
             "pyci_gpu_csr_export": (_int, [_p, _p, _p, _p]),
             "pyci_gpu_csr_get_element": (_int, [_p, _i64, _i64, _p]),
             "pyci_gpu_csr_matvec": (_int, [_p, _p, _p]),
@@ -170,14 +174,11 @@ class Context:
             cap = n.value
 
     def compute_rdms(self, kind, nbasis, nocc_up, nocc_dn, dets, coeffs):
-        r"""(rdm1, rdm2) of a CI vector: DOCI (d0, d2) [n, n]; FullCI [2, n, n], [3, n, n, n, n]."""
+        r"""(rdm1, rdm2) of a CI vector: DOCI (d0, d2) [n, n]; FullCI [2, n, n], [3, n, n, n, n];
+        GenCI (definition-based, spin orbitals) [n, n], [n, n, n, n]."""
         dets = np.ascontiguousarray(dets, dtype=np.uint64)
         coeffs = np.ascontiguousarray(coeffs, dtype=np.float64)
-        n = nbasis
-        if kind == WFN_FULLCI:
-            r1, r2 = np.empty((2, n, n)), np.empty((3, n, n, n, n))
-        else:
-            r1, r2 = np.empty((n, n)), np.empty((n, n))
+        r1, r2 = _rdm_arrays(kind, nbasis)
         check(lib().pyci_gpu_compute_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets.shape[0], _ptr(dets),
                                           _ptr(coeffs), _ptr(r1), _ptr(r2)))
         return r1, r2
@@ -188,11 +189,7 @@ class Context:
         dets2 = np.ascontiguousarray(dets2, dtype=np.uint64)
         coeffs1 = np.ascontiguousarray(coeffs1, dtype=np.float64)
         coeffs2 = np.ascontiguousarray(coeffs2, dtype=np.float64)
-        n = nbasis
-        if kind == WFN_FULLCI:
-            r1, r2 = np.empty((2, n, n)), np.empty((3, n, n, n, n))
-        else:
-            r1, r2 = np.empty((n, n)), np.empty((n, n))
+        r1, r2 = _rdm_arrays(kind, nbasis)
         check(lib().pyci_gpu_compute_transition_rdms(self.handle, kind, nbasis, nocc_up, nocc_dn, dets1.shape[0],
                                                      _ptr(dets1), _ptr(coeffs1), dets2.shape[0], _ptr(dets2),
                                                      _ptr(coeffs2), _ptr(r1), _ptr(r2)))
@@ -215,6 +212,14 @@ class Context:
         out = np.zeros((p, q), dtype=np.float64)
         check(lib().pyci_gpu_gram_device(self.handle, method, a_ptr, p, b_ptr, q, n, _ptr(out)))
         return out
+
+
+def _rdm_arrays(kind, n):
+    if kind == WFN_FULLCI:
+        return np.empty((2, n, n)), np.empty((3, n, n, n, n))
+    if kind == WFN_GENCI:
+        return np.empty((n, n)), np.empty((n, n, n, n))
+    return np.empty((n, n)), np.empty((n, n))
 
 
 class Csr:
@@ -249,6 +254,22 @@ class Csr:
         v = [ctypes.c_int64() for _ in range(4)]
         check(lib().pyci_gpu_csr_shape(self.handle, *[ctypes.byref(x) for x in v]))
         return tuple(x.value for x in v)  # nrow, ncol, size, nnz_stored
+
+    def storage(self):
+        r"""Bit flags STORE_* of the forms the operator holds on the device."""
+        f = _int()
+        check(lib().pyci_gpu_csr_storage(self.handle, ctypes.byref(f)))
+        return f.value
+
+    def product_form(self, precision, k):
+        r"""FORM_* kernel form the autotuner chose for products of `precision` at width k."""
+        f = _int()
+        check(lib().pyci_gpu_csr_product_form(self.handle, precision, k, ctypes.byref(f)))
+        return f.value
+
+    def has_fcix(self):
+        r"""Whether the operator holds the implicit-column form of a full FullCI space."""
+        return bool(self.storage() & STORE_IMPLICIT)
 
     def export(self):
         nrow, ncol, size, _ = self.shape()

@@ -1174,6 +1174,47 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
     }
 }
 
+// Tables of the implicit-column form (fcix.cu) from the string tables: per
+// alpha string a, the targets of its singles and of its doubles in sorted
+// order, the CSR offsets of their groups in the sorted row, and the offset of
+// its own group (one thread per alpha string walks the sorted groups); the
+// beta lists (full: partners of the alpha string itself, sub: of an alpha
+// single) transposed to [position][string].
+__global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
+                                   int grp1, int ns, int nd, int32_t *atab, int32_t *bfull, int32_t *bsub) {
+    const int64_t n_f = static_cast<int64_t>(nbl) * nbeta, n_s = static_cast<int64_t>(grp1) * nbeta;
+    const int64_t total = nalpha + n_f + n_s;
+    const int w = 2 * (ns + nd) + 1;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (i < nalpha) {
+            int32_t *row = atab + i * w;
+            int is = 0, id = 0;
+            for (int g = 0; g < na; ++g) {
+                const int ty = TA.val[i * TA.npad + g] >> 20;
+                const int32_t key = TA.key[i * TA.npad + g], off = TA.off[i * TA.npad + g];
+                if (ty == 1 && is < ns) {
+                    row[is] = key;
+                    row[ns + nd + is] = off;
+                    ++is;
+                } else if (ty == 2 && id < nd) {
+                    row[ns + id] = key;
+                    row[2 * ns + nd + id] = off;
+                    ++id;
+                } else if (ty == 0) {
+                    row[w - 1] = off;
+                }
+            }
+        } else if (i < nalpha + n_f) {
+            const int64_t j = i - nalpha, q = j / nbeta, b = j - q * nbeta;
+            bfull[j] = TB.key[b * TB.npad + q];
+        } else {
+            const int64_t j = i - nalpha - n_f, q = j / nbeta, b = j - q * nbeta;
+            bsub[j] = TB.sub[b * TB.npad + q];
+        }
+    }
+}
+
 // Insert every determinant index into the table (linear probing).
 template<int NWT>
 __global__ void table_insert_kernel(int32_t *slots, uint64_t mask, const uint64_t *dets,
@@ -1540,6 +1581,59 @@ int pick_nw(int64_t nbasis) {
     return 0;
 }
 
+// Keeps the implicit-column tables of a full FullCI space when its beta
+// string count pads to a multiple of 32 with at most 1/4 extra rows (the
+// padding rows are streamed as zeros, still fewer bytes than int32 columns).
+// Tables only: the values are written by pyci_gpu_csr_prepare_mixed.
+int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, const StringTables &TB, int64_t nalpha,
+                int64_t nbeta, int na, int nbl, int grp1, int64_t len) {
+    cudaStream_t st = ctx->stream;
+    const int64_t nbp = (nbeta + 31) / 32 * 32;
+    const int ns = TA.n1, nd = TA.n2;
+    if (nbeta < 32 || nbeta >= 65536 || 4 * (nbp - nbeta) > nbeta || len <= 0 || len > (1 << 20) ||
+        !csr->symmetric || na != 1 + ns + nd ||
+        len != static_cast<int64_t>(nbl) + static_cast<int64_t>(ns) * grp1 + nd)
+        return PYCI_GPU_OK;
+    auto up4 = [](int64_t v) { return (v + 3) / 4 * 4; };
+    // Sections padded to multiples of 4 entries, and each group of section B
+    // too (a 4-entry packet never spans two alpha targets).
+    const int la = static_cast<int>(up4(nbl)), lb = static_cast<int>(ns * up4(grp1)), lc = static_cast<int>(up4(nd));
+    const int w = 2 * (ns + nd) + 1;
+    const size_t sa = sizeof(int32_t) * nalpha * w, sf = sizeof(int32_t) * nbl * nbeta,
+                 ss = sizeof(int32_t) * grp1 * nbeta;
+    int32_t *atab = nullptr, *bfull = nullptr, *bsub = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&atab), sa, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&bfull), sf, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&bsub), ss, st);
+    if (e != cudaSuccess) {
+        for (int32_t *q : {atab, bfull, bsub})
+            if (q)
+                cudaFreeAsync(q, st);
+        return cuda_status(e, "cudaMallocAsync (implicit-column tables)");
+    }
+    const int64_t total = nalpha + (static_cast<int64_t>(nbl) + grp1) * nbeta;
+    fcix_tables_kernel<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
+        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, atab, bfull, bsub);
+    ::pyci_gpu::note_launch();
+    csr->fx_nalpha = nalpha;
+    csr->fx_nbeta = nbeta;
+    csr->fx_nbp = nbp;
+    csr->fx_ns = ns;
+    csr->fx_nd = nd;
+    csr->fx_nlb = nbl;
+    csr->fx_nls = grp1;
+    csr->fx_la = la;
+    csr->fx_lb = lb;
+    csr->fx_lc = lc;
+    csr->fx_npk = (la + lb + lc) / 4;
+    csr->fx_atab = atab;
+    csr->fx_bfull = bfull;
+    csr->fx_bsub = bsub;
+    return PYCI_GPU_OK;
+}
+
 template<int NW>
 int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len,
               bool sorted_fci, bool warp_doci) {
@@ -1676,6 +1770,8 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
                     ::pyci_gpu::note_launch();
             }
         }
+        if (!rc)
+            rc = fcix_tables(ctx, csr, TA, TB, nstr_a, nstr_b, na, nbl, grp1, uniform_len);
         for (void *m : mem)
             cudaFreeAsync(m, st);
         if (rc)

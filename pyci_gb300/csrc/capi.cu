@@ -37,13 +37,24 @@ int cuda_status(cudaError_t err, const char *what) {
     return PYCI_GPU_ECUDA;
 }
 
+// Drops the implicit-column arrays from a handle (their memory is owned
+// elsewhere or already freed).
+static void fx_forget(pyci_gpu_csr *csr) {
+    csr->fx_atab = csr->fx_bfull = csr->fx_bsub = nullptr;
+    csr->fx_hi = csr->fx_lo = nullptr;
+    csr->fx_nalpha = csr->fx_nbeta = csr->fx_nbp = csr->fx_npk = 0;
+    csr->fx_ns = csr->fx_nd = csr->fx_nlb = csr->fx_nls = 0;
+    csr->fx_la = csr->fx_lb = csr->fx_lc = 0;
+}
+
 void csr_release(pyci_gpu_csr *csr) {
     if (!csr || !csr->ctx)
         return;
     cudaStream_t st = csr->ctx->stream;
     void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
                     csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals,
-                    csr->sell_lo};
+                    csr->sell_lo,    csr->fx_atab,  csr->fx_bfull, csr->fx_bsub,   csr->fx_hi,
+                    csr->fx_lo};
     for (void *p : ptrs)
         if (p)
             cudaFreeAsync(p, st);
@@ -60,6 +71,7 @@ void csr_release(pyci_gpu_csr *csr) {
     csr->sell_vals = nullptr;
     csr->sell_lo = nullptr;
     csr->nslice = csr->sell_nnz = 0;
+    fx_forget(csr);
 }
 
 extern "C" {
@@ -243,6 +255,7 @@ int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
     next.sell_vals = nullptr;
     next.sell_lo = nullptr;
     next.nslice = next.sell_nnz = 0;
+    fx_forget(&next);
     next.flags = flags;
     next.ndet = ndet;
     next.nrow = ndet;
@@ -295,6 +308,9 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     c->sell_cols = nullptr;
     c->sell_vals = nullptr;
     c->sell_lo = nullptr;
+    c->fx_atab = c->fx_bfull = c->fx_bsub = nullptr;
+    c->fx_hi = c->fx_lo = nullptr;
+    const int64_t fx_vals = csr->fx_nalpha * (csr->fx_nbp / 32) * csr->fx_npk * 128;
     struct Item {
         void *src;
         void **dst;
@@ -312,6 +328,11 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         {csr->sell_cols, reinterpret_cast<void **>(&c->sell_cols), sizeof(int32_t) * csr->sell_nnz},
         {csr->sell_vals, reinterpret_cast<void **>(&c->sell_vals), sizeof(float) * csr->sell_nnz},
         {csr->sell_lo, reinterpret_cast<void **>(&c->sell_lo), sizeof(float) * csr->sell_nnz},
+        {csr->fx_atab, reinterpret_cast<void **>(&c->fx_atab), sizeof(int32_t) * csr->fx_nalpha * fx_atab_width(csr)},
+        {csr->fx_bfull, reinterpret_cast<void **>(&c->fx_bfull), sizeof(int32_t) * csr->fx_nlb * csr->fx_nbeta},
+        {csr->fx_bsub, reinterpret_cast<void **>(&c->fx_bsub), sizeof(int32_t) * csr->fx_nls * csr->fx_nbeta},
+        {csr->fx_hi, reinterpret_cast<void **>(&c->fx_hi), sizeof(float) * fx_vals},
+        {csr->fx_lo, reinterpret_cast<void **>(&c->fx_lo), sizeof(float) * fx_vals},
     };
     for (auto &it : items) {
         if (!it.src)
@@ -332,6 +353,16 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         return cuda_status(e, "clone");
     }
     *out = c;
+    return PYCI_GPU_OK;
+}
+
+int pyci_gpu_csr_storage(const pyci_gpu_csr *csr, int *flags) {
+    if (!csr || !flags) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    *flags = (csr->vals ? PYCI_STORE_FP64 : 0) | (csr->hi && csr->lo ? PYCI_STORE_SPLIT : 0) |
+             (csr->sell_cols ? PYCI_STORE_SELL : 0) | (csr->fx_hi ? PYCI_STORE_IMPLICIT : 0);
     return PYCI_GPU_OK;
 }
 

@@ -121,9 +121,11 @@ __device__ __forceinline__ void store_rows(T *__restrict__ p, const T (&v)[R]) {
 }
 
 // Row-streaming Gram product: block (x, y) sums A[i][r] * B[j][r] over a
-// grid-stride set of rows for i in [y * PI, y * PI + PI), j < q <= QC, with
-// a per-thread PI x QC register tile (one coalesced pass over the rows), then
-// reduces across the block; partial[x][i * q + j].  QC is the smallest of
+// grid-stride set of rows (row blocks along y) for i in [x * PI, x * PI + PI),
+// j < q <= QC, with a per-thread PI x QC register tile (one coalesced pass
+// over the rows), then reduces across the block; partial[y][i * q + j].  The
+// vector blocks of one row range are neighbouring block indices (x fastest),
+// so they run together and B's rows, read by each of them, come from L2.  QC is the smallest of
 // 1, 2, 4, 8 that holds q, so the tile (and the register count) follows q.
 // R > 1: each thread step takes R consecutive rows with 16-byte loads (N a
 // multiple of R, vectors 16-byte aligned), R times the bytes in flight per
@@ -131,7 +133,7 @@ __device__ __forceinline__ void store_rows(T *__restrict__ p, const T (&v)[R]) {
 template<typename T, int PI, int QC, int R>
 __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
                                                         int q, int64_t N, double *__restrict__ partial) {
-    const int i0 = blockIdx.y * PI;
+    const int i0 = blockIdx.x * PI;
     const int ni = min(PI, p - i0);
     T acc[PI][QC];
 #pragma unroll
@@ -140,8 +142,8 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
         for (int j = 0; j < QC; ++j)
             acc[ii][j] = T(0);
     const int64_t nu = N / R;
-    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
-         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    for (int64_t u = blockIdx.y * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
+         u += static_cast<int64_t>(gridDim.y) * blockDim.x) {
         const int64_t r = u * R;
         T bv[QC][R];
 #pragma unroll
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
         double v = 0.0;
         for (int w = 0; w < nwarps; ++w)
             v += red[w][ii * QC + j];
-        partial[static_cast<int64_t>(blockIdx.x) * p * q + (i0 + ii) * q + j] = v;
+        partial[static_cast<int64_t>(blockIdx.y) * p * q + (i0 + ii) * q + j] = v;
     }
 }
 
@@ -215,7 +217,7 @@ unsigned launch_gram_tile(unsigned budget, cudaStream_t st, const T *A, int p, c
     const unsigned gy = static_cast<unsigned>((p + PI - 1) / PI);
     const unsigned nb = static_cast<unsigned>(
         std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(1, wave / gy), (N / R + 255) / 256)));
-    gram_rows_kernel<T, PI, QC, R><<<dim3(nb, gy), 256, 0, st>>>(A, p, B, q, N, partial);
+    gram_rows_kernel<T, PI, QC, R><<<dim3(gy, nb), 256, 0, st>>>(A, p, B, q, N, partial);
     return nb;
 }
 
@@ -482,7 +484,12 @@ public:
     // converge and are returned (the rest are buffer vectors).
     Davidson(pyci_gpu_csr *csr, int64_t nroot, int64_t nwant, int64_t mmax, bool mixed)
         : csr_(csr), st_(csr->ctx->stream), N_(csr->nrow), nroot_(nroot), nwant_(nwant), mmax_(mmax),
-          mixed_(mixed) {}
+          mixed_(mixed) {
+        // PYCI_GPU_FP64_PRODUCT=native keeps FP64 arithmetic in the FP64
+        // solve's products even when the split is there.
+        const char *e = std::getenv("PYCI_GPU_FP64_PRODUCT");
+        fp64_df_ = !mixed && csr->hi && csr->lo && !csr->lower_only && !(e && !std::strcmp(e, "native"));
+    }
 
     ~Davidson() {
         for (void *p : allocs_)
@@ -601,16 +608,26 @@ private:
 
     // W[0..k) = H V[0..k) (storage precision of T; FP64 uses f64 values).
     int apply(const T *V, int k, T *W, int prec) {
-        // On the SELL-32 copy the FP32 product streams the matrix once per
-        // launch and is bound by that stream, so up to 8 vectors share one
-        // launch (a 5-vector block as one product padded to 8, not 4 + 1).
-        const int chunk = (prec == PYCI_PREC_FP32 && csr_->sell_cols) ? kMaxQ : kSpmmChunk;
+        // On the SELL-32 copy or the implicit-column form the FP32 product
+        // streams the matrix once per launch and is bound by that stream, so
+        // up to 8 vectors share one launch (a 5-vector block as one product
+        // padded to 8, not 4 + 1).  FP64 solves on an operator that holds the
+        // exact high/low split multiply in double-float arithmetic.
+        const int chunk = (prec == PYCI_PREC_FP32 && (csr_->sell_cols || csr_->fx_hi)) ? kMaxQ : kSpmmChunk;
         for (int j0 = 0; j0 < k; j0 += chunk) {
             const int kk = std::min(chunk, k - j0);
             const int kp = padded_width(kk);
-            pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_), ::pyci_gpu::note_launch();
+            const bool df = std::is_same<T, double>::value && fp64_df_;
+            if (df)
+                pack_split_kernel<<<grid(N_), 256, 0, st_>>>(reinterpret_cast<const double *>(V) + static_cast<int64_t>(j0) * N_,
+                                                             N_, kk, kp, reinterpret_cast<float *>(Xi_)),
+                    ::pyci_gpu::note_launch();
+            else
+                pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_),
+                    ::pyci_gpu::note_launch();
             const size_t tk = timer_begin();
-            int rc = csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
+            int rc = df ? csr_spmm_df(csr_, kp, reinterpret_cast<const float *>(Xi_), reinterpret_cast<double *>(Yi_), st_)
+                        : csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
             if (rc)
                 return rc;
             timer_end(tk);
@@ -700,6 +717,12 @@ private:
     int64_t matvecs_ = 0, matvecs64_ = 0;
     unsigned gram_blocks_ = 1;
     T *Xi_ = nullptr, *Yi_ = nullptr, *Sb_ = nullptr;
+    // FP64 solves: products in double-float arithmetic on the exact
+    // high/low split (FP32 instructions, ~2^-44 relative) when the operator
+    // holds the split.  GB300's FP64 rate bounds a 4-vector product with
+    // FP64 arithmetic at 4 FMAs per stored entry / (FP64 FMA rate), several
+    // times the time the same product takes to stream its bytes.
+    bool fp64_df_ = false;
     double *d_partial_ = nullptr, *d_small_ = nullptr;
 };
 

@@ -1,0 +1,426 @@
+// Implicit-column products for full FullCI spaces ("FCIX" form of the
+// operator), part of SparseOp::perform_op (pyci/src/sparseop.cpp:96-112).
+//
+// In a full FullCI space of colex-ranked strings, determinant (a, b) is row
+// a * nbeta + b, and its row holds exactly these entries
+// (pyci/src/sparseop.cpp:260-427 keeps all of them for a full space):
+//   A: (a, b') for b' in {b} + singles(b) + doubles(b)   (diagonal, beta excitations)
+//   B: (a', b') for a' in singles(a), b' in {b} + singles(b)  (alpha singles, opposite-spin doubles)
+//   C: (a', b) for a' in doubles(a)                       (alpha doubles)
+// with column a' * nbeta + b'.  Every column is thus a function of small
+// per-string tables, and a product streams the values only: 4 bytes per
+// entry in FP32 and 8 for FP64-accurate products from the exact high/low
+// split, against 8 and 12 with int32 columns.
+//
+// Layout.  A row is stored as its sections A, B, C; A and C are padded to a
+// multiple of 4 entries and every group of B (one alpha single) to a
+// multiple of 4 (padding: zero values).  Inside a section the entries follow
+// the sorted target lists.  Rows are grouped by alpha string with the beta
+// count padded to a multiple of 32 (nbp); lane l of slice s holds row (a, b),
+// a = s / (nbp / 32), b = 32 (s mod (nbp / 32)) + l (rows with b >= nbeta
+// are padding: zero values, computed with b = nbeta - 1 and not written).
+// Values travel in packets of 4 consecutive entries: entry t of lane l in
+// slice s sits at ((s * npk + t / 4) * 32 + l) * 4 + t mod 4, so a lane's
+// 16-byte load brings 4 entries and a warp's 512 contiguous bytes.
+//
+// Product.  One block serves the slices of one alpha string a (or a part of
+// them), one warp per slice.  Section A reads x's block of rows a * nbeta ..
+// a * nbeta + nbeta - 1 and each group of section B the block of its alpha
+// target: the block stages these x blocks in shared memory one at a time
+// (cp.async, double-buffered, the next block in flight while the current
+// group is multiplied), so the scattered beta gathers of A and B hit shared
+// memory instead of missing L1 towards L2.  Section C's gathers (rows
+// a' * nbeta + b for 32 consecutive b) are coalesced global loads.  Each warp
+// keeps its lanes' section-B partner lists in shared memory.
+//
+// Tables (L1/L2-resident): atab[a] = the targets of a's singles and doubles
+// (sorted), their groups' offsets in the sorted CSR row and that of a's own
+// group (for the fill from the CSR); bfull[p][b] and bsub[p][b], the sorted
+// beta lists, transposed so the 32 lanes of a slice read consecutive words.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cstdint>
+
+#include "internal.h"
+#include "split_bits.h"
+
+namespace pyci_gpu {
+
+struct FxArgs {
+    int64_t nslice, spa, nbeta, npk;
+    int ns, nd, nlb, nls, nlsp, la, lb, lc, aw;
+    int parts;     // blocks per alpha string
+    int xblk;      // floats of one staged x block (nbeta rows, padded to 4)
+    const int32_t *atab, *bfull, *bsub;
+    const float4 *hi, *lo;
+};
+
+// Double-float term (vh + vl)(xh + xl) added to (s, c): p = fl(vh xh), its
+// exact error fma(vh, xh, -p), the small products vh xl + vl xh in FP32, p
+// added with TwoSum (the same arithmetic as the CSR double-float kernels).
+__device__ __forceinline__ void fx_two_sum(float &s, float &c, float p) {
+    const float u = __fadd_rn(s, p);
+    const float z = __fadd_rn(u, -s);
+    const float d = __fadd_rn(__fadd_rn(s, -__fadd_rn(u, -z)), __fadd_rn(p, -z));
+    s = u;
+    c = __fadd_rn(c, d);
+}
+
+template<int K>
+__device__ __forceinline__ void fx_df_term(float vh, float vl, const float xh[K], const float xl[K], float s[K],
+                                           float c[K]) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const float p = __fmul_rn(vh, xh[k]);
+        const float err = fmaf(vh, xh[k], -p);
+        const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
+        fx_two_sum(s[k], c[k], p);
+        c[k] = __fadd_rn(c[k], t);
+    }
+}
+
+// One entry whose x row is at xr (shared or global memory): accumulate
+// value (vh, vl) times that row.
+template<int MODE, int K>
+__device__ __forceinline__ void fx_acc(const float *xr, float vh, float vl, float acc[K], float cc[K]) {
+    if constexpr (MODE == 0) {
+        float xv[K];
+        if constexpr (K % 4 == 0) {
+#pragma unroll
+            for (int v = 0; v < K / 4; ++v) {
+                const float4 q = reinterpret_cast<const float4 *>(xr)[v];
+                xv[4 * v] = q.x, xv[4 * v + 1] = q.y, xv[4 * v + 2] = q.z, xv[4 * v + 3] = q.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                xv[k] = xr[k];
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            acc[k] = fmaf(vh, xv[k], acc[k]);
+    } else {
+        float xh[K], xl[K];
+        if constexpr (K == 4) {
+            const float4 a = reinterpret_cast<const float4 *>(xr)[0];
+            const float4 b = reinterpret_cast<const float4 *>(xr)[1];
+            xh[0] = a.x, xh[1] = a.y, xh[2] = a.z, xh[3] = a.w;
+            xl[0] = b.x, xl[1] = b.y, xl[2] = b.z, xl[3] = b.w;
+        } else if constexpr (K == 2) {
+            const float4 a = reinterpret_cast<const float4 *>(xr)[0];
+            xh[0] = a.x, xh[1] = a.y, xl[0] = a.z, xl[1] = a.w;
+        } else {
+            const float2 a = reinterpret_cast<const float2 *>(xr)[0];
+            xh[0] = a.x, xl[0] = a.y;
+        }
+        fx_df_term<K>(vh, vl, xh, xl, acc, cc);
+    }
+}
+
+// Asynchronous copy of n floats from global src to shared dst by the whole
+// block (16-byte pieces when both ends and n allow it, 4-byte otherwise).
+__device__ __forceinline__ void fx_stage(float *dst, const float *src, int n) {
+    const unsigned sbase = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    if (((reinterpret_cast<uintptr_t>(src) | sbase) & 15) == 0 && (n & 3) == 0) {
+        for (int i = threadIdx.x; i < n / 4; i += blockDim.x)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sbase + 16 * i), "l"(src + 4 * i));
+    } else {
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sbase + 4 * i), "l"(src + i));
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+}
+
+__device__ __forceinline__ void fx_stage_wait() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Shared memory of one block: two staged x blocks, the alpha targets times
+// nbeta (singles then doubles), and per warp its lanes' section-B partner
+// lists (16-bit: nbeta < 65536).
+__host__ __device__ inline size_t fx_smem_bytes(int xblk, int ns, int nd, int nlsp, int warps) {
+    return sizeof(float) * 2 * static_cast<size_t>(xblk) + sizeof(int) * static_cast<size_t>(ns + nd + 3) / 4 * 4 +
+           sizeof(uint16_t) * static_cast<size_t>(warps) * nlsp * 32;
+}
+
+// MODE 0: FP32 values, x [N][K], y [N][K] float (FP32 accumulation).
+// MODE 2: double-float, xs float [N][2K] (high parts then low parts of a
+// row), y double [N][K].  Block (a, h) serves slices [h spa / parts,
+// (h + 1) spa / parts) of alpha string a, one warp per slice.
+template<int MODE, int K>
+__global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float *__restrict__ x,
+                                                           void *__restrict__ yv) {
+    constexpr int XW = MODE == 2 ? 2 * K : K; // floats per x row
+    extern __shared__ __align__(16) unsigned char fx_dyn[];
+    float *xb0 = reinterpret_cast<float *>(fx_dyn);
+    float *xb1 = xb0 + A.xblk;
+    int *aT = reinterpret_cast<int *>(xb1 + A.xblk);
+    uint16_t *jbS = reinterpret_cast<uint16_t *>(aT + (A.ns + A.nd + 3) / 4 * 4);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nbeta = static_cast<int>(A.nbeta);
+    const int64_t a = blockIdx.x / A.parts;
+    const int h = static_cast<int>(blockIdx.x - a * A.parts);
+    const int64_t sb = a * A.spa + h * A.spa / A.parts, se = a * A.spa + (h + 1) * A.spa / A.parts;
+    const int64_t s = sb + warp;
+    const bool active = s < se;
+    const int bb = static_cast<int>((s - a * A.spa) * 32) + lane;
+    const int b = bb < nbeta ? bb : nbeta - 1;
+    const int self = static_cast<int>(a) * nbeta;
+    const int32_t *arow = A.atab + a * A.aw;
+    for (int i = threadIdx.x; i < A.ns + A.nd; i += blockDim.x)
+        aT[i] = __ldg(arow + i) * nbeta;
+    uint16_t *mj = jbS + warp * A.nlsp * 32;
+    if (active)
+        for (int p = 0; p < A.nls; ++p)
+            mj[p * 32 + lane] = static_cast<uint16_t>(__ldg(A.bsub + static_cast<int64_t>(p) * nbeta + b));
+    fx_stage(xb0, x + static_cast<int64_t>(self) * XW, nbeta * XW);
+    fx_stage_wait();
+    __syncthreads();
+    if (A.ns > 0)
+        fx_stage(xb1, x + static_cast<int64_t>(aT[0]) * XW, nbeta * XW);
+    float acc[K], cc[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+        acc[k] = cc[k] = 0.0f;
+    const float4 *hp = A.hi + s * A.npk * 32 + lane;
+    const float4 *lp = A.lo + s * A.npk * 32 + lane;
+    // Section A: (a, every beta partner of b), x block a in xb0.
+    if (active) {
+        const int *tb = A.bfull + b;
+        for (int q = 0; q < A.la / 4; ++q) {
+            const float4 vh = __ldcs(hp + 32 * q);
+            const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
+            const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int t = 4 * q + u;
+                const int jb = t < A.nlb ? __ldg(tb + static_cast<int64_t>(t) * nbeta) : b;
+                fx_acc<MODE, K>(xb0 + jb * XW, h4[u], l4[u], acc, cc);
+            }
+        }
+    }
+    // Section B: group g = alpha single g, x block of its target staged.
+    const int qb = A.la / 4, gq = A.nlsp / 4;
+    for (int g = 0; g < A.ns; ++g) {
+        float *cur = (g & 1) ? xb0 : xb1;
+        fx_stage_wait();
+        __syncthreads(); // block g staged; nobody still reads the other buffer
+        if (g + 1 < A.ns)
+            fx_stage((g & 1) ? xb1 : xb0, x + static_cast<int64_t>(aT[g + 1]) * XW, nbeta * XW);
+        if (active) {
+            for (int qq = 0; qq < gq; ++qq) {
+                const int q = qb + g * gq + qq;
+                const float4 vh = __ldcs(hp + 32 * q);
+                const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
+                const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int p = 4 * qq + u;
+                    const int jb = p < A.nls ? mj[p * 32 + lane] : b;
+                    fx_acc<MODE, K>(cur + jb * XW, h4[u], l4[u], acc, cc);
+                }
+            }
+        }
+    }
+    // Section C: (alpha double, b), coalesced global gathers.
+    if (active) {
+        const int qc = (A.la + A.lb) / 4;
+        for (int q = qc; q < A.npk; ++q) {
+            const float4 vh = __ldcs(hp + 32 * q);
+            const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
+            const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int tt = 4 * (q - qc) + u;
+                const int col = (tt < A.nd ? aT[A.ns + tt] : self) + b;
+                fx_acc<MODE, K>(x + static_cast<int64_t>(col) * XW, h4[u], l4[u], acc, cc);
+            }
+        }
+        if (bb < nbeta) {
+            const int64_t row = static_cast<int64_t>(self) + bb;
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                if constexpr (MODE == 0)
+                    static_cast<float *>(yv)[row * K + k] = acc[k];
+                else
+                    static_cast<double *>(yv)[row * K + k] = static_cast<double>(acc[k]) + static_cast<double>(cc[k]);
+            }
+        }
+    }
+}
+
+// FCIX values from the FP64 CSR (sorted rows of uniform length len): one
+// block per (slice, 32 packets) stages the 32 rows' 128 entries in shared
+// memory, read from the CSR through the section -> sorted-position map of
+// the row's alpha string (atab offsets), splits them exactly (split_bits.h)
+// and writes the packets with coalesced 16-byte stores.
+__global__ void __launch_bounds__(256) fcix_fill_kernel(FxArgs A, int len, const double *__restrict__ vals,
+                                                        float4 *__restrict__ hi, float4 *__restrict__ lo) {
+    __shared__ double tile[32][129];
+    const int64_t chunks = (A.npk + 31) / 32;
+    for (int64_t blk = blockIdx.x; blk < A.nslice * chunks; blk += gridDim.x) {
+        const int64_t s = blk / chunks, qc = blk - s * chunks;
+        const int64_t a = s / A.spa;
+        const int64_t b0 = (s - a * A.spa) * 32;
+        const int64_t t0 = qc * 128;
+        const int32_t *arow = A.atab + a * A.aw;
+        for (int i = threadIdx.x; i < 32 * 128; i += blockDim.x) {
+            const int l = i >> 7, e = i & 127;
+            const int64_t b = b0 + l;
+            const int t = static_cast<int>(t0 + e);
+            int pos = -1; // sorted position in the row
+            if (t < A.la) {
+                if (t < A.nlb)
+                    pos = __ldg(arow + A.aw - 1) + t;
+            } else if (t < A.la + A.lb) {
+                const int tt = t - A.la, g = tt / A.nlsp, p = tt - g * A.nlsp;
+                if (g < A.ns && p < A.nls)
+                    pos = __ldg(arow + A.ns + A.nd + g) + p;
+            } else if (t < A.la + A.lb + A.lc) {
+                const int tt = t - A.la - A.lb;
+                if (tt < A.nd)
+                    pos = __ldg(arow + 2 * A.ns + A.nd + tt);
+            }
+            double v = 0.0;
+            if (b < A.nbeta && pos >= 0)
+                v = __ldcs(vals + (a * A.nbeta + b) * static_cast<int64_t>(len) + pos);
+            tile[l][e] = v;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+            const int pq = i >> 5, l = i & 31;
+            const int64_t q = qc * 32 + pq;
+            if (q < A.npk) {
+                float h[4], o[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    split_hi_lo(tile[l][4 * pq + j], h[j], o[j]);
+                const int64_t at = (s * A.npk + q) * 32 + l;
+                hi[at] = make_float4(h[0], h[1], h[2], h[3]);
+                lo[at] = make_float4(o[0], o[1], o[2], o[3]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+inline FxArgs fx_args(const pyci_gpu_csr *csr) {
+    FxArgs A;
+    A.spa = csr->fx_nbp / 32;
+    A.nslice = csr->fx_nalpha * A.spa;
+    A.nbeta = csr->fx_nbeta;
+    A.npk = csr->fx_npk;
+    A.ns = csr->fx_ns;
+    A.nd = csr->fx_nd;
+    A.nlb = csr->fx_nlb;
+    A.nls = csr->fx_nls;
+    A.nlsp = (csr->fx_nls + 3) / 4 * 4;
+    A.parts = static_cast<int>((A.spa + 15) / 16);
+    A.xblk = 0;
+    A.la = csr->fx_la;
+    A.lb = csr->fx_lb;
+    A.lc = csr->fx_lc;
+    A.aw = fx_atab_width(csr);
+    A.atab = csr->fx_atab;
+    A.bfull = csr->fx_bfull;
+    A.bsub = csr->fx_bsub;
+    A.hi = reinterpret_cast<const float4 *>(csr->fx_hi);
+    A.lo = reinterpret_cast<const float4 *>(csr->fx_lo);
+    return A;
+}
+
+template<int MODE, int K>
+bool fx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
+    FxArgs A = fx_args(csr);
+    constexpr int XW = MODE == 2 ? 2 * K : K;
+    A.xblk = static_cast<int>((A.nbeta * XW + 3) / 4 * 4);
+    const int warps = static_cast<int>((A.spa + A.parts - 1) / A.parts);
+    const size_t smem = fx_smem_bytes(A.xblk, A.ns, A.nd, A.nlsp, warps);
+    // Raise this instantiation's dynamic shared-memory limit once to what the
+    // device allows next to its static arrays.
+    static const size_t limit = [&] {
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, fcix_spmm_kernel<MODE, K>);
+        const size_t lim = csr->ctx->smem_optin > fa.sharedSizeBytes ? csr->ctx->smem_optin - fa.sharedSizeBytes : 0;
+        cudaFuncSetAttribute(fcix_spmm_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(lim));
+        return lim;
+    }();
+    if (smem > limit || A.nbeta >= 65536)
+        return false;
+    const int64_t blocks = csr->fx_nalpha * A.parts;
+    fcix_spmm_kernel<MODE, K><<<static_cast<unsigned>(blocks), 32 * warps, smem, st>>>(
+        A, static_cast<const float *>(x), y);
+    note_launch();
+    return true;
+}
+
+} // namespace pyci_gpu
+
+using namespace pyci_gpu;
+
+int fcix_fill(pyci_gpu_csr *csr) {
+    if (!csr->fx_atab || csr->fx_hi)
+        return PYCI_GPU_OK;
+    if (!csr->vals) {
+        set_error("operator has no FP64 values for its implicit-column form");
+        return PYCI_GPU_EINVAL;
+    }
+    const int64_t len = csr->nrow ? csr->nnz / csr->nrow : 0;
+    if (csr->nrow != csr->fx_nalpha * csr->fx_nbeta || len * csr->nrow != csr->nnz ||
+        len != csr->fx_nlb + static_cast<int64_t>(csr->fx_ns) * csr->fx_nls + csr->fx_nd) {
+        set_error("implicit-column form: operator rows do not match its string tables");
+        return PYCI_GPU_EINVAL;
+    }
+    cudaStream_t st = csr->ctx->stream;
+    const FxArgs A0 = fx_args(csr);
+    const size_t n = static_cast<size_t>(A0.nslice) * csr->fx_npk * 32 * 4;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->fx_hi), sizeof(float) * n, st));
+    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&csr->fx_lo), sizeof(float) * n, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(csr->fx_hi, st);
+        csr->fx_hi = nullptr;
+        return cuda_status(e, "cudaMallocAsync (implicit-column values)");
+    }
+    const FxArgs A = fx_args(csr);
+    const int64_t blocks = std::max<int64_t>(
+        1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 8, A.nslice * ((A.npk + 31) / 32)));
+    fcix_fill_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(A, static_cast<int>(len), csr->vals,
+                                                                     reinterpret_cast<float4 *>(csr->fx_hi),
+                                                                     reinterpret_cast<float4 *>(csr->fx_lo));
+    note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
+                 cudaStream_t st) {
+    if (!csr->fx_hi || !csr->fx_lo || csr->nrow >= INT32_MAX)
+        return false;
+    if (mode == 0) {
+        // Interleaved blocks with row stride K, 16-byte aligned for K = 4, 8.
+        const size_t align = (K % 4 == 0) ? 16 : (K == 2 ? 8 : 4);
+        if (ldx != K || ldy != K || reinterpret_cast<uintptr_t>(x) % align)
+            return false;
+        switch (K) {
+        case 1: return fx_launch_k<0, 1>(csr, x, y, st);
+        case 2: return fx_launch_k<0, 2>(csr, x, y, st);
+        case 3: return fx_launch_k<0, 3>(csr, x, y, st);
+        case 4: return fx_launch_k<0, 4>(csr, x, y, st);
+        case 5: return fx_launch_k<0, 5>(csr, x, y, st);
+        case 6: return fx_launch_k<0, 6>(csr, x, y, st);
+        case 7: return fx_launch_k<0, 7>(csr, x, y, st);
+        case 8: return fx_launch_k<0, 8>(csr, x, y, st);
+        default: return false;
+        }
+    }
+    if (mode != 2 || ldx != 2 * K || ldy != K || reinterpret_cast<uintptr_t>(x) % 16)
+        return false;
+    switch (K) {
+    case 1: return fx_launch_k<2, 1>(csr, x, y, st);
+    case 2: return fx_launch_k<2, 2>(csr, x, y, st);
+    case 4: return fx_launch_k<2, 4>(csr, x, y, st);
+    default: return false;
+    }
+}

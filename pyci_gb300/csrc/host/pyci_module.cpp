@@ -659,13 +659,26 @@ long add_hci(const SQuantOp &ham, Wfn &wfn, Array<double> coeffs, double eps, in
 
 // compute_rdms (pyci/src/rdm.cpp:1011-1055): DOCI (d0, d2), FullCI
 // (rdm1 [2, n, n], rdm2 [3, n, n, n, n]) on the device.
-py::tuple compute_rdms(const Wfn &wfn, Array<double> coeffs) {
+// GenCI (genci_exact=True only): the spin-orbital RDMs from their
+// definition, rdm1 [n, n] = <a+_p a_q>, rdm2 [n, n, n, n] = <a+_p a+_q a_s a_r>
+// (the reference's GenCI compute_rdms writes past its output arrays, so its
+// result is undefined and is not reproduced).
+static void require_genci_exact(const Wfn &wfn, bool exact) {
+    if (wfn.kind() == PYCI_WFN_GENCI && !exact)
+        throw std::invalid_argument("RDMs of a GenCI wave function: the reference's result is undefined (it writes "
+                                    "past its output arrays); pass genci_exact=True for the RDMs from their "
+                                    "definition");
+}
+
+py::tuple compute_rdms(const Wfn &wfn, Array<double> coeffs, bool genci_exact = false) {
+    require_genci_exact(wfn, genci_exact);
     if (coeffs.size() < wfn.ndet)
         throw std::invalid_argument("coeffs has fewer entries than the wave function has determinants");
     const long n = wfn.nbasis;
-    const bool fci = wfn.kind() == PYCI_WFN_FULLCI;
+    const bool fci = wfn.kind() == PYCI_WFN_FULLCI, gen = wfn.kind() == PYCI_WFN_GENCI;
     Array<double> r1 = fci ? Array<double>({2L, n, n}) : Array<double>({n, n});
-    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n}) : Array<double>({n, n});
+    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n})
+                           : (gen ? Array<double>(std::vector<long>{n, n, n, n}) : Array<double>({n, n}));
     auto ctx = default_ctx();
     const double *c = coeffs.data();
     double *p1 = r1.mutable_data(), *p2 = r2.mutable_data();
@@ -699,15 +712,18 @@ double compute_enpt2(const SQuantOp &ham, const Wfn &wfn, Array<double> coeffs, 
 
 // compute_transition_rdms (pyci/src/rdm.cpp:634-902, 1057-1080): same
 // layouts as compute_rdms, between two wave functions of the same space.
-py::tuple compute_transition_rdms(const Wfn &w1, const Wfn &w2, Array<double> c1, Array<double> c2) {
+py::tuple compute_transition_rdms(const Wfn &w1, const Wfn &w2, Array<double> c1, Array<double> c2,
+                                  bool genci_exact = false) {
     if (w1.kind() != w2.kind() || w1.nbasis != w2.nbasis || w1.nocc_up != w2.nocc_up || w1.nocc_dn != w2.nocc_dn)
         throw std::invalid_argument("the two wave functions describe different spaces");
+    require_genci_exact(w1, genci_exact);
     if (c1.size() < w1.ndet || c2.size() < w2.ndet)
         throw std::invalid_argument("a coefficient vector has fewer entries than its wave function has determinants");
     const long n = w1.nbasis;
-    const bool fci = w1.kind() == PYCI_WFN_FULLCI;
+    const bool fci = w1.kind() == PYCI_WFN_FULLCI, gen = w1.kind() == PYCI_WFN_GENCI;
     Array<double> r1 = fci ? Array<double>({2L, n, n}) : Array<double>({n, n});
-    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n}) : Array<double>({n, n});
+    Array<double> r2 = fci ? Array<double>(std::vector<long>{3L, n, n, n, n})
+                           : (gen ? Array<double>(std::vector<long>{n, n, n, n}) : Array<double>({n, n}));
     auto ctx = default_ctx();
     const double *p1c = c1.data(), *p2c = c2.data();
     double *p1 = r1.mutable_data(), *p2 = r2.mutable_data();
@@ -1289,8 +1305,8 @@ PYBIND11_MODULE(_pyci, m) {
           py::arg("coeffs"));
     m.def("compute_rdms", [](const FullCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
           py::arg("coeffs"));
-    m.def("compute_rdms", [](const GenCIWfn &w, Array<double> c) { return compute_rdms(w, c); }, py::arg("wfn"),
-          py::arg("coeffs"));
+    m.def("compute_rdms", [](const GenCIWfn &w, Array<double> c, bool exact) { return compute_rdms(w, c, exact); },
+          py::arg("wfn"), py::arg("coeffs"), py::arg("genci_exact") = false);
     m.def("compute_enpt2", [](const SQuantOp &h, const DOCIWfn &w, Array<double> c, double e, double eps, long) {
         return compute_enpt2(h, w, c, e, eps);
     }, py::arg("ham"), py::arg("wfn"), py::arg("coeffs"), py::arg("energy"), py::arg("eps") = 1.0e-5,
@@ -1309,9 +1325,9 @@ PYBIND11_MODULE(_pyci, m) {
     m.def("compute_transition_rdms", [](const FullCIWfn &w1, const FullCIWfn &w2, Array<double> c1, Array<double> c2) {
         return compute_transition_rdms(w1, w2, c1, c2);
     }, py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"));
-    m.def("compute_transition_rdms", [](const GenCIWfn &w1, const GenCIWfn &w2, Array<double> c1, Array<double> c2) {
-        return compute_transition_rdms(w1, w2, c1, c2);
-    }, py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"));
+    m.def("compute_transition_rdms", [](const GenCIWfn &w1, const GenCIWfn &w2, Array<double> c1, Array<double> c2,
+                                        bool exact) { return compute_transition_rdms(w1, w2, c1, c2, exact); },
+          py::arg("wfn1"), py::arg("wfn2"), py::arg("coeffs1"), py::arg("coeffs2"), py::arg("genci_exact") = false);
     m.def("get_num_threads", []() { return g_threads; });
     m.def("set_num_threads", [](long n) { g_threads = std::max(1L, n); }, py::arg("n"));
     m.def("popcnt", [](Array<ulong_t> d) {

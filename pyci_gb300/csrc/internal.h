@@ -71,7 +71,31 @@ struct pyci_gpu_csr {
     int32_t *sell_cols = nullptr; // [sell_nnz]
     float *sell_vals = nullptr;   // [sell_nnz] high parts
     float *sell_lo = nullptr;     // [sell_nnz] low parts
+    // Implicit-column form of a full FullCI space (fcix.cu): the columns of
+    // row (a, b) follow from per-string tables, so products stream values
+    // only.  Each row is stored as three sections: A = the alpha string
+    // itself with every beta partner (sorted {b} + singles + doubles), B =
+    // each alpha single with sorted {b} + beta singles (one group per
+    // single), C = each alpha double with b; A, C and each group of B padded
+    // to a multiple of 4 entries.  Tables come from the sorted FullCI build,
+    // values (FP32 high and low parts, in 4-entry packets) from
+    // pyci_gpu_csr_prepare_mixed.  Null when the operator is not a full
+    // FullCI space.
+    int64_t fx_nalpha = 0, fx_nbeta = 0, fx_nbp = 0; // strings per spin; beta count padded to 32
+    int64_t fx_npk = 0;           // 4-entry packets per row (padded length / 4)
+    int fx_ns = 0, fx_nd = 0;     // alpha singles / doubles per alpha string
+    int fx_nlb = 0, fx_nls = 0;   // beta partners in section A / per group of section B
+    int fx_la = 0, fx_lb = 0, fx_lc = 0; // padded section lengths
+    int32_t *fx_atab = nullptr;   // [nalpha][2 (ns + nd) + 1]: single targets, double targets,
+                                  // their CSR offsets in the sorted row, the offset of section A's group
+    int32_t *fx_bfull = nullptr;  // [nlb][nbeta]: sorted {b} + singles + doubles, transposed
+    int32_t *fx_bsub = nullptr;   // [nls][nbeta]: sorted {b} + singles, transposed
+    float *fx_hi = nullptr;       // [nslice][npk][32][4] high parts
+    float *fx_lo = nullptr;       // [nslice][npk][32][4] low parts
 };
+
+// Width of one alpha string's row of pyci_gpu_csr::fx_atab.
+inline int fx_atab_width(const pyci_gpu_csr *c) { return 2 * (c->fx_ns + c->fx_nd) + 1; }
 
 namespace pyci_gpu {
 // Kernel launches issued by this library (diagnostic counter).
@@ -101,6 +125,17 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
 // xs[N][2K] holds each row's FP32 high parts then low parts; K = 1, 2 or 4.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t stream);
 void csr_release(pyci_gpu_csr *csr);
+// Implicit-column form (fcix.cu).  fcix_fill writes fx_hi / fx_lo from the
+// FP64 values; fcix_launch runs one product on it: mode 0 FP32 (x, y
+// float [N][K], K <= 8), mode 2 double-float (xs float [N][2K], y double
+// [N][K], K = 1, 2, 4).  FP64 arithmetic is not offered: forming hi + lo in
+// FP64 costs three FP64 instructions per entry on top of the FMA, and this
+// GPU's FP64 pipe already bounds the CSR FP64 product.  Returns false when
+// the operator has no values in this form or the operands do not fit it (the
+// caller then uses another kernel).
+int fcix_fill(pyci_gpu_csr *csr);
+bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
+                 cudaStream_t st);
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
 int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,
                       double *vabs, double *vwsum);

@@ -386,7 +386,11 @@ int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
             split_kernel<<<grid_for(csr->ctx, csr->nnz, 256), 256, 0, st>>>(csr->nnz, csr->vals,
                                                                            csr->hi, csr->lo), ::pyci_gpu::note_launch();
         PYCI_CUDA_TRY(cudaGetLastError());
-        int rc = sell_build(csr);
+        // A full FullCI space also gets its values in the implicit-column
+        // form (fcix.cu); the autotuner picks per product.
+        int rc = csr->fx_atab ? fcix_fill(csr) : PYCI_GPU_OK;
+        if (!rc)
+            rc = sell_build(csr);
         if (rc)
             return rc;
     }

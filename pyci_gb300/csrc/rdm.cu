@@ -17,7 +17,8 @@
 //
 // Layouts (as pyci.compute_rdms returns them): DOCI d0 = rdm1 [n][n],
 // d2 = rdm2 [n][n]; FullCI rdm1 = [aa, bb] [2][n][n], rdm2 = [aaaa, bbbb,
-// abab] [3][n][n][n][n].
+// abab] [3][n][n][n][n]; GenCI (definition-based, rdm_genci_kernel) rdm1
+// [n][n], rdm2 [n][n][n][n] over spin orbitals.
 #include <cuda_runtime.h>
 
 #include <vector>
@@ -210,6 +211,111 @@ __global__ void __launch_bounds__(128) rdm_kernel(RdmParams p) {
     }
 }
 
+// GenCI spin-orbital RDMs from their definition (no reference counterpart:
+// the reference's GenCI compute_rdms, pyci/src/rdm.cpp:532-632, writes past
+// its output arrays and repeats index factors).  One thread per ket
+// determinant J (wave function p.dets / p.coeffs) walks its diagonal, single
+// and double excitations I, looks I up in the bra (p.table / p.coeffs2) and
+// adds c_I c_J <I| a+_p a_q |J> and c_I c_J <I| a+_p a+_q a_s a_r |J> with
+// every antisymmetric image (rdm1 [n][n], rdm2 [n][n][n][n]).  The sign of an
+// operator string is (-1) to the number of occupied orbitals below each
+// acted orbital, applied right to left.
+template<int NW>
+__device__ __forceinline__ int below_sign(const uint64_t *d, int p) {
+    int c = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+        if (64 * (w + 1) <= p)
+            c += __popcll(d[w]);
+        else if (64 * w < p)
+            c += __popcll(d[w] & ((1ULL << (p - 64 * w)) - 1));
+    }
+    return (c & 1) ? -1 : 1;
+}
+
+template<int NW>
+__global__ void __launch_bounds__(128) rdm_genci_kernel(RdmParams p) {
+    const int64_t jdet = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (jdet >= p.ndet)
+        return;
+    const int64_t n1 = p.n, n2 = n1 * n1, n3 = n1 * n2;
+    uint64_t det[NW], kdet[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+        det[w] = kdet[w] = p.dets[jdet * NW + w];
+    const double cj = p.coeffs[jdet];
+    auto flip = [&](uint64_t *d, int a) { d[a >> 6] ^= 1ULL << (a & 63); };
+    int16_t occ[kMaxOcc], vir[kMaxVir];
+    const int no = occ_list<NW>(det, occ), nv = vir_list<NW>(det, p.n, vir);
+    double *r1 = p.rdm1, *r2 = p.rdm2;
+    int64_t idet = p.table.find<NW>(det);
+    if (idet != -1) {
+        const double v = p.coeffs2[idet] * cj;
+        for (int x = 0; x < no; ++x) {
+            const int q0 = occ[x];
+            add(r1, q0 * (n1 + 1), v);
+            for (int y = 0; y < no; ++y) {
+                const int q1 = occ[y];
+                if (q1 == q0)
+                    continue;
+                add(r2, q0 * n3 + q1 * n2 + q0 * n1 + q1, v);
+                add(r2, q0 * n3 + q1 * n2 + q1 * n1 + q0, -v);
+            }
+        }
+    }
+    for (int x = 0; x < no; ++x) {
+        const int i = occ[x];
+        for (int y = 0; y < nv; ++y) {
+            const int a = vir[y];
+            int sg = below_sign<NW>(det, i);
+            flip(det, i);
+            sg *= below_sign<NW>(det, a);
+            flip(det, a);
+            idet = p.table.find<NW>(det);
+            if (idet != -1) {
+                const double v = p.coeffs2[idet] * cj * sg;
+                add(r1, a * n1 + i, v);
+                for (int z = 0; z < no; ++z) {
+                    const int k = occ[z];
+                    if (k == i)
+                        continue;
+                    add(r2, a * n3 + k * n2 + i * n1 + k, v);
+                    add(r2, k * n3 + a * n2 + i * n1 + k, -v);
+                    add(r2, a * n3 + k * n2 + k * n1 + i, -v);
+                    add(r2, k * n3 + a * n2 + k * n1 + i, v);
+                }
+            }
+            flip(det, a);
+            flip(det, i);
+        }
+    }
+    for (int x = 0; x < no; ++x)
+        for (int x2 = x + 1; x2 < no; ++x2)
+            for (int y = 0; y < nv; ++y)
+                for (int y2 = y + 1; y2 < nv; ++y2) {
+                    const int i = occ[x], j = occ[x2], a = vir[y], b = vir[y2];
+                    int sg = below_sign<NW>(det, i);
+                    flip(det, i);
+                    sg *= below_sign<NW>(det, j);
+                    flip(det, j);
+                    sg *= below_sign<NW>(det, b);
+                    flip(det, b);
+                    sg *= below_sign<NW>(det, a);
+                    flip(det, a);
+                    idet = p.table.find<NW>(det);
+                    if (idet != -1) {
+                        const double v = p.coeffs2[idet] * cj * sg;
+                        add(r2, a * n3 + b * n2 + i * n1 + j, v);
+                        add(r2, b * n3 + a * n2 + i * n1 + j, -v);
+                        add(r2, a * n3 + b * n2 + j * n1 + i, -v);
+                        add(r2, b * n3 + a * n2 + j * n1 + i, v);
+                    }
+#pragma unroll
+                    for (int w = 0; w < NW; ++w)
+                        det[w] = kdet[w];
+                }
+}
+
 template<bool TR>
 void launch_rdm(int nwd, int kind, unsigned blocks, cudaStream_t st, const RdmParams &p) {
     switch (nwd) {
@@ -230,6 +336,14 @@ void launch_rdm(int nwd, int kind, unsigned blocks, cudaStream_t st, const RdmPa
     }
 }
 
+void launch_rdm_genci(int nw, unsigned blocks, cudaStream_t st, const RdmParams &p) {
+    switch (nw) {
+    case 1: rdm_genci_kernel<1><<<blocks, 128, 0, st>>>(p); break;
+    case 2: rdm_genci_kernel<2><<<blocks, 128, 0, st>>>(p); break;
+    default: rdm_genci_kernel<4><<<blocks, 128, 0, st>>>(p); break;
+    }
+}
+
 } // namespace
 
 } // namespace pyci_gpu
@@ -247,10 +361,11 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
         set_error("nbasis = %lld exceeds the 256 orbitals the GPU path supports", static_cast<long long>(n));
         return PYCI_GPU_EUNSUPPORTED;
     }
-    if (kind != PYCI_WFN_DOCI && kind != PYCI_WFN_FULLCI) {
-        set_error("compute_rdms on the GPU supports DOCI and FullCI wave functions");
+    if (kind != PYCI_WFN_DOCI && kind != PYCI_WFN_FULLCI && kind != PYCI_WFN_GENCI) {
+        set_error("compute_rdms on the GPU supports DOCI, FullCI and (definition-based) GenCI wave functions");
         return PYCI_GPU_EUNSUPPORTED;
     }
+    const bool genci = kind == PYCI_WFN_GENCI;
     if (ndet >= INT32_MAX || ndet2 >= INT32_MAX) {
         set_error("more than 2^31 - 1 determinants is not supported");
         return PYCI_GPU_EUNSUPPORTED;
@@ -258,7 +373,7 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
     const int nstr = kind == PYCI_WFN_FULLCI ? 2 : 1;
     const int64_t n2 = n * n;
     const int64_t len1 = (kind == PYCI_WFN_FULLCI ? 2 : 1) * n2;
-    const int64_t len2 = kind == PYCI_WFN_FULLCI ? 3 * n2 * n2 : n2;
+    const int64_t len2 = kind == PYCI_WFN_FULLCI ? 3 * n2 * n2 : (genci ? n2 * n2 : n2);
     const int64_t host_nword = (n + 63) / 64;
     const int nwd = nstr * nw;
     std::vector<void *> bufs;
@@ -327,9 +442,27 @@ int rdm_compute_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t ndet
         p.coeffs2 = tr ? d_coef + ndet : d_coef;
         p.rdm1 = d_r1;
         p.rdm2 = d_r2;
-        const unsigned blocks = static_cast<unsigned>((ndet + 127) / 128);
+        if (genci) {
+            // Ket-driven: threads over wave function 2 (the wave function
+            // itself for compute_rdms), lookups in wave function 1 (the bra).
+            p.ndet = tr ? ndet2 : ndet;
+            p.dets = tr ? d_dets + ndet * nwd : d_dets;
+            p.coeffs = tr ? d_coef + ndet : d_coef;
+            p.coeffs2 = d_coef;
+            if (tr) {
+                int32_t *slots1 = nullptr;
+                uint64_t mask1 = 0;
+                if ((rc = det_table_build(d_dets, ndet, nwd, st, d_err, &slots1, &mask1)))
+                    break;
+                bufs.push_back(slots1);
+                p.table = DetTable{slots1, d_dets, mask1, nwd};
+            }
+        }
+        const unsigned blocks = static_cast<unsigned>((p.ndet + 127) / 128);
         if (blocks) {
-            if (tr)
+            if (genci)
+                launch_rdm_genci(nwd, blocks, st, p);
+            else if (tr)
                 launch_rdm<true>(nwd, kind, blocks, st, p);
             else
                 launch_rdm<false>(nwd, kind, blocks, st, p);

@@ -448,6 +448,15 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
 // the FP32 values of an operator that has one, the SELL-32 copy.
 constexpr int kVariants = 6;
 constexpr int kSellVariant = 0x100; // FP32: + 0 (4 warps per slice) or + 1 (one warp)
+constexpr int kFxVariant = 0x200;   // implicit-column form of a full FullCI space (fcix.cu)
+
+// The implicit-column form serves the FP32 products (mode 0) and the
+// double-float ones (csr_spmm_df); FP64 arithmetic stays on the CSR, whose
+// product this GPU's FP64 pipe already bounds.
+template<int VK>
+inline bool fx_usable(const pyci_gpu_csr *csr, int K) {
+    return VK == kF32 && csr->fx_hi && K <= 8;
+}
 inline int variant_lanes(int v) { return v % 3 == 0 ? 8 : (v % 3 == 1 ? 16 : 32); }
 inline int variant_map(int v) { return v / 3; }
 
@@ -456,6 +465,11 @@ inline int heuristic_variant(const pyci_gpu_csr *csr);
 template<int VK, int K>
 void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                     int64_t ldy, cudaStream_t st) {
+    if (v == kFxVariant) {
+        if (VK == kF32 && fcix_launch(csr, 0, K, x, ldx, y, ldy, st))
+            return;
+        v = heuristic_variant(csr); // a cached choice from an operator of the same shape without the form
+    }
     if (v == kSellVariant || v == kSellVariant + 1) {
         if constexpr (VK == kF32) {
             if (csr->sell_cols) {
@@ -542,14 +556,17 @@ bool autotune_enabled() {
     return on;
 }
 
-// PYCI_GPU_SPMM=sell, =sell1 or =csr pins the FP32 and double-float
-// products of operators built after it is set to the SELL-32 copy (FP32: 4
-// warps or one warp per slice) or to the CSR heuristic (read when an
-// operator makes its first product of a kind, so a process can compare them).
+// PYCI_GPU_SPMM=fcix, =sell, =sell1 or =csr pins the products of an operator
+// (read when it makes its first product of a kind, so a process can compare
+// them): the implicit-column form (FP32 and double-float; full FullCI
+// spaces), the SELL-32 copy (FP32 and double-float; FP32 with 4 warps or one
+// warp per slice) or the CSR heuristic (all precisions).
 int forced_sell_variant(const pyci_gpu_csr *csr) {
     const char *e = std::getenv("PYCI_GPU_SPMM");
     if (!e)
         return -1;
+    if (!std::strcmp(e, "fcix"))
+        return csr->fx_hi ? kFxVariant : heuristic_variant(csr);
     if (!std::strcmp(e, "sell"))
         return csr->sell_cols ? kSellVariant : heuristic_variant(csr);
     if (!std::strcmp(e, "sell1"))
@@ -574,6 +591,11 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
         int &choice = csr->tuned[VK][K];
         if (choice < 0 && VK == kF32)
             choice = forced_sell_variant(csr);
+        if (choice < 0 && VK != kF32) {
+            const char *e = std::getenv("PYCI_GPU_SPMM");
+            if (e && (!std::strcmp(e, "csr") || !std::strcmp(e, "sell") || !std::strcmp(e, "sell1")))
+                choice = heuristic_variant(csr);
+        }
         if (choice < 0)
             choice = tuning_cache_lookup(csr, VK, K);
         if (choice < 0) {
@@ -600,6 +622,21 @@ void launch_vk(const pyci_gpu_csr *csr, Values<VK> vals, int64_t k, const void *
                     }
                 }
                 const int best_csr = best_v;
+                // The implicit-column form.
+                if (fx_usable<VK>(csr, K)) {
+                    launch_k<VK>(kFxVariant, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(a, st);
+                    launch_k<VK>(kFxVariant, csr, vals, K, xs, k, ys, k, st);
+                    launch_k<VK>(kFxVariant, csr, vals, K, xs, k, ys, k, st);
+                    cudaEventRecord(b, st);
+                    cudaEventSynchronize(b);
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (ms < best) {
+                        best = ms;
+                        best_v = kFxVariant;
+                    }
+                }
                 // The SELL-32 copy (FP32 values only), both splits.
                 for (int sv = kSellVariant; VK == kF32 && csr->sell_cols && sv <= kSellVariant + 1; ++sv) {
                     launch_k<VK>(sv, csr, vals, K, xs, k, ys, k, st);
@@ -845,6 +882,11 @@ __global__ void __launch_bounds__(256) spmm_df_sell_kernel(int64_t nrow, int64_t
 
 template<int K>
 void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
+    if (v == kFxVariant) {
+        if (fcix_launch(csr, 2, K, xs, 2 * K, y, K, st))
+            return;
+        v = heuristic_variant(csr);
+    }
     if (v >= kSellVariant && csr->sell_lo) {
         const int64_t blocks = std::max<int64_t>(
             1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 32, (csr->nslice * 32 + 255) / 256));
@@ -926,6 +968,20 @@ int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cuda
                     best_v = v;
                 }
             }
+            if (csr->fx_hi) {
+                launch_df(kFxVariant, csr, K, xs, y, st);
+                cudaEventRecord(a, st);
+                launch_df(kFxVariant, csr, K, xs, y, st);
+                launch_df(kFxVariant, csr, K, xs, y, st);
+                cudaEventRecord(b, st);
+                cudaEventSynchronize(b);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, a, b);
+                if (ms < best) {
+                    best = ms;
+                    best_v = kFxVariant;
+                }
+            }
             if (csr->sell_lo) {
                 launch_df(kSellVariant, csr, K, xs, y, st);
                 cudaEventRecord(a, st);
@@ -967,6 +1023,27 @@ static int spmm_lower(const pyci_gpu_csr *csr, int precision, int64_t k, const v
                                                          csr->hi, csr->lo, static_cast<const double *>(x),
                                                          static_cast<int>(k), static_cast<double *>(y)), ::pyci_gpu::note_launch();
     PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+extern "C" int pyci_gpu_csr_product_form(const pyci_gpu_csr *csr, int precision, int64_t k, int *form) {
+    if (!csr || !form) {
+        set_error("NULL argument");
+        return PYCI_GPU_EINVAL;
+    }
+    const int K = static_cast<int>(std::min<int64_t>(std::max<int64_t>(k, 1), 8));
+    int vk;
+    switch (precision) {
+    case PYCI_PREC_FP64: vk = csr->vals ? kF64 : kSplit; break;
+    case PYCI_PREC_FP32: vk = kF32; break;
+    case PYCI_PREC_FP64_SPLIT: vk = kSplit; break;
+    case PYCI_PREC_FP64_DF: vk = kSplitDF; break;
+    default: set_error("unknown precision %d", precision); return PYCI_GPU_EINVAL;
+    }
+    const int v = csr->tuned[vk][K];
+    *form = v < 0 ? PYCI_FORM_UNTUNED
+                  : (v == kFxVariant ? PYCI_FORM_IMPLICIT
+                                     : (v >= kSellVariant && v < kFxVariant ? PYCI_FORM_SELL : PYCI_FORM_CSR));
     return PYCI_GPU_OK;
 }
 

@@ -91,11 +91,54 @@ def test_compute_rdms_energies(golden, kat):
     npt.assert_allclose(energy, es[0], rtol=0.0, atol=1.0e-9)
 
 
-def test_compute_rdms_rejects_genci(ctx):
-    ecore, one, two = synthetic_integrals(6, 3)
-    dets = O.all_dets(O.GENCI, 6, 3, 0)
-    with pytest.raises(capi.GpuError):
-        ctx.compute_rdms(capi.WFN_GENCI, 6, 3, 0, dets, np.ones(dets.shape[0]))
+@pytest.mark.parametrize("n,nocc", [(10, 4), (70, 2), (16, 5)])
+def test_genci_rdms_match_oracle(ctx, n, nocc):
+    r"""GenCI spin-orbital RDMs (definition-based; the reference's GenCI
+    compute_rdms is undefined) and transition RDMs against the oracle's,
+    which the CPU tests pin to operator algebra; 70 spin orbitals use two
+    words per determinant, (16, 5) a random subset."""
+    full = O.all_dets(O.GENCI, n, nocc, 0)
+    rng = np.random.default_rng(n + nocc)
+    dets = full if full.shape[0] <= 5000 else full[np.sort(rng.choice(full.shape[0], 5000, replace=False))]
+    c = rng.normal(size=dets.shape[0])
+    c /= np.linalg.norm(c)
+    r1, r2 = ctx.compute_rdms(capi.WFN_GENCI, n, nocc, 0, dets, c)
+    o1, o2 = O.compute_rdms_genci(n, dets, c)
+    npt.assert_allclose(r1, o1, rtol=0, atol=1e-12)
+    npt.assert_allclose(r2, o2, rtol=0, atol=1e-12)
+    assert np.trace(r1) == pytest.approx(nocc, abs=1e-10)
+    sub = np.sort(rng.choice(dets.shape[0], dets.shape[0] // 2, replace=False))
+    c2 = rng.normal(size=sub.shape[0])
+    t1, t2 = ctx.compute_transition_rdms(capi.WFN_GENCI, n, nocc, 0, dets, c, dets[sub], c2)
+    u1, u2 = O.compute_rdms_genci(n, dets, c, dets[sub], c2)
+    npt.assert_allclose(t1, u1, rtol=0, atol=1e-12)
+    npt.assert_allclose(t2, u2, rtol=0, atol=1e-12)
+
+
+def test_genci_rdms_drop_in_need_the_exact_flag():
+    # Through the drop-in API: genci_exact=True gives the definition-based
+    # spin-orbital RDMs, whose energy equals the GenCI eigenvalue; without the
+    # flag the call raises (the reference's result is undefined).
+    ecore, one, two = synthetic_integrals(3, 5)
+    nsp = 3
+    n = 2 * nsp
+    h = np.kron(np.eye(2), one)
+    g = np.zeros((n,) * 4)
+    for s in (0, nsp):
+        for t in (0, nsp):
+            g[s:s + nsp, t:t + nsp, s:s + nsp, t:t + nsp] = two
+    ham = pyci.secondquant_op(ecore, h, g)
+    wfn = pyci.genci_wfn(n, 3, 0)
+    for d in O.all_dets(O.GENCI, n, 3, 0):
+        wfn.add_det(d)
+    op = pyci.sparse_op(ham, wfn, genci_exact=True)
+    es, cs = op.solve(n=1, tol=1e-12)
+    with pytest.raises(ValueError):
+        pyci.compute_rdms(wfn, cs[0])
+    r1, r2 = pyci.compute_rdms(wfn, cs[0], genci_exact=True)
+    assert r1.shape == (n, n) and r2.shape == (n, n, n, n)
+    energy = ecore + np.einsum("pq,pq", h, r1) + 0.5 * np.einsum("pqrs,pqrs", g, r2)
+    npt.assert_allclose(energy, es[0], rtol=0.0, atol=1.0e-9)
 
 
 def test_transition_rdms_match_reference(ctx, golden):

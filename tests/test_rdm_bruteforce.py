@@ -195,3 +195,84 @@ def test_spinized_doci_transition_rdms_equal_their_definition(n, npair):
     g1, g2 = brute_force_transition_rdms(O.DOCI, n, dets[keep], c1[keep], dets, c2)
     npt.assert_allclose(t1, g1, rtol=0, atol=1e-13)
     npt.assert_allclose(t2, g2, rtol=0, atol=1e-13)
+
+
+def genci_states(dets, n):
+    out = []
+    for d in dets:
+        bits = sum(int(w) << (64 * i) for i, w in enumerate(d))
+        out.append(tuple(p for p in range(n) if bits >> p & 1))
+    return out
+
+
+def brute_force_genci(n, dets1, c1, dets2, c2):
+    r"""<1| a+_p a_q |2> and <1| a+_p a+_q a_s a_r |2> over n spin orbitals."""
+    bra = {s: c1[i] for i, s in enumerate(genci_states(dets1, n))}
+    g1 = np.zeros((n, n))
+    g2 = np.zeros((n, n, n, n))
+    for sj, cj in zip(genci_states(dets2, n), c2):
+        for p, q in itertools.product(range(n), repeat=2):
+            r = apply([(create, p), (annihilate, q)], sj)
+            if r is not None and r[1] in bra:
+                g1[p, q] += bra[r[1]] * r[0] * cj
+        for p, q, r_, s in itertools.product(range(n), repeat=4):
+            r = apply([(create, p), (create, q), (annihilate, s), (annihilate, r_)], sj)
+            if r is not None and r[1] in bra:
+                g2[p, q, r_, s] += bra[r[1]] * r[0] * cj
+    return g1, g2
+
+
+@pytest.mark.parametrize("n,nocc,pattern", [(4, 2, "sqrt"), (6, 3, "random"), (7, 2, "random"), (6, 4, "subset")])
+def test_genci_rdms_equal_their_definition(n, nocc, pattern):
+    r"""The oracle's definition-based GenCI RDMs (spin orbitals, GenCI's own
+    index space) against operator algebra on every determinant; traces N
+    and N (N - 1); a subset wave function drops the excitations that leave it."""
+    dets = O.all_dets(O.GENCI, n, nocc, 0)
+    N = dets.shape[0]
+    rng = np.random.default_rng(7 * n + nocc)
+    if pattern == "subset":
+        keep = np.sort(rng.choice(N, size=N - 4, replace=False))
+        dets = dets[keep]
+        N = dets.shape[0]
+    c = np.sqrt(np.arange(1.0, N + 1.0)) if pattern == "sqrt" else rng.normal(size=N)
+    c /= np.linalg.norm(c)
+    r1, r2 = O.compute_rdms_genci(n, dets, c)
+    g1, g2 = brute_force_genci(n, dets, c, dets, c)
+    npt.assert_allclose(r1, g1, rtol=0, atol=1e-13)
+    npt.assert_allclose(r2, g2, rtol=0, atol=1e-13)
+    assert np.trace(r1) == pytest.approx(nocc, abs=1e-12)
+    assert np.einsum("pqpq", r2) == pytest.approx(nocc * (nocc - 1), abs=1e-12)
+    # Transition form: a different ket on a proper subset of the bra's space.
+    c2 = rng.normal(size=N)
+    sub = np.sort(rng.choice(N, size=N - 2, replace=False))
+    t1, t2 = O.compute_rdms_genci(n, dets, c, dets[sub], c2[sub])
+    h1, h2 = brute_force_genci(n, dets, c, dets[sub], c2[sub])
+    npt.assert_allclose(t1, h1, rtol=0, atol=1e-13)
+    npt.assert_allclose(t2, h2, rtol=0, atol=1e-13)
+
+
+def test_genci_rdms_give_the_genci_energy():
+    r"""E = sum h_pq rdm1[p][q] + 1/2 sum <pq|rs> rdm2[p][q][r][s] over spin
+    orbitals, for the lowest eigenvector of the exact GenCI Hamiltonian (the
+    oracle's GenCI build over the true virtuals) of a spin-orbital space
+    built from seeded spatial integrals."""
+    from pyci_gb300.synth import synthetic_integrals
+    nsp, nocc = 4, 3
+    ecore, one, two = synthetic_integrals(nsp, 33)
+    n = 2 * nsp
+    # Spin-orbital integrals: orbital p < nsp is alpha, p >= nsp beta.
+    h = np.zeros((n, n))
+    g = np.zeros((n, n, n, n))
+    for s1 in (0, 1):
+        h[s1 * nsp:(s1 + 1) * nsp, s1 * nsp:(s1 + 1) * nsp] = one
+        for s2 in (0, 1):
+            g[s1 * nsp:(s1 + 1) * nsp, s2 * nsp:(s2 + 1) * nsp, s1 * nsp:(s1 + 1) * nsp,
+              s2 * nsp:(s2 + 1) * nsp] = two
+    dets = O.all_dets(O.GENCI, n, nocc, 0)
+    N = dets.shape[0]
+    ref = O.build_csr(O.GENCI, n, nocc, 0, dets, h, g)
+    H = np.stack([O.spmv(*ref, e) for e in np.eye(N)], axis=1)
+    w, v = np.linalg.eigh(H)
+    r1, r2 = O.compute_rdms_genci(n, dets, v[:, 0])
+    energy = np.sum(h * r1) + 0.5 * np.einsum("pqrs,pqrs", g, r2)
+    assert energy == pytest.approx(w[0], abs=1e-10)
