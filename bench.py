@@ -52,12 +52,37 @@ WORKLOADS = {
 }
 WORKLOAD = WORKLOADS["fci12"]
 METRIC = WORKLOAD["metric"]
-# DRAM bytes moved per algorithmic byte by the FP32 k = 4 SpMM (SELL-32 kernel),
-# from one ncu capture of the same kernel on the 11-orbital 5a5b FullCI
-# operator (2.1617 GB moved for 2.1621 GB algorithmic).  Both operators stream
-# the matrix once per launch with the x block in L2, so traffic scales with the
-# entries processed.
-TRAFFIC_PER_ALGORITHMIC_BYTE = 1.000
+# DRAM bytes moved per algorithmic byte by the FP32 k = 4 SpMM, per kernel
+# form, from one ncu capture of the same kernel on the 11-orbital 5a5b FullCI
+# operator (SELL-32: 2.1617 GB moved for 2.1621 GB algorithmic).  Both
+# operators stream the matrix once per launch with the x block in L2, so
+# traffic scales with the entries processed.
+FORM_NAMES = {-1: "untuned", 0: "csr", 1: "sell32", 2: "implicit"}
+KERNEL_NAMES = {-1: "untuned", 0: "CSR spmm_kernel tile", 1: "spmm_sell_kernel (SELL-32)",
+                2: "fcix_spmm_kernel (implicit columns, values only)"}
+TRAFFIC_PER_ALGORITHMIC_BYTE = {-1: 1.0, 0: 1.024, 1: 1.000, 2: 1.000}
+# The implicit-column form streams padded packets (beta strings padded to a
+# multiple of 32 rows per alpha string, row sections to multiples of 4
+# entries); on the 11-orbital 5a5b operator ncu measured 1.023 DRAM bytes per
+# byte of padded values + x + y (1.1581 GB for 1.1316 GB).
+IMPLICIT_TRAFFIC_PER_PADDED_BYTE = 1.023
+
+
+def implicit_padded_bytes(nb, na, nbeta_occ, k):
+    r"""Bytes of one implicit-column FP32 product at width k: padded value
+    packets plus x read once and y written once."""
+    from math import comb
+    nalpha, nbeta = comb(nb, na), comb(nb, nbeta_occ)
+    nbp = (nbeta + 31) // 32 * 32
+
+    def up4(v):
+        return (v + 3) // 4 * 4
+
+    sa, sb = na * (nb - na), nbeta_occ * (nb - nbeta_occ)
+    da = comb(na, 2) * comb(nb - na, 2)
+    db = comb(nbeta_occ, 2) * comb(nb - nbeta_occ, 2)
+    row = up4(1 + sb + db) + sa * up4(1 + sb) + up4(da)
+    return nalpha * nbp * row * 4 + 2 * nalpha * nbeta * k * 4
 TOL = 1.0e-6  # residual <= 1e-6 * |E| (~1e-5 Ha): eigenvalues converge quadratically, well inside 1 uHa
 
 
@@ -365,17 +390,28 @@ def run_ours(args, world, rank, local):
     ms_step = ms_total / args.steps
     value = ms_step / 1e3 / (nroot * world)
 
-    # ---- FP64 path on the same resident CSR (for the mixed-vs-FP64 speedup)
-    solve(capi.SOLVE_FP64)
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
+    # ---- FP64 path on the same resident operator (for the mixed-vs-FP64
+    # speedup): FP64 vectors, Gram products and Rayleigh-Ritz; products
+    # FP64-accurate in double-float arithmetic on the exact high/low split.
+    # The same solve with FP64-arithmetic products is timed beside it.
+    def time_solves(mode, reps):
+        solve(mode)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(reps):
+            ev_, _, st_ = solve(mode)
+        f1.record(stream)
+        f1.synchronize()
+        return f0.elapsed_time(f1) / reps / 1e3 / nroot, ev_, st_
+
     nf = max(1, min(2, args.steps))
-    f0.record(stream)
-    for _ in range(nf):
-        evals64, _, st64 = solve(capi.SOLVE_FP64)
-    f1.record(stream)
-    f1.synchronize()
-    fp64_spr = f0.elapsed_time(f1) / nf / 1e3 / nroot
+    fp64_spr, evals64, st64 = time_solves(capi.SOLVE_FP64, nf)
+    os.environ["PYCI_GPU_FP64_PRODUCT"] = "native"
+    try:
+        fp64n_spr, evals64n, st64n = time_solves(capi.SOLVE_FP64, 1)
+    finally:
+        os.environ.pop("PYCI_GPU_FP64_PRODUCT", None)
 
     # ---- SpMV / SpMM bandwidth (dominant kernel), events on the launch stream
     N = nrow
@@ -398,12 +434,24 @@ def run_ours(args, world, rank, local):
 
     t32 = time_spmm(capi.PREC_FP32, nroot, x32, y32)
     t64 = time_spmm(capi.PREC_FP64, 1, x64, y64)
-    # FP64-accurate 4-vector product in FP32 arithmetic (the refinement's product)
+    # FP64-accurate 4-vector product in FP32 arithmetic (the refinement's and
+    # the FP64 solve's product)
     xdf = torch.randn((N, 8), dtype=torch.float32, device="cuda")
     ydf = torch.empty((N, 4), dtype=torch.float64, device="cuda")
     tdf = time_spmm(capi.PREC_FP64_DF, 4, xdf, ydf)
     del xdf, ydf
-    bytes32 = stored * (4 + 4) + (N + 1) * 8 + 2 * N * nroot * 4
+    form32 = csr.product_form(capi.PREC_FP32, nroot)
+    formdf = csr.product_form(capi.PREC_FP64_DF, 4)
+    # Algorithmic bytes of one launch: the stored values (+ int32 columns and
+    # row pointers unless the columns are implicit), x read once, y written once.
+    if form32 == capi.FORM_IMPLICIT:
+        bytes32 = stored * 4 + 2 * N * nroot * 4
+    else:
+        bytes32 = stored * (4 + 4) + (N + 1) * 8 + 2 * N * nroot * 4
+    if formdf == capi.FORM_IMPLICIT:
+        bytesdf = stored * 8 + N * (32 + 32)
+    else:
+        bytesdf = stored * 12 + (N + 1) * 8 + N * (32 + 32)
     bytes64 = stored * (8 + 4) + (N + 1) * 8 + 2 * N * 8
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
@@ -450,8 +498,12 @@ def run_ours(args, world, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic seeded integrals (seed %d)" % WORKLOAD["seed"],
         "config": workload_config(N, stored, size, world),
-        "fp64": {"s_per_root": fp64_spr, "iterations": st64["iterations"], "matvecs": st64["matvecs"]},
+        "fp64": {"s_per_root": fp64_spr, "iterations": st64["iterations"], "matvecs": st64["matvecs"],
+                 "products": "double-float (FP32 arithmetic, FP64-accurate) on the exact high/low split"},
+        "fp64_native": {"s_per_root": fp64n_spr, "iterations": st64n["iterations"], "matvecs": st64n["matvecs"],
+                        "products": "FP64 arithmetic on the FP64 CSR (bound by the FP64 pipe)"},
         "speedup_mixed_vs_fp64": fp64_spr / (ms_step / 1e3 / nroot),
+        "speedup_mixed_vs_fp64_native": fp64n_spr / (ms_step / 1e3 / nroot),
         "mixed": {"iterations": stats[-1]["iterations"], "matvecs": stats[-1]["matvecs"],
                   "matvecs_fp64": stats[-1]["matvecs_fp64"], "refinements": stats[-1]["refinements"],
                   "spmm_seconds": stats[-1]["seconds_spmm"], "max_residual": stats[-1]["max_residual"],
@@ -459,16 +511,18 @@ def run_ours(args, world, rank, local):
                   "solve_seconds": stats[-1]["seconds"]},
         "error_vs_fp64_oracle": errs,
         "build_seconds": build_s,
-        "spmv": {"fp32_k4_gbs": gbs32, "fp32_k4_ms": t32 * 1e3, "fp64_k1_gbs": gbs64, "fp64_k1_ms": t64 * 1e3,
-                 "fp64_k1_frac": gbs64 / hbm, "df_k4_ms": tdf * 1e3,
-                 "df_k4_gbs": (stored * 12 + (N + 1) * 8 + N * (32 + 32)) / tdf / 1e9},
+        "spmv": {"fp32_k4_gbs": gbs32, "fp32_k4_ms": t32 * 1e3, "fp32_k4_form": FORM_NAMES[form32],
+                 "fp64_k1_gbs": gbs64, "fp64_k1_ms": t64 * 1e3, "fp64_k1_frac": gbs64 / hbm,
+                 "df_k4_ms": tdf * 1e3, "df_k4_gbs": bytesdf / tdf / 1e9, "df_k4_frac": bytesdf / tdf / 1e9 / hbm,
+                 "df_k4_form": FORM_NAMES[formdf]},
         "roofline": {"bound": "hbm", "achieved": gbs32, "peak": hbm, "unit": "GB/s", "frac": gbs32 / hbm,
-                     "traffic": int(bytes32 * TRAFFIC_PER_ALGORITHMIC_BYTE) if fci else None,
+                     "traffic": (int(IMPLICIT_TRAFFIC_PER_PADDED_BYTE * implicit_padded_bytes(nb, nu, nd, nroot))
+                                 if form32 == capi.FORM_IMPLICIT
+                                 else int(bytes32 * TRAFFIC_PER_ALGORITHMIC_BYTE[form32])) if fci else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel on "
                                        "FullCI 11o 5a5b, scaled by entries processed" if fci else None,
                      "peak_source": peak_kind, "peak_note": "of measured" if peak_kind == "measured" else "of fallback",
-                     "kernel": "FP32 k=4 SpMM, autotuned: spmm_sell_kernel (SELL-32, 4 or 1 warps per slice) "
-                               "or a CSR spmm_kernel tile", "algorithmic_bytes": bytes32},
+                     "kernel": "FP32 k=4 SpMM, autotuned: " + KERNEL_NAMES[form32], "algorithmic_bytes": bytes32},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_spr, "unit": "s/root", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -1181,9 +1181,11 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
 // beta lists (full: partners of the alpha string itself, sub: of an alpha
 // single) transposed to [position][string].
 __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
-                                   int grp1, int ns, int nd, int32_t *atab, int32_t *bfull, int32_t *bsub) {
+                                   int grp1, int ns, int nd, int la, int32_t *atab, int32_t *bfull, int32_t *bsub,
+                                   uint16_t *bq) {
     const int64_t n_f = static_cast<int64_t>(nbl) * nbeta, n_s = static_cast<int64_t>(grp1) * nbeta;
-    const int64_t total = nalpha + n_f + n_s;
+    const int64_t n_q = static_cast<int64_t>(la) * nbeta;
+    const int64_t total = nalpha + n_f + n_s + n_q;
     const int w = 2 * (ns + nd) + 1;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -1208,9 +1210,14 @@ __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nal
         } else if (i < nalpha + n_f) {
             const int64_t j = i - nalpha, q = j / nbeta, b = j - q * nbeta;
             bfull[j] = TB.key[b * TB.npad + q];
-        } else {
+        } else if (i < nalpha + n_f + n_s) {
             const int64_t j = i - nalpha - n_f, q = j / nbeta, b = j - q * nbeta;
             bsub[j] = TB.sub[b * TB.npad + q];
+        } else {
+            // bq[(t / 4) * nbeta + b][t % 4] = partner t of b (b past the list).
+            const int64_t j = i - nalpha - n_f - n_s, t = j / nbeta, b = j - t * nbeta;
+            bq[((t >> 2) * nbeta + b) * 4 + (t & 3)] =
+                static_cast<uint16_t>(t < nbl ? TB.key[b * TB.npad + t] : static_cast<int32_t>(b));
         }
     }
 }
@@ -1602,20 +1609,24 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
     const size_t sa = sizeof(int32_t) * nalpha * w, sf = sizeof(int32_t) * nbl * nbeta,
                  ss = sizeof(int32_t) * grp1 * nbeta;
     int32_t *atab = nullptr, *bfull = nullptr, *bsub = nullptr;
+    uint16_t *bq = nullptr;
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&atab), sa, st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&bfull), sf, st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&bsub), ss, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&bq), sizeof(uint16_t) * la * nbeta, st);
     if (e != cudaSuccess) {
-        for (int32_t *q : {atab, bfull, bsub})
+        for (void *q : {static_cast<void *>(atab), static_cast<void *>(bfull), static_cast<void *>(bsub),
+                        static_cast<void *>(bq)})
             if (q)
                 cudaFreeAsync(q, st);
         return cuda_status(e, "cudaMallocAsync (implicit-column tables)");
     }
-    const int64_t total = nalpha + (static_cast<int64_t>(nbl) + grp1) * nbeta;
+    const int64_t total = nalpha + (static_cast<int64_t>(nbl) + grp1 + la) * nbeta;
     fcix_tables_kernel<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
-        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, atab, bfull, bsub);
+        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, la, atab, bfull, bsub, bq);
     ::pyci_gpu::note_launch();
     csr->fx_nalpha = nalpha;
     csr->fx_nbeta = nbeta;
@@ -1631,6 +1642,7 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
     csr->fx_atab = atab;
     csr->fx_bfull = bfull;
     csr->fx_bsub = bsub;
+    csr->fx_bq = bq;
     return PYCI_GPU_OK;
 }
 

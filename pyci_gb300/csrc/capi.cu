@@ -41,6 +41,7 @@ int cuda_status(cudaError_t err, const char *what) {
 // elsewhere or already freed).
 static void fx_forget(pyci_gpu_csr *csr) {
     csr->fx_atab = csr->fx_bfull = csr->fx_bsub = nullptr;
+    csr->fx_bq = nullptr;
     csr->fx_hi = csr->fx_lo = nullptr;
     csr->fx_nalpha = csr->fx_nbeta = csr->fx_nbp = csr->fx_npk = 0;
     csr->fx_ns = csr->fx_nd = csr->fx_nlb = csr->fx_nls = 0;
@@ -54,7 +55,7 @@ void csr_release(pyci_gpu_csr *csr) {
     void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
                     csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals,
                     csr->sell_lo,    csr->fx_atab,  csr->fx_bfull, csr->fx_bsub,   csr->fx_hi,
-                    csr->fx_lo};
+                    csr->fx_lo,      csr->fx_bq};
     for (void *p : ptrs)
         if (p)
             cudaFreeAsync(p, st);
@@ -309,6 +310,7 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     c->sell_vals = nullptr;
     c->sell_lo = nullptr;
     c->fx_atab = c->fx_bfull = c->fx_bsub = nullptr;
+    c->fx_bq = nullptr;
     c->fx_hi = c->fx_lo = nullptr;
     const int64_t fx_vals = csr->fx_nalpha * (csr->fx_nbp / 32) * csr->fx_npk * 128;
     struct Item {
@@ -331,6 +333,7 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         {csr->fx_atab, reinterpret_cast<void **>(&c->fx_atab), sizeof(int32_t) * csr->fx_nalpha * fx_atab_width(csr)},
         {csr->fx_bfull, reinterpret_cast<void **>(&c->fx_bfull), sizeof(int32_t) * csr->fx_nlb * csr->fx_nbeta},
         {csr->fx_bsub, reinterpret_cast<void **>(&c->fx_bsub), sizeof(int32_t) * csr->fx_nls * csr->fx_nbeta},
+        {csr->fx_bq, reinterpret_cast<void **>(&c->fx_bq), sizeof(uint16_t) * csr->fx_la * csr->fx_nbeta},
         {csr->fx_hi, reinterpret_cast<void **>(&c->fx_hi), sizeof(float) * fx_vals},
         {csr->fx_lo, reinterpret_cast<void **>(&c->fx_lo), sizeof(float) * fx_vals},
     };

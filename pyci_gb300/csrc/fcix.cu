@@ -36,7 +36,8 @@
 // Tables (L1/L2-resident): atab[a] = the targets of a's singles and doubles
 // (sorted), their groups' offsets in the sorted CSR row and that of a's own
 // group (for the fill from the CSR); bfull[p][b] and bsub[p][b], the sorted
-// beta lists, transposed so the 32 lanes of a slice read consecutive words.
+// beta lists, transposed so the 32 lanes of a slice read consecutive words,
+// and bq, section A's list as 16-bit indices 4 per packet (one 8-byte load).
 
 #include <cuda_runtime.h>
 
@@ -55,6 +56,7 @@ struct FxArgs {
     int parts;     // blocks per alpha string
     int xblk;      // floats of one staged x block (nbeta rows, padded to 4)
     const int32_t *atab, *bfull, *bsub;
+    const ushort4 *bq; // [la / 4][nbeta]: section A's beta partners, 4 per packet (padding: b)
     const float4 *hi, *lo;
 };
 
@@ -137,10 +139,13 @@ __device__ __forceinline__ void fx_stage(float *dst, const float *src, int n) {
 __device__ __forceinline__ void fx_stage_wait() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
 // Shared memory of one block: two staged x blocks, the alpha targets times
-// nbeta (singles then doubles), and per warp its lanes' section-B partner
-// lists (16-bit: nbeta < 65536).
-__host__ __device__ inline size_t fx_smem_bytes(int xblk, int ns, int nd, int nlsp, int warps) {
-    return sizeof(float) * 2 * static_cast<size_t>(xblk) + sizeof(int) * static_cast<size_t>(ns + nd + 3) / 4 * 4 +
+// nbeta (singles padded to a multiple of 4, then doubles padded to lc with
+// the row's own block), and per warp its lanes' section-B partner lists
+// (16-bit: nbeta < 65536; 4 consecutive positions of a lane together, so a
+// packet's 4 partners are one 8-byte load).
+__host__ __device__ inline int fx_up4(int v) { return (v + 3) / 4 * 4; }
+__host__ __device__ inline size_t fx_smem_bytes(int xblk, int ns, int lc, int nlsp, int warps) {
+    return sizeof(float) * 2 * static_cast<size_t>(xblk) + sizeof(int) * static_cast<size_t>(fx_up4(ns) + lc) +
            sizeof(uint16_t) * static_cast<size_t>(warps) * nlsp * 32;
 }
 
@@ -155,8 +160,9 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
     extern __shared__ __align__(16) unsigned char fx_dyn[];
     float *xb0 = reinterpret_cast<float *>(fx_dyn);
     float *xb1 = xb0 + A.xblk;
+    const int ns4 = fx_up4(A.ns);
     int *aT = reinterpret_cast<int *>(xb1 + A.xblk);
-    uint16_t *jbS = reinterpret_cast<uint16_t *>(aT + (A.ns + A.nd + 3) / 4 * 4);
+    uint16_t *jbS = reinterpret_cast<uint16_t *>(aT + ns4 + A.lc);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nbeta = static_cast<int>(A.nbeta);
     const int64_t a = blockIdx.x / A.parts;
@@ -168,12 +174,19 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
     const int b = bb < nbeta ? bb : nbeta - 1;
     const int self = static_cast<int>(a) * nbeta;
     const int32_t *arow = A.atab + a * A.aw;
-    for (int i = threadIdx.x; i < A.ns + A.nd; i += blockDim.x)
-        aT[i] = __ldg(arow + i) * nbeta;
+    for (int i = threadIdx.x; i < ns4 + A.lc; i += blockDim.x) {
+        int v = self;
+        if (i < A.ns)
+            v = __ldg(arow + i) * nbeta;
+        else if (i >= ns4 && i - ns4 < A.nd)
+            v = __ldg(arow + A.ns + (i - ns4)) * nbeta;
+        aT[i] = v;
+    }
     uint16_t *mj = jbS + warp * A.nlsp * 32;
     if (active)
-        for (int p = 0; p < A.nls; ++p)
-            mj[p * 32 + lane] = static_cast<uint16_t>(__ldg(A.bsub + static_cast<int64_t>(p) * nbeta + b));
+        for (int p = 0; p < A.nlsp; ++p)
+            mj[((p >> 2) * 32 + lane) * 4 + (p & 3)] =
+                static_cast<uint16_t>(p < A.nls ? __ldg(A.bsub + static_cast<int64_t>(p) * nbeta + b) : b);
     fx_stage(xb0, x + static_cast<int64_t>(self) * XW, nbeta * XW);
     fx_stage_wait();
     __syncthreads();
@@ -185,18 +198,34 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
         acc[k] = cc[k] = 0.0f;
     const float4 *hp = A.hi + s * A.npk * 32 + lane;
     const float4 *lp = A.lo + s * A.npk * 32 + lane;
+    // Packets are read kD at a time (all loads issued before the first is
+    // used), so each warp keeps several 512-byte value loads in flight.
+    constexpr int kD = 4;
+    float4 vh[kD], vl[kD];
+    auto load_packets = [&](int q, int qend) {
+#pragma unroll
+        for (int i = 0; i < kD; ++i) {
+            vh[i] = q + i < qend ? __ldcs(hp + 32 * (q + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            if (MODE == 2)
+                vl[i] = q + i < qend ? __ldcs(lp + 32 * (q + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
     // Section A: (a, every beta partner of b), x block a in xb0.
     if (active) {
-        const int *tb = A.bfull + b;
-        for (int q = 0; q < A.la / 4; ++q) {
-            const float4 vh = __ldcs(hp + 32 * q);
-            const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
-            const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+        const ushort4 *tb = A.bq + b;
+        for (int q0 = 0; q0 < A.la / 4; q0 += kD) {
+            load_packets(q0, A.la / 4);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int t = 4 * q + u;
-                const int jb = t < A.nlb ? __ldg(tb + static_cast<int64_t>(t) * nbeta) : b;
-                fx_acc<MODE, K>(xb0 + jb * XW, h4[u], l4[u], acc, cc);
+            for (int i = 0; i < kD; ++i) {
+                if (q0 + i >= A.la / 4)
+                    break;
+                const float h4[4] = {vh[i].x, vh[i].y, vh[i].z, vh[i].w};
+                const float l4[4] = {vl[i].x, vl[i].y, vl[i].z, vl[i].w};
+                const ushort4 j4 = __ldg(tb + static_cast<int64_t>(q0 + i) * nbeta);
+                const int jb[4] = {j4.x, j4.y, j4.z, j4.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    fx_acc<MODE, K>(xb0 + jb[u] * XW, h4[u], l4[u], acc, cc);
             }
         }
     }
@@ -209,16 +238,19 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
         if (g + 1 < A.ns)
             fx_stage((g & 1) ? xb1 : xb0, x + static_cast<int64_t>(aT[g + 1]) * XW, nbeta * XW);
         if (active) {
-            for (int qq = 0; qq < gq; ++qq) {
-                const int q = qb + g * gq + qq;
-                const float4 vh = __ldcs(hp + 32 * q);
-                const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
-                const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+            for (int qq0 = 0; qq0 < gq; qq0 += kD) {
+                load_packets(qb + g * gq + qq0, qb + (g + 1) * gq);
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int p = 4 * qq + u;
-                    const int jb = p < A.nls ? mj[p * 32 + lane] : b;
-                    fx_acc<MODE, K>(cur + jb * XW, h4[u], l4[u], acc, cc);
+                for (int i = 0; i < kD; ++i) {
+                    if (qq0 + i >= gq)
+                        break;
+                    const float h4[4] = {vh[i].x, vh[i].y, vh[i].z, vh[i].w};
+                    const float l4[4] = {vl[i].x, vl[i].y, vl[i].z, vl[i].w};
+                    const ushort4 j4 = reinterpret_cast<const ushort4 *>(mj)[(qq0 + i) * 32 + lane];
+                    const int jb[4] = {j4.x, j4.y, j4.z, j4.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        fx_acc<MODE, K>(cur + jb[u] * XW, h4[u], l4[u], acc, cc);
                 }
             }
         }
@@ -226,15 +258,19 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
     // Section C: (alpha double, b), coalesced global gathers.
     if (active) {
         const int qc = (A.la + A.lb) / 4;
-        for (int q = qc; q < A.npk; ++q) {
-            const float4 vh = __ldcs(hp + 32 * q);
-            const float4 vl = MODE == 2 ? __ldcs(lp + 32 * q) : vh;
-            const float h4[4] = {vh.x, vh.y, vh.z, vh.w}, l4[4] = {vl.x, vl.y, vl.z, vl.w};
+        for (int q0 = qc; q0 < A.npk; q0 += kD) {
+            load_packets(q0, static_cast<int>(A.npk));
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int tt = 4 * (q - qc) + u;
-                const int col = (tt < A.nd ? aT[A.ns + tt] : self) + b;
-                fx_acc<MODE, K>(x + static_cast<int64_t>(col) * XW, h4[u], l4[u], acc, cc);
+            for (int i = 0; i < kD; ++i) {
+                if (q0 + i >= A.npk)
+                    break;
+                const float h4[4] = {vh[i].x, vh[i].y, vh[i].z, vh[i].w};
+                const float l4[4] = {vl[i].x, vl[i].y, vl[i].z, vl[i].w};
+                const int4 d4 = reinterpret_cast<const int4 *>(aT + ns4)[q0 + i - qc];
+                const int col[4] = {d4.x + b, d4.y + b, d4.z + b, d4.w + b};
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    fx_acc<MODE, K>(x + static_cast<int64_t>(col[u]) * XW, h4[u], l4[u], acc, cc);
             }
         }
         if (bb < nbeta) {
@@ -325,6 +361,7 @@ inline FxArgs fx_args(const pyci_gpu_csr *csr) {
     A.atab = csr->fx_atab;
     A.bfull = csr->fx_bfull;
     A.bsub = csr->fx_bsub;
+    A.bq = reinterpret_cast<const ushort4 *>(csr->fx_bq);
     A.hi = reinterpret_cast<const float4 *>(csr->fx_hi);
     A.lo = reinterpret_cast<const float4 *>(csr->fx_lo);
     return A;
@@ -336,7 +373,7 @@ bool fx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t s
     constexpr int XW = MODE == 2 ? 2 * K : K;
     A.xblk = static_cast<int>((A.nbeta * XW + 3) / 4 * 4);
     const int warps = static_cast<int>((A.spa + A.parts - 1) / A.parts);
-    const size_t smem = fx_smem_bytes(A.xblk, A.ns, A.nd, A.nlsp, warps);
+    const size_t smem = fx_smem_bytes(A.xblk, A.ns, A.lc, A.nlsp, warps);
     // Raise this instantiation's dynamic shared-memory limit once to what the
     // device allows next to its static arrays.
     static const size_t limit = [&] {

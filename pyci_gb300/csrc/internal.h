@@ -90,6 +90,7 @@ struct pyci_gpu_csr {
                                   // their CSR offsets in the sorted row, the offset of section A's group
     int32_t *fx_bfull = nullptr;  // [nlb][nbeta]: sorted {b} + singles + doubles, transposed
     int32_t *fx_bsub = nullptr;   // [nls][nbeta]: sorted {b} + singles, transposed
+    uint16_t *fx_bq = nullptr;    // [la / 4][nbeta][4]: section A's partners by packet (padding: b)
     float *fx_hi = nullptr;       // [nslice][npk][32][4] high parts
     float *fx_lo = nullptr;       // [nslice][npk][32][4] low parts
 };
