@@ -63,9 +63,9 @@ KERNEL_NAMES = {-1: "untuned", 0: "CSR spmm_kernel tile", 1: "spmm_sell_kernel (
 TRAFFIC_PER_ALGORITHMIC_BYTE = {-1: 1.0, 0: 1.024, 1: 1.000, 2: 1.000}
 # The implicit-column form streams padded packets (beta strings padded to a
 # multiple of 32 rows per alpha string, row sections to multiples of 4
-# entries); on the 11-orbital 5a5b operator ncu measured 1.023 DRAM bytes per
-# byte of padded values + x + y (1.1581 GB for 1.1316 GB).
-IMPLICIT_TRAFFIC_PER_PADDED_BYTE = 1.023
+# entries); on the 11-orbital 5a5b operator ncu measured 1.001 DRAM bytes per
+# byte of padded values + x + y (1.1581 GB for 1.1564 GB).
+IMPLICIT_TRAFFIC_PER_PADDED_BYTE = 1.001
 
 
 def implicit_padded_bytes(nb, na, nbeta_occ, k):
