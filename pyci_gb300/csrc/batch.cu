@@ -1408,7 +1408,10 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
     const int mmax = 64; // per-problem subspace (restarts keep 16)
     if (mode == PYCI_SOLVE_MIXED) {
         for (auto *c : v) {
+            // The batched kernels read the CSR-order split.
             int rc = csr_prepare_mixed_device(c, 0);
+            if (!rc)
+                rc = csr_ensure_split(c);
             if (rc)
                 return rc;
         }

@@ -22,6 +22,7 @@
 
 #include "detops.cuh"
 #include "internal.h"
+#include "split_bits.h"
 
 namespace pyci_gpu {
 
@@ -51,6 +52,13 @@ struct BuildParams {
     int32_t *lower_len;
     double *diag;
     int *error;             // set to a nonzero code on an internal inconsistency
+    // Implicit-column form written by the sorted FullCI fill (fcix.cu
+    // layout); hi null: not written.  grank[a][g]: the rank of alpha group
+    // g among the groups of its type (single or double).
+    float *fx_hi, *fx_lo;
+    const int16_t *fx_grank;
+    int64_t fx_spa, fx_npk;
+    int fx_la, fx_lb, fx_nlsp, fx_na;
 };
 
 // Column limit of a row's own (lower / general) entries: update() keeps the
@@ -1171,6 +1179,18 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
         }
         p.cols[start + t] = static_cast<int32_t>(col);
         p.vals[start + t] = val;
+        if (p.fx_hi) {
+            // The same entry in the implicit-column form: section A, B
+            // (group = rank of the alpha single) or C, then its packet slot.
+            const int gr = __ldg(p.fx_grank + ra * p.fx_na + g);
+            const int pos = tya == 0 ? qpos : (tya == 1 ? p.fx_la + gr * p.fx_nlsp + qpos : p.fx_la + p.fx_lb + gr);
+            const int64_t sl = ra * p.fx_spa + (rb >> 5);
+            const int64_t at = ((sl * p.fx_npk + (pos >> 2)) * 32 + (rb & 31)) * 4 + (pos & 3);
+            float h, l;
+            split_hi_lo(val, h, l);
+            p.fx_hi[at] = h;
+            p.fx_lo[at] = l;
+        }
     }
 }
 
@@ -1182,7 +1202,7 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
 // single) transposed to [position][string].
 __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
                                    int grp1, int ns, int nd, int la, int32_t *atab, int32_t *bfull, int32_t *bsub,
-                                   uint16_t *bq) {
+                                   uint16_t *bq, int16_t *grank) {
     const int64_t n_f = static_cast<int64_t>(nbl) * nbeta, n_s = static_cast<int64_t>(grp1) * nbeta;
     const int64_t n_q = static_cast<int64_t>(la) * nbeta;
     const int64_t total = nalpha + n_f + n_s + n_q;
@@ -1198,13 +1218,16 @@ __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nal
                 if (ty == 1 && is < ns) {
                     row[is] = key;
                     row[ns + nd + is] = off;
+                    grank[i * na + g] = static_cast<int16_t>(is);
                     ++is;
                 } else if (ty == 2 && id < nd) {
                     row[ns + id] = key;
                     row[2 * ns + nd + id] = off;
+                    grank[i * na + g] = static_cast<int16_t>(id);
                     ++id;
                 } else if (ty == 0) {
                     row[w - 1] = off;
+                    grank[i * na + g] = 0;
                 }
             }
         } else if (i < nalpha + n_f) {
@@ -1588,12 +1611,15 @@ int pick_nw(int64_t nbasis) {
     return 0;
 }
 
-// Keeps the implicit-column tables of a full FullCI space when its beta
+// Sets up the implicit-column form of a full FullCI space when its beta
 // string count pads to a multiple of 32 with at most 1/4 extra rows (the
-// padding rows are streamed as zeros, still fewer bytes than int32 columns).
-// Tables only: the values are written by pyci_gpu_csr_prepare_mixed.
-int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, const StringTables &TB, int64_t nalpha,
-                int64_t nbeta, int na, int nbl, int grp1, int64_t len) {
+// padding rows are streamed as zeros, still fewer bytes than int32 columns):
+// the tables, and zeroed value arrays that the sorted fill then writes in
+// the same pass as the CSR (p.fx_*).  grank goes to `scratch`, freed after
+// the fill.
+int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, BuildParams &p, std::vector<void *> &scratch,
+                const StringTables &TA, const StringTables &TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
+                int grp1, int64_t len) {
     cudaStream_t st = ctx->stream;
     const int64_t nbp = (nbeta + 31) / 32 * 32;
     const int ns = TA.n1, nd = TA.n2;
@@ -1608,8 +1634,12 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
     const int w = 2 * (ns + nd) + 1;
     const size_t sa = sizeof(int32_t) * nalpha * w, sf = sizeof(int32_t) * nbl * nbeta,
                  ss = sizeof(int32_t) * grp1 * nbeta;
+    const int64_t npk = (la + lb + lc) / 4;
+    const size_t nval = static_cast<size_t>(nalpha) * (nbp / 32) * npk * 128;
     int32_t *atab = nullptr, *bfull = nullptr, *bsub = nullptr;
     uint16_t *bq = nullptr;
+    int16_t *grank = nullptr;
+    float *hi = nullptr, *lo = nullptr;
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&atab), sa, st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&bfull), sf, st);
@@ -1617,16 +1647,29 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
         e = cudaMallocAsync(reinterpret_cast<void **>(&bsub), ss, st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&bq), sizeof(uint16_t) * la * nbeta, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&grank), sizeof(int16_t) * nalpha * na, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&hi), sizeof(float) * nval, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&lo), sizeof(float) * nval, st);
+    // Padding entries and padding rows stay zero; the fill writes the rest.
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(hi, 0, sizeof(float) * nval, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(lo, 0, sizeof(float) * nval, st);
     if (e != cudaSuccess) {
         for (void *q : {static_cast<void *>(atab), static_cast<void *>(bfull), static_cast<void *>(bsub),
-                        static_cast<void *>(bq)})
+                        static_cast<void *>(bq), static_cast<void *>(grank), static_cast<void *>(hi),
+                        static_cast<void *>(lo)})
             if (q)
                 cudaFreeAsync(q, st);
-        return cuda_status(e, "cudaMallocAsync (implicit-column tables)");
+        return cuda_status(e, "cudaMallocAsync (implicit-column form)");
     }
+    scratch.push_back(grank);
     const int64_t total = nalpha + (static_cast<int64_t>(nbl) + grp1 + la) * nbeta;
     fcix_tables_kernel<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
-        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, la, atab, bfull, bsub, bq);
+        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, la, atab, bfull, bsub, bq, grank);
     ::pyci_gpu::note_launch();
     csr->fx_nalpha = nalpha;
     csr->fx_nbeta = nbeta;
@@ -1638,11 +1681,22 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
     csr->fx_la = la;
     csr->fx_lb = lb;
     csr->fx_lc = lc;
-    csr->fx_npk = (la + lb + lc) / 4;
+    csr->fx_npk = npk;
     csr->fx_atab = atab;
     csr->fx_bfull = bfull;
     csr->fx_bsub = bsub;
     csr->fx_bq = bq;
+    csr->fx_hi = hi;
+    csr->fx_lo = lo;
+    p.fx_hi = hi;
+    p.fx_lo = lo;
+    p.fx_grank = grank;
+    p.fx_spa = nbp / 32;
+    p.fx_npk = npk;
+    p.fx_la = la;
+    p.fx_lb = lb;
+    p.fx_nlsp = static_cast<int>(up4(grp1));
+    p.fx_na = na;
     return PYCI_GPU_OK;
 }
 
@@ -1762,6 +1816,8 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
                 ::pyci_gpu::note_launch();
             TB = TA;
         }
+        if (!rc)
+            rc = fcix_tables(ctx, csr, p, mem, TA, TB, nstr_a, nstr_b, na, nbl, grp1, uniform_len);
         if (!rc) {
             const int nsg = no_a * nv_a + no_b * nv_b;
             const size_t per_warp = (sizeof(RowState) + sizeof(double) * nsg + sizeof(int) * na + 15) & ~static_cast<size_t>(15);
@@ -1782,8 +1838,6 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
                     ::pyci_gpu::note_launch();
             }
         }
-        if (!rc)
-            rc = fcix_tables(ctx, csr, TA, TB, nstr_a, nstr_b, na, nbl, grp1, uniform_len);
         for (void *m : mem)
             cudaFreeAsync(m, st);
         if (rc)

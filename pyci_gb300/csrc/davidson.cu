@@ -488,7 +488,8 @@ public:
         // PYCI_GPU_FP64_PRODUCT=native keeps FP64 arithmetic in the FP64
         // solve's products even when the split is there.
         const char *e = std::getenv("PYCI_GPU_FP64_PRODUCT");
-        fp64_df_ = !mixed && csr->hi && csr->lo && !csr->lower_only && !(e && !std::strcmp(e, "native"));
+        fp64_df_ = !mixed && ((csr->hi && csr->lo) || csr->fx_hi) && !csr->lower_only &&
+                   !(e && !std::strcmp(e, "native"));
     }
 
     ~Davidson() {

@@ -33,9 +33,12 @@
 // a' * nbeta + b for 32 consecutive b) are coalesced global loads.  Each warp
 // keeps its lanes' section-B partner lists in shared memory.
 //
+// The build writes the values in this layout in the same pass as the CSR
+// (build.cu, fill_fci_tables_kernel).
+//
 // Tables (L1/L2-resident): atab[a] = the targets of a's singles and doubles
 // (sorted), their groups' offsets in the sorted CSR row and that of a's own
-// group (for the fill from the CSR); bfull[p][b] and bsub[p][b], the sorted
+// group; bfull[p][b] and bsub[p][b], the sorted
 // beta lists, transposed so the 32 lanes of a slice read consecutive words,
 // and bq, section A's list as 16-bit indices 4 per packet (one 8-byte load).
 
@@ -46,7 +49,6 @@
 #include <cstdint>
 
 #include "internal.h"
-#include "split_bits.h"
 
 namespace pyci_gpu {
 
@@ -286,61 +288,6 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
     }
 }
 
-// FCIX values from the FP64 CSR (sorted rows of uniform length len): one
-// block per (slice, 32 packets) stages the 32 rows' 128 entries in shared
-// memory, read from the CSR through the section -> sorted-position map of
-// the row's alpha string (atab offsets), splits them exactly (split_bits.h)
-// and writes the packets with coalesced 16-byte stores.
-__global__ void __launch_bounds__(256) fcix_fill_kernel(FxArgs A, int len, const double *__restrict__ vals,
-                                                        float4 *__restrict__ hi, float4 *__restrict__ lo) {
-    __shared__ double tile[32][129];
-    const int64_t chunks = (A.npk + 31) / 32;
-    for (int64_t blk = blockIdx.x; blk < A.nslice * chunks; blk += gridDim.x) {
-        const int64_t s = blk / chunks, qc = blk - s * chunks;
-        const int64_t a = s / A.spa;
-        const int64_t b0 = (s - a * A.spa) * 32;
-        const int64_t t0 = qc * 128;
-        const int32_t *arow = A.atab + a * A.aw;
-        for (int i = threadIdx.x; i < 32 * 128; i += blockDim.x) {
-            const int l = i >> 7, e = i & 127;
-            const int64_t b = b0 + l;
-            const int t = static_cast<int>(t0 + e);
-            int pos = -1; // sorted position in the row
-            if (t < A.la) {
-                if (t < A.nlb)
-                    pos = __ldg(arow + A.aw - 1) + t;
-            } else if (t < A.la + A.lb) {
-                const int tt = t - A.la, g = tt / A.nlsp, p = tt - g * A.nlsp;
-                if (g < A.ns && p < A.nls)
-                    pos = __ldg(arow + A.ns + A.nd + g) + p;
-            } else if (t < A.la + A.lb + A.lc) {
-                const int tt = t - A.la - A.lb;
-                if (tt < A.nd)
-                    pos = __ldg(arow + 2 * A.ns + A.nd + tt);
-            }
-            double v = 0.0;
-            if (b < A.nbeta && pos >= 0)
-                v = __ldcs(vals + (a * A.nbeta + b) * static_cast<int64_t>(len) + pos);
-            tile[l][e] = v;
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
-            const int pq = i >> 5, l = i & 31;
-            const int64_t q = qc * 32 + pq;
-            if (q < A.npk) {
-                float h[4], o[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j)
-                    split_hi_lo(tile[l][4 * pq + j], h[j], o[j]);
-                const int64_t at = (s * A.npk + q) * 32 + l;
-                hi[at] = make_float4(h[0], h[1], h[2], h[3]);
-                lo[at] = make_float4(o[0], o[1], o[2], o[3]);
-            }
-        }
-        __syncthreads();
-    }
-}
-
 inline FxArgs fx_args(const pyci_gpu_csr *csr) {
     FxArgs A;
     A.spa = csr->fx_nbp / 32;
@@ -396,40 +343,6 @@ bool fx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t s
 } // namespace pyci_gpu
 
 using namespace pyci_gpu;
-
-int fcix_fill(pyci_gpu_csr *csr) {
-    if (!csr->fx_atab || csr->fx_hi)
-        return PYCI_GPU_OK;
-    if (!csr->vals) {
-        set_error("operator has no FP64 values for its implicit-column form");
-        return PYCI_GPU_EINVAL;
-    }
-    const int64_t len = csr->nrow ? csr->nnz / csr->nrow : 0;
-    if (csr->nrow != csr->fx_nalpha * csr->fx_nbeta || len * csr->nrow != csr->nnz ||
-        len != csr->fx_nlb + static_cast<int64_t>(csr->fx_ns) * csr->fx_nls + csr->fx_nd) {
-        set_error("implicit-column form: operator rows do not match its string tables");
-        return PYCI_GPU_EINVAL;
-    }
-    cudaStream_t st = csr->ctx->stream;
-    const FxArgs A0 = fx_args(csr);
-    const size_t n = static_cast<size_t>(A0.nslice) * csr->fx_npk * 32 * 4;
-    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->fx_hi), sizeof(float) * n, st));
-    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&csr->fx_lo), sizeof(float) * n, st);
-    if (e != cudaSuccess) {
-        cudaFreeAsync(csr->fx_hi, st);
-        csr->fx_hi = nullptr;
-        return cuda_status(e, "cudaMallocAsync (implicit-column values)");
-    }
-    const FxArgs A = fx_args(csr);
-    const int64_t blocks = std::max<int64_t>(
-        1, std::min<int64_t>(static_cast<int64_t>(csr->ctx->num_sms) * 8, A.nslice * ((A.npk + 31) / 32)));
-    fcix_fill_kernel<<<static_cast<unsigned>(blocks), 256, 0, st>>>(A, static_cast<int>(len), csr->vals,
-                                                                     reinterpret_cast<float4 *>(csr->fx_hi),
-                                                                     reinterpret_cast<float4 *>(csr->fx_lo));
-    note_launch();
-    PYCI_CUDA_TRY(cudaGetLastError());
-    return PYCI_GPU_OK;
-}
 
 bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
                  cudaStream_t st) {

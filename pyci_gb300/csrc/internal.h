@@ -77,10 +77,10 @@ struct pyci_gpu_csr {
     // itself with every beta partner (sorted {b} + singles + doubles), B =
     // each alpha single with sorted {b} + beta singles (one group per
     // single), C = each alpha double with b; A, C and each group of B padded
-    // to a multiple of 4 entries.  Tables come from the sorted FullCI build,
-    // values (FP32 high and low parts, in 4-entry packets) from
-    // pyci_gpu_csr_prepare_mixed.  Null when the operator is not a full
-    // FullCI space.
+    // to a multiple of 4 entries.  Tables and values (FP32 high and low
+    // parts, in 4-entry packets) are written by the sorted FullCI build, in
+    // the same pass as the CSR.  Null when the operator is not a full FullCI
+    // space.
     int64_t fx_nalpha = 0, fx_nbeta = 0, fx_nbp = 0; // strings per spin; beta count padded to 32
     int64_t fx_npk = 0;           // 4-entry packets per row (padded length / 4)
     int fx_ns = 0, fx_nd = 0;     // alpha singles / doubles per alpha string
@@ -126,21 +126,20 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
 // xs[N][2K] holds each row's FP32 high parts then low parts; K = 1, 2 or 4.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t stream);
 void csr_release(pyci_gpu_csr *csr);
-// Implicit-column form (fcix.cu).  fcix_fill writes fx_hi / fx_lo from the
-// FP64 values; fcix_launch runs one product on it: mode 0 FP32 (x, y
+// Implicit-column form (fcix.cu).  fcix_launch runs one product on it: mode 0 FP32 (x, y
 // float [N][K], K <= 8), mode 2 double-float (xs float [N][2K], y double
 // [N][K], K = 1, 2, 4).  FP64 arithmetic is not offered: forming hi + lo in
 // FP64 costs three FP64 instructions per entry on top of the FMA, and this
 // GPU's FP64 pipe already bounds the CSR FP64 product.  Returns false when
 // the operator has no values in this form or the operands do not fit it (the
 // caller then uses another kernel).
-int fcix_fill(pyci_gpu_csr *csr);
 bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
                  cudaStream_t st);
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
 int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,
                       double *vabs, double *vwsum);
 int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64);
+int csr_ensure_split(pyci_gpu_csr *csr);
 int add_all_dets_device(pyci_gpu_ctx *ctx, int kind, int64_t nbasis, int64_t nocc_up,
                         int64_t nocc_dn, uint64_t *dets_host);
 int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, int64_t maxiter,

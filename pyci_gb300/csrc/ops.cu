@@ -372,9 +372,38 @@ static int sell_build(pyci_gpu_csr *csr) {
     return PYCI_GPU_OK;
 }
 
+// The exact FP32 high/low split in CSR order (for the CSR and SELL-32
+// kernels and the batched solver); a no-op once it exists.
+int csr_ensure_split(pyci_gpu_csr *csr) {
+    if (csr->hi && csr->lo)
+        return PYCI_GPU_OK;
+    cudaStream_t st = csr->ctx->stream;
+    if (!csr->vals) {
+        set_error("operator has no FP64 values to split");
+        return PYCI_GPU_EINVAL;
+    }
+    const int64_t n = csr->nnz ? csr->nnz : 1;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->hi), sizeof(float) * n, st));
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->lo), sizeof(float) * n, st));
+    if (csr->nnz > 0)
+        split_kernel<<<grid_for(csr->ctx, csr->nnz, 256), 256, 0, st>>>(csr->nnz, csr->vals, csr->hi, csr->lo),
+            ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
 int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
     cudaStream_t st = csr->ctx->stream;
-    if (!csr->hi) {
+    if (csr->fx_hi) {
+        // A full FullCI space: the build wrote the implicit-column form, which
+        // serves the FP32 and double-float products; the CSR-order split is
+        // made on demand (csr_ensure_split), or here when the FP64 values go.
+        if (drop_fp64 && csr->vals) {
+            int rc = csr_ensure_split(csr);
+            if (rc)
+                return rc;
+        }
+    } else if (!csr->hi) {
         if (!csr->vals) {
             set_error("operator has no FP64 values to split");
             return PYCI_GPU_EINVAL;
@@ -386,11 +415,7 @@ int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
             split_kernel<<<grid_for(csr->ctx, csr->nnz, 256), 256, 0, st>>>(csr->nnz, csr->vals,
                                                                            csr->hi, csr->lo), ::pyci_gpu::note_launch();
         PYCI_CUDA_TRY(cudaGetLastError());
-        // A full FullCI space also gets its values in the implicit-column
-        // form (fcix.cu); the autotuner picks per product.
-        int rc = csr->fx_atab ? fcix_fill(csr) : PYCI_GPU_OK;
-        if (!rc)
-            rc = sell_build(csr);
+        int rc = sell_build(csr);
         if (rc)
             return rc;
     }

@@ -556,6 +556,12 @@ bool autotune_enabled() {
     return on;
 }
 
+// Whether PYCI_GPU_SPMM pins products to the CSR or SELL-32 kernels.
+bool pinned_to_csr() {
+    const char *e = std::getenv("PYCI_GPU_SPMM");
+    return e && (!std::strcmp(e, "csr") || !std::strcmp(e, "sell") || !std::strcmp(e, "sell1"));
+}
+
 // PYCI_GPU_SPMM=fcix, =sell, =sell1 or =csr pins the products of an operator
 // (read when it makes its first product of a kind, so a process can compare
 // them): the implicit-column form (FP32 and double-float; full FullCI
@@ -930,6 +936,17 @@ using namespace pyci_gpu;
 // arithmetic with double-float accumulation; the tile variant (lanes per row x
 // entry mapping, as the other products) is tuned on first use.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
+    if ((!csr->hi || !csr->lo) && csr->fx_hi) {
+        // Implicit-column form only (a full FullCI space).
+        if ((K == 1 || K == 2 || K == 4) && !pinned_to_csr() && fcix_launch(csr, 2, K, xs, 2 * K, y, K, st)) {
+            csr->tuned[kSplitDF][K] = kFxVariant;
+            PYCI_CUDA_TRY(cudaGetLastError());
+            return PYCI_GPU_OK;
+        }
+        int rc = csr_ensure_split(const_cast<pyci_gpu_csr *>(csr));
+        if (rc)
+            return rc;
+    }
     if (!csr->hi || !csr->lo) {
         set_error("split product needs pyci_gpu_csr_prepare_mixed first");
         return PYCI_GPU_EINVAL;
@@ -1075,6 +1092,18 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
         }
         break;
     case PYCI_PREC_FP32:
+        if (!csr->hi && csr->fx_hi) {
+            // Only the implicit-column form holds FP32 values (a full FullCI
+            // space): up to 8 vectors in one launch; the CSR-order split is
+            // made on demand for anything else.
+            if (k <= 8 && !pinned_to_csr() && fcix_launch(csr, 0, static_cast<int>(k), x, k, y, k, stream)) {
+                csr->tuned[kF32][k] = kFxVariant;
+                break;
+            }
+            int rc = csr_ensure_split(const_cast<pyci_gpu_csr *>(csr));
+            if (rc)
+                return rc;
+        }
         if (!csr->hi) {
             set_error("FP32 product needs pyci_gpu_csr_prepare_mixed first");
             return PYCI_GPU_EINVAL;
@@ -1082,6 +1111,11 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
         launch_vk<kF32>(csr, Values<kF32>{csr->hi}, k, x, y, stream);
         break;
     case PYCI_PREC_FP64_SPLIT:
+        if (!csr->hi && csr->fx_hi) {
+            int rc = csr_ensure_split(const_cast<pyci_gpu_csr *>(csr));
+            if (rc)
+                return rc;
+        }
         if (!csr->hi || !csr->lo) {
             set_error("split product needs pyci_gpu_csr_prepare_mixed first");
             return PYCI_GPU_EINVAL;
