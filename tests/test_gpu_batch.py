@@ -97,3 +97,37 @@ def test_batch_rejects_bad_input(ctx):
     with pytest.raises(TypeError):
         capi.batch_solve(ctx, [rect], [0.0])
     rect.free()
+
+
+def test_batch_with_the_largest_workload_problems(ctx):
+    r"""Problems of the 64-problem workload (problem i: seed 5000 + i, nbasis
+    and alpha = beta drawn from default_rng(4242)) including the largest it
+    holds, 12 orbitals with 6 + 6 electrons (853,776 rows, 1.55e9 stored
+    entries), and a spread of small and medium ones, in one batched mixed
+    solve: every problem's 4 roots within 1 uHa of its own single FP64
+    solve (tol 1e-9)."""
+    from math import comb
+    rng = np.random.default_rng(4242)
+    draws = []
+    for i in range(64):
+        n = int(rng.choice([8, 10, 12]))
+        a = int(rng.integers(2, n // 2 + 1))
+        draws.append((n, a, 5000 + i))
+    big = next(d for d in draws if d[0] == 12 and d[1] == 6)
+    rest = sorted({(n, a): (n, a, s) for n, a, s in draws if (n, a) != (12, 6)}.values())
+    chosen = [big] + rest[::2]
+    ops, ecore = [], []
+    for n, a, seed in chosen:
+        e, one, two = synthetic_integrals(n, seed)
+        csr = capi.Csr(ctx, capi.WFN_FULLCI, n, a, a, None, one, two, flags=capi.BUILD_FULL_COLEX,
+                       ndet=comb(n, a) ** 2)
+        csr.prepare_mixed()
+        ops.append(csr)
+        ecore.append(e)
+    assert ops[0].shape()[0] == 853776
+    evals, stats = capi.batch_solve(ctx, ops, ecore, n=4, tol=1e-6, mode=capi.SOLVE_MIXED)
+    for p, c in enumerate(ops):
+        ref, _, _ = c.solve(n=4, tol=1e-9, ecore=ecore[p], mode=capi.SOLVE_FP64, evecs=False)
+        np.testing.assert_allclose(evals[p], ref, rtol=0, atol=1e-6)
+    for c in ops:
+        c.free()
