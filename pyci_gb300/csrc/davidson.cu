@@ -383,15 +383,26 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
          r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const double d = diag[r];
-        for (int c = 0; c < cols.n; ++c) {
-            const int j = cols.src[c];
-            double den = cols.theta[c] - d;
-            if (fabs(den) < 1e-8)
-                den = (den < 0.0) ? -1e-8 : 1e-8;
-            if constexpr (sizeof(TO) == 4)
-                out[c * N + r] = static_cast<float>(R[j * N + r]) / static_cast<float>(den);
-            else
+        if constexpr (sizeof(TO) == 4) {
+            // FP32 corrections: the quotient in FP32 arithmetic (one FP64
+            // conversion per row; this GPU's FP64 rate is a small fraction of
+            // its FP32 rate, and a preconditioner needs no FP64 accuracy).
+            const float df = static_cast<float>(d);
+            for (int c = 0; c < cols.n; ++c) {
+                const int j = cols.src[c];
+                float den = static_cast<float>(cols.theta[c]) - df;
+                if (fabsf(den) < 1e-8f)
+                    den = (den < 0.0f) ? -1e-8f : 1e-8f;
+                out[c * N + r] = static_cast<float>(R[j * N + r]) * __frcp_rn(den);
+            }
+        } else {
+            for (int c = 0; c < cols.n; ++c) {
+                const int j = cols.src[c];
+                double den = cols.theta[c] - d;
+                if (fabs(den) < 1e-8)
+                    den = (den < 0.0) ? -1e-8 : 1e-8;
                 out[c * N + r] = static_cast<TO>(static_cast<double>(R[j * N + r]) / den);
+            }
         }
     }
 }
@@ -463,6 +474,65 @@ __global__ void unit_kernel(T *V, int64_t N, const int64_t *idx, int k) {
 }
 
 // v = e_idx + amp * noise(., col): one perturbed start vector.
+// Arg-min of (d[r], r) over the rows whose pair is above *prev (pairs
+// ordered by value, then row; all rows when prev is null), as (value, row)
+// in a double2 per block (row as a double: exact below 2^53; (+inf, -1)
+// when a block has no candidate).  argmin_final_kernel reduces the blocks.
+__device__ __forceinline__ bool pair_less(double va, double ia, double vb, double ib) {
+    return va < vb || (va == vb && ia < ib);
+}
+
+__device__ __forceinline__ void pair_min_block(double &v, double &i) {
+    __shared__ double sv[32], si[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
+        if (pair_less(ov, oi, v, i))
+            v = ov, i = oi;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0)
+        sv[w] = v, si[w] = i;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < static_cast<int>(blockDim.x >> 5) ? sv[lane] : INFINITY;
+        i = lane < static_cast<int>(blockDim.x >> 5) ? si[lane] : -1.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
+            if (pair_less(ov, oi, v, i))
+                v = ov, i = oi;
+        }
+    }
+}
+
+__global__ void argmin_above_kernel(const double *__restrict__ d, int64_t N, const double2 *prev,
+                                    double2 *__restrict__ partial) {
+    const double lv = prev ? prev->x : -INFINITY, li = prev ? prev->y : -1.0;
+    double bv = INFINITY, bi = -1.0;
+    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double v = d[r], ri = static_cast<double>(r);
+        if (pair_less(lv, li, v, ri) && pair_less(v, ri, bv, bi))
+            bv = v, bi = ri;
+    }
+    pair_min_block(bv, bi);
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] = make_double2(bv, bi);
+}
+
+__global__ void argmin_final_kernel(const double2 *__restrict__ partial, int nb, double2 *out) {
+    double bv = INFINITY, bi = -1.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+        const double2 p = partial[b];
+        if (p.y >= 0.0 && pair_less(p.x, p.y, bv, bi))
+            bv = p.x, bi = p.y;
+    }
+    pair_min_block(bv, bi);
+    if (threadIdx.x == 0)
+        *out = make_double2(bv, bi);
+}
+
 template<typename T>
 __global__ void guess_kernel(T *v, int64_t N, int64_t idx, double amp, int col) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
@@ -661,6 +731,30 @@ private:
             precondition_kernel<U, T><<<grid(N_), 256, 0, st_>>>(R, diag, make_cols(todo, c0, theta), N_,
                                                                   out + static_cast<int64_t>(c0) * N_),
                 ::pyci_gpu::note_launch();
+    }
+
+    // Rows of the k lowest diagonal elements, ascending (ties by row), found
+    // on the device: k passes of a grid-wide arg-min over the (value, row)
+    // pairs above the previous pick, one read of the diagonal each.
+    int lowest_diagonal(const double *d_diag, int64_t N, int k, std::vector<int64_t> &order) {
+        double2 *picks = nullptr, *partial = nullptr;
+        const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, 2 * csr_->ctx->num_sms)));
+        int rc;
+        if ((rc = alloc(&picks, k)) || (rc = alloc(&partial, nb)))
+            return rc;
+        for (int j = 0; j < k; ++j) {
+            argmin_above_kernel<<<nb, 256, 0, st_>>>(d_diag, N, j > 0 ? picks + j - 1 : nullptr, partial);
+            argmin_final_kernel<<<1, 256, 0, st_>>>(partial, nb, picks + j);
+            ::pyci_gpu::note_launch();
+            ::pyci_gpu::note_launch();
+        }
+        std::vector<double2> h(k);
+        PYCI_CUDA_TRY(cudaMemcpyAsync(h.data(), picks, sizeof(double2) * k, cudaMemcpyDeviceToHost, st_));
+        PYCI_CUDA_TRY(wait());
+        order.resize(k);
+        for (int j = 0; j < k; ++j)
+            order[j] = static_cast<int64_t>(h[j].y);
+        return PYCI_GPU_OK;
     }
 
     // Orthonormalise vectors V[m..m+k) against V[0..m) and each other;
@@ -937,10 +1031,6 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     }
     double *d_diag = csr_->diag;
 
-    // Diagonal on the host for the initial guess.
-    std::vector<double> diag(N);
-    PYCI_CUDA_TRY(cudaMemcpyAsync(diag.data(), d_diag, sizeof(double) * N, cudaMemcpyDeviceToHost, st_));
-    PYCI_CUDA_TRY(wait());
 
     // Initial block.
     int m = 0, knew = 0;
@@ -959,11 +1049,10 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         // Unit vectors on the lowest diagonal elements (after c0, if given),
         // each with a small seeded component in every row, topped up until
         // the block holds b independent vectors.
-        std::vector<int64_t> order(N);
-        std::iota(order.begin(), order.end(), 0);
         const int64_t nsort = std::min<int64_t>(N, 2 * b + 8);
-        std::partial_sort(order.begin(), order.begin() + nsort, order.end(),
-                          [&](int64_t x, int64_t y) { return diag[x] < diag[y] || (diag[x] == diag[y] && x < y); });
+        std::vector<int64_t> order;
+        if ((rc = lowest_diagonal(d_diag, N, static_cast<int>(nsort), order)))
+            return rc;
         const double amp = kGuessNoise / std::sqrt(static_cast<double>(N));
         int64_t next = 0;
         if (c0) {
@@ -975,14 +1064,19 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if ((rc = orthonormalize(V, 0, 1, knew)))
                 return rc;
         }
+        // All missing start vectors at once, then one block
+        // orthonormalisation (a few host round trips instead of several per
+        // vector); dependent ones are dropped and replaced.
         while (knew < b && next < N) {
-            const int64_t pick = (next < nsort) ? order[next] : next;
-            guess_kernel<T><<<grid(N), 256, 0, st_>>>(V + static_cast<int64_t>(knew) * N, N, pick, amp,
-                                                        static_cast<int>(next)),
-                ::pyci_gpu::note_launch();
-            ++next;
+            const int need = static_cast<int>(std::min<int64_t>(b - knew, N - next));
+            for (int j = 0; j < need; ++j, ++next) {
+                const int64_t pick = (next < nsort) ? order[next] : next;
+                guess_kernel<T><<<grid(N), 256, 0, st_>>>(V + static_cast<int64_t>(knew + j) * N, N, pick, amp,
+                                                            static_cast<int>(next)),
+                    ::pyci_gpu::note_launch();
+            }
             int got = 0;
-            if ((rc = orthonormalize(V, knew, 1, got)))
+            if ((rc = orthonormalize(V, knew, need, got)))
                 return rc;
             knew += got;
         }
