@@ -152,6 +152,88 @@ __global__ void __launch_bounds__(256) batch_spmm_kernel(const BatchOp *__restri
     }
 }
 
+// One SpMM tile: rows [lr0, lr1) of problem prob, `lanes` lanes per row.
+struct BatchTile {
+    int64_t lr0, lr1;
+    int prob, lanes;
+};
+
+// Rows [lr0, lr1) of one problem at LANES lanes per row, by one block.
+template<int VK, int K, int LANES, typename XT>
+__device__ __forceinline__ void tile_rows(const BatchOp &op, int64_t lr0, int64_t lr1, const XT *__restrict__ x,
+                                          XT *__restrict__ y) {
+    typedef typename std::conditional<VK == 1, float, double>::type acc_t;
+    const int lane = threadIdx.x % LANES;
+    const int group = threadIdx.x / LANES, ngroups = blockDim.x / LANES;
+    const XT *xb = x + op.row0 * K;
+    for (int64_t lr = lr0 + group; lr < lr1; lr += ngroups) {
+        const int64_t start = op.rowptr[lr], end = op.rowptr[lr + 1];
+        acc_t acc[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            acc[j] = 0;
+        for (int64_t e = start + lane; e < end; e += LANES) {
+            const int64_t col = __ldcs(op.cols + e);
+            acc_t v;
+            if (VK == 0)
+                v = static_cast<acc_t>(__ldcs(op.vals + e));
+            else if (VK == 1)
+                v = static_cast<acc_t>(__ldcs(op.hi + e));
+            else
+                v = static_cast<acc_t>(static_cast<double>(__ldcs(op.hi + e)) + static_cast<double>(__ldcs(op.lo + e)));
+            const XT *xr = xb + col * K;
+            if constexpr (K == 4 && sizeof(XT) == 4) {
+                const float4 q = __ldg(reinterpret_cast<const float4 *>(xr));
+                acc[0] += v * q.x;
+                acc[1] += v * q.y;
+                acc[2] += v * q.z;
+                acc[3] += v * q.w;
+            } else {
+#pragma unroll
+                for (int j = 0; j < K; ++j)
+                    acc[j] += v * static_cast<acc_t>(__ldg(xr + j));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+#pragma unroll
+            for (int o = LANES / 2; o > 0; o >>= 1)
+                acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o, LANES);
+        }
+        if (lane < K) {
+            acc_t out = acc[0];
+#pragma unroll
+            for (int j = 1; j < K; ++j)
+                if (lane == j)
+                    out = acc[j];
+            y[(op.row0 + lr) * K + lane] = static_cast<XT>(out);
+        }
+    }
+}
+
+// The block-diagonal product of every active problem in one persistent
+// launch: a grid of (SMs x resident blocks) walks the tile list (tile t by
+// block t mod grid), each tile at its problem's tuned lanes per row.  Tiles
+// and their count live in device memory, so a captured graph replays the
+// launch with the current active set.
+template<int VK, int K, typename XT>
+__global__ void __launch_bounds__(256) batch_tile_spmm_kernel(const BatchOp *__restrict__ ops,
+                                                              const BatchTile *__restrict__ tiles,
+                                                              const int *__restrict__ ntiles,
+                                                              const XT *__restrict__ x, XT *__restrict__ y) {
+    const int nt = *ntiles;
+    for (int t = blockIdx.x; t < nt; t += gridDim.x) {
+        const BatchTile T = tiles[t];
+        const BatchOp op = ops[T.prob];
+        if (T.lanes == 8)
+            tile_rows<VK, K, 8>(op, T.lr0, T.lr1, x, y);
+        else if (T.lanes == 16)
+            tile_rows<VK, K, 16>(op, T.lr0, T.lr1, x, y);
+        else
+            tile_rows<VK, K, 32>(op, T.lr0, T.lr1, x, y);
+    }
+}
+
 // Block-diagonal FP64-accurate product in FP32 arithmetic for the final
 // Rayleigh-Ritz step: y[r][0..4) = (hi + lo) x over problem rows, x split as
 // xs[r] = (4 high parts, 4 low parts); exact products via FMA and
@@ -599,6 +681,7 @@ private:
     // Active set (rows and Gram tiles) = the problems with mask[p] != 0.
     int set_active(const std::vector<int> &mask) {
         int rc;
+        tiles_dirty_ = true;
         if ((rc = set_rowset(act_, mask)))
             return rc;
         for (int c = 0; c < kClasses; ++c) {
@@ -747,6 +830,45 @@ private:
         }
     }
 
+    // Tile list of the active problems: row blocks of about target stored
+    // entries (a multiple of the rows one block covers at once), at each
+    // problem's class lanes per row; uploaded with its count.
+    int build_tiles(int64_t target) {
+        std::vector<BatchTile> t;
+        for (int p : act_.members) {
+            const pyci_gpu_csr *c = ops_[p];
+            const int lanes = cls_lanes_[cls_of_[p]];
+            const int64_t per = 256 / lanes;
+            const double avg = c->nrow ? static_cast<double>(c->nnz) / c->nrow : 1.0;
+            int64_t rows = std::max<int64_t>(per, static_cast<int64_t>(target / std::max(avg, 1.0)));
+            rows = (rows + per - 1) / per * per;
+            for (int64_t r = 0; r < c->nrow; r += rows)
+                t.push_back(BatchTile{r, std::min(r + rows, c->nrow), p, lanes});
+        }
+        if (static_cast<int64_t>(t.size()) > tile_cap_) {
+            set_error("batched SpMM: %zu tiles exceed the %lld allocated", t.size(), static_cast<long long>(tile_cap_));
+            return PYCI_GPU_EUNSUPPORTED;
+        }
+        const int n = static_cast<int>(t.size());
+        if (n)
+            PYCI_CUDA_TRY(cudaMemcpyAsync(d_tiles_, t.data(), sizeof(BatchTile) * n, cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaMemcpyAsync(d_ntiles_, &n, sizeof(int), cudaMemcpyHostToDevice, st_));
+        PYCI_CUDA_TRY(cudaStreamSynchronize(st_)); // host sources are temporaries
+        tiles_dirty_ = false;
+        return PYCI_GPU_OK;
+    }
+
+    // The block-diagonal product Xi_ -> Yi_ of every active problem in one
+    // persistent launch over the tile list.
+    void spmm_tiles(int prec) {
+        if (prec == PYCI_PREC_FP32)
+            batch_tile_spmm_kernel<1, 4, T><<<tile_grid_, 256, 0, st_>>>(d_ops_, d_tiles_, d_ntiles_, Xi_, Yi_);
+        else if (prec == PYCI_PREC_FP64_SPLIT)
+            batch_tile_spmm_kernel<2, 4, T><<<tile_grid_, 256, 0, st_>>>(d_ops_, d_tiles_, d_ntiles_, Xi_, Yi_);
+        else
+            batch_tile_spmm_kernel<0, 4, T><<<tile_grid_, 256, 0, st_>>>(d_ops_, d_tiles_, d_ntiles_, Xi_, Yi_);
+    }
+
     // Two Cholesky-QR passes of the b vectors in Tnew_ inside each active
     // problem's block: columns with use == 0 are left out, dependent ones are
     // dropped (use set to 0).  The kept orthonormal vectors of problem p are
@@ -781,6 +903,14 @@ private:
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_prec_ = -1;
     const void *graph_v_ = nullptr;
+    // Persistent SpMM tiles (batch_tile_spmm_kernel): the active problems'
+    // row blocks of about tile_nnz_ stored entries each, at their class's
+    // lanes per row; rebuilt when the active set changes.
+    BatchTile *d_tiles_ = nullptr;
+    int *d_ntiles_ = nullptr;
+    int64_t tile_cap_ = 0, tile_nnz_ = 1 << 18;
+    bool tiles_dirty_ = true, tiles_tuned_ = false;
+    unsigned tile_grid_ = 1;
     bool all_vals_ = true;
     int64_t matvecs_ = 0;
     double spmm_ms_ = 0.0;
@@ -845,11 +975,64 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             cudaEventDestroy(eb);
             cls_tuned_ = true;
         }
+        if (!tiles_tuned_) {
+            // Row-block size of the persistent product: time the tile lists
+            // of ~64K, ~256K and ~1M stored entries per tile (lanes per row
+            // as tuned above) and keep the fastest.
+            int64_t nnz_act = 0;
+            for (int p : act_.members)
+                nnz_act += ops_[p]->nnz;
+            const auto key = std::make_tuple(prec + 16, act_.total, nnz_act);
+            bool cached = false;
+            {
+                std::lock_guard<std::mutex> lock(g_class_tune_mutex);
+                auto it = g_class_tune.find(key);
+                if (it != g_class_tune.end()) {
+                    tile_nnz_ = int64_t(1) << it->second;
+                    cached = true;
+                }
+            }
+            if (!cached) {
+                batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
+                cudaEvent_t ea, eb;
+                cudaEventCreate(&ea);
+                cudaEventCreate(&eb);
+                float best = 1e30f;
+                int best_sh = 18;
+                for (int sh : {16, 18, 20}) {
+                    int rc = build_tiles(int64_t(1) << sh);
+                    if (rc)
+                        return rc;
+                    spmm_tiles(prec);
+                    cudaEventRecord(ea, st_);
+                    spmm_tiles(prec);
+                    cudaEventRecord(eb, st_);
+                    PYCI_CUDA_TRY(cudaEventSynchronize(eb));
+                    float ms = 0.0f;
+                    cudaEventElapsedTime(&ms, ea, eb);
+                    if (ms < best) {
+                        best = ms;
+                        best_sh = sh;
+                    }
+                }
+                cudaEventDestroy(ea);
+                cudaEventDestroy(eb);
+                tile_nnz_ = int64_t(1) << best_sh;
+                tiles_dirty_ = true;
+                std::lock_guard<std::mutex> lock(g_class_tune_mutex);
+                g_class_tune[key] = best_sh;
+            }
+            tiles_tuned_ = true;
+        }
+        if (tiles_dirty_) {
+            int rc = build_tiles(tile_nnz_);
+            if (rc)
+                return rc;
+        }
         cudaGraph_t g;
         PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
-        for (int c = 0; c < kClasses; ++c)
-            spmm_class(prec, cls_lanes_[c], cls_[c]);
+        spmm_tiles(prec);
         batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, d_base_, rs, d_row0_, W, Wnew_);
         cudaError_t e = cudaStreamEndCapture(st_, &g);
         if (e != cudaSuccess)
@@ -861,12 +1044,17 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
         graph_prec_ = prec;
         graph_v_ = V;
     }
+    if (tiles_dirty_) {
+        int rc = build_tiles(tile_nnz_); // active set changed: the graph reads the new list
+        if (rc)
+            return rc;
+    }
     cudaEvent_t a, c;
     cudaEventCreate(&a);
     cudaEventCreate(&c);
     cudaEventRecord(a, st_);
     PYCI_CUDA_TRY(cudaGraphLaunch(graph_exec_, st_));
-    for (int i = 0; i < 2 + kClasses; ++i) // pack, one product per class, unpack
+    for (int i = 0; i < 3; ++i) // pack, one persistent product, unpack
         ::pyci_gpu::note_launch();
     cudaEventRecord(c, st_);
     PYCI_CUDA_TRY(cudaEventSynchronize(c));
@@ -998,6 +1186,22 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         (rc = alloc_rowset(act_)) || (rc = alloc_rowset(sel_)) || (rc = alloc_rowset(cls_[0])) ||
         (rc = alloc_rowset(cls_[1])) || (rc = alloc_rowset(cls_[2])))
         return rc;
+    // Tile capacity: every problem cut at the smallest tile size the tuner
+    // tries (2^16 entries) or 8 rows, whichever gives more tiles.
+    for (int p = 0; p < P; ++p) {
+        const double avg = ops_[p]->nrow ? static_cast<double>(ops_[p]->nnz) / ops_[p]->nrow : 1.0;
+        const int64_t rows = std::max<int64_t>(8, static_cast<int64_t>((int64_t(1) << 16) / std::max(avg, 1.0)) / 8 * 8);
+        tile_cap_ += (ops_[p]->nrow + rows - 1) / rows + 1;
+    }
+    if ((rc = alloc(&d_tiles_, tile_cap_)) || (rc = alloc(&d_ntiles_, 1)))
+        return rc;
+    {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_tile_spmm_kernel<1, 4, T>, 256, 0) !=
+                cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        tile_grid_ = static_cast<unsigned>(ctx_->num_sms * per_sm);
+    }
     // Every vector buffer starts at zero, so slots a problem has not written
     // yet hold finite values wherever a kernel reads them.
     for (auto pr : {std::make_pair(V, mmax), std::make_pair(W, mmax), std::make_pair(X, nt), std::make_pair(AX, nt),
