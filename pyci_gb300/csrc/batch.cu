@@ -905,7 +905,8 @@ private:
     const void *graph_v_ = nullptr;
     // Persistent SpMM tiles (batch_tile_spmm_kernel): the active problems'
     // row blocks of about tile_nnz_ stored entries each, at their class's
-    // lanes per row; rebuilt when the active set changes.
+    // lanes per row; rebuilt when the active set changes.  tile_nnz_ = 0:
+    // the tuner chose the per-class launches instead.
     BatchTile *d_tiles_ = nullptr;
     int *d_ntiles_ = nullptr;
     int64_t tile_cap_ = 0, tile_nnz_ = 1 << 18;
@@ -976,9 +977,10 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             cls_tuned_ = true;
         }
         if (!tiles_tuned_) {
-            // Row-block size of the persistent product: time the tile lists
-            // of ~64K, ~256K and ~1M stored entries per tile (lanes per row
-            // as tuned above) and keep the fastest.
+            // Form of the product: one grid-stride launch per tile class, or
+            // the persistent launch over tile lists of ~64K, ~256K or ~1M
+            // stored entries per tile (lanes per row as tuned above); the
+            // fastest is kept (tile_nnz_ = 0: per-class launches).
             int64_t nnz_act = 0;
             for (int p : act_.members)
                 nnz_act += ops_[p]->nnz;
@@ -988,7 +990,7 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
                 std::lock_guard<std::mutex> lock(g_class_tune_mutex);
                 auto it = g_class_tune.find(key);
                 if (it != g_class_tune.end()) {
-                    tile_nnz_ = int64_t(1) << it->second;
+                    tile_nnz_ = it->second ? int64_t(1) << it->second : 0;
                     cached = true;
                 }
             }
@@ -997,8 +999,17 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
                 cudaEvent_t ea, eb;
                 cudaEventCreate(&ea);
                 cudaEventCreate(&eb);
+                // Candidate 0: one grid-stride launch per tile class.
+                for (int c = 0; c < kClasses; ++c)
+                    spmm_class(prec, cls_lanes_[c], cls_[c]);
+                cudaEventRecord(ea, st_);
+                for (int c = 0; c < kClasses; ++c)
+                    spmm_class(prec, cls_lanes_[c], cls_[c]);
+                cudaEventRecord(eb, st_);
+                PYCI_CUDA_TRY(cudaEventSynchronize(eb));
                 float best = 1e30f;
-                int best_sh = 18;
+                cudaEventElapsedTime(&best, ea, eb);
+                int best_sh = 0;
                 for (int sh : {16, 18, 20}) {
                     int rc = build_tiles(int64_t(1) << sh);
                     if (rc)
@@ -1017,14 +1028,14 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
                 }
                 cudaEventDestroy(ea);
                 cudaEventDestroy(eb);
-                tile_nnz_ = int64_t(1) << best_sh;
+                tile_nnz_ = best_sh ? int64_t(1) << best_sh : 0;
                 tiles_dirty_ = true;
                 std::lock_guard<std::mutex> lock(g_class_tune_mutex);
                 g_class_tune[key] = best_sh;
             }
             tiles_tuned_ = true;
         }
-        if (tiles_dirty_) {
+        if (tiles_dirty_ && tile_nnz_) {
             int rc = build_tiles(tile_nnz_);
             if (rc)
                 return rc;
@@ -1032,7 +1043,12 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
         cudaGraph_t g;
         PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
-        spmm_tiles(prec);
+        if (tile_nnz_) {
+            spmm_tiles(prec);
+        } else {
+            for (int c = 0; c < kClasses; ++c)
+                spmm_class(prec, cls_lanes_[c], cls_[c]);
+        }
         batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, d_base_, rs, d_row0_, W, Wnew_);
         cudaError_t e = cudaStreamEndCapture(st_, &g);
         if (e != cudaSuccess)
@@ -1044,7 +1060,7 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
         graph_prec_ = prec;
         graph_v_ = V;
     }
-    if (tiles_dirty_) {
+    if (tiles_dirty_ && tile_nnz_) {
         int rc = build_tiles(tile_nnz_); // active set changed: the graph reads the new list
         if (rc)
             return rc;
@@ -1054,7 +1070,7 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
     cudaEventCreate(&c);
     cudaEventRecord(a, st_);
     PYCI_CUDA_TRY(cudaGraphLaunch(graph_exec_, st_));
-    for (int i = 0; i < 3; ++i) // pack, one persistent product, unpack
+    for (int i = 0; i < (tile_nnz_ ? 3 : 2 + kClasses); ++i) // pack, the product(s), unpack
         ::pyci_gpu::note_launch();
     cudaEventRecord(c, st_);
     PYCI_CUDA_TRY(cudaEventSynchronize(c));
