@@ -42,10 +42,13 @@ constexpr int kMaxGramP = 128;
 constexpr int kMaxQ = 8;
 // FP32 Gram products with at least this many A vectors run on the tensor
 // cores (gram_tc.cu); narrower ones on the CUDA cores, where the tensor-core
-// version is bound by its per-tile MMA latency (measured on 10.5M-row
-// vectors, q = 4: p = 64 1.18 ms vs 1.31 ms on CUDA cores, p = 128 (q = 8)
-// 2.0 vs 2.9 ms, but p = 32 0.93 vs 0.72 ms and p = 8 0.81 vs 0.30 ms).
-constexpr int kGramTcMinP = 48;
+// version is bound by its per-tile MMA latency.  With the CUDA-core kernel's
+// vector blocks of one row range running together (B re-read from L2), the
+// tensor cores win only for the widest blocks (10.5M-row vectors, wall time
+// per call: p = 128, q = 8: 2.06 vs 2.42 ms; p = 64, q = 4: 1.07 vs 1.20 ms
+// with ~0.5 ms of call overhead in both; in the 32-orbital DOCI solve the
+// p >= 48 tensor-core Grams took 0.92 ms of device time each).
+constexpr int kGramTcMinP = 96;
 
 // Xi[r * kp + j] = V[j * N + r] for j < k, 0 for k <= j < kp (padding to a
 // width the SpMM gathers with vector loads).
@@ -510,8 +513,21 @@ __global__ void argmin_above_kernel(const double *__restrict__ d, int64_t N, con
                                     double2 *__restrict__ partial) {
     const double lv = prev ? prev->x : -INFINITY, li = prev ? prev->y : -1.0;
     double bv = INFINITY, bi = -1.0;
-    for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    for (; r + 3 * stride < N; r += 4 * stride) {
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            v[u] = __ldg(d + r + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double ri = static_cast<double>(r + u * stride);
+            if (pair_less(lv, li, v[u], ri) && pair_less(v[u], ri, bv, bi))
+                bv = v[u], bi = ri;
+        }
+    }
+    for (; r < N; r += stride) {
         const double v = d[r], ri = static_cast<double>(r);
         if (pair_less(lv, li, v, ri) && pair_less(v, ri, bv, bi))
             bv = v, bi = ri;
@@ -738,7 +754,7 @@ private:
     // pairs above the previous pick, one read of the diagonal each.
     int lowest_diagonal(const double *d_diag, int64_t N, int k, std::vector<int64_t> &order) {
         double2 *picks = nullptr, *partial = nullptr;
-        const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, 2 * csr_->ctx->num_sms)));
+        const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, 8 * csr_->ctx->num_sms)));
         int rc;
         if ((rc = alloc(&picks, k)) || (rc = alloc(&partial, nb)))
             return rc;
