@@ -46,6 +46,9 @@ extern "C" {
 #define PYCI_BUILD_GENCI_EXACT 0x2  /* GenCI: Slater-Condon rules over the true virtuals
                                        instead of the reference's virtual-count quirk       */
 #define PYCI_BUILD_FORCE_HASH 0x4   /* look columns up in the hash table even for full spaces */
+#define PYCI_BUILD_EAGER_CSR 0x8    /* write the CSR entries during the build even when the operator
+                                       has the implicit-column form (by default they are written on
+                                       first use: export, get_element, FP64 products, update) */
 
 /* Solve modes. */
 #define PYCI_SOLVE_FP64 0  /* FP64 CSR values, FP64 vectors, FP64 SpMM                      */
@@ -155,7 +158,10 @@ int pyci_gpu_csr_matvec(const pyci_gpu_csr *csr, const double *x, double *y);
  * or ncol exceeds the maximum.  The first call on a device looks up the
  * arrays' device addresses (once per device); make it before any stream
  * capture.  All calls on a device share the arrays: calls that overlap on the
- * GPU race, so serialise them.  Synchronous, like pyci_gpu_csr_matvec. */
+ * GPU race, so serialise them.  Synchronous, like pyci_gpu_csr_matvec.  An
+ * operator built with its CSR entries deferred (PYCI_STORE_DEFERRED) gets
+ * them on its first FP64 product, so a first call on it allocates them;
+ * build with PYCI_BUILD_EAGER_CSR, or make one allocating call first. */
 int pyci_gpu_csr_matvec_noalloc(const pyci_gpu_csr *csr, const double *x, double *y);
 
 /* Y = H X on device buffers for k vectors stored interleaved ([ncol][k] and
@@ -224,11 +230,13 @@ int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_csr *const *
  * PYCI_STORE_FP64 FP64 CSR values, PYCI_STORE_SPLIT the exact FP32 high/low
  * split in CSR order, PYCI_STORE_SELL the SELL-32 copy of the split,
  * PYCI_STORE_IMPLICIT the implicit-column form of a full FullCI space
- * (columns derived from per-string tables, values only). */
+ * (columns derived from per-string tables, values only), PYCI_STORE_DEFERRED
+ * the CSR entries not written yet (they are written on first use). */
 #define PYCI_STORE_FP64 0x1
 #define PYCI_STORE_SPLIT 0x2
 #define PYCI_STORE_SELL 0x4
 #define PYCI_STORE_IMPLICIT 0x8
+#define PYCI_STORE_DEFERRED 0x10
 int pyci_gpu_csr_storage(const pyci_gpu_csr *csr, int *flags);
 
 /* Kernel form the autotuner chose for the products of `precision` at width k

@@ -16,11 +16,11 @@ LIBRARY = os.path.join(_HERE, "lib", "libpyci_gb300.so")
 
 OK, EINVAL, ETYPE, ENOCONV, ECUDA, ENOMEM, EUNSUPPORTED = 0, -1, -2, -3, -4, -5, -6
 WFN_DOCI, WFN_FULLCI, WFN_GENCI = 0, 1, 2
-BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH = 0x1, 0x2, 0x4
+BUILD_FULL_COLEX, BUILD_GENCI_EXACT, BUILD_FORCE_HASH, BUILD_EAGER_CSR = 0x1, 0x2, 0x4, 0x8
 SOLVE_FP64, SOLVE_MIXED = 0, 1
 GRAM_CUDA_CORES, GRAM_TENSOR_CORES = 0, 1
 PREC_FP64, PREC_FP32, PREC_FP64_SPLIT, PREC_FP64_DF = 0, 1, 2, 3
-STORE_FP64, STORE_SPLIT, STORE_SELL, STORE_IMPLICIT = 0x1, 0x2, 0x4, 0x8
+STORE_FP64, STORE_SPLIT, STORE_SELL, STORE_IMPLICIT, STORE_DEFERRED = 0x1, 0x2, 0x4, 0x8, 0x10
 FORM_UNTUNED, FORM_CSR, FORM_SELL, FORM_IMPLICIT = -1, 0, 1, 2
 
 # Every symbol the header declares.

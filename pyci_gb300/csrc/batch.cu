@@ -1624,6 +1624,12 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
         }
     }
     PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
+    for (auto *c : v) {
+        // The batched kernels read the CSR: write deferred entries first.
+        int rc = csr_materialize(c);
+        if (rc)
+            return rc;
+    }
     const int64_t iters = (maxiter > 0) ? maxiter : 1000;
     const int mmax = 64; // per-problem subspace (restarts keep 16)
     if (mode == PYCI_SOLVE_MIXED) {

@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <climits>
 #include <cstdio>
+#include <mutex>
+#include <new>
 #include <vector>
 
 #include "detops.cuh"
@@ -52,13 +54,6 @@ struct BuildParams {
     int32_t *lower_len;
     double *diag;
     int *error;             // set to a nonzero code on an internal inconsistency
-    // Implicit-column form written by the sorted FullCI fill (fcix.cu
-    // layout); hi null: not written.  grank[a][g]: the rank of alpha group
-    // g among the groups of its type (single or double).
-    float *fx_hi, *fx_lo;
-    const int16_t *fx_grank;
-    int64_t fx_spa, fx_npk;
-    int fx_la, fx_lb, fx_nlsp, fx_na;
 };
 
 // Column limit of a row's own (lower / general) entries: update() keeps the
@@ -1179,30 +1174,20 @@ __global__ void __launch_bounds__(256) fill_fci_tables_kernel(BuildParams p, int
         }
         p.cols[start + t] = static_cast<int32_t>(col);
         p.vals[start + t] = val;
-        if (p.fx_hi) {
-            // The same entry in the implicit-column form: section A, B
-            // (group = rank of the alpha single) or C, then its packet slot.
-            const int gr = __ldg(p.fx_grank + ra * p.fx_na + g);
-            const int pos = tya == 0 ? qpos : (tya == 1 ? p.fx_la + gr * p.fx_nlsp + qpos : p.fx_la + p.fx_lb + gr);
-            const int64_t sl = ra * p.fx_spa + (rb >> 5);
-            const int64_t at = ((sl * p.fx_npk + (pos >> 2)) * 32 + (rb & 31)) * 4 + (pos & 3);
-            float h, l;
-            split_hi_lo(val, h, l);
-            p.fx_hi[at] = h;
-            p.fx_lo[at] = l;
-        }
     }
 }
 
 // Tables of the implicit-column form (fcix.cu) from the string tables: per
 // alpha string a, the targets of its singles and of its doubles in sorted
 // order, the CSR offsets of their groups in the sorted row, and the offset of
-// its own group (one thread per alpha string walks the sorted groups); the
-// beta lists (full: partners of the alpha string itself, sub: of an alpha
-// single) transposed to [position][string].
+// its own group (one thread per alpha string walks the sorted groups), plus
+// adesc[a] = the string-table codes (type << 20 | index) of those singles and
+// doubles in the same order, for the value fill; the beta lists (full:
+// partners of the alpha string itself, sub: of an alpha single) transposed
+// to [position][string].
 __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
                                    int grp1, int ns, int nd, int la, int32_t *atab, int32_t *bfull, int32_t *bsub,
-                                   uint16_t *bq, int16_t *grank) {
+                                   uint16_t *bq, int32_t *adesc) {
     const int64_t n_f = static_cast<int64_t>(nbl) * nbeta, n_s = static_cast<int64_t>(grp1) * nbeta;
     const int64_t n_q = static_cast<int64_t>(la) * nbeta;
     const int64_t total = nalpha + n_f + n_s + n_q;
@@ -1210,24 +1195,24 @@ __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nal
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         if (i < nalpha) {
-            int32_t *row = atab + i * w;
+            int32_t *row = atab + i * w, *code = adesc + i * (ns + nd);
             int is = 0, id = 0;
             for (int g = 0; g < na; ++g) {
-                const int ty = TA.val[i * TA.npad + g] >> 20;
+                const int32_t v = TA.val[i * TA.npad + g];
+                const int ty = v >> 20;
                 const int32_t key = TA.key[i * TA.npad + g], off = TA.off[i * TA.npad + g];
                 if (ty == 1 && is < ns) {
                     row[is] = key;
                     row[ns + nd + is] = off;
-                    grank[i * na + g] = static_cast<int16_t>(is);
+                    code[is] = v;
                     ++is;
                 } else if (ty == 2 && id < nd) {
                     row[ns + id] = key;
                     row[2 * ns + nd + id] = off;
-                    grank[i * na + g] = static_cast<int16_t>(id);
+                    code[ns + id] = v;
                     ++id;
                 } else if (ty == 0) {
                     row[w - 1] = off;
-                    grank[i * na + g] = 0;
                 }
             }
         } else if (i < nalpha + n_f) {
@@ -1243,6 +1228,141 @@ __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nal
                 static_cast<uint16_t>(t < nbl ? TB.key[b * TB.npad + t] : static_cast<int32_t>(b));
         }
     }
+}
+
+// Values of the implicit-column form (fcix.cu layout) of a full FullCI
+// space, written without the CSR.  Block (a, h) serves slices [h spa / parts,
+// (h + 1) spa / parts) of alpha string a, one warp per slice; lane l computes
+// the entries of row (a, b), b = 32 (slice mod spa) + l, in the form's order
+// and the warp stores each 4-entry packet's high and low parts as two
+// coalesced 512-byte writes.  Every value is add_row's
+// (pyci/src/sparseop.cpp:260-427) with the formulas and summation order of
+// fill_fci_tables_kernel, so the form holds the exact split of the CSR
+// values whenever the CSR is written.  Padding entries and the rows past
+// nbeta are written as zeros.  Also writes lower_len.
+struct FxFill {
+    float4 *hi, *lo;
+    const int32_t *atab, *adesc;
+    int64_t spa, npk;
+    int parts, aw, ns, nd, nbl, nls, nlsp, la, lc;
+};
+
+template<int NW>
+__global__ void __launch_bounds__(512) fcix_fill_kernel(BuildParams p, StringTables A, StringTables B, FxFill F) {
+    extern __shared__ double fx_pre[]; // [ns]: one-electron term + alpha sums of a's singles
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int n = p.nbasis;
+    const int nbeta = static_cast<int>(p.nbeta);
+    const double *one = p.one_mo, *two = p.two_mo;
+    const int64_t a = blockIdx.x / F.parts;
+    const int h = static_cast<int>(blockIdx.x - a * F.parts);
+    const int64_t sb = a * F.spa + h * F.spa / F.parts, se = a * F.spa + (h + 1) * F.spa / F.parts;
+    uint64_t wa[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+        wa[w] = __ldg(A.bits + a * NW + w);
+    const int32_t *AD = F.adesc + a * (F.ns + F.nd);
+    // Alpha single g of row (a, b): one[ii][jj] + sum over a's occupied k of
+    // (<ii k|jj k> - <ii k|k jj>), then (per row) + sum over b's occupied k of
+    // <ii k|jj k>: the first part is the same for every b.
+    for (int g = threadIdx.x; g < F.ns; g += blockDim.x) {
+        const int da = __ldg(A.sdesc + a * A.n1 + (__ldg(AD + g) & 0xFFFFF));
+        const int ii = da & 255, jj = (da >> 8) & 255;
+        double v1 = __ldg(&one[ii * n + jj]);
+        for (int k = next_bit<NW>(wa, 0); k >= 0; k = next_bit<NW>(wa, k + 1))
+            v1 += two_mo_at(two, n, ii, k, jj, k) - two_mo_at(two, n, ii, k, k, jj);
+        fx_pre[g] = v1;
+    }
+    __syncthreads();
+    const int64_t s = sb + warp;
+    if (s >= se)
+        return;
+    const int bb = static_cast<int>((s - a * F.spa) * 32) + lane;
+    const bool valid = bb < nbeta;
+    const int b = valid ? bb : nbeta - 1;
+    const int64_t row = a * nbeta + b;
+    uint64_t wb[NW];
+#pragma unroll
+    for (int w = 0; w < NW; ++w)
+        wb[w] = __ldg(B.bits + static_cast<int64_t>(b) * NW + w);
+    float4 *hp = F.hi + s * F.npk * 32 + lane, *lp = F.lo + s * F.npk * 32 + lane;
+    // One packet: 4 consecutive entries (t0 .. t0 + 3) from value(t).
+    auto packet = [&](int t0, auto value) {
+        float h4[4], l4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            h4[u] = l4[u] = 0.0f;
+            const double v = value(t0 + u);
+            if (valid)
+                split_hi_lo(v, h4[u], l4[u]);
+        }
+        hp[32 * static_cast<int64_t>(t0 >> 2)] = make_float4(h4[0], h4[1], h4[2], h4[3]);
+        lp[32 * static_cast<int64_t>(t0 >> 2)] = make_float4(l4[0], l4[1], l4[2], l4[3]);
+    };
+    const bool idx32 = n <= 215; // n^4 < 2^31: 32-bit integral offsets
+    // Section A: the alpha string itself with every beta partner of b.
+    const int32_t *BV = B.val + static_cast<int64_t>(b) * B.npad;
+    const double dval = p.diag[row]; // fci_diag_kernel ran first
+    auto value_a = [&](int t) -> double {
+        if (t >= F.nbl)
+            return 0.0;
+        const int code = __ldg(BV + t);
+        const int ty = code >> 20, ib = code & 0xFFFFF;
+        if (ty == 0)
+            return dval;
+        if (ty != 1)
+            return __ldg(B.dval + static_cast<int64_t>(b) * B.n2 + ib); // beta double
+        // Beta single ii -> jj (0-1 excitation).
+        const int db = __ldg(B.sdesc + static_cast<int64_t>(b) * B.n1 + ib);
+        const int ii = db & 255, jj = (db >> 8) & 255;
+        double v1 = __ldg(&one[ii * n + jj]);
+        for (int k = next_bit<NW>(wa, 0); k >= 0; k = next_bit<NW>(wa, k + 1))
+            v1 += two_mo_at(two, n, ii, k, jj, k);
+        for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
+            v1 += two_mo_at(two, n, ii, k, jj, k) - two_mo_at(two, n, ii, k, k, jj);
+        return apply_phase((db >> 16) & 1 ? -1 : 1, v1);
+    };
+    for (int t = 0; t < F.la; t += 4)
+        packet(t, value_a);
+    // Section B: each alpha single with {b} + the beta singles of b.
+    const int32_t *SV = B.subval + static_cast<int64_t>(b) * B.npad;
+    int tb = F.la;
+    for (int g = 0; g < F.ns; ++g, tb += F.nlsp) {
+        const int da = __ldg(A.sdesc + a * A.n1 + (__ldg(AD + g) & 0xFFFFF));
+        const int ii = da & 255, jj = (da >> 8) & 255;
+        const double pre = fx_pre[g];
+        auto value_b = [&](int t) -> double {
+            const int q = t - tb;
+            if (q >= F.nls)
+                return 0.0;
+            const int code = __ldg(SV + q);
+            if ((code >> 20) == 0) {
+                // Alpha single ii -> jj (1-0 excitation).
+                double v1 = pre;
+                for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
+                    v1 += two_mo_at(two, n, ii, k, jj, k);
+                return apply_phase((da >> 16) & 1 ? -1 : 1, v1);
+            }
+            // Opposite-spin double: alpha ii -> jj, beta kk -> ll.
+            const int db = __ldg(B.sdesc + static_cast<int64_t>(b) * B.n1 + (code & 0xFFFFF));
+            const int kk = db & 255, ll = (db >> 8) & 255;
+            const double g2 = idx32 ? __ldg(p.two_mo + (((ii * n + kk) * n + jj) * n + ll))
+                                    : two_mo_at(p.two_mo, n, ii, kk, jj, ll);
+            return apply_phase(((da ^ db) >> 16) & 1 ? -1 : 1, g2);
+        };
+        for (int t = tb; t < tb + F.nlsp; t += 4)
+            packet(t, value_b);
+    }
+    // Section C: each alpha double with b.
+    const int tc = tb;
+    auto value_c = [&](int t) -> double {
+        const int d = t - tc;
+        return d < F.nd ? __ldg(A.dval + a * A.n2 + (__ldg(AD + F.ns + d) & 0xFFFFF)) : 0.0;
+    };
+    for (int t = tc; t < tc + F.lc; t += 4)
+        packet(t, value_c);
+    if (valid && p.lower_len)
+        p.lower_len[row] = __ldg(F.atab + a * F.aw + F.aw - 1) + __ldg(B.self + b) + 1;
 }
 
 // Insert every determinant index into the table (linear probing).
@@ -1614,13 +1734,13 @@ int pick_nw(int64_t nbasis) {
 // Sets up the implicit-column form of a full FullCI space when its beta
 // string count pads to a multiple of 32 with at most 1/4 extra rows (the
 // padding rows are streamed as zeros, still fewer bytes than int32 columns):
-// the tables, and zeroed value arrays that the sorted fill then writes in
-// the same pass as the CSR (p.fx_*).  grank goes to `scratch`, freed after
-// the fill.
-int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, BuildParams &p, std::vector<void *> &scratch,
-                const StringTables &TA, const StringTables &TB, int64_t nalpha, int64_t nbeta, int na, int nbl,
-                int grp1, int64_t len) {
+// the tables and the value arrays (csr->fx_*), which fcix_fill_kernel then
+// writes.  *adesc: the per-alpha-string codes the fill reads (the caller
+// frees it).  Leaves csr->fx_hi null when the space does not qualify.
+int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, const StringTables &TB, int64_t nalpha,
+                int64_t nbeta, int na, int nbl, int grp1, int64_t len, int32_t **adesc) {
     cudaStream_t st = ctx->stream;
+    *adesc = nullptr;
     const int64_t nbp = (nbeta + 31) / 32 * 32;
     const int ns = TA.n1, nd = TA.n2;
     if (nbeta < 32 || nbeta >= 65536 || 4 * (nbp - nbeta) > nbeta || len <= 0 || len > (1 << 20) ||
@@ -1636,9 +1756,8 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, BuildParams &p, std::vecto
                  ss = sizeof(int32_t) * grp1 * nbeta;
     const int64_t npk = (la + lb + lc) / 4;
     const size_t nval = static_cast<size_t>(nalpha) * (nbp / 32) * npk * 128;
-    int32_t *atab = nullptr, *bfull = nullptr, *bsub = nullptr;
+    int32_t *atab = nullptr, *bfull = nullptr, *bsub = nullptr, *codes = nullptr;
     uint16_t *bq = nullptr;
-    int16_t *grank = nullptr;
     float *hi = nullptr, *lo = nullptr;
     cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&atab), sa, st);
     if (e == cudaSuccess)
@@ -1648,28 +1767,22 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, BuildParams &p, std::vecto
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&bq), sizeof(uint16_t) * la * nbeta, st);
     if (e == cudaSuccess)
-        e = cudaMallocAsync(reinterpret_cast<void **>(&grank), sizeof(int16_t) * nalpha * na, st);
+        e = cudaMallocAsync(reinterpret_cast<void **>(&codes), sizeof(int32_t) * nalpha * std::max(ns + nd, 1), st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&hi), sizeof(float) * nval, st);
     if (e == cudaSuccess)
         e = cudaMallocAsync(reinterpret_cast<void **>(&lo), sizeof(float) * nval, st);
-    // Padding entries and padding rows stay zero; the fill writes the rest.
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(hi, 0, sizeof(float) * nval, st);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(lo, 0, sizeof(float) * nval, st);
     if (e != cudaSuccess) {
         for (void *q : {static_cast<void *>(atab), static_cast<void *>(bfull), static_cast<void *>(bsub),
-                        static_cast<void *>(bq), static_cast<void *>(grank), static_cast<void *>(hi),
+                        static_cast<void *>(bq), static_cast<void *>(codes), static_cast<void *>(hi),
                         static_cast<void *>(lo)})
             if (q)
                 cudaFreeAsync(q, st);
         return cuda_status(e, "cudaMallocAsync (implicit-column form)");
     }
-    scratch.push_back(grank);
     const int64_t total = nalpha + (static_cast<int64_t>(nbl) + grp1 + la) * nbeta;
     fcix_tables_kernel<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(
-        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, la, atab, bfull, bsub, bq, grank);
+        TA, TB, nalpha, nbeta, na, nbl, grp1, ns, nd, la, atab, bfull, bsub, bq, codes);
     ::pyci_gpu::note_launch();
     csr->fx_nalpha = nalpha;
     csr->fx_nbeta = nbeta;
@@ -1688,17 +1801,188 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, BuildParams &p, std::vecto
     csr->fx_bq = bq;
     csr->fx_hi = hi;
     csr->fx_lo = lo;
-    p.fx_hi = hi;
-    p.fx_lo = lo;
-    p.fx_grank = grank;
-    p.fx_spa = nbp / 32;
-    p.fx_npk = npk;
-    p.fx_la = la;
-    p.fx_lb = lb;
-    p.fx_nlsp = static_cast<int>(up4(grp1));
-    p.fx_na = na;
+    *adesc = codes;
     return PYCI_GPU_OK;
 }
+
+// Launch fcix_fill_kernel over every slice of the implicit-column form.
+template<int NW>
+int fcix_fill(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const BuildParams &p, const StringTables &TA,
+              const StringTables &TB, const int32_t *adesc) {
+    FxFill F{};
+    F.hi = reinterpret_cast<float4 *>(csr->fx_hi);
+    F.lo = reinterpret_cast<float4 *>(csr->fx_lo);
+    F.atab = csr->fx_atab;
+    F.adesc = adesc;
+    F.spa = csr->fx_nbp / 32;
+    F.npk = csr->fx_npk;
+    F.parts = static_cast<int>((F.spa + 15) / 16);
+    F.aw = fx_atab_width(csr);
+    F.ns = csr->fx_ns;
+    F.nd = csr->fx_nd;
+    F.nbl = csr->fx_nlb;
+    F.nls = csr->fx_nls;
+    F.nlsp = (csr->fx_nls + 3) / 4 * 4;
+    F.la = csr->fx_la;
+    F.lc = csr->fx_lc;
+    const int warps = static_cast<int>((F.spa + F.parts - 1) / F.parts);
+    const size_t smem = sizeof(double) * std::max(F.ns, 1);
+    if (smem > 48 * 1024) {
+        set_error("implicit-column fill: %d alpha singles per string exceed its shared memory", F.ns);
+        return PYCI_GPU_EUNSUPPORTED;
+    }
+    fcix_fill_kernel<NW><<<static_cast<unsigned>(csr->fx_nalpha * F.parts), 32 * warps, smem, ctx->stream>>>(
+        p, TA, TB, F);
+    ::pyci_gpu::note_launch();
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+// Device arrays of the CSR entries (int32 columns, FP64 values) for
+// csr->nnz entries.
+int csr_alloc_entries(pyci_gpu_csr *csr) {
+    cudaStream_t st = csr->ctx->stream;
+    const int64_t nnz = csr->nnz ? csr->nnz : 1;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->cols), sizeof(int32_t) * nnz, st));
+    const cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&csr->vals), sizeof(double) * nnz, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(csr->cols, st);
+        csr->cols = nullptr;
+        return cuda_status(e, "cudaMallocAsync (CSR entries)");
+    }
+    return PYCI_GPU_OK;
+}
+
+// The sorted FullCI row fill over every row (the diagonal must be in p.diag).
+template<int NW>
+int launch_fci_fill(pyci_gpu_ctx *ctx, const BuildParams &p, const StringTables &TA, const StringTables &TB, int na,
+                    int nsg) {
+    cudaStream_t st = ctx->stream;
+    const size_t per_warp = (sizeof(RowState) + sizeof(double) * nsg + sizeof(int) * na + 15) & ~static_cast<size_t>(15);
+    const size_t dsm = per_warp * kFillRowsPerBlock;
+    if (dsm > 48 * 1024)
+        PYCI_CUDA_TRY(cudaFuncSetAttribute(fill_fci_tables_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           static_cast<int>(dsm)));
+    const int64_t rows_per_launch = (static_cast<int64_t>(1) << 20) * kFillRowsPerBlock;
+    for (int64_t r0 = 0; r0 < p.nrow; r0 += rows_per_launch) {
+        const int64_t nr = (p.nrow - r0 < rows_per_launch) ? p.nrow - r0 : rows_per_launch;
+        const unsigned nb = static_cast<unsigned>((nr + kFillRowsPerBlock - 1) / kFillRowsPerBlock);
+        fill_fci_tables_kernel<NW><<<nb, 32 * kFillRowsPerBlock, dsm, st>>>(p, r0, TA, TB, na, nsg),
+            ::pyci_gpu::note_launch();
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+// What the sorted FullCI fill needs to write the CSR later: the build's
+// parameters, the string tables and device copies of the integrals.
+struct DeferredCsr {
+    BuildParams p{};
+    StringTables TA{}, TB{};
+    int na = 0, nsg = 0, nw = 1;
+    std::vector<void *> mem; // device arrays owned here
+};
+
+// Keeps the string tables (taking the arrays in `mem`) so that
+// csr_materialize can write the CSR; the caller has written the
+// implicit-column form and the diagonal.
+int defer_csr(pyci_gpu_csr *csr, const BuildParams &p, const StringTables &TA, const StringTables &TB, int na,
+              int nsg, int nw, std::vector<void *> &mem) {
+    cudaStream_t st = csr->ctx->stream;
+    DeferredCsr *d = new (std::nothrow) DeferredCsr();
+    if (!d) {
+        set_error("out of host memory");
+        return PYCI_GPU_ENOMEM;
+    }
+    const int64_t n = p.nbasis, n2 = n * n, n4 = n2 * n2;
+    double *one = nullptr, *two = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&one), sizeof(double) * n2, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&two), sizeof(double) * n4, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(one, p.one_mo, sizeof(double) * n2, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(two, p.two_mo, sizeof(double) * n4, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+        if (one)
+            cudaFreeAsync(one, st);
+        if (two)
+            cudaFreeAsync(two, st);
+        delete d;
+        return cuda_status(e, "deferred CSR (integrals)");
+    }
+    d->p = p;
+    d->p.one_mo = one;
+    d->p.two_mo = two;
+    // Only the tables, the integrals and the row arrays serve the sorted fill.
+    d->p.binom = nullptr;
+    d->p.dets = nullptr;
+    d->p.h = d->p.v = d->p.w = nullptr;
+    d->p.counts = nullptr;
+    d->p.error = nullptr;
+    d->p.cols = nullptr;
+    d->p.vals = nullptr;
+    d->p.lower_len = nullptr;
+    d->TA = TA;
+    d->TB = TB;
+    d->na = na;
+    d->nsg = nsg;
+    d->nw = nw;
+    d->mem = mem;
+    d->mem.push_back(one);
+    d->mem.push_back(two);
+    mem.clear();
+    csr->deferred = d;
+    return PYCI_GPU_OK;
+}
+
+} // namespace
+
+void csr_deferred_free(pyci_gpu_csr *csr) {
+    if (!csr || !csr->deferred)
+        return;
+    auto *d = static_cast<DeferredCsr *>(csr->deferred);
+    for (void *m : d->mem)
+        cudaFreeAsync(m, csr->ctx->stream);
+    delete d;
+    csr->deferred = nullptr;
+}
+
+int csr_materialize(const pyci_gpu_csr *ccsr) {
+    pyci_gpu_csr *csr = const_cast<pyci_gpu_csr *>(ccsr);
+    if (!csr || !csr->deferred)
+        return PYCI_GPU_OK;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!csr->deferred)
+        return PYCI_GPU_OK;
+    auto *d = static_cast<DeferredCsr *>(csr->deferred);
+    int rc = csr_alloc_entries(csr);
+    if (rc)
+        return rc;
+    BuildParams p = d->p;
+    p.rowptr = csr->rowptr;
+    p.diag = csr->diag;
+    p.cols = csr->cols;
+    p.vals = csr->vals;
+    p.lower_len = nullptr; // written with the implicit-column form
+    switch (d->nw) {
+    case 1: rc = launch_fci_fill<1>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+    case 2: rc = launch_fci_fill<2>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+    default: rc = launch_fci_fill<4>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+    }
+    if (rc) {
+        cudaFreeAsync(csr->cols, csr->ctx->stream);
+        cudaFreeAsync(csr->vals, csr->ctx->stream);
+        csr->cols = nullptr;
+        csr->vals = nullptr;
+        return rc;
+    }
+    csr_deferred_free(csr);
+    return PYCI_GPU_OK;
+}
+
+namespace {
 
 template<int NW>
 int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int64_t uniform_len,
@@ -1730,14 +2014,17 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
     PYCI_CUDA_TRY(cudaMemcpyAsync(&nnz, csr->rowptr + p.nrow, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     PYCI_CUDA_TRY(cudaStreamSynchronize(st));
     csr->nnz = nnz;
-    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->cols), sizeof(int32_t) * (nnz ? nnz : 1), st));
-    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->vals), sizeof(double) * (nnz ? nnz : 1), st));
     PYCI_CUDA_TRY(cudaMemsetAsync(csr->diag, 0, sizeof(double) * (p.nrow ? p.nrow : 1), st));
     p.rowptr = csr->rowptr;
-    p.cols = csr->cols;
-    p.vals = csr->vals;
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
+    if (!sorted_fci) {
+        int rc = csr_alloc_entries(csr);
+        if (rc)
+            return rc;
+        p.cols = csr->cols;
+        p.vals = csr->vals;
+    }
     if (warp_doci) {
         // Full DOCI space: thread-per-row diagonal, then one warp per row.
         doci_diag_kernel<NW><<<static_cast<unsigned>((p.nrow + 255) / 256), 256, 0, st>>>(p), ::pyci_gpu::note_launch();
@@ -1816,27 +2103,33 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
                 ::pyci_gpu::note_launch();
             TB = TA;
         }
+        int32_t *adesc = nullptr;
         if (!rc)
-            rc = fcix_tables(ctx, csr, p, mem, TA, TB, nstr_a, nstr_b, na, nbl, grp1, uniform_len);
+            rc = fcix_tables(ctx, csr, TA, TB, nstr_a, nstr_b, na, nbl, grp1, uniform_len, &adesc);
         if (!rc) {
-            const int nsg = no_a * nv_a + no_b * nv_b;
-            const size_t per_warp = (sizeof(RowState) + sizeof(double) * nsg + sizeof(int) * na + 15) & ~static_cast<size_t>(15);
-            const size_t dsm = per_warp * kFillRowsPerBlock;
-            if (dsm > 48 * 1024) {
-                const cudaError_t e = cudaFuncSetAttribute(fill_fci_tables_kernel<NW>,
-                                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(dsm));
-                if (e != cudaSuccess)
-                    rc = cuda_status(e, "fill shared memory");
-            }
             fci_diag_kernel<NW><<<static_cast<unsigned>((p.nrow + 255) / 256), 256, 0, st>>>(p, TA, TB),
                 ::pyci_gpu::note_launch();
-            const int64_t rows_per_launch = chunk * kFillRowsPerBlock;
-            for (int64_t r0 = 0; !rc && r0 < p.nrow; r0 += rows_per_launch) {
-                const int64_t nr = (p.nrow - r0 < rows_per_launch) ? p.nrow - r0 : rows_per_launch;
-                const unsigned nb = static_cast<unsigned>((nr + kFillRowsPerBlock - 1) / kFillRowsPerBlock);
-                fill_fci_tables_kernel<NW><<<nb, 32 * kFillRowsPerBlock, dsm, st>>>(p, r0, TA, TB, na, nsg),
-                    ::pyci_gpu::note_launch();
-            }
+            if (csr->fx_hi)
+                rc = fcix_fill<NW>(ctx, csr, p, TA, TB, adesc);
+        }
+        if (adesc)
+            cudaFreeAsync(adesc, st);
+        const int nsg = no_a * nv_a + no_b * nv_b;
+        if (!rc && csr->fx_hi && !(csr->flags & PYCI_BUILD_EAGER_CSR)) {
+            // The implicit-column form serves the products: the CSR is written
+            // on first use (csr_materialize), from these tables.
+            rc = defer_csr(csr, p, TA, TB, na, nsg, NW, mem);
+            if (!rc)
+                return PYCI_GPU_OK;
+        }
+        if (!rc) {
+            rc = csr_alloc_entries(csr);
+            p.cols = csr->cols;
+            p.vals = csr->vals;
+        }
+        if (!rc) {
+            p.lower_len = csr->fx_hi ? nullptr : csr->lower_len; // written by the implicit-column fill
+            rc = launch_fci_fill<NW>(ctx, p, TA, TB, na, nsg);
         }
         for (void *m : mem)
             cudaFreeAsync(m, st);

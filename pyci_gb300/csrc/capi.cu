@@ -52,6 +52,7 @@ void csr_release(pyci_gpu_csr *csr) {
     if (!csr || !csr->ctx)
         return;
     cudaStream_t st = csr->ctx->stream;
+    csr_deferred_free(csr);
     void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
                     csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals,
                     csr->sell_lo,    csr->fx_atab,  csr->fx_bfull, csr->fx_bsub,   csr->fx_hi,
@@ -257,6 +258,7 @@ int pyci_gpu_csr_update(pyci_gpu_csr *csr, int64_t ndet, const uint64_t *dets,
     next.sell_lo = nullptr;
     next.nslice = next.sell_nnz = 0;
     fx_forget(&next);
+    next.deferred = nullptr; // the old handle's, freed with it
     next.flags = flags;
     next.ndet = ndet;
     next.nrow = ndet;
@@ -293,11 +295,16 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     }
     PYCI_CUDA_TRY(cudaSetDevice(csr->ctx->device));
     cudaStream_t st = csr->ctx->stream;
+    // The copy gets the CSR entries: write a deferred CSR first.
+    int rc0 = csr_materialize(csr);
+    if (rc0)
+        return rc0;
     pyci_gpu_csr *c = new (std::nothrow) pyci_gpu_csr(*csr);
     if (!c) {
         set_error("out of host memory");
         return PYCI_GPU_ENOMEM;
     }
+    c->deferred = nullptr;
     c->rowptr = nullptr;
     c->cols = nullptr;
     c->vals = nullptr;
@@ -365,7 +372,8 @@ int pyci_gpu_csr_storage(const pyci_gpu_csr *csr, int *flags) {
         return PYCI_GPU_EINVAL;
     }
     *flags = (csr->vals ? PYCI_STORE_FP64 : 0) | (csr->hi && csr->lo ? PYCI_STORE_SPLIT : 0) |
-             (csr->sell_cols ? PYCI_STORE_SELL : 0) | (csr->fx_hi ? PYCI_STORE_IMPLICIT : 0);
+             (csr->sell_cols ? PYCI_STORE_SELL : 0) | (csr->fx_hi ? PYCI_STORE_IMPLICIT : 0) |
+             (csr->deferred ? PYCI_STORE_DEFERRED : 0);
     return PYCI_GPU_OK;
 }
 
@@ -406,6 +414,9 @@ int pyci_gpu_csr_get_element(const pyci_gpu_csr *csr, int64_t i, int64_t j, doub
     }
     PYCI_CUDA_TRY(cudaSetDevice(csr->ctx->device));
     cudaStream_t st = csr->ctx->stream;
+    int rc0 = csr_materialize(csr);
+    if (rc0)
+        return rc0;
     int64_t ptr[2];
     int32_t len = 0;
     PYCI_CUDA_TRY(cudaMemcpyAsync(ptr, csr->rowptr + i, sizeof(int64_t) * 2, cudaMemcpyDeviceToHost, st));

@@ -1487,12 +1487,13 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
         Davidson<float> d(csr, blk, n, mmax, true);
         return d.run(c0, iters, tol, ecore, evals, evecs, stats);
     }
-    if (!csr->vals && !(csr->hi && csr->lo)) {
+    if (!csr->vals && !(csr->hi && csr->lo) && !csr->fx_hi && !csr->deferred) {
         set_error("operator has no values");
         return PYCI_GPU_EINVAL;
     }
-    // Without FP64 values (dropped after the split), the FP64 products use
-    // high + low, equal to the FP64 values within 2^-48 relative.
+    // Without FP64 values (dropped after the split, or a deferred CSR), the
+    // FP64 products use high + low, equal to the FP64 values within 2^-48
+    // relative (in double-float arithmetic on the implicit-column form).
     Davidson<double> d(csr, blk, n, mmax, false);
     return d.run(c0, iters, tol, ecore, evals, evecs, stats);
 }

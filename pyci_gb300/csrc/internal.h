@@ -93,6 +93,11 @@ struct pyci_gpu_csr {
     uint16_t *fx_bq = nullptr;    // [la / 4][nbeta][4]: section A's partners by packet (padding: b)
     float *fx_hi = nullptr;       // [nslice][npk][32][4] high parts
     float *fx_lo = nullptr;       // [nslice][npk][32][4] low parts
+    // Deferred CSR: an operator with the implicit-column form is built
+    // without its CSR entries (cols, vals null) unless PYCI_BUILD_EAGER_CSR
+    // asks for them; this holds what the CSR fill needs (build.cu), and
+    // csr_materialize() writes the entries on first use.  Null otherwise.
+    void *deferred = nullptr;
 };
 
 // Width of one alpha string's row of pyci_gpu_csr::fx_atab.
@@ -135,6 +140,11 @@ void csr_release(pyci_gpu_csr *csr);
 // caller then uses another kernel).
 bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
                  cudaStream_t st);
+// Writes a deferred CSR's entries (no-op when there is nothing deferred);
+// every path that reads cols or vals calls it first.  Logically const: the
+// operator's contents do not change.
+int csr_materialize(const pyci_gpu_csr *csr);
+void csr_deferred_free(pyci_gpu_csr *csr);
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr);
 int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,
                       double *vabs, double *vwsum);

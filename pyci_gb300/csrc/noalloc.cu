@@ -21,7 +21,10 @@
 //     other's results; serialise them;
 //   * the first call on a device looks the arrays' device addresses up
 //     (cudaGetSymbolAddress, once per device, with that device current); make
-//     that first call before any stream capture begins.
+//     that first call before any stream capture begins;
+//   * an operator whose CSR entries are deferred (built with the
+//     implicit-column form and without PYCI_BUILD_EAGER_CSR) gets them on
+//     its first FP64 product, so a first call on it allocates them.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -232,6 +232,11 @@ static unsigned grid_for(const pyci_gpu_ctx *ctx, int64_t n, int threads) {
 
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr) {
     cudaStream_t st = csr->ctx->stream;
+    if (data || indices) {
+        int rc = csr_materialize(csr);
+        if (rc)
+            return rc;
+    }
     const int64_t nrow = csr->nrow;
     const int64_t *d_refptr = csr->symmetric ? csr->ref_rowptr : csr->rowptr;
     std::vector<int64_t> ptr(nrow + 1);
@@ -288,6 +293,9 @@ int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, i
 int csr_digest_device(const pyci_gpu_csr *csr, uint64_t *psum, uint64_t *pxor, double *vsum,
                       double *vabs, double *vwsum) {
     cudaStream_t st = csr->ctx->stream;
+    int rc0 = csr_materialize(csr);
+    if (rc0)
+        return rc0;
     struct Acc {
         unsigned long long s, x;
         double a, b, c;
@@ -378,6 +386,9 @@ int csr_ensure_split(pyci_gpu_csr *csr) {
     if (csr->hi && csr->lo)
         return PYCI_GPU_OK;
     cudaStream_t st = csr->ctx->stream;
+    int rc = csr_materialize(csr);
+    if (rc)
+        return rc;
     if (!csr->vals) {
         set_error("operator has no FP64 values to split");
         return PYCI_GPU_EINVAL;

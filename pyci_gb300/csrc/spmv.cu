@@ -1082,6 +1082,11 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
     }
     switch (precision) {
     case PYCI_PREC_FP64:
+        if (!csr->vals && csr->deferred) {
+            int rc = csr_materialize(csr);
+            if (rc)
+                return rc;
+        }
         if (csr->vals) {
             launch_vk<kF64>(csr, Values<kF64>{csr->vals}, k, x, y, stream);
         } else if (csr->hi && csr->lo) {

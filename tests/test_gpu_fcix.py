@@ -127,3 +127,58 @@ def test_fcix_clone(ctx, monkeypatch):
     Y_ref = np.stack([O.spmv(*ref, X[:, j]) for j in range(4)], axis=1)
     np.testing.assert_allclose(res[1][1], Y_ref, rtol=1e-11, atol=1e-11 * np.abs(Y_ref).max())
     b.free()
+
+
+def test_deferred_csr_written_on_first_use(ctx, monkeypatch):
+    r"""An operator with the implicit-column form is built without its CSR
+    entries: shape and size are known, solves run on the form and leave them
+    unwritten, and the first export writes them, equal to the oracle's CSR
+    and to an eagerly built operator's.  Both operators' implicit-column
+    values are the exact split of the CSR values: products with unit vectors
+    (one term per row) return the same columns from the form and from the
+    CSR, in FP32 and in double-float arithmetic."""
+    import torch
+    n, na, nb = 9, 4, 3
+    csr, ref, dets, ecore = build(ctx, n, na, nb, seed=1011)
+    st = csr.storage()
+    assert st & capi.STORE_IMPLICIT and st & capi.STORE_DEFERRED and not st & capi.STORE_FP64
+    nrow, ncol, size, _ = csr.shape()
+    assert (nrow, ncol, size) == (dets.shape[0], dets.shape[0], ref[0].size)
+    e_ref = O.lowest_eigenvalues(*ref, nroot=2)
+    monkeypatch.setenv("PYCI_GPU_SPMM", "fcix")
+    for mode, tol, atol in ((capi.SOLVE_MIXED, 1e-8, 1e-6), (capi.SOLVE_FP64, 1e-10, 1e-9)):
+        evals, _, _ = csr.solve(n=2, tol=tol, mode=mode)
+        np.testing.assert_allclose(np.sort(evals), e_ref, atol=atol)
+    assert csr.storage() & capi.STORE_DEFERRED, "a solve on the implicit-column form wrote the CSR"
+    data, indices, indptr = csr.export()
+    st = csr.storage()
+    assert st & capi.STORE_FP64 and not st & capi.STORE_DEFERRED
+    assert np.array_equal(data, ref[0]) and np.array_equal(indices, ref[1]) and np.array_equal(indptr, ref[2])
+    eager = capi.Csr(ctx, capi.WFN_FULLCI, n, na, nb, dets, *synthetic_integrals(n, 1011)[1:],
+                     flags=capi.BUILD_FULL_COLEX | capi.BUILD_EAGER_CSR)
+    st = eager.storage()
+    assert st & capi.STORE_FP64 and st & capi.STORE_IMPLICIT and not st & capi.STORE_DEFERRED
+    d2, i2, p2 = eager.export()
+    assert np.array_equal(d2, ref[0]) and np.array_equal(i2, ref[1]) and np.array_equal(p2, ref[2])
+    N = dets.shape[0]
+    cols = [0, 1, N // 3, N // 2 + 7]
+    X = np.zeros((N, 4))
+    X[cols, np.arange(4)] = 1.0
+    xf = torch.tensor(X, dtype=torch.float32, device="cuda")
+    xs = torch.tensor(split_rows(X), device="cuda")
+    out = []
+    for op, pin in ((csr, "fcix"), (eager, "csr")):
+        monkeypatch.setenv("PYCI_GPU_SPMM", pin)
+        yf = torch.empty((N, 4), dtype=torch.float32, device="cuda")
+        yd = torch.empty((N, 4), dtype=torch.float64, device="cuda")
+        op.spmm_device(capi.PREC_FP32, 4, xf.data_ptr(), yf.data_ptr(), None)
+        op.spmm_device(capi.PREC_FP64_DF, 4, xs.data_ptr(), yd.data_ptr(), None)
+        torch.cuda.synchronize()
+        out.append((yf.cpu().numpy(), yd.cpu().numpy()))
+    assert csr.product_form(capi.PREC_FP32, 4) == capi.FORM_IMPLICIT
+    assert eager.product_form(capi.PREC_FP32, 4) != capi.FORM_IMPLICIT
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    full = O.full_matrix(*ref).toarray()
+    np.testing.assert_allclose(out[0][1], full[:, cols], rtol=2e-14, atol=0)
+    csr.free()
+    eager.free()
