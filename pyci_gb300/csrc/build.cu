@@ -1240,18 +1240,81 @@ __global__ void fcix_tables_kernel(StringTables TA, StringTables TB, int64_t nal
 // fill_fci_tables_kernel, so the form holds the exact split of the CSR
 // values whenever the CSR is written.  Padding entries and the rows past
 // nbeta are written as zeros.  Also writes lower_len.
+//
+// What depends on one string only comes from tables that
+// fcix_fill_prep_kernel lays out with the beta string fastest, so the 32
+// lanes of a slice read consecutive words: section A's codes and the split
+// values of its beta doubles, section B's beta partner descriptors, and the
+// split values of section C's alpha doubles (one per alpha string and
+// double, read by the whole warp).  Section B's opposite-spin doubles
+// <ii kk|jj ll> (ii -> jj the group's alpha single) come from a table of
+// all (kk, ll) for the group's (ii, jj) that the block stages in shared
+// memory, FP64 and split, double-buffered with one barrier per group.
 struct FxFill {
     float4 *hi, *lo;
     const int32_t *atab, *adesc;
+    const int32_t *acode; // [nbl][nbeta]: section A's string-table codes
+    const float *ahi, *alo; // [nbl][nbeta]: split values of section A's beta doubles (0 elsewhere)
+    const int32_t *bdesc; // [nlsp][nbeta]: section B partner q of b: kk n + ll | phase << 20; -1 b itself, -2 padding
+    const float *chi, *clo; // [nalpha][nd]: split values of the alpha doubles in rank order
+    const int32_t *spos, *sdb; // [nsb][nbeta]: section-A position and descriptor of beta single j of b
     int64_t spa, npk;
-    int parts, aw, ns, nd, nbl, nls, nlsp, la, lc;
+    int parts, aw, ns, nd, nbl, nls, nlsp, la, lc, nsb;
 };
+
+__global__ void fcix_fill_prep_kernel(StringTables A, StringTables B, int64_t nalpha, int nbeta, int n, int ns,
+                                      int nd, int nbl, int nls, int nlsp, const int32_t *adesc, int32_t *acode,
+                                      float *ahi, float *alo, int32_t *bdesc, float *chi, float *clo, int32_t *spos,
+                                      int32_t *sdb) {
+    const int64_t na_ = static_cast<int64_t>(nbl) * nbeta, nb_ = static_cast<int64_t>(nlsp) * nbeta;
+    const int64_t total = na_ + nb_ + nalpha * nd;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if (i < na_) {
+            const int t = static_cast<int>(i / nbeta), b = static_cast<int>(i - static_cast<int64_t>(t) * nbeta);
+            const int code = B.val[static_cast<int64_t>(b) * B.npad + t];
+            float h = 0.0f, l = 0.0f;
+            if ((code >> 20) == 2)
+                split_hi_lo(B.dval[static_cast<int64_t>(b) * B.n2 + (code & 0xFFFFF)], h, l);
+            if ((code >> 20) == 1) {
+                const int j = code & 0xFFFFF;
+                spos[static_cast<int64_t>(j) * nbeta + b] = t;
+                sdb[static_cast<int64_t>(j) * nbeta + b] = B.sdesc[static_cast<int64_t>(b) * B.n1 + j];
+            }
+            acode[i] = code;
+            ahi[i] = h;
+            alo[i] = l;
+        } else if (i < na_ + nb_) {
+            const int64_t j = i - na_;
+            const int q = static_cast<int>(j / nbeta), b = static_cast<int>(j - static_cast<int64_t>(q) * nbeta);
+            int d = -2;
+            if (q < nls) {
+                const int code = B.subval[static_cast<int64_t>(b) * B.npad + q];
+                if ((code >> 20) == 0) {
+                    d = -1;
+                } else {
+                    const int db = B.sdesc[static_cast<int64_t>(b) * B.n1 + (code & 0xFFFFF)];
+                    d = ((db & 255) * n + ((db >> 8) & 255)) | (((db >> 16) & 1) << 20);
+                }
+            }
+            bdesc[j] = d;
+        } else {
+            const int64_t j = i - na_ - nb_, a = j / nd;
+            const int dd = static_cast<int>(j - a * nd);
+            const int ia = adesc[a * (ns + nd) + ns + dd] & 0xFFFFF;
+            split_hi_lo(A.dval[a * A.n2 + ia], chi[j], clo[j]);
+        }
+    }
+}
 
 template<int NW>
 __global__ void __launch_bounds__(512) fcix_fill_kernel(BuildParams p, StringTables A, StringTables B, FxFill F) {
-    extern __shared__ double fx_pre[]; // [ns]: one-electron term + alpha sums of a's singles
+    extern __shared__ __align__(16) unsigned char fx_smem[];
+    const int n = p.nbasis, nn = n * n;
+    double *pre = reinterpret_cast<double *>(fx_smem); // [ns]: one-electron term + alpha sums of a's singles
+    double *t64 = pre + F.ns;                          // [2][nn]: <ii kk|jj ll> of the group's (ii, jj)
+    float *thi = reinterpret_cast<float *>(t64 + 2 * nn), *tlo = thi + 2 * nn; // [2][nn]: its split
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n = p.nbasis;
     const int nbeta = static_cast<int>(p.nbeta);
     const double *one = p.one_mo, *two = p.two_mo;
     const int64_t a = blockIdx.x / F.parts;
@@ -1271,93 +1334,125 @@ __global__ void __launch_bounds__(512) fcix_fill_kernel(BuildParams p, StringTab
         double v1 = __ldg(&one[ii * n + jj]);
         for (int k = next_bit<NW>(wa, 0); k >= 0; k = next_bit<NW>(wa, k + 1))
             v1 += two_mo_at(two, n, ii, k, jj, k) - two_mo_at(two, n, ii, k, k, jj);
-        fx_pre[g] = v1;
+        pre[g] = v1;
     }
+    // Group g's integrals <ii kk|jj ll> for every (kk, ll) into buffer buf.
+    auto stage = [&](int g, int buf) {
+        const int da = __ldg(A.sdesc + a * A.n1 + (__ldg(AD + g) & 0xFFFFF));
+        const int ii = da & 255, jj = (da >> 8) & 255;
+        for (int idx = threadIdx.x; idx < nn; idx += blockDim.x) {
+            const int kk = idx / n, ll = idx - kk * n;
+            const double v = two_mo_at(two, n, ii, kk, jj, ll);
+            t64[buf * nn + idx] = v;
+            split_hi_lo(v, thi[buf * nn + idx], tlo[buf * nn + idx]);
+        }
+    };
+    if (F.ns > 0)
+        stage(0, 0);
     __syncthreads();
     const int64_t s = sb + warp;
-    if (s >= se)
-        return;
-    const int bb = static_cast<int>((s - a * F.spa) * 32) + lane;
-    const bool valid = bb < nbeta;
+    const bool active = s < se; // every warp takes part in the barriers below
+    const int bb = active ? static_cast<int>((s - a * F.spa) * 32) + lane : 0;
+    const bool valid = active && bb < nbeta;
     const int b = valid ? bb : nbeta - 1;
     const int64_t row = a * nbeta + b;
     uint64_t wb[NW];
 #pragma unroll
     for (int w = 0; w < NW; ++w)
         wb[w] = __ldg(B.bits + static_cast<int64_t>(b) * NW + w);
-    float4 *hp = F.hi + s * F.npk * 32 + lane, *lp = F.lo + s * F.npk * 32 + lane;
-    // One packet: 4 consecutive entries (t0 .. t0 + 3) from value(t).
+    float4 *hp = F.hi + (active ? s : 0) * F.npk * 32 + lane, *lp = F.lo + (active ? s : 0) * F.npk * 32 + lane;
+    // One packet: entries t0 .. t0 + 3, value(t) returning (high, low).
     auto packet = [&](int t0, auto value) {
         float h4[4], l4[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            h4[u] = l4[u] = 0.0f;
-            const double v = value(t0 + u);
-            if (valid)
-                split_hi_lo(v, h4[u], l4[u]);
+            const float2 v = value(t0 + u);
+            h4[u] = valid ? v.x : 0.0f;
+            l4[u] = valid ? v.y : 0.0f;
         }
         hp[32 * static_cast<int64_t>(t0 >> 2)] = make_float4(h4[0], h4[1], h4[2], h4[3]);
         lp[32 * static_cast<int64_t>(t0 >> 2)] = make_float4(l4[0], l4[1], l4[2], l4[3]);
     };
-    const bool idx32 = n <= 215; // n^4 < 2^31: 32-bit integral offsets
-    // Section A: the alpha string itself with every beta partner of b.
-    const int32_t *BV = B.val + static_cast<int64_t>(b) * B.npad;
-    const double dval = p.diag[row]; // fci_diag_kernel ran first
-    auto value_a = [&](int t) -> double {
-        if (t >= F.nbl)
-            return 0.0;
-        const int code = __ldg(BV + t);
-        const int ty = code >> 20, ib = code & 0xFFFFF;
-        if (ty == 0)
-            return dval;
-        if (ty != 1)
-            return __ldg(B.dval + static_cast<int64_t>(b) * B.n2 + ib); // beta double
-        // Beta single ii -> jj (0-1 excitation).
-        const int db = __ldg(B.sdesc + static_cast<int64_t>(b) * B.n1 + ib);
-        const int ii = db & 255, jj = (db >> 8) & 255;
-        double v1 = __ldg(&one[ii * n + jj]);
-        for (int k = next_bit<NW>(wa, 0); k >= 0; k = next_bit<NW>(wa, k + 1))
-            v1 += two_mo_at(two, n, ii, k, jj, k);
-        for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
-            v1 += two_mo_at(two, n, ii, k, jj, k) - two_mo_at(two, n, ii, k, k, jj);
-        return apply_phase((db >> 16) & 1 ? -1 : 1, v1);
+    auto split2 = [](double v) {
+        float hv, lv;
+        split_hi_lo(v, hv, lv);
+        return make_float2(hv, lv);
     };
-    for (int t = 0; t < F.la; t += 4)
-        packet(t, value_a);
+    if (active) {
+        // Section A: the alpha string itself with every beta partner of b.
+        // The beta singles sit at different positions in different lanes'
+        // rows: they are written as zeros here and then one single at a time
+        // in every lane (no lane waits on another lane's FP64 sums).
+        const float2 dsp = split2(p.diag[row]); // fci_diag_kernel ran first
+        auto value_a = [&](int t) -> float2 {
+            if (t >= F.nbl)
+                return make_float2(0.0f, 0.0f);
+            const int64_t at = static_cast<int64_t>(t) * nbeta + b;
+            const int ty = __ldg(F.acode + at) >> 20;
+            if (ty == 0)
+                return dsp;
+            return ty == 2 ? make_float2(__ldg(F.ahi + at), __ldg(F.alo + at)) : make_float2(0.0f, 0.0f);
+        };
+        for (int t = 0; t < F.la; t += 4)
+            packet(t, value_a);
+        float *hf = reinterpret_cast<float *>(F.hi), *lf = reinterpret_cast<float *>(F.lo);
+        for (int j = 0; j < F.nsb; ++j) {
+            // Beta single j, ii -> jj (0-1 excitation).
+            const int t = __ldg(F.spos + static_cast<int64_t>(j) * nbeta + b);
+            const int db = __ldg(F.sdb + static_cast<int64_t>(j) * nbeta + b);
+            const int ii = db & 255, jj = (db >> 8) & 255;
+            double v1 = __ldg(&one[ii * n + jj]);
+            for (int k = next_bit<NW>(wa, 0); k >= 0; k = next_bit<NW>(wa, k + 1))
+                v1 += two_mo_at(two, n, ii, k, jj, k);
+            for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
+                v1 += two_mo_at(two, n, ii, k, jj, k) - two_mo_at(two, n, ii, k, k, jj);
+            if (valid) {
+                const int64_t at = ((s * F.npk + (t >> 2)) * 32 + lane) * 4 + (t & 3);
+                split_hi_lo(apply_phase((db >> 16) & 1 ? -1 : 1, v1), hf[at], lf[at]);
+            }
+        }
+    }
     // Section B: each alpha single with {b} + the beta singles of b.
-    const int32_t *SV = B.subval + static_cast<int64_t>(b) * B.npad;
     int tb = F.la;
     for (int g = 0; g < F.ns; ++g, tb += F.nlsp) {
-        const int da = __ldg(A.sdesc + a * A.n1 + (__ldg(AD + g) & 0xFFFFF));
-        const int ii = da & 255, jj = (da >> 8) & 255;
-        const double pre = fx_pre[g];
-        auto value_b = [&](int t) -> double {
-            const int q = t - tb;
-            if (q >= F.nls)
-                return 0.0;
-            const int code = __ldg(SV + q);
-            if ((code >> 20) == 0) {
-                // Alpha single ii -> jj (1-0 excitation).
-                double v1 = pre;
-                for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
-                    v1 += two_mo_at(two, n, ii, k, jj, k);
-                return apply_phase((da >> 16) & 1 ? -1 : 1, v1);
-            }
-            // Opposite-spin double: alpha ii -> jj, beta kk -> ll.
-            const int db = __ldg(B.sdesc + static_cast<int64_t>(b) * B.n1 + (code & 0xFFFFF));
-            const int kk = db & 255, ll = (db >> 8) & 255;
-            const double g2 = idx32 ? __ldg(p.two_mo + (((ii * n + kk) * n + jj) * n + ll))
-                                    : two_mo_at(p.two_mo, n, ii, kk, jj, ll);
-            return apply_phase(((da ^ db) >> 16) & 1 ? -1 : 1, g2);
-        };
-        for (int t = tb; t < tb + F.nlsp; t += 4)
-            packet(t, value_b);
+        if (g + 1 < F.ns)
+            stage(g + 1, (g + 1) & 1); // last read in group g - 1, before the barrier below
+        if (active) {
+            const int da = __ldg(A.sdesc + a * A.n1 + (__ldg(AD + g) & 0xFFFFF));
+            const int pha = (da >> 16) & 1;
+            const double *T64 = t64 + (g & 1) * nn;
+            const float *Th = thi + (g & 1) * nn, *Tl = tlo + (g & 1) * nn;
+            // Alpha single ii -> jj (1-0 excitation), the group's entry for b
+            // itself: computed in every lane, used where the partner is b.
+            double v1 = pre[g];
+            for (int k = next_bit<NW>(wb, 0); k >= 0; k = next_bit<NW>(wb, k + 1))
+                v1 += T64[k * n + k];
+            const float2 selfv = split2(apply_phase(pha ? -1 : 1, v1));
+            auto value_b = [&](int t) -> float2 {
+                const int d = __ldg(F.bdesc + static_cast<int64_t>(t - tb) * nbeta + b);
+                if (d == -2)
+                    return make_float2(0.0f, 0.0f);
+                if (d == -1)
+                    return selfv;
+                // Opposite-spin double: alpha ii -> jj, beta kk -> ll; the
+                // split of -v is (-high, -low).
+                const int off = d & 0xFFFFF;
+                const float hv = Th[off], lv = Tl[off];
+                return ((d >> 20) ^ pha) ? make_float2(-hv, -lv) : make_float2(hv, lv);
+            };
+            for (int t = tb; t < tb + F.nlsp; t += 4)
+                packet(t, value_b);
+        }
+        __syncthreads();
     }
+    if (!active)
+        return;
     // Section C: each alpha double with b.
     const int tc = tb;
-    auto value_c = [&](int t) -> double {
+    const float *CH = F.chi + a * F.nd, *CL = F.clo + a * F.nd;
+    auto value_c = [&](int t) -> float2 {
         const int d = t - tc;
-        return d < F.nd ? __ldg(A.dval + a * A.n2 + (__ldg(AD + F.ns + d) & 0xFFFFF)) : 0.0;
+        return d < F.nd ? make_float2(__ldg(CH + d), __ldg(CL + d)) : make_float2(0.0f, 0.0f);
     };
     for (int t = tc; t < tc + F.lc; t += 4)
         packet(t, value_c);
@@ -1805,10 +1900,12 @@ int fcix_tables(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const StringTables &TA, co
     return PYCI_GPU_OK;
 }
 
-// Launch fcix_fill_kernel over every slice of the implicit-column form.
+// Lay out fcix_fill_kernel's per-string tables (fcix_fill_prep_kernel), then
+// launch it over every slice of the implicit-column form.
 template<int NW>
 int fcix_fill(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const BuildParams &p, const StringTables &TA,
               const StringTables &TB, const int32_t *adesc) {
+    cudaStream_t st = ctx->stream;
     FxFill F{};
     F.hi = reinterpret_cast<float4 *>(csr->fx_hi);
     F.lo = reinterpret_cast<float4 *>(csr->fx_lo);
@@ -1825,16 +1922,52 @@ int fcix_fill(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const BuildParams &p, const 
     F.nlsp = (csr->fx_nls + 3) / 4 * 4;
     F.la = csr->fx_la;
     F.lc = csr->fx_lc;
+    const int n = p.nbasis, nbeta = static_cast<int>(csr->fx_nbeta);
     const int warps = static_cast<int>((F.spa + F.parts - 1) / F.parts);
-    const size_t smem = sizeof(double) * std::max(F.ns, 1);
+    const size_t smem = sizeof(double) * std::max(F.ns, 1) + static_cast<size_t>(n) * n * 2 * (sizeof(double) + 2 * sizeof(float));
     if (smem > 48 * 1024) {
-        set_error("implicit-column fill: %d alpha singles per string exceed its shared memory", F.ns);
+        set_error("implicit-column fill: %d orbitals and %d alpha singles exceed its shared memory", n, F.ns);
         return PYCI_GPU_EUNSUPPORTED;
     }
-    fcix_fill_kernel<NW><<<static_cast<unsigned>(csr->fx_nalpha * F.parts), 32 * warps, smem, ctx->stream>>>(
-        p, TA, TB, F);
-    ::pyci_gpu::note_launch();
-    PYCI_CUDA_TRY(cudaGetLastError());
+    const int64_t na_ = static_cast<int64_t>(F.nbl) * nbeta, nb_ = static_cast<int64_t>(F.nlsp) * nbeta,
+                  nc_ = csr->fx_nalpha * std::max(F.nd, 1);
+    F.nsb = TB.n1;
+    const int64_t ns_ = static_cast<int64_t>(std::max(F.nsb, 1)) * nbeta;
+    int32_t *acode = nullptr, *bdesc = nullptr, *sps = nullptr;
+    float *ahl = nullptr, *chl = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&acode), sizeof(int32_t) * na_, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&sps), sizeof(int32_t) * 2 * ns_, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&ahl), sizeof(float) * 2 * na_, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&bdesc), sizeof(int32_t) * nb_, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&chl), sizeof(float) * 2 * nc_, st);
+    if (e == cudaSuccess) {
+        const int64_t total = na_ + nb_ + csr->fx_nalpha * F.nd;
+        fcix_fill_prep_kernel<<<static_cast<unsigned>(std::min<int64_t>((total + 255) / 256, 8192)), 256, 0, st>>>(
+            TA, TB, csr->fx_nalpha, nbeta, n, F.ns, F.nd, F.nbl, F.nls, F.nlsp, adesc, acode, ahl, ahl + na_, bdesc,
+            chl, chl + nc_, sps, sps + ns_);
+        ::pyci_gpu::note_launch();
+        F.spos = sps;
+        F.sdb = sps + ns_;
+        F.acode = acode;
+        F.ahi = ahl;
+        F.alo = ahl + na_;
+        F.bdesc = bdesc;
+        F.chi = chl;
+        F.clo = chl + nc_;
+        fcix_fill_kernel<NW><<<static_cast<unsigned>(csr->fx_nalpha * F.parts), 32 * warps, smem, st>>>(p, TA, TB, F);
+        ::pyci_gpu::note_launch();
+        e = cudaGetLastError();
+    }
+    for (void *q : {static_cast<void *>(acode), static_cast<void *>(ahl), static_cast<void *>(bdesc),
+                    static_cast<void *>(chl), static_cast<void *>(sps)})
+        if (q)
+            cudaFreeAsync(q, st);
+    if (e != cudaSuccess)
+        return cuda_status(e, "implicit-column fill");
     return PYCI_GPU_OK;
 }
 
