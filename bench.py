@@ -61,6 +61,7 @@ FORM_NAMES = {-1: "untuned", 0: "csr", 1: "sell32", 2: "implicit"}
 KERNEL_NAMES = {-1: "untuned", 0: "CSR spmm_kernel tile", 1: "spmm_sell_kernel (SELL-32)",
                 2: "fcix_spmm_kernel (implicit columns, values only)"}
 TRAFFIC_PER_ALGORITHMIC_BYTE = {-1: 1.0, 0: 1.024, 1: 1.000, 2: 1.000}
+DOCI_IMPLICIT_KERNEL = "docx_spmm_kernel (columns from each row's occupation, values from the pair integrals)"
 # The implicit-column form streams padded packets (beta strings padded to a
 # multiple of 32 rows per alpha string, row sections to multiples of 4
 # entries); on the 11-orbital 5a5b operator ncu measured 1.001 DRAM bytes per
@@ -444,12 +445,14 @@ def run_ours(args, world, rank, local):
     formdf = csr.product_form(capi.PREC_FP64_DF, 4)
     # Algorithmic bytes of one launch: the stored values (+ int32 columns and
     # row pointers unless the columns are implicit), x read once, y written once.
+    # The implicit DOCI form stores nothing per entry: x, y and the FP64
+    # diagonal are its only HBM traffic.
     if form32 == capi.FORM_IMPLICIT:
-        bytes32 = stored * 4 + 2 * N * nroot * 4
+        bytes32 = (stored * 4 if fci else N * 8) + 2 * N * nroot * 4
     else:
         bytes32 = stored * (4 + 4) + (N + 1) * 8 + 2 * N * nroot * 4
     if formdf == capi.FORM_IMPLICIT:
-        bytesdf = stored * 8 + N * (32 + 32)
+        bytesdf = (stored * 8 if fci else N * 8) + N * (32 + 32)
     else:
         bytesdf = stored * 12 + (N + 1) * 8 + N * (32 + 32)
     bytes64 = stored * (8 + 4) + (N + 1) * 8 + 2 * N * 8
@@ -522,7 +525,9 @@ def run_ours(args, world, rank, local):
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel on "
                                        "FullCI 11o 5a5b, scaled by entries processed" if fci else None,
                      "peak_source": peak_kind, "peak_note": "of measured" if peak_kind == "measured" else "of fallback",
-                     "kernel": "FP32 k=4 SpMM, autotuned: " + KERNEL_NAMES[form32], "algorithmic_bytes": bytes32},
+                     "kernel": "FP32 k=4 SpMM, autotuned: " + (KERNEL_NAMES[form32] if fci or form32 != capi.FORM_IMPLICIT
+                                                                  else DOCI_IMPLICIT_KERNEL),
+                     "algorithmic_bytes": bytes32},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_spr, "unit": "s/root", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),

@@ -28,7 +28,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["build.cu", "spmv.cu", "ops.cu", "davidson.cu", "batch.cu", "capi.cu", "noalloc.cu", "gram_tc.cu", "hci.cu", "rdm.cu", "fcix.cu"]
+CU_SOURCES = ["build.cu", "spmv.cu", "ops.cu", "davidson.cu", "batch.cu", "capi.cu", "noalloc.cu", "gram_tc.cu", "hci.cu", "rdm.cu", "fcix.cu", "docx.cu"]
 CPP_SOURCES = ["dense.cpp"]
 HEADERS = ["internal.h", "detops.cuh", "dense.h", "split_bits.h"]
 

@@ -1986,6 +1986,31 @@ int csr_alloc_entries(pyci_gpu_csr *csr) {
     return PYCI_GPU_OK;
 }
 
+// Reference-layout row pointers of a symmetric operator: the prefix sums of
+// lower_len, and nnz_ref.
+int ref_rowptr_from_lower_len(pyci_gpu_csr *csr) {
+    cudaStream_t st = csr->ctx->stream;
+    int64_t *lens64 = nullptr;
+    PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&lens64), sizeof(int64_t) * std::max<int64_t>(csr->nrow, 1), st));
+    if (csr->nrow > 0)
+        widen_kernel<<<static_cast<unsigned>(std::min<int64_t>((csr->nrow + 255) / 256, 1 << 16)), 256, 0, st>>>(
+            csr->lower_len, lens64, csr->nrow), ::pyci_gpu::note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&csr->ref_rowptr), sizeof(int64_t) * (csr->nrow + 1), st);
+    int rc = e == cudaSuccess ? device_exclusive_scan(lens64, csr->nrow, csr->ref_rowptr, st)
+                              : cuda_status(e, "reference row pointers");
+    if (!rc) {
+        e = cudaMemcpyAsync(&csr->nnz_ref, csr->ref_rowptr + csr->nrow, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess)
+            rc = cuda_status(e, "reference row pointers");
+    }
+    cudaFreeAsync(lens64, st);
+    return rc;
+}
+
 // The sorted FullCI row fill over every row (the diagonal must be in p.diag).
 template<int NW>
 int launch_fci_fill(pyci_gpu_ctx *ctx, const BuildParams &p, const StringTables &TA, const StringTables &TB, int na,
@@ -2007,12 +2032,28 @@ int launch_fci_fill(pyci_gpu_ctx *ctx, const BuildParams &p, const StringTables 
     return PYCI_GPU_OK;
 }
 
-// What the sorted FullCI fill needs to write the CSR later: the build's
-// parameters, the string tables and device copies of the integrals.
+// The full-DOCI row fill over every row (the diagonal must be in p.diag).
+template<int NW>
+int launch_doci_fill(pyci_gpu_ctx *ctx, const BuildParams &p) {
+    const int64_t rows_per_block = 8 * kDociRowsPerWarp;
+    const int64_t rows_per_launch = static_cast<int64_t>(1) << 30;
+    for (int64_t r0 = 0; r0 < p.nrow; r0 += rows_per_launch) {
+        const int64_t nr = std::min<int64_t>(p.nrow - r0, rows_per_launch);
+        fill_doci_warp_kernel<NW><<<static_cast<unsigned>((nr + rows_per_block - 1) / rows_per_block), 256, 0,
+                                    ctx->stream>>>(p, r0),
+            ::pyci_gpu::note_launch();
+    }
+    PYCI_CUDA_TRY(cudaGetLastError());
+    return PYCI_GPU_OK;
+}
+
+// What a row fill needs to write the CSR later: the build's parameters and
+// device copies of what they point to (FullCI: the string tables and the
+// integrals; DOCI: the binomial table, the pair integrals and an error flag).
 struct DeferredCsr {
     BuildParams p{};
     StringTables TA{}, TB{};
-    int na = 0, nsg = 0, nw = 1;
+    int kind = 0, na = 0, nsg = 0, nw = 1;
     std::vector<void *> mem; // device arrays owned here
 };
 
@@ -2058,6 +2099,7 @@ int defer_csr(pyci_gpu_csr *csr, const BuildParams &p, const StringTables &TA, c
     d->p.lower_len = nullptr;
     d->TA = TA;
     d->TB = TB;
+    d->kind = PYCI_WFN_FULLCI;
     d->na = na;
     d->nsg = nsg;
     d->nw = nw;
@@ -2065,6 +2107,54 @@ int defer_csr(pyci_gpu_csr *csr, const BuildParams &p, const StringTables &TA, c
     d->mem.push_back(one);
     d->mem.push_back(two);
     mem.clear();
+    csr->deferred = d;
+    return PYCI_GPU_OK;
+}
+
+// Keeps what fill_doci_warp_kernel reads (the diagonal is written) so that
+// csr_materialize can write the CSR of a full DOCI space.
+int defer_csr_doci(pyci_gpu_csr *csr, const BuildParams &p, int nw) {
+    cudaStream_t st = csr->ctx->stream;
+    DeferredCsr *d = new (std::nothrow) DeferredCsr();
+    if (!d) {
+        set_error("out of host memory");
+        return PYCI_GPU_ENOMEM;
+    }
+    const int64_t n = p.nbasis, nb = (n + 1) * p.ldk;
+    int64_t *binom = nullptr;
+    double *v = nullptr;
+    int *err = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&binom), sizeof(int64_t) * nb, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&v), sizeof(double) * n * n, st);
+    if (e == cudaSuccess)
+        e = cudaMallocAsync(reinterpret_cast<void **>(&err), sizeof(int), st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(binom, p.binom, sizeof(int64_t) * nb, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(v, p.v, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(err, 0, sizeof(int), st);
+    if (e != cudaSuccess) {
+        for (void *q : {static_cast<void *>(binom), static_cast<void *>(v), static_cast<void *>(err)})
+            if (q)
+                cudaFreeAsync(q, st);
+        delete d;
+        return cuda_status(e, "deferred CSR (DOCI tables)");
+    }
+    d->p = p;
+    d->p.binom = binom;
+    d->p.v = v;
+    d->p.error = err;
+    d->p.one_mo = d->p.two_mo = d->p.h = d->p.w = nullptr;
+    d->p.dets = nullptr;
+    d->p.counts = nullptr;
+    d->p.cols = nullptr;
+    d->p.vals = nullptr;
+    d->p.lower_len = nullptr;
+    d->kind = PYCI_WFN_DOCI;
+    d->nw = nw;
+    d->mem = {binom, v, err};
     csr->deferred = d;
     return PYCI_GPU_OK;
 }
@@ -2098,11 +2188,36 @@ int csr_materialize(const pyci_gpu_csr *ccsr) {
     p.diag = csr->diag;
     p.cols = csr->cols;
     p.vals = csr->vals;
-    p.lower_len = nullptr; // written with the implicit-column form
-    switch (d->nw) {
-    case 1: rc = launch_fci_fill<1>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
-    case 2: rc = launch_fci_fill<2>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
-    default: rc = launch_fci_fill<4>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+    if (d->kind == PYCI_WFN_DOCI) {
+        // The DOCI fill also writes lower_len; the reference-layout row
+        // pointers follow from it.
+        p.lower_len = csr->lower_len;
+        switch (d->nw) {
+        case 1: rc = launch_doci_fill<1>(csr->ctx, p); break;
+        case 2: rc = launch_doci_fill<2>(csr->ctx, p); break;
+        default: rc = launch_doci_fill<4>(csr->ctx, p); break;
+        }
+        if (!rc && csr->symmetric && !csr->ref_rowptr)
+            rc = ref_rowptr_from_lower_len(csr);
+        int herr = 0;
+        if (!rc) {
+            cudaError_t e = cudaMemcpyAsync(&herr, p.error, sizeof(int), cudaMemcpyDeviceToHost, csr->ctx->stream);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(csr->ctx->stream);
+            if (e != cudaSuccess)
+                rc = cuda_status(e, "deferred CSR");
+            else if (herr) {
+                set_error("internal inconsistency in the CSR build (code %d)", herr);
+                rc = PYCI_GPU_ECUDA;
+            }
+        }
+    } else {
+        p.lower_len = nullptr; // written with the implicit-column form
+        switch (d->nw) {
+        case 1: rc = launch_fci_fill<1>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+        case 2: rc = launch_fci_fill<2>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+        default: rc = launch_fci_fill<4>(csr->ctx, p, d->TA, d->TB, d->na, d->nsg); break;
+        }
     }
     if (rc) {
         cudaFreeAsync(csr->cols, csr->ctx->stream);
@@ -2151,7 +2266,7 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
     p.rowptr = csr->rowptr;
     p.diag = csr->diag;
     p.lower_len = csr->lower_len;
-    if (!sorted_fci) {
+    if (!sorted_fci && !warp_doci) {
         int rc = csr_alloc_entries(csr);
         if (rc)
             return rc;
@@ -2159,17 +2274,17 @@ int run_build(pyci_gpu_ctx *ctx, BuildParams &p, pyci_gpu_csr *csr, int cap, int
         p.vals = csr->vals;
     }
     if (warp_doci) {
-        // Full DOCI space: thread-per-row diagonal, then one warp per row.
+        // Full DOCI space: thread-per-row diagonal, then one warp per row
+        // (on first use when the implicit DOCI form serves the products).
         doci_diag_kernel<NW><<<static_cast<unsigned>((p.nrow + 255) / 256), 256, 0, st>>>(p), ::pyci_gpu::note_launch();
-        const int64_t rows_per_block = 8 * kDociRowsPerWarp;
-        const int64_t rows_per_launch = static_cast<int64_t>(1) << 30;
-        for (int64_t r0 = 0; r0 < p.nrow; r0 += rows_per_launch) {
-            const int64_t nr = std::min<int64_t>(p.nrow - r0, rows_per_launch);
-            fill_doci_warp_kernel<NW><<<static_cast<unsigned>((nr + rows_per_block - 1) / rows_per_block), 256, 0, st>>>(p, r0),
-                ::pyci_gpu::note_launch();
-        }
-        PYCI_CUDA_TRY(cudaGetLastError());
-        return PYCI_GPU_OK;
+        if (csr->dx_v && !(csr->flags & PYCI_BUILD_EAGER_CSR))
+            return defer_csr_doci(csr, p, NW);
+        int rc = csr_alloc_entries(csr);
+        if (rc)
+            return rc;
+        p.cols = csr->cols;
+        p.vals = csr->vals;
+        return launch_doci_fill<NW>(ctx, p);
     }
     if (sorted_fci) {
         // Per-string tables (alpha and beta; one set when both spins have the
@@ -2405,6 +2520,7 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
     // Integrals and the seniority-zero h, v, w (pyci/src/squantop.cpp:175-182).
     const int64_t n2 = n * n, n4 = n2 * n2;
     double *d_one = nullptr, *d_two = nullptr, *d_h = nullptr, *d_v = nullptr, *d_w = nullptr;
+    std::vector<float> dx_v; // DOCI: v split into high and low parts (the implicit form's table)
     PYCI_CUDA_TRY(tmp.alloc(&d_one, n2));
     PYCI_CUDA_TRY(tmp.alloc(&d_two, n4));
     PYCI_CUDA_TRY(cudaMemcpyAsync(d_one, one_mo, sizeof(double) * n2, cudaMemcpyHostToDevice, st));
@@ -2424,6 +2540,9 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_h, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_v, v.data(), sizeof(double) * n2, cudaMemcpyHostToDevice, st));
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_w, w.data(), sizeof(double) * n2, cudaMemcpyHostToDevice, st));
+        dx_v.resize(2 * n2);
+        for (int64_t i = 0; i < n2; ++i)
+            split_hi_lo(v[i], dx_v[i], dx_v[n2 + i]);
         // The host vectors die at scope end: wait for the copies.
         PYCI_CUDA_TRY(cudaStreamSynchronize(st));
     }
@@ -2535,6 +2654,23 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         const bool sorted_fci = uniform && kind == PYCI_WFN_FULLCI && p.ncache > 0 && na <= kSortedMax &&
                                 nbb <= kSortedMax && no_a * nv_a + no_b * nv_b <= kTableMaxSingles &&
                                 !(csr->flags & PYCI_BUILD_FORCE_HASH);
+        // Implicit form of a full DOCI space (docx.cu): the binomial table and
+        // the split pair integrals; products then read no stored entries.
+        if (warp_doci && csr->symmetric && n <= 64 && !dx_v.empty()) {
+            const size_t nb = binom.size();
+            cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&csr->dx_binom), sizeof(int64_t) * nb, st);
+            if (e == cudaSuccess)
+                e = cudaMallocAsync(reinterpret_cast<void **>(&csr->dx_v), sizeof(float) * dx_v.size(), st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(csr->dx_binom, binom.data(), sizeof(int64_t) * nb, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(csr->dx_v, dx_v.data(), sizeof(float) * dx_v.size(), cudaMemcpyHostToDevice, st);
+            if (e != cudaSuccess)
+                return cuda_status(e, "implicit DOCI tables");
+            csr->dx_n = static_cast<int>(n);
+            csr->dx_m = static_cast<int>(csr->nocc_up);
+            csr->dx_ldk = ldk;
+        }
         switch (nw) {
         case 1: rc = run_build<1>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci, warp_doci); break;
         case 2: rc = run_build<2>(ctx, p, csr, static_cast<int>(cap), ulen, sorted_fci, warp_doci); break;
@@ -2545,19 +2681,14 @@ int csr_build_device(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const uint64_t *dets_
         return rc;
 
     // Reference-layout row pointers (symmetric: prefix sums of lower_len).
-    if (csr->symmetric) {
-        int64_t *lens64 = nullptr;
-        PYCI_CUDA_TRY(tmp.alloc(&lens64, csr->nrow));
-        if (csr->nrow > 0)
-            widen_kernel<<<static_cast<unsigned>(std::min<int64_t>((csr->nrow + 255) / 256, 1 << 16)), 256, 0, st>>>(
-                csr->lower_len, lens64, csr->nrow), ::pyci_gpu::note_launch();
-        PYCI_CUDA_TRY(cudaGetLastError());
-        PYCI_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void **>(&csr->ref_rowptr), sizeof(int64_t) * (csr->nrow + 1), st));
-        rc = device_exclusive_scan(lens64, csr->nrow, csr->ref_rowptr, st);
+    // A deferred DOCI operator gets them with its entries; its pattern is
+    // symmetric, so the reference's count is the lower triangle + diagonal.
+    if (csr->symmetric && csr->deferred && kind == PYCI_WFN_DOCI) {
+        csr->nnz_ref = (csr->nnz - csr->nrow) / 2 + csr->nrow;
+    } else if (csr->symmetric) {
+        rc = ref_rowptr_from_lower_len(csr);
         if (rc)
             return rc;
-        PYCI_CUDA_TRY(cudaMemcpyAsync(&csr->nnz_ref, csr->ref_rowptr + csr->nrow, sizeof(int64_t),
-                                      cudaMemcpyDeviceToHost, st));
     } else {
         csr->nnz_ref = csr->nnz;
     }

@@ -46,6 +46,9 @@ static void fx_forget(pyci_gpu_csr *csr) {
     csr->fx_nalpha = csr->fx_nbeta = csr->fx_nbp = csr->fx_npk = 0;
     csr->fx_ns = csr->fx_nd = csr->fx_nlb = csr->fx_nls = 0;
     csr->fx_la = csr->fx_lb = csr->fx_lc = 0;
+    csr->dx_binom = nullptr;
+    csr->dx_v = nullptr;
+    csr->dx_n = csr->dx_m = csr->dx_ldk = 0;
 }
 
 void csr_release(pyci_gpu_csr *csr) {
@@ -56,7 +59,7 @@ void csr_release(pyci_gpu_csr *csr) {
     void *ptrs[] = {csr->rowptr,     csr->cols,     csr->vals,     csr->hi,        csr->lo,        csr->lower_len,
                     csr->ref_rowptr, csr->diag,     csr->sell_off, csr->sell_cols, csr->sell_vals,
                     csr->sell_lo,    csr->fx_atab,  csr->fx_bfull, csr->fx_bsub,   csr->fx_hi,
-                    csr->fx_lo,      csr->fx_bq};
+                    csr->fx_lo,      csr->fx_bq,    csr->dx_binom, csr->dx_v};
     for (void *p : ptrs)
         if (p)
             cudaFreeAsync(p, st);
@@ -319,6 +322,8 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
     c->fx_atab = c->fx_bfull = c->fx_bsub = nullptr;
     c->fx_bq = nullptr;
     c->fx_hi = c->fx_lo = nullptr;
+    c->dx_binom = nullptr;
+    c->dx_v = nullptr;
     const int64_t fx_vals = csr->fx_nalpha * (csr->fx_nbp / 32) * csr->fx_npk * 128;
     struct Item {
         void *src;
@@ -343,6 +348,8 @@ int pyci_gpu_csr_clone(const pyci_gpu_csr *csr, pyci_gpu_csr **out) {
         {csr->fx_bq, reinterpret_cast<void **>(&c->fx_bq), sizeof(uint16_t) * csr->fx_la * csr->fx_nbeta},
         {csr->fx_hi, reinterpret_cast<void **>(&c->fx_hi), sizeof(float) * fx_vals},
         {csr->fx_lo, reinterpret_cast<void **>(&c->fx_lo), sizeof(float) * fx_vals},
+        {csr->dx_binom, reinterpret_cast<void **>(&c->dx_binom), sizeof(int64_t) * (csr->dx_n + 1) * csr->dx_ldk},
+        {csr->dx_v, reinterpret_cast<void **>(&c->dx_v), sizeof(float) * 2 * csr->dx_n * csr->dx_n},
     };
     for (auto &it : items) {
         if (!it.src)
@@ -372,7 +379,7 @@ int pyci_gpu_csr_storage(const pyci_gpu_csr *csr, int *flags) {
         return PYCI_GPU_EINVAL;
     }
     *flags = (csr->vals ? PYCI_STORE_FP64 : 0) | (csr->hi && csr->lo ? PYCI_STORE_SPLIT : 0) |
-             (csr->sell_cols ? PYCI_STORE_SELL : 0) | (csr->fx_hi ? PYCI_STORE_IMPLICIT : 0) |
+             (csr->sell_cols ? PYCI_STORE_SELL : 0) | (has_implicit(csr) ? PYCI_STORE_IMPLICIT : 0) |
              (csr->deferred ? PYCI_STORE_DEFERRED : 0);
     return PYCI_GPU_OK;
 }

@@ -574,7 +574,7 @@ public:
         // PYCI_GPU_FP64_PRODUCT=native keeps FP64 arithmetic in the FP64
         // solve's products even when the split is there.
         const char *e = std::getenv("PYCI_GPU_FP64_PRODUCT");
-        fp64_df_ = !mixed && ((csr->hi && csr->lo) || csr->fx_hi) && !csr->lower_only &&
+        fp64_df_ = !mixed && ((csr->hi && csr->lo) || has_implicit(csr)) && !csr->lower_only &&
                    !(e && !std::strcmp(e, "native"));
     }
 
@@ -700,7 +700,7 @@ private:
         // up to 8 vectors share one launch (a 5-vector block as one product
         // padded to 8, not 4 + 1).  FP64 solves on an operator that holds the
         // exact high/low split multiply in double-float arithmetic.
-        const int chunk = (prec == PYCI_PREC_FP32 && (csr_->sell_cols || csr_->fx_hi)) ? kMaxQ : kSpmmChunk;
+        const int chunk = (prec == PYCI_PREC_FP32 && (csr_->sell_cols || has_implicit(csr_))) ? kMaxQ : kSpmmChunk;
         for (int j0 = 0; j0 < k; j0 += chunk) {
             const int kk = std::min(chunk, k - j0);
             const int kp = padded_width(kk);
@@ -1487,7 +1487,7 @@ int davidson_solve(pyci_gpu_csr *csr, int64_t n, const double *c0, int64_t ncv, 
         Davidson<float> d(csr, blk, n, mmax, true);
         return d.run(c0, iters, tol, ecore, evals, evecs, stats);
     }
-    if (!csr->vals && !(csr->hi && csr->lo) && !csr->fx_hi && !csr->deferred) {
+    if (!csr->vals && !(csr->hi && csr->lo) && !has_implicit(csr) && !csr->deferred) {
         set_error("operator has no values");
         return PYCI_GPU_EINVAL;
     }

@@ -48,6 +48,7 @@
 #include <climits>
 #include <cstdint>
 
+#include "dfarith.cuh"
 #include "internal.h"
 
 namespace pyci_gpu {
@@ -61,68 +62,6 @@ struct FxArgs {
     const ushort4 *bq; // [la / 4][nbeta]: section A's beta partners, 4 per packet (padding: b)
     const float4 *hi, *lo;
 };
-
-// Double-float term (vh + vl)(xh + xl) added to (s, c): p = fl(vh xh), its
-// exact error fma(vh, xh, -p), the small products vh xl + vl xh in FP32, p
-// added with TwoSum (the same arithmetic as the CSR double-float kernels).
-__device__ __forceinline__ void fx_two_sum(float &s, float &c, float p) {
-    const float u = __fadd_rn(s, p);
-    const float z = __fadd_rn(u, -s);
-    const float d = __fadd_rn(__fadd_rn(s, -__fadd_rn(u, -z)), __fadd_rn(p, -z));
-    s = u;
-    c = __fadd_rn(c, d);
-}
-
-template<int K>
-__device__ __forceinline__ void fx_df_term(float vh, float vl, const float xh[K], const float xl[K], float s[K],
-                                           float c[K]) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const float p = __fmul_rn(vh, xh[k]);
-        const float err = fmaf(vh, xh[k], -p);
-        const float t = fmaf(vh, xl[k], fmaf(vl, xh[k], err));
-        fx_two_sum(s[k], c[k], p);
-        c[k] = __fadd_rn(c[k], t);
-    }
-}
-
-// One entry whose x row is at xr (shared or global memory): accumulate
-// value (vh, vl) times that row.
-template<int MODE, int K>
-__device__ __forceinline__ void fx_acc(const float *xr, float vh, float vl, float acc[K], float cc[K]) {
-    if constexpr (MODE == 0) {
-        float xv[K];
-        if constexpr (K % 4 == 0) {
-#pragma unroll
-            for (int v = 0; v < K / 4; ++v) {
-                const float4 q = reinterpret_cast<const float4 *>(xr)[v];
-                xv[4 * v] = q.x, xv[4 * v + 1] = q.y, xv[4 * v + 2] = q.z, xv[4 * v + 3] = q.w;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < K; ++k)
-                xv[k] = xr[k];
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            acc[k] = fmaf(vh, xv[k], acc[k]);
-    } else {
-        float xh[K], xl[K];
-        if constexpr (K == 4) {
-            const float4 a = reinterpret_cast<const float4 *>(xr)[0];
-            const float4 b = reinterpret_cast<const float4 *>(xr)[1];
-            xh[0] = a.x, xh[1] = a.y, xh[2] = a.z, xh[3] = a.w;
-            xl[0] = b.x, xl[1] = b.y, xl[2] = b.z, xl[3] = b.w;
-        } else if constexpr (K == 2) {
-            const float4 a = reinterpret_cast<const float4 *>(xr)[0];
-            xh[0] = a.x, xh[1] = a.y, xl[0] = a.z, xl[1] = a.w;
-        } else {
-            const float2 a = reinterpret_cast<const float2 *>(xr)[0];
-            xh[0] = a.x, xl[0] = a.y;
-        }
-        fx_df_term<K>(vh, vl, xh, xl, acc, cc);
-    }
-}
 
 // Asynchronous copy of n floats from global src to shared dst by the whole
 // block (16-byte pieces when both ends and n allow it, 4-byte otherwise).
@@ -227,7 +166,7 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
                 const int jb[4] = {j4.x, j4.y, j4.z, j4.w};
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    fx_acc<MODE, K>(xb0 + jb[u] * XW, h4[u], l4[u], acc, cc);
+                    df_acc<MODE, K>(xb0 + jb[u] * XW, h4[u], l4[u], acc, cc);
             }
         }
     }
@@ -252,7 +191,7 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
                     const int jb[4] = {j4.x, j4.y, j4.z, j4.w};
 #pragma unroll
                     for (int u = 0; u < 4; ++u)
-                        fx_acc<MODE, K>(cur + jb[u] * XW, h4[u], l4[u], acc, cc);
+                        df_acc<MODE, K>(cur + jb[u] * XW, h4[u], l4[u], acc, cc);
                 }
             }
         }
@@ -272,7 +211,7 @@ __global__ void __launch_bounds__(512, 2) fcix_spmm_kernel(FxArgs A, const float
                 const int col[4] = {d4.x + b, d4.y + b, d4.z + b, d4.w + b};
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    fx_acc<MODE, K>(x + static_cast<int64_t>(col[u]) * XW, h4[u], l4[u], acc, cc);
+                    df_acc<MODE, K>(x + static_cast<int64_t>(col[u]) * XW, h4[u], l4[u], acc, cc);
             }
         }
         if (bb < nbeta) {

@@ -93,6 +93,12 @@ struct pyci_gpu_csr {
     uint16_t *fx_bq = nullptr;    // [la / 4][nbeta][4]: section A's partners by packet (padding: b)
     float *fx_hi = nullptr;       // [nslice][npk][32][4] high parts
     float *fx_lo = nullptr;       // [nslice][npk][32][4] low parts
+    // Implicit form of a full DOCI space (docx.cu): columns from each row's
+    // occupation, values from the pair-integral table, so a product reads no
+    // stored entries.  Null when the operator is not a full DOCI space.
+    int dx_n = 0, dx_m = 0, dx_ldk = 0; // orbitals, pairs, binomial row length (m + 2)
+    int64_t *dx_binom = nullptr;        // [(n + 1) * ldk]: C(o, k)
+    float *dx_v = nullptr;              // [2][n][n]: v split into high and low parts
     // Deferred CSR: an operator with the implicit-column form is built
     // without its CSR entries (cols, vals null) unless PYCI_BUILD_EAGER_CSR
     // asks for them; this holds what the CSR fill needs (build.cu), and
@@ -102,6 +108,10 @@ struct pyci_gpu_csr {
 
 // Width of one alpha string's row of pyci_gpu_csr::fx_atab.
 inline int fx_atab_width(const pyci_gpu_csr *c) { return 2 * (c->fx_ns + c->fx_nd) + 1; }
+
+// Whether the operator has an implicit form (full FullCI or full DOCI space)
+// that serves its FP32 and double-float products.
+inline bool has_implicit(const pyci_gpu_csr *c) { return c->fx_hi || c->dx_v; }
 
 namespace pyci_gpu {
 // Kernel launches issued by this library (diagnostic counter).
@@ -140,6 +150,14 @@ void csr_release(pyci_gpu_csr *csr);
 // caller then uses another kernel).
 bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
                  cudaStream_t st);
+// The same on the implicit form of a full DOCI space (docx.cu).
+bool docx_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
+                 cudaStream_t st);
+// Whichever implicit form the operator has.
+inline bool implicit_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y,
+                            int64_t ldy, cudaStream_t st) {
+    return csr->dx_v ? docx_launch(csr, mode, K, x, ldx, y, ldy, st) : fcix_launch(csr, mode, K, x, ldx, y, ldy, st);
+}
 // Writes a deferred CSR's entries (no-op when there is nothing deferred);
 // every path that reads cols or vals calls it first.  Logically const: the
 // operator's contents do not change.

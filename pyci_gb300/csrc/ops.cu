@@ -232,7 +232,7 @@ static unsigned grid_for(const pyci_gpu_ctx *ctx, int64_t n, int threads) {
 
 int csr_export_device(const pyci_gpu_csr *csr, double *data, int64_t *indices, int64_t *indptr) {
     cudaStream_t st = csr->ctx->stream;
-    if (data || indices) {
+    if (data || indices || !(csr->symmetric ? csr->ref_rowptr : csr->rowptr)) {
         int rc = csr_materialize(csr);
         if (rc)
             return rc;
@@ -405,8 +405,8 @@ int csr_ensure_split(pyci_gpu_csr *csr) {
 
 int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
     cudaStream_t st = csr->ctx->stream;
-    if (csr->fx_hi) {
-        // A full FullCI space: the build wrote the implicit-column form, which
+    if (has_implicit(csr)) {
+        // A full FullCI or DOCI space: the implicit form, which
         // serves the FP32 and double-float products; the CSR-order split is
         // made on demand (csr_ensure_split), or here when the FP64 values go.
         if (drop_fp64 && csr->vals) {

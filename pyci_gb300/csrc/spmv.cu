@@ -455,7 +455,7 @@ constexpr int kFxVariant = 0x200;   // implicit-column form of a full FullCI spa
 // product this GPU's FP64 pipe already bounds.
 template<int VK>
 inline bool fx_usable(const pyci_gpu_csr *csr, int K) {
-    return VK == kF32 && csr->fx_hi && K <= 8;
+    return VK == kF32 && has_implicit(csr) && K <= 8;
 }
 inline int variant_lanes(int v) { return v % 3 == 0 ? 8 : (v % 3 == 1 ? 16 : 32); }
 inline int variant_map(int v) { return v / 3; }
@@ -466,7 +466,7 @@ template<int VK, int K>
 void launch_variant(int v, const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t ldx, void *y,
                     int64_t ldy, cudaStream_t st) {
     if (v == kFxVariant) {
-        if (VK == kF32 && fcix_launch(csr, 0, K, x, ldx, y, ldy, st))
+        if (VK == kF32 && implicit_launch(csr, 0, K, x, ldx, y, ldy, st))
             return;
         v = heuristic_variant(csr); // a cached choice from an operator of the same shape without the form
     }
@@ -572,7 +572,7 @@ int forced_sell_variant(const pyci_gpu_csr *csr) {
     if (!e)
         return -1;
     if (!std::strcmp(e, "fcix"))
-        return csr->fx_hi ? kFxVariant : heuristic_variant(csr);
+        return has_implicit(csr) ? kFxVariant : heuristic_variant(csr);
     if (!std::strcmp(e, "sell"))
         return csr->sell_cols ? kSellVariant : heuristic_variant(csr);
     if (!std::strcmp(e, "sell1"))
@@ -889,7 +889,7 @@ __global__ void __launch_bounds__(256) spmm_df_sell_kernel(int64_t nrow, int64_t
 template<int K>
 void launch_df_variant(int v, const pyci_gpu_csr *csr, const float *xs, double *y, cudaStream_t st) {
     if (v == kFxVariant) {
-        if (fcix_launch(csr, 2, K, xs, 2 * K, y, K, st))
+        if (implicit_launch(csr, 2, K, xs, 2 * K, y, K, st))
             return;
         v = heuristic_variant(csr);
     }
@@ -936,9 +936,9 @@ using namespace pyci_gpu;
 // arithmetic with double-float accumulation; the tile variant (lanes per row x
 // entry mapping, as the other products) is tuned on first use.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
-    if ((!csr->hi || !csr->lo) && csr->fx_hi) {
+    if ((!csr->hi || !csr->lo) && has_implicit(csr)) {
         // Implicit-column form only (a full FullCI space).
-        if ((K == 1 || K == 2 || K == 4) && !pinned_to_csr() && fcix_launch(csr, 2, K, xs, 2 * K, y, K, st)) {
+        if ((K == 1 || K == 2 || K == 4) && !pinned_to_csr() && implicit_launch(csr, 2, K, xs, 2 * K, y, K, st)) {
             csr->tuned[kSplitDF][K] = kFxVariant;
             PYCI_CUDA_TRY(cudaGetLastError());
             return PYCI_GPU_OK;
@@ -985,7 +985,7 @@ int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cuda
                     best_v = v;
                 }
             }
-            if (csr->fx_hi) {
+            if (has_implicit(csr)) {
                 launch_df(kFxVariant, csr, K, xs, y, st);
                 cudaEventRecord(a, st);
                 launch_df(kFxVariant, csr, K, xs, y, st);
@@ -1097,11 +1097,11 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
         }
         break;
     case PYCI_PREC_FP32:
-        if (!csr->hi && csr->fx_hi) {
+        if (!csr->hi && has_implicit(csr)) {
             // Only the implicit-column form holds FP32 values (a full FullCI
             // space): up to 8 vectors in one launch; the CSR-order split is
             // made on demand for anything else.
-            if (k <= 8 && !pinned_to_csr() && fcix_launch(csr, 0, static_cast<int>(k), x, k, y, k, stream)) {
+            if (k <= 8 && !pinned_to_csr() && implicit_launch(csr, 0, static_cast<int>(k), x, k, y, k, stream)) {
                 csr->tuned[kF32][k] = kFxVariant;
                 break;
             }
@@ -1116,7 +1116,7 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
         launch_vk<kF32>(csr, Values<kF32>{csr->hi}, k, x, y, stream);
         break;
     case PYCI_PREC_FP64_SPLIT:
-        if (!csr->hi && csr->fx_hi) {
+        if (!csr->hi && has_implicit(csr)) {
             int rc = csr_ensure_split(const_cast<pyci_gpu_csr *>(csr));
             if (rc)
                 return rc;
