@@ -11,13 +11,15 @@
 // columns from its occupation and reads v from shared memory; only x, y and
 // the diagonal move through HBM.
 //
-// Column of p -> q.  With a = index of p in S and b = number of members
-// below q (p included when p < q): moving p to q shifts the index of every
-// member between them by one, so
-//   q > p:  rank' = rank - C(p, a + 1) + C(q, b) + sum_{a < i < b} (C(o_i, i) - C(o_i, i + 1))
-//   q < p:  rank' = rank - C(p, a + 1) + C(q, b + 1) + sum_{b <= i < a} (C(o_i, i + 2) - C(o_i, i + 1))
-// and the sums are differences of per-row prefix sums Dd, Du that each lane
-// keeps in shared memory; b is a population count.
+// Column of p -> q.  With S_p = S - {p} (members sp_0 < ... < sp_{m-2}) and
+// k = the number of members of S_p below q, the members below q keep their
+// index, q takes index k and the members above move up by one, so
+//   rank(S_p + q) = H_p[k] + C(q, k + 1),
+//   H_p[k] = sum_{i < k} C(sp_i, i + 1) + sum_{i >= k} C(sp_i, i + 2).
+// Each lane builds H_p (m values) once per occupied p in shared memory; per
+// move the column is a population count, two shared-memory reads and an
+// add.  Ranks are below 2^31; the sums run in 32-bit unsigned arithmetic
+// (binomials reduced mod 2^32), exact because the result is.
 //
 // Tables: binomials C(o, k) for o <= n, k <= m + 1 (int64), and v split into
 // FP32 high and low parts.  The diagonal is the operator's (FP64, split per
@@ -45,32 +47,37 @@ struct DxArgs {
 
 __host__ __device__ inline size_t dx_align16(size_t b) { return (b + 15) / 16 * 16; }
 
-// Shared memory: binomials, v (high, low), then per warp the lanes'
-// occupied orbitals [m][32] (int) and prefix sums Dd, Du [m + 1][32] (int64).
+// Shared memory: binomials (int64 for the unranking, uint32 mod 2^32 for the
+// columns), v (high, low), then per warp the lanes' occupied orbitals and
+// H_p, [m][32] each.
 __host__ __device__ inline size_t dx_fixed_bytes(int n, int ldk) {
-    return dx_align16(sizeof(int64_t) * (n + 1) * ldk) + dx_align16(sizeof(float) * 2 * n * n);
+    return dx_align16(sizeof(int64_t) * (n + 1) * ldk) + dx_align16(sizeof(uint32_t) * (n + 1) * ldk) +
+           dx_align16(sizeof(float) * 2 * n * n);
 }
-__host__ __device__ inline size_t dx_warp_bytes(int m) {
-    return dx_align16(sizeof(int) * m * 32) + 2 * dx_align16(sizeof(int64_t) * (m + 1) * 32);
-}
+__host__ __device__ inline size_t dx_warp_bytes(int m) { return 2 * dx_align16(sizeof(int) * m * 32); }
 
 // MODE 0: FP32 (x, y float [N][K]); MODE 2: double-float (xs float [N][2K],
-// y double [N][K]).  One warp per 32 consecutive rows.
-template<int MODE, int K>
+// y double [N][K]).  One warp per 32 consecutive rows; M: the occupation
+// mask type (32 bits when n <= 32).
+template<int MODE, int K, typename M>
 __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *__restrict__ x, void *__restrict__ yv) {
     constexpr int XW = MODE == 2 ? 2 * K : K; // floats per x row
+    constexpr int MB = 8 * sizeof(M);
     extern __shared__ __align__(16) unsigned char dx_smem[];
-    const int n = A.n, m = A.m, ldk = A.ldk;
+    const int n = A.n, m = A.m, ldk = A.ldk, nb = (n + 1) * ldk;
     int64_t *bn = reinterpret_cast<int64_t *>(dx_smem);
-    float *vh = reinterpret_cast<float *>(dx_smem + dx_align16(sizeof(int64_t) * (n + 1) * ldk));
+    uint32_t *bu = reinterpret_cast<uint32_t *>(dx_smem + dx_align16(sizeof(int64_t) * nb));
+    float *vh = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(bu) + dx_align16(sizeof(uint32_t) * nb));
     float *vl = vh + n * n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char *mine = dx_smem + dx_fixed_bytes(n, ldk) + dx_warp_bytes(m) * warp;
     int *occ = reinterpret_cast<int *>(mine);
-    int64_t *Dd = reinterpret_cast<int64_t *>(mine + dx_align16(sizeof(int) * m * 32));
-    int64_t *Du = Dd + dx_align16(sizeof(int64_t) * (m + 1) * 32) / sizeof(int64_t);
-    for (int i = threadIdx.x; i < (n + 1) * ldk; i += blockDim.x)
-        bn[i] = __ldg(A.binom + i);
+    uint32_t *H = reinterpret_cast<uint32_t *>(mine + dx_align16(sizeof(int) * m * 32));
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        const int64_t c = __ldg(A.binom + i);
+        bn[i] = c;
+        bu[i] = static_cast<uint32_t>(c);
+    }
     for (int i = threadIdx.x; i < 2 * n * n; i += blockDim.x)
         vh[i] = __ldg(A.v + i);
     __syncthreads();
@@ -78,35 +85,21 @@ __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *_
     if (row - lane >= A.nrow)
         return;
     const bool valid = row < A.nrow;
-    const int64_t s = valid ? row : A.nrow - 1;
-    // Occupation of row s (colex unranking), then the prefix sums.
-    uint64_t S = 0;
+    const int s = static_cast<int>(valid ? row : A.nrow - 1);
+    // Occupation of row s (colex unranking).
+    M S = 0;
     {
         int64_t r = s;
         int o = n - 1;
         for (int j = m; j >= 1; --j) {
             while (bn[o * ldk + j] > r)
                 --o;
-            S |= 1ULL << o;
+            S |= M(1) << o;
+            occ[(j - 1) * 32 + lane] = o;
             r -= bn[o * ldk + j];
             --o;
         }
-        uint64_t w = S;
-        int64_t dd = 0, du = 0;
-        Dd[lane] = 0;
-        Du[lane] = 0;
-        for (int i = 0; i < m; ++i) {
-            const int oi = __ffsll(static_cast<long long>(w)) - 1;
-            w &= w - 1;
-            occ[i * 32 + lane] = oi;
-            const int64_t c1 = bn[oi * ldk + i + 1];
-            dd += bn[oi * ldk + i] - c1;
-            du += bn[oi * ldk + i + 2] - c1;
-            Dd[(i + 1) * 32 + lane] = dd;
-            Du[(i + 1) * 32 + lane] = du;
-        }
     }
-    __syncwarp();
     float acc[K], cc[K];
 #pragma unroll
     for (int k = 0; k < K; ++k)
@@ -114,38 +107,60 @@ __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *_
     {
         float dh, dl;
         split_hi_lo(__ldg(A.diag + s), dh, dl);
-        df_acc<MODE, K>(x + s * XW, dh, dl, acc, cc);
+        df_acc<MODE, K>(x + static_cast<int64_t>(s) * XW, dh, dl, acc, cc);
     }
-    const uint64_t full = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    const M full = n >= MB ? ~M(0) : ((M(1) << n) - 1);
     const int nv = n - m;
+    const int last = static_cast<int>(A.nrow - 1);
     for (int a = 0; a < m; ++a) {
         const int p = occ[a * 32 + lane];
-        const int64_t base = s - bn[p * ldk + a + 1];
-        const int64_t dda = Dd[(a + 1) * 32 + lane], dua = Du[a * 32 + lane];
+        const M Sp = S & ~(M(1) << p);
+        // H_p[k], k = 0 .. m - 1: suffix sums of C(sp_i, i + 2), then the
+        // prefix sums of C(sp_i, i + 1) added (sp_i = occ[i] below a, occ[i + 1] from a on).
+        {
+            uint32_t hs = 0;
+            H[(m - 1) * 32 + lane] = 0;
+            for (int k = m - 2; k >= 0; --k) {
+                const int sp = occ[(k < a ? k : k + 1) * 32 + lane];
+                hs += bu[sp * ldk + k + 2];
+                H[k * 32 + lane] = hs;
+            }
+            uint32_t ls = 0;
+            for (int k = 0; k < m; ++k) {
+                H[k * 32 + lane] += ls;
+                if (k < m - 1)
+                    ls += bu[occ[(k < a ? k : k + 1) * 32 + lane] * ldk + k + 1];
+            }
+        }
         const float *ph = vh + p * n, *pl = vl + p * n;
-        uint64_t vir = ~S & full;
+        M vir = ~S & full;
         // Four moves at a time: their x rows are loaded before any is used.
         for (int j0 = 0; j0 < nv; j0 += 4) {
-            int64_t rr[4];
+            int rr[4];
             float wh[4], wl[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 rr[u] = s;
                 wh[u] = wl[u] = 0.0f;
                 if (j0 + u < nv) {
-                    const int q = __ffsll(static_cast<long long>(vir)) - 1;
+                    int q;
+                    if constexpr (MB == 32)
+                        q = __ffs(static_cast<int>(vir)) - 1;
+                    else
+                        q = __ffsll(static_cast<long long>(vir)) - 1;
                     vir &= vir - 1;
-                    const int b = __popcll(S & ((1ULL << q) - 1));
-                    const int64_t r = q > p ? base + bn[q * ldk + b] + Dd[b * 32 + lane] - dda
-                                            : base + bn[q * ldk + b + 1] + dua - Du[b * 32 + lane];
-                    rr[u] = min(max(r, static_cast<int64_t>(0)), A.nrow - 1); // in range by construction
+                    const M below = Sp & ((M(1) << q) - 1);
+                    const int kq = MB == 32 ? __popc(static_cast<unsigned>(below)) : __popcll(below);
+                    const int r = static_cast<int>(H[kq * 32 + lane] + bu[q * ldk + kq + 1]);
+                    rr[u] = min(max(r, 0), last); // in range by construction
                     wh[u] = ph[q];
-                    wl[u] = pl[q];
+                    if (MODE == 2)
+                        wl[u] = pl[q];
                 }
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                df_acc<MODE, K>(x + rr[u] * XW, wh[u], wl[u], acc, cc);
+                df_acc<MODE, K>(x + static_cast<int64_t>(rr[u]) * XW, wh[u], wl[u], acc, cc);
         }
     }
     if (valid) {
@@ -159,8 +174,8 @@ __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *_
     }
 }
 
-template<int MODE, int K>
-bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
+template<int MODE, int K, typename M>
+bool dx_launch_m(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
     DxArgs A;
     A.nrow = csr->nrow;
     A.n = csr->dx_n;
@@ -171,9 +186,9 @@ bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t s
     A.diag = csr->diag;
     static const size_t limit = [&] {
         cudaFuncAttributes fa{};
-        cudaFuncGetAttributes(&fa, docx_spmm_kernel<MODE, K>);
+        cudaFuncGetAttributes(&fa, docx_spmm_kernel<MODE, K, M>);
         const size_t lim = csr->ctx->smem_optin > fa.sharedSizeBytes ? csr->ctx->smem_optin - fa.sharedSizeBytes : 0;
-        cudaFuncSetAttribute(docx_spmm_kernel<MODE, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(docx_spmm_kernel<MODE, K, M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(lim));
         return lim;
     }();
@@ -189,10 +204,15 @@ bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t s
     const int64_t blocks = (A.nrow + rows_per_block - 1) / rows_per_block;
     if (blocks <= 0)
         return true;
-    docx_spmm_kernel<MODE, K><<<static_cast<unsigned>(blocks), 32 * warps, smem, st>>>(
+    docx_spmm_kernel<MODE, K, M><<<static_cast<unsigned>(blocks), 32 * warps, smem, st>>>(
         A, static_cast<const float *>(x), y);
     note_launch();
     return true;
+}
+
+template<int MODE, int K>
+bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
+    return csr->dx_n <= 32 ? dx_launch_m<MODE, K, uint32_t>(csr, x, y, st) : dx_launch_m<MODE, K, uint64_t>(csr, x, y, st);
 }
 
 } // namespace pyci_gpu
