@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -34,7 +35,9 @@
 #include <vector>
 
 #include "dense.h"
+#include "dfarith.cuh"
 #include "internal.h"
+#include "split_bits.h"
 
 namespace pyci_gpu {
 
@@ -200,6 +203,68 @@ __global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A,
     }
 }
 
+// The FP64 solve's Gram products in double-float arithmetic: each FP64
+// element is split into FP32 high and low parts (integer arithmetic, exact),
+// each product (ah + al)(bh + bl) formed with an FMA for the error of ah bh
+// and FP32 cross terms, summed with TwoSum per thread, and the thread sums
+// added in FP64 from the warp reduction on.  About 2^-47 relative per
+// product against 2^-53 in FP64, at FP32 issue rates: this GPU's FP64 pipe
+// runs a small fraction of them, and bounds the FP64 form of this product
+// (2 p q FMAs per row against 8 (p + q) bytes read).
+template<int PI, int QC>
+__global__ void __launch_bounds__(256) gram_rows_df_kernel(const double *__restrict__ A, int p,
+                                                           const double *__restrict__ B, int q, int64_t N,
+                                                           double *__restrict__ partial) {
+    const int i0 = blockIdx.x * PI;
+    const int ni = min(PI, p - i0);
+    float s[PI][QC], c[PI][QC];
+#pragma unroll
+    for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+        for (int j = 0; j < QC; ++j)
+            s[ii][j] = c[ii][j] = 0.0f;
+    for (int64_t r = blockIdx.y * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
+         r += static_cast<int64_t>(gridDim.y) * blockDim.x) {
+        float bh[QC], bl[QC];
+#pragma unroll
+        for (int j = 0; j < QC; ++j) {
+            bh[j] = bl[j] = 0.0f;
+            if (j < q)
+                split_hi_lo(B[j * N + r], bh[j], bl[j]);
+        }
+#pragma unroll
+        for (int ii = 0; ii < PI; ++ii) {
+            if (ii < ni) {
+                float ah, al;
+                split_hi_lo(A[(i0 + ii) * N + r], ah, al);
+                df_term<QC>(ah, al, bh, bl, s[ii], c[ii]);
+            }
+        }
+    }
+    __shared__ double red[8][PI * QC];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int ii = 0; ii < PI; ++ii)
+#pragma unroll
+        for (int j = 0; j < QC; ++j) {
+            double v = static_cast<double>(s[ii][j]) + static_cast<double>(c[ii][j]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0)
+                red[warp][ii * QC + j] = v;
+        }
+    __syncthreads();
+    const int nwarps = blockDim.x >> 5;
+    for (int idx = threadIdx.x; idx < ni * q; idx += blockDim.x) {
+        const int ii = idx / q, j = idx % q;
+        double v = 0.0;
+        for (int w = 0; w < nwarps; ++w)
+            v += red[w][ii * QC + j];
+        partial[static_cast<int64_t>(blockIdx.y) * p * q + (i0 + ii) * q + j] = v;
+    }
+}
+
 // Launch gram_rows_kernel with the register tile that fits q (<= 8): rows
 // of A per block PI = 8 (4 when q > 4).  budget: blocks to aim for.  Returns
 // the number of partial sums per entry (blocks along x).
@@ -238,6 +303,36 @@ unsigned launch_gram_rows_r(unsigned budget, cudaStream_t st, const T *A, int p,
 
 // 16-byte row loads when N is a multiple of 16 / sizeof(T) and both vector
 // sets start on 16-byte boundaries (every vector then does).
+// launch_gram_tile's grid for gram_rows_df_kernel (one row per thread step).
+template<int PI, int QC>
+unsigned launch_gram_df_tile(unsigned budget, cudaStream_t st, const double *A, int p, const double *B, int q,
+                             int64_t N, double *partial) {
+    static const int per_sm = [] {
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gram_rows_df_kernel<PI, QC>, 256, 0) != cudaSuccess)
+            n = 1;
+        return std::max(1, std::min(4, n));
+    }();
+    const int64_t wave = static_cast<int64_t>(budget / 4) * per_sm;
+    const unsigned gy = static_cast<unsigned>((p + PI - 1) / PI);
+    const unsigned nb = static_cast<unsigned>(
+        std::max<int64_t>(1, std::min<int64_t>(std::max<int64_t>(1, wave / gy), (N + 255) / 256)));
+    gram_rows_df_kernel<PI, QC><<<dim3(gy, nb), 256, 0, st>>>(A, p, B, q, N, partial);
+    return nb;
+}
+
+unsigned launch_gram_df(unsigned budget, cudaStream_t st, const double *A, int p, const double *B, int q, int64_t N,
+                        double *partial) {
+    // Register tiles of at most 16 (sum, error) pairs per thread.
+    if (q <= 1)
+        return launch_gram_df_tile<8, 1>(budget, st, A, p, B, q, N, partial);
+    if (q <= 2)
+        return launch_gram_df_tile<8, 2>(budget, st, A, p, B, q, N, partial);
+    if (q <= 4)
+        return launch_gram_df_tile<4, 4>(budget, st, A, p, B, q, N, partial);
+    return launch_gram_df_tile<2, 8>(budget, st, A, p, B, q, N, partial);
+}
+
 template<typename T>
 unsigned launch_gram_rows(unsigned budget, cudaStream_t st, const T *A, int p, const T *B, int q, int64_t N,
                           double *partial) {
@@ -265,6 +360,73 @@ __global__ void reduce_partials_kernel(const double *__restrict__ partial, int n
             s += __shfl_xor_sync(0xffffffffu, s, o);
         if (threadIdx.x == 0)
             out[idx] = s;
+    }
+}
+
+// Coefficients of one double-float combination launch: FP32 high and low
+// parts of each FP64 coefficient.
+struct CoefBlockDF {
+    float h[kMaxGramP * kMaxQ], l[kMaxGramP * kMaxQ];
+};
+
+// The FP64 solve's combinations in double-float arithmetic (see
+// gram_rows_df_kernel): out[j][r] = beta out[j][r] + sum_i Y[i][j] V[i][r]
+// with V's elements split exactly into FP32 high and low parts, products and
+// sums in FP32 with TwoSum, and FP64 only for the final beta step.  Two rows
+// per thread step (16-byte loads) when N is even and the vectors 16-byte
+// aligned (R = 2), else one.
+template<int R>
+__global__ void __launch_bounds__(256) combine_df_kernel(const double *__restrict__ V, int p, int64_t N,
+                                                         const __grid_constant__ CoefBlockDF Y, int q, double beta,
+                                                         double *__restrict__ out) {
+    const int64_t nu = N / R;
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
+         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = u * R;
+        float s[kMaxQ][R], c[kMaxQ][R];
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+#pragma unroll
+            for (int t = 0; t < R; ++t)
+                s[j][t] = c[j][t] = 0.0f;
+#pragma unroll 4
+        for (int i = 0; i < p; ++i) {
+            double v[R];
+            if constexpr (R == 2) {
+                const double2 w = *reinterpret_cast<const double2 *>(V + i * N + r);
+                v[0] = w.x;
+                v[1] = w.y;
+            } else {
+                v[0] = V[i * N + r];
+            }
+            float vh[R], vl[R];
+#pragma unroll
+            for (int t = 0; t < R; ++t)
+                split_hi_lo(v[t], vh[t], vl[t]);
+#pragma unroll
+            for (int j = 0; j < kMaxQ; ++j)
+                if (j < q) {
+                    const float yh = Y.h[i * q + j], yl = Y.l[i * q + j];
+#pragma unroll
+                    for (int t = 0; t < R; ++t) {
+                        const float pr = __fmul_rn(yh, vh[t]);
+                        const float err = fmaf(yh, vh[t], -pr);
+                        const float tt = fmaf(yh, vl[t], fmaf(yl, vh[t], err));
+                        df_two_sum(s[j][t], c[j][t], pr);
+                        c[j][t] = __fadd_rn(c[j][t], tt);
+                    }
+                }
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+            if (j < q) {
+                double *o = out + j * N + r;
+#pragma unroll
+                for (int t = 0; t < R; ++t) {
+                    const double sum = static_cast<double>(s[j][t]) + static_cast<double>(c[j][t]);
+                    o[t] = beta == 0.0 ? sum : fma(beta, o[t], sum);
+                }
+            }
     }
 }
 
@@ -476,20 +638,29 @@ __global__ void unit_kernel(T *V, int64_t N, const int64_t *idx, int k) {
             V[j * N + r] = (r == idx[j]) ? T(1) : T(0);
 }
 
-// v = e_idx + amp * noise(., col): one perturbed start vector.
 // Arg-min of (d[r], r) over the rows whose pair is above *prev (pairs
-// ordered by value, then row; all rows when prev is null), as (value, row)
-// in a double2 per block (row as a double: exact below 2^53; (+inf, -1)
-// when a block has no candidate).  argmin_final_kernel reduces the blocks.
-__device__ __forceinline__ bool pair_less(double va, double ia, double vb, double ib) {
-    return va < vb || (va == vb && ia < ib);
+// ordered by value, then row; all rows when prev is null), as (key, row) in
+// a longlong2 per block ((LLONG_MAX, -1) when a block has no candidate);
+// argmin_final_kernel reduces the blocks.  The comparisons run on an
+// order-preserving integer key of the value (sign-magnitude bits mapped to
+// two's complement, -0 as +0): no FP64 instruction, whose rate on this GPU
+// would bound the pass rather than its bytes.
+__device__ __forceinline__ long long order_key(double v) {
+    long long b = __double_as_longlong(v);
+    if (b == static_cast<long long>(0x8000000000000000ULL))
+        b = 0;
+    return b >= 0 ? b : b ^ 0x7FFFFFFFFFFFFFFFLL;
 }
 
-__device__ __forceinline__ void pair_min_block(double &v, double &i) {
-    __shared__ double sv[32], si[32];
+__device__ __forceinline__ bool pair_less(long long ka, long long ia, long long kb, long long ib) {
+    return ka < kb || (ka == kb && ia < ib);
+}
+
+__device__ __forceinline__ void pair_min_block(long long &v, long long &i) {
+    __shared__ long long sv[32], si[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
+        const long long ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
         if (pair_less(ov, oi, v, i))
             v = ov, i = oi;
     }
@@ -498,21 +669,21 @@ __device__ __forceinline__ void pair_min_block(double &v, double &i) {
         sv[w] = v, si[w] = i;
     __syncthreads();
     if (w == 0) {
-        v = lane < static_cast<int>(blockDim.x >> 5) ? sv[lane] : INFINITY;
-        i = lane < static_cast<int>(blockDim.x >> 5) ? si[lane] : -1.0;
+        v = lane < static_cast<int>(blockDim.x >> 5) ? sv[lane] : LLONG_MAX;
+        i = lane < static_cast<int>(blockDim.x >> 5) ? si[lane] : -1;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
+            const long long ov = __shfl_xor_sync(0xffffffffu, v, o), oi = __shfl_xor_sync(0xffffffffu, i, o);
             if (pair_less(ov, oi, v, i))
                 v = ov, i = oi;
         }
     }
 }
 
-__global__ void argmin_above_kernel(const double *__restrict__ d, int64_t N, const double2 *prev,
-                                    double2 *__restrict__ partial) {
-    const double lv = prev ? prev->x : -INFINITY, li = prev ? prev->y : -1.0;
-    double bv = INFINITY, bi = -1.0;
+__global__ void argmin_above_kernel(const double *__restrict__ d, int64_t N, const longlong2 *prev,
+                                    longlong2 *__restrict__ partial) {
+    const long long lv = prev ? prev->x : LLONG_MIN, li = prev ? prev->y : -1;
+    long long bv = LLONG_MAX, bi = -1;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     for (; r + 3 * stride < N; r += 4 * stride) {
@@ -522,33 +693,34 @@ __global__ void argmin_above_kernel(const double *__restrict__ d, int64_t N, con
             v[u] = __ldg(d + r + u * stride);
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const double ri = static_cast<double>(r + u * stride);
-            if (pair_less(lv, li, v[u], ri) && pair_less(v[u], ri, bv, bi))
-                bv = v[u], bi = ri;
+            const long long kv = order_key(v[u]), ri = r + u * stride;
+            if (pair_less(lv, li, kv, ri) && pair_less(kv, ri, bv, bi))
+                bv = kv, bi = ri;
         }
     }
     for (; r < N; r += stride) {
-        const double v = d[r], ri = static_cast<double>(r);
-        if (pair_less(lv, li, v, ri) && pair_less(v, ri, bv, bi))
-            bv = v, bi = ri;
+        const long long kv = order_key(d[r]), ri = r;
+        if (pair_less(lv, li, kv, ri) && pair_less(kv, ri, bv, bi))
+            bv = kv, bi = ri;
     }
     pair_min_block(bv, bi);
     if (threadIdx.x == 0)
-        partial[blockIdx.x] = make_double2(bv, bi);
+        partial[blockIdx.x] = make_longlong2(bv, bi);
 }
 
-__global__ void argmin_final_kernel(const double2 *__restrict__ partial, int nb, double2 *out) {
-    double bv = INFINITY, bi = -1.0;
+__global__ void argmin_final_kernel(const longlong2 *__restrict__ partial, int nb, longlong2 *out) {
+    long long bv = LLONG_MAX, bi = -1;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-        const double2 p = partial[b];
-        if (p.y >= 0.0 && pair_less(p.x, p.y, bv, bi))
+        const longlong2 p = partial[b];
+        if (p.y >= 0 && pair_less(p.x, p.y, bv, bi))
             bv = p.x, bi = p.y;
     }
     pair_min_block(bv, bi);
     if (threadIdx.x == 0)
-        *out = make_double2(bv, bi);
+        *out = make_longlong2(bv, bi);
 }
 
+// v = e_idx + amp * noise(., col): one perturbed start vector.
 template<typename T>
 __global__ void guess_kernel(T *v, int64_t N, int64_t idx, double amp, int col) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
@@ -576,6 +748,10 @@ public:
         const char *e = std::getenv("PYCI_GPU_FP64_PRODUCT");
         fp64_df_ = !mixed && ((csr->hi && csr->lo) || has_implicit(csr)) && !csr->lower_only &&
                    !(e && !std::strcmp(e, "native"));
+        // PYCI_GPU_FP64_LINALG=native keeps FP64 arithmetic in the FP64
+        // Gram products and combinations (double-float by default).
+        const char *l = std::getenv("PYCI_GPU_FP64_LINALG");
+        df_linalg_ = !(l && !std::strcmp(l, "native"));
     }
 
     ~Davidson() {
@@ -628,6 +804,10 @@ private:
                 if (on_tc) {
                     nb = launch_gram_tc(gram_blocks_, st_, reinterpret_cast<const float *>(Ai), pp,
                                         reinterpret_cast<const float *>(Bj), qq, N_, d_partial_);
+                } else if (std::is_same<U, double>::value && df_linalg_) {
+                    nb = launch_gram_df(gram_blocks_, st_, reinterpret_cast<const double *>(Ai), pp,
+                                        reinterpret_cast<const double *>(Bj), qq, N_, d_partial_);
+                    ::pyci_gpu::note_launch();
                 } else {
                     nb = launch_gram_rows<U>(gram_blocks_, st_, Ai, pp, Bj, qq, N_, d_partial_);
                     ::pyci_gpu::note_launch();
@@ -670,6 +850,11 @@ private:
     // out[j] = beta out[j] + sum_i Y[i][j] V[i]  (Y host, p x q row-major).
     template<typename TV, typename TO, typename ACC>
     int combine(const TV *V, int p, const std::vector<double> &Y, int q, double beta, TO *out) {
+        if constexpr (std::is_same<TV, double>::value && std::is_same<TO, double>::value &&
+                      std::is_same<ACC, double>::value) {
+            if (df_linalg_)
+                return combine_df(V, p, Y, q, beta, out);
+        }
         for (int j0 = 0; j0 < q; j0 += kMaxQ) {
             const int qq = std::min(kMaxQ, q - j0);
             for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
@@ -687,6 +872,30 @@ private:
                     combine_kernel<TV, TO, ACC, R><<<grid(N_ / R), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
                 else
                     combine_kernel<TV, TO, ACC, 1><<<grid(N_), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
+                ::pyci_gpu::note_launch();
+            }
+        }
+        return PYCI_GPU_OK;
+    }
+
+    // combine<double, double, double> in double-float arithmetic
+    // (combine_df_kernel).
+    int combine_df(const double *V, int p, const std::vector<double> &Y, int q, double beta, double *out) {
+        for (int j0 = 0; j0 < q; j0 += kMaxQ) {
+            const int qq = std::min(kMaxQ, q - j0);
+            for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
+                const int pp = std::min(kMaxGramP, p - i0);
+                CoefBlockDF sub;
+                for (int i = 0; i < pp; ++i)
+                    for (int j = 0; j < qq; ++j)
+                        split_hi_lo(Y[static_cast<size_t>(i0 + i) * q + j0 + j], sub.h[i * qq + j], sub.l[i * qq + j]);
+                const double *Vi = V + static_cast<int64_t>(i0) * N_;
+                double *Oj = out + static_cast<int64_t>(j0) * N_;
+                const double bt = (i0 == 0) ? beta : 1.0;
+                if (N_ % 2 == 0 && reinterpret_cast<uintptr_t>(Vi) % 16 == 0 && reinterpret_cast<uintptr_t>(Oj) % 16 == 0)
+                    combine_df_kernel<2><<<grid(N_ / 2), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
+                else
+                    combine_df_kernel<1><<<grid(N_), 256, 0, st_>>>(Vi, pp, N_, sub, qq, bt, Oj);
                 ::pyci_gpu::note_launch();
             }
         }
@@ -753,7 +962,7 @@ private:
     // on the device: k passes of a grid-wide arg-min over the (value, row)
     // pairs above the previous pick, one read of the diagonal each.
     int lowest_diagonal(const double *d_diag, int64_t N, int k, std::vector<int64_t> &order) {
-        double2 *picks = nullptr, *partial = nullptr;
+        longlong2 *picks = nullptr, *partial = nullptr;
         const unsigned nb = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>((N + 255) / 256, 8 * csr_->ctx->num_sms)));
         int rc;
         if ((rc = alloc(&picks, k)) || (rc = alloc(&partial, nb)))
@@ -764,8 +973,8 @@ private:
             ::pyci_gpu::note_launch();
             ::pyci_gpu::note_launch();
         }
-        std::vector<double2> h(k);
-        PYCI_CUDA_TRY(cudaMemcpyAsync(h.data(), picks, sizeof(double2) * k, cudaMemcpyDeviceToHost, st_));
+        std::vector<longlong2> h(k);
+        PYCI_CUDA_TRY(cudaMemcpyAsync(h.data(), picks, sizeof(longlong2) * k, cudaMemcpyDeviceToHost, st_));
         PYCI_CUDA_TRY(wait());
         order.resize(k);
         for (int j = 0; j < k; ++j)
@@ -834,6 +1043,10 @@ private:
     // FP64 arithmetic at 4 FMAs per stored entry / (FP64 FMA rate), several
     // times the time the same product takes to stream its bytes.
     bool fp64_df_ = false;
+    // FP64 Gram products and combinations in double-float arithmetic
+    // (gram_rows_df_kernel, combine_df_kernel): the FP64 forms are bound by
+    // the FP64 pipe, not by the vectors' bytes.
+    bool df_linalg_ = true;
     double *d_partial_ = nullptr, *d_small_ = nullptr;
 };
 
@@ -888,13 +1101,62 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
         }
         return true;
     };
+    // T' = (T - V C1) L^{-T} from C1 = V^T T and L L^T = S (the Gram of
+    // T - V C1) as one combination of [V T] into Sb_, then copied to T.
+    auto apply_fused = [&](const std::vector<double> &C1, const std::vector<double> &Linv) -> int {
+        std::vector<double> Y(static_cast<size_t>(m + k) * k, 0.0);
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < k; ++j) {
+                double x = 0.0;
+                for (int t = 0; t < k; ++t)
+                    x -= C1[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(j) * k + t];
+                Y[static_cast<size_t>(i) * k + j] = x;
+            }
+        for (int i = 0; i < k; ++i)
+            for (int j = 0; j < k; ++j)
+                Y[static_cast<size_t>(m + i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
+        int r2 = combine<T, T, T>(V, m + k, Y, k, 0.0, Sb_);
+        if (r2)
+            return r2;
+        PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
+        return PYCI_GPU_OK;
+    };
     if (k > 1 && k <= kMaxQ) {
         bool ok = true;
         int passes_left = 2; // Cholesky-QR passes still to do
+        bool single = false;
         if (m > 0) {
-            // Pass 1.
-            if ((rc = gram<T>(V, m, Tb, k, C)))
+            // One Gram product [V T]^T T gives C1 = V^T T and T^T T, so
+            // T - V C1 has the Gram S = T^T T - C1^T C1.  When every column
+            // keeps at least half its squared norm (||t'|| >= ||t|| / sqrt 2:
+            // one classical Gram-Schmidt pass is then enough, the criterion
+            // of Daniel, Gragg, Kaufman and Stewart) and S is well
+            // conditioned, one combination finishes the block: 1 Gram product
+            // and 1 combination instead of 2 and 2.
+            if ((rc = gram<T>(V, m + k, Tb, k, C)))
                 return rc;
+            std::vector<double> S1(static_cast<size_t>(k) * k);
+            bool keeps = true;
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) {
+                    double x = C[static_cast<size_t>(m + i) * k + j];
+                    for (int t = 0; t < m; ++t)
+                        x -= C[static_cast<size_t>(t) * k + i] * C[static_cast<size_t>(t) * k + j];
+                    S1[static_cast<size_t>(i) * k + j] = x;
+                    if (i == j && !(x >= 0.5 * C[static_cast<size_t>(m + i) * k + i]))
+                        keeps = false;
+                }
+            std::vector<double> Linv;
+            if (keeps && cholesky_inv(S1, Linv) && kappa < 10.0) {
+                if ((rc = apply_fused(C, Linv)))
+                    return rc;
+                single = true;
+                passes_left = 0;
+            }
+        }
+        if (m > 0 && !single) {
+            // Pass 1 (C holds [V T]^T T: its first m rows are V^T T).
+            C.resize(static_cast<size_t>(m) * k);
             for (double &c : C)
                 c = -c;
             if ((rc = combine<T, T, T>(V, m, C, k, 1.0, Tb)))
@@ -917,21 +1179,9 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
                 }
             std::vector<double> Linv;
             if (smin > 0.0 && cmax * cmax <= 1e-4 * smin && cholesky_inv(Sm, Linv)) {
-                // new = (T - V C2) L^{-T}: rows i < m: -(C2 Linv^T)[i][j]; rows m + i: Linv[j][i].
-                std::vector<double> Y(static_cast<size_t>(m + k) * k, 0.0);
-                for (int i = 0; i < m; ++i)
-                    for (int j = 0; j < k; ++j) {
-                        double x = 0.0;
-                        for (int t = 0; t < k; ++t)
-                            x -= C[static_cast<size_t>(i) * k + t] * Linv[static_cast<size_t>(j) * k + t];
-                        Y[static_cast<size_t>(i) * k + j] = x;
-                    }
-                for (int i = 0; i < k; ++i)
-                    for (int j = 0; j < k; ++j)
-                        Y[static_cast<size_t>(m + i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
-                if ((rc = combine<T, T, T>(V, m + k, Y, k, 0.0, Sb_)))
+                // new = (T - V C2) L^{-T}.
+                if ((rc = apply_fused(C, Linv)))
                     return rc;
-                PYCI_CUDA_TRY(cudaMemcpyAsync(Tb, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
                 // A well-conditioned block is orthonormal to ~kappa * eps
                 // after one pass: skip the second (one product and one
                 // synchronisation fewer per iteration).
