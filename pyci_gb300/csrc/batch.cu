@@ -1624,18 +1624,17 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
         }
     }
     PYCI_CUDA_TRY(cudaSetDevice(ctx->device));
-    for (auto *c : v) {
-        // The batched kernels read the CSR: write deferred entries first.
-        int rc = csr_materialize(c);
-        if (rc)
-            return rc;
-    }
     const int64_t iters = (maxiter > 0) ? maxiter : 1000;
     const int mmax = 64; // per-problem subspace (restarts keep 16)
     if (mode == PYCI_SOLVE_MIXED) {
         for (auto *c : v) {
-            // The batched kernels read the CSR-order split.
-            int rc = csr_prepare_mixed_device(c, 0);
+            // The batched kernels read the CSR-order split.  One operator at
+            // a time: a deferred CSR is written, split, and its FP64 values
+            // freed again when prepare_mixed(drop_fp64) asked for that, so
+            // the FP64 values of all operators never coexist.
+            int rc = csr_materialize(c);
+            if (!rc)
+                rc = csr_prepare_mixed_device(c, 0);
             if (!rc)
                 rc = csr_ensure_split(c);
             if (rc)
@@ -1644,11 +1643,16 @@ extern "C" int pyci_gpu_batch_solve(pyci_gpu_ctx *ctx, int64_t nprob, pyci_gpu_c
         Batch<float> bsolve(ctx, v, static_cast<int>(n), mmax, true);
         return bsolve.run(iters, tol, ecore, evals, evecs, iterations, stats);
     }
-    for (auto *c : v)
+    for (auto *c : v) {
+        // The batched kernels read the CSR: write deferred entries first.
+        int rc = csr_materialize(c);
+        if (rc)
+            return rc;
         if (!c->vals && !(c->hi && c->lo)) {
             set_error("FP64 batched solve needs FP64 values");
             return PYCI_GPU_EINVAL;
         }
+    }
     Batch<double> bsolve(ctx, v, static_cast<int>(n), mmax, false);
     return bsolve.run(iters, tol, ecore, evals, evecs, iterations, stats);
 }

@@ -104,6 +104,9 @@ struct pyci_gpu_csr {
     // asks for them; this holds what the CSR fill needs (build.cu), and
     // csr_materialize() writes the entries on first use.  Null otherwise.
     void *deferred = nullptr;
+    // prepare_mixed(drop_fp64) was asked for: FP64 values written later (a
+    // deferred CSR) are freed again once the CSR-order split exists.
+    bool drop_fp64 = false;
 };
 
 // Width of one alpha string's row of pyci_gpu_csr::fx_atab.

@@ -400,11 +400,17 @@ int csr_ensure_split(pyci_gpu_csr *csr) {
         split_kernel<<<grid_for(csr->ctx, csr->nnz, 256), 256, 0, st>>>(csr->nnz, csr->vals, csr->hi, csr->lo),
             ::pyci_gpu::note_launch();
     PYCI_CUDA_TRY(cudaGetLastError());
+    if (csr->drop_fp64) {
+        PYCI_CUDA_TRY(cudaFreeAsync(csr->vals, st));
+        csr->vals = nullptr;
+    }
     return PYCI_GPU_OK;
 }
 
 int csr_prepare_mixed_device(pyci_gpu_csr *csr, int drop_fp64) {
     cudaStream_t st = csr->ctx->stream;
+    if (drop_fp64)
+        csr->drop_fp64 = true;
     if (has_implicit(csr)) {
         // A full FullCI or DOCI space: the implicit form, which
         // serves the FP32 and double-float products; the CSR-order split is
