@@ -33,6 +33,8 @@
 #include <numeric>
 #include <vector>
 
+#include <type_traits>
+
 #include "dense.h"
 #include "internal.h"
 
@@ -685,10 +687,12 @@ private:
         if ((rc = set_rowset(act_, mask)))
             return rc;
         for (int c = 0; c < kClasses; ++c) {
-            std::vector<int> mc(P_, 0);
-            for (int p = 0; p < P_; ++p)
+            std::vector<int> mc(P_, 0), m32(P_, 0);
+            for (int p = 0; p < P_; ++p) {
                 mc[p] = mask[p] && cls_of_[p] == c;
-            if ((rc = set_rowset(cls_[c], mc)))
+                m32[p] = mc[p] && !imp_[p];
+            }
+            if ((rc = set_rowset(cls_[c], mc)) || (rc = set_rowset(cls32_[c], m32)))
                 return rc;
         }
         std::vector<int64_t> tlo, thi;
@@ -830,12 +834,34 @@ private:
         }
     }
 
-    // Tile list of the active problems: row blocks of about target stored
-    // entries (a multiple of the rows one block covers at once), at each
-    // problem's class lanes per row; uploaded with its count.
-    int build_tiles(int64_t target) {
+    // The CSR launches' row set of class c at precision prec.
+    const DevRowSet &cls_for(int prec, int c) const { return prec == PYCI_PREC_FP32 ? cls32_[c] : cls_[c]; }
+
+    // FP32 products of the active problems with an implicit form, one launch
+    // each on their rows of Xi_ / Yi_ (K = 4, row stride 4); returns the
+    // number of launches.
+    int spmm_implicit(int prec) {
+        int n = 0;
+        if constexpr (std::is_same<T, float>::value) {
+            if (prec != PYCI_PREC_FP32)
+                return 0;
+            for (int p : act_.members)
+                if (imp_[p] && implicit_launch(ops_[p], 0, 4, Xi_ + row0_[p] * 4, 4, Yi_ + row0_[p] * 4, 4, st_))
+                    ++n;
+        }
+        return n;
+    }
+
+    // Tile list of the active problems (at FP32 without those with an
+    // implicit form): row blocks of about target stored entries (a multiple
+    // of the rows one block covers at once), at each problem's class lanes
+    // per row; uploaded with its count.
+    int build_tiles(int64_t target, int prec) {
         std::vector<BatchTile> t;
+        tiles_prec_ = prec;
         for (int p : act_.members) {
+            if (prec == PYCI_PREC_FP32 && imp_[p])
+                continue;
             const pyci_gpu_csr *c = ops_[p];
             const int lanes = cls_lanes_[cls_of_[p]];
             const int64_t per = 256 / lanes;
@@ -891,6 +917,16 @@ private:
     // cls_lanes_[c] the lanes per row the autotuner chose for it.
     static constexpr int kClasses = 3;
     DevRowSet cls_[kClasses];
+    // The FP32 products of problems with an implicit form (full FullCI or
+    // DOCI spaces) run on that form, one launch per such active problem on
+    // its rows of Xi_ / Yi_; cls32_[c] holds the active members of class c
+    // without them, for the FP32 CSR launches.
+    std::vector<char> imp_;
+    DevRowSet cls32_[kClasses];
+    std::vector<int> graph_members_;
+    int graph_imp_launches_ = 0;
+    bool imp_warm_ = false;
+    int tiles_prec_ = -1;
     std::vector<int> cls_of_;
     int cls_lanes_[kClasses] = {8, 16, 32};
     bool cls_tuned_ = false;
@@ -923,7 +959,11 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
     // is captured once per precision and replayed every iteration.
     if (prec == PYCI_PREC_FP64 && !all_vals_)
         prec = PYCI_PREC_FP64_SPLIT;
-    if (!graph_exec_ || graph_prec_ != prec || graph_v_ != V) {
+    // Graphs that launch implicit-form products bake in the active set.
+    bool any_imp = false;
+    for (int p : act_.members)
+        any_imp = any_imp || (prec == PYCI_PREC_FP32 && imp_[p]);
+    if (!graph_exec_ || graph_prec_ != prec || graph_v_ != V || (any_imp && graph_members_ != act_.members)) {
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
             graph_exec_ = nullptr;
@@ -938,12 +978,13 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             cudaEventCreate(&ea);
             cudaEventCreate(&eb);
             for (int c = 0; c < kClasses; ++c) {
-                if (cls_[c].total == 0)
+                const DevRowSet &rc_ = cls_for(prec, c);
+                if (rc_.total == 0)
                     continue;
                 int64_t cls_nnz = 0;
-                for (int p : cls_[c].members)
+                for (int p : rc_.members)
                     cls_nnz += ops_[p]->nnz;
-                const auto key = std::make_tuple(prec, cls_[c].total, cls_nnz);
+                const auto key = std::make_tuple(prec, rc_.total, cls_nnz);
                 {
                     std::lock_guard<std::mutex> lock(g_class_tune_mutex);
                     auto it = g_class_tune.find(key);
@@ -957,7 +998,7 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
                     for (int rep = 0; rep < 2; ++rep) {
                         if (rep == 1)
                             cudaEventRecord(ea, st_);
-                        spmm_class(prec, lanes, cls_[c]);
+                        spmm_class(prec, lanes, rc_);
                         if (rep == 1)
                             cudaEventRecord(eb, st_);
                     }
@@ -983,7 +1024,8 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             // fastest is kept (tile_nnz_ = 0: per-class launches).
             int64_t nnz_act = 0;
             for (int p : act_.members)
-                nnz_act += ops_[p]->nnz;
+                if (!(prec == PYCI_PREC_FP32 && imp_[p]))
+                    nnz_act += ops_[p]->nnz;
             const auto key = std::make_tuple(prec + 16, act_.total, nnz_act);
             bool cached = false;
             {
@@ -1001,17 +1043,17 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
                 cudaEventCreate(&eb);
                 // Candidate 0: one grid-stride launch per tile class.
                 for (int c = 0; c < kClasses; ++c)
-                    spmm_class(prec, cls_lanes_[c], cls_[c]);
+                    spmm_class(prec, cls_lanes_[c], cls_for(prec, c));
                 cudaEventRecord(ea, st_);
                 for (int c = 0; c < kClasses; ++c)
-                    spmm_class(prec, cls_lanes_[c], cls_[c]);
+                    spmm_class(prec, cls_lanes_[c], cls_for(prec, c));
                 cudaEventRecord(eb, st_);
                 PYCI_CUDA_TRY(cudaEventSynchronize(eb));
                 float best = 1e30f;
                 cudaEventElapsedTime(&best, ea, eb);
                 int best_sh = 0;
                 for (int sh : {16, 18, 20}) {
-                    int rc = build_tiles(int64_t(1) << sh);
+                    int rc = build_tiles(int64_t(1) << sh, prec);
                     if (rc)
                         return rc;
                     spmm_tiles(prec);
@@ -1035,10 +1077,17 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             }
             tiles_tuned_ = true;
         }
-        if (tiles_dirty_ && tile_nnz_) {
-            int rc = build_tiles(tile_nnz_);
+        if ((tiles_dirty_ || tiles_prec_ != prec) && tile_nnz_) {
+            int rc = build_tiles(tile_nnz_, prec);
             if (rc)
                 return rc;
+        }
+        // One run outside any capture: the implicit-form launchers set their
+        // kernels' shared-memory limits on first use.
+        if (any_imp && !imp_warm_) {
+            batch_pack_kernel<T, 4><<<gr, 256, 0, st_>>>(V, N_, d_base_, rs, d_row0_, Xi_);
+            spmm_implicit(prec);
+            imp_warm_ = true;
         }
         cudaGraph_t g;
         PYCI_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
@@ -1047,8 +1096,9 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             spmm_tiles(prec);
         } else {
             for (int c = 0; c < kClasses; ++c)
-                spmm_class(prec, cls_lanes_[c], cls_[c]);
+                spmm_class(prec, cls_lanes_[c], cls_for(prec, c));
         }
+        graph_imp_launches_ = spmm_implicit(prec);
         batch_unpack_kernel<T, 4><<<gr, 256, 0, st_>>>(Yi_, N_, d_base_, rs, d_row0_, W, Wnew_);
         cudaError_t e = cudaStreamEndCapture(st_, &g);
         if (e != cudaSuccess)
@@ -1059,9 +1109,10 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
             return cuda_status(e, "graph instantiate");
         graph_prec_ = prec;
         graph_v_ = V;
+        graph_members_ = act_.members;
     }
-    if (tiles_dirty_ && tile_nnz_) {
-        int rc = build_tiles(tile_nnz_); // active set changed: the graph reads the new list
+    if ((tiles_dirty_ || tiles_prec_ != prec) && tile_nnz_) {
+        int rc = build_tiles(tile_nnz_, prec); // active set changed: the graph reads the new list
         if (rc)
             return rc;
     }
@@ -1070,7 +1121,7 @@ int Batch<T>::apply_block(int prec, T *V, T *W) {
     cudaEventCreate(&c);
     cudaEventRecord(a, st_);
     PYCI_CUDA_TRY(cudaGraphLaunch(graph_exec_, st_));
-    for (int i = 0; i < (tile_nnz_ ? 3 : 2 + kClasses); ++i) // pack, the product(s), unpack
+    for (int i = 0; i < (tile_nnz_ ? 3 : 2 + kClasses) + graph_imp_launches_; ++i) // pack, the products, unpack
         ::pyci_gpu::note_launch();
     cudaEventRecord(c, st_);
     PYCI_CUDA_TRY(cudaEventSynchronize(c));
@@ -1200,7 +1251,8 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         (rc = alloc(&d_coef_, static_cast<int64_t>(P) * mmax * std::max(mmax, kSegMaxQ))) ||
         (rc = alloc(&d_theta_, static_cast<int64_t>(P) * nt)) || (rc = alloc(&d_diag_, N)) || (rc = alloc(&d_ops_, P)) ||
         (rc = alloc_rowset(act_)) || (rc = alloc_rowset(sel_)) || (rc = alloc_rowset(cls_[0])) ||
-        (rc = alloc_rowset(cls_[1])) || (rc = alloc_rowset(cls_[2])))
+        (rc = alloc_rowset(cls_[1])) || (rc = alloc_rowset(cls_[2])) || (rc = alloc_rowset(cls32_[0])) ||
+        (rc = alloc_rowset(cls32_[1])) || (rc = alloc_rowset(cls32_[2])))
         return rc;
     // Tile capacity: every problem cut at the smallest tile size the tuner
     // tries (2^16 entries) or 8 rows, whichever gives more tiles.
@@ -1233,9 +1285,11 @@ int Batch<T>::run(int64_t maxiter, double tol, const double *ecore, double *eval
         PYCI_CUDA_TRY(cudaMemcpyAsync(d_diag_ + row0_[p], ops_[p]->diag, sizeof(double) * ops_[p]->nrow,
                                       cudaMemcpyDeviceToDevice, st_));
     cls_of_.assign(P, 0);
+    imp_.assign(P, 0);
     for (int p = 0; p < P; ++p) {
         const double avg = ops_[p]->nrow ? static_cast<double>(ops_[p]->nnz) / ops_[p]->nrow : 0.0;
         cls_of_[p] = avg >= 96 ? 2 : (avg >= 24 ? 1 : 0);
+        imp_[p] = mixed_ && has_implicit(ops_[p]) && !pinned_to_csr();
     }
     std::vector<int> active(P, 1);
     if ((rc = set_active(active)))

@@ -119,6 +119,8 @@ inline bool has_implicit(const pyci_gpu_csr *c) { return c->fx_hi || c->dx_v; }
 namespace pyci_gpu {
 // Kernel launches issued by this library (diagnostic counter).
 void note_launch();
+// Whether PYCI_GPU_SPMM pins products to the CSR or SELL-32 kernels (spmv.cu).
+bool pinned_to_csr();
 } // namespace pyci_gpu
 
 // Thread-local error message.
