@@ -475,14 +475,15 @@ def run_ours(args, world, rank, local):
     wfn.add_all_dets()
     csr.free()  # make room: the e2e path builds its own operator
     e2e_times = []
-    for i in range(max(1, min(5, args.steps)) + 1):
+    e2e_warm = max(1, min(3, args.warmup))
+    for i in range(max(1, min(5, args.steps)) + e2e_warm):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         op = pyci.sparse_op(ham, wfn)
         es, cs = op.solve(n=nroot, tol=tol, mode="mixed")
         t1 = time.perf_counter()
         del op
-        if i > 0:  # first is a warm-up
+        if i >= e2e_warm:  # the first W steps are warm-up
             e2e_times.append(t1 - t0)
     e2e_spr = max_over_ranks(statistics.median(e2e_times), world) / (nroot * world)
     h2d = one.nbytes + two.nbytes

@@ -1913,7 +1913,7 @@ int fcix_fill(pyci_gpu_ctx *ctx, pyci_gpu_csr *csr, const BuildParams &p, const 
     F.adesc = adesc;
     F.spa = csr->fx_nbp / 32;
     F.npk = csr->fx_npk;
-    F.parts = static_cast<int>((F.spa + 15) / 16);
+    F.parts = static_cast<int>((F.spa + 7) / 8); // blocks of <= 8 warps: more of them resident (registers)
     F.aw = fx_atab_width(csr);
     F.ns = csr->fx_ns;
     F.nd = csr->fx_nd;

@@ -146,6 +146,8 @@ int pyci_gpu_ctx_destroy(pyci_gpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     delete ctx->ring;
+    if (ctx->mapped_host)
+        cudaFreeHost(ctx->mapped_host);
     cudaStreamDestroy(ctx->stream);
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess)

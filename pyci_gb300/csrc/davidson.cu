@@ -31,6 +31,7 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -137,7 +138,8 @@ __device__ __forceinline__ void store_rows(T *__restrict__ p, const T (&v)[R]) {
 // multiple of R, vectors 16-byte aligned), R times the bytes in flight per
 // load instruction of the one-row form.
 template<typename T, int PI, int QC, int R>
-__global__ void __launch_bounds__(256) gram_rows_kernel(const T *__restrict__ A, int p, const T *__restrict__ B,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) gram_rows_kernel(const T *__restrict__ A, int p,
+                                                                            const T *__restrict__ B,
                                                         int q, int64_t N, double *__restrict__ partial) {
     const int i0 = blockIdx.x * PI;
     const int ni = min(PI, p - i0);
@@ -444,7 +446,8 @@ struct CoefBlock {
 // vectors); R = 1 otherwise.  Y is read from the parameter bank with
 // warp-uniform indices (broadcast).
 template<typename TV, typename TO, typename ACC, int R>
-__global__ void __launch_bounds__(256) combine_kernel(const TV *__restrict__ V, int p, int64_t N,
+__global__ void __launch_bounds__(256, sizeof(TV) == 4 ? 4 : 2) combine_kernel(const TV *__restrict__ V, int p,
+                                                                              int64_t N,
                                                       const __grid_constant__ CoefBlock<ACC> Y, int q,
                                                       double beta, TO *__restrict__ out) {
     const ACC *sy = Y.y;
@@ -762,7 +765,9 @@ public:
             cudaEventDestroy(pr.second);
         }
         cudaStreamSynchronize(st_);
-        if (h_small_)
+        if (holds_ctx_buffer_)
+            csr_->ctx->mapped_busy = false;
+        else if (h_small_)
             cudaFreeHost(h_small_);
     }
 
@@ -773,7 +778,9 @@ private:
     template<typename U>
     int alloc(U **p, int64_t n) {
         void *q = nullptr;
+        const auto t0 = std::chrono::steady_clock::now();
         cudaError_t e = cudaMallocAsync(&q, sizeof(U) * std::max<int64_t>(n, 1), st_);
+        alloc_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         if (e != cudaSuccess)
             return cuda_status(e, "cudaMallocAsync (eigensolver workspace)");
         allocs_.push_back(q);
@@ -1028,6 +1035,8 @@ private:
     const bool trace_ = std::getenv("PYCI_GPU_SOLVE_TRACE") != nullptr;
     double *h_small_ = nullptr;  // pinned [kMaxGramP * kMaxQ]
     double *d_mapped_ = nullptr; // device alias of h_small_ (mapped), or null
+    bool holds_ctx_buffer_ = false; // h_small_ is the context's buffer
+    double alloc_s_ = 0.0, evec_s_ = 0.0; // host time in workspace allocations / the eigenvector copies (trace)
     bool eig(int m, const std::vector<double> &a, std::vector<double> &w, std::vector<double> &z) {
         const auto t0 = std::chrono::steady_clock::now();
         const bool ok = symmetric_eigen(m, a, w, z);
@@ -1271,6 +1280,22 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     const int prec = mixed_ ? PYCI_PREC_FP32 : PYCI_PREC_FP64;
     int rc;
     gram_blocks_ = static_cast<unsigned>(csr_->ctx->num_sms * 4);
+    // The eigenvector buffer is written once, at the end; the first touch of
+    // fresh host memory (page faults, up to ~9 ms for the 20 MB of four
+    // 627,264-row vectors) runs on another host thread while the GPU
+    // iterates.  Joined before the copies, and on every return.
+    std::thread prefault;
+    if (evecs)
+        prefault = std::thread([evecs, bytes = sizeof(double) * static_cast<size_t>(nw) * static_cast<size_t>(N)] {
+            std::memset(evecs, 0, bytes);
+        });
+    struct Join {
+        std::thread &t;
+        ~Join() {
+            if (t.joinable())
+                t.join();
+        }
+    } join_prefault{prefault};
 
 
     T *V, *W, *Xr, *AXr, *R;
@@ -1285,15 +1310,36 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         (rc = alloc(&Yi_, N * kMaxQ)) || (rc = alloc(&Sb_, N * kMaxQ)) || (rc = alloc(&d_partial_, static_cast<int64_t>(gram_blocks_) * kMaxGramP * kMaxQ)) ||
         (rc = alloc(&d_small_, kMaxGramP * kMaxQ)))
         return rc;
-    PYCI_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(&h_small_), sizeof(double) * kMaxGramP * kMaxQ,
-                                cudaHostAllocMapped));
     {
-        int can_map = 0;
-        cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, csr_->ctx->device);
-        void *dp = nullptr;
-        if (can_map && cudaHostGetDevicePointer(&dp, h_small_, 0) == cudaSuccess)
-            d_mapped_ = static_cast<double *>(dp);
-        cudaGetLastError();
+        // The context's mapped buffer when no other solve holds it, else one
+        // of this solve's own.
+        pyci_gpu_ctx *ctx = csr_->ctx;
+        bool expected = false;
+        const bool shared = ctx->mapped_busy.compare_exchange_strong(expected, true);
+        double **host = shared ? &ctx->mapped_host : &h_small_;
+        if (!*host) {
+            const cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(host), sizeof(double) * kMaxGramP * kMaxQ,
+                                                cudaHostAllocMapped);
+            if (e != cudaSuccess) {
+                if (shared)
+                    ctx->mapped_busy = false;
+                return cuda_status(e, "cudaHostAlloc (eigensolver read-back)");
+            }
+            int can_map = 0;
+            cudaDeviceGetAttribute(&can_map, cudaDevAttrCanMapHostMemory, ctx->device);
+            void *dp = nullptr;
+            if (shared)
+                ctx->mapped_dev = (can_map && cudaHostGetDevicePointer(&dp, *host, 0) == cudaSuccess)
+                                      ? static_cast<double *>(dp) : nullptr;
+            else if (can_map && cudaHostGetDevicePointer(&dp, *host, 0) == cudaSuccess)
+                d_mapped_ = static_cast<double *>(dp);
+            cudaGetLastError();
+        }
+        if (shared) {
+            h_small_ = ctx->mapped_host;
+            d_mapped_ = ctx->mapped_dev;
+            holds_ctx_buffer_ = true;
+        }
     }
     double *d_diag = csr_->diag;
 
@@ -1609,7 +1655,9 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         return PYCI_GPU_ENOCONV;
     }
     // Results: decreasing order (Spectra's result order).
-    std::vector<double> h(static_cast<size_t>(N));
+    const auto t_evec = std::chrono::steady_clock::now();
+    if (prefault.joinable())
+        prefault.join();
     for (int c = 0; c < nw; ++c) {
         const int src = nw - 1 - c;
         evals[c] = final_theta[src] + ecore;
@@ -1624,6 +1672,7 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         }
     }
     PYCI_CUDA_TRY(wait());
+    evec_s_ = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_evec).count();
     if (stats) {
         stats->iterations = iter + 1;
         stats->matvecs = matvecs_;
@@ -1639,10 +1688,11 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     // PYCI_GPU_SOLVE_TRACE: one line per solve on stderr with the host-side
     // breakdown (blocked in read-backs, Rayleigh-Ritz).
     if (trace_)
-        std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), eig %.3f ms, iters %lld\n",
+        std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), eig %.3f ms, "
+                             "allocations %.3f ms, eigenvectors out %.3f ms, iters %lld\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() * 1e3,
-                     timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), eig_s_ * 1e3,
-                     static_cast<long long>(iter + 1));
+                     timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), eig_s_ * 1e3, alloc_s_ * 1e3,
+                     evec_s_ * 1e3, static_cast<long long>(iter + 1));
     return PYCI_GPU_OK;
 }
 

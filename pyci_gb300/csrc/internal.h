@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -20,6 +21,13 @@ struct pyci_gpu_ctx {
     size_t smem_optin = 0;
     cudaStream_t stream = nullptr;
     PinnedRing *ring = nullptr; // pinned staging for small uploads (created with the context)
+    // Mapped pinned buffer of the eigensolver's Gram read-backs, pinned once
+    // per context rather than once per solve (pinning host memory takes
+    // milliseconds, at varying cost); one solve at a time holds it, others
+    // pin their own.  Freed with the context.
+    double *mapped_host = nullptr;
+    double *mapped_dev = nullptr; // its device alias, or null
+    std::atomic<bool> mapped_busy{false};
 };
 
 // Device-resident CSR of the CI Hamiltonian.
