@@ -33,8 +33,8 @@
 // a' * nbeta + b for 32 consecutive b) are coalesced global loads.  Each warp
 // keeps its lanes' section-B partner lists in shared memory.
 //
-// The build writes the values in this layout in the same pass as the CSR
-// (build.cu, fill_fci_tables_kernel).
+// The build writes the values in this layout without the CSR (build.cu,
+// fcix_fill_kernel); the CSR follows on first use.
 //
 // Tables (L1/L2-resident): atab[a] = the targets of a's singles and doubles
 // (sorted), their groups' offsets in the sorted CSR row and that of a's own

@@ -86,9 +86,9 @@ struct pyci_gpu_csr {
     // each alpha single with sorted {b} + beta singles (one group per
     // single), C = each alpha double with b; A, C and each group of B padded
     // to a multiple of 4 entries.  Tables and values (FP32 high and low
-    // parts, in 4-entry packets) are written by the sorted FullCI build, in
-    // the same pass as the CSR.  Null when the operator is not a full FullCI
-    // space.
+    // parts, in 4-entry packets) are written by the sorted FullCI build
+    // (fcix_fill_kernel), the CSR on first use.  Null when the operator is
+    // not a full FullCI space.
     int64_t fx_nalpha = 0, fx_nbeta = 0, fx_nbp = 0; // strings per spin; beta count padded to 32
     int64_t fx_npk = 0;           // 4-entry packets per row (padded length / 4)
     int fx_ns = 0, fx_nd = 0;     // alpha singles / doubles per alpha string

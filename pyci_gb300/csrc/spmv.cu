@@ -448,7 +448,7 @@ void launch_one(const pyci_gpu_csr *csr, Values<VK> vals, const void *x, int64_t
 // the FP32 values of an operator that has one, the SELL-32 copy.
 constexpr int kVariants = 6;
 constexpr int kSellVariant = 0x100; // FP32: + 0 (4 warps per slice) or + 1 (one warp)
-constexpr int kFxVariant = 0x200;   // implicit-column form of a full FullCI space (fcix.cu)
+constexpr int kFxVariant = 0x200;   // implicit form of a full FullCI (fcix.cu) or DOCI (docx.cu) space
 
 // The implicit-column form serves the FP32 products (mode 0) and the
 // double-float ones (csr_spmm_df); FP64 arithmetic stays on the CSR, whose
@@ -564,7 +564,7 @@ bool pinned_to_csr() {
 
 // PYCI_GPU_SPMM=fcix, =sell, =sell1 or =csr pins the products of an operator
 // (read when it makes its first product of a kind, so a process can compare
-// them): the implicit-column form (FP32 and double-float; full FullCI
+// them): the implicit form (FP32 and double-float; full FullCI and DOCI
 // spaces), the SELL-32 copy (FP32 and double-float; FP32 with 4 warps or one
 // warp per slice) or the CSR heuristic (all precisions).
 int forced_sell_variant(const pyci_gpu_csr *csr) {
@@ -937,7 +937,7 @@ using namespace pyci_gpu;
 // entry mapping, as the other products) is tuned on first use.
 int csr_spmm_df(const pyci_gpu_csr *csr, int K, const float *xs, double *y, cudaStream_t st) {
     if ((!csr->hi || !csr->lo) && has_implicit(csr)) {
-        // Implicit-column form only (a full FullCI space).
+        // Implicit form only (a full FullCI or DOCI space).
         if ((K == 1 || K == 2 || K == 4) && !pinned_to_csr() && implicit_launch(csr, 2, K, xs, 2 * K, y, K, st)) {
             csr->tuned[kSplitDF][K] = kFxVariant;
             PYCI_CUDA_TRY(cudaGetLastError());
@@ -1098,9 +1098,9 @@ int csr_spmm(const pyci_gpu_csr *csr, int precision, int64_t k, const void *x, v
         break;
     case PYCI_PREC_FP32:
         if (!csr->hi && has_implicit(csr)) {
-            // Only the implicit-column form holds FP32 values (a full FullCI
-            // space): up to 8 vectors in one launch; the CSR-order split is
-            // made on demand for anything else.
+            // Only the implicit form serves FP32 products (a full FullCI or
+            // DOCI space): up to 8 vectors in one launch; the CSR-order split
+            // is made on demand for anything else.
             if (k <= 8 && !pinned_to_csr() && implicit_launch(csr, 0, static_cast<int>(k), x, k, y, k, stream)) {
                 csr->tuned[kF32][k] = kFxVariant;
                 break;
