@@ -15,8 +15,9 @@ from pyci_gb300.synth import synthetic_integrals
 
 pytestmark = pytest.mark.gpu
 
-# (nbasis, pairs): 70, 252, 220 and 1820 rows; 7 rows; 1 pair.
-CASES = [(8, 4), (10, 5), (12, 3), (16, 4), (7, 6), (9, 1)]
+# (nbasis, pairs): 70, 252, 220 and 1820 rows; 7 rows; 1 pair; more than 32
+# orbitals (64-bit occupation masks): 7140 and 528 rows.
+CASES = [(8, 4), (10, 5), (12, 3), (16, 4), (7, 6), (9, 1), (36, 3), (33, 2)]
 
 
 @pytest.fixture(scope="module")
