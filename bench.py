@@ -222,13 +222,21 @@ def load_oracle():
 def workload_config(ndet, stored, size, world):
     r"""The `config` object of both arms: the workload, its sizes (stored =
     both triangles, as the GPU keeps them; reference = the reference's lower
-    layout), roots, tolerance, L2 note and parallelism."""
-    bytes32 = stored * (4 + 4) + (ndet + 1) * 8 + 2 * ndet * WORKLOAD["nroot"] * 4
+    layout), roots, tolerance, L2 note and parallelism.  The L2 note names
+    what a step streams: the FP32 values of the implicit-column FullCI form
+    (none per entry for the implicit DOCI form) and the eigensolver's FP32
+    subspace (V and H V, 16 vectors per root)."""
+    values = 0 if WORKLOAD["wfn"] == "doci" else stored * 4
+    subspace = 2 * 16 * WORKLOAD["nroot"] * ndet * 4
+    streamed = ("no per-entry bytes (implicit DOCI form)" if values == 0
+                else "%.2f GB of FP32 values per product" % (values / 1e9))
+    big = max(values, subspace) > 2**28
+    l2 = "%s; subspace %.2f GB; %s" % (streamed, subspace / 1e9,
+                                       "> 129 MB L2, no flush needed" if big
+                                       else "fits in the 129 MB L2: figures are L2-resident")
     return {"workload": WORKLOAD["workload"], "ndet": int(ndet), "nnz_stored": int(stored),
             "nnz_reference": int(size), "roots": WORKLOAD["nroot"], "tol": WORKLOAD.get("tol", TOL),
-            "l2": ("matrix (%.1f GB) >> 129 MB L2; no flush needed" % (bytes32 / 1e9)) if bytes32 > 2**28
-            else "matrix (%.0f MB) fits in the 129 MB L2: SpMV figures are L2-resident" % (bytes32 / 1e6),
-            "parallelism": "replicas" if world > 1 else "single GPU"}
+            "l2": l2, "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def cpu_problem(O):

@@ -575,6 +575,276 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
     }
 }
 
+// Fused Ritz step of the FP32 solve: one pass over the rows of V and W (m
+// vectors each) for the Q Ritz pairs with coefficients Y (m x Q, row-major)
+// and values theta:
+//   X_j = sum_i Y[i][j] V_i, AX_j = sum_i Y[i][j] W_i   (combine_kernel's sums)
+//   R_j = AX_j - theta_j X_j                            (residual_kernel's FMAs)
+//   T_j = R_j / (theta_j - D), |.| floored at 1e-8      (precondition_kernel's quotient)
+// T_j goes to T + j N.  Per block it writes the partial sums
+//   partial[b][i Q + j]    = sum_r A_i[r] T_j[r],  A = [V_0 .. V_{m-1}, T_0 .. T_{Q-1}]
+//   partial[b][MA Q + j]   = sum_r R_j[r]^2        (MA = m + Q <= kRitzMaxA)
+// i.e. the residual norms and the first Gram product [V T]^T T of the block
+// orthonormalisation, without a second read of V from memory: each 256-row
+// tile's V and T rows are staged in shared memory (MA x 1 KB) and the Gram
+// sums taken there, warp w owning the A rows w, w + 8, ..., lane l the tile
+// rows l, l + 32, ...  Sums as in gram_rows_kernel: FP32 per thread and warp,
+// FP64 across warps and blocks.
+constexpr int kRitzTile = 256;
+constexpr int kRitzRowsPerWarp = 9;
+constexpr int kRitzMaxA = (kRitzTile / 32) * kRitzRowsPerWarp;
+
+// Gram sums of one staged tile: acc[ii][j] += sum over the lane's tile rows
+// of A_i T_j, A_i = As[i][.] (i = warp + 8 ii < MA), T_j = As[m + j][.].
+template<int Q>
+__device__ __forceinline__ void tile_gram(const float *As, int m, int MA, int warp, int lane,
+                                          float (&acc)[kRitzRowsPerWarp][Q]) {
+#pragma unroll 2
+    for (int s = 0; s < kRitzTile / 32; ++s) {
+        const int c = lane + 32 * s;
+        float tq[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j)
+            tq[j] = As[(m + j) * kRitzTile + c];
+#pragma unroll
+        for (int ii = 0; ii < kRitzRowsPerWarp; ++ii) {
+            const int i = warp + 8 * ii;
+            if (i < MA) {
+                const float a = As[i * kRitzTile + c];
+#pragma unroll
+                for (int j = 0; j < Q; ++j)
+                    acc[ii][j] += a * tq[j];
+            }
+        }
+    }
+}
+
+// Warp sums of the Gram entries (each (i, j) belongs to one warp) to
+// out[i Q + j].
+template<int Q>
+__device__ __forceinline__ void write_gram(const float (&acc)[kRitzRowsPerWarp][Q], int MA, int warp, int lane,
+                                           double *out) {
+#pragma unroll
+    for (int ii = 0; ii < kRitzRowsPerWarp; ++ii) {
+        const int i = warp + 8 * ii;
+        if (i < MA) {
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                float v = acc[ii][j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                if (lane == 0)
+                    out[i * Q + j] = static_cast<double>(v);
+            }
+        }
+    }
+}
+
+template<int Q>
+__global__ void __launch_bounds__(kRitzTile, 2) ritz_fused_kernel(const float *__restrict__ V,
+                                                                  const float *__restrict__ W, int m, int64_t N,
+                                                                  const __grid_constant__ CoefBlock<float> Y,
+                                                                  const __grid_constant__ Theta th,
+                                                                  const double *__restrict__ diag,
+                                                                  float *__restrict__ T, double *__restrict__ partial) {
+    extern __shared__ float As[]; // [MA][kRitzTile]
+    const int MA = m + Q;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float th_hi[Q], th_lo[Q], nrm[Q], acc[kRitzRowsPerWarp][Q];
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        th_hi[j] = static_cast<float>(th.t[j]);
+        th_lo[j] = static_cast<float>(th.t[j] - static_cast<double>(th_hi[j]));
+        nrm[j] = 0.0f;
+#pragma unroll
+        for (int ii = 0; ii < kRitzRowsPerWarp; ++ii)
+            acc[ii][j] = 0.0f;
+    }
+    for (int64_t base = static_cast<int64_t>(blockIdx.x) * kRitzTile; base < N;
+         base += static_cast<int64_t>(gridDim.x) * kRitzTile) {
+        const int64_t r = base + tid;
+        const bool ok = r < N;
+        float x[Q], ax[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j)
+            x[j] = ax[j] = 0.0f;
+#pragma unroll 8
+        for (int i = 0; i < m; ++i) {
+            const float v = ok ? V[i * N + r] : 0.0f;
+            const float w = ok ? W[i * N + r] : 0.0f;
+            As[i * kRitzTile + tid] = v;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) {
+                const float y = Y.y[i * Q + j];
+                x[j] += y * v;
+                ax[j] += y * w;
+            }
+        }
+        const float df = ok ? static_cast<float>(diag[r]) : 0.0f;
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            const float res = fmaf(-th_lo[j], x[j], fmaf(-th_hi[j], x[j], ax[j]));
+            nrm[j] += res * res;
+            float den = th_hi[j] - df;
+            if (fabsf(den) < 1e-8f)
+                den = (den < 0.0f) ? -1e-8f : 1e-8f;
+            const float t = res * __frcp_rn(den);
+            As[(m + j) * kRitzTile + tid] = ok ? t : 0.0f;
+            if (ok)
+                T[j * N + r] = t;
+        }
+        __syncthreads();
+        tile_gram<Q>(As, m, MA, warp, lane, acc);
+        __syncthreads();
+    }
+    const int64_t pq = static_cast<int64_t>(MA) * Q + Q;
+    double *out = partial + static_cast<int64_t>(blockIdx.x) * pq;
+    write_gram<Q>(acc, MA, warp, lane, out);
+    // Residual norms: warp sums in FP32, then the 8 warps in FP64 (the
+    // staging array is free after the last tile's barrier).
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        float v = nrm[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0)
+            As[warp * Q + j] = v;
+    }
+    __syncthreads();
+    if (tid < Q) {
+        double s = 0.0;
+        for (int w = 0; w < kRitzTile / 32; ++w)
+            s += static_cast<double>(As[w * Q + tid]);
+        out[static_cast<int64_t>(MA) * Q + tid] = s;
+    }
+}
+
+// First Gram-Schmidt pass of a block orthonormalisation fused with the
+// Gram product of the second: for c < Q
+//   T1_c = sum_{i < m} Y[i][c] V_i + sum_{a < b} Y[m + a][c] Tsrc_a
+// (combine2_kernel's sums) to out + c N, and per block
+//   partial[b][i Q + c] = sum_r A_i[r] T1_c[r],  A = [V_0 .. V_{m-1}, T1_0 .. T1_{Q-1}]
+// with the tile staging of ritz_fused_kernel (V read once).
+template<int Q>
+__global__ void __launch_bounds__(kRitzTile, 2) project_gram_kernel(const float *__restrict__ V, int m,
+                                                                    const float *__restrict__ Tsrc, int b, int64_t N,
+                                                                    const __grid_constant__ CoefBlock<float> Y,
+                                                                    float *__restrict__ out,
+                                                                    double *__restrict__ partial) {
+    extern __shared__ float As[]; // [MA][kRitzTile]
+    const int MA = m + Q;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float acc[kRitzRowsPerWarp][Q];
+#pragma unroll
+    for (int ii = 0; ii < kRitzRowsPerWarp; ++ii)
+#pragma unroll
+        for (int j = 0; j < Q; ++j)
+            acc[ii][j] = 0.0f;
+    for (int64_t base = static_cast<int64_t>(blockIdx.x) * kRitzTile; base < N;
+         base += static_cast<int64_t>(gridDim.x) * kRitzTile) {
+        const int64_t r = base + tid;
+        const bool ok = r < N;
+        float t1[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j)
+            t1[j] = 0.0f;
+#pragma unroll 8
+        for (int i = 0; i < m; ++i) {
+            const float v = ok ? V[i * N + r] : 0.0f;
+            As[i * kRitzTile + tid] = v;
+#pragma unroll
+            for (int j = 0; j < Q; ++j)
+                t1[j] += Y.y[i * Q + j] * v;
+        }
+        for (int a = 0; a < b; ++a) {
+            const float v = ok ? Tsrc[a * N + r] : 0.0f;
+#pragma unroll
+            for (int j = 0; j < Q; ++j)
+                t1[j] += Y.y[(m + a) * Q + j] * v;
+        }
+#pragma unroll
+        for (int j = 0; j < Q; ++j) {
+            As[(m + j) * kRitzTile + tid] = t1[j];
+            if (ok)
+                out[j * N + r] = t1[j];
+        }
+        __syncthreads();
+        tile_gram<Q>(As, m, MA, warp, lane, acc);
+        __syncthreads();
+    }
+    write_gram<Q>(acc, MA, warp, lane, partial + static_cast<int64_t>(blockIdx.x) * MA * Q);
+}
+
+// out[j][r] = sum_{i < p1} Y[i][j] V1[i][r] + sum_{i < p2} Y[p1 + i][j] V2[i][r]
+// for j < q (FP32, i ascending: combine_kernel's sums over the two vector
+// sets as one); when xi is given, the same values also go to xi[r kp + j]
+// (zero for q <= j < kp), the packed operand of the next product
+// (pack_kernel's layout).  out must not overlap V1 or V2.  R = 4: four
+// consecutive rows per thread step with 16-byte loads and stores (N a
+// multiple of 4, 16-byte aligned vectors); R = 1 otherwise.
+template<int R>
+__global__ void __launch_bounds__(256, 2) combine2_kernel(const float *__restrict__ V1, int p1,
+                                                          const float *__restrict__ V2, int p2, int64_t N,
+                                                          const __grid_constant__ CoefBlock<float> Y, int q,
+                                                          float *__restrict__ out, float *__restrict__ xi, int kp) {
+    const int p = p1 + p2;
+    const int64_t nu = N / R;
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < nu;
+         u += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int64_t r = u * R;
+        float acc[kMaxQ][R];
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+#pragma unroll
+            for (int t = 0; t < R; ++t)
+                acc[j][t] = 0.0f;
+#pragma unroll 8
+        for (int i = 0; i < p; ++i) {
+            const float *src = (i < p1) ? V1 + i * N : V2 + (i - p1) * N;
+            float v[R];
+            load_rows<float, R>(src + r, v);
+#pragma unroll
+            for (int j = 0; j < kMaxQ; ++j)
+                if (j < q) {
+                    const float y = Y.y[i * q + j];
+#pragma unroll
+                    for (int t = 0; t < R; ++t)
+                        acc[j][t] += y * v[t];
+                }
+        }
+#pragma unroll
+        for (int j = 0; j < kMaxQ; ++j)
+            if (j < q) {
+                float w[R];
+#pragma unroll
+                for (int t = 0; t < R; ++t)
+                    w[t] = acc[j][t];
+                store_rows<float, R>(out + j * N + r, w);
+            }
+        if (xi) {
+#pragma unroll
+            for (int t = 0; t < R; ++t) {
+                float *row = xi + (r + t) * kp;
+                if (kp % 4 == 0) {
+#pragma unroll
+                    for (int j4 = 0; j4 < kMaxQ; j4 += 4)
+                        if (j4 < kp)
+                            *reinterpret_cast<float4 *>(row + j4) =
+                                make_float4(j4 < q ? acc[j4][t] : 0.0f, j4 + 1 < q ? acc[j4 + 1][t] : 0.0f,
+                                            j4 + 2 < q ? acc[j4 + 2][t] : 0.0f, j4 + 3 < q ? acc[j4 + 3][t] : 0.0f);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < kMaxQ; ++j)
+                        if (j < kp)
+                            row[j] = j < q ? acc[j][t] : 0.0f;
+                }
+            }
+        }
+    }
+}
+
 // L^{-1} (row-major, lower) for the Cholesky factor S = L L^T of a k x k
 // symmetric matrix (row-major); false when a pivot is not above tol times its
 // diagonal entry (S not safely positive definite).
@@ -755,6 +1025,8 @@ public:
         // Gram products and combinations (double-float by default).
         const char *l = std::getenv("PYCI_GPU_FP64_LINALG");
         df_linalg_ = !(l && !std::strcmp(l, "native"));
+        const char *f = std::getenv("PYCI_GPU_RITZ");
+        ritz_fused_ = !(f && !std::strcmp(f, "separate"));
     }
 
     ~Davidson() {
@@ -909,6 +1181,140 @@ private:
         return PYCI_GPU_OK;
     }
 
+    // Staged-tile kernels (ritz_fused_kernel, project_gram_kernel): the
+    // shared-memory limit for the widest tile, set once.
+    static void staged_attributes() {
+        static const bool done = [] {
+            const int most = static_cast<int>(sizeof(float) * kRitzTile * kRitzMaxA);
+            for (auto k : {ritz_fused_kernel<1>, ritz_fused_kernel<2>, ritz_fused_kernel<3>, ritz_fused_kernel<4>,
+                           ritz_fused_kernel<5>, ritz_fused_kernel<6>, ritz_fused_kernel<7>, ritz_fused_kernel<8>})
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            for (auto k : {project_gram_kernel<1>, project_gram_kernel<2>, project_gram_kernel<3>,
+                           project_gram_kernel<4>, project_gram_kernel<5>, project_gram_kernel<6>,
+                           project_gram_kernel<7>, project_gram_kernel<8>})
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            return true;
+        }();
+        (void)done;
+    }
+
+    // Blocks for a staged-tile kernel with MA staged rows: the resident
+    // blocks of one wave, at most gram_blocks_ (the partial sums' rows).
+    unsigned staged_grid(const void *fn, int MA) const {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRitzTile, sizeof(float) * kRitzTile * MA) !=
+            cudaSuccess)
+            per_sm = 1;
+        per_sm = std::max(1, per_sm);
+        return static_cast<unsigned>(std::max<int64_t>(
+            1, std::min<int64_t>({static_cast<int64_t>(gram_blocks_), static_cast<int64_t>(per_sm) * csr_->ctx->num_sms,
+                                  (N_ + kRitzTile - 1) / kRitzTile})));
+    }
+
+    // Sums the nb blocks' pq partial sums and reads them back (one host
+    // synchronisation).
+    int read_partials(unsigned nb, int pq, std::vector<double> &h, const char *what) {
+        reduce_partials_kernel<<<pq, 256, 0, st_>>>(d_partial_, nb, pq, d_mapped_ ? d_mapped_ : d_small_),
+            ::pyci_gpu::note_launch();
+        const auto t0 = std::chrono::steady_clock::now();
+        cudaError_t e = cudaSuccess;
+        if (!d_mapped_)
+            e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pq, cudaMemcpyDeviceToHost, st_);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st_);
+        wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        ++syncs_;
+        if (e != cudaSuccess)
+            return cuda_status(e, what);
+        h.assign(h_small_, h_small_ + pq);
+        return PYCI_GPU_OK;
+    }
+
+    // Fused Ritz step (ritz_fused_kernel, FP32 vectors): Tb[0..q) = the
+    // preconditioned residuals of the q Ritz pairs with coefficients Yb
+    // (m x q) and values theta; P = [V Tb]^T Tb ((m + q) x q, row-major);
+    // rn2 = squared residual norms.  One host synchronisation.
+    int ritz_fused(const float *V, const float *W, int m, const std::vector<double> &Yb, int q,
+                   const std::vector<double> &theta, const double *diag, float *Tb, std::vector<double> &P,
+                   std::vector<double> &rn2) {
+        staged_attributes();
+        CoefBlock<float> y;
+        for (int i = 0; i < m; ++i)
+            for (int j = 0; j < q; ++j)
+                y.y[i * q + j] = static_cast<float>(Yb[static_cast<size_t>(i) * q + j]);
+        Theta th{};
+        for (int j = 0; j < q; ++j)
+            th.t[j] = theta[j];
+        const int MA = m + q;
+        const size_t smem = sizeof(float) * kRitzTile * MA;
+        unsigned nb = 0;
+        auto launch = [&](auto kernel) {
+            nb = staged_grid(reinterpret_cast<const void *>(kernel), MA);
+            kernel<<<nb, kRitzTile, smem, st_>>>(V, W, m, N_, y, th, diag, Tb, d_partial_);
+            ::pyci_gpu::note_launch();
+        };
+        switch (q) {
+        case 1: launch(ritz_fused_kernel<1>); break;
+        case 2: launch(ritz_fused_kernel<2>); break;
+        case 3: launch(ritz_fused_kernel<3>); break;
+        case 4: launch(ritz_fused_kernel<4>); break;
+        case 5: launch(ritz_fused_kernel<5>); break;
+        case 6: launch(ritz_fused_kernel<6>); break;
+        case 7: launch(ritz_fused_kernel<7>); break;
+        default: launch(ritz_fused_kernel<8>); break;
+        }
+        std::vector<double> h;
+        const int pq = MA * q + q;
+        int rc = read_partials(nb, pq, h, "fused Ritz step");
+        if (rc)
+            return rc;
+        P.assign(h.begin(), h.begin() + static_cast<size_t>(MA) * q);
+        rn2.assign(h.begin() + static_cast<size_t>(MA) * q, h.end());
+        return PYCI_GPU_OK;
+    }
+
+    // T1 = [V Tsrc] Y (project_gram_kernel; V: m vectors, Tsrc: b, Y
+    // (m + b) x k row-major, k <= kMaxQ) into out; P = [V T1]^T T1
+    // ((m + k) x k).  One host synchronisation.
+    int project_gram(const float *V, int m, const float *Tsrc, int b, const CoefBlock<float> &y, int k, float *out,
+                     std::vector<double> &P) {
+        staged_attributes();
+        const int MA = m + k;
+        const size_t smem = sizeof(float) * kRitzTile * MA;
+        unsigned nb = 0;
+        auto launch = [&](auto kernel) {
+            nb = staged_grid(reinterpret_cast<const void *>(kernel), MA);
+            kernel<<<nb, kRitzTile, smem, st_>>>(V, m, Tsrc, b, N_, y, out, d_partial_);
+            ::pyci_gpu::note_launch();
+        };
+        switch (k) {
+        case 1: launch(project_gram_kernel<1>); break;
+        case 2: launch(project_gram_kernel<2>); break;
+        case 3: launch(project_gram_kernel<3>); break;
+        case 4: launch(project_gram_kernel<4>); break;
+        case 5: launch(project_gram_kernel<5>); break;
+        case 6: launch(project_gram_kernel<6>); break;
+        case 7: launch(project_gram_kernel<7>); break;
+        default: launch(project_gram_kernel<8>); break;
+        }
+        return read_partials(nb, MA * k, P, "orthonormalisation pass");
+    }
+
+    // The fused Ritz step applies (FP32 solve, no full-space Rayleigh-Ritz,
+    // at most kMaxQ pairs and kRitzMaxA rows of [V T]); PYCI_GPU_RITZ=separate
+    // keeps the separate combinations, residual, norms, preconditioner and
+    // Gram product.
+    bool ritz_fused_on(int m, int q) const {
+        return std::is_same<T, float>::value && mixed_ && ritz_fused_ && q >= 1 && q <= kMaxQ && m + q <= kRitzMaxA;
+    }
+
+    // Vectors per product launch: on the SELL-32 copy or the implicit-column
+    // form the FP32 product streams the matrix once per launch and is bound by
+    // that stream, so up to 8 vectors share one launch.
+    int spmm_chunk(int prec) const {
+        return (prec == PYCI_PREC_FP32 && (csr_->sell_cols || has_implicit(csr_))) ? kMaxQ : kSpmmChunk;
+    }
+
     // W[0..k) = H V[0..k) (storage precision of T; FP64 uses f64 values).
     int apply(const T *V, int k, T *W, int prec) {
         // On the SELL-32 copy or the implicit-column form the FP32 product
@@ -916,12 +1322,18 @@ private:
         // up to 8 vectors share one launch (a 5-vector block as one product
         // padded to 8, not 4 + 1).  FP64 solves on an operator that holds the
         // exact high/low split multiply in double-float arithmetic.
-        const int chunk = (prec == PYCI_PREC_FP32 && (csr_->sell_cols || has_implicit(csr_))) ? kMaxQ : kSpmmChunk;
+        const int chunk = spmm_chunk(prec);
+        // The block orthonormalisation may have written the packed operand
+        // already (combine2_kernel).
+        const bool packed = (xi_src_ == V && xi_k_ == k && k <= chunk);
+        xi_src_ = nullptr;
         for (int j0 = 0; j0 < k; j0 += chunk) {
             const int kk = std::min(chunk, k - j0);
             const int kp = padded_width(kk);
             const bool df = std::is_same<T, double>::value && fp64_df_;
-            if (df)
+            if (packed)
+                ;
+            else if (df)
                 pack_split_kernel<<<grid(N_), 256, 0, st_>>>(reinterpret_cast<const double *>(V) + static_cast<int64_t>(j0) * N_,
                                                              N_, kk, kp, reinterpret_cast<float *>(Xi_)),
                     ::pyci_gpu::note_launch();
@@ -995,6 +1407,17 @@ private:
     // Vector-by-vector classical Gram-Schmidt (two passes); drops
     // near-dependent vectors.
     int orthonormalize_mgs(T *V, int m, int k, int &kept);
+    // orthonormalize for the columns todo of Tb (b vectors apart from V)
+    // into V[m..), given C1 = V[0..m)^T Tb (m x b) and TT = Tb^T Tb (b x b)
+    // from the fused Ritz step: one combination when one Gram-Schmidt pass is
+    // enough (orthonormalize's criterion), else the columns are copied to
+    // V[m..) and orthonormalised there.
+    int orthonormalize_pre(T *V, int m, const T *Tb, int b, const std::vector<int> &todo,
+                           const std::vector<double> &C1, const std::vector<double> &TT, int prec, int &kept);
+    // Set when the last block orthonormalisation also wrote the packed
+    // product operand of xi_src_[0..xi_k_) into Xi_.
+    const T *xi_src_ = nullptr;
+    int xi_k_ = 0;
 
     pyci_gpu_csr *csr_;
     cudaStream_t st_;
@@ -1056,6 +1479,8 @@ private:
     // (gram_rows_df_kernel, combine_df_kernel): the FP64 forms are bound by
     // the FP64 pipe, not by the vectors' bytes.
     bool df_linalg_ = true;
+    // Fused Ritz step of the FP32 solve (ritz_fused_kernel).
+    bool ritz_fused_ = true;
     double *d_partial_ = nullptr, *d_small_ = nullptr;
 };
 
@@ -1269,6 +1694,144 @@ int Davidson<T>::orthonormalize_mgs(T *V, int m, int k, int &kept) {
 }
 
 template<typename T>
+int Davidson<T>::orthonormalize_pre(T *V, int m, const T *Tb, int b, const std::vector<int> &todo,
+                                    const std::vector<double> &C1, const std::vector<double> &TT, int prec,
+                                    int &kept) {
+    const int k = static_cast<int>(todo.size());
+    kept = 0;
+    if (k == 0)
+        return PYCI_GPU_OK;
+    T *out = V + static_cast<int64_t>(m) * N_;
+    if constexpr (std::is_same<T, float>::value) {
+        const bool pack = k <= spmm_chunk(prec);
+        const int kp = padded_width(k);
+        // (Q - V C) L^{-T} for the block Q (b vectors, columns cols of it
+        // chosen, k of them) into out (also packed into Xi_ when xi): rows of
+        // V, then the rows of Q.
+        auto finish = [&](const float *Q, int nq, const std::vector<int> &cols, const std::vector<double> &C, int ldc,
+                          const std::vector<double> &Linv, bool xi) {
+            CoefBlock<float> y{};
+            for (int i = 0; i < m; ++i)
+                for (int c = 0; c < k; ++c) {
+                    double x = 0.0;
+                    for (int a = 0; a < k; ++a)
+                        x -= C[static_cast<size_t>(i) * ldc + cols[a]] * Linv[static_cast<size_t>(c) * k + a];
+                    y.y[i * k + c] = static_cast<float>(x);
+                }
+            for (int a = 0; a < k; ++a)
+                for (int c = 0; c < k; ++c)
+                    y.y[(m + cols[a]) * k + c] = static_cast<float>(Linv[static_cast<size_t>(c) * k + a]);
+            float *xp = xi ? reinterpret_cast<float *>(Xi_) : nullptr;
+            if (N_ % 4 == 0)
+                combine2_kernel<4><<<grid(N_ / 4), 256, 0, st_>>>(V, m, Q, nq, N_, y, k, out, xp, kp);
+            else
+                combine2_kernel<1><<<grid(N_), 256, 0, st_>>>(V, m, Q, nq, N_, y, k, out, xp, kp);
+            ::pyci_gpu::note_launch();
+            if (xi) {
+                xi_src_ = out;
+                xi_k_ = k;
+            }
+        };
+        // Cholesky of S with the conditioning estimate (max L_jj / min L_jj)^2.
+        auto chol = [&](const std::vector<double> &S, std::vector<double> &Linv, double &kappa) -> bool {
+            if (!cholesky_inverse(S, k, 1e-6, Linv))
+                return false;
+            double lmax = 0.0, lmin = std::numeric_limits<double>::infinity();
+            for (int j = 0; j < k; ++j) {
+                const double l = 1.0 / Linv[static_cast<size_t>(j) * k + j];
+                lmax = std::max(lmax, l);
+                lmin = std::min(lmin, l);
+            }
+            kappa = (lmax / lmin) * (lmax / lmin);
+            return true;
+        };
+        // S = Tc^T Tc - C^T C for the chosen columns Tc (C = V^T Tc): the Gram
+        // of Tc - V C.  One pass is enough when every column keeps at least
+        // half its squared norm and S is well conditioned (orthonormalize's
+        // criterion).
+        std::vector<double> S(static_cast<size_t>(k) * k);
+        bool keeps = true;
+        for (int a = 0; a < k; ++a)
+            for (int c = 0; c < k; ++c) {
+                const int ta = todo[a], tc = todo[c];
+                double x = TT[static_cast<size_t>(ta) * b + tc];
+                for (int i = 0; i < m; ++i)
+                    x -= C1[static_cast<size_t>(i) * b + ta] * C1[static_cast<size_t>(i) * b + tc];
+                S[static_cast<size_t>(a) * k + c] = x;
+                if (a == c && !(x >= 0.5 * TT[static_cast<size_t>(ta) * b + ta]))
+                    keeps = false;
+            }
+        std::vector<double> Linv;
+        double kappa = 0.0;
+        if (keeps && chol(S, Linv, kappa) && kappa < 10.0) {
+            finish(Tb, b, todo, C1, b, Linv, pack);
+            kept = k;
+            return PYCI_GPU_OK;
+        }
+        // Two passes: T1 = Tc - V C (into Sb_) with the Gram product
+        // [V T1]^T T1 in the same read of V, then (T1 - V C2) L^{-T} from the
+        // Cholesky factor of T1^T T1 - C2^T C2 when T1 is nearly orthogonal
+        // to V (orthonormalize's second pass).
+        {
+            CoefBlock<float> y{};
+            for (int i = 0; i < m; ++i)
+                for (int c = 0; c < k; ++c)
+                    y.y[i * k + c] = static_cast<float>(-C1[static_cast<size_t>(i) * b + todo[c]]);
+            for (int c = 0; c < k; ++c)
+                y.y[(m + todo[c]) * k + c] = 1.0f;
+            std::vector<double> P2;
+            int rc = project_gram(V, m, Tb, b, y, k, Sb_, P2);
+            if (rc)
+                return rc;
+            std::vector<double> Sm(static_cast<size_t>(k) * k);
+            double cmax = 0.0, smin = std::numeric_limits<double>::infinity();
+            for (int i = 0; i < k; ++i)
+                smin = std::min(smin, P2[static_cast<size_t>(m + i) * k + i]);
+            for (size_t e = 0; e < static_cast<size_t>(m) * k; ++e)
+                cmax = std::max(cmax, std::fabs(P2[e]));
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) {
+                    double x = P2[static_cast<size_t>(m + i) * k + j];
+                    for (int t = 0; t < m; ++t)
+                        x -= P2[static_cast<size_t>(t) * k + i] * P2[static_cast<size_t>(t) * k + j];
+                    Sm[static_cast<size_t>(i) * k + j] = x;
+                }
+            std::vector<int> ident(k);
+            std::iota(ident.begin(), ident.end(), 0);
+            if (smin > 0.0 && cmax * cmax <= 1e-4 * smin && chol(Sm, Linv, kappa)) {
+                const bool again = !(kappa < 10.0);
+                finish(Sb_, k, ident, P2, k, Linv, pack && !again);
+                kept = k;
+                if (!again)
+                    return PYCI_GPU_OK;
+                // One Cholesky-QR pass more (orthonormalize's criterion).
+                std::vector<double> G2;
+                if ((rc = gram<T>(out, k, out, k, G2)))
+                    return rc;
+                if (!cholesky_inverse(G2, k, 1e-6, Linv))
+                    return orthonormalize(V, m, k, kept);
+                std::vector<double> Y(static_cast<size_t>(k) * k);
+                for (int i = 0; i < k; ++i)
+                    for (int j = 0; j < k; ++j)
+                        Y[static_cast<size_t>(i) * k + j] = Linv[static_cast<size_t>(j) * k + i];
+                if ((rc = combine<T, T, T>(out, k, Y, k, 0.0, Sb_)))
+                    return rc;
+                PYCI_CUDA_TRY(cudaMemcpyAsync(out, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
+                return PYCI_GPU_OK;
+            }
+            // Far from orthogonal after one pass: the general path on T1.
+            PYCI_CUDA_TRY(cudaMemcpyAsync(out, Sb_, sizeof(T) * k * N_, cudaMemcpyDeviceToDevice, st_));
+            return orthonormalize(V, m, k, kept);
+        }
+    } else {
+        for (int c = 0; c < k; ++c)
+            PYCI_CUDA_TRY(cudaMemcpyAsync(out + static_cast<int64_t>(c) * N_, Tb + static_cast<int64_t>(todo[c]) * N_,
+                                          sizeof(T) * N_, cudaMemcpyDeviceToDevice, st_));
+        return orthonormalize(V, m, k, kept);
+    }
+}
+
+template<typename T>
 int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore, double *evals,
                      double *evecs, pyci_gpu_solve_stats *stats) {
     const auto t_start = std::chrono::steady_clock::now();
@@ -1438,15 +2001,28 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
         for (int i = 0; i < m; ++i)
             for (int j = 0; j < b; ++j)
                 Yb[static_cast<size_t>(i) * b + j] = Y[static_cast<size_t>(i) * m + j];
-        if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
-            return rc;
-        residuals<T>(AXr, Xr, b, theta, R);
+        // Fused (FP32): R holds the preconditioned residuals of all b pairs,
+        // Pf = [V R]^T R; Xr and AXr are formed only where needed.
+        const bool fused = ritz_fused_on(m, b);
+        std::vector<double> Pf, rn2(b);
+        if (fused) {
+            if constexpr (std::is_same<T, float>::value) {
+                if ((rc = ritz_fused(V, W, m, Yb, b, theta, d_diag, R, Pf, rn2)))
+                    return rc;
+            }
+        } else {
+            if ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) || (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr)))
+                return rc;
+            residuals<T>(AXr, Xr, b, theta, R);
+            if ((rc = gram<T>(R, b, R, b, Gc)))
+                return rc;
+            for (int j = 0; j < b; ++j)
+                rn2[j] = Gc[static_cast<size_t>(j) * b + j];
+        }
         bool all = true;
         std::vector<int> todo;
-        if ((rc = gram<T>(R, b, R, b, Gc)))
-            return rc;
         for (int j = 0; j < b; ++j) {
-            rnorm[j] = std::sqrt(std::max(Gc[static_cast<size_t>(j) * b + j], 0.0));
+            rnorm[j] = std::sqrt(std::max(rn2[j], 0.0));
             double thr = tol * std::max(eps23, std::fabs(theta[j]));
             if (mixed_)
                 thr = std::max(thr, mixed_floor);
@@ -1603,6 +2179,9 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             if (m + static_cast<int>(todo.size()) > mmax) {
                 // Collapse onto the b FP32 Ritz vectors of this iteration
                 // (projected matrix diag(theta)).
+                if (fused && ((rc = combine<T, T, T>(V, m, Yb, b, 0.0, Xr)) ||
+                              (rc = combine<T, T, T>(W, m, Yb, b, 0.0, AXr))))
+                    return rc;
                 PYCI_CUDA_TRY(cudaMemcpyAsync(V, Xr, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
                 PYCI_CUDA_TRY(cudaMemcpyAsync(W, AXr, sizeof(T) * b * N, cudaMemcpyDeviceToDevice, st_));
                 std::fill(G.begin(), G.end(), 0.0);
@@ -1637,14 +2216,35 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             std::fill(G.begin(), G.end(), 0.0);
             for (int i = 0; i < nkeep; ++i)
                 G[static_cast<size_t>(i) * mmax + i] = theta[i];
+            if (fused) {
+                // The kept basis is V Yk: its products with R are Yk^T (V^T R).
+                std::vector<double> Pk(static_cast<size_t>(nkeep + b) * b, 0.0);
+                for (int a = 0; a < nkeep; ++a)
+                    for (int j = 0; j < b; ++j) {
+                        double x = 0.0;
+                        for (int i = 0; i < m; ++i)
+                            x += Yk[static_cast<size_t>(i) * nkeep + a] * Pf[static_cast<size_t>(i) * b + j];
+                        Pk[static_cast<size_t>(a) * b + j] = x;
+                    }
+                std::copy(Pf.begin() + static_cast<size_t>(m) * b, Pf.begin() + static_cast<size_t>(m + b) * b,
+                          Pk.begin() + static_cast<size_t>(nkeep) * b);
+                Pf.swap(Pk);
+            }
             m = nkeep;
             ++restarts;
         }
         // Preconditioned residuals of the unconverged roots.
         const int q = static_cast<int>(todo.size());
-        precondition<T>(R, d_diag, todo, theta, V + static_cast<int64_t>(m) * N);
-        if ((rc = orthonormalize(V, m, q, knew)))
-            return rc;
+        if (fused) {
+            const std::vector<double> C1(Pf.begin(), Pf.begin() + static_cast<size_t>(m) * b),
+                TT(Pf.begin() + static_cast<size_t>(m) * b, Pf.begin() + static_cast<size_t>(m + b) * b);
+            if ((rc = orthonormalize_pre(V, m, R, b, todo, C1, TT, prec, knew)))
+                return rc;
+        } else {
+            precondition<T>(R, d_diag, todo, theta, V + static_cast<int64_t>(m) * N);
+            if ((rc = orthonormalize(V, m, q, knew)))
+                return rc;
+        }
         if (knew == 0) {
             set_error("did not converge");
             return PYCI_GPU_ENOCONV;
