@@ -31,7 +31,9 @@
 #include <cstring>
 #include <limits>
 #include <numeric>
+#include <string>
 #include <thread>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -593,27 +595,83 @@ __global__ void precondition_kernel(const TI *__restrict__ R, const double *__re
 constexpr int kRitzTile = 256;
 constexpr int kRitzRowsPerWarp = 9;
 constexpr int kRitzMaxA = (kRitzTile / 32) * kRitzRowsPerWarp;
+// Shared memory of a staged-tile kernel at most (the tiles' rows, 1 KB
+// each; two buffers of them where they fit).
+constexpr int kStagedMaxBytes = 220 * 1024;
+
+// Bulk-copy staging of the tiles (BULK kernels, N a multiple of 4 so that
+// every row range of every vector starts on 16 bytes): one mbarrier per
+// block, armed with the tile's byte count by one lane; the lanes of warp 0
+// issue one cp.async.bulk per vector (up to 1 KB each), so a whole tile is
+// in flight at once.  Waits are bounded: a block that gives up writes NaN
+// partial sums, which the host reports.
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t stage_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void stage_init(uint32_t bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Arms the barrier for `bytes` (after the generic-proxy accesses of the
+// previous tile, which the block barrier before this call has ordered).
+__device__ __forceinline__ void stage_arm(uint32_t bar, uint32_t bytes) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Rows [base, base + bytes / 4) of vectors src_0 .. src_{n-1} (stride N)
+// into dst[i][0 ..), one bulk copy per vector, issued by the 32 lanes.
+__device__ __forceinline__ void stage_rows(float *dst, const float *src, int n, int64_t N, int64_t base,
+                                           uint32_t bytes, uint32_t bar, int lane) {
+    for (int i = lane; i < n; i += 32)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         stage_addr(dst + i * kRitzTile)),
+                     "l"(src + i * N + base), "r"(bytes), "r"(bar)
+                     : "memory");
+}
+
+__device__ __forceinline__ bool stage_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kStageWaitLimit; ++i) {
+        uint32_t ok;
+        asm volatile("{\n\t.reg .pred p;\n\t"
+                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok)
+            return true;
+    }
+    return false;
+}
 
 // Gram sums of one staged tile: acc[ii][j] += sum over the lane's tile rows
-// of A_i T_j, A_i = As[i][.] (i = warp + 8 ii < MA), T_j = As[m + j][.].
-template<int Q>
-__device__ __forceinline__ void tile_gram(const float *As, int m, int MA, int warp, int lane,
-                                          float (&acc)[kRitzRowsPerWarp][Q]) {
-#pragma unroll 2
-    for (int s = 0; s < kRitzTile / 32; ++s) {
-        const int c = lane + 32 * s;
-        float tq[Q];
+// of A_i T_j, A = [Av_0 .. Av_{m-1}, At_0 .. At_{Q-1}] (i = warp + 8 ii < MA),
+// T_j = At_j (rows of kRitzTile floats).  Lane l takes the rows
+// 4 l .. 4 l + 3 and 128 + 4 l .. 128 + 4 l + 3 with 16-byte shared loads.
+template<int Q, int RPW>
+__device__ __forceinline__ void tile_gram(const float *Av, const float *At, int m, int MA, int warp, int lane,
+                                          float (&acc)[RPW][Q]) {
+#pragma unroll
+    for (int h = 0; h < kRitzTile / 128; ++h) {
+        const int c = 4 * lane + 128 * h;
+        float4 tq[Q];
 #pragma unroll
         for (int j = 0; j < Q; ++j)
-            tq[j] = As[(m + j) * kRitzTile + c];
+            tq[j] = *reinterpret_cast<const float4 *>(At + j * kRitzTile + c);
 #pragma unroll
-        for (int ii = 0; ii < kRitzRowsPerWarp; ++ii) {
+        for (int ii = 0; ii < RPW; ++ii) {
             const int i = warp + 8 * ii;
             if (i < MA) {
-                const float a = As[i * kRitzTile + c];
+                const float4 a = *reinterpret_cast<const float4 *>(i < m ? Av + i * kRitzTile + c
+                                                                         : At + (i - m) * kRitzTile + c);
 #pragma unroll
                 for (int j = 0; j < Q; ++j)
-                    acc[ii][j] += a * tq[j];
+                    acc[ii][j] += a.x * tq[j].x + a.y * tq[j].y + a.z * tq[j].z + a.w * tq[j].w;
             }
         }
     }
@@ -621,11 +679,10 @@ __device__ __forceinline__ void tile_gram(const float *As, int m, int MA, int wa
 
 // Warp sums of the Gram entries (each (i, j) belongs to one warp) to
 // out[i Q + j].
-template<int Q>
-__device__ __forceinline__ void write_gram(const float (&acc)[kRitzRowsPerWarp][Q], int MA, int warp, int lane,
-                                           double *out) {
+template<int Q, int RPW>
+__device__ __forceinline__ void write_gram(const float (&acc)[RPW][Q], int MA, int warp, int lane, double *out) {
 #pragma unroll
-    for (int ii = 0; ii < kRitzRowsPerWarp; ++ii) {
+    for (int ii = 0; ii < RPW; ++ii) {
         const int i = warp + 8 * ii;
         if (i < MA) {
 #pragma unroll
@@ -641,39 +698,117 @@ __device__ __forceinline__ void write_gram(const float (&acc)[kRitzRowsPerWarp][
     }
 }
 
-template<int Q>
-__global__ void __launch_bounds__(kRitzTile, 2) ritz_fused_kernel(const float *__restrict__ V,
+// Tile t of a block (grid stride over 256-row tiles) and its row count.
+__device__ __forceinline__ int64_t tile_base(int64_t t) {
+    return (static_cast<int64_t>(blockIdx.x) + t * gridDim.x) * kRitzTile;
+}
+
+__device__ __forceinline__ int64_t block_tiles(int64_t N) {
+    const int64_t all = (N + kRitzTile - 1) / kRitzTile;
+    return all > blockIdx.x ? (all - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+}
+
+// Bulk-copy staging with `stages` (1 or 2) buffers per block: tile t goes
+// to buffer t % stages and is waited for with parity (t / stages) & 1; the
+// copies of tile t + stages are issued once tile t's buffer is free, so with
+// two buffers the next tile lands while this one is computed.  Each
+// buffer holds the rows of two vector sets (n1 and n2 vectors).
+struct StagedTiles {
+    float *buf;          // buffer s at buf + s * (n1 + n2) * kRitzTile
+    uint64_t *bars;      // one mbarrier per buffer
+    int stages, n1, n2;
+    const float *src1, *src2;
+    int64_t N;
+    __device__ float *set1(int s) const { return buf + static_cast<size_t>(s) * (n1 + n2) * kRitzTile; }
+    __device__ float *set2(int s) const { return set1(s) + static_cast<size_t>(n1) * kRitzTile; }
+    // Warp 0 only.
+    __device__ void issue(int64_t t, int lane) const {
+        const int s = static_cast<int>(t % stages);
+        const int64_t base = tile_base(t);
+        const int rows = static_cast<int>(N - base < kRitzTile ? N - base : kRitzTile);
+        const uint32_t bytes = static_cast<uint32_t>(rows) * 4u, bar = stage_addr(&bars[s]);
+        if (lane == 0)
+            stage_arm(bar, static_cast<uint32_t>(n1 + n2) * bytes);
+        __syncwarp();
+        stage_rows(set1(s), src1, n1, N, base, bytes, bar, lane);
+        stage_rows(set2(s), src2, n2, N, base, bytes, bar, lane);
+    }
+    __device__ bool wait(int64_t t) const {
+        return stage_wait(stage_addr(&bars[t % stages]), static_cast<uint32_t>((t / stages) & 1));
+    }
+};
+
+template<int Q, bool BULK, int RPW>
+__global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel(const float *__restrict__ V,
                                                                   const float *__restrict__ W, int m, int64_t N,
                                                                   const __grid_constant__ CoefBlock<float> Y,
                                                                   const __grid_constant__ Theta th,
                                                                   const double *__restrict__ diag,
-                                                                  float *__restrict__ T, double *__restrict__ partial) {
-    extern __shared__ float As[]; // [MA][kRitzTile]
+                                                                  float *__restrict__ T, double *__restrict__ partial,
+                                                                  int stages) {
+    // T rows [Q][kRitzTile], then V rows [m][kRitzTile] (register loads), or
+    // `stages` buffers of V and W rows (bulk copies).
+    extern __shared__ __align__(16) float sm[];
+    __shared__ __align__(8) uint64_t bars[2];
     const int MA = m + Q;
+    float *Tt = sm;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float th_hi[Q], th_lo[Q], nrm[Q], acc[kRitzRowsPerWarp][Q];
+    const int64_t pq = static_cast<int64_t>(MA) * Q + Q;
+    double *out = partial + static_cast<int64_t>(blockIdx.x) * pq;
+    float th_hi[Q], th_lo[Q], nrm[Q], acc[RPW][Q];
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
         th_hi[j] = static_cast<float>(th.t[j]);
         th_lo[j] = static_cast<float>(th.t[j] - static_cast<double>(th_hi[j]));
         nrm[j] = 0.0f;
 #pragma unroll
-        for (int ii = 0; ii < kRitzRowsPerWarp; ++ii)
+        for (int ii = 0; ii < RPW; ++ii)
             acc[ii][j] = 0.0f;
     }
-    for (int64_t base = static_cast<int64_t>(blockIdx.x) * kRitzTile; base < N;
-         base += static_cast<int64_t>(gridDim.x) * kRitzTile) {
+    const StagedTiles st{sm + Q * kRitzTile, bars, stages, m, m, V, W, N};
+    const int64_t ntile = block_tiles(N);
+    if constexpr (BULK) {
+        if (tid < stages)
+            stage_init(stage_addr(&bars[tid]));
+        __syncthreads();
+        if (warp == 0)
+            for (int64_t t = 0; t < stages && t < ntile; ++t)
+                st.issue(t, lane);
+    }
+    bool failed = false;
+    int64_t t = 0;
+    for (; t < ntile; ++t) {
+        const int64_t base = tile_base(t);
+        const int rows = static_cast<int>(N - base < kRitzTile ? N - base : kRitzTile);
         const int64_t r = base + tid;
-        const bool ok = r < N;
+        const bool ok = tid < rows;
+        const int s = BULK ? static_cast<int>(t % stages) : 0;
+        float *Vs = BULK ? st.set1(s) : sm + Q * kRitzTile;
+        const float *Ws = st.set2(s);
+        if constexpr (BULK) {
+            if (__syncthreads_or(!st.wait(t))) {
+                failed = true;
+                break;
+            }
+        }
         float x[Q], ax[Q];
 #pragma unroll
         for (int j = 0; j < Q; ++j)
             x[j] = ax[j] = 0.0f;
 #pragma unroll 8
         for (int i = 0; i < m; ++i) {
-            const float v = ok ? V[i * N + r] : 0.0f;
-            const float w = ok ? W[i * N + r] : 0.0f;
-            As[i * kRitzTile + tid] = v;
+            float v, w;
+            if constexpr (BULK) {
+                // Rows past N: zeros for the Gram sums (the copy left them).
+                v = ok ? Vs[i * kRitzTile + tid] : 0.0f;
+                w = ok ? Ws[i * kRitzTile + tid] : 0.0f;
+                if (!ok)
+                    Vs[i * kRitzTile + tid] = 0.0f;
+            } else {
+                v = ok ? V[i * N + r] : 0.0f;
+                w = ok ? W[i * N + r] : 0.0f;
+                Vs[i * kRitzTile + tid] = v;
+            }
 #pragma unroll
             for (int j = 0; j < Q; ++j) {
                 const float y = Y.y[i * Q + j];
@@ -689,20 +824,33 @@ __global__ void __launch_bounds__(kRitzTile, 2) ritz_fused_kernel(const float *_
             float den = th_hi[j] - df;
             if (fabsf(den) < 1e-8f)
                 den = (den < 0.0f) ? -1e-8f : 1e-8f;
-            const float t = res * __frcp_rn(den);
-            As[(m + j) * kRitzTile + tid] = ok ? t : 0.0f;
+            const float tv = res * __frcp_rn(den);
+            Tt[j * kRitzTile + tid] = ok ? tv : 0.0f;
             if (ok)
-                T[j * N + r] = t;
+                T[j * N + r] = tv;
         }
         __syncthreads();
-        tile_gram<Q>(As, m, MA, warp, lane, acc);
+        tile_gram<Q, RPW>(Vs, Tt, m, MA, warp, lane, acc);
         __syncthreads();
+        if constexpr (BULK) {
+            if (warp == 0 && t + stages < ntile)
+                st.issue(t + stages, lane);
+        }
     }
-    const int64_t pq = static_cast<int64_t>(MA) * Q + Q;
-    double *out = partial + static_cast<int64_t>(blockIdx.x) * pq;
-    write_gram<Q>(acc, MA, warp, lane, out);
-    // Residual norms: warp sums in FP32, then the 8 warps in FP64 (the
-    // staging array is free after the last tile's barrier).
+    if constexpr (BULK) {
+        if (failed) {
+            // Let the copies in flight land (bounded), then report through
+            // NaN sums.
+            for (int64_t u = t; u < t + stages && u < ntile; ++u)
+                st.wait(u);
+            for (int64_t e = tid; e < pq; e += kRitzTile)
+                out[e] = __longlong_as_double(0x7ff8000000000000LL);
+            return;
+        }
+    }
+    write_gram<Q, RPW>(acc, MA, warp, lane, out);
+    // Residual norms: warp sums in FP32, then the 8 warps in FP64 (the T
+    // rows are free after the last tile's barrier).
 #pragma unroll
     for (int j = 0; j < Q; ++j) {
         float v = nrm[j];
@@ -710,14 +858,14 @@ __global__ void __launch_bounds__(kRitzTile, 2) ritz_fused_kernel(const float *_
         for (int o = 16; o > 0; o >>= 1)
             v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0)
-            As[warp * Q + j] = v;
+            Tt[warp * Q + j] = v;
     }
     __syncthreads();
     if (tid < Q) {
-        double s = 0.0;
+        double sum = 0.0;
         for (int w = 0; w < kRitzTile / 32; ++w)
-            s += static_cast<double>(As[w * Q + tid]);
-        out[static_cast<int64_t>(MA) * Q + tid] = s;
+            sum += static_cast<double>(Tt[w * Q + tid]);
+        out[static_cast<int64_t>(MA) * Q + tid] = sum;
     }
 }
 
@@ -727,54 +875,105 @@ __global__ void __launch_bounds__(kRitzTile, 2) ritz_fused_kernel(const float *_
 // (combine2_kernel's sums) to out + c N, and per block
 //   partial[b][i Q + c] = sum_r A_i[r] T1_c[r],  A = [V_0 .. V_{m-1}, T1_0 .. T1_{Q-1}]
 // with the tile staging of ritz_fused_kernel (V read once).
-template<int Q>
-__global__ void __launch_bounds__(kRitzTile, 2) project_gram_kernel(const float *__restrict__ V, int m,
+template<int Q, bool BULK, int RPW>
+__global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) project_gram_kernel(const float *__restrict__ V, int m,
                                                                     const float *__restrict__ Tsrc, int b, int64_t N,
                                                                     const __grid_constant__ CoefBlock<float> Y,
                                                                     float *__restrict__ out,
-                                                                    double *__restrict__ partial) {
-    extern __shared__ float As[]; // [MA][kRitzTile]
+                                                                    double *__restrict__ partial, int stages) {
+    // T1 rows [Q][kRitzTile], then V rows [m][kRitzTile] (register loads),
+    // or `stages` buffers of V and Tsrc rows (bulk copies).
+    extern __shared__ __align__(16) float sm[];
+    __shared__ __align__(8) uint64_t bars[2];
     const int MA = m + Q;
+    float *Tt = sm;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    float acc[kRitzRowsPerWarp][Q];
+    double *pout = partial + static_cast<int64_t>(blockIdx.x) * MA * Q;
+    float acc[RPW][Q];
 #pragma unroll
-    for (int ii = 0; ii < kRitzRowsPerWarp; ++ii)
+    for (int ii = 0; ii < RPW; ++ii)
 #pragma unroll
         for (int j = 0; j < Q; ++j)
             acc[ii][j] = 0.0f;
-    for (int64_t base = static_cast<int64_t>(blockIdx.x) * kRitzTile; base < N;
-         base += static_cast<int64_t>(gridDim.x) * kRitzTile) {
+    const StagedTiles st{sm + Q * kRitzTile, bars, stages, m, b, V, Tsrc, N};
+    const int64_t ntile = block_tiles(N);
+    if constexpr (BULK) {
+        if (tid < stages)
+            stage_init(stage_addr(&bars[tid]));
+        __syncthreads();
+        if (warp == 0)
+            for (int64_t t = 0; t < stages && t < ntile; ++t)
+                st.issue(t, lane);
+    }
+    bool failed = false;
+    int64_t t = 0;
+    for (; t < ntile; ++t) {
+        const int64_t base = tile_base(t);
+        const int rows = static_cast<int>(N - base < kRitzTile ? N - base : kRitzTile);
         const int64_t r = base + tid;
-        const bool ok = r < N;
+        const bool ok = tid < rows;
+        const int s = BULK ? static_cast<int>(t % stages) : 0;
+        float *Vs = BULK ? st.set1(s) : sm + Q * kRitzTile;
+        const float *Ts = st.set2(s);
+        if constexpr (BULK) {
+            if (__syncthreads_or(!st.wait(t))) {
+                failed = true;
+                break;
+            }
+        }
         float t1[Q];
 #pragma unroll
         for (int j = 0; j < Q; ++j)
             t1[j] = 0.0f;
 #pragma unroll 8
         for (int i = 0; i < m; ++i) {
-            const float v = ok ? V[i * N + r] : 0.0f;
-            As[i * kRitzTile + tid] = v;
+            float v;
+            if constexpr (BULK) {
+                v = ok ? Vs[i * kRitzTile + tid] : 0.0f;
+                if (!ok)
+                    Vs[i * kRitzTile + tid] = 0.0f;
+            } else {
+                v = ok ? V[i * N + r] : 0.0f;
+                Vs[i * kRitzTile + tid] = v;
+            }
 #pragma unroll
             for (int j = 0; j < Q; ++j)
                 t1[j] += Y.y[i * Q + j] * v;
         }
         for (int a = 0; a < b; ++a) {
-            const float v = ok ? Tsrc[a * N + r] : 0.0f;
+            float v;
+            if constexpr (BULK)
+                v = ok ? Ts[a * kRitzTile + tid] : 0.0f;
+            else
+                v = ok ? Tsrc[a * N + r] : 0.0f;
 #pragma unroll
             for (int j = 0; j < Q; ++j)
                 t1[j] += Y.y[(m + a) * Q + j] * v;
         }
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
-            As[(m + j) * kRitzTile + tid] = t1[j];
+            Tt[j * kRitzTile + tid] = t1[j];
             if (ok)
                 out[j * N + r] = t1[j];
         }
         __syncthreads();
-        tile_gram<Q>(As, m, MA, warp, lane, acc);
+        tile_gram<Q, RPW>(Vs, Tt, m, MA, warp, lane, acc);
         __syncthreads();
+        if constexpr (BULK) {
+            if (warp == 0 && t + stages < ntile)
+                st.issue(t + stages, lane);
+        }
     }
-    write_gram<Q>(acc, MA, warp, lane, partial + static_cast<int64_t>(blockIdx.x) * MA * Q);
+    if constexpr (BULK) {
+        if (failed) {
+            for (int64_t u = t; u < t + stages && u < ntile; ++u)
+                st.wait(u);
+            for (int64_t e = tid; e < static_cast<int64_t>(MA) * Q; e += kRitzTile)
+                pout[e] = __longlong_as_double(0x7ff8000000000000LL);
+            return;
+        }
+    }
+    write_gram<Q, RPW>(acc, MA, warp, lane, pout);
 }
 
 // out[j][r] = sum_{i < p1} Y[i][j] V1[i][r] + sum_{i < p2} Y[p1 + i][j] V2[i][r]
@@ -1080,6 +1279,7 @@ private:
                 if constexpr (std::is_same<U, float>::value) {
                     on_tc = gram_tc_enabled() && pp >= kGramTcMinP;
                 }
+                const int trg = tr_open(kTrGram);
                 if (on_tc) {
                     nb = launch_gram_tc(gram_blocks_, st_, reinterpret_cast<const float *>(Ai), pp,
                                         reinterpret_cast<const float *>(Bj), qq, N_, d_partial_);
@@ -1096,6 +1296,7 @@ private:
                 reduce_partials_kernel<<<pp * qq, 256, 0, st_>>>(d_partial_, nb, pp * qq,
                                                                  d_mapped_ ? d_mapped_ : d_small_),
                     ::pyci_gpu::note_launch();
+                tr_close(trg);
                 // Otherwise read back through the pinned buffer: one DMA,
                 // then one synchronisation (a pageable copy would block
                 // inside the copy call instead).
@@ -1105,7 +1306,9 @@ private:
                     e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pp * qq, cudaMemcpyDeviceToHost, st_);
                 if (e != cudaSuccess)
                     return cuda_status(e, "gram copy");
+                const int trs = tr_open(kTrSync);
                 e = cudaStreamSynchronize(st_);
+                tr_close(trs);
                 wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
                 ++syncs_;
                 if (e != cudaSuccess)
@@ -1134,6 +1337,12 @@ private:
             if (df_linalg_)
                 return combine_df(V, p, Y, q, beta, out);
         }
+        const int trk = tr_open(kTrCombine);
+        struct Close {
+            Davidson *d;
+            int h;
+            ~Close() { d->tr_close(h); }
+        } close{this, trk};
         for (int j0 = 0; j0 < q; j0 += kMaxQ) {
             const int qq = std::min(kMaxQ, q - j0);
             for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
@@ -1160,6 +1369,12 @@ private:
     // combine<double, double, double> in double-float arithmetic
     // (combine_df_kernel).
     int combine_df(const double *V, int p, const std::vector<double> &Y, int q, double beta, double *out) {
+        const int trk = tr_open(kTrCombine);
+        struct Close {
+            Davidson *d;
+            int h;
+            ~Close() { d->tr_close(h); }
+        } close{this, trk};
         for (int j0 = 0; j0 < q; j0 += kMaxQ) {
             const int qq = std::min(kMaxQ, q - j0);
             for (int i0 = 0; i0 < p; i0 += kMaxGramP) {
@@ -1181,29 +1396,52 @@ private:
         return PYCI_GPU_OK;
     }
 
-    // Staged-tile kernels (ritz_fused_kernel, project_gram_kernel): the
-    // shared-memory limit for the widest tile, set once.
+    // Staged-tile kernels (ritz_fused_kernel, project_gram_kernel), by
+    // Q - 1 and by BULK (bulk-copy staging when N is a multiple of 4).
+    using RitzFn = void (*)(const float *, const float *, int, int64_t, CoefBlock<float>, Theta, const double *,
+                            float *, double *, int);
+    using ProjectFn = void (*)(const float *, int, const float *, int, int64_t, CoefBlock<float>, float *, double *,
+                               int);
+    // Rows of [V T] per warp in the Gram sums: 5 (MA <= 40 and at most 5
+    // pairs: three blocks per SM in 80 registers) or 9.
+    static int staged_rpw(int MA, int q) { return (MA <= 40 && q <= 5) ? 5 : kRitzRowsPerWarp; }
+#define PYCI_STAGED_TABLE(K, B, R)                                                                                  \
+    { K<1, B, R>, K<2, B, R>, K<3, B, R>, K<4, B, R>, K<5, B, R>, K<6, B, R>, K<7, B, R>, K<8, B, R> }
+    static RitzFn ritz_fn(int q, bool bulk, int rpw) {
+        static const RitzFn f[2][2][kMaxQ] = {
+            {PYCI_STAGED_TABLE(ritz_fused_kernel, false, 5), PYCI_STAGED_TABLE(ritz_fused_kernel, false, 9)},
+            {PYCI_STAGED_TABLE(ritz_fused_kernel, true, 5), PYCI_STAGED_TABLE(ritz_fused_kernel, true, 9)}};
+        return f[bulk ? 1 : 0][rpw <= 5 ? 0 : 1][q - 1];
+    }
+    static ProjectFn project_fn(int q, bool bulk, int rpw) {
+        static const ProjectFn f[2][2][kMaxQ] = {
+            {PYCI_STAGED_TABLE(project_gram_kernel, false, 5), PYCI_STAGED_TABLE(project_gram_kernel, false, 9)},
+            {PYCI_STAGED_TABLE(project_gram_kernel, true, 5), PYCI_STAGED_TABLE(project_gram_kernel, true, 9)}};
+        return f[bulk ? 1 : 0][rpw <= 5 ? 0 : 1][q - 1];
+    }
+#undef PYCI_STAGED_TABLE
+    // The shared-memory limit of every staged-tile kernel, set once.
     static void staged_attributes() {
         static const bool done = [] {
-            const int most = static_cast<int>(sizeof(float) * kRitzTile * kRitzMaxA);
-            for (auto k : {ritz_fused_kernel<1>, ritz_fused_kernel<2>, ritz_fused_kernel<3>, ritz_fused_kernel<4>,
-                           ritz_fused_kernel<5>, ritz_fused_kernel<6>, ritz_fused_kernel<7>, ritz_fused_kernel<8>})
-                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-            for (auto k : {project_gram_kernel<1>, project_gram_kernel<2>, project_gram_kernel<3>,
-                           project_gram_kernel<4>, project_gram_kernel<5>, project_gram_kernel<6>,
-                           project_gram_kernel<7>, project_gram_kernel<8>})
-                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+            for (int bulk = 0; bulk < 2; ++bulk)
+                for (int rpw : {5, kRitzRowsPerWarp})
+                    for (int q = 1; q <= kMaxQ; ++q) {
+                        cudaFuncSetAttribute(ritz_fn(q, bulk, rpw), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kStagedMaxBytes);
+                        cudaFuncSetAttribute(project_fn(q, bulk, rpw), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             kStagedMaxBytes);
+                    }
             return true;
         }();
         (void)done;
     }
 
-    // Blocks for a staged-tile kernel with MA staged rows: the resident
-    // blocks of one wave, at most gram_blocks_ (the partial sums' rows).
-    unsigned staged_grid(const void *fn, int MA) const {
+    // Blocks for a staged-tile kernel with `smem` bytes of tiles: the
+    // resident blocks of one wave, at most gram_blocks_ (the partial sums'
+    // rows).
+    unsigned staged_grid(const void *fn, size_t smem) const {
         int per_sm = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRitzTile, sizeof(float) * kRitzTile * MA) !=
-            cudaSuccess)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kRitzTile, smem) != cudaSuccess)
             per_sm = 1;
         per_sm = std::max(1, per_sm);
         return static_cast<unsigned>(std::max<int64_t>(
@@ -1220,8 +1458,10 @@ private:
         cudaError_t e = cudaSuccess;
         if (!d_mapped_)
             e = cudaMemcpyAsync(h_small_, d_small_, sizeof(double) * pq, cudaMemcpyDeviceToHost, st_);
+        const int trs = tr_open(kTrSync);
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(st_);
+        tr_close(trs);
         wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         ++syncs_;
         if (e != cudaSuccess)
@@ -1246,28 +1486,30 @@ private:
         for (int j = 0; j < q; ++j)
             th.t[j] = theta[j];
         const int MA = m + q;
-        const size_t smem = sizeof(float) * kRitzTile * MA;
-        unsigned nb = 0;
-        auto launch = [&](auto kernel) {
-            nb = staged_grid(reinterpret_cast<const void *>(kernel), MA);
-            kernel<<<nb, kRitzTile, smem, st_>>>(V, W, m, N_, y, th, diag, Tb, d_partial_);
-            ::pyci_gpu::note_launch();
-        };
-        switch (q) {
-        case 1: launch(ritz_fused_kernel<1>); break;
-        case 2: launch(ritz_fused_kernel<2>); break;
-        case 3: launch(ritz_fused_kernel<3>); break;
-        case 4: launch(ritz_fused_kernel<4>); break;
-        case 5: launch(ritz_fused_kernel<5>); break;
-        case 6: launch(ritz_fused_kernel<6>); break;
-        case 7: launch(ritz_fused_kernel<7>); break;
-        default: launch(ritz_fused_kernel<8>); break;
-        }
+        // Bulk copies when every row range starts on 16 bytes; one buffer
+        // (two buffers, one block per SM, took 1.6x as long on a 10.5M-row
+        // subspace: the tile arithmetic, not the copies, bounds this kernel,
+        // and it needs the blocks).
+        const bool bulk = N_ % 4 == 0;
+        const size_t row = sizeof(float) * kRitzTile;
+        const int stages = 1;
+        const size_t smem = row * (bulk ? q + stages * 2 * m : q + m);
+        const RitzFn fn = ritz_fn(q, bulk, staged_rpw(MA, q));
+        const unsigned nb = staged_grid(reinterpret_cast<const void *>(fn), smem);
+        const int trk = tr_open(kTrRitz);
+        fn<<<nb, kRitzTile, smem, st_>>>(V, W, m, N_, y, th, diag, Tb, d_partial_, stages);
+        ::pyci_gpu::note_launch();
+        tr_close(trk);
         std::vector<double> h;
         const int pq = MA * q + q;
         int rc = read_partials(nb, pq, h, "fused Ritz step");
         if (rc)
             return rc;
+        for (double v : h)
+            if (!std::isfinite(v)) {
+                set_error("fused Ritz step: non-finite sums (a staged-tile wait timed out, or non-finite vectors)");
+                return PYCI_GPU_ECUDA;
+            }
         P.assign(h.begin(), h.begin() + static_cast<size_t>(MA) * q);
         rn2.assign(h.begin() + static_cast<size_t>(MA) * q, h.end());
         return PYCI_GPU_OK;
@@ -1280,24 +1522,25 @@ private:
                      std::vector<double> &P) {
         staged_attributes();
         const int MA = m + k;
-        const size_t smem = sizeof(float) * kRitzTile * MA;
-        unsigned nb = 0;
-        auto launch = [&](auto kernel) {
-            nb = staged_grid(reinterpret_cast<const void *>(kernel), MA);
-            kernel<<<nb, kRitzTile, smem, st_>>>(V, m, Tsrc, b, N_, y, out, d_partial_);
-            ::pyci_gpu::note_launch();
-        };
-        switch (k) {
-        case 1: launch(project_gram_kernel<1>); break;
-        case 2: launch(project_gram_kernel<2>); break;
-        case 3: launch(project_gram_kernel<3>); break;
-        case 4: launch(project_gram_kernel<4>); break;
-        case 5: launch(project_gram_kernel<5>); break;
-        case 6: launch(project_gram_kernel<6>); break;
-        case 7: launch(project_gram_kernel<7>); break;
-        default: launch(project_gram_kernel<8>); break;
-        }
-        return read_partials(nb, MA * k, P, "orthonormalisation pass");
+        const bool bulk = N_ % 4 == 0;
+        const size_t row = sizeof(float) * kRitzTile;
+        const int stages = 1;
+        const size_t smem = row * (bulk ? k + stages * (m + b) : k + m);
+        const ProjectFn fn = project_fn(k, bulk, staged_rpw(MA, k));
+        const unsigned nb = staged_grid(reinterpret_cast<const void *>(fn), smem);
+        const int trk = tr_open(kTrProject);
+        fn<<<nb, kRitzTile, smem, st_>>>(V, m, Tsrc, b, N_, y, out, d_partial_, stages);
+        ::pyci_gpu::note_launch();
+        tr_close(trk);
+        int rc = read_partials(nb, MA * k, P, "orthonormalisation pass");
+        if (rc)
+            return rc;
+        for (double v : P)
+            if (!std::isfinite(v)) {
+                set_error("orthonormalisation pass: non-finite sums (a staged-tile wait timed out, or non-finite vectors)");
+                return PYCI_GPU_ECUDA;
+            }
+        return PYCI_GPU_OK;
     }
 
     // The fused Ritz step applies (FP32 solve, no full-space Rayleigh-Ritz,
@@ -1331,6 +1574,7 @@ private:
             const int kk = std::min(chunk, k - j0);
             const int kp = padded_width(kk);
             const bool df = std::is_same<T, double>::value && fp64_df_;
+            const int trp = tr_open(kTrPack);
             if (packed)
                 ;
             else if (df)
@@ -1340,13 +1584,16 @@ private:
             else
                 pack_kernel<T><<<grid(N_), 256, 0, st_>>>(V + static_cast<int64_t>(j0) * N_, N_, kk, kp, Xi_),
                     ::pyci_gpu::note_launch();
+            tr_close(trp);
             const size_t tk = timer_begin();
             int rc = df ? csr_spmm_df(csr_, kp, reinterpret_cast<const float *>(Xi_), reinterpret_cast<double *>(Yi_), st_)
                         : csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
             if (rc)
                 return rc;
             timer_end(tk);
+            const int tru = tr_open(kTrPack);
             unpack_kernel<T><<<grid(N_), 256, 0, st_>>>(Yi_, N_, kk, kp, W + static_cast<int64_t>(j0) * N_), ::pyci_gpu::note_launch();
+            tr_close(tru);
             matvecs_ += kk;
         }
         return PYCI_GPU_OK;
@@ -1362,7 +1609,9 @@ private:
             Theta th{};
             for (int j = 0; j < qq; ++j)
                 th.t[j] = theta[j0 + j];
+            const int trk = tr_open(kTrRows);
             residual_kernel<U><<<grid(N_), 256, 0, st_>>>(AX + o, X + o, th, qq, N_, R + o), ::pyci_gpu::note_launch();
+            tr_close(trk);
         }
     }
 
@@ -1371,10 +1620,12 @@ private:
     template<typename U>
     void precondition(const U *R, const double *diag, const std::vector<int> &todo, const std::vector<double> &theta,
                       T *out) {
+        const int trk = tr_open(kTrRows);
         for (size_t c0 = 0; c0 < todo.size(); c0 += kMaxQ)
             precondition_kernel<U, T><<<grid(N_), 256, 0, st_>>>(R, diag, make_cols(todo, c0, theta), N_,
                                                                   out + static_cast<int64_t>(c0) * N_),
                 ::pyci_gpu::note_launch();
+        tr_close(trk);
     }
 
     // Rows of the k lowest diagonal elements, ascending (ties by row), found
@@ -1436,6 +1687,47 @@ private:
         return timers_.size() - 1;
     }
     void timer_end(size_t k) { cudaEventRecord(timers_[k].second, st_); }
+    // PYCI_GPU_SOLVE_TRACE: device time by kind of step, from event pairs
+    // around its launches, and the gaps at the host synchronisations (from
+    // the end of the queued work to the host's next enqueue).
+    enum { kTrGram, kTrRitz, kTrProject, kTrCombine, kTrPack, kTrRows, kTrSync, kTrKinds };
+    std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>> tr_;
+    int tr_open(int kind) {
+        if (!trace_)
+            return -1;
+        cudaEvent_t a = nullptr, b = nullptr;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st_);
+        tr_.emplace_back(kind, a, b);
+        return static_cast<int>(tr_.size()) - 1;
+    }
+    void tr_close(int h) {
+        if (h >= 0)
+            cudaEventRecord(std::get<2>(tr_[static_cast<size_t>(h)]), st_);
+    }
+    std::string tr_summary() {
+        static const char *names[kTrKinds] = {"gram", "ritz", "project", "combine", "pack", "rows", "sync gaps"};
+        double t[kTrKinds] = {};
+        int n[kTrKinds] = {};
+        for (auto &e : tr_) {
+            float ms = 0.0f;
+            if (cudaEventSynchronize(std::get<2>(e)) == cudaSuccess &&
+                cudaEventElapsedTime(&ms, std::get<1>(e), std::get<2>(e)) == cudaSuccess)
+                t[std::get<0>(e)] += ms;
+            ++n[std::get<0>(e)];
+            cudaEventDestroy(std::get<1>(e));
+            cudaEventDestroy(std::get<2>(e));
+        }
+        tr_.clear();
+        std::string out;
+        char buf[96];
+        for (int k = 0; k < kTrKinds; ++k) {
+            std::snprintf(buf, sizeof(buf), "%s%s %.3f ms (%d)", k ? ", " : "", names[k], t[k], n[k]);
+            out += buf;
+        }
+        return out;
+    }
     double timed_total_ms() {
         double total = 0.0;
         for (auto &pr : timers_) {
@@ -1448,7 +1740,9 @@ private:
     // Host-side synchronisation with the stream, counted and timed.
     cudaError_t wait() {
         const auto t0 = std::chrono::steady_clock::now();
+        const int trs = tr_open(kTrSync);
         const cudaError_t e = cudaStreamSynchronize(st_);
+        tr_close(trs);
         wait_s_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         ++syncs_;
         return e;
@@ -1722,11 +2016,13 @@ int Davidson<T>::orthonormalize_pre(T *V, int m, const T *Tb, int b, const std::
                 for (int c = 0; c < k; ++c)
                     y.y[(m + cols[a]) * k + c] = static_cast<float>(Linv[static_cast<size_t>(c) * k + a]);
             float *xp = xi ? reinterpret_cast<float *>(Xi_) : nullptr;
+            const int trk = tr_open(kTrCombine);
             if (N_ % 4 == 0)
                 combine2_kernel<4><<<grid(N_ / 4), 256, 0, st_>>>(V, m, Q, nq, N_, y, k, out, xp, kp);
             else
                 combine2_kernel<1><<<grid(N_), 256, 0, st_>>>(V, m, Q, nq, N_, y, k, out, xp, kp);
             ::pyci_gpu::note_launch();
+            tr_close(trk);
             if (xi) {
                 xi_src_ = out;
                 xi_k_ = k;
@@ -1963,8 +2259,11 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
 
     std::vector<double> G(static_cast<size_t>(mmax) * mmax, 0.0), theta, Y, Gc;
     std::vector<double> rnorm(b, 0.0);
-    // Previous iteration's FP32 residual norms (mixed mode's stall test).
+    // Previous iteration's FP32 residual norms and the last kPlateau of them
+    // per root (mixed mode's stall tests).
     std::vector<double> rprev(b, std::numeric_limits<double>::infinity());
+    constexpr int kPlateau = 5;
+    std::vector<std::vector<double>> rhist(b);
     const double eps23 = std::pow(std::numeric_limits<double>::epsilon(), 2.0 / 3.0);
     const double mixed_floor = 1e-5;
     int64_t iter = 0, restarts = 0, refinements = 0;
@@ -2032,9 +2331,19 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
             // less than 30 % since the last iteration sits on the FP32
             // rounding floor of H x (~1e-6 |theta|); more FP32 iterations
             // cannot lower it, so the root goes to the FP64 refinement, whose
-            // own test decides.
-            const bool stalled = mixed_ && rnorm[j] <= 2.0 * thr && rnorm[j] > 0.7 * rprev[j];
+            // own test decides.  So does one within 4x of the threshold that
+            // has not improved by 10 % on the best of its last 5 values (a
+            // floor slightly above 2x: seen at 2.0-2.4e-5 against 1e-5 over
+            // 270 restarts of a 16-vector subspace).
+            double best = std::numeric_limits<double>::infinity();
+            if (static_cast<int>(rhist[j].size()) == kPlateau)
+                best = *std::min_element(rhist[j].begin(), rhist[j].end());
+            const bool stalled = mixed_ && ((rnorm[j] <= 2.0 * thr && rnorm[j] > 0.7 * rprev[j]) ||
+                                            (rnorm[j] <= 4.0 * thr && rnorm[j] > 0.9 * best));
             rprev[j] = rnorm[j];
+            if (static_cast<int>(rhist[j].size()) == kPlateau)
+                rhist[j].erase(rhist[j].begin());
+            rhist[j].push_back(rnorm[j]);
             if (!(rnorm[j] <= thr) && !stalled) {
                 if (j < nw)
                     all = false;
@@ -2289,10 +2598,10 @@ int Davidson<T>::run(const double *c0, int64_t maxiter, double tol, double ecore
     // breakdown (blocked in read-backs, Rayleigh-Ritz).
     if (trace_)
         std::fprintf(stderr, "solve trace: total %.3f ms, spmm %.3f ms, wait %.3f ms (%lld syncs), eig %.3f ms, "
-                             "allocations %.3f ms, eigenvectors out %.3f ms, iters %lld\n",
+                             "allocations %.3f ms, eigenvectors out %.3f ms, iters %lld; device: %s\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count() * 1e3,
                      timed_total_ms(), wait_s_ * 1e3, static_cast<long long>(syncs_), eig_s_ * 1e3, alloc_s_ * 1e3,
-                     evec_s_ * 1e3, static_cast<long long>(iter + 1));
+                     evec_s_ * 1e3, static_cast<long long>(iter + 1), tr_summary().c_str());
     return PYCI_GPU_OK;
 }
 
