@@ -79,12 +79,30 @@ __global__ void pack_split_kernel(const double *__restrict__ V, int64_t N, int k
         }
 }
 
+// W[j * N + r] = Yi[r * kp + j] for j < k; FP32 rows of a multiple of 4
+// entries are read with 16-byte loads (one per 4 entries instead of 4).
 template<typename T>
 __global__ void unpack_kernel(const T *__restrict__ Yi, int64_t N, int k, int kp, T *__restrict__ W) {
     for (int64_t r = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; r < N;
-         r += static_cast<int64_t>(gridDim.x) * blockDim.x)
+         r += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        if constexpr (sizeof(T) == 4) {
+            if (kp % 4 == 0) {
+                for (int j4 = 0; j4 < k; j4 += 4) {
+                    const float4 v = *reinterpret_cast<const float4 *>(Yi + r * kp + j4);
+                    W[j4 * N + r] = v.x;
+                    if (j4 + 1 < k)
+                        W[(j4 + 1) * N + r] = v.y;
+                    if (j4 + 2 < k)
+                        W[(j4 + 2) * N + r] = v.z;
+                    if (j4 + 3 < k)
+                        W[(j4 + 3) * N + r] = v.w;
+                }
+                continue;
+            }
+        }
         for (int j = 0; j < k; ++j)
             W[j * N + r] = Yi[r * kp + j];
+    }
 }
 
 // Width the SpMM reads with 8/16-byte vector gathers: 3 -> 4, 5..7 -> 8.
