@@ -803,6 +803,9 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel
         const int s = BULK ? static_cast<int>(t % stages) : 0;
         float *Vs = BULK ? st.set1(s) : sm + Q * kRitzTile;
         const float *Ws = st.set2(s);
+        // The diagonal before the tile's wait: its memory latency overlaps
+        // the copies instead of following them.
+        const float df = ok ? static_cast<float>(diag[r]) : 0.0f;
         if constexpr (BULK) {
             if (__syncthreads_or(!st.wait(t))) {
                 failed = true;
@@ -834,7 +837,6 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel
                 ax[j] += y * w;
             }
         }
-        const float df = ok ? static_cast<float>(diag[r]) : 0.0f;
 #pragma unroll
         for (int j = 0; j < Q; ++j) {
             const float res = fmaf(-th_lo[j], x[j], fmaf(-th_hi[j], x[j], ax[j]));
@@ -1811,7 +1813,12 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
     int rc;
     const double piv_tol = mixed_ ? 1e-6 : 1e-14;
     // Cholesky S = L L^T and Linv = L^{-1}; false when S is not safely positive
-    // definite.  kappa: (max L_jj / min L_jj)^2, a cheap estimate of cond(S).
+    // definite.  kappa: (max r_j / min r_j)^2 with r_j = L_jj / sqrt(S_jj), a
+    // cheap estimate of the condition of S with its columns scaled to unit
+    // norm.  The FP32 combination T L^{-T} rounds each term relative to
+    // |t_a| |(L^{-T})_ac|, which does not change under column scaling, so
+    // corrections of very different norms (converged roots topping up a
+    // block) need no extra pass on that account.
     double kappa = 0.0;
     auto cholesky_inv = [&](const std::vector<double> &Sm, std::vector<double> &Linv) -> bool {
         std::vector<double> L(static_cast<size_t>(k) * k, 0.0);
@@ -1831,8 +1838,9 @@ int Davidson<T>::orthonormalize(T *V, int m, int k, int &kept) {
         }
         double lmax = 0.0, lmin = std::numeric_limits<double>::infinity();
         for (int j = 0; j < k; ++j) {
-            lmax = std::max(lmax, L[static_cast<size_t>(j) * k + j]);
-            lmin = std::min(lmin, L[static_cast<size_t>(j) * k + j]);
+            const double r = L[static_cast<size_t>(j) * k + j] / std::sqrt(Sm[static_cast<size_t>(j) * k + j]);
+            lmax = std::max(lmax, r);
+            lmin = std::min(lmin, r);
         }
         kappa = (lmax / lmin) * (lmax / lmin);
         Linv.assign(static_cast<size_t>(k) * k, 0.0);
@@ -2046,13 +2054,14 @@ int Davidson<T>::orthonormalize_pre(T *V, int m, const T *Tb, int b, const std::
                 xi_k_ = k;
             }
         };
-        // Cholesky of S with the conditioning estimate (max L_jj / min L_jj)^2.
+        // Cholesky of S with orthonormalize's column-scaled conditioning
+        // estimate.
         auto chol = [&](const std::vector<double> &S, std::vector<double> &Linv, double &kappa) -> bool {
             if (!cholesky_inverse(S, k, 1e-6, Linv))
                 return false;
             double lmax = 0.0, lmin = std::numeric_limits<double>::infinity();
             for (int j = 0; j < k; ++j) {
-                const double l = 1.0 / Linv[static_cast<size_t>(j) * k + j];
+                const double l = 1.0 / Linv[static_cast<size_t>(j) * k + j] / std::sqrt(S[static_cast<size_t>(j) * k + j]);
                 lmax = std::max(lmax, l);
                 lmin = std::min(lmin, l);
             }
