@@ -1571,6 +1571,12 @@ private:
         return std::is_same<T, float>::value && mixed_ && ritz_fused_ && q >= 1 && q <= kMaxQ && m + q <= kRitzMaxA;
     }
 
+    // Row width of the packed FP32 operand of a k-vector product: the
+    // implicit DOCI form takes 5 vectors as they are (4.0 ms on the 32o DOCI
+    // against 5.5 ms padded to 8, which its 6- and 7-wide forms match);
+    // otherwise padded_width.
+    int xwidth(int k) const { return (csr_->dx_v && k == 5) ? 5 : padded_width(k); }
+
     // Vectors per product launch: on the SELL-32 copy or the implicit-column
     // form the FP32 product streams the matrix once per launch and is bound by
     // that stream, so up to 8 vectors share one launch.
@@ -1592,8 +1598,8 @@ private:
         xi_src_ = nullptr;
         for (int j0 = 0; j0 < k; j0 += chunk) {
             const int kk = std::min(chunk, k - j0);
-            const int kp = padded_width(kk);
             const bool df = std::is_same<T, double>::value && fp64_df_;
+            const int kp = df ? padded_width(kk) : xwidth(kk);
             const int trp = tr_open(kTrPack);
             if (packed)
                 ;
@@ -1606,6 +1612,16 @@ private:
                     ::pyci_gpu::note_launch();
             tr_close(trp);
             const size_t tk = timer_begin();
+            // The implicit DOCI form writes the FP32 block straight into W's
+            // columns (no unpack) when it needs no padding.
+            if constexpr (std::is_same<T, float>::value) {
+                if (prec == PYCI_PREC_FP32 && kp == kk && csr_->dx_v &&
+                    docx_launch_columns(csr_, kk, Xi_, W + static_cast<int64_t>(j0) * N_, st_)) {
+                    timer_end(tk);
+                    matvecs_ += kk;
+                    continue;
+                }
+            }
             int rc = df ? csr_spmm_df(csr_, kp, reinterpret_cast<const float *>(Xi_), reinterpret_cast<double *>(Yi_), st_)
                         : csr_spmm(csr_, prec, kp, Xi_, Yi_, st_);
             if (rc)
@@ -2024,7 +2040,7 @@ int Davidson<T>::orthonormalize_pre(T *V, int m, const T *Tb, int b, const std::
     T *out = V + static_cast<int64_t>(m) * N_;
     if constexpr (std::is_same<T, float>::value) {
         const bool pack = k <= spmm_chunk(prec);
-        const int kp = padded_width(k);
+        const int kp = xwidth(k);
         // (Q - V C) L^{-T} for the block Q (b vectors, columns cols of it
         // chosen, k of them) into out (also packed into Xi_ when xi): rows of
         // V, then the rows of Q.

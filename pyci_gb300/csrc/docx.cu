@@ -43,6 +43,7 @@ struct DxArgs {
     const int64_t *binom; // [(n + 1) * ldk]
     const float *v;       // [2][n][n]: high parts, then low parts
     const double *diag;   // [nrow]
+    int64_t ycol;         // FP32 output: 0 = rows of K values, else column k at y + k * ycol
 };
 
 __host__ __device__ inline size_t dx_align16(size_t b) { return (b + 15) / 16 * 16; }
@@ -167,7 +168,7 @@ __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *_
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             if constexpr (MODE == 0)
-                static_cast<float *>(yv)[row * K + k] = acc[k];
+                static_cast<float *>(yv)[A.ycol ? k * A.ycol + row : row * K + k] = acc[k];
             else
                 static_cast<double *>(yv)[row * K + k] = static_cast<double>(acc[k]) + static_cast<double>(cc[k]);
         }
@@ -175,8 +176,9 @@ __global__ void __launch_bounds__(256) docx_spmm_kernel(DxArgs A, const float *_
 }
 
 template<int MODE, int K, typename M>
-bool dx_launch_m(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
+bool dx_launch_m(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st, int64_t ycol) {
     DxArgs A;
+    A.ycol = ycol;
     A.nrow = csr->nrow;
     A.n = csr->dx_n;
     A.m = csr->dx_m;
@@ -211,8 +213,9 @@ bool dx_launch_m(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t s
 }
 
 template<int MODE, int K>
-bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st) {
-    return csr->dx_n <= 32 ? dx_launch_m<MODE, K, uint32_t>(csr, x, y, st) : dx_launch_m<MODE, K, uint64_t>(csr, x, y, st);
+bool dx_launch_k(const pyci_gpu_csr *csr, const void *x, void *y, cudaStream_t st, int64_t ycol = 0) {
+    return csr->dx_n <= 32 ? dx_launch_m<MODE, K, uint32_t>(csr, x, y, st, ycol)
+                           : dx_launch_m<MODE, K, uint64_t>(csr, x, y, st, ycol);
 }
 
 } // namespace pyci_gpu
@@ -245,6 +248,26 @@ bool docx_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_
     case 1: return dx_launch_k<2, 1>(csr, x, y, st);
     case 2: return dx_launch_k<2, 2>(csr, x, y, st);
     case 4: return dx_launch_k<2, 4>(csr, x, y, st);
+    default: return false;
+    }
+}
+
+bool docx_launch_columns(const pyci_gpu_csr *csr, int K, const float *x, float *y, cudaStream_t st) {
+    if (!csr->dx_v || !csr->dx_binom || !csr->diag || csr->nrow >= INT32_MAX)
+        return false;
+    const size_t align = (K % 4 == 0) ? 16 : (K == 2 ? 8 : 4);
+    if (reinterpret_cast<uintptr_t>(x) % align)
+        return false;
+    const int64_t n = csr->nrow;
+    switch (K) {
+    case 1: return dx_launch_k<0, 1>(csr, x, y, st, n);
+    case 2: return dx_launch_k<0, 2>(csr, x, y, st, n);
+    case 3: return dx_launch_k<0, 3>(csr, x, y, st, n);
+    case 4: return dx_launch_k<0, 4>(csr, x, y, st, n);
+    case 5: return dx_launch_k<0, 5>(csr, x, y, st, n);
+    case 6: return dx_launch_k<0, 6>(csr, x, y, st, n);
+    case 7: return dx_launch_k<0, 7>(csr, x, y, st, n);
+    case 8: return dx_launch_k<0, 8>(csr, x, y, st, n);
     default: return false;
     }
 }

@@ -166,6 +166,10 @@ bool fcix_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_
 // The same on the implicit form of a full DOCI space (docx.cu).
 bool docx_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y, int64_t ldy,
                  cudaStream_t st);
+// FP32 product on the implicit DOCI form with x as rows of K values and y
+// written as K columns of nrow values (y + k * nrow); false when it does not
+// apply.
+bool docx_launch_columns(const pyci_gpu_csr *csr, int K, const float *x, float *y, cudaStream_t st);
 // Whichever implicit form the operator has.
 inline bool implicit_launch(const pyci_gpu_csr *csr, int mode, int K, const void *x, int64_t ldx, void *y,
                             int64_t ldy, cudaStream_t st) {
