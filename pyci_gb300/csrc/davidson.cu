@@ -802,7 +802,7 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel
         const bool ok = tid < rows;
         const int s = BULK ? static_cast<int>(t % stages) : 0;
         float *Vs = BULK ? st.set1(s) : sm + Q * kRitzTile;
-        const float *Ws = st.set2(s);
+        float *Ws = st.set2(s);
         // The diagonal before the tile's wait: its memory latency overlaps
         // the copies instead of following them.
         const float df = ok ? static_cast<float>(diag[r]) : 0.0f;
@@ -811,6 +811,12 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel
                 failed = true;
                 break;
             }
+            // Rows past N (last tile): zeros in this thread's own staged
+            // column (the copy left it), so the loop reads without a test
+            // and the Gram sums see zeros.
+            if (!ok)
+                for (int i = 0; i < m; ++i)
+                    Vs[i * kRitzTile + tid] = Ws[i * kRitzTile + tid] = 0.0f;
         }
         float x[Q], ax[Q];
 #pragma unroll
@@ -820,11 +826,8 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) ritz_fused_kernel
         for (int i = 0; i < m; ++i) {
             float v, w;
             if constexpr (BULK) {
-                // Rows past N: zeros for the Gram sums (the copy left them).
-                v = ok ? Vs[i * kRitzTile + tid] : 0.0f;
-                w = ok ? Ws[i * kRitzTile + tid] : 0.0f;
-                if (!ok)
-                    Vs[i * kRitzTile + tid] = 0.0f;
+                v = Vs[i * kRitzTile + tid];
+                w = Ws[i * kRitzTile + tid];
             } else {
                 v = ok ? V[i * N + r] : 0.0f;
                 w = ok ? W[i * N + r] : 0.0f;
@@ -934,11 +937,17 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) project_gram_kern
         const bool ok = tid < rows;
         const int s = BULK ? static_cast<int>(t % stages) : 0;
         float *Vs = BULK ? st.set1(s) : sm + Q * kRitzTile;
-        const float *Ts = st.set2(s);
+        float *Ts = st.set2(s);
         if constexpr (BULK) {
             if (__syncthreads_or(!st.wait(t))) {
                 failed = true;
                 break;
+            }
+            if (!ok) {
+                for (int i = 0; i < m; ++i)
+                    Vs[i * kRitzTile + tid] = 0.0f;
+                for (int a = 0; a < b; ++a)
+                    Ts[a * kRitzTile + tid] = 0.0f;
             }
         }
         float t1[Q];
@@ -949,9 +958,7 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) project_gram_kern
         for (int i = 0; i < m; ++i) {
             float v;
             if constexpr (BULK) {
-                v = ok ? Vs[i * kRitzTile + tid] : 0.0f;
-                if (!ok)
-                    Vs[i * kRitzTile + tid] = 0.0f;
+                v = Vs[i * kRitzTile + tid];
             } else {
                 v = ok ? V[i * N + r] : 0.0f;
                 Vs[i * kRitzTile + tid] = v;
@@ -963,7 +970,7 @@ __global__ void __launch_bounds__(kRitzTile, RPW <= 5 ? 3 : 2) project_gram_kern
         for (int a = 0; a < b; ++a) {
             float v;
             if constexpr (BULK)
-                v = ok ? Ts[a * kRitzTile + tid] : 0.0f;
+                v = Ts[a * kRitzTile + tid];
             else
                 v = ok ? Tsrc[a * N + r] : 0.0f;
 #pragma unroll
